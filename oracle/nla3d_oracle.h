@@ -1,0 +1,68 @@
+/* Oracle for the nla3d assembly path: a plain-C restatement of the reference
+ * algorithm (see nla3d_oracle.c).  TEST INFRASTRUCTURE ONLY -- the tests, the
+ * smoke check and bench.py's CPU-baseline leg are the only callers; nothing on
+ * the product path links or loads it.
+ *
+ * The model API mirrors the reference's FEStorage set-up sequence
+ * (FEStorage.h:255-270): build the model, add constraints and rigid-body MPC
+ * collections, orc_setup() (initDofs + setConstrainedNodeDof +
+ * assignEquationNumbers + initSolutionData), then per iteration
+ * orc_set_U() -> orc_update() -> orc_assemble().
+ */
+#ifndef NLA3D_ORACLE_H
+#define NLA3D_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct orc_model orc_model;
+
+/* elem_type: reference ElementType (sys.h:151-163): 2 SOLID81, 3 TETRA0, 5 QUADTH.
+ * mat_id: reference MaterialFactory::matId (MaterialFactory.h:12-18):
+ *   1 Neo-Hookean (G, K), 2 Biderman (C10, C20, C30, C01, K),
+ *   3 Mooney-Rivlin (C10, C01, K); 0 = none.
+ * elem_params: two doubles per element (TETRA0: E, my; QUADTH: k, unused). */
+orc_model* orc_new(int elem_type, uint32_t n_nodes, const double* xyz, uint32_t n_elems,
+                   const uint32_t* conn, int mat_id, const double* mat_c, int n_mat_c,
+                   const double* elem_params);
+void orc_free(orc_model* m);
+const char* orc_error(orc_model* m);
+int orc_add_fix(orc_model* m, uint32_t n, const uint32_t* nodes, const int32_t* dofs);
+int orc_add_rigid_body(orc_model* m, uint32_t master, uint32_t n_slaves, const uint32_t* slaves,
+                       uint32_t n_dofs, const int32_t* dofs);
+/* max_in_row: the reference's pre-compress row capacity (BlockSparseMatrix.h:42,
+ * default 100); overflow is reported as an error like SparseMatrix.cpp:84. */
+int orc_setup(orc_model* m, uint32_t max_in_row);
+/* out[0..3] = nDofs, nConstrained, nUnknown, nMpc;
+ * out[4..12] = (rows, cols, nnz) of block(1), block(1,2), block(2). */
+void orc_info(orc_model* m, uint32_t* out);
+int orc_pattern(orc_model* m, int block, uint32_t* iofeir, uint32_t* columns);
+int orc_eq_numbers(orc_model* m, uint32_t* node_eq, uint32_t* elem_eq);
+int orc_set_U(orc_model* m, const double* U, uint32_t n);
+int orc_update(orc_model* m);
+int orc_assemble(orc_model* m);
+int orc_get_K(orc_model* m, int block, double* values);
+int orc_get_F(orc_model* m, double* F);
+
+/* Element-level pieces (for tests against the reference's own fixtures). */
+void orc_hex_jacobian(const double* X /*8x3*/, int int_order, double* NiXj /*np x 8 x 3*/,
+                      double* det /*np*/);
+void orc_material_S(int mat_id, const double* mc, const double* C, double p, double* S);
+void orc_material_D(int mat_id, const double* mc, const double* C, double p, double* Dd,
+                    double* Dp);
+/* The dense kernels of Mat.h:686-801 on row-major arrays. */
+void orc_matBTDBprod(int M, int N, const double* B, const double* Dsym, double coef, double* Rsym);
+void orc_matBTVprod(int M, int N, const double* B, const double* V, double coef, double* R);
+void orc_matBVprod(int M, int N, const double* B, const double* V, double coef, double* R);
+void orc_matABprod(int M1, int N1, int N2, const double* A, const double* B, double coef,
+                   double* R);
+void orc_matATBprod(int M1, int N1, int N2, const double* A, const double* B, double coef,
+                    double* R);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

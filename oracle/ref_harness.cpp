@@ -1,0 +1,253 @@
+// Harness around the COMPILED REFERENCE (nla3d sources built unmodified from
+// the reference checkout by oracle/Makefile into oracle/_ref/).  Test
+// infrastructure only: it lets the tests and the golden-fixture script drive
+// the reference's own FEStorage / SOLID81 / TETRA0 / QUADTH / RigidBodyMpc code
+// on synthetic meshes and read back its DoF numbering, CSR pattern, K and F.
+//
+// It follows the reference's own set-up sequence:
+//   createNodes / createElements        (main.cpp:189-205)
+//   addMpcCollection(RigidBodyMpc)      (main.cpp:262-279)
+//   initDofs, setConstrainedNodeDof,
+//   assignEquationNumbers, initSolutionData   (FESolver.cpp:175, 221-226, 417)
+// and the per-iteration pair updateResults() -> assembleGlobalEqMatrices()
+// (FESolver.cpp:471 -> :446).
+//
+// Only SOLID81, TETRA0 and QUADTH are instantiated, so ElementFactory is
+// provided here (the reference's factory also instantiates element types that
+// are outside the assembly path and need the full third-party library).
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "FEStorage.h"
+#include "Mpc.h"
+#include "Node.h"
+#include "elements/QUADTH.h"
+#include "elements/SOLID81.h"
+#include "elements/TETRA0.h"
+#include "materials/MaterialFactory.h"
+
+using namespace nla3d;
+
+namespace nla3d {
+ElementType ElementFactory::elName2elType(std::string elName) {
+  for (int i = 0; i < (int)ElementType::UNDEFINED; i++)
+    if (elName == elTypeLabels[i]) return (ElementType)i;
+  return ElementType::UNDEFINED;
+}
+
+void ElementFactory::createElements(ElementType elId, const uint32 n, std::vector<Element*>& ptr) {
+  ptr.reserve(ptr.size() + n);
+  for (uint32 i = 0; i < n; i++) {
+    switch (elId) {
+      case ElementType::SOLID81: ptr.push_back(new ElementSOLID81()); break;
+      case ElementType::TETRA0: ptr.push_back(new ElementTETRA0()); break;
+      case ElementType::QUADTH: ptr.push_back(new ElementQUADTH()); break;
+      default: LOG(FATAL) << "element type not built into the oracle harness";
+    }
+  }
+}
+}  // namespace nla3d
+
+namespace {
+
+struct RefModel {
+  FEStorage storage;
+  ElementType type = ElementType::UNDEFINED;
+  std::vector<std::pair<uint32, int>> fixes;
+  std::string err;
+  double t_update = 0.0, t_assemble = 0.0;
+};
+
+template <class F>
+int guarded(RefModel* m, F&& f) {
+  try {
+    f();
+    return 0;
+  } catch (const std::exception& e) {
+    if (m) m->err = e.what();
+    return 1;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+// elem_type: reference ElementType code (sys.h:151-163): 2 SOLID81, 3 TETRA0, 5 QUADTH.
+// mat_id: reference MaterialFactory::matId (MaterialFactory.h:12-18): 1 Neo-Hookean,
+//         2 Biderman, 3 Mooney-Rivlin; 0 = no material (TETRA0 / QUADTH).
+// elem_params: per element, two doubles (TETRA0: E, my; QUADTH: k, unused).
+void* ref_new(int elem_type, unsigned n_nodes, const double* xyz, unsigned n_elems,
+              const unsigned* conn, int mat_id, const double* mat_c, int n_mat_c,
+              const double* elem_params) {
+  RefModel* m = new RefModel();
+  int rc = guarded(m, [&] {
+    m->type = (ElementType)elem_type;
+    auto nind = m->storage.createNodes(n_nodes);
+    for (unsigned i = 0; i < n_nodes; i++) {
+      Node& nd = m->storage.getNode(nind[i]);
+      nd.pos[0] = xyz[3 * i + 0];
+      nd.pos[1] = xyz[3 * i + 1];
+      nd.pos[2] = xyz[3 * i + 2];
+    }
+    auto eind = m->storage.createElements(n_elems, m->type);
+    for (unsigned e = 0; e < n_elems; e++) {
+      Element& el = m->storage.getElement(eind[e]);
+      const unsigned nn = el.getNNodes();
+      for (unsigned j = 0; j < nn; j++) el.getNodeNumber(j) = conn[e * nn + j];
+      if (m->type == ElementType::TETRA0) {
+        auto& t = dynamic_cast<ElementTETRA0&>(el);
+        t.E = elem_params[2 * e + 0];
+        t.my = elem_params[2 * e + 1];
+      } else if (m->type == ElementType::QUADTH) {
+        auto& q = dynamic_cast<ElementQUADTH&>(el);
+        q.k = elem_params[2 * e + 0];
+      }
+    }
+    if (mat_id > 0) {
+      Material* mat = MaterialFactory::createMaterial(MaterialFactory::matModelLabels[mat_id]);
+      if (!mat) LOG(FATAL) << "bad material id";
+      for (int i = 0; i < n_mat_c; i++) mat->Ci(i) = mat_c[i];
+      m->storage.material = mat;
+    }
+  });
+  if (rc) {
+    delete m;
+    return nullptr;
+  }
+  return m;
+}
+
+void ref_free(void* h) { delete static_cast<RefModel*>(h); }
+
+const char* ref_error(void* h) { return static_cast<RefModel*>(h)->err.c_str(); }
+
+int ref_add_fix(void* h, unsigned n, const unsigned* nodes, const int* dofs) {
+  RefModel* m = static_cast<RefModel*>(h);
+  for (unsigned i = 0; i < n; i++) m->fixes.emplace_back(nodes[i], dofs[i]);
+  return 0;
+}
+
+int ref_add_rigid_body(void* h, unsigned master, unsigned n_slaves, const unsigned* slaves,
+                       unsigned n_dofs, const int* dofs) {
+  RefModel* m = static_cast<RefModel*>(h);
+  return guarded(m, [&] {
+    RigidBodyMpc* mpc = new RigidBodyMpc;
+    mpc->storage = &m->storage;
+    mpc->masterNode = master;
+    mpc->slaveNodes.assign(slaves, slaves + n_slaves);
+    for (unsigned i = 0; i < n_dofs; i++) mpc->dofs.push_back((Dof::dofType)dofs[i]);
+    m->storage.addMpcCollection(mpc);
+  });
+}
+
+int ref_setup(void* h) {
+  RefModel* m = static_cast<RefModel*>(h);
+  return guarded(m, [&] {
+    m->storage.initDofs();
+    for (auto& f : m->fixes) m->storage.setConstrainedNodeDof(f.first, (Dof::dofType)f.second);
+    m->storage.assignEquationNumbers();
+    m->storage.initSolutionData();
+  });
+}
+
+// out[0..3]  = nDofs, nConstrainedDofs, nUnknownDofs, nMpc
+// out[4..12] = (rows, cols, nnz) of block(1), block(1,2), block(2)
+void ref_info(void* h, unsigned* out) {
+  RefModel* m = static_cast<RefModel*>(h);
+  FEStorage& s = m->storage;
+  out[0] = s.nDofs();
+  out[1] = s.nConstrainedDofs();
+  out[2] = s.nUnknownDofs();
+  out[3] = s.nMpc();
+  auto* K = s.getK();
+  math::BaseSparseMatrix* blocks[3] = {K->block(1), K->block(1, 2), K->block(2)};
+  for (int b = 0; b < 3; b++) {
+    out[4 + 3 * b + 0] = blocks[b]->nRows();
+    out[4 + 3 * b + 1] = blocks[b]->nColumns();
+    out[4 + 3 * b + 2] = blocks[b]->nValues();
+  }
+}
+
+static math::BaseSparseMatrix* pick_block(RefModel* m, int block) {
+  auto* K = m->storage.getK();
+  if (block == 1) return K->block(1);
+  if (block == 2) return K->block(2);
+  return K->block(1, 2);
+}
+
+// block: 1, 2, or 12 (= block(1,2)).  iofeir gets rows+1 entries, columns nnz.
+int ref_pattern(void* h, int block, unsigned* iofeir, unsigned* columns) {
+  RefModel* m = static_cast<RefModel*>(h);
+  return guarded(m, [&] {
+    math::BaseSparseMatrix* B = pick_block(m, block);
+    if (B->nRows() == 0 && B->nValues() == 0) return;
+    std::memcpy(iofeir, B->getIofeirArray(), sizeof(unsigned) * (B->nRows() + 1));
+    std::memcpy(columns, B->getColumnsArray(), sizeof(unsigned) * B->nValues());
+  });
+}
+
+// Equation numbers per (entity, Dof::dofType) (Dof.h:15-25), 0 = DoF not used.
+int ref_eq_numbers(void* h, unsigned* node_eq, unsigned* elem_eq) {
+  RefModel* m = static_cast<RefModel*>(h);
+  return guarded(m, [&] {
+    FEStorage& s = m->storage;
+    for (uint32 n = 1; n <= s.nNodes(); n++)
+      for (int t = 0; t < Dof::numberOfDofTypes; t++)
+        node_eq[(n - 1) * 8 + t] = s.isNodeDofUsed(n, (Dof::dofType)t)
+                                       ? s.getNodeDofEqNumber(n, (Dof::dofType)t) : 0;
+    for (uint32 e = 1; e <= s.nElements(); e++)
+      for (int t = 0; t < Dof::numberOfDofTypes; t++)
+        elem_eq[(e - 1) * 8 + t] = s.isElementDofUsed(e, (Dof::dofType)t)
+                                       ? s.getElementDofEqNumber(e, (Dof::dofType)t) : 0;
+  });
+}
+
+int ref_set_U(void* h, const double* U, unsigned n) {
+  RefModel* m = static_cast<RefModel*>(h);
+  return guarded(m, [&] {
+    math::dVec* v = m->storage.getU();
+    if (v->size() != n) LOG(FATAL) << "U size mismatch";
+    for (unsigned i = 0; i < n; i++) (*v)[i] = U[i];
+  });
+}
+
+int ref_update(void* h, double* seconds) {
+  RefModel* m = static_cast<RefModel*>(h);
+  return guarded(m, [&] {
+    auto& t = nla3d_shim::timers();
+    t["updateSolutionResults"] = 0.0;
+    m->storage.updateResults();
+    if (seconds) *seconds = t["updateSolutionResults"];
+  });
+}
+
+int ref_assemble(void* h, double* seconds) {
+  RefModel* m = static_cast<RefModel*>(h);
+  return guarded(m, [&] {
+    auto& t = nla3d_shim::timers();
+    t["assembleGlobalEqMatrix"] = 0.0;
+    m->storage.assembleGlobalEqMatrices();
+    if (seconds) *seconds = t["assembleGlobalEqMatrix"];
+  });
+}
+
+int ref_get_K(void* h, int block, double* values) {
+  RefModel* m = static_cast<RefModel*>(h);
+  return guarded(m, [&] {
+    math::BaseSparseMatrix* B = pick_block(m, block);
+    if (B->nValues() == 0) return;
+    std::memcpy(values, B->getValuesArray(), sizeof(double) * B->nValues());
+  });
+}
+
+int ref_get_F(void* h, double* F) {
+  RefModel* m = static_cast<RefModel*>(h);
+  return guarded(m, [&] {
+    math::dVec* v = m->storage.getF();
+    for (uint32 i = 0; i < v->size(); i++) F[i] = (*v)[i];
+  });
+}
+
+}  // extern "C"

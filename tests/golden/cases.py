@@ -1,0 +1,66 @@
+"""Small parity cases shared by the golden-fixture script and the tests.
+
+Each case returns (mesh, u, p, extra, do_update):
+  u (n_nodes, 3) nodal displacements, p (n_elems,) element pressures,
+  extra {(node, dof): value} for DoFs outside the elements (rigid-body master),
+  do_update: whether the per-iteration protocol calls updateResults() before
+  assembleGlobalEqMatrices() (SOLID81, FESolver.cpp:471 -> :446); the linear
+  elements are assembled from their fresh state (FESolver.cpp:364).
+"""
+import numpy as np
+
+from nla3d_gb300 import meshgen as mg
+
+
+def cube3_nh():
+    mesh, u, p = mg.config_cube(3, seed=1)
+    return mesh, u, p, None, True
+
+
+def cube4_nh_clamped():
+    mesh, u, p = mg.config_cube(4, seed=5, clamp_z0=True)
+    return mesh, u, p, None, True
+
+
+def mr_twist_3x2x4():
+    m = mg.solid81_block(3, 2, 4, 0.5, mg.MAT_MOONEY_RIVLIN, (0.4, 0.1, 2000.0))
+    u, p = mg.twist_state(m, seed=3)
+    return m, u, p, None, True
+
+
+def biderman_3x3x3_clamped():
+    m = mg.solid81_block(3, 3, 3, 1.0, mg.MAT_BIDERMAN, (0.5, 0.05, 0.01, 0.1, 800.0),
+                         clamp_z0=True)
+    u, p = mg.stretch_state(m, 1.3, seed=4)
+    return m, u, p, None, True
+
+
+def bar_mpc_2x2x3():
+    m = mg.solid81_bar_mpc(2, 2, 3, 1.0)
+    u, p = mg.stretch_state(m, 1.1, seed=7)
+    master = m.n_nodes
+    extra = {(master, mg.UZ): 0.3, (master, mg.ROTZ): 0.4, (master, mg.ROTX): 0.05,
+             (master, mg.UX): 0.01}
+    return m, u, p, extra, True
+
+
+def tetra0_3x3x3():
+    m = mg.tetra0_block(3, 3, 3, 0.5)
+    return m, np.zeros((m.n_nodes, 3)), None, None, False
+
+
+def quadth_5x4():
+    m = mg.quadth_plate(5, 4, 0.2, k=3.0)
+    return m, np.zeros((m.n_nodes, 3)), None, None, False
+
+
+def cube10_nh():
+    """The 10^3 unit-cube workload (1000 SOLID81, 4993 equations)."""
+    mesh, u, p = mg.config_cube(10, seed=1)
+    return mesh, u, p, None, True
+
+
+FULL_CASES = {f.__name__: f for f in (cube3_nh, cube4_nh_clamped, mr_twist_3x2x4,
+                                       biderman_3x3x3_clamped, bar_mpc_2x2x3, tetra0_3x3x3,
+                                       quadth_5x4)}
+DIGEST_CASES = {f.__name__: f for f in (cube10_nh,)}
