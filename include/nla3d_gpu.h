@@ -1,0 +1,177 @@
+/* nla3d_gpu.h -- C ABI of the GB300 (sm_103a) implementation of nla3d's
+ * per-iteration global assembly.
+ *
+ * The entry points replace the FEStorage member functions of the reference
+ * (paths relative to the reference's src/lib/) for the assembly path:
+ *
+ *   nla3d_create                 FEStorage::createNodes / createElements  FEStorage.h:211,223
+ *                                (+ node positions, the Material instance  FEStorage.h:48)
+ *   nla3d_add_fix                FEStorage::setConstrainedNodeDof           FEStorage.h:159
+ *   nla3d_add_rigid_body         FEStorage::addMpcCollection(RigidBodyMpc)  FEStorage.h:200, Mpc.h:51
+ *   nla3d_build_pattern          initDofs + assignEquationNumbers + the
+ *                                sparsity part of initSolutionData (host)   FEStorage.h:259,263,265
+ *   nla3d_init_solution_data     initSolutionData: the above + device
+ *                                allocation and upload                      FEStorage.h:265
+ *   nla3d_set_U / _device        writes of FEStorage::getU() (vecU)         FEStorage.h:109
+ *   nla3d_update_results         FEStorage::updateResults                   FEStorage.h:270
+ *   nla3d_assemble               FEStorage::assembleGlobalEqMatrices        FEStorage.h:115
+ *   nla3d_get_K / nla3d_pattern  FEStorage::getK() -> BlockSparseSymMatrix<2>::block(..)
+ *                                getValuesArray / getColumnsArray /
+ *                                getIofeirArray                             FEStorage.h:100,
+ *                                                                           SparseMatrix.h:206-221
+ *   nla3d_get_F                  FEStorage::getF()                          FEStorage.h:105
+ *   nla3d_eq_numbers             FEStorage::getNodeDofEqNumber /
+ *                                getElementDofEqNumber                      FEStorage.h:148-149
+ *
+ * Conventions kept from the reference: node, element and equation numbers
+ * start at 1; constrained equations are numbered first; K is split into
+ * block(1) (constrained x constrained, symmetric upper), block(1,2)
+ * (constrained x unknown+MPC, general) and block(2) (unknown+MPC, symmetric
+ * upper), each a 1-based 3-array CSR with sorted columns.
+ *
+ * Errors: every function returns an int status (NLA3D_OK == 0).  Nothing
+ * aborts the process; nla3d_last_error() describes the last failure.
+ * Threading: one context = one CUDA stream; calls on a context must be
+ * serialised by the caller (the reference is single-threaded too).
+ */
+#ifndef NLA3D_GPU_H
+#define NLA3D_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NLA3D_OK 0
+#define NLA3D_ERR_ARG 1      /* bad argument or call order                       */
+#define NLA3D_ERR_CUDA 2     /* a CUDA runtime call failed                        */
+#define NLA3D_ERR_PATTERN 3  /* a contribution has no CSR slot (SparseMatrix.cpp:400) */
+#define NLA3D_ERR_NOMEM 4    /* host or device allocation failed                  */
+#define NLA3D_ERR_RANGE 5    /* a size exceeds an index type or a fixed limit     */
+#define NLA3D_ERR_ELEMENT 6  /* an element reported J <= 0 or a non-finite value  */
+
+/* Element types: the reference's ElementType codes (sys.h:151-163). */
+#define NLA3D_SOLID81 2
+#define NLA3D_TETRA0 3
+#define NLA3D_QUADTH 5
+
+/* Materials: the reference's MaterialFactory::matId (MaterialFactory.h:12-18).
+ * Constants in the reference's order (materials_hyperelastic.h:45-105). */
+#define NLA3D_MAT_NEO_HOOKEAN 1   /* G, K                 */
+#define NLA3D_MAT_BIDERMAN 2      /* C10, C20, C30, C01, K */
+#define NLA3D_MAT_MOONEY_RIVLIN 3 /* C10, C01, K           */
+
+/* DoF types: Dof::dofType (Dof.h:15-25). */
+#define NLA3D_UX 0
+#define NLA3D_UY 1
+#define NLA3D_UZ 2
+#define NLA3D_ROTX 3
+#define NLA3D_ROTY 4
+#define NLA3D_ROTZ 5
+#define NLA3D_HYDRO_PRESSURE 6
+#define NLA3D_TEMP 7
+
+/* Arithmetic of the SOLID81 element kernel. */
+#define NLA3D_PREC_FP64 0  /* everything in FP64 (parity path, <=1e-12 vs the reference) */
+#define NLA3D_PREC_MIXED 1 /* FP32 tangent (B^T.D.B, geometric term); FP64 for F, J,
+                              J-1, the pressure coupling, the residual and CSR sums */
+
+typedef struct nla3d_ctx nla3d_ctx;
+
+typedef struct {
+  int32_t elem_type;          /* NLA3D_SOLID81 / NLA3D_TETRA0 / NLA3D_QUADTH          */
+  uint32_t n_nodes;
+  uint32_t n_elems;
+  const double* xyz;          /* 3 * n_nodes, host                                    */
+  const uint32_t* conn;       /* nodes_per_elem * n_elems, 1-based node ids, host     */
+  int32_t mat_id;             /* NLA3D_MAT_* (SOLID81), 0 otherwise                   */
+  double mat_c[5];
+  const double* elem_params;  /* 2 * n_elems: TETRA0 (E, my), QUADTH (k, 0); or NULL */
+} nla3d_mesh_desc;
+
+/* Create a model (FEStorage with nodes, elements and material).  `precision`
+ * selects the SOLID81 arithmetic (NLA3D_PREC_*).  Makes no CUDA call. */
+int nla3d_create(const nla3d_mesh_desc* mesh, int precision, nla3d_ctx** out);
+int nla3d_destroy(nla3d_ctx* ctx);
+const char* nla3d_last_error(const nla3d_ctx* ctx);
+
+/* Run on this CUDA stream (cudaStream_t passed as void*); default: the
+ * context's own non-blocking stream. */
+int nla3d_set_stream(nla3d_ctx* ctx, void* stream);
+void* nla3d_get_stream(const nla3d_ctx* ctx);
+
+int nla3d_add_fix(nla3d_ctx* ctx, uint32_t n, const uint32_t* nodes, const int32_t* dofs);
+int nla3d_add_rigid_body(nla3d_ctx* ctx, uint32_t master, uint32_t n_slaves,
+                         const uint32_t* slaves, uint32_t n_dofs, const int32_t* dofs);
+
+/* Host-only set-up: DoF registration, equation numbering, the CSR pattern
+ * (bit-exact with the reference) and the element -> CSR slot maps with their
+ * fixed-order gather lists.  Makes no CUDA call.  Idempotent. */
+int nla3d_build_pattern(nla3d_ctx* ctx);
+/* nla3d_build_pattern (if not done yet), device allocation and upload, and
+ * the once-per-mesh Jacobian precompute.  Synchronous.  Selects the device
+ * that is current at this call. */
+int nla3d_init_solution_data(nla3d_ctx* ctx);
+/* Element -> slot maps (valid after nla3d_build_pattern and until
+ * nla3d_init_solution_data releases them): kslot[e * nk + c] is the index
+ * into the concatenated K values (block(1) | block(1,2) | block(2)) of K
+ * contribution c of element e (reference assembly order); fslot[e * nf + c]
+ * is the 0-based F row.  nk, nf: out[13], out[14] of nla3d_info. */
+int nla3d_slot_maps(const nla3d_ctx* ctx, uint32_t* kslot, uint32_t* fslot);
+
+/* out[0..3] = nDofs, nConstrainedDofs, nUnknownDofs, nMpc;
+ * out[4..12] = (rows, cols, nnz) of block(1), block(1,2), block(2);
+ * out[13], out[14] = K and F contributions per element; out[15] reserved.
+ * Valid after nla3d_build_pattern. */
+int nla3d_info(const nla3d_ctx* ctx, uint32_t out[16]);
+/* block: 1, 2 or 12 (= block(1,2)).  iofeir: rows+1 entries; columns: nnz. */
+int nla3d_pattern(const nla3d_ctx* ctx, int block, uint32_t* iofeir, uint32_t* columns);
+/* Equation number per (node, Dof type) and (element, Dof type), 8 types each,
+ * 0 = unused. */
+int nla3d_eq_numbers(const nla3d_ctx* ctx, uint32_t* node_eq, uint32_t* elem_eq);
+
+/* vecU (nDofs + nMpc doubles) from host memory (copied on the context
+ * stream) or from device memory. */
+int nla3d_set_U(nla3d_ctx* ctx, const double* U, uint64_t n);
+int nla3d_set_U_device(nla3d_ctx* ctx, const double* U_dev, uint64_t n);
+
+/* FEStorage::updateResults: the per-Gauss-point state of the next assembly is
+ * taken from the current U (asynchronous). */
+int nla3d_update_results(nla3d_ctx* ctx);
+/* FEStorage::assembleGlobalEqMatrices: element tangents and residuals,
+ * fixed-order CSR sums, MPC rows (asynchronous; K and F stay on the device). */
+int nla3d_assemble(nla3d_ctx* ctx);
+
+/* Results.  Host copies synchronise the stream. */
+int nla3d_get_K(nla3d_ctx* ctx, int block, double* values);
+int nla3d_get_F(nla3d_ctx* ctx, double* F);
+/* Device pointers (valid until nla3d_destroy): K values of one block, F. */
+int nla3d_device_K(const nla3d_ctx* ctx, int block, double** values, uint64_t* n);
+int nla3d_device_F(const nla3d_ctx* ctx, double** F, uint64_t* n);
+int nla3d_synchronize(nla3d_ctx* ctx);
+
+/* Elements flagged by the last assembly (J <= 0, det J <= 0 or a non-finite
+ * value): count and smallest 1-based element number (0 if none).
+ * Synchronises.  Returns NLA3D_ERR_ELEMENT when count > 0. */
+int nla3d_element_status(nla3d_ctx* ctx, uint32_t* count, uint32_t* first);
+
+/* Number of kernels launched by the library on this context so far. */
+uint64_t nla3d_kernel_launches(const nla3d_ctx* ctx);
+
+/* Measurement helpers (no counterpart in the reference, which has no GPU).
+ * nla3d_set_timing(ctx, 1) records CUDA events on the context stream around
+ * each kernel of nla3d_assemble; nla3d_kernel_times() returns the last
+ * assembly's times in ms: [0] element kernel, [1] K gather, [2] F gather,
+ * [3] MPC rows (synchronises). */
+int nla3d_set_timing(nla3d_ctx* ctx, int on);
+int nla3d_kernel_times(nla3d_ctx* ctx, float ms[4]);
+/* Throughput probe of dependent-chain-free FMA on the current device:
+ * fp64 != 0 -> DFMA, else FFMA.  Returns FLOP/s (2 per FMA) in *flops. */
+int nla3d_probe_fma_peak(int fp64, double* flops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NLA3D_GPU_H */

@@ -1,0 +1,101 @@
+"""ctypes binding of libnla3d_gpu.so (include/nla3d_gpu.h).
+
+The library is built in-tree by nla3d_gb300.build (``__graft_entry__.build()``).
+There is no fallback: if the shared library is missing or cannot be loaded,
+every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libnla3d_gpu.so")
+
+NLA3D_OK = 0
+ERR_NAMES = {1: "NLA3D_ERR_ARG", 2: "NLA3D_ERR_CUDA", 3: "NLA3D_ERR_PATTERN",
+             4: "NLA3D_ERR_NOMEM", 5: "NLA3D_ERR_RANGE", 6: "NLA3D_ERR_ELEMENT"}
+PREC_FP64 = 0
+PREC_MIXED = 1
+
+# Every symbol declared in include/nla3d_gpu.h.
+EXPORTS = [
+    "nla3d_create", "nla3d_destroy", "nla3d_last_error", "nla3d_set_stream", "nla3d_get_stream",
+    "nla3d_add_fix", "nla3d_add_rigid_body", "nla3d_build_pattern", "nla3d_init_solution_data",
+    "nla3d_slot_maps", "nla3d_info",
+    "nla3d_pattern", "nla3d_eq_numbers", "nla3d_set_U", "nla3d_set_U_device",
+    "nla3d_update_results", "nla3d_assemble", "nla3d_get_K", "nla3d_get_F", "nla3d_device_K",
+    "nla3d_device_F", "nla3d_synchronize", "nla3d_element_status", "nla3d_kernel_launches",
+    "nla3d_set_timing", "nla3d_kernel_times", "nla3d_probe_fma_peak",
+]
+
+
+class MeshDesc(ctypes.Structure):
+    _fields_ = [
+        ("elem_type", ctypes.c_int32),
+        ("n_nodes", ctypes.c_uint32),
+        ("n_elems", ctypes.c_uint32),
+        ("xyz", ctypes.c_void_p),
+        ("conn", ctypes.c_void_p),
+        ("mat_id", ctypes.c_int32),
+        ("mat_c", ctypes.c_double * 5),
+        ("elem_params", ctypes.c_void_p),
+    ]
+
+
+class Nla3dError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERR_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load the shared library once; raise if it is not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(
+            f"{path} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`"
+            " (the CUDA path has no fallback)")
+    lib = ctypes.CDLL(path)
+    P, U32, U64, I32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int32
+    sig = {
+        "nla3d_create": ([ctypes.POINTER(MeshDesc), ctypes.c_int, ctypes.POINTER(P)], ctypes.c_int),
+        "nla3d_destroy": ([P], ctypes.c_int),
+        "nla3d_last_error": ([P], ctypes.c_char_p),
+        "nla3d_set_stream": ([P, P], ctypes.c_int),
+        "nla3d_get_stream": ([P], P),
+        "nla3d_add_fix": ([P, U32, P, P], ctypes.c_int),
+        "nla3d_add_rigid_body": ([P, U32, U32, P, U32, P], ctypes.c_int),
+        "nla3d_build_pattern": ([P], ctypes.c_int),
+        "nla3d_init_solution_data": ([P], ctypes.c_int),
+        "nla3d_slot_maps": ([P, P, P], ctypes.c_int),
+        "nla3d_info": ([P, P], ctypes.c_int),
+        "nla3d_pattern": ([P, ctypes.c_int, P, P], ctypes.c_int),
+        "nla3d_eq_numbers": ([P, P, P], ctypes.c_int),
+        "nla3d_set_U": ([P, P, U64], ctypes.c_int),
+        "nla3d_set_U_device": ([P, P, U64], ctypes.c_int),
+        "nla3d_update_results": ([P], ctypes.c_int),
+        "nla3d_assemble": ([P], ctypes.c_int),
+        "nla3d_get_K": ([P, ctypes.c_int, P], ctypes.c_int),
+        "nla3d_get_F": ([P, P], ctypes.c_int),
+        "nla3d_device_K": ([P, ctypes.c_int, ctypes.POINTER(P), ctypes.POINTER(U64)], ctypes.c_int),
+        "nla3d_device_F": ([P, ctypes.POINTER(P), ctypes.POINTER(U64)], ctypes.c_int),
+        "nla3d_synchronize": ([P], ctypes.c_int),
+        "nla3d_element_status": ([P, ctypes.POINTER(U32), ctypes.POINTER(U32)], ctypes.c_int),
+        "nla3d_kernel_launches": ([P], U64),
+        "nla3d_set_timing": ([P, ctypes.c_int], ctypes.c_int),
+        "nla3d_kernel_times": ([P, P], ctypes.c_int),
+        "nla3d_probe_fma_peak": ([ctypes.c_int, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = res
+    del I32
+    _lib = lib
+    return lib

@@ -1,0 +1,98 @@
+// Host-side model of the assembly path: DoF tables, equation numbering, the
+// block CSR pattern of K, and the element -> CSR slot maps with their
+// fixed-order gather lists.  Everything here is integer work done once per
+// mesh (the reference's FEStorage::initDofs / assignEquationNumbers /
+// initSolutionData, FEStorage.cpp:338-550).
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace nla3d_gpu {
+
+constexpr int kDofTypes = 8;  // Dof::numberOfDofTypes (Dof.h:15-25)
+enum DofType { UX = 0, UY, UZ, ROTX, ROTY, ROTZ, HYDRO_PRESSURE, TEMP };
+enum ElemType { SOLID81 = 2, TETRA0 = 3, QUADTH = 5 };
+
+struct RigidBody {
+  uint32_t master = 0;
+  std::vector<uint32_t> slaves;
+  std::vector<int> dofs;
+  uint32_t first_mpc = 0;
+};
+
+// One MPC equation of a rigid body (Mpc.cpp:52-68): 5 terms.
+struct MpcEq {
+  uint32_t eq = 0;
+  uint32_t node[5];
+  int dof[5];
+  uint32_t rb = 0;       // owning rigid body
+  uint32_t slave = 0;    // slave node
+  int slave_dof = 0;     // UX/UY/UZ of this equation
+};
+
+// 1-based 3-array CSR block (SparseMatrix.h:53-69).
+struct CsrBlock {
+  uint32_t rows = 0, cols = 0;
+  std::vector<uint32_t> iofeir;   // rows + 1, iofeir[0] = 1
+  std::vector<uint32_t> columns;  // nnz, 1-based, sorted per row
+  uint64_t nnz() const { return columns.size(); }
+};
+
+struct HostModel {
+  // mesh
+  int etype = SOLID81;
+  int npe = 8;        // nodes per element
+  int nodal_dofs = 3; // DoFs per node used by the element (3 for solids, 1 for QUADTH)
+  uint32_t n_nodes = 0, n_elems = 0;
+  std::vector<double> xyz;
+  std::vector<uint32_t> conn;
+  int mat_id = 0;
+  double mat_c[5] = {0, 0, 0, 0, 0};
+  std::vector<double> eparams;
+  // constraints and MPC
+  std::vector<uint32_t> fix_node;
+  std::vector<int> fix_dof;
+  std::vector<RigidBody> rbs;
+  std::vector<MpcEq> mpcs;
+  // DoF tables
+  std::vector<uint8_t> node_mask, elem_mask, node_fix;
+  std::vector<uint32_t> node_eq, elem_eq;  // (entity, type) -> eq, 0 = unused
+  uint32_t n_dofs = 0, n_con = 0, n_unk = 0, n_mpc = 0;
+  // K pattern: blk[0] = block(1), blk[1] = block(1,2), blk[2] = block(2)
+  CsrBlock blk[3];
+  uint64_t val_off[3] = {0, 0, 0};  // offsets of each block in the concatenated values
+  uint64_t nnz_total = 0;
+  // element contributions: per element n_kc K values then n_fc F values
+  int n_kc = 0, n_fc = 0;
+  // gather lists: slot s of the concatenated K values sums contributions
+  // k_ids[k_ptr[s] .. k_ptr[s+1]) (element-ascending, local order within an
+  // element: the reference's own summation order, FEStorage.cpp:36 +
+  // SOLID81.h:62-93); F row r likewise with f_ptr / f_ids.
+  std::vector<uint32_t> kslot, fslot;  // element -> slot maps (freed after upload)
+  std::vector<uint32_t> k_ptr, k_ids;
+  std::vector<uint32_t> f_ptr, f_ids;
+  // MPC term slots (n_mpc * 5) in the concatenated K values
+  std::vector<uint32_t> mpc_slot;
+
+  uint32_t n_total() const { return n_dofs + n_mpc; }
+  uint32_t neq(uint32_t node, int t) const { return node_eq[(size_t)(node - 1) * kDofTypes + t]; }
+  uint32_t eeq(uint32_t el, int t) const { return elem_eq[(size_t)(el - 1) * kDofTypes + t]; }
+};
+
+// Build DoF tables, numbering, pattern, slot maps.  Returns "" on success,
+// else a message.  n_threads <= 0 means "use the hardware concurrency".
+std::string build_host_model(HostModel& m, int n_threads);
+
+// Local contribution layout of one element in the reference's assembly order:
+// for contribution c < n_kc, the (row entity dof, col entity dof) pair.
+// entity >= 0 is the element-local node index; entity == -1 the element's own
+// DoF (HYDRO_PRESSURE).
+struct LocalPair {
+  int8_t ei, ti, ej, tj;
+};
+std::vector<LocalPair> element_k_layout(int etype);
+std::vector<LocalPair> element_f_layout(int etype);
+
+}  // namespace nla3d_gpu

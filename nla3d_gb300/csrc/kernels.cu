@@ -1,0 +1,790 @@
+// Assembly kernels for sm_103a: SOLID81 (FP64 and mixed), its Jacobian
+// precompute, TETRA0 / QUADTH, the fixed-order CSR gather and the rigid-body
+// MPC rows.
+//
+// SOLID81 algebra (reference: SOLID81.cpp:29-82, 85-115):
+//   B = 2 (B_L + Omega B_NL) is 2 * Bh, where for node a, displacement
+//   component i and Voigt row (jk):  Bh[(jk)][i] = F_ij G_ak + F_ik G_aj
+//   (j != k), F_ij G_aj (j == k);  F = I + O, G_a = dN_a/dX.
+//   Kuu(a,i; b,k) += w * (Bh_a^T Dd' Bh_b)[i][k] + w * delta_ik G_a . S G_b
+//       with Dd' = 2 * Dd (the reference halves Dd, materials_hyperelastic.cpp:124,
+//       and scales B^T Dd B by w/2 with B = 2 Bh);
+//   Fu_a   += -w * (F S G_a)              ( = -w/2 B^T S,  SOLID81.cpp:73 )
+//   Kup_a  +=  w * (cof(F) G_a)           ( = w/2 B^T J C^-1, since J F C^-1 = cof F )
+//   Fp     += -(J - 1 - p/k) w ;  Kpp += -w / k
+// These are the reference's products with the structural zeros of B, B_NL
+// and Omega removed; they agree with the reference to rounding (the tests
+// bound the difference at 1e-12 relative).
+#include <cmath>
+#include <cstdio>
+
+#include "kernels.cuh"
+
+namespace nla3d_gpu {
+
+namespace {
+
+constexpr int kWarpsPerBlock = 4;
+constexpr int kEPW = 4;                              // elements per warp
+constexpr int kKuuPerElem = 300;
+constexpr int kOwned = (kEPW * kKuuPerElem + 31) / 32;  // Kuu entries per lane (38)
+constexpr double kGaussA = 0.5773502691896258;        // isoparametric.h:127
+
+// Kuu entry t (assemble3 order, SOLID81.h:62-74) -> (a, i, b, k) packed.
+__constant__ uchar4 c_kuu_entry[kKuuPerElem];
+
+template <typename TT>
+struct WarpSmem {
+  double F[9][32];     // per (element q, Gauss point g): deformation gradient
+  double wP[9][32];    // -w F S
+  double wCof[9][32];  //  w cof(F)
+  double wS[6][32];    //  w S (Voigt xx xy xz yy yz zz)
+  TT wD[21][32];       //  w * 2 Dd, packed upper
+  TT Bh[18][32];       // per (element q, node a) of the current Gauss point: Bh[r*3+i]
+  TT DB[18][32];       // (w 2 Dd) Bh
+  TT SG[3][32];        // w S G_a
+  TT Ga[3][32];        // G_a
+};
+
+__device__ __forceinline__ int sym6(int r, int s) {  // packed upper index, r <= s
+  return 6 * r - ((r - 1) * r) / 2 + (s - r);
+}
+
+__device__ __forceinline__ void flag_element(ElementStatus* st, uint32_t el1) {
+  atomicAdd(&st->count, 1u);
+  atomicMin(&st->first, el1);
+}
+
+// Material response at one Gauss point (materials_hyperelastic.cpp:30-129).
+// Inputs: C (Voigt), p_state (for S), p_cur (for Dd).  Outputs: S, J and the
+// coefficient form of w*2*Dd:
+//   wD = A (x) P + B (x) Q + Ci (x) R + sIIt * IIt + sI * (I (x) I - II)
+template <typename TT>
+struct MatOut {
+  double S[6];
+  double J;
+};
+
+template <typename TT>
+__device__ __forceinline__ void material(int mat_id, const double* mc, const double C[6],
+                                         double p_state, double p_cur, double w, MatOut<TT>& o,
+                                         TT wD[21]) {
+  const double I1 = C[0] + C[3] + C[5];
+  const double I2 = C[0] * C[3] + C[3] * C[5] + C[0] * C[5] - C[1] * C[1] - C[4] * C[4] -
+                    C[2] * C[2];
+  const double detC = C[0] * (C[3] * C[5] - C[4] * C[4]) - C[1] * (C[1] * C[5] - C[4] * C[2]) +
+                      C[2] * (C[1] * C[4] - C[3] * C[2]);
+  const double J = sqrt(detC);
+  const double rc = rcbrt(J);
+  const double pp = rc * rc;       // J^(-2/3)
+  const double pppp = pp * pp;     // J^(-4/3)
+  const double oo = 1.0 / (J * J);
+  double Ci[6];
+  Ci[0] = oo * (C[3] * C[5] - C[4] * C[4]);
+  Ci[1] = oo * (C[2] * C[4] - C[1] * C[5]);
+  Ci[2] = oo * (C[1] * C[4] - C[2] * C[3]);
+  Ci[3] = oo * (C[0] * C[5] - C[2] * C[2]);
+  Ci[4] = oo * (C[1] * C[2] - C[0] * C[4]);
+  Ci[5] = oo * (C[0] * C[3] - C[1] * C[1]);
+  const double t13 = (1.0 / 3.0) * I1, t23 = (2.0 / 3.0) * I2;
+  // W derivatives at (I1 J^-2/3, I2 J^-4/3) (materials_hyperelastic.cpp:135-204)
+  double a1, a2 = 0.0, a11 = 0.0;
+  if (mat_id == 1) {
+    a1 = 0.5 * mc[0];
+  } else if (mat_id == 2) {
+    const double d = I1 * pp - 3.0;
+    a1 = mc[0] + 2 * mc[1] * d + 3 * mc[2] * d * d;
+    a2 = mc[3];
+    a11 = 2 * mc[1] + 6 * mc[2] * d;
+  } else {
+    a1 = mc[0];
+    a2 = mc[1];
+  }
+  const double I6[6] = {1.0, 0.0, 0.0, 1.0, 0.0, 1.0};
+  double A[6], B[6];
+#pragma unroll
+  for (int i = 0; i < 6; i++) {
+    A[i] = I6[i] - t13 * Ci[i];
+    B[i] = I1 * I6[i] - C[i] - t23 * Ci[i];
+  }
+  const double ko1 = 2 * a1 * pp, ko2 = 2 * a2 * pppp, pJs = p_state * J;
+#pragma unroll
+  for (int i = 0; i < 6; i++) o.S[i] = ko1 * A[i] + ko2 * B[i] + pJs * Ci[i];
+  o.J = J;
+  // tangent coefficients (Dd before the reference's /2, times w)
+  const double k11 = 4.0 * a11 * pppp, k1 = (4.0 / 3.0) * a1 * pp, k2 = (8.0 / 3.0) * a2 * pppp;
+  const double pj = p_cur * J;
+  const double c0 = pj - k1 * t13 - k2 * t23;
+  const TT sIIt = (TT)(w * (2.0 * pj - k1 * I1 - k2 * I2));
+  const TT sI = (TT)(w * 1.5 * k2);
+  TT P[6], Q[6], R[6], At[6], Bt[6], Ct[6];
+#pragma unroll
+  for (int i = 0; i < 6; i++) {
+    P[i] = (TT)(w * (k11 * A[i] - k1 * Ci[i]));
+    Q[i] = (TT)(w * (-k2 * Ci[i]));
+    R[i] = (TT)(w * (-k1 * A[i] - k2 * B[i] + c0 * Ci[i]));
+    At[i] = (TT)A[i];
+    Bt[i] = (TT)B[i];
+    Ct[i] = (TT)Ci[i];
+  }
+  // IIt (materials_hyperelastic.cpp:97-108): -sym(Ci (x) Ci), packed upper
+  const TT c_xx = Ct[0], c_xy = Ct[1], c_xz = Ct[2], c_yy = Ct[3], c_yz = Ct[4], c_zz = Ct[5];
+  const TT h = (TT)0.5;
+  const TT IIt[21] = {
+      -c_xx * c_xx, -c_xx * c_xy, -c_xx * c_xz, -c_xy * c_xy, -c_xy * c_xz, -c_xz * c_xz,
+      -h * (c_xx * c_yy + c_xy * c_xy), -h * (c_xx * c_yz + c_xz * c_xy), -c_xy * c_yy,
+      -h * (c_xy * c_yz + c_xz * c_yy), -c_xz * c_yz,
+      -h * (c_xx * c_zz + c_xz * c_xz), -c_xy * c_yz, -h * (c_xy * c_zz + c_xz * c_yz),
+      -c_xz * c_zz,
+      -c_yy * c_yy, -c_yy * c_yz, -c_yz * c_yz,
+      -h * (c_yy * c_zz + c_yz * c_yz), -c_yz * c_zz,
+      -c_zz * c_zz};
+  // I (x) I - II, packed upper: +1 at (0,3),(0,5),(3,5); -1/2 at (1,1),(2,2),(4,4)
+  int idx = 0;
+#pragma unroll
+  for (int r = 0; r < 6; r++)
+#pragma unroll
+    for (int s = r; s < 6; s++, idx++) {
+      TT v = At[r] * P[s] + Bt[r] * Q[s] + Ct[r] * R[s] + sIIt * IIt[idx];
+      const bool plus = (r == 0 && (s == 3 || s == 5)) || (r == 3 && s == 5);
+      const bool minus = (r == s) && (r == 1 || r == 2 || r == 4);
+      if (plus) v += sI;
+      if (minus) v -= h * sI;
+      wD[idx] = v;
+    }
+  (void)B;
+}
+
+template <typename TT>
+__global__ void __launch_bounds__(kWarpsPerBlock * 32)
+    solid81_kernel(const Solid81Args a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint32_t* dec = reinterpret_cast<uint32_t*>(smem_raw);  // [kOwned][32]
+  WarpSmem<TT>* sm =
+      reinterpret_cast<WarpSmem<TT>*>(smem_raw + sizeof(uint32_t) * kOwned * 32) +
+      (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+
+  // Ownership of Kuu entries: lane owns x = lane + 32 m of the 4*300 entries
+  // of its warp's element quad.  Decode once: smem offsets of Bh[.][i, slot a]
+  // and DB[.][k, slot b].
+  for (int v = threadIdx.x; v < kOwned * 32; v += blockDim.x) {
+    const int m = v / 32, l = v % 32;
+    const int x = l + 32 * m;
+    uint32_t word = 0xFFFFFFFFu;
+    if (x < kEPW * kKuuPerElem) {
+      const int q = x / kKuuPerElem, t = x - q * kKuuPerElem;
+      const uchar4 en = c_kuu_entry[t];
+      const uint32_t bh = en.y * 32 + q * 8 + en.x;
+      const uint32_t db = en.w * 32 + q * 8 + en.z;
+      word = bh | (db << 16);
+    }
+    dec[m * 32 + l] = word;
+  }
+  __syncthreads();
+
+  const uint32_t E = a.n_elems;
+  const uint64_t E8 = (uint64_t)E * 8;
+  const uint64_t n_quads = (E + kEPW - 1) / kEPW;
+  const uint64_t warp_global = (uint64_t)blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+  const uint64_t warp_stride = (uint64_t)gridDim.x * kWarpsPerBlock;
+  const double kb = a.kbulk;
+
+  for (uint64_t quad = warp_global; quad < n_quads; quad += warp_stride) {
+    const uint32_t e0 = (uint32_t)(quad * kEPW);
+    const int q = lane >> 3;
+    const int sub = lane & 7;  // Gauss point in phase 1, node in phase 2
+    const uint32_t e = e0 + q;
+    const bool valid = e < E;
+    const uint32_t ec = valid ? e : E - 1;
+
+    // ---------------- phase 1: lane = (element q, Gauss point g) ----------------
+    double Fp_part, Kpp_part;
+    {
+      const int g = sub;
+      const uint64_t tg = (uint64_t)ec * 8 + g;
+      const double w = a.wdet[tg];
+      const double pc = a.U_cur[a.p_eq[ec] - 1];
+      double O[9];
+      double C[6];
+      double ps = 0.0;
+      if (a.have_state) {
+        double G[24];
+#pragma unroll
+        for (int c = 0; c < 24; c++) G[c] = __ldg(a.Gt + c * E8 + tg);
+#pragma unroll
+        for (int c = 0; c < 9; c++) O[c] = 0.0;
+#pragma unroll
+        for (int n = 0; n < 8; n++) {
+          const uint32_t nid = __ldg(a.conn + (uint64_t)ec * 8 + n);
+          const uint4 eq = __ldg(reinterpret_cast<const uint4*>(a.node_eq3) + (nid - 1));
+          const double ux = a.U_state[eq.x - 1], uy = a.U_state[eq.y - 1],
+                       uz = a.U_state[eq.z - 1];
+#pragma unroll
+          for (int j = 0; j < 3; j++) {
+            O[0 + j] = fma(ux, G[3 * n + j], O[0 + j]);
+            O[3 + j] = fma(uy, G[3 * n + j], O[3 + j]);
+            O[6 + j] = fma(uz, G[3 * n + j], O[6 + j]);
+          }
+        }
+        ps = a.U_state[a.p_eq[ec] - 1];
+        // C = F^T F from O (SOLID81.cpp:105-110)
+        C[0] = 1.0 + 2 * O[0] + O[0] * O[0] + O[3] * O[3] + O[6] * O[6];
+        C[3] = 1.0 + 2 * O[4] + O[1] * O[1] + O[4] * O[4] + O[7] * O[7];
+        C[5] = 1.0 + 2 * O[8] + O[2] * O[2] + O[5] * O[5] + O[8] * O[8];
+        C[1] = O[1] + O[3] + O[0] * O[1] + O[3] * O[4] + O[6] * O[7];
+        C[4] = O[5] + O[7] + O[1] * O[2] + O[4] * O[5] + O[7] * O[8];
+        C[2] = O[2] + O[6] + O[0] * O[2] + O[3] * O[5] + O[6] * O[8];
+      } else {
+        // state right after Element::pre(): C = I, S = 0, O = 0 (SOLID81.cpp:17-19)
+#pragma unroll
+        for (int c = 0; c < 9; c++) O[c] = 0.0;
+        C[0] = C[3] = C[5] = 1.0;
+        C[1] = C[2] = C[4] = 0.0;
+      }
+      MatOut<TT> mo;
+      TT wD[21];
+      material<TT>(a.mat_id, a.mc, C, ps, pc, w, mo, wD);
+      if (!a.have_state) {
+#pragma unroll
+        for (int i = 0; i < 6; i++) mo.S[i] = 0.0;
+      }
+      const double J = mo.J;
+      const double F[9] = {1.0 + O[0], O[1], O[2], O[3], 1.0 + O[4], O[5], O[6], O[7], 1.0 + O[8]};
+      const double S3[9] = {mo.S[0], mo.S[1], mo.S[2], mo.S[1], mo.S[3], mo.S[4],
+                            mo.S[2], mo.S[4], mo.S[5]};
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          const double fs = F[3 * i + 0] * S3[0 + k] + F[3 * i + 1] * S3[3 + k] +
+                            F[3 * i + 2] * S3[6 + k];
+          sm->wP[3 * i + k][lane] = -w * fs;
+        }
+      const double cof[9] = {F[4] * F[8] - F[5] * F[7], F[5] * F[6] - F[3] * F[8],
+                             F[3] * F[7] - F[4] * F[6], F[2] * F[7] - F[1] * F[8],
+                             F[0] * F[8] - F[2] * F[6], F[1] * F[6] - F[0] * F[7],
+                             F[1] * F[5] - F[2] * F[4], F[2] * F[3] - F[0] * F[5],
+                             F[0] * F[4] - F[1] * F[3]};
+#pragma unroll
+      for (int c = 0; c < 9; c++) {
+        sm->F[c][lane] = F[c];
+        sm->wCof[c][lane] = w * cof[c];
+      }
+#pragma unroll
+      for (int c = 0; c < 6; c++) sm->wS[c][lane] = w * mo.S[c];
+#pragma unroll
+      for (int c = 0; c < 21; c++) sm->wD[c][lane] = wD[c];
+      Fp_part = -(J - 1 - pc / kb) * w;
+      Kpp_part = -1.0 / kb * w;
+      // J = sqrt(det C) cannot see an inverted element; det F can
+      const double detF = F[0] * cof[0] + F[1] * cof[1] + F[2] * cof[2];
+      const bool bad = valid && !(J > 0.0 && isfinite(J) && detF > 0.0 && w > 0.0);
+      const unsigned ballot = __ballot_sync(0xFFFFFFFFu, bad);
+      if (sub == 0 && ((ballot >> (q * 8)) & 0xFFu)) flag_element(a.status, e + 1);
+    }
+#pragma unroll
+    for (int off = 1; off < 8; off <<= 1) {
+      Fp_part += __shfl_xor_sync(0xFFFFFFFFu, Fp_part, off);
+      Kpp_part += __shfl_xor_sync(0xFFFFFFFFu, Kpp_part, off);
+    }
+    __syncwarp();
+
+    // ---------------- phases 2 + 3 per Gauss point ----------------
+    TT acc[kOwned];
+#pragma unroll
+    for (int m = 0; m < kOwned; m++) acc[m] = (TT)0;
+    double Fu[3] = {0.0, 0.0, 0.0}, Kup[3] = {0.0, 0.0, 0.0};
+    const int node = sub;
+    for (int g = 0; g < 8; g++) {
+      const int s1 = q * 8 + g;
+      {
+        // phase 2: lane = (element q, node a)
+        const uint64_t tg = (uint64_t)ec * 8 + g;
+        const double G0 = __ldg(a.Gt + (3 * node + 0) * E8 + tg);
+        const double G1 = __ldg(a.Gt + (3 * node + 1) * E8 + tg);
+        const double G2 = __ldg(a.Gt + (3 * node + 2) * E8 + tg);
+        // residual and pressure coupling in FP64
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+          Fu[i] += sm->wP[3 * i + 0][s1] * G0 + sm->wP[3 * i + 1][s1] * G1 +
+                   sm->wP[3 * i + 2][s1] * G2;
+          Kup[i] += sm->wCof[3 * i + 0][s1] * G0 + sm->wCof[3 * i + 1][s1] * G1 +
+                    sm->wCof[3 * i + 2][s1] * G2;
+        }
+        const TT g0 = (TT)G0, g1 = (TT)G1, g2 = (TT)G2;
+        TT Fm[9];
+#pragma unroll
+        for (int c = 0; c < 9; c++) Fm[c] = (TT)sm->F[c][s1];
+        TT Bh[18];
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+          const TT f0 = Fm[3 * i + 0], f1 = Fm[3 * i + 1], f2 = Fm[3 * i + 2];
+          Bh[0 * 3 + i] = f0 * g0;
+          Bh[1 * 3 + i] = f1 * g0 + f0 * g1;
+          Bh[2 * 3 + i] = f2 * g0 + f0 * g2;
+          Bh[3 * 3 + i] = f1 * g1;
+          Bh[4 * 3 + i] = f2 * g1 + f1 * g2;
+          Bh[5 * 3 + i] = f2 * g2;
+        }
+        TT D[21];
+#pragma unroll
+        for (int c = 0; c < 21; c++) D[c] = sm->wD[c][s1];
+#pragma unroll
+        for (int r = 0; r < 6; r++)
+#pragma unroll
+          for (int k = 0; k < 3; k++) {
+            TT v = (TT)0;
+#pragma unroll
+            for (int s = 0; s < 6; s++) v += D[r <= s ? sym6(r, s) : sym6(s, r)] * Bh[s * 3 + k];
+            sm->DB[r * 3 + k][lane] = v;
+          }
+#pragma unroll
+        for (int c = 0; c < 18; c++) sm->Bh[c][lane] = Bh[c];
+        const TT sxx = (TT)sm->wS[0][s1], sxy = (TT)sm->wS[1][s1], sxz = (TT)sm->wS[2][s1],
+                 syy = (TT)sm->wS[3][s1], syz = (TT)sm->wS[4][s1], szz = (TT)sm->wS[5][s1];
+        sm->SG[0][lane] = sxx * g0 + sxy * g1 + sxz * g2;
+        sm->SG[1][lane] = sxy * g0 + syy * g1 + syz * g2;
+        sm->SG[2][lane] = sxz * g0 + syz * g1 + szz * g2;
+        sm->Ga[0][lane] = g0;
+        sm->Ga[1][lane] = g1;
+        sm->Ga[2][lane] = g2;
+      }
+      __syncwarp();
+      {
+        // phase 3: owned Kuu entries
+        const TT* Bf = &sm->Bh[0][0];
+        const TT* Df = &sm->DB[0][0];
+#pragma unroll
+        for (int m = 0; m < kOwned; m++) {
+          const uint32_t word = dec[m * 32 + lane];
+          if (word != 0xFFFFFFFFu) {
+            const uint32_t bh = word & 0xFFFFu, db = word >> 16;
+            TT v = acc[m];
+#pragma unroll
+            for (int r = 0; r < 6; r++) v += Bf[bh + r * 96] * Df[db + r * 96];
+            if ((bh >> 5) == (db >> 5)) {
+              const uint32_t sa = bh & 31u, sb = db & 31u;
+              v += sm->Ga[0][sa] * sm->SG[0][sb] + sm->Ga[1][sa] * sm->SG[1][sb] +
+                   sm->Ga[2][sa] * sm->SG[2][sb];
+            }
+            acc[m] = v;
+          }
+        }
+      }
+      __syncwarp();
+    }
+
+    // ---------------- write the element contributions ----------------
+#pragma unroll
+    for (int m = 0; m < kOwned; m++) {
+      const int x = lane + 32 * m;
+      if (x < kEPW * kKuuPerElem) {
+        const int qq = x / kKuuPerElem, t = x - qq * kKuuPerElem;
+        const uint32_t ee = e0 + qq;
+        if (ee < E) a.contribK[(uint64_t)ee * kSolidKc + t] = (double)acc[m];
+      }
+    }
+    if (valid) {
+      double* ck = a.contribK + (uint64_t)e * kSolidKc;
+      double* cf = a.contribF + (uint64_t)e * kSolidFc;
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        ck[300 + 3 * node + i] = Kup[i];
+        cf[3 * node + i] = Fu[i];
+      }
+      if (node == 0) {
+        ck[324] = Kpp_part;
+        cf[24] = Fp_part;
+      }
+    }
+    __syncwarp();
+  }
+}
+
+__global__ void solid81_jacobian_kernel(const JacobianArgs a) {
+  const uint64_t E8 = (uint64_t)a.n_elems * 8;
+  const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= E8) return;
+  const uint32_t e = (uint32_t)(t >> 3);
+  const int g = (int)(t & 7);
+  // Gauss point of ElementIsoParamHEXAHEDRON, order 2 (isoparametric.h:126-136)
+  const double r = (g & 1) ? kGaussA : -kGaussA;
+  const double s = (g & 2) ? kGaussA : -kGaussA;
+  const double u = (g & 4) ? kGaussA : -kGaussA;
+  // formFuncDeriv (isoparametric.cpp:211-221)
+  const double dN[24] = {
+      -0.125 * (1.0 - s) * (1.0 - u), -0.125 * (1.0 - r) * (1.0 - u), -0.125 * (1.0 - r) * (1.0 - s),
+      +0.125 * (1.0 - s) * (1.0 - u), -0.125 * (1.0 + r) * (1.0 - u), -0.125 * (1.0 + r) * (1.0 - s),
+      +0.125 * (1.0 + s) * (1.0 - u), +0.125 * (1.0 + r) * (1.0 - u), -0.125 * (1.0 + r) * (1.0 + s),
+      -0.125 * (1.0 + s) * (1.0 - u), +0.125 * (1.0 - r) * (1.0 - u), -0.125 * (1.0 - r) * (1.0 + s),
+      -0.125 * (1.0 - s) * (1.0 + u), -0.125 * (1.0 - r) * (1.0 + u), +0.125 * (1.0 - r) * (1.0 - s),
+      +0.125 * (1.0 - s) * (1.0 + u), -0.125 * (1.0 + r) * (1.0 + u), +0.125 * (1.0 + r) * (1.0 - s),
+      +0.125 * (1.0 + s) * (1.0 + u), +0.125 * (1.0 + r) * (1.0 + u), +0.125 * (1.0 + r) * (1.0 + s),
+      -0.125 * (1.0 + s) * (1.0 + u), +0.125 * (1.0 - r) * (1.0 + u), +0.125 * (1.0 - r) * (1.0 + s)};
+  double J[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (int n = 0; n < 8; n++) {
+    const uint32_t nid = a.conn[(uint64_t)e * 8 + n];
+    const double* X = a.xyz + (uint64_t)(nid - 1) * 3;
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) J[3 * i + j] += dN[3 * n + i] * X[j];
+  }
+  // Mat<3,3>::det / inv (Mat.cpp:23-46)
+  const double det = J[0] * (J[4] * J[8] - J[5] * J[7]) - J[1] * (J[3] * J[8] - J[5] * J[6]) +
+                     J[2] * (J[3] * J[7] - J[4] * J[6]);
+  const double sc = 1.0 / det;
+  const double Ji[9] = {(J[4] * J[8] - J[5] * J[7]) * sc, (J[2] * J[7] - J[1] * J[8]) * sc,
+                        (J[1] * J[5] - J[2] * J[4]) * sc, (J[6] * J[5] - J[3] * J[8]) * sc,
+                        (J[0] * J[8] - J[2] * J[6]) * sc, (J[3] * J[2] - J[0] * J[5]) * sc,
+                        (J[3] * J[7] - J[4] * J[6]) * sc, (J[1] * J[6] - J[0] * J[7]) * sc,
+                        (J[0] * J[4] - J[1] * J[3]) * sc};
+  for (int n = 0; n < 8; n++)
+    for (int i = 0; i < 3; i++) {
+      double v = 0.0;
+      for (int j = 0; j < 3; j++) v += Ji[3 * i + j] * dN[3 * n + j];
+      a.Gt[(uint64_t)(3 * n + i) * E8 + t] = v;
+    }
+  a.wdet[t] = 1.0 * det;
+  // isoparametric.cpp:177 logs det < 1e-20; here it is an element status
+  if (!(det >= 1.0e-20) && g == 0) flag_element(a.status, e + 1);
+}
+
+// K[s] = sum of its contributions in ascending contribution order (the
+// reference's element-ascending accumulation order), starting from 0.
+__global__ void gather_kernel(const GatherArgs a) {
+  const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= a.n_slots) return;
+  const uint32_t b = a.ptr[s], e = a.ptr[s + 1];
+  double v = 0.0;
+  for (uint32_t k = b; k < e; k++) v += a.contrib[a.ids[k]];
+  a.out[s] = v;
+}
+
+// Rigid-body MPC rows (RigidBodyMpc::update, Mpc.cpp:70-164, and
+// FEStorage.cpp:51-61): one thread per MPC equation.
+__global__ void mpc_kernel(const MpcArgs a) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= a.n_mpc) return;
+  const uint32_t* me = a.master_eq6 + (uint64_t)k * 6;
+  const double w0[3] = {a.U[me[0] - 1], a.U[me[1] - 1], a.U[me[2] - 1]};
+  const double th[3] = {a.U[me[3] - 1], a.U[me[4] - 1], a.U[me[5] - 1]};
+  const double tn = sqrt(th[0] * th[0] + th[1] * th[1] + th[2] * th[2]);
+  double c1, c2, c3, c4;
+  if (tn < 1.0e-3) {
+    c1 = 1.0;
+    c2 = 0.5;
+    c3 = -1.0 / 3.0;
+    c4 = -1.0 / 12.0;
+  } else {
+    const double sn = sin(tn), cs = cos(tn);
+    c1 = sn / tn;
+    c2 = (1.0 - cs) / (tn * tn);
+    c3 = (tn * cs - sn) / (tn * tn * tn);
+    c4 = (tn * sn - 2.0 + 2.0 * cs) / (tn * tn * tn * tn);
+  }
+  // Levi-Civita e_{i m j} with the reference's table (solidmech.h:24-33)
+  auto lc = [](int i, int m, int j) -> double {
+    if (i == m || m == j || i == j) return 0.0;
+    return ((i == 0 && m == 1 && j == 2) || (i == 1 && m == 2 && j == 0) ||
+            (i == 2 && m == 0 && j == 1))
+               ? 1.0
+               : -1.0;
+  };
+  const int i = a.slave_dof[k];
+  const double ct = cos(tn);
+  double Crow[3];
+  for (int j = 0; j < 3; j++) {
+    const double tm = lc(i, 0, j) * th[0] + lc(i, 1, j) * th[1] + lc(i, 2, j) * th[2];
+    Crow[j] = ct * (i == j ? 1.0 : 0.0) + c1 * tm + c2 * th[i] * th[j];
+  }
+  const double* mp = a.xyz + (uint64_t)(a.master[k] - 1) * 3;
+  const double* sp = a.xyz + (uint64_t)(a.slave[k] - 1) * 3;
+  const double pq[3] = {sp[0] - mp[0], sp[1] - mp[1], sp[2] - mp[2]};
+  double cD[3][3];
+  for (int j = 0; j < 3; j++)
+    for (int l = 0; l < 3; l++) {
+      const double Iij = i == j ? 1.0 : 0.0, Iil = i == l ? 1.0 : 0.0, Ijl = j == l ? 1.0 : 0.0;
+      cD[j][l] = Iij * (-c1) * th[l] +
+                 c3 * th[l] * (lc(i, 0, j) * th[0] + lc(i, 1, j) * th[1] + lc(i, 2, j) * th[2]) +
+                 c1 * lc(i, l, j) + c4 * th[l] * th[i] * th[j] + c2 * (Iil * th[j] + th[i] * Ijl);
+    }
+  const double b = w0[i] + (Crow[0] - (i == 0)) * pq[0] + (Crow[1] - (i == 1)) * pq[1] +
+                   (Crow[2] - (i == 2)) * pq[2] - a.U[a.slave_eq[k] - 1];
+  const uint32_t* sl = a.slot + (uint64_t)k * 5;
+  a.K[sl[0]] += 1.0;
+  a.K[sl[1]] += -1.0;
+  for (int l = 0; l < 3; l++)
+    a.K[sl[2 + l]] += -(cD[0][l] * pq[0] + cD[1][l] * pq[1] + cD[2][l] * pq[2]);
+  a.F[a.eq[k] - 1] = b;
+}
+
+// TETRA0 (TETRA0.cpp:18-78, 110-199) and QUADTH (QUADTH.cpp:22-49): one
+// thread per element; contributions in Element::assembleK order.
+__device__ double det4_lu(double* m) {
+  double det = 1.0;
+  for (int k = 0; k < 4; k++) {
+    int p = k;
+    double best = fabs(m[k * 4 + k]);
+    for (int i = k + 1; i < 4; i++) {
+      const double v = fabs(m[i * 4 + k]);
+      if (v > best) {
+        best = v;
+        p = i;
+      }
+    }
+    if (best == 0.0) return 0.0;
+    if (p != k) {
+      for (int j = 0; j < 4; j++) {
+        const double t = m[k * 4 + j];
+        m[k * 4 + j] = m[p * 4 + j];
+        m[p * 4 + j] = t;
+      }
+      det = -det;
+    }
+    const double piv = m[k * 4 + k];
+    det *= piv;
+    for (int i = k + 1; i < 4; i++) {
+      const double f = m[i * 4 + k] / piv;
+      for (int j = k + 1; j < 4; j++) m[i * 4 + j] -= f * m[k * 4 + j];
+    }
+  }
+  return det;
+}
+
+__global__ void linear_kernel(const LinearArgs a) {
+  const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= a.n_elems) return;
+  const uint32_t* c = a.conn + (uint64_t)e * 4;
+  double P[4][3];
+  for (int n = 0; n < 4; n++)
+    for (int d = 0; d < 3; d++) P[n][d] = a.xyz[(uint64_t)(c[n] - 1) * 3 + d];
+  if (a.etype == 3) {
+    double S[16];
+    for (int n = 0; n < 4; n++) {
+      S[n * 4 + 0] = 1.0;
+      S[n * 4 + 1] = P[n][0];
+      S[n * 4 + 2] = P[n][1];
+      S[n * 4 + 3] = P[n][2];
+    }
+    const double vol = det4_lu(S) / 6.0;
+    if (!(vol > 0.0)) flag_element(a.status, e + 1);
+    const double Em = a.eparams[2 * (uint64_t)e], my = a.eparams[2 * (uint64_t)e + 1];
+    const double Ac = Em / ((1. + my) * (1. - 2. * my));
+    // C (6x6, makeC) as dense
+    double Cm[6][6] = {};
+    Cm[0][0] = Cm[1][1] = Cm[2][2] = (1. - my) * Ac;
+    Cm[0][1] = Cm[1][0] = Cm[0][2] = Cm[2][0] = Cm[1][2] = Cm[2][1] = my * Ac;
+    Cm[3][3] = Cm[4][4] = Cm[5][5] = (1. / 2. - my) * Ac;
+    // makeB: b, c, d coefficients
+    auto X = [&](int n, int d) { return P[n][d]; };
+    const double x12 = X(0, 0) - X(1, 0), x13 = X(0, 0) - X(2, 0), x14 = X(0, 0) - X(3, 0);
+    const double x23 = X(1, 0) - X(2, 0), x24 = X(1, 0) - X(3, 0), x34 = X(2, 0) - X(3, 0);
+    const double y12 = X(0, 1) - X(1, 1), y13 = X(0, 1) - X(2, 1), y14 = X(0, 1) - X(3, 1);
+    const double y23 = X(1, 1) - X(2, 1), y24 = X(1, 1) - X(3, 1), y34 = X(2, 1) - X(3, 1);
+    const double z12 = X(0, 2) - X(1, 2), z13 = X(0, 2) - X(2, 2), z14 = X(0, 2) - X(3, 2);
+    const double z23 = X(1, 2) - X(2, 2), z24 = X(1, 2) - X(3, 2), z34 = X(2, 2) - X(3, 2);
+    const double x21 = -x12, x31 = -x13, x32 = -x23, x42 = -x24, x43 = -x34;
+    const double y21 = -y12, y31 = -y13, y32 = -y23, y42 = -y24, y43 = -y34;
+    const double z21 = -z12, z31 = -z13, z32 = -z23, z42 = -z24, z43 = -z34;
+    const double bb[4] = {y42 * z32 - y32 * z42, y31 * z43 - y34 * z13, y24 * z14 - y14 * z24,
+                          y13 * z21 - y12 * z31};
+    const double cc[4] = {x32 * z42 - x42 * z32, x43 * z31 - x13 * z34, x14 * z24 - x24 * z14,
+                          x21 * z13 - x31 * z12};
+    const double dd[4] = {x42 * y32 - x32 * y42, x31 * y43 - x34 * y13, x24 * y14 - x14 * y24,
+                          x13 * y21 - x12 * y31};
+    const double Af = -1. / 6. / vol;
+    double B[6][12] = {};
+    for (int i = 0; i < 4; i++) {
+      B[0][3 * i + 0] = bb[i] * Af;
+      B[1][3 * i + 1] = cc[i] * Af;
+      B[2][3 * i + 2] = dd[i] * Af;
+      B[3][3 * i + 0] = cc[i] * Af;
+      B[3][3 * i + 1] = bb[i] * Af;
+      B[4][3 * i + 1] = dd[i] * Af;
+      B[4][3 * i + 2] = cc[i] * Af;
+      B[5][3 * i + 0] = dd[i] * Af;
+      B[5][3 * i + 2] = bb[i] * Af;
+    }
+    double* out = a.contribK + (uint64_t)e * 78;
+    int idx = 0;
+    for (int r = 0; r < 12; r++)
+      for (int col = r; col < 12; col++, idx++) {
+        double v = 0.0;
+        for (int k = 0; k < 6; k++) {
+          double cb = 0.0;
+          for (int l = 0; l < 6; l++) cb += Cm[k][l] * B[l][col];
+          v += B[k][r] * cb;
+        }
+        out[idx] = v * vol;
+      }
+  } else {
+    // QUADTH: 2x2 Gauss (isoparametric.h:80-85), conduction k (QUADTH.cpp:22-49)
+    const double kc = a.eparams[2 * (uint64_t)e];
+    double Ke[10] = {};
+    for (int g = 0; g < 4; g++) {
+      const double r = (g & 1) ? kGaussA : -kGaussA;
+      const double s = (g & 2) ? kGaussA : -kGaussA;
+      const double dN[4][2] = {{-0.25 * (1.0 - s), -0.25 * (1.0 - r)},
+                               {+0.25 * (1.0 - s), -0.25 * (1.0 + r)},
+                               {+0.25 * (1.0 + s), +0.25 * (1.0 + r)},
+                               {-0.25 * (1.0 + s), +0.25 * (1.0 - r)}};
+      double J[2][2] = {};
+      for (int n = 0; n < 4; n++)
+        for (int i = 0; i < 2; i++)
+          for (int j = 0; j < 2; j++) J[i][j] += dN[n][i] * P[n][j];
+      const double det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+      if (!(det >= 1.0e-20)) flag_element(a.status, e + 1);
+      const double s1 = 1.0 / det;
+      const double Ji[2][2] = {{J[1][1] * s1, -J[0][1] * s1}, {-J[1][0] * s1, J[0][0] * s1}};
+      double G[4][2];
+      for (int n = 0; n < 4; n++)
+        for (int i = 0; i < 2; i++) G[n][i] = Ji[i][0] * dN[n][0] + Ji[i][1] * dN[n][1];
+      const double w = 1.0 * det;
+      int idx = 0;
+      for (int i = 0; i < 4; i++)
+        for (int j = i; j < 4; j++, idx++)
+          Ke[idx] += (G[i][0] * kc * G[j][0] + G[i][1] * kc * G[j][1]) * w;
+    }
+    double* out = a.contribK + (uint64_t)e * 10;
+    for (int i = 0; i < 10; i++) out[i] = Ke[i];
+    double* f = a.contribF + (uint64_t)e * 4;
+    for (int i = 0; i < 4; i++) f[i] = 0.0;  // volFlux = 0 (QUADTH.cpp:34-36)
+  }
+}
+
+// FMA throughput probe: 8 independent chains per thread, enough warps per SM
+// to cover the pipe latency; every result is folded into one store so the
+// chains cannot be removed.
+template <typename T>
+__global__ void fma_probe_kernel(T* out, int iters, T a, T b) {
+  T x[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) x[k] = (T)(threadIdx.x + k);
+  for (int i = 0; i < iters; i++)
+#pragma unroll
+    for (int k = 0; k < 8; k++) x[k] = x[k] * a + b;
+  T s = 0;
+#pragma unroll
+  for (int k = 0; k < 8; k++) s += x[k];
+  if (s == (T)-12345.0) out[0] = s;
+}
+
+int g_tables_ready_device = -1;
+
+cudaError_t ensure_tables() {
+  int dev = 0;
+  cudaError_t err = cudaGetDevice(&dev);
+  if (err != cudaSuccess) return err;
+  if (g_tables_ready_device == dev) return cudaSuccess;
+  uchar4 h[kKuuPerElem];
+  int t = 0;
+  for (int i = 0; i < 8; i++)
+    for (int di = 0; di < 3; di++)
+      for (int j = i; j < 8; j++)
+        for (int dj = 0; dj < 3; dj++) {
+          if (i == j && dj < di) continue;
+          h[t++] = make_uchar4((unsigned char)i, (unsigned char)di, (unsigned char)j,
+                               (unsigned char)dj);
+        }
+  err = cudaMemcpyToSymbol(c_kuu_entry, h, sizeof(h));
+  if (err == cudaSuccess) g_tables_ready_device = dev;
+  return err;
+}
+
+}  // namespace
+
+size_t solid81_smem_bytes(bool mixed) {
+  const size_t dec = sizeof(uint32_t) * kOwned * 32;
+  return dec + kWarpsPerBlock * (mixed ? sizeof(WarpSmem<float>) : sizeof(WarpSmem<double>));
+}
+
+cudaError_t launch_solid81_jacobian(const JacobianArgs& a, cudaStream_t s) {
+  const uint64_t n = (uint64_t)a.n_elems * 8;
+  if (n == 0) return cudaSuccess;
+  const int bs = 256;
+  solid81_jacobian_kernel<<<(unsigned)((n + bs - 1) / bs), bs, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_solid81(const Solid81Args& a, bool mixed, int blocks_per_sm_hint,
+                           cudaStream_t s) {
+  if (a.n_elems == 0) return cudaSuccess;
+  cudaError_t err = ensure_tables();
+  if (err != cudaSuccess) return err;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const size_t smem = solid81_smem_bytes(mixed);
+  auto kern = mixed ? solid81_kernel<float> : solid81_kernel<double>;
+  err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (err != cudaSuccess) return err;
+  int per_sm = blocks_per_sm_hint;
+  if (per_sm <= 0) {
+    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kWarpsPerBlock * 32, smem);
+    if (err != cudaSuccess) return err;
+    if (per_sm < 1) per_sm = 1;
+  }
+  const uint64_t quads = ((uint64_t)a.n_elems + kEPW - 1) / kEPW;
+  uint64_t blocks = (uint64_t)sms * per_sm;
+  const uint64_t need = (quads + kWarpsPerBlock - 1) / kWarpsPerBlock;
+  if (blocks > need) blocks = need;
+  kern<<<(unsigned)blocks, kWarpsPerBlock * 32, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t probe_fma_peak(bool fp64, double* flops) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  void* buf = nullptr;
+  cudaError_t e = cudaMalloc(&buf, 16);
+  if (e != cudaSuccess) return e;
+  const int threads = 512, blocks = sms * 4;
+  const int iters = fp64 ? 4096 : 65536;
+  cudaEvent_t t0, t1;
+  cudaEventCreate(&t0);
+  cudaEventCreate(&t1);
+  float best = 1e30f;
+  for (int rep = 0; rep < 4; rep++) {
+    cudaEventRecord(t0);
+    if (fp64)
+      fma_probe_kernel<double><<<blocks, threads>>>((double*)buf, iters, 0.999999, 1e-7);
+    else
+      fma_probe_kernel<float><<<blocks, threads>>>((float*)buf, iters, 0.9999f, 1e-7f);
+    cudaEventRecord(t1);
+    e = cudaEventSynchronize(t1);
+    if (e != cudaSuccess) break;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, t0, t1);
+    if (rep > 0 && ms < best) best = ms;
+  }
+  if (e == cudaSuccess) e = cudaGetLastError();
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  cudaFree(buf);
+  *flops = 2.0 * 8.0 * (double)iters * threads * blocks / (best * 1e-3);
+  return e;
+}
+
+cudaError_t launch_gather(const GatherArgs& a, cudaStream_t s) {
+  if (a.n_slots == 0) return cudaSuccess;
+  const int bs = 256;
+  gather_kernel<<<(unsigned)((a.n_slots + bs - 1) / bs), bs, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mpc(const MpcArgs& a, cudaStream_t s) {
+  if (a.n_mpc == 0) return cudaSuccess;
+  const int bs = 128;
+  mpc_kernel<<<(a.n_mpc + bs - 1) / bs, bs, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_linear(const LinearArgs& a, cudaStream_t s) {
+  if (a.n_elems == 0) return cudaSuccess;
+  const int bs = 128;
+  linear_kernel<<<(a.n_elems + bs - 1) / bs, bs, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace nla3d_gpu

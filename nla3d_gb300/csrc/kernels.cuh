@@ -1,0 +1,88 @@
+// Device-side argument blocks and launchers of the assembly kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace nla3d_gpu {
+
+constexpr int kSolidKc = 325;  // SOLID81 K contributions per element (300 Kuu + 24 Kup + 1 Kpp)
+constexpr int kSolidFc = 25;   // SOLID81 F contributions per element (24 Fu + 1 Fp)
+
+struct ElementStatus {
+  uint32_t count;  // elements flagged (J <= 0, det J <= 0, non-finite)
+  uint32_t first;  // smallest flagged 1-based element number, 0xFFFFFFFF if none
+};
+
+struct Solid81Args {
+  uint32_t n_elems;
+  const double* Gt;         // dN/dX, structure of arrays: Gt[c * E8 + e*8 + g], c = 3*node + dim
+  const double* wdet;       // Gauss weight * det J, [e*8 + g]
+  const uint32_t* conn;     // 8 node ids per element, 1-based
+  const uint32_t* node_eq3; // per node: equation numbers of UX, UY, UZ (1-based), 4 per node
+  const uint32_t* p_eq;     // per element: equation number of HYDRO_PRESSURE
+  const double* U_state;    // vecU captured by the last updateResults()
+  const double* U_cur;      // current vecU
+  int have_state;           // 0: state of Element::pre() (C = I, S = 0, O = 0)
+  int mat_id;
+  double mc[5];
+  double kbulk;
+  double* contribK;         // [E * 325]
+  double* contribF;         // [E * 25]
+  ElementStatus* status;
+};
+
+struct JacobianArgs {
+  uint32_t n_elems;
+  const double* xyz;
+  const uint32_t* conn;
+  double* Gt;
+  double* wdet;
+  ElementStatus* status;
+};
+
+struct GatherArgs {
+  uint64_t n_slots;
+  const uint32_t* ptr;   // n_slots + 1
+  const uint32_t* ids;   // contribution ids
+  const double* contrib;
+  double* out;
+};
+
+struct MpcArgs {
+  uint32_t n_mpc;
+  const uint32_t* master;     // per MPC: master node
+  const uint32_t* slave;      // per MPC: slave node
+  const int32_t* slave_dof;   // per MPC: UX/UY/UZ
+  const uint32_t* eq;         // per MPC: its equation number
+  const uint32_t* master_eq6; // per MPC: eqs of master UX,UY,UZ,ROTX,ROTY,ROTZ (6 each)
+  const uint32_t* slave_eq;   // per MPC: eq of the slave DoF
+  const uint32_t* slot;       // per MPC: 5 K slots
+  const double* xyz;
+  const double* U;
+  double* K;                  // concatenated K values
+  double* F;
+};
+
+struct LinearArgs {
+  int etype;
+  uint32_t n_elems;
+  const double* xyz;
+  const uint32_t* conn;
+  const double* eparams;
+  double* contribK;
+  double* contribF;
+  ElementStatus* status;
+};
+
+// Launchers (return cudaError_t of the launch).
+cudaError_t launch_solid81_jacobian(const JacobianArgs& a, cudaStream_t s);
+cudaError_t launch_solid81(const Solid81Args& a, bool mixed, int blocks_per_sm_hint,
+                           cudaStream_t s);
+cudaError_t launch_gather(const GatherArgs& a, cudaStream_t s);
+cudaError_t launch_mpc(const MpcArgs& a, cudaStream_t s);
+cudaError_t launch_linear(const LinearArgs& a, cudaStream_t s);
+size_t solid81_smem_bytes(bool mixed);
+cudaError_t probe_fma_peak(bool fp64, double* flops);
+
+}  // namespace nla3d_gpu

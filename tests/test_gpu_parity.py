@@ -1,0 +1,134 @@
+"""GPU parity of the assembly path through the C ABI (libnla3d_gpu.so).
+
+Tolerance (FP64 path): max |K_gpu - K_ref| / max |K_ref| <= 1e-12 per K block
+and the same for F, against (a) the committed fixtures produced by the
+reference's own compiled sources and (b) the bit-exact CPU oracle.  The mixed
+path keeps F in FP64 (same 1e-12 bound) and its FP32 tangent within 2e-5.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import cases
+from nla3d_gb300 import meshgen as mg
+from nla3d_gb300.storage import FEStorage, assemble_state
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+TOL_FP64 = 1e-12
+TOL_MIXED_K = 2e-5
+
+
+def rel(a, b):
+    if b.size == 0:
+        return 0.0
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def _gpu(case, precision="fp64"):
+    mesh, u, p, extra, do_update = case()
+    return assemble_state(mesh, u, p, precision, extra, do_update)
+
+
+@pytest.mark.parametrize("name", sorted(cases.FULL_CASES))
+def test_fp64_matches_reference_fixtures(name):
+    g = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    s, U, K, F = _gpu(cases.FULL_CASES[name])
+    assert np.array_equal(U, g["U"])
+    for b in (1, 12, 2):
+        assert rel(K[b], g[f"K_{b}"]) <= TOL_FP64, (b, rel(K[b], g[f"K_{b}"]))
+    assert rel(F, g["F"]) <= TOL_FP64, rel(F, g["F"])
+    assert s.element_status() == (0, 0)
+
+
+def test_fp64_cube10_matches_oracle():
+    mesh, u, p, extra, do_update = cases.cube10_nh()
+    s, U, K, F = assemble_state(mesh, u, p, "fp64")
+    m, Uo, Ko, Fo = O.solve_state(mesh, u, p, "port")
+    assert np.array_equal(U, Uo)
+    for b in (1, 12, 2):
+        assert rel(K[b], Ko[b]) <= TOL_FP64
+    assert rel(F, Fo) <= TOL_FP64
+
+
+def test_mixed_precision_bounds():
+    mesh, u, p, extra, do_update = cases.cube10_nh()
+    _, _, K64, F64 = assemble_state(mesh, u, p, "fp64")
+    _, _, K32, F32 = assemble_state(mesh, u, p, "mixed")
+    assert rel(F32, F64) <= TOL_FP64       # residual stays FP64
+    assert rel(K32[2], K64[2]) <= TOL_MIXED_K
+    assert rel(K32[2], K64[2]) > 0.0       # the tangent really ran in FP32
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_run_to_run_bitwise_reproducible(precision):
+    mesh, u, p, extra, do_update = cases.cube4_nh_clamped()
+    s = FEStorage(mesh, precision).initSolutionData()
+    ne, ee = s.eq_numbers()
+    s.setU(mg.u_to_vector(ne, ee, u, p, s.n_total))
+    s.updateResults()
+    s.assembleGlobalEqMatrices()
+    first = [s.K(b).copy() for b in (1, 12, 2)] + [s.F().copy()]
+    for _ in range(3):
+        s.assembleGlobalEqMatrices()
+        again = [s.K(b) for b in (1, 12, 2)] + [s.F()]
+        for x, y in zip(first, again):
+            assert np.array_equal(x.view(np.uint64), y.view(np.uint64))
+
+
+def test_fresh_state_and_stale_state_semantics():
+    """assemble() before any updateResults() uses the Element::pre() state
+    (C = I, S = 0); after updateResults(U1), a new U2 changes only the
+    pressure read by buildK (SOLID81.cpp:48) -- exactly as the reference."""
+    mesh, u, p, _, _ = cases.cube3_nh()
+    o = O.OracleModel(mesh, "port")
+    s = FEStorage(mesh).initSolutionData()
+    ne, ee = s.eq_numbers()
+    U1 = mg.u_to_vector(ne, ee, u, p, s.n_total)
+    # fresh
+    o.set_U(U1); o.assemble()
+    s.setU(U1); s.assembleGlobalEqMatrices()
+    assert rel(s.K(2), o.K(2)) <= TOL_FP64 and rel(s.F(), o.F()) <= TOL_FP64
+    # stale: update with U1, assemble with U2
+    U2 = mg.u_to_vector(ne, ee, 0.5 * u, p + 0.05, s.n_total)
+    o.update(); o.set_U(U2); o.assemble()
+    s.updateResults(); s.setU(U2); s.assembleGlobalEqMatrices()
+    assert rel(s.K(2), o.K(2)) <= TOL_FP64 and rel(s.F(), o.F()) <= TOL_FP64
+
+
+@pytest.mark.parametrize("mat", [(mg.MAT_NEO_HOOKEAN, (1.3, 700.0)),
+                                 (mg.MAT_MOONEY_RIVLIN, (0.4, 0.1, 2000.0)),
+                                 (mg.MAT_BIDERMAN, (0.4, 0.03, 0.002, 0.05, 900.0))])
+def test_fp64_materials_twist_vs_oracle(mat):
+    mesh = mg.solid81_block(6, 5, 7, 0.2, mat[0], mat[1], clamp_z0=True)
+    u, p = mg.twist_state(mesh, angle_deg=25.0, stretch=1.4, noise_frac=0.01, seed=9)
+    _, _, K, F = assemble_state(mesh, u, p, "fp64")
+    _, _, Ko, Fo = O.solve_state(mesh, u, p, "port")
+    for b in (1, 12, 2):
+        assert rel(K[b], Ko[b]) <= TOL_FP64
+    assert rel(F, Fo) <= TOL_FP64
+
+
+def test_element_status_flags_inverted_element():
+    mesh, u, p, _, _ = cases.cube3_nh()
+    u = u.copy()
+    # fold node 14 (an interior node) far through its neighbours: J <= 0 nearby
+    u[13] = [-3.0, -3.0, -3.0]
+    s, _, K, F = assemble_state(mesh, u, p, "fp64")
+    count, first = s.element_status()
+    assert count > 0 and 1 <= first <= mesh.n_elems
+
+
+def test_larger_mesh_properties():
+    """40^3 twisted Mooney-Rivlin block: free body => sum of internal nodal
+    forces ~ 0; FP64 vs port at 1e-12 on the full K."""
+    mesh, u, p = mg.config_twist(n=24, seed=4)
+    s, U, K, F = assemble_state(mesh, u, p, "fp64")
+    ne, ee = s.eq_numbers()
+    for d in range(3):
+        fd = F[ne[:, d].astype(np.int64) - 1]
+        assert abs(fd.sum()) <= 1e-12 * np.abs(fd).sum() * 10
+    _, _, Ko, Fo = O.solve_state(mesh, u, p, "port")
+    assert rel(K[2], Ko[2]) <= TOL_FP64 and rel(F, Fo) <= TOL_FP64
