@@ -1,0 +1,416 @@
+"""Benchmark of the SOLID81 per-iteration global assembly on GB300.
+
+Workload (one "step" = FEStorage::updateResults + assembleGlobalEqMatrices of
+the whole mesh): a 100x100x100 block of SOLID81 u/p hexahedra on the unit cube
+(1e6 elements, 1,030,301 nodes, 4,090,903 equations, 149,264,506 upper-CSR
+nonzeros), Mooney-Rivlin C10 = 0.4, C01 = 0.1, K = 2000; nodal displacements
+from a 30 degree end twist plus 1.5 stretch with seeded +-0.005h noise;
+element pressures ~ N(0, 0.1).  Synthetic inputs (no dataset exists).
+
+Arms:
+  default            this repo's GPU path (libnla3d_gpu.so through its C ABI)
+  --impl reference   the reference's algorithm on the host cores (the oracle
+                     port, oracle/nla3d_oracle.c, which reproduces the
+                     reference bit for bit), all cores, independent samples
+
+Output: one JSON line (rank 0).  `value` = elements/s / 1e6 with inputs
+resident in HBM; `e2e` = the same through the C ABI with host buffers (U
+copied in, all K blocks and F copied out every step).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FLOP_PER_ELEM = 69072          # FP64 structured algorithm, 8 Gauss points x 8634
+BYTES_PER_ELEM_ALGO = 2700     # compulsory HBM traffic per element (connectivity,
+                               # X/U, p, slot map, K written once, F)
+METRIC = "SOLID81 assembly Melem/s"
+UNIT = "Melem/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=100, help="hex elements per side")
+    ap.add_argument("--cpu-sample-n", type=int, default=30)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def workload(n):
+    from nla3d_gb300 import meshgen as mg
+    mesh, u, p = mg.config_twist(n=n, seed=2)
+    return mesh, u, p
+
+
+def workload_config(mesh, extra=None):
+    cfg = {
+        "workload": f"SOLID81 u/p hex block {round(mesh.n_elems ** (1 / 3))}^3 on the unit cube, "
+                    "Mooney-Rivlin C10=0.4 C01=0.1 K=2000, 30deg twist + 1.5 stretch, "
+                    "+-0.005h noise, p~N(0,0.1); step = updateResults + "
+                    "assembleGlobalEqMatrices",
+        "elements": mesh.n_elems,
+        "nodes": mesh.n_nodes,
+        "l2": "no flush: inputs larger than L2 (element contributions 2.6 GB, gather lists "
+              "1.9 GB, K 1.2 GB per step at 1e6 elements)",
+    }
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+# ---------------------------------------------------------------------------
+# CPU side: the reference's algorithm (oracle port), bounded sample.
+# ---------------------------------------------------------------------------
+
+def _cpu_sample_worker(args):
+    n, reps, budget_s = args
+    sys.path.insert(0, ROOT)
+    from oracle import oracle as O
+    from nla3d_gb300 import meshgen as mg
+    mesh, u, p = mg.config_twist(n=n, seed=2)
+    m = O.OracleModel(mesh, "port")
+    ne, ee = m.eq_numbers()
+    m.set_U(mg.u_to_vector(ne, ee, u, p, m.n_total))
+    m.update()
+    m.assemble()                      # warm-up
+    times = []
+    t_start = time.perf_counter()
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        m.update()
+        m.assemble()
+        times.append(time.perf_counter() - t0)
+        if time.perf_counter() - t_start > budget_s:
+            break
+    return mesh.n_elems, times
+
+
+def cpu_baseline_single(n, budget_s=15.0):
+    """One host thread, the reference algorithm on an n^3 sample."""
+    ne, times = _cpu_sample_worker((n, 50, budget_s))
+    t = statistics.median(times)
+    return {"value": ne / t / 1e6, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{n}^3 = {ne} SOLID81 elements of the same workload (twist+stretch, "
+                      f"Mooney-Rivlin), median of {len(times)} updateResults+assemble calls "
+                      "on 1 host thread; oracle/nla3d_oracle.c reproduces the reference "
+                      "bit for bit"}
+
+
+_WORKER = {}
+
+
+def _worker_init(n):
+    sys.path.insert(0, ROOT)
+    from oracle import oracle as O
+    from nla3d_gb300 import meshgen as mg
+    mesh, u, p = mg.config_twist(n=n, seed=2)
+    m = O.OracleModel(mesh, "port")
+    ne, ee = m.eq_numbers()
+    m.set_U(mg.u_to_vector(ne, ee, u, p, m.n_total))
+    _WORKER["m"], _WORKER["ne"] = m, mesh.n_elems
+
+
+def _worker_step(_):
+    m = _WORKER["m"]
+    t0 = time.perf_counter()
+    m.update()
+    m.assemble()
+    return _WORKER["ne"], time.perf_counter() - t0
+
+
+def run_reference(args):
+    """The reference's algorithm on all host cores: one independent sample
+    per core (the reference itself is single-threaded)."""
+    import multiprocessing as mp
+    from oracle import oracle as O
+    O.build_port()
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    n = args.cpu_sample_n
+    steps = []
+    with ctx.Pool(cores, initializer=_worker_init, initargs=(n,)) as pool:
+        for i in range(args.warmup + args.steps):
+            res = pool.map(_worker_step, range(cores), chunksize=1)
+            if i >= args.warmup:
+                steps.append((sum(r[0] for r in res), max(r[1] for r in res)))
+    ne = steps[0][0]
+    t = statistics.median(s[1] for s in steps)
+    value = ne / t / 1e6
+    mesh = workload(n)[0]
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "impl": "reference",
+        "config": workload_config(mesh, {"note": f"{cores} independent {n}^3 samples, one per "
+                                                 "host core (the reference is single-threaded)"}),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{cores} processes x {n}^3 = {ne // cores} SOLID81 elements, "
+                                   "one updateResults+assemble each per step; "
+                                   "oracle/nla3d_oracle.c reproduces the reference bit for bit"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU side
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def time_steps(st, U_dev, n_total, steps, torch, stream):
+    """Device-resident steps: U already in HBM; returns seconds per step."""
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(steps):
+        st.setU_device(U_dev.data_ptr(), n_total)
+        st.updateResults()
+        st.assembleGlobalEqMatrices()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    return ev0.elapsed_time(ev1) / 1e3 / steps
+
+
+def run_ours(args):
+    import torch
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    torch.cuda.set_device(local)
+    from nla3d_gb300 import meshgen as mg
+    from nla3d_gb300.storage import FEStorage, probe_fma_peak
+
+    # CPU baseline first (rank 0, N=1 only), before any GPU work
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline_single(args.cpu_sample_n)
+
+    mesh, u, p = workload(args.n)
+    stream = torch.cuda.Stream()
+    t0 = time.perf_counter()
+    st = FEStorage(mesh, "fp64", stream=stream.cuda_stream).initSolutionData()
+    setup_s = time.perf_counter() - t0
+    ne, ee = st.eq_numbers()
+    U = mg.u_to_vector(ne, ee, u, p, st.n_total)
+    U_dev = torch.from_numpy(U).to(f"cuda:{local}")
+    nnz = sum(st.blocks[b][2] for b in (1, 12, 2))
+
+    # warm-up
+    for _ in range(args.warmup):
+        st.setU_device(U_dev.data_ptr(), st.n_total)
+        st.updateResults()
+        st.assembleGlobalEqMatrices()
+    torch.cuda.synchronize()
+    count, _first = st.element_status()
+
+    # timed region: device-resident inputs, per-kernel CUDA events on the same stream
+    st.set_timing(True)
+    launches0 = st.kernel_launches()
+    if dist:
+        dist.barrier()
+    with ClockSampler(local) as clk:
+        sec = time_steps(st, U_dev, st.n_total, args.steps, torch, stream)
+    launches = st.kernel_launches() - launches0
+    kt, kcount = st.kernel_times()
+    st.set_timing(False)
+    if dist:
+        t = torch.tensor([sec], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        sec = float(t.item())
+    value = world * mesh.n_elems / sec / 1e6
+
+    # e2e through the C ABI with host buffers (pinned): U in, K blocks + F out
+    e2e = None
+    if not args.no_e2e:
+        Uh = torch.from_numpy(U).pin_memory()
+        Kh = {b: torch.empty(st.blocks[b][2], dtype=torch.float64).pin_memory() for b in (1, 12, 2)}
+        Fh = torch.empty(st.n_total, dtype=torch.float64).pin_memory()
+        Uh_np, Fh_np = Uh.numpy(), Fh.numpy()
+        Kh_np = {b: Kh[b].numpy() for b in Kh}
+        lib, h = st.lib, st.h
+
+        def e2e_step():
+            lib.nla3d_set_U(h, Uh_np.ctypes.data, st.n_total)
+            lib.nla3d_update_results(h)
+            lib.nla3d_assemble(h)
+            for b in (1, 12, 2):
+                if Kh_np[b].size:
+                    lib.nla3d_get_K(h, b, Kh_np[b].ctypes.data)
+            lib.nla3d_get_F(h, Fh_np.ctypes.data)
+
+        for _ in range(max(1, args.warmup)):
+            e2e_step()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        torch.cuda.synchronize()
+        e2e_sec = (time.perf_counter() - t0) / args.steps
+        if dist:
+            t = torch.tensor([e2e_sec], dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_sec = float(t.item())
+        e2e = {"value": world * mesh.n_elems / e2e_sec / 1e6, "unit": UNIT,
+               "h2d_bytes_per_step": int(U.nbytes),
+               "d2h_bytes_per_step": int(8 * nnz + 8 * st.n_total),
+               "ms_per_step": e2e_sec * 1e3}
+        assert np.array_equal(Kh_np[2], st.K(2)), "e2e K differs from the device result"
+
+    # mixed precision path on the same workload
+    mixed = None
+    if not args.no_mixed:
+        sm = FEStorage(mesh, "mixed", stream=stream.cuda_stream).initSolutionData()
+        for _ in range(args.warmup):
+            sm.setU_device(U_dev.data_ptr(), sm.n_total)
+            sm.updateResults()
+            sm.assembleGlobalEqMatrices()
+        sm.set_timing(True)
+        msec = time_steps(sm, U_dev, sm.n_total, args.steps, torch, stream)
+        mkt, _ = sm.kernel_times()
+        K64, K32 = st.K(2), sm.K(2)
+        F64, F32 = st.F(), sm.F()
+        mixed = {"value": world * mesh.n_elems / msec / 1e6, "unit": UNIT,
+                 "ms_per_step": msec * 1e3, "speedup_vs_fp64": sec / msec,
+                 "kernel_ms": {"element": float(mkt[0]), "gather_K": float(mkt[1]),
+                               "gather_F": float(mkt[2])},
+                 "K_rel_err_vs_fp64": float(np.abs(K32 - K64).max() / np.abs(K64).max()),
+                 "F_rel_err_vs_fp64": float(np.abs(F32 - F64).max() / np.abs(F64).max()),
+                 "dtype": "f32 tangent / f64 residual, volumetric terms and CSR sums"}
+        sm.close()
+
+    if rank != 0:
+        return
+    fp64_peak = probe_fma_peak(True)
+    elem_ms = float(kt[0])
+    achieved = FLOP_PER_ELEM * mesh.n_elems / (elem_ms * 1e-3)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm = peaks.get("hbm_gbs")
+    gather_ms = float(kt[1] + kt[2])
+    gather_bytes = (4 + 8) * mesh.n_elems * 350 + 4 * (nnz + st.n_total) + 8 * (nnz + st.n_total)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(mesh, {"equations": st.n_total, "nnz_upper": nnz,
+                                         "precision": "fp64",
+                                         "parallelism": f"replicas x{world}" if world > 1
+                                         else "single GPU"}),
+        "e2e": e2e,
+        "gpu_launches": int(launches),
+        "kernel_ms": {"element": elem_ms, "gather_K": float(kt[1]), "gather_F": float(kt[2]),
+                      "mpc": float(kt[3]), "assemblies_averaged": int(kcount)},
+        "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": fp64_peak / 1e12,
+                     "unit": "TFLOP/s", "frac": achieved / fp64_peak, "traffic": None,
+                     "kernel": "solid81_kernel<double>",
+                     "algorithmic": f"{FLOP_PER_ELEM} FP64 flop/element x {mesh.n_elems}",
+                     "peak_source": "FP64 FMA throughput probe in this run "
+                                    "(MEASURED_PEAKS.json has no FP64 figure)"},
+        "roofline_gather": {"bound": "hbm", "achieved": gather_bytes / (gather_ms * 1e-3) / 1e9,
+                            "peak": hbm, "unit": "GB/s",
+                            "frac": (gather_bytes / (gather_ms * 1e-3) / 1e9 / hbm) if hbm else None,
+                            "traffic": None, "kernel": "gather_kernel (K + F)",
+                            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
+        "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+        "mixed": mixed,
+        "setup_s": setup_s,
+        "element_status": {"flagged": int(count)},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        if int(os.environ.get("RANK", "0")) != 0:
+            return
+        run_reference(args)
+        return
+    run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

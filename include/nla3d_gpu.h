@@ -162,11 +162,13 @@ uint64_t nla3d_kernel_launches(const nla3d_ctx* ctx);
 
 /* Measurement helpers (no counterpart in the reference, which has no GPU).
  * nla3d_set_timing(ctx, 1) records CUDA events on the context stream around
- * each kernel of nla3d_assemble; nla3d_kernel_times() returns the last
- * assembly's times in ms: [0] element kernel, [1] K gather, [2] F gather,
- * [3] MPC rows (synchronises). */
+ * each kernel of every nla3d_assemble (a ring of the last 256 assemblies);
+ * nla3d_kernel_times() returns the mean time in ms per assembly over the
+ * assemblies recorded since the previous call (or since timing was switched
+ * on): [0] element kernel, [1] K gather, [2] F gather, [3] MPC rows, and in
+ * *count how many assemblies the mean covers (synchronises). */
 int nla3d_set_timing(nla3d_ctx* ctx, int on);
-int nla3d_kernel_times(nla3d_ctx* ctx, float ms[4]);
+int nla3d_kernel_times(nla3d_ctx* ctx, float ms[4], uint32_t* count);
 /* Throughput probe of dependent-chain-free FMA on the current device:
  * fp64 != 0 -> DFMA, else FFMA.  Returns FLOP/s (2 per FMA) in *flops. */
 int nla3d_probe_fma_peak(int fp64, double* flops);

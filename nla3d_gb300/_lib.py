@@ -89,7 +89,7 @@ def load(path: str = LIB_PATH):
         "nla3d_element_status": ([P, ctypes.POINTER(U32), ctypes.POINTER(U32)], ctypes.c_int),
         "nla3d_kernel_launches": ([P], U64),
         "nla3d_set_timing": ([P, ctypes.c_int], ctypes.c_int),
-        "nla3d_kernel_times": ([P, P], ctypes.c_int),
+        "nla3d_kernel_times": ([P, P, ctypes.POINTER(U32)], ctypes.c_int),
         "nla3d_probe_fma_peak": ([ctypes.c_int, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
     }
     for name, (args, res) in sig.items():

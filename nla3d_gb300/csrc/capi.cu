@@ -60,7 +60,9 @@ struct nla3d_ctx {
   ElementStatus* d_status = nullptr;
   std::vector<void*> allocs;
   bool timing = false;
-  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  static constexpr int kRing = 256;
+  std::vector<cudaEvent_t> ev;  // kRing x 5
+  uint64_t timed = 0;           // assemblies recorded since the last read
 };
 
 namespace {
@@ -132,8 +134,7 @@ int nla3d_destroy(nla3d_ctx* c) {
   for (void* p : c->allocs) cudaFree(p);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   c->allocs.clear();
-  for (auto& v : c->ev)
-    if (v) cudaEventDestroy(v);
+  for (auto& v : c->ev) cudaEventDestroy(v);
   delete c;
   return NLA3D_OK;
 }
@@ -353,8 +354,9 @@ int nla3d_assemble(nla3d_ctx* c) {
   e = cudaMemsetAsync(c->d_status, 0, sizeof(ElementStatus), c->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(&c->d_status->first, 0xFF, sizeof(uint32_t), c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "assemble: status reset");
+  const uint64_t slot = (c->timed % nla3d_ctx::kRing) * 5;
   auto mark = [&](int i) {
-    if (c->timing) cudaEventRecord(c->ev[i], c->stream);
+    if (c->timing) cudaEventRecord(c->ev[slot + i], c->stream);
   };
   mark(0);
   if (m.etype == NLA3D_SOLID81) {
@@ -415,6 +417,7 @@ int nla3d_assemble(nla3d_ctx* c) {
     c->launches++;
   }
   mark(4);
+  if (c->timing) c->timed++;
   return NLA3D_OK;
 }
 
@@ -474,23 +477,35 @@ uint64_t nla3d_kernel_launches(const nla3d_ctx* c) { return c ? c->launches : 0;
 
 int nla3d_set_timing(nla3d_ctx* c, int on) {
   if (!c) return NLA3D_ERR_ARG;
-  if (on && !c->ev[0])
+  if (on && c->ev.empty()) {
+    c->ev.resize(nla3d_ctx::kRing * 5);
     for (auto& v : c->ev) {
       cudaError_t e = cudaEventCreate(&v);
       if (e != cudaSuccess) return cuda_fail(c, e, "set_timing");
     }
+  }
   c->timing = on != 0;
+  c->timed = 0;
   return NLA3D_OK;
 }
 
-int nla3d_kernel_times(nla3d_ctx* c, float ms[4]) {
-  if (!c || !ms || !c->timing) return NLA3D_ERR_ARG;
-  cudaError_t e = cudaEventSynchronize(c->ev[4]);
-  if (e != cudaSuccess) return cuda_fail(c, e, "kernel_times");
-  for (int i = 0; i < 4; i++) {
-    ms[i] = 0.0f;
-    cudaEventElapsedTime(&ms[i], c->ev[i], c->ev[i + 1]);
+int nla3d_kernel_times(nla3d_ctx* c, float ms[4], uint32_t* count) {
+  if (!c || !ms || c->ev.empty()) return NLA3D_ERR_ARG;
+  const uint64_t n = c->timed < (uint64_t)nla3d_ctx::kRing ? c->timed : nla3d_ctx::kRing;
+  double acc[4] = {0, 0, 0, 0};
+  for (uint64_t k = 0; k < n; k++) {
+    const uint64_t slot = ((c->timed - 1 - k) % nla3d_ctx::kRing) * 5;
+    cudaError_t e = cudaEventSynchronize(c->ev[slot + 4]);
+    if (e != cudaSuccess) return cuda_fail(c, e, "kernel_times");
+    for (int i = 0; i < 4; i++) {
+      float t = 0.0f;
+      cudaEventElapsedTime(&t, c->ev[slot + i], c->ev[slot + i + 1]);
+      acc[i] += t;
+    }
   }
+  for (int i = 0; i < 4; i++) ms[i] = n ? (float)(acc[i] / n) : 0.0f;
+  if (count) *count = (uint32_t)n;
+  c->timed = 0;
   return NLA3D_OK;
 }
 

@@ -263,9 +263,12 @@ class FEStorage:
         self._check(self.lib.nla3d_set_timing(self.h, 1 if on else 0))
 
     def kernel_times(self):
+        """Mean per-assembly kernel times (ms) since the last call:
+        element, K gather, F gather, MPC; and the number of assemblies."""
         ms = np.zeros(4, np.float32)
-        self._check(self.lib.nla3d_kernel_times(self.h, _p(ms)))
-        return ms
+        n = ctypes.c_uint32()
+        self._check(self.lib.nla3d_kernel_times(self.h, _p(ms), ctypes.byref(n)))
+        return ms, n.value
 
     def kernel_launches(self):
         return int(self.lib.nla3d_kernel_launches(self.h))

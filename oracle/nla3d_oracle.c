@@ -36,7 +36,7 @@ static const uint32_t INVALID = 0xFFFFFFFFu; /* SparseMatrix.cpp:11 */
 /* dense kernels, Mat.h:686-801 (row-major, packed-upper symmetric)         */
 /* ----------------------------------------------------------------------- */
 
-void orc_matBTDBprod(int M, int N, const double* B, const double* D, double coef, double* R) {
+static inline __attribute__((always_inline)) void k_matBTDBprod(int M, int N, const double* B, const double* D, double coef, double* R) {
   /* Mat<dimN,dimM> A on the stack, zeroed (Mat.h:689-690) */
   double A[24 * 24];
   if (N * M > 24 * 24) abort();
@@ -65,17 +65,17 @@ void orc_matBTDBprod(int M, int N, const double* B, const double* D, double coef
     }
 }
 
-void orc_matBTVprod(int M, int N, const double* B, const double* V, double coef, double* R) {
+static inline __attribute__((always_inline)) void k_matBTVprod(int M, int N, const double* B, const double* V, double coef, double* R) {
   for (int i = 0; i < N; i++)
     for (int j = 0; j < M; j++) R[i] += B[j * N + i] * V[j] * coef;
 }
 
-void orc_matBVprod(int M, int N, const double* B, const double* V, double coef, double* R) {
+static inline __attribute__((always_inline)) void k_matBVprod(int M, int N, const double* B, const double* V, double coef, double* R) {
   for (int i = 0; i < M; i++)
     for (int j = 0; j < N; j++) R[i] += B[i * N + j] * V[j] * coef;
 }
 
-void orc_matABprod(int M1, int N1, int N2, const double* A, const double* B, double coef,
+static inline __attribute__((always_inline)) void k_matABprod(int M1, int N1, int N2, const double* A, const double* B, double coef,
                    double* R) {
   double* Rp = R;
   for (int i = 0; i < M1; i++)
@@ -85,7 +85,7 @@ void orc_matABprod(int M1, int N1, int N2, const double* A, const double* B, dou
     }
 }
 
-void orc_matATBprod(int M1, int N1, int N2, const double* A, const double* B, double coef,
+static inline __attribute__((always_inline)) void k_matATBprod(int M1, int N1, int N2, const double* A, const double* B, double coef,
                     double* R) {
   double* Rp = R;
   for (int i = 0; i < N1; i++)
@@ -93,6 +93,25 @@ void orc_matATBprod(int M1, int N1, int N2, const double* A, const double* B, do
       for (int k = 0; k < M1; k++) *Rp += A[k * N1 + i] * B[k * N2 + j] * coef;
       Rp++;
     }
+}
+
+/* exported wrappers (the mat_prod known-answer tests call these) */
+void orc_matBTDBprod(int M, int N, const double* B, const double* D, double coef, double* R) {
+  k_matBTDBprod(M, N, B, D, coef, R);
+}
+void orc_matBTVprod(int M, int N, const double* B, const double* V, double coef, double* R) {
+  k_matBTVprod(M, N, B, V, coef, R);
+}
+void orc_matBVprod(int M, int N, const double* B, const double* V, double coef, double* R) {
+  k_matBVprod(M, N, B, V, coef, R);
+}
+void orc_matABprod(int M1, int N1, int N2, const double* A, const double* B, double coef,
+                   double* R) {
+  k_matABprod(M1, N1, N2, A, B, coef, R);
+}
+void orc_matATBprod(int M1, int N1, int N2, const double* A, const double* B, double coef,
+                    double* R) {
+  k_matATBprod(M1, N1, N2, A, B, coef, R);
 }
 
 /* Mat<3,3>::det / inv (Mat.cpp:23-46) */
@@ -933,7 +952,7 @@ static void solid81_update(orc_model* m, uint32_t e) {
     make_B_NL(m->NiXj + ((size_t)e * 8 + g) * 24, B_NL);
     double* O = m->O + ((size_t)e * 8 + g) * 9;
     memset(O, 0, sizeof(double) * 9);
-    orc_matBVprod(9, 24, B_NL, U, 1.0, O);
+    k_matBVprod(9, 24, B_NL, U, 1.0, O);
     double* C = m->Cst + ((size_t)e * 8 + g) * 6;
     C[M_XX] = 1.0 + 2 * O[0] + pow(O[0], 2) + pow(O[3], 2) + pow(O[6], 2);
     C[M_YY] = 1.0 + 2 * O[4] + pow(O[1], 2) + pow(O[4], 2) + pow(O[7], 2);
@@ -968,11 +987,11 @@ static int solid81_buildK(orc_model* m, uint32_t e) {
     make_S9(m->S + ((size_t)e * 8 + g) * 6, S9);
     make_Omega(m->O + ((size_t)e * 8 + g) * 9, Om);
     make_B_NL(G, B_NL);
-    orc_matABprod(6, 9, 24, Om, B_NL, 2.0, B);
-    orc_matBTDBprod(6, 24, B, Dd, 0.5 * dWt, Kuu);
-    orc_matBTDBprod(9, 24, B_NL, S9, dWt, Kuu);
-    orc_matBTVprod(6, 24, B, m->S + ((size_t)e * 8 + g) * 6, -0.5 * dWt, Fu);
-    orc_matBTVprod(6, 24, B, Dp, 0.5 * dWt, Kup);
+    k_matABprod(6, 9, 24, Om, B_NL, 2.0, B);
+    k_matBTDBprod(6, 24, B, Dd, 0.5 * dWt, Kuu);
+    k_matBTDBprod(9, 24, B_NL, S9, dWt, Kuu);
+    k_matBTVprod(6, 24, B, m->S + ((size_t)e * 8 + g) * 6, -0.5 * dWt, Fu);
+    k_matBTVprod(6, 24, B, Dp, 0.5 * dWt, Kup);
     Fp += -(J - 1 - p_e / k) * dWt;
     Kpp += -1.0 / k * dWt;
   }
@@ -1101,7 +1120,7 @@ static int tetra0_buildK(orc_model* m, uint32_t e) {
     B[60 + 3 * i] = d[i] * Af;
     B[62 + 3 * i] = b[i] * Af;
   }
-  orc_matBTDBprod(6, 12, B, Cm, vol, Ke);
+  k_matBTDBprod(6, 12, B, Cm, vol, Ke);
   /* Element::assembleK(Ke, {UX,UY,UZ}) (element.h:281-303) */
   const double* Kp = Ke;
   int rc = 0;
@@ -1130,7 +1149,7 @@ static int quadth_buildK(orc_model* m, uint32_t e) {
     const double dWt = m->wts[g] * m->det[(size_t)e * 4 + g];
     const double* G = m->NiXj + ((size_t)e * 4 + g) * 8;
     const double Bm[8] = {G[0], G[2], G[4], G[6], G[1], G[3], G[5], G[7]};
-    orc_matBTDBprod(2, 4, Bm, matk, dWt, Ke);
+    k_matBTDBprod(2, 4, Bm, matk, dWt, Ke);
   }
   const uint32_t* c = m->conn + (size_t)e * 4;
   const double* Kp = Ke;
