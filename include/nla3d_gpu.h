@@ -173,6 +173,66 @@ int nla3d_kernel_times(nla3d_ctx* ctx, float ms[4], uint32_t* count);
  * fp64 != 0 -> DFMA, else FFMA.  Returns FLOP/s (2 per FMA) in *flops. */
 int nla3d_probe_fma_peak(int fp64, double* flops);
 
+/* ---------------------------------------------------------------------------
+ * SOLID81 assembly without device allocation.  No counterpart in the
+ * reference (which has no GPU code); it is an extra entry point for callers
+ * that may not allocate device memory: host frameworks that own all device
+ * memory through their own pool and forbid a plugin from calling cudaMalloc,
+ * and time-critical loops that cannot afford cudaMalloc's implicit device
+ * synchronisation.
+ *
+ * The caller passes every input and output as device memory it owns; the
+ * library keeps its intermediate data (shape-function gradients and element
+ * contributions, 4400 bytes per element) in a fixed array of
+ * NLA3D_NOALLOC_SCRATCH_BYTES compiled into the library, which every GPU that
+ * loads the library holds until exit.  Hence at most NLA3D_NOALLOC_MAX_ELEMS
+ * elements per call; larger meshes are rejected with NLA3D_ERR_RANGE before
+ * anything runs.  The call makes no cudaMalloc / cudaFree and uses no
+ * allocating library routine.
+ *
+ * All calls share that array: calls whose kernels overlap on the GPU (other
+ * streams or threads without ordering) race and corrupt each other.  The
+ * first call on a device looks up the array's device address with that
+ * device current; make that first call before any stream capture.
+ *
+ * Semantics: updateResults() followed by assembleGlobalEqMatrices() on the
+ * same U, SOLID81 elements only (no MPC rows), FP64.  Inputs:
+ *   node_eq  4 per node: equations of UX, UY, UZ (nla3d_eq_numbers) and a pad
+ *            word; 16-byte aligned;
+ *   p_eq     the HYDRO_PRESSURE equation of each element;
+ *   k_ptr / k_ids, f_ptr / f_ids: the inverse of nla3d_slot_maps -- for each
+ *            K slot (F row) the ids e * 325 + c (e * 25 + c) of its
+ *            contributions in ascending order, as CSR (nnz + 1 / n_eq + 1
+ *            offsets).
+ * Asynchronous on `stream` unless `flagged` is non-NULL, in which case it
+ * synchronises and stores the number of flagged elements there
+ * (NLA3D_ERR_ELEMENT if any). */
+#define NLA3D_NOALLOC_SCRATCH_BYTES (64ull << 20)
+#define NLA3D_NOALLOC_MAX_ELEMS 15252u
+
+typedef struct {
+  uint32_t n_elems;        /* 1 .. NLA3D_NOALLOC_MAX_ELEMS                */
+  uint32_t n_nodes;
+  uint32_t n_eq;           /* vecU and F length (nDofs + nMpc)            */
+  uint64_t nnz;            /* K values, block(1) | block(1,2) | block(2)  */
+  const double* xyz;       /* 3 * n_nodes                                 */
+  const uint32_t* conn;    /* 8 * n_elems, 1-based node ids               */
+  const uint32_t* node_eq; /* 4 * n_nodes                                 */
+  const uint32_t* p_eq;    /* n_elems                                     */
+  const double* U;         /* n_eq                                        */
+  const uint32_t* k_ptr;   /* nnz + 1                                     */
+  const uint32_t* k_ids;   /* 325 * n_elems                               */
+  const uint32_t* f_ptr;   /* n_eq + 1                                    */
+  const uint32_t* f_ids;   /* 25 * n_elems                                */
+  int32_t mat_id;          /* NLA3D_MAT_*                                 */
+  double mat_c[5];
+  double* K;               /* out: nnz                                    */
+  double* F;               /* out: n_eq                                   */
+} nla3d_solid81_noalloc_args;
+
+int nla3d_assemble_solid81_noalloc(const nla3d_solid81_noalloc_args* args, void* stream,
+                                   uint32_t* flagged);
+
 #ifdef __cplusplus
 }
 #endif

@@ -27,7 +27,33 @@ EXPORTS = [
     "nla3d_update_results", "nla3d_assemble", "nla3d_get_K", "nla3d_get_F", "nla3d_device_K",
     "nla3d_device_F", "nla3d_synchronize", "nla3d_element_status", "nla3d_kernel_launches",
     "nla3d_set_timing", "nla3d_kernel_times", "nla3d_probe_fma_peak",
+    "nla3d_assemble_solid81_noalloc",
 ]
+
+NOALLOC_MAX_ELEMS = 15252
+
+
+class NoAllocArgs(ctypes.Structure):
+    """nla3d_solid81_noalloc_args: every pointer is device memory owned by the caller."""
+    _fields_ = [
+        ("n_elems", ctypes.c_uint32),
+        ("n_nodes", ctypes.c_uint32),
+        ("n_eq", ctypes.c_uint32),
+        ("nnz", ctypes.c_uint64),
+        ("xyz", ctypes.c_void_p),
+        ("conn", ctypes.c_void_p),
+        ("node_eq", ctypes.c_void_p),
+        ("p_eq", ctypes.c_void_p),
+        ("U", ctypes.c_void_p),
+        ("k_ptr", ctypes.c_void_p),
+        ("k_ids", ctypes.c_void_p),
+        ("f_ptr", ctypes.c_void_p),
+        ("f_ids", ctypes.c_void_p),
+        ("mat_id", ctypes.c_int32),
+        ("mat_c", ctypes.c_double * 5),
+        ("K", ctypes.c_void_p),
+        ("F", ctypes.c_void_p),
+    ]
 
 
 class MeshDesc(ctypes.Structure):
@@ -91,6 +117,8 @@ def load(path: str = LIB_PATH):
         "nla3d_set_timing": ([P, ctypes.c_int], ctypes.c_int),
         "nla3d_kernel_times": ([P, P, ctypes.POINTER(U32)], ctypes.c_int),
         "nla3d_probe_fma_peak": ([ctypes.c_int, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
+        "nla3d_assemble_solid81_noalloc": ([ctypes.POINTER(NoAllocArgs), P, ctypes.POINTER(U32)],
+                                           ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
