@@ -94,6 +94,29 @@ typedef struct {
 /* Create a model (FEStorage with nodes, elements and material).  `precision`
  * selects the SOLID81 arithmetic (NLA3D_PREC_*).  Makes no CUDA call. */
 int nla3d_create(const nla3d_mesh_desc* mesh, int precision, nla3d_ctx** out);
+
+/* A batch of independent meshes in one context (each one a separate reference
+ * FEStorage with its own numbering, pattern, K and F; same element type, any
+ * material constants).  Every kernel of an assembly then runs once over all
+ * meshes.  vecU, F and K of the batch are the concatenation of the meshes'
+ * arrays; nla3d_mesh_info gives each mesh's offsets.  The single-mesh calls
+ * (nla3d_info, nla3d_pattern, nla3d_eq_numbers, nla3d_slot_maps, nla3d_get_K,
+ * nla3d_add_fix, nla3d_add_rigid_body) refer to mesh 0; nla3d_set_U,
+ * nla3d_get_F and nla3d_device_F take the whole concatenation. */
+int nla3d_create_batch(const nla3d_mesh_desc* meshes, uint32_t n_meshes, int precision,
+                       nla3d_ctx** out);
+uint32_t nla3d_mesh_count(const nla3d_ctx* ctx);
+int nla3d_mesh_add_fix(nla3d_ctx* ctx, uint32_t mesh, uint32_t n, const uint32_t* nodes,
+                       const int32_t* dofs);
+int nla3d_mesh_add_rigid_body(nla3d_ctx* ctx, uint32_t mesh, uint32_t master, uint32_t n_slaves,
+                              const uint32_t* slaves, uint32_t n_dofs, const int32_t* dofs);
+/* out as nla3d_info; offsets[0..4] = the mesh's first element, node, equation
+ * (index into vecU / F), K value and MPC equation in the concatenation. */
+int nla3d_mesh_info(const nla3d_ctx* ctx, uint32_t mesh, uint32_t out[16], uint64_t offsets[5]);
+int nla3d_mesh_pattern(const nla3d_ctx* ctx, uint32_t mesh, int block, uint32_t* iofeir,
+                       uint32_t* columns);
+int nla3d_mesh_eq_numbers(const nla3d_ctx* ctx, uint32_t mesh, uint32_t* node_eq,
+                          uint32_t* elem_eq);
 int nla3d_destroy(nla3d_ctx* ctx);
 const char* nla3d_last_error(const nla3d_ctx* ctx);
 
@@ -147,7 +170,10 @@ int nla3d_assemble(nla3d_ctx* ctx);
 /* Results.  Host copies synchronise the stream. */
 int nla3d_get_K(nla3d_ctx* ctx, int block, double* values);
 int nla3d_get_F(nla3d_ctx* ctx, double* F);
-/* Device pointers (valid until nla3d_destroy): K values of one block, F. */
+/* All K values of the context (every mesh: block(1) | block(1,2) | block(2)). */
+int nla3d_get_K_all(nla3d_ctx* ctx, double* values);
+/* Device pointers (valid until nla3d_destroy): K values of one block (block 0
+ * = all K values of the context), F. */
 int nla3d_device_K(const nla3d_ctx* ctx, int block, double** values, uint64_t* n);
 int nla3d_device_F(const nla3d_ctx* ctx, double** F, uint64_t* n);
 int nla3d_synchronize(nla3d_ctx* ctx);
@@ -159,6 +185,21 @@ int nla3d_element_status(nla3d_ctx* ctx, uint32_t* count, uint32_t* first);
 
 /* Number of kernels launched by the library on this context so far. */
 uint64_t nla3d_kernel_launches(const nla3d_ctx* ctx);
+
+/* Launch shape of the element kernel (warps per block 2/4/8, resident blocks
+ * per SM, 0 = as many as fit) and the gather block size (128..1024).
+ * nla3d_autotune times each candidate on this context's own mesh(es) with
+ * `reps` assemblies, keeps the fastest and reports it in chosen[3] and
+ * *best_ms (time of one assembly).  No counterpart in the reference. */
+int nla3d_set_launch_shape(nla3d_ctx* ctx, int warps_per_block, int blocks_per_sm,
+                           int gather_block);
+int nla3d_autotune(nla3d_ctx* ctx, int reps, int32_t chosen[3], float* best_ms);
+
+/* Record updateResults + assembleGlobalEqMatrices (on the current vecU buffer)
+ * as a CUDA graph on the context stream, and replay it.  A new launch shape
+ * or stream releases the graph.  No counterpart in the reference. */
+int nla3d_graph_capture(nla3d_ctx* ctx);
+int nla3d_graph_launch(nla3d_ctx* ctx);
 
 /* Measurement helpers (no counterpart in the reference, which has no GPU).
  * nla3d_set_timing(ctx, 1) records CUDA events on the context stream around

@@ -28,6 +28,9 @@ EXPORTS = [
     "nla3d_device_F", "nla3d_synchronize", "nla3d_element_status", "nla3d_kernel_launches",
     "nla3d_set_timing", "nla3d_kernel_times", "nla3d_probe_fma_peak",
     "nla3d_assemble_solid81_noalloc",
+    "nla3d_create_batch", "nla3d_mesh_count", "nla3d_mesh_add_fix", "nla3d_mesh_add_rigid_body",
+    "nla3d_mesh_info", "nla3d_mesh_pattern", "nla3d_mesh_eq_numbers", "nla3d_get_K_all",
+    "nla3d_set_launch_shape", "nla3d_autotune", "nla3d_graph_capture", "nla3d_graph_launch",
 ]
 
 NOALLOC_MAX_ELEMS = 15252
@@ -119,6 +122,18 @@ def load(path: str = LIB_PATH):
         "nla3d_probe_fma_peak": ([ctypes.c_int, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
         "nla3d_assemble_solid81_noalloc": ([ctypes.POINTER(NoAllocArgs), P, ctypes.POINTER(U32)],
                                            ctypes.c_int),
+        "nla3d_create_batch": ([P, U32, ctypes.c_int, ctypes.POINTER(P)], ctypes.c_int),
+        "nla3d_mesh_count": ([P], U32),
+        "nla3d_mesh_add_fix": ([P, U32, U32, P, P], ctypes.c_int),
+        "nla3d_mesh_add_rigid_body": ([P, U32, U32, U32, P, U32, P], ctypes.c_int),
+        "nla3d_mesh_info": ([P, U32, P, P], ctypes.c_int),
+        "nla3d_mesh_pattern": ([P, U32, ctypes.c_int, P, P], ctypes.c_int),
+        "nla3d_mesh_eq_numbers": ([P, U32, P, P], ctypes.c_int),
+        "nla3d_get_K_all": ([P, P], ctypes.c_int),
+        "nla3d_set_launch_shape": ([P, ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+        "nla3d_autotune": ([P, ctypes.c_int, P, ctypes.POINTER(ctypes.c_float)], ctypes.c_int),
+        "nla3d_graph_capture": ([P], ctypes.c_int),
+        "nla3d_graph_launch": ([P], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

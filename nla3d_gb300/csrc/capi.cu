@@ -1,23 +1,30 @@
 // C ABI of the assembly path (include/nla3d_gpu.h): context, device memory
 // layout and the launch sequence of one assembly.
 //
-// Device layout of one context (E elements, N nodes, nnz = K nonzeros):
+// A context holds one mesh (nla3d_create) or a batch of independent meshes
+// (nla3d_create_batch).  The meshes keep their own equation numbering, CSR
+// pattern, K and F (each is one reference FEStorage); on the device they are
+// concatenated so that one launch of each kernel assembles all of them:
+//
 //   Gt      24 x 8E  double  dN/dX per Gauss point, structure of arrays
 //   wdet    8E       double  Gauss weight * det J
-//   conn    8E       uint32  node ids (1-based)
-//   node_eq 4N       uint32  equations of UX, UY, UZ (+ pad) per node
-//   p_eq    E        uint32  equation of each element's pressure DoF
-//   U, U_state       double  current vecU / vecU at the last updateResults()
+//   conn    8E       uint32  node ids, global (mesh node offset added)
+//   node_eq 4N       uint32  equations of UX, UY, UZ (+ pad), global 1-based
+//   p_eq    E        uint32  pressure equation per element, global 1-based
+//   U, U_state       double  concatenated vecU / snapshot at updateResults()
 //   contribK 325E, contribF 25E  double   element contributions, reference order
 //   k_ptr nnz+1, k_ids 325E  uint32   fixed-order gather lists of K
 //   f_ptr n+1,   f_ids 25E   uint32   same for F
-//   K (block(1) | block(1,2) | block(2) values), F    double
+//   K (per mesh: block(1) | block(1,2) | block(2)), F   double
+//   elem_mesh E, mesh_mat 8M  per-element material (only when meshes differ)
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/nla3d_gpu.h"
@@ -27,7 +34,7 @@
 using namespace nla3d_gpu;
 
 struct nla3d_ctx {
-  HostModel hm;
+  std::vector<HostModel> hm;  // one per mesh
   int precision = NLA3D_PREC_FP64;
   std::string err;
   bool host_ready = false;  // nla3d_build_pattern done
@@ -37,6 +44,9 @@ struct nla3d_ctx {
   bool own_stream = false;
   bool have_state = false;
   uint64_t launches = 0;
+  // per-mesh offsets into the concatenated device arrays (n_meshes + 1 each)
+  std::vector<uint64_t> elem_off, node_off, u_off, k_off, mpc_off;
+  bool uniform_material = true;
   // device buffers
   double* d_xyz = nullptr;
   uint32_t* d_conn = nullptr;
@@ -55,14 +65,29 @@ struct nla3d_ctx {
   uint32_t* d_fids = nullptr;
   double* d_K = nullptr;
   double* d_F = nullptr;
+  uint32_t* d_elem_mesh = nullptr;
+  double* d_mesh_mat = nullptr;
   uint32_t* d_mpc_u32 = nullptr;  // master, slave, eq, slave_eq, master_eq6 (6), slot (5)
   int32_t* d_mpc_dof = nullptr;
   ElementStatus* d_status = nullptr;
   std::vector<void*> allocs;
+  // launch shape (nla3d_autotune / nla3d_set_launch_shape)
+  Solid81Shape shape;
+  int gather_bs = 256;
+  // CUDA graph of update_results + assemble
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  // per-kernel timing ring
   bool timing = false;
   static constexpr int kRing = 256;
   std::vector<cudaEvent_t> ev;  // kRing x 5
   uint64_t timed = 0;           // assemblies recorded since the last read
+
+  uint64_t E() const { return elem_off.empty() ? 0 : elem_off.back(); }
+  uint64_t Ntot() const { return node_off.empty() ? 0 : node_off.back(); }
+  uint64_t Utot() const { return u_off.empty() ? 0 : u_off.back(); }
+  uint64_t Ktot() const { return k_off.empty() ? 0 : k_off.back(); }
+  uint64_t Mtot() const { return mpc_off.empty() ? 0 : mpc_off.back(); }
 };
 
 namespace {
@@ -94,25 +119,19 @@ cudaError_t upload(nla3d_ctx* c, T** p, const T* host, uint64_t n) {
 
 int block_slot(int block) { return block == 1 ? 0 : (block == 2 ? 2 : (block == 12 ? 1 : -1)); }
 
-}  // namespace
-
-extern "C" {
-
-int nla3d_create(const nla3d_mesh_desc* mesh, int precision, nla3d_ctx** out) {
-  if (!out) return NLA3D_ERR_ARG;
-  *out = nullptr;
+int check_mesh(const nla3d_mesh_desc* mesh) {
   if (!mesh || (mesh->n_elems && (!mesh->conn || !mesh->xyz))) return NLA3D_ERR_ARG;
   if (mesh->elem_type != NLA3D_SOLID81 && mesh->elem_type != NLA3D_TETRA0 &&
       mesh->elem_type != NLA3D_QUADTH)
     return NLA3D_ERR_ARG;
-  if (precision != NLA3D_PREC_FP64 && precision != NLA3D_PREC_MIXED) return NLA3D_ERR_ARG;
   if (mesh->elem_type == NLA3D_SOLID81 &&
       (mesh->mat_id < NLA3D_MAT_NEO_HOOKEAN || mesh->mat_id > NLA3D_MAT_MOONEY_RIVLIN))
     return NLA3D_ERR_ARG;
   if (mesh->elem_type != NLA3D_SOLID81 && !mesh->elem_params && mesh->n_elems) return NLA3D_ERR_ARG;
-  nla3d_ctx* c = new (std::nothrow) nla3d_ctx();
-  if (!c) return NLA3D_ERR_NOMEM;
-  HostModel& m = c->hm;
+  return NLA3D_OK;
+}
+
+void fill_model(HostModel& m, const nla3d_mesh_desc* mesh) {
   m.etype = mesh->elem_type;
   m.npe = m.etype == NLA3D_SOLID81 ? 8 : 4;
   m.n_nodes = mesh->n_nodes;
@@ -123,14 +142,134 @@ int nla3d_create(const nla3d_mesh_desc* mesh, int precision, nla3d_ctx** out) {
   for (int i = 0; i < 5; i++) m.mat_c[i] = mesh->mat_c[i];
   if (mesh->elem_params)
     m.eparams.assign(mesh->elem_params, mesh->elem_params + 2 * (size_t)mesh->n_elems);
+}
+
+double bulk_of(const HostModel& m) {
+  return m.mat_id == NLA3D_MAT_NEO_HOOKEAN ? m.mat_c[1]
+                                           : (m.mat_id == NLA3D_MAT_BIDERMAN ? m.mat_c[4] : m.mat_c[2]);
+}
+
+bool valid_mesh(const nla3d_ctx* c, uint32_t mesh) { return c && mesh < c->hm.size(); }
+
+void graph_release(nla3d_ctx* c) {
+  if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+  if (c->graph) cudaGraphDestroy(c->graph);
+  c->graph_exec = nullptr;
+  c->graph = nullptr;
+}
+
+// The kernels of one assembly (everything nla3d_assemble enqueues).
+cudaError_t enqueue_assembly(nla3d_ctx* c) {
+  const HostModel& m0 = c->hm[0];
+  const uint64_t slot = (c->timed % nla3d_ctx::kRing) * 5;
+  auto mark = [&](int i) {
+    if (c->timing) cudaEventRecord(c->ev[slot + i], c->stream);
+  };
+  cudaError_t e = cudaMemsetAsync(c->d_status, 0, sizeof(ElementStatus), c->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(&c->d_status->first, 0xFF, sizeof(uint32_t), c->stream);
+  if (e != cudaSuccess) return e;
+  mark(0);
+  if (m0.etype == NLA3D_SOLID81) {
+    Solid81Args a{};
+    a.n_elems = (uint32_t)c->E();
+    a.Gt = c->d_Gt;
+    a.wdet = c->d_wdet;
+    a.conn = c->d_conn;
+    a.node_eq3 = c->d_node_eq3;
+    a.p_eq = c->d_p_eq;
+    a.U_state = c->d_Ustate;
+    a.U_cur = c->d_U;
+    a.have_state = c->have_state ? 1 : 0;
+    a.mat_id = m0.mat_id;
+    for (int i = 0; i < 5; i++) a.mc[i] = m0.mat_c[i];
+    a.kbulk = bulk_of(m0);
+    a.elem_mesh = c->uniform_material ? nullptr : c->d_elem_mesh;
+    a.mesh_mat = c->uniform_material ? nullptr : c->d_mesh_mat;
+    a.contribK = c->d_contribK;
+    a.contribF = c->d_contribF;
+    a.status = c->d_status;
+    e = launch_solid81_shaped(a, c->precision == NLA3D_PREC_MIXED, c->shape, c->stream);
+  } else {
+    LinearArgs a{m0.etype, (uint32_t)c->E(), c->d_xyz, c->d_conn, c->d_eparams, c->d_contribK,
+                 c->d_contribF, c->d_status};
+    e = launch_linear(a, c->stream);
+  }
+  if (e != cudaSuccess) return e;
+  c->launches++;
+  mark(1);
+  GatherArgs gk{c->Ktot(), c->d_kptr, c->d_kids, c->d_contribK, c->d_K};
+  e = launch_gather_bs(gk, c->gather_bs, c->stream);
+  if (e != cudaSuccess) return e;
+  c->launches += c->Ktot() ? 1 : 0;
+  mark(2);
+  GatherArgs gf{c->Utot(), c->d_fptr, c->d_fids, c->d_contribF, c->d_F};
+  e = launch_gather_bs(gf, c->gather_bs, c->stream);
+  if (e != cudaSuccess) return e;
+  c->launches++;
+  mark(3);
+  if (c->Mtot()) {
+    const uint64_t M = c->Mtot();
+    MpcArgs a{};
+    a.n_mpc = (uint32_t)M;
+    a.master = c->d_mpc_u32;
+    a.slave = c->d_mpc_u32 + M;
+    a.eq = c->d_mpc_u32 + 2 * M;
+    a.slave_eq = c->d_mpc_u32 + 3 * M;
+    a.master_eq6 = c->d_mpc_u32 + 4 * M;
+    a.slot = c->d_mpc_u32 + 10 * M;
+    a.slave_dof = c->d_mpc_dof;
+    a.xyz = c->d_xyz;
+    a.U = c->d_U;
+    a.K = c->d_K;
+    a.F = c->d_F;
+    e = launch_mpc(a, c->stream);
+    if (e != cudaSuccess) return e;
+    c->launches++;
+  }
+  mark(4);
+  if (c->timing) c->timed++;
+  return cudaSuccess;
+}
+
+cudaError_t enqueue_update(nla3d_ctx* c) {
+  return cudaMemcpyAsync(c->d_Ustate, c->d_U, sizeof(double) * c->Utot(), cudaMemcpyDeviceToDevice,
+                         c->stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+int nla3d_create(const nla3d_mesh_desc* mesh, int precision, nla3d_ctx** out) {
+  return nla3d_create_batch(mesh, 1, precision, out);
+}
+
+int nla3d_create_batch(const nla3d_mesh_desc* meshes, uint32_t n_meshes, int precision,
+                       nla3d_ctx** out) {
+  if (!out) return NLA3D_ERR_ARG;
+  *out = nullptr;
+  if (!meshes || n_meshes == 0) return NLA3D_ERR_ARG;
+  if (precision != NLA3D_PREC_FP64 && precision != NLA3D_PREC_MIXED) return NLA3D_ERR_ARG;
+  for (uint32_t i = 0; i < n_meshes; i++) {
+    int rc = check_mesh(&meshes[i]);
+    if (rc) return rc;
+    if (meshes[i].elem_type != meshes[0].elem_type) return NLA3D_ERR_ARG;
+  }
+  nla3d_ctx* c = new (std::nothrow) nla3d_ctx();
+  if (!c) return NLA3D_ERR_NOMEM;
+  c->hm.resize(n_meshes);
+  for (uint32_t i = 0; i < n_meshes; i++) fill_model(c->hm[i], &meshes[i]);
   c->precision = precision;
   *out = c;
   return NLA3D_OK;
 }
 
+uint32_t nla3d_mesh_count(const nla3d_ctx* c) { return c ? (uint32_t)c->hm.size() : 0; }
+
 int nla3d_destroy(nla3d_ctx* c) {
   if (!c) return NLA3D_OK;
   if (c->stream) cudaStreamSynchronize(c->stream);
+  graph_release(c);
   for (void* p : c->allocs) cudaFree(p);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   c->allocs.clear();
@@ -147,6 +286,7 @@ int nla3d_set_stream(nla3d_ctx* c, void* stream) {
     cudaStreamSynchronize(c->stream);
     cudaStreamDestroy(c->stream);
   }
+  graph_release(c);
   c->stream = (cudaStream_t)stream;
   c->own_stream = false;
   return NLA3D_OK;
@@ -154,46 +294,110 @@ int nla3d_set_stream(nla3d_ctx* c, void* stream) {
 
 void* nla3d_get_stream(const nla3d_ctx* c) { return c ? (void*)c->stream : nullptr; }
 
-int nla3d_add_fix(nla3d_ctx* c, uint32_t n, const uint32_t* nodes, const int32_t* dofs) {
-  if (!c || c->host_ready || (n && (!nodes || !dofs))) return fail(c, NLA3D_ERR_ARG, "add_fix");
+int nla3d_mesh_add_fix(nla3d_ctx* c, uint32_t mesh, uint32_t n, const uint32_t* nodes,
+                       const int32_t* dofs) {
+  if (!valid_mesh(c, mesh) || c->host_ready || (n && (!nodes || !dofs)))
+    return fail(c, NLA3D_ERR_ARG, "add_fix");
   for (uint32_t i = 0; i < n; i++) {
-    c->hm.fix_node.push_back(nodes[i]);
-    c->hm.fix_dof.push_back(dofs[i]);
+    c->hm[mesh].fix_node.push_back(nodes[i]);
+    c->hm[mesh].fix_dof.push_back(dofs[i]);
   }
   return NLA3D_OK;
 }
 
-int nla3d_add_rigid_body(nla3d_ctx* c, uint32_t master, uint32_t n_slaves, const uint32_t* slaves,
-                         uint32_t n_dofs, const int32_t* dofs) {
-  if (!c || c->host_ready || n_dofs > 3 || (n_slaves && !slaves) || (n_dofs && !dofs))
+int nla3d_add_fix(nla3d_ctx* c, uint32_t n, const uint32_t* nodes, const int32_t* dofs) {
+  return nla3d_mesh_add_fix(c, 0, n, nodes, dofs);
+}
+
+int nla3d_mesh_add_rigid_body(nla3d_ctx* c, uint32_t mesh, uint32_t master, uint32_t n_slaves,
+                              const uint32_t* slaves, uint32_t n_dofs, const int32_t* dofs) {
+  if (!valid_mesh(c, mesh) || c->host_ready || n_dofs > 3 || (n_slaves && !slaves) ||
+      (n_dofs && !dofs))
     return fail(c, NLA3D_ERR_ARG, "add_rigid_body");
   RigidBody rb;
   rb.master = master;
   rb.slaves.assign(slaves, slaves + n_slaves);
   rb.dofs.assign(dofs, dofs + n_dofs);
-  c->hm.rbs.push_back(rb);
+  c->hm[mesh].rbs.push_back(rb);
   return NLA3D_OK;
+}
+
+int nla3d_add_rigid_body(nla3d_ctx* c, uint32_t master, uint32_t n_slaves, const uint32_t* slaves,
+                         uint32_t n_dofs, const int32_t* dofs) {
+  return nla3d_mesh_add_rigid_body(c, 0, master, n_slaves, slaves, n_dofs, dofs);
 }
 
 int nla3d_build_pattern(nla3d_ctx* c) {
   if (!c) return NLA3D_ERR_ARG;
   if (c->host_ready) return NLA3D_OK;
-  std::string msg = build_host_model(c->hm, 0);
-  if (!msg.empty()) return fail(c, msg.find("2^32") != std::string::npos ||
-                                           msg.find("too many") != std::string::npos
-                                       ? NLA3D_ERR_RANGE
-                                       : NLA3D_ERR_PATTERN,
-                                msg);
+  const size_t M = c->hm.size();
+  std::vector<std::string> msgs(M);
+  if (M == 1) {
+    msgs[0] = build_host_model(c->hm[0], 0);
+  } else {
+    // many meshes: one mesh per worker thread
+    const unsigned nt =
+        std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), (unsigned)M));
+    std::vector<std::thread> th;
+    std::mutex mu;
+    size_t next = 0;
+    for (unsigned t = 0; t < nt; t++)
+      th.emplace_back([&] {
+        for (;;) {
+          size_t i;
+          {
+            std::lock_guard<std::mutex> l(mu);
+            if (next >= M) return;
+            i = next++;
+          }
+          msgs[i] = build_host_model(c->hm[i], 1);
+        }
+      });
+    for (auto& t : th) t.join();
+  }
+  for (size_t i = 0; i < M; i++)
+    if (!msgs[i].empty()) {
+      std::string msg = M > 1 ? "mesh " + std::to_string(i) + ": " + msgs[i] : msgs[i];
+      return fail(c, msgs[i].find("2^32") != std::string::npos ||
+                             msgs[i].find("too many") != std::string::npos
+                         ? NLA3D_ERR_RANGE
+                         : NLA3D_ERR_PATTERN,
+                  msg);
+    }
+  // offsets of the concatenation
+  c->elem_off.assign(M + 1, 0);
+  c->node_off.assign(M + 1, 0);
+  c->u_off.assign(M + 1, 0);
+  c->k_off.assign(M + 1, 0);
+  c->mpc_off.assign(M + 1, 0);
+  for (size_t i = 0; i < M; i++) {
+    const HostModel& m = c->hm[i];
+    c->elem_off[i + 1] = c->elem_off[i] + m.n_elems;
+    c->node_off[i + 1] = c->node_off[i] + m.n_nodes;
+    c->u_off[i + 1] = c->u_off[i] + m.n_total();
+    c->k_off[i + 1] = c->k_off[i] + m.nnz_total;
+    c->mpc_off[i + 1] = c->mpc_off[i] + m.n_mpc;
+  }
+  const uint64_t n_kc = c->hm[0].n_kc, n_fc = c->hm[0].n_fc;
+  if (c->E() * (n_kc + n_fc) >= 0xFFFFFFF0ull || c->Ktot() >= 0xFFFFFFF0ull ||
+      c->Utot() >= 0xFFFFFFF0ull || c->Ntot() >= 0xFFFFFFF0ull)
+    return fail(c, NLA3D_ERR_RANGE, "batch exceeds 32-bit device indexing");
+  c->uniform_material = true;
+  for (size_t i = 1; i < M; i++) {
+    const HostModel& a = c->hm[0];
+    const HostModel& b = c->hm[i];
+    if (a.mat_id != b.mat_id || std::memcmp(a.mat_c, b.mat_c, sizeof(a.mat_c)) != 0)
+      c->uniform_material = false;
+  }
   c->host_ready = true;
   return NLA3D_OK;
 }
 
 int nla3d_slot_maps(const nla3d_ctx* c, uint32_t* kslot, uint32_t* fslot) {
   if (!c || !c->host_ready || c->ready) return NLA3D_ERR_ARG;
-  if (kslot && !c->hm.kslot.empty())
-    std::memcpy(kslot, c->hm.kslot.data(), sizeof(uint32_t) * c->hm.kslot.size());
-  if (fslot && !c->hm.fslot.empty())
-    std::memcpy(fslot, c->hm.fslot.data(), sizeof(uint32_t) * c->hm.fslot.size());
+  const HostModel& m = c->hm[0];
+  if (kslot && !m.kslot.empty()) std::memcpy(kslot, m.kslot.data(), sizeof(uint32_t) * m.kslot.size());
+  if (fslot && !m.fslot.empty()) std::memcpy(fslot, m.fslot.data(), sizeof(uint32_t) * m.fslot.size());
   return NLA3D_OK;
 }
 
@@ -201,7 +405,6 @@ int nla3d_init_solution_data(nla3d_ctx* c) {
   if (!c || c->ready) return fail(c, NLA3D_ERR_ARG, "init_solution_data: bad call order");
   int rc = nla3d_build_pattern(c);
   if (rc) return rc;
-  HostModel& m = c->hm;
   cudaError_t e = cudaGetDevice(&c->device);
   if (e != cudaSuccess) return cuda_fail(c, e, "cudaGetDevice");
   if (!c->stream) {
@@ -209,86 +412,136 @@ int nla3d_init_solution_data(nla3d_ctx* c) {
     if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamCreate");
     c->own_stream = true;
   }
-  const uint64_t E = m.n_elems, N = m.n_nodes, ntot = m.n_total();
-  // node equations of UX, UY, UZ (TEMP for QUADTH is handled by the linear kernel's
-  // slot maps only), padded to 4 per node for 16-byte loads
-  std::vector<uint32_t> neq3(4 * N, 0);
-  for (uint64_t n = 0; n < N; n++)
-    for (int d = 0; d < 3; d++) neq3[4 * n + d] = m.node_eq[n * kDofTypes + d];
-  std::vector<uint32_t> peq(E, 0);
-  for (uint64_t el = 0; el < E; el++) peq[el] = m.elem_eq[el * kDofTypes + HYDRO_PRESSURE];
+  const size_t M = c->hm.size();
+  const uint64_t E = c->E(), N = c->Ntot(), ntot = c->Utot(), nnz = c->Ktot(), NM = c->Mtot();
+  const int npe = c->hm[0].npe;
+  const uint64_t n_kc = c->hm[0].n_kc, n_fc = c->hm[0].n_fc;
+  // concatenated host arrays with global offsets
+  std::vector<double> xyz(3 * N);
+  std::vector<uint32_t> conn(npe * E), neq3(4 * N, 0), peq(E, 0), elem_mesh;
+  std::vector<double> eparams, mesh_mat;
+  std::vector<uint32_t> kptr(nnz + 1), kids(E * n_kc), fptr(ntot + 1), fids(E * n_fc);
+  if (!c->uniform_material) {
+    elem_mesh.resize(E);
+    mesh_mat.assign(8 * M, 0.0);
+  }
+  if (!c->hm[0].eparams.empty()) eparams.resize(2 * E);
+  for (size_t i = 0; i < M; i++) {
+    const HostModel& m = c->hm[i];
+    const uint64_t eo = c->elem_off[i], no = c->node_off[i], uo = c->u_off[i], ko = c->k_off[i];
+    std::memcpy(&xyz[3 * no], m.xyz.data(), sizeof(double) * 3 * m.n_nodes);
+    for (uint64_t k = 0; k < (uint64_t)npe * m.n_elems; k++)
+      conn[npe * eo + k] = m.conn[k] + (uint32_t)no;
+    for (uint64_t n = 0; n < m.n_nodes; n++)
+      for (int d = 0; d < 3; d++) {
+        const uint32_t q = m.node_eq[n * kDofTypes + d];
+        neq3[4 * (no + n) + d] = q ? q + (uint32_t)uo : 0;
+      }
+    for (uint64_t el = 0; el < m.n_elems; el++) {
+      const uint32_t q = m.elem_eq[el * kDofTypes + HYDRO_PRESSURE];
+      peq[eo + el] = q ? q + (uint32_t)uo : 0;
+    }
+    if (!eparams.empty())
+      std::memcpy(&eparams[2 * eo], m.eparams.data(), sizeof(double) * 2 * m.n_elems);
+    for (uint64_t s = 0; s < m.nnz_total; s++) kptr[ko + s] = m.k_ptr[s] + (uint32_t)(eo * n_kc);
+    for (uint64_t k = 0; k < m.k_ids.size(); k++)
+      kids[eo * n_kc + k] = m.k_ids[k] + (uint32_t)(eo * n_kc);
+    for (uint64_t s = 0; s < m.n_total(); s++) fptr[uo + s] = m.f_ptr[s] + (uint32_t)(eo * n_fc);
+    for (uint64_t k = 0; k < m.f_ids.size(); k++)
+      fids[eo * n_fc + k] = m.f_ids[k] + (uint32_t)(eo * n_fc);
+    if (!c->uniform_material) {
+      for (uint64_t el = 0; el < m.n_elems; el++) elem_mesh[eo + el] = (uint32_t)i;
+      mesh_mat[8 * i + 0] = m.mat_id;
+      for (int k = 0; k < 5; k++) mesh_mat[8 * i + 1 + k] = m.mat_c[k];
+      mesh_mat[8 * i + 6] = bulk_of(m);
+    }
+  }
+  kptr[nnz] = (uint32_t)(E * n_kc);
+  fptr[ntot] = (uint32_t)(E * n_fc);
 
-#define CK(x)                                    \
-  do {                                           \
-    cudaError_t _e = (x);                        \
+#define CK(x)                                           \
+  do {                                                  \
+    cudaError_t _e = (x);                               \
     if (_e != cudaSuccess) return cuda_fail(c, _e, #x); \
   } while (0)
-  CK(upload(c, &c->d_xyz, m.xyz.data(), m.xyz.size()));
-  CK(upload(c, &c->d_conn, m.conn.data(), m.conn.size()));
+  CK(upload(c, &c->d_xyz, xyz.data(), xyz.size()));
+  CK(upload(c, &c->d_conn, conn.data(), conn.size()));
   CK(upload(c, &c->d_node_eq3, neq3.data(), neq3.size()));
   CK(upload(c, &c->d_p_eq, peq.data(), peq.size()));
-  if (!m.eparams.empty()) CK(upload(c, &c->d_eparams, m.eparams.data(), m.eparams.size()));
-  CK(upload(c, &c->d_kptr, m.k_ptr.data(), m.k_ptr.size()));
-  CK(upload(c, &c->d_kids, m.k_ids.data(), m.k_ids.size()));
-  CK(upload(c, &c->d_fptr, m.f_ptr.data(), m.f_ptr.size()));
-  CK(upload(c, &c->d_fids, m.f_ids.data(), m.f_ids.size()));
+  if (!eparams.empty()) CK(upload(c, &c->d_eparams, eparams.data(), eparams.size()));
+  if (!c->uniform_material) {
+    CK(upload(c, &c->d_elem_mesh, elem_mesh.data(), elem_mesh.size()));
+    CK(upload(c, &c->d_mesh_mat, mesh_mat.data(), mesh_mat.size()));
+  }
+  CK(upload(c, &c->d_kptr, kptr.data(), kptr.size()));
+  CK(upload(c, &c->d_kids, kids.data(), kids.size()));
+  CK(upload(c, &c->d_fptr, fptr.data(), fptr.size()));
+  CK(upload(c, &c->d_fids, fids.data(), fids.size()));
   CK(dalloc(c, &c->d_U, ntot));
   CK(dalloc(c, &c->d_Ustate, ntot));
   CK(cudaMemsetAsync(c->d_U, 0, sizeof(double) * ntot, c->stream));
   CK(cudaMemsetAsync(c->d_Ustate, 0, sizeof(double) * ntot, c->stream));
-  CK(dalloc(c, &c->d_contribK, E * m.n_kc));
-  CK(dalloc(c, &c->d_contribF, E * (m.n_fc ? m.n_fc : 1)));
-  CK(dalloc(c, &c->d_K, m.nnz_total));
+  CK(dalloc(c, &c->d_contribK, E * n_kc));
+  CK(dalloc(c, &c->d_contribF, E * (n_fc ? n_fc : 1)));
+  CK(dalloc(c, &c->d_K, nnz));
   CK(dalloc(c, &c->d_F, ntot));
   CK(dalloc(c, &c->d_status, 1));
-  if (m.n_mpc) {
-    // per MPC: master, slave, eq, slave_eq, master_eq6[6], slot[5]  (15 words)
-    std::vector<uint32_t> w(15ull * m.n_mpc);
-    std::vector<int32_t> dof(m.n_mpc);
-    const uint64_t M = m.n_mpc;
-    for (uint64_t k = 0; k < M; k++) {
-      const MpcEq& q = m.mpcs[k];
-      w[k] = q.node[1];
-      w[M + k] = q.slave;
-      w[2 * M + k] = q.eq;
-      w[3 * M + k] = m.neq(q.slave, q.slave_dof);
-      for (int t = 0; t < 6; t++) w[4 * M + 6 * k + t] = m.neq(q.node[1], t);
-      for (int t = 0; t < 5; t++) w[10 * M + 5 * k + t] = m.mpc_slot[5 * k + t];
-      dof[k] = q.slave_dof;
+  if (NM) {
+    // per MPC: master, slave, eq, slave_eq, master_eq6[6], slot[5]  (15 words), global
+    std::vector<uint32_t> w(15ull * NM);
+    std::vector<int32_t> dof(NM);
+    for (size_t i = 0; i < M; i++) {
+      const HostModel& m = c->hm[i];
+      const uint32_t no = (uint32_t)c->node_off[i], uo = (uint32_t)c->u_off[i],
+                     ko = (uint32_t)c->k_off[i];
+      // the MPC kernel adds each coefficient to its slot; slots are distinct by
+      // construction (one column per MPC equation), verify before trusting it
+      std::vector<uint32_t> sl(m.mpc_slot);
+      std::sort(sl.begin(), sl.end());
+      if (std::adjacent_find(sl.begin(), sl.end()) != sl.end())
+        return fail(c, NLA3D_ERR_PATTERN, "two MPC terms share one K slot");
+      for (uint64_t k = 0; k < m.n_mpc; k++) {
+        const uint64_t g = c->mpc_off[i] + k;
+        const MpcEq& q = m.mpcs[k];
+        w[g] = q.node[1] + no;
+        w[NM + g] = q.slave + no;
+        w[2 * NM + g] = q.eq + uo;
+        w[3 * NM + g] = m.neq(q.slave, q.slave_dof) + uo;
+        for (int t = 0; t < 6; t++) w[4 * NM + 6 * g + t] = m.neq(q.node[1], t) + uo;
+        for (int t = 0; t < 5; t++) w[10 * NM + 5 * g + t] = m.mpc_slot[5 * k + t] + ko;
+        dof[g] = q.slave_dof;
+      }
     }
-    // the MPC kernel adds each coefficient to its slot; slots are distinct by
-    // construction (one column per MPC equation), verify before trusting it
-    std::vector<uint32_t> sl(m.mpc_slot);
-    std::sort(sl.begin(), sl.end());
-    if (std::adjacent_find(sl.begin(), sl.end()) != sl.end())
-      return fail(c, NLA3D_ERR_PATTERN, "two MPC terms share one K slot");
     CK(upload(c, &c->d_mpc_u32, w.data(), w.size()));
     CK(upload(c, &c->d_mpc_dof, dof.data(), dof.size()));
   }
-  if (m.etype == NLA3D_SOLID81) {
+  CK(cudaMemsetAsync(c->d_status, 0, sizeof(ElementStatus), c->stream));
+  CK(cudaMemsetAsync(&c->d_status->first, 0xFF, sizeof(uint32_t), c->stream));
+  if (c->hm[0].etype == NLA3D_SOLID81) {
     CK(dalloc(c, &c->d_Gt, 24 * 8 * E));
     CK(dalloc(c, &c->d_wdet, 8 * E));
-    CK(cudaMemsetAsync(c->d_status, 0, sizeof(ElementStatus), c->stream));
-    CK(cudaMemsetAsync(&c->d_status->first, 0xFF, sizeof(uint32_t), c->stream));
     JacobianArgs ja{(uint32_t)E, c->d_xyz, c->d_conn, c->d_Gt, c->d_wdet, c->d_status};
     CK(launch_solid81_jacobian(ja, c->stream));
     c->launches++;
   }
+  CK(prepare_device_tables());
   CK(cudaStreamSynchronize(c->stream));
-  // the gather lists now live on the device only
-  std::vector<uint32_t>().swap(m.kslot);
-  std::vector<uint32_t>().swap(m.fslot);
-  std::vector<uint32_t>().swap(m.k_ids);
-  std::vector<uint32_t>().swap(m.f_ids);
-  std::vector<uint32_t>().swap(m.k_ptr);
-  std::vector<uint32_t>().swap(m.f_ptr);
+  // the gather lists and slot maps now live on the device only
+  for (HostModel& m : c->hm) {
+    std::vector<uint32_t>().swap(m.kslot);
+    std::vector<uint32_t>().swap(m.fslot);
+    std::vector<uint32_t>().swap(m.k_ids);
+    std::vector<uint32_t>().swap(m.f_ids);
+    std::vector<uint32_t>().swap(m.k_ptr);
+    std::vector<uint32_t>().swap(m.f_ptr);
+  }
   c->ready = true;
   return NLA3D_OK;
 }
 
-int nla3d_info(const nla3d_ctx* c, uint32_t out[16]) {
-  if (!c || !out || !c->host_ready) return NLA3D_ERR_ARG;
-  const HostModel& m = c->hm;
+int nla3d_mesh_info(const nla3d_ctx* c, uint32_t mesh, uint32_t out[16], uint64_t offsets[5]) {
+  if (!valid_mesh(c, mesh) || !c->host_ready || !out) return NLA3D_ERR_ARG;
+  const HostModel& m = c->hm[mesh];
   std::memset(out, 0, sizeof(uint32_t) * 16);
   out[0] = m.n_dofs;
   out[1] = m.n_con;
@@ -301,13 +554,23 @@ int nla3d_info(const nla3d_ctx* c, uint32_t out[16]) {
   }
   out[13] = (uint32_t)m.n_kc;
   out[14] = (uint32_t)m.n_fc;
+  if (offsets) {
+    offsets[0] = c->elem_off[mesh];
+    offsets[1] = c->node_off[mesh];
+    offsets[2] = c->u_off[mesh];
+    offsets[3] = c->k_off[mesh];
+    offsets[4] = c->mpc_off[mesh];
+  }
   return NLA3D_OK;
 }
 
-int nla3d_pattern(const nla3d_ctx* c, int block, uint32_t* iofeir, uint32_t* columns) {
+int nla3d_info(const nla3d_ctx* c, uint32_t out[16]) { return nla3d_mesh_info(c, 0, out, nullptr); }
+
+int nla3d_mesh_pattern(const nla3d_ctx* c, uint32_t mesh, int block, uint32_t* iofeir,
+                       uint32_t* columns) {
   const int b = block_slot(block);
-  if (!c || !c->host_ready || b < 0 || !iofeir) return NLA3D_ERR_ARG;
-  const CsrBlock& B = c->hm.blk[b];
+  if (!valid_mesh(c, mesh) || !c->host_ready || b < 0 || !iofeir) return NLA3D_ERR_ARG;
+  const CsrBlock& B = c->hm[mesh].blk[b];
   std::memcpy(iofeir, B.iofeir.data(), sizeof(uint32_t) * (B.rows + 1));
   if (B.nnz()) {
     if (!columns) return NLA3D_ERR_ARG;
@@ -316,21 +579,30 @@ int nla3d_pattern(const nla3d_ctx* c, int block, uint32_t* iofeir, uint32_t* col
   return NLA3D_OK;
 }
 
-int nla3d_eq_numbers(const nla3d_ctx* c, uint32_t* node_eq, uint32_t* elem_eq) {
-  if (!c || !c->host_ready) return NLA3D_ERR_ARG;
-  if (node_eq) std::memcpy(node_eq, c->hm.node_eq.data(), sizeof(uint32_t) * c->hm.node_eq.size());
-  if (elem_eq) std::memcpy(elem_eq, c->hm.elem_eq.data(), sizeof(uint32_t) * c->hm.elem_eq.size());
+int nla3d_pattern(const nla3d_ctx* c, int block, uint32_t* iofeir, uint32_t* columns) {
+  return nla3d_mesh_pattern(c, 0, block, iofeir, columns);
+}
+
+int nla3d_mesh_eq_numbers(const nla3d_ctx* c, uint32_t mesh, uint32_t* node_eq, uint32_t* elem_eq) {
+  if (!valid_mesh(c, mesh) || !c->host_ready) return NLA3D_ERR_ARG;
+  const HostModel& m = c->hm[mesh];
+  if (node_eq) std::memcpy(node_eq, m.node_eq.data(), sizeof(uint32_t) * m.node_eq.size());
+  if (elem_eq) std::memcpy(elem_eq, m.elem_eq.data(), sizeof(uint32_t) * m.elem_eq.size());
   return NLA3D_OK;
 }
 
+int nla3d_eq_numbers(const nla3d_ctx* c, uint32_t* node_eq, uint32_t* elem_eq) {
+  return nla3d_mesh_eq_numbers(c, 0, node_eq, elem_eq);
+}
+
 int nla3d_set_U(nla3d_ctx* c, const double* U, uint64_t n) {
-  if (!c || !c->ready || !U || n != c->hm.n_total()) return fail(c, NLA3D_ERR_ARG, "set_U size");
+  if (!c || !c->ready || !U || n != c->Utot()) return fail(c, NLA3D_ERR_ARG, "set_U size");
   cudaError_t e = cudaMemcpyAsync(c->d_U, U, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream);
   return e == cudaSuccess ? NLA3D_OK : cuda_fail(c, e, "set_U");
 }
 
 int nla3d_set_U_device(nla3d_ctx* c, const double* U, uint64_t n) {
-  if (!c || !c->ready || !U || n != c->hm.n_total()) return fail(c, NLA3D_ERR_ARG, "set_U size");
+  if (!c || !c->ready || !U || n != c->Utot()) return fail(c, NLA3D_ERR_ARG, "set_U size");
   cudaError_t e =
       cudaMemcpyAsync(c->d_U, U, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream);
   return e == cudaSuccess ? NLA3D_OK : cuda_fail(c, e, "set_U_device");
@@ -340,8 +612,7 @@ int nla3d_update_results(nla3d_ctx* c) {
   if (!c || !c->ready) return fail(c, NLA3D_ERR_ARG, "update_results before init");
   // SOLID81 keeps its Gauss-point state as a snapshot of vecU; the linear
   // elements have no state on the assembly path.
-  cudaError_t e = cudaMemcpyAsync(c->d_Ustate, c->d_U, sizeof(double) * c->hm.n_total(),
-                                  cudaMemcpyDeviceToDevice, c->stream);
+  cudaError_t e = enqueue_update(c);
   if (e != cudaSuccess) return cuda_fail(c, e, "update_results");
   c->have_state = true;
   return NLA3D_OK;
@@ -349,110 +620,56 @@ int nla3d_update_results(nla3d_ctx* c) {
 
 int nla3d_assemble(nla3d_ctx* c) {
   if (!c || !c->ready) return fail(c, NLA3D_ERR_ARG, "assemble before init");
-  HostModel& m = c->hm;
-  cudaError_t e;
-  e = cudaMemsetAsync(c->d_status, 0, sizeof(ElementStatus), c->stream);
-  if (e == cudaSuccess) e = cudaMemsetAsync(&c->d_status->first, 0xFF, sizeof(uint32_t), c->stream);
-  if (e != cudaSuccess) return cuda_fail(c, e, "assemble: status reset");
-  const uint64_t slot = (c->timed % nla3d_ctx::kRing) * 5;
-  auto mark = [&](int i) {
-    if (c->timing) cudaEventRecord(c->ev[slot + i], c->stream);
-  };
-  mark(0);
-  if (m.etype == NLA3D_SOLID81) {
-    Solid81Args a{};
-    a.n_elems = m.n_elems;
-    a.Gt = c->d_Gt;
-    a.wdet = c->d_wdet;
-    a.conn = c->d_conn;
-    a.node_eq3 = c->d_node_eq3;
-    a.p_eq = c->d_p_eq;
-    a.U_state = c->d_Ustate;
-    a.U_cur = c->d_U;
-    a.have_state = c->have_state ? 1 : 0;
-    a.mat_id = m.mat_id;
-    for (int i = 0; i < 5; i++) a.mc[i] = m.mat_c[i];
-    a.kbulk = m.mat_id == NLA3D_MAT_NEO_HOOKEAN ? m.mat_c[1]
-                                                : (m.mat_id == NLA3D_MAT_BIDERMAN ? m.mat_c[4]
-                                                                                  : m.mat_c[2]);
-    a.contribK = c->d_contribK;
-    a.contribF = c->d_contribF;
-    a.status = c->d_status;
-    e = launch_solid81(a, c->precision == NLA3D_PREC_MIXED, 0, c->stream);
-  } else {
-    LinearArgs a{m.etype, m.n_elems, c->d_xyz, c->d_conn, c->d_eparams, c->d_contribK,
-                 c->d_contribF, c->d_status};
-    e = launch_linear(a, c->stream);
-  }
-  if (e != cudaSuccess) return cuda_fail(c, e, "assemble: element kernel");
-  c->launches++;
-  mark(1);
-  GatherArgs gk{m.nnz_total, c->d_kptr, c->d_kids, c->d_contribK, c->d_K};
-  e = launch_gather(gk, c->stream);
-  if (e != cudaSuccess) return cuda_fail(c, e, "assemble: K gather");
-  c->launches += m.nnz_total ? 1 : 0;
-  mark(2);
-  GatherArgs gf{m.n_total(), c->d_fptr, c->d_fids, c->d_contribF, c->d_F};
-  e = launch_gather(gf, c->stream);
-  if (e != cudaSuccess) return cuda_fail(c, e, "assemble: F gather");
-  c->launches++;
-  mark(3);
-  if (m.n_mpc) {
-    const uint64_t M = m.n_mpc;
-    MpcArgs a{};
-    a.n_mpc = m.n_mpc;
-    a.master = c->d_mpc_u32;
-    a.slave = c->d_mpc_u32 + M;
-    a.eq = c->d_mpc_u32 + 2 * M;
-    a.slave_eq = c->d_mpc_u32 + 3 * M;
-    a.master_eq6 = c->d_mpc_u32 + 4 * M;
-    a.slot = c->d_mpc_u32 + 10 * M;
-    a.slave_dof = c->d_mpc_dof;
-    a.xyz = c->d_xyz;
-    a.U = c->d_U;
-    a.K = c->d_K;
-    a.F = c->d_F;
-    e = launch_mpc(a, c->stream);
-    if (e != cudaSuccess) return cuda_fail(c, e, "assemble: MPC rows");
-    c->launches++;
-  }
-  mark(4);
-  if (c->timing) c->timed++;
-  return NLA3D_OK;
+  cudaError_t e = enqueue_assembly(c);
+  return e == cudaSuccess ? NLA3D_OK : cuda_fail(c, e, "assemble");
 }
 
 int nla3d_get_K(nla3d_ctx* c, int block, double* values) {
   const int b = block_slot(block);
   if (!c || !c->ready || b < 0) return fail(c, NLA3D_ERR_ARG, "get_K");
-  const uint64_t n = c->hm.blk[b].nnz();
+  const uint64_t n = c->hm[0].blk[b].nnz();
   if (!n) return NLA3D_OK;
   if (!values) return fail(c, NLA3D_ERR_ARG, "get_K: null output");
-  cudaError_t e = cudaMemcpyAsync(values, c->d_K + c->hm.val_off[b], sizeof(double) * n,
+  cudaError_t e = cudaMemcpyAsync(values, c->d_K + c->hm[0].val_off[b], sizeof(double) * n,
                                   cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   return e == cudaSuccess ? NLA3D_OK : cuda_fail(c, e, "get_K");
 }
 
+int nla3d_get_K_all(nla3d_ctx* c, double* values) {
+  if (!c || !c->ready || !values) return fail(c, NLA3D_ERR_ARG, "get_K_all");
+  cudaError_t e = cudaMemcpyAsync(values, c->d_K, sizeof(double) * c->Ktot(),
+                                  cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  return e == cudaSuccess ? NLA3D_OK : cuda_fail(c, e, "get_K_all");
+}
+
 int nla3d_get_F(nla3d_ctx* c, double* F) {
   if (!c || !c->ready || !F) return fail(c, NLA3D_ERR_ARG, "get_F");
-  cudaError_t e = cudaMemcpyAsync(F, c->d_F, sizeof(double) * c->hm.n_total(),
-                                  cudaMemcpyDeviceToHost, c->stream);
+  cudaError_t e = cudaMemcpyAsync(F, c->d_F, sizeof(double) * c->Utot(), cudaMemcpyDeviceToHost,
+                                  c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   return e == cudaSuccess ? NLA3D_OK : cuda_fail(c, e, "get_F");
 }
 
 int nla3d_device_K(const nla3d_ctx* c, int block, double** values, uint64_t* n) {
+  if (!c || !c->ready || !values || !n) return NLA3D_ERR_ARG;
+  if (block == 0) {
+    *values = c->d_K;
+    *n = c->Ktot();
+    return NLA3D_OK;
+  }
   const int b = block_slot(block);
-  if (!c || !c->ready || b < 0 || !values || !n) return NLA3D_ERR_ARG;
-  *values = c->d_K + c->hm.val_off[b];
-  *n = c->hm.blk[b].nnz();
+  if (b < 0) return NLA3D_ERR_ARG;
+  *values = c->d_K + c->hm[0].val_off[b];
+  *n = c->hm[0].blk[b].nnz();
   return NLA3D_OK;
 }
 
 int nla3d_device_F(const nla3d_ctx* c, double** F, uint64_t* n) {
   if (!c || !c->ready || !F || !n) return NLA3D_ERR_ARG;
   *F = c->d_F;
-  *n = c->hm.n_total();
+  *n = c->Utot();
   return NLA3D_OK;
 }
 
@@ -474,6 +691,129 @@ int nla3d_element_status(nla3d_ctx* c, uint32_t* count, uint32_t* first) {
 }
 
 uint64_t nla3d_kernel_launches(const nla3d_ctx* c) { return c ? c->launches : 0; }
+
+int nla3d_set_launch_shape(nla3d_ctx* c, int warps_per_block, int blocks_per_sm,
+                           int gather_block) {
+  if (!c) return NLA3D_ERR_ARG;
+  if (warps_per_block != 2 && warps_per_block != 4 && warps_per_block != 8) return NLA3D_ERR_ARG;
+  if (gather_block != 128 && gather_block != 256 && gather_block != 512 && gather_block != 1024)
+    return NLA3D_ERR_ARG;
+  c->shape.warps_per_block = warps_per_block;
+  c->shape.blocks_per_sm = blocks_per_sm < 0 ? 0 : blocks_per_sm;
+  c->gather_bs = gather_block;
+  graph_release(c);
+  return NLA3D_OK;
+}
+
+int nla3d_autotune(nla3d_ctx* c, int reps, int32_t chosen[3], float* best_ms) {
+  if (!c || !c->ready) return fail(c, NLA3D_ERR_ARG, "autotune before init");
+  if (reps < 1) reps = 1;
+  graph_release(c);
+  const bool mixed = c->precision == NLA3D_PREC_MIXED;
+  const bool solid = c->hm[0].etype == NLA3D_SOLID81;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  if (cudaEventCreate(&t0) != cudaSuccess || cudaEventCreate(&t1) != cudaSuccess)
+    return fail(c, NLA3D_ERR_CUDA, "autotune events");
+  const bool was_timing = c->timing;
+  c->timing = false;
+  auto measure = [&](float* ms) -> cudaError_t {
+    cudaError_t e = enqueue_assembly(c);  // warm
+    if (e != cudaSuccess) return e;
+    cudaEventRecord(t0, c->stream);
+    for (int r = 0; r < reps; r++) {
+      e = enqueue_assembly(c);
+      if (e != cudaSuccess) return e;
+    }
+    cudaEventRecord(t1, c->stream);
+    e = cudaEventSynchronize(t1);
+    if (e != cudaSuccess) return e;
+    cudaEventElapsedTime(ms, t0, t1);
+    *ms /= reps;
+    return cudaSuccess;
+  };
+  Solid81Shape best_shape = c->shape;
+  int best_bs = c->gather_bs;
+  float best = 3.4e38f;
+  cudaError_t e = cudaSuccess;
+  const int wpbs[3] = {2, 4, 8};
+  for (int wi = 0; wi < (solid ? 3 : 1) && e == cudaSuccess; wi++) {
+    const int maxb = solid ? solid81_max_blocks_per_sm(mixed, wpbs[wi]) : 1;
+    for (int b = 1; b <= maxb && e == cudaSuccess; b++) {
+      c->shape.warps_per_block = wpbs[wi];
+      c->shape.blocks_per_sm = b;
+      float ms = 0;
+      e = measure(&ms);
+      if (e == cudaSuccess && ms < best) {
+        best = ms;
+        best_shape = c->shape;
+      }
+    }
+  }
+  c->shape = best_shape;
+  const int bss[4] = {128, 256, 512, 1024};
+  best = 3.4e38f;
+  for (int i = 0; i < 4 && e == cudaSuccess; i++) {
+    c->gather_bs = bss[i];
+    float ms = 0;
+    e = measure(&ms);
+    if (e == cudaSuccess && ms < best) {
+      best = ms;
+      best_bs = bss[i];
+    }
+  }
+  c->gather_bs = best_bs;
+  c->timing = was_timing;
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  if (e != cudaSuccess) return cuda_fail(c, e, "autotune");
+  if (chosen) {
+    chosen[0] = c->shape.warps_per_block;
+    chosen[1] = c->shape.blocks_per_sm;
+    chosen[2] = c->gather_bs;
+  }
+  if (best_ms) *best_ms = best;
+  return NLA3D_OK;
+}
+
+int nla3d_graph_capture(nla3d_ctx* c) {
+  if (!c || !c->ready) return fail(c, NLA3D_ERR_ARG, "graph_capture before init");
+  graph_release(c);
+  cudaError_t e = prepare_device_tables();
+  if (e != cudaSuccess) return cuda_fail(c, e, "graph_capture: tables");
+  const bool was_timing = c->timing;
+  c->timing = false;
+  e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) {
+    c->timing = was_timing;
+    return cuda_fail(c, e, "graph_capture: begin");
+  }
+  const uint64_t launches0 = c->launches;
+  cudaError_t eu = enqueue_update(c);
+  cudaError_t ea = eu == cudaSuccess ? enqueue_assembly(c) : eu;
+  e = cudaStreamEndCapture(c->stream, &c->graph);
+  c->launches = launches0;  // nothing ran yet
+  c->timing = was_timing;
+  if (ea != cudaSuccess) {
+    graph_release(c);
+    return cuda_fail(c, ea, "graph_capture: enqueue");
+  }
+  if (e != cudaSuccess) return cuda_fail(c, e, "graph_capture: end");
+  e = cudaGraphInstantiate(&c->graph_exec, c->graph, 0);
+  if (e != cudaSuccess) {
+    graph_release(c);
+    return cuda_fail(c, e, "graph_capture: instantiate");
+  }
+  c->have_state = true;
+  return NLA3D_OK;
+}
+
+int nla3d_graph_launch(nla3d_ctx* c) {
+  if (!c || !c->graph_exec) return fail(c, NLA3D_ERR_ARG, "graph_launch without a captured graph");
+  cudaError_t e = cudaGraphLaunch(c->graph_exec, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "graph_launch");
+  c->launches += 3 + (c->Mtot() ? 1 : 0);
+  return NLA3D_OK;
+}
 
 int nla3d_set_timing(nla3d_ctx* c, int on) {
   if (!c) return NLA3D_ERR_ARG;

@@ -24,7 +24,7 @@ namespace nla3d_gpu {
 
 namespace {
 
-constexpr int kWarpsPerBlock = 4;
+constexpr int kWarpsPerBlock = 4;  // default launch shape
 constexpr int kEPW = 4;                              // elements per warp
 constexpr int kKuuPerElem = 300;
 constexpr int kOwned = (kEPW * kKuuPerElem + 31) / 32;  // Kuu entries per lane (38)
@@ -35,10 +35,10 @@ __constant__ uchar4 c_kuu_entry[kKuuPerElem];
 
 template <typename TT>
 struct WarpSmem {
-  double F[9][32];     // per (element q, Gauss point g): deformation gradient
-  double wP[9][32];    // -w F S
+  double wP[9][32];    // per (element q, Gauss point g): -w F S
   double wCof[9][32];  //  w cof(F)
-  double wS[6][32];    //  w S (Voigt xx xy xz yy yz zz)
+  TT Ft[9][32];        //  F = I + O in the tangent type
+  TT wSt[6][32];       //  w S (Voigt xx xy xz yy yz zz) in the tangent type
   TT wD[21][32];       //  w * 2 Dd, packed upper
   TT Bh[18][32];       // per (element q, node a) of the current Gauss point: Bh[r*3+i]
   TT DB[18][32];       // (w 2 Dd) Bh
@@ -117,15 +117,17 @@ __device__ __forceinline__ void material(int mat_id, const double* mc, const dou
   const double c0 = pj - k1 * t13 - k2 * t23;
   const TT sIIt = (TT)(w * (2.0 * pj - k1 * I1 - k2 * I2));
   const TT sI = (TT)(w * 1.5 * k2);
+  // scalar coefficients in FP64, the 6-vectors P, Q, R in the tangent type
+  const TT wk11 = (TT)(w * k11), wk1 = (TT)(w * k1), wk2 = (TT)(w * k2), wc0 = (TT)(w * c0);
   TT P[6], Q[6], R[6], At[6], Bt[6], Ct[6];
 #pragma unroll
   for (int i = 0; i < 6; i++) {
-    P[i] = (TT)(w * (k11 * A[i] - k1 * Ci[i]));
-    Q[i] = (TT)(w * (-k2 * Ci[i]));
-    R[i] = (TT)(w * (-k1 * A[i] - k2 * B[i] + c0 * Ci[i]));
     At[i] = (TT)A[i];
     Bt[i] = (TT)B[i];
     Ct[i] = (TT)Ci[i];
+    P[i] = wk11 * At[i] - wk1 * Ct[i];
+    Q[i] = -wk2 * Ct[i];
+    R[i] = -wk1 * At[i] - wk2 * Bt[i] + wc0 * Ct[i];
   }
   // IIt (materials_hyperelastic.cpp:97-108): -sym(Ci (x) Ci), packed upper
   const TT c_xx = Ct[0], c_xy = Ct[1], c_xz = Ct[2], c_yy = Ct[3], c_yz = Ct[4], c_zz = Ct[5];
@@ -155,8 +157,8 @@ __device__ __forceinline__ void material(int mat_id, const double* mc, const dou
   (void)B;
 }
 
-template <typename TT>
-__global__ void __launch_bounds__(kWarpsPerBlock * 32)
+template <typename TT, int WPB>
+__global__ void __launch_bounds__(WPB * 32)
     solid81_kernel(const Solid81Args a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   uint32_t* dec = reinterpret_cast<uint32_t*>(smem_raw);  // [kOwned][32]
@@ -186,9 +188,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
   const uint32_t E = a.n_elems;
   const uint64_t E8 = (uint64_t)E * 8;
   const uint64_t n_quads = (E + kEPW - 1) / kEPW;
-  const uint64_t warp_global = (uint64_t)blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
-  const uint64_t warp_stride = (uint64_t)gridDim.x * kWarpsPerBlock;
-  const double kb = a.kbulk;
+  const uint64_t warp_global = (uint64_t)blockIdx.x * WPB + (threadIdx.x >> 5);
+  const uint64_t warp_stride = (uint64_t)gridDim.x * WPB;
 
   for (uint64_t quad = warp_global; quad < n_quads; quad += warp_stride) {
     const uint32_t e0 = (uint32_t)(quad * kEPW);
@@ -242,9 +243,19 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
         C[0] = C[3] = C[5] = 1.0;
         C[1] = C[2] = C[4] = 0.0;
       }
+      int mat_id = a.mat_id;
+      const double* mc = a.mc;
+      double kbulk = a.kbulk;
+      if (a.elem_mesh) {
+        const double* mm = a.mesh_mat + 8 * (uint64_t)__ldg(a.elem_mesh + ec);
+        mat_id = (int)mm[0];
+        mc = mm + 1;
+        kbulk = mm[6];
+      }
+      const double inv_kb = 1.0 / kbulk;
       MatOut<TT> mo;
       TT wD[21];
-      material<TT>(a.mat_id, a.mc, C, ps, pc, w, mo, wD);
+      material<TT>(mat_id, mc, C, ps, pc, w, mo, wD);
       if (!a.have_state) {
 #pragma unroll
         for (int i = 0; i < 6; i++) mo.S[i] = 0.0;
@@ -267,16 +278,15 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
                              F[1] * F[5] - F[2] * F[4], F[2] * F[3] - F[0] * F[5],
                              F[0] * F[4] - F[1] * F[3]};
 #pragma unroll
-      for (int c = 0; c < 9; c++) {
-        sm->F[c][lane] = F[c];
-        sm->wCof[c][lane] = w * cof[c];
-      }
+      for (int c = 0; c < 9; c++) sm->wCof[c][lane] = w * cof[c];
 #pragma unroll
-      for (int c = 0; c < 6; c++) sm->wS[c][lane] = w * mo.S[c];
+      for (int c = 0; c < 9; c++) sm->Ft[c][lane] = (TT)F[c];
+#pragma unroll
+      for (int c = 0; c < 6; c++) sm->wSt[c][lane] = (TT)(w * mo.S[c]);
 #pragma unroll
       for (int c = 0; c < 21; c++) sm->wD[c][lane] = wD[c];
-      Fp_part = -(J - 1 - pc / kb) * w;
-      Kpp_part = -1.0 / kb * w;
+      Fp_part = -(J - 1 - pc * inv_kb) * w;
+      Kpp_part = -inv_kb * w;
       // J = sqrt(det C) cannot see an inverted element; det F can
       const double detF = F[0] * cof[0] + F[1] * cof[1] + F[2] * cof[2];
       const bool bad = valid && !(J > 0.0 && isfinite(J) && detF > 0.0 && w > 0.0);
@@ -315,7 +325,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
         const TT g0 = (TT)G0, g1 = (TT)G1, g2 = (TT)G2;
         TT Fm[9];
 #pragma unroll
-        for (int c = 0; c < 9; c++) Fm[c] = (TT)sm->F[c][s1];
+        for (int c = 0; c < 9; c++) Fm[c] = sm->Ft[c][s1];
         TT Bh[18];
 #pragma unroll
         for (int i = 0; i < 3; i++) {
@@ -341,8 +351,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
           }
 #pragma unroll
         for (int c = 0; c < 18; c++) sm->Bh[c][lane] = Bh[c];
-        const TT sxx = (TT)sm->wS[0][s1], sxy = (TT)sm->wS[1][s1], sxz = (TT)sm->wS[2][s1],
-                 syy = (TT)sm->wS[3][s1], syz = (TT)sm->wS[4][s1], szz = (TT)sm->wS[5][s1];
+        const TT sxx = sm->wSt[0][s1], sxy = sm->wSt[1][s1], sxz = sm->wSt[2][s1],
+                 syy = sm->wSt[3][s1], syz = sm->wSt[4][s1], szz = sm->wSt[5][s1];
         sm->SG[0][lane] = sxx * g0 + sxy * g1 + sxz * g2;
         sm->SG[1][lane] = sxy * g0 + syy * g1 + syz * g2;
         sm->SG[2][lane] = sxz * g0 + syz * g1 + szz * g2;
@@ -693,9 +703,66 @@ cudaError_t ensure_tables() {
 
 }  // namespace
 
-size_t solid81_smem_bytes(bool mixed) {
+size_t solid81_smem_bytes_wpb(bool mixed, int wpb) {
   const size_t dec = sizeof(uint32_t) * kOwned * 32;
-  return dec + kWarpsPerBlock * (mixed ? sizeof(WarpSmem<float>) : sizeof(WarpSmem<double>));
+  return dec + wpb * (mixed ? sizeof(WarpSmem<float>) : sizeof(WarpSmem<double>));
+}
+
+size_t solid81_smem_bytes(bool mixed) { return solid81_smem_bytes_wpb(mixed, kWarpsPerBlock); }
+
+template <typename TT>
+void* solid81_fn(int wpb) {
+  switch (wpb) {
+    case 2: return (void*)solid81_kernel<TT, 2>;
+    case 8: return (void*)solid81_kernel<TT, 8>;
+    default: return (void*)solid81_kernel<TT, 4>;
+  }
+}
+
+cudaError_t prepare_device_tables() { return ensure_tables(); }
+
+int solid81_max_blocks_per_sm(bool mixed, int wpb) {
+  void* fn = mixed ? solid81_fn<float>(wpb) : solid81_fn<double>(wpb);
+  const size_t smem = solid81_smem_bytes_wpb(mixed, wpb);
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess)
+    return 0;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, wpb * 32, smem) != cudaSuccess)
+    return 0;
+  return per_sm;
+}
+
+cudaError_t launch_solid81_shaped(const Solid81Args& a, bool mixed, Solid81Shape shape,
+                                  cudaStream_t s) {
+  if (a.n_elems == 0) return cudaSuccess;
+  const int wpb = (shape.warps_per_block == 2 || shape.warps_per_block == 8)
+                      ? shape.warps_per_block : 4;
+  cudaError_t err = ensure_tables();
+  if (err != cudaSuccess) return err;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const size_t smem = solid81_smem_bytes_wpb(mixed, wpb);
+  const int max_per_sm = solid81_max_blocks_per_sm(mixed, wpb);
+  if (max_per_sm < 1) return cudaErrorInvalidConfiguration;
+  int per_sm = shape.blocks_per_sm;
+  if (per_sm <= 0 || per_sm > max_per_sm) per_sm = max_per_sm;
+  const uint64_t quads = ((uint64_t)a.n_elems + kEPW - 1) / kEPW;
+  uint64_t blocks = (uint64_t)sms * per_sm;
+  const uint64_t need = (quads + wpb - 1) / wpb;
+  if (blocks > need) blocks = need;
+  const dim3 grid((unsigned)blocks), block(wpb * 32);
+  if (mixed) {
+    if (wpb == 2) solid81_kernel<float, 2><<<grid, block, smem, s>>>(a);
+    else if (wpb == 8) solid81_kernel<float, 8><<<grid, block, smem, s>>>(a);
+    else solid81_kernel<float, 4><<<grid, block, smem, s>>>(a);
+  } else {
+    if (wpb == 2) solid81_kernel<double, 2><<<grid, block, smem, s>>>(a);
+    else if (wpb == 8) solid81_kernel<double, 8><<<grid, block, smem, s>>>(a);
+    else solid81_kernel<double, 4><<<grid, block, smem, s>>>(a);
+  }
+  return cudaGetLastError();
 }
 
 cudaError_t launch_solid81_jacobian(const JacobianArgs& a, cudaStream_t s) {
@@ -708,28 +775,10 @@ cudaError_t launch_solid81_jacobian(const JacobianArgs& a, cudaStream_t s) {
 
 cudaError_t launch_solid81(const Solid81Args& a, bool mixed, int blocks_per_sm_hint,
                            cudaStream_t s) {
-  if (a.n_elems == 0) return cudaSuccess;
-  cudaError_t err = ensure_tables();
-  if (err != cudaSuccess) return err;
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const size_t smem = solid81_smem_bytes(mixed);
-  auto kern = mixed ? solid81_kernel<float> : solid81_kernel<double>;
-  err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (err != cudaSuccess) return err;
-  int per_sm = blocks_per_sm_hint;
-  if (per_sm <= 0) {
-    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kWarpsPerBlock * 32, smem);
-    if (err != cudaSuccess) return err;
-    if (per_sm < 1) per_sm = 1;
-  }
-  const uint64_t quads = ((uint64_t)a.n_elems + kEPW - 1) / kEPW;
-  uint64_t blocks = (uint64_t)sms * per_sm;
-  const uint64_t need = (quads + kWarpsPerBlock - 1) / kWarpsPerBlock;
-  if (blocks > need) blocks = need;
-  kern<<<(unsigned)blocks, kWarpsPerBlock * 32, smem, s>>>(a);
-  return cudaGetLastError();
+  Solid81Shape shape;
+  shape.warps_per_block = kWarpsPerBlock;
+  shape.blocks_per_sm = blocks_per_sm_hint;
+  return launch_solid81_shaped(a, mixed, shape, s);
 }
 
 cudaError_t probe_fma_peak(bool fp64, double* flops) {
@@ -766,12 +815,14 @@ cudaError_t probe_fma_peak(bool fp64, double* flops) {
   return e;
 }
 
-cudaError_t launch_gather(const GatherArgs& a, cudaStream_t s) {
+cudaError_t launch_gather_bs(const GatherArgs& a, int bs, cudaStream_t s) {
   if (a.n_slots == 0) return cudaSuccess;
-  const int bs = 256;
+  if (bs != 128 && bs != 256 && bs != 512 && bs != 1024) bs = 256;
   gather_kernel<<<(unsigned)((a.n_slots + bs - 1) / bs), bs, 0, s>>>(a);
   return cudaGetLastError();
 }
+
+cudaError_t launch_gather(const GatherArgs& a, cudaStream_t s) { return launch_gather_bs(a, 256, s); }
 
 cudaError_t launch_mpc(const MpcArgs& a, cudaStream_t s) {
   if (a.n_mpc == 0) return cudaSuccess;

@@ -27,6 +27,11 @@ struct Solid81Args {
   int mat_id;
   double mc[5];
   double kbulk;
+  // optional per-element material (several meshes in one launch): when
+  // elem_mesh != nullptr, element e uses mesh_mat[8 * elem_mesh[e] + ...] =
+  // (mat_id, c0..c4, K) instead of mat_id / mc / kbulk
+  const uint32_t* elem_mesh;
+  const double* mesh_mat;
   double* contribK;         // [E * 325]
   double* contribF;         // [E * 25]
   ElementStatus* status;
@@ -79,6 +84,19 @@ struct LinearArgs {
 cudaError_t launch_solid81_jacobian(const JacobianArgs& a, cudaStream_t s);
 cudaError_t launch_solid81(const Solid81Args& a, bool mixed, int blocks_per_sm_hint,
                            cudaStream_t s);
+// Launch shape of the SOLID81 element kernel: warps per block (2, 4 or 8) and
+// resident blocks per SM (0 = as many as fit).
+struct Solid81Shape {
+  int warps_per_block = 4;
+  int blocks_per_sm = 0;
+};
+cudaError_t launch_solid81_shaped(const Solid81Args& a, bool mixed, Solid81Shape shape,
+                                  cudaStream_t s);
+int solid81_max_blocks_per_sm(bool mixed, int warps_per_block);
+cudaError_t launch_gather_bs(const GatherArgs& a, int block_size, cudaStream_t s);
+// kernel tables (constant memory) for the current device; call before any
+// stream capture
+cudaError_t prepare_device_tables();
 cudaError_t launch_gather(const GatherArgs& a, cudaStream_t s);
 cudaError_t launch_mpc(const MpcArgs& a, cudaStream_t s);
 cudaError_t launch_linear(const LinearArgs& a, cudaStream_t s);
