@@ -36,7 +36,7 @@ sys.path.insert(0, ROOT)
 FLOP_PER_ELEM = 69072          # FP64 structured algorithm, 8 Gauss points x 8634
 BYTES_PER_ELEM_ALGO = 2700     # compulsory HBM traffic per element (connectivity,
                                # X/U, p, slot map, K written once, F)
-METRIC = "SOLID81 assembly Melem/s"
+METRIC = "SOLID81 assembly Melem/s"  # Newton iterations per load step (plain vs learned) in "newton"
 UNIT = "Melem/s"
 
 
@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batch-meshes", type=int, default=256)
+    ap.add_argument("--no-newton", action="store_true")
     return ap.parse_args()
 
 
@@ -406,6 +407,11 @@ def run_ours(args):
     if not args.no_batched:
         batched = run_batched(args, torch, stream, local)
 
+    newton = None
+    if not args.no_newton and rank == 0:
+        from nla3d_gb300 import learned
+        newton = learned.benchmark()
+
     if rank != 0:
         return
     fp64_peak = probe_fma_peak(True)
@@ -446,6 +452,7 @@ def run_ours(args):
         "clocks": clk.summary(),
         "mixed": mixed,
         "batched": batched,
+        "newton": newton,
         "setup_s": setup_s,
         "element_status": {"flagged": int(count)},
     }

@@ -215,6 +215,31 @@ int nla3d_kernel_times(nla3d_ctx* ctx, float ms[4], uint32_t* count);
 int nla3d_probe_fma_peak(int fp64, double* flops);
 
 /* ---------------------------------------------------------------------------
+ * Learned Newton start: kernels of a small MLP (BF16 weights, FP32
+ * accumulation) trained on converged increments.  No counterpart in the
+ * reference (it always restarts Newton from the previous converged state).
+ * All pointers are device memory; calls are asynchronous on `stream`.
+ *   nla3d_mlp_gemm    C[m,n] = act(sum_k A[m,k] B[k,n] + bias[n]); A[m,k] is at
+ *                     A + m*lda_m + k*lda_k (B likewise), a_bf16 / b_bf16 select
+ *                     BF16 inputs; act 0 = identity, 1 = tanh; bias may be NULL.
+ *   nla3d_mlp_tanh_backward   dY *= 1 - Y*Y (in place)
+ *   nla3d_mlp_column_sum      out[c] = sum_r X[r, c] (row-major rows x cols)
+ *   nla3d_mlp_adam    Adam step on FP32 master weights (step >= 1), refreshing
+ *                     the BF16 copy w_bf16 when non-NULL
+ *   nla3d_mlp_mse_grad dY = scale * (Y - T)
+ *   nla3d_mlp_to_bf16 round-to-nearest-even FP32 -> BF16 */
+int nla3d_mlp_gemm(int M, int N, int K, const void* A, int a_bf16, int64_t lda_m, int64_t lda_k,
+                   const void* B, int b_bf16, int64_t ldb_k, int64_t ldb_n, float* C, int64_t ldc,
+                   const float* bias, int act, void* stream);
+int nla3d_mlp_tanh_backward(const float* Y, float* dY, int64_t n, void* stream);
+int nla3d_mlp_column_sum(const float* X, int64_t rows, int64_t cols, float* out, void* stream);
+int nla3d_mlp_adam(float* w, const float* g, float* m, float* v, int64_t n, float lr, float beta1,
+                   float beta2, float eps, int step, uint16_t* w_bf16, void* stream);
+int nla3d_mlp_mse_grad(const float* Y, const float* T, float* dY, int64_t n, float scale,
+                       void* stream);
+int nla3d_mlp_to_bf16(const float* x, uint16_t* y, int64_t n, void* stream);
+
+/* ---------------------------------------------------------------------------
  * SOLID81 assembly without device allocation.  No counterpart in the
  * reference (which has no GPU code); it is an extra entry point for callers
  * that may not allocate device memory: host frameworks that own all device

@@ -31,6 +31,8 @@ EXPORTS = [
     "nla3d_create_batch", "nla3d_mesh_count", "nla3d_mesh_add_fix", "nla3d_mesh_add_rigid_body",
     "nla3d_mesh_info", "nla3d_mesh_pattern", "nla3d_mesh_eq_numbers", "nla3d_get_K_all",
     "nla3d_set_launch_shape", "nla3d_autotune", "nla3d_graph_capture", "nla3d_graph_launch",
+    "nla3d_mlp_gemm", "nla3d_mlp_tanh_backward", "nla3d_mlp_column_sum", "nla3d_mlp_adam",
+    "nla3d_mlp_to_bf16", "nla3d_mlp_mse_grad",
 ]
 
 NOALLOC_MAX_ELEMS = 15252
@@ -92,6 +94,7 @@ def load(path: str = LIB_PATH):
             " (the CUDA path has no fallback)")
     lib = ctypes.CDLL(path)
     P, U32, U64, I32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int32
+    I64 = ctypes.c_int64
     sig = {
         "nla3d_create": ([ctypes.POINTER(MeshDesc), ctypes.c_int, ctypes.POINTER(P)], ctypes.c_int),
         "nla3d_destroy": ([P], ctypes.c_int),
@@ -134,6 +137,14 @@ def load(path: str = LIB_PATH):
         "nla3d_autotune": ([P, ctypes.c_int, P, ctypes.POINTER(ctypes.c_float)], ctypes.c_int),
         "nla3d_graph_capture": ([P], ctypes.c_int),
         "nla3d_graph_launch": ([P], ctypes.c_int),
+        "nla3d_mlp_gemm": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, P, ctypes.c_int, I64, I64, P,
+                            ctypes.c_int, I64, I64, P, I64, P, ctypes.c_int, P], ctypes.c_int),
+        "nla3d_mlp_tanh_backward": ([P, P, I64, P], ctypes.c_int),
+        "nla3d_mlp_column_sum": ([P, I64, I64, P, P], ctypes.c_int),
+        "nla3d_mlp_adam": ([P, P, P, P, I64, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                            ctypes.c_float, ctypes.c_int, P, P], ctypes.c_int),
+        "nla3d_mlp_to_bf16": ([P, P, I64, P], ctypes.c_int),
+        "nla3d_mlp_mse_grad": ([P, P, P, I64, ctypes.c_float, P], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

@@ -5,6 +5,7 @@ Translation units (compiled in parallel, then linked by nvcc):
   csrc/capi.cu         C ABI (include/nla3d_gpu.h)
   csrc/host_model.cpp  DoF numbering, CSR pattern, slot maps (host C++)
   csrc/noalloc.cu      SOLID81 assembly with a fixed, library-owned scratch array
+  csrc/mlp.cu          kernels of the learned Newton start (BF16 MLP)
 """
 from __future__ import annotations
 
@@ -21,7 +22,7 @@ LIB = os.path.join(HERE, "libnla3d_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O3",
               "-I" + os.path.join(ROOT, "include")]
-SOURCES = ["kernels.cu", "capi.cu", "host_model.cpp", "noalloc.cu"]
+SOURCES = ["kernels.cu", "capi.cu", "host_model.cpp", "noalloc.cu", "mlp.cu"]
 
 
 def nvcc() -> str:

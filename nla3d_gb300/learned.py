@@ -1,0 +1,450 @@
+"""Learned Newton start.
+
+A small MLP proposes each load step's starting state from the last two
+converged increments, the load factor and the material constants; the Newton
+driver (nla3d_gb300.newton) keeps the reference's plain start (previous
+converged state + linearised constrained increment) whenever the proposal's
+residual is not smaller, and the unchanged residual tolerance decides
+convergence either way.
+
+Proposal:  dU_n = a1 dU_{n-1} + a2 dU_{n-2} + s Q c
+  Q   64 orthonormal coarse modes of the free (unknown + MPC) DoFs: Legendre
+      polynomials of total degree <= 3 on the normalised geometry for each
+      displacement component (60) and degree <= 1 for the element pressure (4);
+  s   |Q^T dU_{n-1}|, so that the network sees scale-free inputs;
+  (a1, a2, c) = MLP(Q^T dU_{n-1} / s, Q^T dU_{n-2} / s, t, dt_n/dt_{n-1}, C10, log10 K / 4).
+Training targets are the least-squares coefficients of the converged dU_n on
+[dU_{n-1}, dU_{n-2}, s Q], from solves run with the plain start.
+
+The network (4 hidden layers of 256, tanh, BF16 weights, FP32 accumulation)
+is trained on the GPU by the library's own kernels (csrc/mlp.cu) through its
+C ABI; torch only provides device memory.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import math
+
+import numpy as np
+
+from . import _lib
+from . import meshgen as mg
+
+N_MODES = 64
+N_IN = 2 * N_MODES + 4
+N_OUT = 2 + N_MODES
+HIDDEN = (256, 256, 256, 256)
+
+
+# ---------------------------------------------------------------------------
+# coarse modes and features
+# ---------------------------------------------------------------------------
+
+def _legendre(k, x):
+    return [np.ones_like(x), x, 0.5 * (3 * x * x - 1), 0.5 * (5 * x ** 3 - 3 * x)][k]
+
+
+class CoarseBasis:
+    def __init__(self, mesh: mg.Mesh, ne, ee, nc, n_total):
+        self.nc, self.n = nc, n_total
+        lo, hi = mesh.xyz.min(axis=0), mesh.xyz.max(axis=0)
+        span = np.where(hi - lo > 0, hi - lo, 1.0)
+        xn = 2.0 * (mesh.xyz - lo) / span - 1.0
+        cen = xn[mesh.conn.astype(np.int64) - 1].mean(axis=1)
+        degs = [(i, j, k) for i in range(4) for j in range(4) for k in range(4) if i + j + k <= 3]
+        nf = n_total - nc
+        phi = []
+        for comp in range(3):
+            eq = ne[: mesh.n_nodes, comp].astype(np.int64)
+            ok = eq > nc
+            for (i, j, k) in degs:
+                col = np.zeros(nf)
+                v = _legendre(i, xn[:, 0]) * _legendre(j, xn[:, 1]) * _legendre(k, xn[:, 2])
+                col[eq[ok] - 1 - nc] = v[ok]
+                phi.append(col)
+        eqp = ee[:, mg.HYDRO_PRESSURE].astype(np.int64)
+        okp = eqp > nc
+        for f in (np.ones(len(cen)), cen[:, 0], cen[:, 1], cen[:, 2]):
+            col = np.zeros(nf)
+            col[eqp[okp] - 1 - nc] = f[okp]
+            phi.append(col)
+        Phi = np.stack(phi, axis=1)
+        self.Q, _ = np.linalg.qr(Phi)
+
+    def project(self, dU):
+        return self.Q.T @ dU[self.nc:]
+
+
+def features(basis: CoarseBasis, dU1, dU2, t, ratio, c10, kbulk):
+    p1, p2 = basis.project(dU1), basis.project(dU2)
+    s = float(np.linalg.norm(p1)) + 1e-300
+    x = np.concatenate([p1 / s, p2 / s, [t, ratio, c10, math.log10(kbulk) / 4.0]])
+    return x, s
+
+
+def target(basis: CoarseBasis, dU1, dU2, dU, s):
+    nc = basis.nc
+    A = np.concatenate([dU1[nc:, None], dU2[nc:, None], s * basis.Q], axis=1)
+    y, *_ = np.linalg.lstsq(A, dU[nc:], rcond=None)
+    return y
+
+
+def compose(basis: CoarseBasis, dU1, dU2, s, y):
+    out = np.zeros_like(dU1)
+    nc = basis.nc
+    out[nc:] = y[0] * dU1[nc:] + y[1] * dU2[nc:] + s * (basis.Q @ y[2:])
+    return out
+
+
+# ---------------------------------------------------------------------------
+# the MLP on the GPU (library kernels; torch buffers)
+# ---------------------------------------------------------------------------
+
+class MLP:
+    def __init__(self, sizes=(N_IN,) + HIDDEN + (N_OUT,), seed=0, device="cuda:0"):
+        import torch
+        self.torch = torch
+        self.lib = _lib.load()
+        self.sizes = tuple(sizes)
+        self.dev = torch.device(device)
+        self.stream = torch.cuda.current_stream(self.dev).cuda_stream
+        rng = np.random.default_rng(seed)
+        self.W, self.Wb, self.b, self.state = [], [], [], []
+        for fan_in, fan_out in zip(self.sizes[:-1], self.sizes[1:]):
+            lim = math.sqrt(6.0 / (fan_in + fan_out))
+            W = torch.from_numpy(rng.uniform(-lim, lim, (fan_out, fan_in)).astype(np.float32)).to(self.dev)
+            self.W.append(W)
+            self.Wb.append(torch.empty(W.shape, dtype=torch.bfloat16, device=self.dev))
+            self.b.append(torch.zeros(fan_out, dtype=torch.float32, device=self.dev))
+            self.state.append([torch.zeros_like(W), torch.zeros_like(W),
+                               torch.zeros(fan_out, device=self.dev),
+                               torch.zeros(fan_out, device=self.dev)])
+        for W, Wb in zip(self.W, self.Wb):
+            self._ck(self.lib.nla3d_mlp_to_bf16(W.data_ptr(), Wb.data_ptr(), W.numel(), self.stream))
+        self.step_count = 0
+        self.x_mean = self.x_std = self.y_mean = self.y_std = None
+
+    def _ck(self, rc):
+        if rc:
+            raise _lib.Nla3dError(rc, "MLP kernel launch failed")
+
+    def forward(self, X):
+        """X: float32 cuda tensor (B, in).  Returns activations [X, h1, ..., out]."""
+        acts = [X]
+        L = len(self.W)
+        for l in range(L):
+            out_dim, in_dim = self.W[l].shape
+            Y = self.torch.empty((X.shape[0], out_dim), dtype=self.torch.float32, device=self.dev)
+            # Y = act(A W^T + b): A[m,k] at m*in + k; (W^T)[k,n] = W[n,k] at n*in + k
+            self._ck(self.lib.nla3d_mlp_gemm(X.shape[0], out_dim, in_dim, acts[-1].data_ptr(), 0,
+                                             in_dim, 1, self.Wb[l].data_ptr(), 1, 1, in_dim,
+                                             Y.data_ptr(), out_dim, self.b[l].data_ptr(),
+                                             1 if l < L - 1 else 0, self.stream))
+            acts.append(Y)
+        return acts
+
+    def backward(self, acts, dOut):
+        """Gradients (dW, db) per layer for the output gradient dOut (B, out)."""
+        torch = self.torch
+        L = len(self.W)
+        B = dOut.shape[0]
+        gW, gb = [None] * L, [None] * L
+        d = dOut
+        for l in range(L - 1, -1, -1):
+            out_dim, in_dim = self.W[l].shape
+            if l < L - 1:
+                self._ck(self.lib.nla3d_mlp_tanh_backward(acts[l + 1].data_ptr(), d.data_ptr(),
+                                                          d.numel(), self.stream))
+            dW = torch.empty((out_dim, in_dim), dtype=torch.float32, device=self.dev)
+            # dW[o,i] = sum_b d[b,o] X[b,i]: A = d^T (A[o,b] at b*out + o), B = X (B[b,i] at b*in + i)
+            self._ck(self.lib.nla3d_mlp_gemm(out_dim, in_dim, B, d.data_ptr(), 0, 1, out_dim,
+                                             acts[l].data_ptr(), 0, in_dim, 1, dW.data_ptr(), in_dim,
+                                             None, 0, self.stream))
+            db = torch.empty(out_dim, dtype=torch.float32, device=self.dev)
+            self._ck(self.lib.nla3d_mlp_column_sum(d.data_ptr(), B, out_dim, db.data_ptr(),
+                                                   self.stream))
+            gW[l], gb[l] = dW, db
+            if l > 0:
+                dX = torch.empty((B, in_dim), dtype=torch.float32, device=self.dev)
+                # dX[b,i] = sum_o d[b,o] W[o,i]: A = d (A[b,o] at b*out + o), B = W (B[o,i] at o*in + i)
+                self._ck(self.lib.nla3d_mlp_gemm(B, in_dim, out_dim, d.data_ptr(), 0, out_dim, 1,
+                                                 self.Wb[l].data_ptr(), 1, in_dim, 1, dX.data_ptr(),
+                                                 in_dim, None, 0, self.stream))
+                d = dX
+        return gW, gb
+
+    def loss_grad(self, out, T):
+        """MSE loss gradient 2 (out - T) / n (library kernel)."""
+        d = self.torch.empty_like(out)
+        self._ck(self.lib.nla3d_mlp_mse_grad(out.data_ptr(), T.data_ptr(), d.data_ptr(), out.numel(),
+                                             2.0 / out.numel(), self.stream))
+        return d
+
+    def adam(self, gW, gb, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8):
+        self.step_count += 1
+        for l in range(len(self.W)):
+            mW, vW, mb, vb = self.state[l]
+            self._ck(self.lib.nla3d_mlp_adam(self.W[l].data_ptr(), gW[l].data_ptr(), mW.data_ptr(),
+                                             vW.data_ptr(), self.W[l].numel(), lr, b1, b2, eps,
+                                             self.step_count, self.Wb[l].data_ptr(), self.stream))
+            self._ck(self.lib.nla3d_mlp_adam(self.b[l].data_ptr(), gb[l].data_ptr(), mb.data_ptr(),
+                                             vb.data_ptr(), self.b[l].numel(), lr, b1, b2, eps,
+                                             self.step_count, None, self.stream))
+
+    # ---- training on numpy data ----
+    def fit(self, X, Y, epochs=200, batch=256, lr=1e-3, seed=0, log=None):
+        torch = self.torch
+        self.x_mean, self.x_std = X.mean(0), X.std(0) + 1e-8
+        self.y_mean, self.y_std = Y.mean(0), Y.std(0) + 1e-8
+        Xn = torch.from_numpy(((X - self.x_mean) / self.x_std).astype(np.float32)).to(self.dev)
+        Yn = torch.from_numpy(((Y - self.y_mean) / self.y_std).astype(np.float32)).to(self.dev)
+        rng = np.random.default_rng(seed)
+        n = X.shape[0]
+        history = []
+        for ep in range(epochs):
+            perm = torch.from_numpy(rng.permutation(n)).to(self.dev)
+            for i in range(0, n, batch):
+                idx = perm[i:i + batch]
+                xb, yb = Xn[idx].contiguous(), Yn[idx].contiguous()
+                acts = self.forward(xb)
+                gW, gb = self.backward(acts, self.loss_grad(acts[-1], yb))
+                self.adam(gW, gb, lr=lr * (0.5 * (1 + math.cos(math.pi * ep / epochs))))
+            if ep % 20 == 0 or ep == epochs - 1:
+                out = self.forward(Xn)[-1]
+                loss = float(((out - Yn) ** 2).mean())
+                history.append((ep, loss))
+                if log:
+                    log(f"epoch {ep} loss {loss:.4e}")
+        return history
+
+    def predict(self, X):
+        torch = self.torch
+        Xn = torch.from_numpy(((np.atleast_2d(X) - self.x_mean) / self.x_std).astype(np.float32)).to(self.dev)
+        out = self.forward(Xn)[-1].cpu().numpy().astype(np.float64)
+        return out * self.y_std + self.y_mean
+
+    def weights(self):
+        return ([W.cpu().numpy().astype(np.float64) for W in self.W],
+                [b.cpu().numpy().astype(np.float64) for b in self.b])
+
+
+# ---------------------------------------------------------------------------
+# predictors for the Newton driver
+# ---------------------------------------------------------------------------
+
+class History:
+    """on_converged hook: converged U and load factors, starting from U = 0 at t = 0."""
+
+    def __init__(self, n_total):
+        self.U = [np.zeros(n_total)]
+        self.t = [0.0]
+
+    def __call__(self, solver, t):
+        self.U.append(solver.U.copy())
+        self.t.append(t)
+
+
+class ExtrapolationPredictor:
+    """Secant extrapolation of the last converged increment (a baseline)."""
+
+    def __init__(self, history):
+        self.h = history
+
+    def propose(self, solver, t):
+        h = self.h
+        if len(h.U) < 3:
+            return None
+        r = (t - h.t[-1]) / (h.t[-1] - h.t[-2])
+        return h.U[-1] + r * (h.U[-1] - h.U[-2])
+
+
+class MLPPredictor:
+    def __init__(self, mlp: MLP, basis: CoarseBasis, history: History, c10, kbulk):
+        self.mlp, self.basis, self.h = mlp, basis, history
+        self.c10, self.kbulk = c10, kbulk
+
+    def propose(self, solver, t):
+        h = self.h
+        if len(h.U) < 3:
+            return None
+        dU1, dU2 = h.U[-1] - h.U[-2], h.U[-2] - h.U[-3]
+        ratio = (t - h.t[-1]) / (h.t[-1] - h.t[-2])
+        x, s = features(self.basis, dU1, dU2, t, ratio, self.c10, self.kbulk)
+        y = self.mlp.predict(x)[0]
+        return h.U[-1] + compose(self.basis, dU1, dU2, s, y)
+
+
+# ---------------------------------------------------------------------------
+# problem families (seeded)
+# ---------------------------------------------------------------------------
+
+@dataclasses.dataclass
+class Problem:
+    mesh: mg.Mesh
+    fixes: list
+    c10: float
+    kbulk: float
+    n_loadsteps: int
+    label: str = ""
+
+
+def block_problem(n, c10, kbulk, stretch, n_loadsteps=20):
+    """n^3 block on the unit cube, z=0 clamped, z=1 face pulled to `stretch`
+    (UZ prescribed, UX/UY free); Neo-Hookean G = 2 C10, K."""
+    m = mg.solid81_block(n, n, n, 1.0 / n, mg.MAT_NEO_HOOKEAN, (2 * c10, kbulk), clamp_z0=True)
+    top = (np.nonzero(np.abs(m.xyz[:, 2] - 1.0) < 1e-12)[0] + 1).astype(np.uint32)
+    m.fix_nodes = np.concatenate([m.fix_nodes, top])
+    m.fix_dofs = np.concatenate([m.fix_dofs, np.full(top.size, mg.UZ, np.int32)])
+    fixes = [(int(a), int(b), 0.0) for a, b in zip(m.fix_nodes[:-top.size], m.fix_dofs[:-top.size])]
+    fixes += [(int(a), mg.UZ, stretch - 1.0) for a in top]
+    return Problem(m, fixes, c10, kbulk, n_loadsteps,
+                   f"block{n} C10={c10:.3f} K={kbulk:.0f} stretch={stretch:.3f}")
+
+
+def bar_problem(nx, nz, c10, kbulk, stretch, twist_rad, n_loadsteps=50):
+    """nx x nx x nz bar (h = 1), z=0 clamped, z=L face slaved to a master node
+    (RigidBodyMpc) driven to UZ = (stretch-1) L and ROTZ = twist; Neo-Hookean."""
+    m = mg.solid81_bar_mpc(nx, nx, nz, 1.0, mg.MAT_NEO_HOOKEAN, (2 * c10, kbulk))
+    master = m.n_nodes
+    L = float(nz)
+    mf = [(master, mg.UX, 0.0), (master, mg.UY, 0.0), (master, mg.UZ, (stretch - 1.0) * L),
+          (master, mg.ROTX, 0.0), (master, mg.ROTY, 0.0), (master, mg.ROTZ, twist_rad)]
+    m.fix_nodes = np.concatenate([m.fix_nodes, np.full(6, master, np.uint32)])
+    m.fix_dofs = np.concatenate([m.fix_dofs, np.arange(6, dtype=np.int32)])
+    fixes = [(int(a), int(b), 0.0) for a, b in zip(m.fix_nodes[:-6], m.fix_dofs[:-6])] + mf
+    return Problem(m, fixes, c10, kbulk, n_loadsteps,
+                   f"bar{nx}x{nx}x{nz} C10={c10:.3f} K={kbulk:.0f} stretch={stretch:.3f} "
+                   f"twist={math.degrees(twist_rad):.1f}deg")
+
+
+def sample_block_problems(count, n=4, seed=0, n_loadsteps=20):
+    """C10 ~ U(0.2, 1.0), K ~ U(500, 5000), target stretch ~ U(1.0, 2.0)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    return [block_problem(n, rng.uniform(0.2, 1.0), rng.uniform(500.0, 5000.0),
+                          rng.uniform(1.0, 2.0), n_loadsteps) for _ in range(count)]
+
+
+def sample_bar_problems(count, nx=3, nz=12, seed=0, n_loadsteps=50):
+    """Around the torsion+stretch bar: C10 ~ U(0.3, 0.7), K ~ U(500, 2000),
+    stretch ~ U(1.5, 2.0), twist ~ U(45, 90) deg."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    return [bar_problem(nx, nz, rng.uniform(0.3, 0.7), rng.uniform(500.0, 2000.0),
+                        rng.uniform(1.5, 2.0), math.radians(rng.uniform(45.0, 90.0)),
+                        n_loadsteps) for _ in range(count)]
+
+
+# ---------------------------------------------------------------------------
+# data generation, training and evaluation
+# ---------------------------------------------------------------------------
+
+def solve(problem: Problem, backend, predictor_factory=None, residual_tol=1e-8, n_iterations=25):
+    """Run the Newton driver; returns (solver, history)."""
+    from .newton import NewtonSolver
+    solver = NewtonSolver(backend, problem.fixes, n_loadsteps=problem.n_loadsteps,
+                          n_iterations=n_iterations, residual_tol=residual_tol)
+    hist = History(backend.n_total)
+    pred = predictor_factory(solver, hist) if predictor_factory else None
+    solver.solve(predictor=pred, on_converged=hist)
+    return solver, hist
+
+
+def samples_from_history(basis, hist, c10, kbulk):
+    X, Y = [], []
+    for n in range(3, len(hist.U)):
+        dU = hist.U[n] - hist.U[n - 1]
+        dU1 = hist.U[n - 1] - hist.U[n - 2]
+        dU2 = hist.U[n - 2] - hist.U[n - 3]
+        t = hist.t[n]
+        ratio = (t - hist.t[n - 1]) / (hist.t[n - 1] - hist.t[n - 2])
+        x, s = features(basis, dU1, dU2, t, ratio, c10, kbulk)
+        X.append(x)
+        Y.append(target(basis, dU1, dU2, dU, s))
+    return X, Y
+
+
+def make_backend(problem: Problem, kind="gpu", precision="fp64"):
+    if kind == "gpu":
+        from .storage import FEStorage
+        return FEStorage(problem.mesh, precision).initSolutionData()
+    from oracle import oracle as O  # CPU oracle backend (tests only)
+    return O.OracleModel(problem.mesh, "port")
+
+
+def basis_for(problem: Problem, backend):
+    ne, ee = backend.eq_numbers()
+    return CoarseBasis(problem.mesh, ne, ee, backend.n_con, backend.n_total)
+
+
+def generate(problems, kind="gpu", precision="fp64"):
+    X, Y, iters = [], [], []
+    for pb in problems:
+        be = make_backend(pb, kind, precision)
+        solver, hist = solve(pb, be)
+        x, y = samples_from_history(basis_for(pb, be), hist, pb.c10, pb.kbulk)
+        X += x
+        Y += y
+        iters.append([r.iterations for r in solver.records])
+    return np.array(X), np.array(Y), iters
+
+
+def evaluate(problems, mlp, kind="gpu", precision="fp64"):
+    """Mean Newton iterations per load step: plain start, secant extrapolation
+    and the learned start (with the plain-start fallback)."""
+    out = {"plain": [], "extrapolation": [], "learned": [], "learned_used": []}
+    for pb in problems:
+        be = make_backend(pb, kind, precision)
+        basis = basis_for(pb, be)
+        s, _ = solve(pb, be)
+        out["plain"] += [r.iterations for r in s.records]
+        be = make_backend(pb, kind, precision)
+        s, _ = solve(pb, be, lambda sv, h: ExtrapolationPredictor(h))
+        out["extrapolation"] += [r.iterations for r in s.records]
+        be = make_backend(pb, kind, precision)
+        s, _ = solve(pb, be, lambda sv, h: MLPPredictor(mlp, basis, h, pb.c10, pb.kbulk))
+        out["learned"] += [r.iterations for r in s.records]
+        out["learned_used"] += [r.predicted for r in s.records]
+    return {k: float(np.mean(v)) for k, v in out.items()} | {"steps": len(out["plain"])}
+
+
+def benchmark(n_block_train=40, n_block_eval=8, n_bar_train=12, log=None):
+    """Newton iterations per load step, plain vs learned start, at a 1e-8
+    residual tolerance, on the two problem families (shrunk so that a run takes
+    about a minute on one GPU):
+      blocks: 4^3 SOLID81 on the unit cube, C10 ~ U(0.2, 1), K ~ U(500, 5000),
+              stretch ~ U(1, 2), 20 load steps (held-out seeds);
+      bar:    3x3x12 torsion + stretch bar (rigid-body MPC end) at C10 = 0.5,
+              K = 1000, stretch 2.0, 90 deg, 50 load steps, trained on bars with
+              C10 ~ U(0.3, 0.7), K ~ U(500, 2000), stretch ~ U(1.5, 2), twist
+              ~ U(45, 90) deg.
+    Also FP64 vs mixed assembly iteration counts on that bar."""
+    import time
+    out = {}
+    t0 = time.perf_counter()
+    X, Y, _ = generate(sample_block_problems(n_block_train, n=4, seed=11))
+    mlp = MLP(seed=0)
+    h = mlp.fit(X, Y, epochs=300, batch=128, lr=2e-3)
+    out["blocks"] = evaluate(sample_block_problems(n_block_eval, n=4, seed=99), mlp)
+    out["blocks"].update({"train_samples": int(X.shape[0]), "final_loss": h[-1][1],
+                          "mesh": "4x4x4 SOLID81", "load_steps": 20})
+    if log:
+        log(f"blocks: {out['blocks']}")
+    Xb, Yb, _ = generate(sample_bar_problems(n_bar_train, nx=3, nz=12, seed=5, n_loadsteps=50))
+    mlpb = MLP(seed=1)
+    hb = mlpb.fit(Xb, Yb, epochs=300, batch=128, lr=2e-3)
+    cfg = bar_problem(3, 12, 0.5, 1000.0, 2.0, math.pi / 2, 50)
+    out["bar"] = evaluate([cfg], mlpb)
+    out["bar"].update({"train_samples": int(Xb.shape[0]), "final_loss": hb[-1][1],
+                       "mesh": "3x3x12 SOLID81 + rigid-body MPC end", "load_steps": 50})
+    its = {}
+    for precision in ("fp64", "mixed"):
+        be = make_backend(cfg, "gpu", precision)
+        s, _ = solve(cfg, be)
+        its[precision] = float(np.mean([r.iterations for r in s.records]))
+    out["bar"]["iterations_fp64_assembly"] = its["fp64"]
+    out["bar"]["iterations_mixed_assembly"] = its["mixed"]
+    out["residual_tol"] = 1e-8
+    out["seconds"] = time.perf_counter() - t0
+    if log:
+        log(f"bar: {out['bar']}")
+    return out

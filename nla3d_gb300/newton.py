@@ -1,0 +1,225 @@
+"""Quasi-static Newton-Raphson driver around the GPU assembly.
+
+Mirrors NonlinearFESolver::solve (FESolver.cpp:407-508) with TimeControl
+(FESolver.cpp:34-56): per load step the fixed DoFs move to value * t, each
+equilibrium iteration assembles K and F (on the GPU), solves
+
+    K(2) dU_sl = F_sl + R_sl - K(1,2)^T dU_c          (FESolver.cpp:449-457)
+
+updates U_s += dU_s, U_l = dU_l, recovers the reactions
+R_c = K(1) dU_c + K(1,2) dU_sl - F_c (FESolver.cpp:464-467) and calls
+updateResults.  The reference's kinematic criterion (mean |dU_s| / tol < tol,
+FESolver.cpp:511-521) is kept; a residual criterion ||F_sl + R_sl|| < tol can
+be selected instead.  The linear solve runs on the host (SciPy's sparse LU),
+standing in for the reference's EquationSolver (EquationSolver.h:19-34).
+
+A predictor may propose each load step's starting state (the learned start);
+the plain start (previous converged state) is kept whenever the proposal's
+residual is not smaller.
+"""
+from __future__ import annotations
+
+import dataclasses
+
+import numpy as np
+import scipy.sparse as sp
+import scipy.sparse.linalg as spla
+
+
+class TimeControl:
+    """Load stepping of the reference (FESolver.h:27-56, FESolver.cpp:34-56)."""
+
+    def __init__(self, start=0.0, end=1.0):
+        self.start, self.end = start, end
+        self.t = start
+        self.dt = 0.0
+        self.step = 0
+        self.eq_step = 0
+
+    def next_step(self, delta):
+        if self.t >= self.end:
+            return False
+        if self.t + delta >= self.end:
+            self.dt = self.end - self.t
+        elif self.t + 2 * delta >= self.end:
+            self.dt = (self.end - self.t) / 2.0
+        else:
+            self.dt = delta
+        self.t += self.dt
+        self.step += 1
+        self.eq_step = 0
+        return True
+
+    def normalized(self):
+        return (self.t - self.start) / (self.end - self.start)
+
+
+def csr_full(iofeir, columns, values, rows, cols, symmetric_upper):
+    ind = iofeir.astype(np.int64) - 1
+    m = sp.csr_matrix((values, columns.astype(np.int64) - 1, ind), shape=(rows, cols))
+    if symmetric_upper:
+        m = (m + sp.triu(m, 1).T).tocsr()
+    return m
+
+
+@dataclasses.dataclass
+class StepRecord:
+    time: float
+    iterations: int
+    residuals: list
+    criteria: list
+    predicted: bool = False
+    prediction_residual: float | None = None
+    plain_residual: float | None = None
+
+
+class NewtonSolver:
+    """backend: an object with eq_numbers(), pattern(b), K(b), F(), set_U(U),
+    update(), assemble(), n_con, n_unk, n_mpc, n_total, blocks -- the GPU
+    FEStorage (nla3d_gb300.storage) or the CPU oracle model."""
+
+    def __init__(self, backend, fixes, n_loadsteps=10, n_iterations=15, kinematic_tol=1e-3,
+                 residual_tol=None, loads=()):
+        self.b = backend
+        self.n_loadsteps = n_loadsteps
+        self.n_iterations = n_iterations
+        self.kinematic_tol = kinematic_tol
+        self.residual_tol = residual_tol
+        ne, ee = backend.eq_numbers()
+        self.ne = ne
+        self.nc, self.nu, self.nm = backend.n_con, backend.n_unk, backend.n_mpc
+        self.n = backend.n_total
+        # fixes: (node, dof, value) -- FESolver::addFix; loads: (node, dof, value)
+        self.fix_eq = np.array([int(ne[n - 1, d]) for n, d, _ in fixes], dtype=np.int64)
+        self.fix_val = np.array([v for _, _, v in fixes], dtype=np.float64)
+        assert np.all(self.fix_eq >= 1) and np.all(self.fix_eq <= self.nc), "fix on an unconstrained DoF"
+        self.load_eq = np.array([int(ne[n - 1, d]) for n, d, _ in loads], dtype=np.int64)
+        self.load_val = np.array([v for _, _, v in loads], dtype=np.float64)
+        self.patterns = {blk: backend.pattern(blk) for blk in (1, 12, 2)}
+        self.U = np.zeros(self.n)
+        self.R = np.zeros(self.n)
+        self.records: list[StepRecord] = []
+        self.reactions: list[np.ndarray] = [np.zeros(self.nc)]
+
+    # ---- the global system ----
+    def _matrices(self):
+        rows1, cols1, _ = self.b.blocks[1]
+        rows12, cols12, _ = self.b.blocks[12]
+        rows2, cols2, _ = self.b.blocks[2]
+        K1 = csr_full(*self.patterns[1], self.b.K(1), rows1, cols1, True)
+        K12 = csr_full(*self.patterns[12], self.b.K(12), rows12, cols12, False)
+        K2 = csr_full(*self.patterns[2], self.b.K(2), rows2, cols2, True)
+        return K1, K12, K2
+
+    def _apply_bc(self, t):
+        """FESolver::applyBoundaryConditions (FESolver.cpp:229-247)."""
+        self.R[:] = 0.0
+        if self.load_eq.size:
+            np.add.at(self.R, self.load_eq - 1, self.load_val * t)
+        Uc = self.U[: self.nc].copy()
+        Uc[self.fix_eq - 1] = self.fix_val * t
+        return Uc
+
+    def _assemble(self, U):
+        self.b.set_U(U)
+        self.b.assemble()
+        return self.b.F()
+
+    def residual(self, F, K12, K2, dUc):
+        """Equilibrium residual of the unknown + MPC rows.  The reference solves
+        the Lagrange multipliers as totals (vecUl = deltaUl, FESolver.cpp:461),
+        so its right-hand side F_sl + R_sl - K12^T dUc still contains the
+        constraint forces; the residual removes them: r = rhs - K2 [0; U_l]."""
+        lam = np.zeros(self.nu + self.nm)
+        lam[self.nu:] = self.U[self.nc + self.nu:]
+        return F[self.nc:] + self.R[self.nc:] - K12.T @ dUc - K2 @ lam
+
+    # ---- the load-step loop ----
+    def solve(self, predictor=None, on_converged=None):
+        tc = TimeControl()
+        delta = (tc.end - tc.start) / self.n_loadsteps
+        Ucprev = np.zeros(self.nc)
+        self.b.set_U(self.U)
+        self.b.update()
+        while tc.next_step(delta):
+            t = tc.normalized()
+            rec = StepRecord(time=t, iterations=0, residuals=[], criteria=[])
+            self.current = rec
+            Uc_new = self._apply_bc(t)
+            if predictor is not None:
+                prop = predictor.propose(self, t)
+                if prop is not None:
+                    # residual of the plain start: F(U_prev) - K12^T dUc (linearised)
+                    F0 = self._assemble(self.U)
+                    _, K12, K2 = self._matrices()
+                    r_plain = self.residual(F0, K12, K2, Uc_new - Ucprev)
+                    Up = prop.copy()
+                    Up[: self.nc] = Uc_new
+                    Uold = self.U
+                    self.U = Up
+                    self.b.set_U(Up)
+                    self.b.update()
+                    Fp = self._assemble(Up)
+                    _, K12p, K2p = self._matrices()
+                    r_pred = float(np.linalg.norm(self.residual(Fp, K12p, K2p, 0.0 * Uc_new)))
+                    self.U = Uold
+                    rec.prediction_residual, rec.plain_residual = r_pred, float(np.linalg.norm(r_plain))
+                    if np.isfinite(r_pred) and r_pred < rec.plain_residual:
+                        self.U = Up
+                        Ucprev = Uc_new.copy()
+                        rec.predicted = True
+                    else:
+                        self.b.set_U(self.U)
+                        self.b.update()
+            converged = False
+            while True:
+                tc.eq_step += 1
+                F = self._assemble(self.U)
+                Uc = self._apply_bc(t)
+                dUc = Uc - Ucprev
+                K1, K12, K2 = self._matrices()
+                rhs = F[self.nc:] + self.R[self.nc:] - K12.T @ dUc
+                rnorm = float(np.linalg.norm(self.residual(F, K12, K2, dUc)))
+                rec.residuals.append(rnorm)
+                if self.residual_tol is not None and tc.eq_step > 1 and rnorm < self.residual_tol \
+                        and not np.any(dUc):
+                    # converged without a further solve: reactions for a zero increment
+                    sl = np.zeros(self.nu + self.nm)
+                    sl[self.nu:] = self.U[self.nc + self.nu:]
+                    self.R[: self.nc] = K12 @ sl - F[: self.nc]
+                    rec.iterations = tc.eq_step - 1
+                    converged = True
+                    break
+                dUsl = spla.spsolve(K2.tocsc(), rhs, permc_spec="MMD_AT_PLUS_A")
+                self.U[: self.nc] = Uc
+                self.U[self.nc: self.nc + self.nu] += dUsl[: self.nu]
+                self.U[self.nc + self.nu:] = dUsl[self.nu:]
+                Rc = K1 @ dUc + K12 @ dUsl - F[: self.nc]
+                self.R[: self.nc] = Rc
+                Ucprev = Uc.copy()
+                self.b.set_U(self.U)
+                self.b.update()
+                crit = float(np.abs(dUsl[: self.nu]).sum() / max(self.nu, 1)) / self.kinematic_tol
+                rec.criteria.append(crit)
+                if not np.isfinite(crit) or crit > 1e6:
+                    raise RuntimeError("The solution is diverged!")
+                if self.residual_tol is None and crit < self.kinematic_tol:
+                    rec.iterations = tc.eq_step
+                    converged = True
+                    break
+                if tc.eq_step >= self.n_iterations:
+                    rec.iterations = tc.eq_step
+                    break
+            if not converged:
+                raise RuntimeError(f"The solution is not converged with {tc.eq_step} equilibrium "
+                                   "iterations")
+            self.records.append(rec)
+            self.reactions.append(self.R[: self.nc].copy())
+            if on_converged is not None:
+                on_converged(self, t)
+        return self
+
+    def reaction(self, node, dof):
+        """Reaction history of one constrained DoF (ReactionProcessor, summed per step)."""
+        eq = int(self.ne[node - 1, dof])
+        return np.array([r[eq - 1] for r in self.reactions])

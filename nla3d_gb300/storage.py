@@ -212,6 +212,16 @@ class FEStorage:
     def updateResults(self):
         self._check(self.lib.nla3d_update_results(self.h))
 
+    # short names shared with the oracle model (the Newton driver's backend API)
+    def set_U(self, U):
+        self.setU(U)
+
+    def update(self):
+        self.updateResults()
+
+    def assemble(self):
+        self.assembleGlobalEqMatrices()
+
     def assembleGlobalEqMatrices(self):
         self._check(self.lib.nla3d_assemble(self.h))
 

@@ -51,7 +51,67 @@ def digest(a):
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 
 
+def read_rigid_body_case(cdb_path, curve_path):
+    """The reference's `rigid_body_mpc_block_ROTX` test input (test/CMakeLists.txt:51-57):
+    nodes (NBLOCK), the SOLID81 connectivity (EBLOCK, last 8 fields), node
+    components (CMBLOCK) and fixed DoFs (D lines) of its .cdb, plus the
+    reference reaction curve (third column, test/rigid_body_mpc/)."""
+    lines = open(cdb_path).read().splitlines()
+    nodes, elems, comps, fixes = {}, [], {}, []
+    i = 0
+    while i < len(lines):
+        ln = lines[i]
+        if ln.startswith("NBLOCK"):
+            i += 2
+            while not lines[i].startswith("N,"):
+                t = lines[i]
+                nid = int(t[0:9])
+                nodes[nid] = [float(t[27 + 20 * k: 47 + 20 * k]) for k in range(3)]
+                i += 1
+        elif ln.startswith("EBLOCK"):
+            i += 2
+            while lines[i].strip() != "-1":
+                f = [int(lines[i][9 * k: 9 * k + 9]) for k in range(len(lines[i]) // 9)]
+                elems.append(f[11:19])
+                i += 1
+        elif ln.startswith("CMBLOCK"):
+            name = ln.split(",")[1].strip()
+            i += 2
+            comps[name] = [int(v) for v in lines[i].split()]
+        elif ln.startswith("D,"):
+            f = [v.strip() for v in ln.split(",")]
+            fixes.append((int(f[1]), f[2], float(f[3])))
+        i += 1
+    curve = []
+    with open(curve_path) as fh:
+        next(fh)
+        for row in fh:
+            if row.strip():
+                curve.append(float(row.split()[2]))
+    return nodes, elems, comps, fixes, curve
+
+
+def write_rigid_body_fixture():
+    base = "/root/reference/test/rigid_body_mpc"
+    nodes, elems, comps, fixes, curve = read_rigid_body_case(
+        f"{base}/block_ROTX.cdb", f"{base}/reference_MOMZ_reaction.txt")
+    labels = ["UX", "UY", "UZ", "ROTX", "ROTY", "ROTZ", "HYDRO_PRESSURE", "TEMP"]
+    n = max(nodes)
+    xyz = np.array([nodes[k] for k in range(1, n + 1)], dtype=np.float64)
+    np.savez_compressed(
+        os.path.join(HERE, "rigid_body_mpc_block_rotx.npz"),
+        xyz=xyz, conn=np.array(elems, dtype=np.uint32),
+        top_side=np.array(comps["TOP_SIDE"], dtype=np.uint32),
+        master=np.array(comps["MASTER_NODE"], dtype=np.uint32),
+        fix_node=np.array([f[0] for f in fixes], dtype=np.uint32),
+        fix_dof=np.array([labels.index(f[1]) for f in fixes], dtype=np.int32),
+        fix_value=np.array([f[2] for f in fixes], dtype=np.float64),
+        ref_curve=np.array(curve, dtype=np.float64))
+    print("wrote rigid_body_mpc_block_rotx")
+
+
 def main():
+    write_rigid_body_fixture()
     if not O.build_ref():
         sys.exit("reference sources not found; cannot regenerate goldens")
     for name, case in cases.FULL_CASES.items():
