@@ -187,13 +187,19 @@ int nla3d_element_status(nla3d_ctx* ctx, uint32_t* count, uint32_t* first);
 uint64_t nla3d_kernel_launches(const nla3d_ctx* ctx);
 
 /* Launch shape of the element kernel (warps per block 2/4/8, resident blocks
- * per SM, 0 = as many as fit) and the gather block size (128..1024).
- * nla3d_autotune times each candidate on this context's own mesh(es) with
- * `reps` assemblies, keeps the fastest and reports it in chosen[3] and
- * *best_ms (time of one assembly).  No counterpart in the reference. */
+ * per SM, 0 = as many as fit), the gather block size (128..1024), and the
+ * layout of the element contributions (0: element order, K gathered through
+ * an index list; 1: the element kernel writes each contribution at its slot
+ * position and K is a contiguous sum).  Every choice sums each K slot in the
+ * same order, so the results do not depend on them.  nla3d_autotune times the
+ * candidates on this context's own mesh(es) with `reps` assemblies, keeps the
+ * fastest and reports it in chosen[4] = (warps per block, blocks per SM,
+ * gather block, layout) and *best_ms (one assembly).  No counterpart in the
+ * reference. */
 int nla3d_set_launch_shape(nla3d_ctx* ctx, int warps_per_block, int blocks_per_sm,
                            int gather_block);
-int nla3d_autotune(nla3d_ctx* ctx, int reps, int32_t chosen[3], float* best_ms);
+int nla3d_set_contrib_layout(nla3d_ctx* ctx, int layout);
+int nla3d_autotune(nla3d_ctx* ctx, int reps, int32_t chosen[4], float* best_ms);
 
 /* Record updateResults + assembleGlobalEqMatrices (on the current vecU buffer)
  * as a CUDA graph on the context stream, and replay it.  A new launch shape

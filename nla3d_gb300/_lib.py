@@ -10,7 +10,7 @@ import ctypes
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libnla3d_gpu.so")
+LIB_PATH = os.environ.get("NLA3D_GPU_LIB") or os.path.join(HERE, "libnla3d_gpu.so")
 
 NLA3D_OK = 0
 ERR_NAMES = {1: "NLA3D_ERR_ARG", 2: "NLA3D_ERR_CUDA", 3: "NLA3D_ERR_PATTERN",
@@ -32,7 +32,7 @@ EXPORTS = [
     "nla3d_mesh_info", "nla3d_mesh_pattern", "nla3d_mesh_eq_numbers", "nla3d_get_K_all",
     "nla3d_set_launch_shape", "nla3d_autotune", "nla3d_graph_capture", "nla3d_graph_launch",
     "nla3d_mlp_gemm", "nla3d_mlp_tanh_backward", "nla3d_mlp_column_sum", "nla3d_mlp_adam",
-    "nla3d_mlp_to_bf16", "nla3d_mlp_mse_grad",
+    "nla3d_mlp_to_bf16", "nla3d_mlp_mse_grad", "nla3d_set_contrib_layout",
 ]
 
 NOALLOC_MAX_ELEMS = 15252
@@ -135,6 +135,7 @@ def load(path: str = LIB_PATH):
         "nla3d_get_K_all": ([P, P], ctypes.c_int),
         "nla3d_set_launch_shape": ([P, ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
         "nla3d_autotune": ([P, ctypes.c_int, P, ctypes.POINTER(ctypes.c_float)], ctypes.c_int),
+        "nla3d_set_contrib_layout": ([P, ctypes.c_int], ctypes.c_int),
         "nla3d_graph_capture": ([P], ctypes.c_int),
         "nla3d_graph_launch": ([P], ctypes.c_int),
         "nla3d_mlp_gemm": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, P, ctypes.c_int, I64, I64, P,

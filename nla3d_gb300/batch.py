@@ -165,11 +165,14 @@ class BatchAssembly:
                                                     gather_block))
 
     def autotune(self, reps=3):
-        chosen = np.zeros(3, np.int32)
+        chosen = np.zeros(4, np.int32)
         ms = ctypes.c_float()
         self._check(self.lib.nla3d_autotune(self.h, reps, _p(chosen), ctypes.byref(ms)))
         return {"warps_per_block": int(chosen[0]), "blocks_per_sm": int(chosen[1]),
-                "gather_block": int(chosen[2]), "ms": float(ms.value)}
+                "gather_block": int(chosen[2]), "layout": int(chosen[3]), "ms": float(ms.value)}
+
+    def set_contrib_layout(self, layout):
+        self._check(self.lib.nla3d_set_contrib_layout(self.h, layout))
 
     def capture_graph(self):
         self._check(self.lib.nla3d_graph_capture(self.h))

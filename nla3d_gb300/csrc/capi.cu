@@ -13,8 +13,17 @@
 //   p_eq    E        uint32  pressure equation per element, global 1-based
 //   U, U_state       double  concatenated vecU / snapshot at updateResults()
 //   contribK 325E, contribF 25E  double   element contributions, reference order
-//   k_ptr nnz+1, k_ids 325E  uint32   fixed-order gather lists of K
-//   f_ptr n+1,   f_ids 25E   uint32   same for F
+//   k_ptr nnz+1      uint32  start of each K slot's contributions in slot order
+//   k_ids 325E       uint32  slot order -> element contribution id e*325+c
+//                            (ascending within a slot: element order, then the
+//                            reference's local order)
+//   k_pos 325E       uint32  the inverse map (element contribution -> slot order)
+//   f_ptr n+1, f_ids, f_pos 25E   same for F
+// Two contribution layouts (nla3d_set_contrib_layout / nla3d_autotune):
+//   0  element order: contribK[e*325+c]; K[s] gathers contribK[k_ids[k]]
+//   1  slot order: the element kernel writes contribK[k_pos[e*325+c]]; K[s]
+//      sums the contiguous contribK[k_ptr[s] .. k_ptr[s+1])
+// Both sum each slot in the same order, so K is bitwise the same.
 //   K (per mesh: block(1) | block(1,2) | block(2)), F   double
 //   elem_mesh E, mesh_mat 8M  per-element material (only when meshes differ)
 #include <cuda_runtime.h>
@@ -61,8 +70,11 @@ struct nla3d_ctx {
   double* d_contribF = nullptr;
   uint32_t* d_kptr = nullptr;
   uint32_t* d_kids = nullptr;
+  uint32_t* d_kpos = nullptr;
   uint32_t* d_fptr = nullptr;
   uint32_t* d_fids = nullptr;
+  uint32_t* d_fpos = nullptr;
+  int layout = 0;
   double* d_K = nullptr;
   double* d_F = nullptr;
   uint32_t* d_elem_mesh = nullptr;
@@ -185,25 +197,38 @@ cudaError_t enqueue_assembly(nla3d_ctx* c) {
     a.kbulk = bulk_of(m0);
     a.elem_mesh = c->uniform_material ? nullptr : c->d_elem_mesh;
     a.mesh_mat = c->uniform_material ? nullptr : c->d_mesh_mat;
+    a.kpos = c->layout ? c->d_kpos : nullptr;
+    a.fpos = c->layout ? c->d_fpos : nullptr;
     a.contribK = c->d_contribK;
     a.contribF = c->d_contribF;
     a.status = c->d_status;
     e = launch_solid81_shaped(a, c->precision == NLA3D_PREC_MIXED, c->shape, c->stream);
   } else {
     LinearArgs a{m0.etype, (uint32_t)c->E(), c->d_xyz, c->d_conn, c->d_eparams, c->d_contribK,
-                 c->d_contribF, c->d_status};
+                 c->d_contribF, c->d_status, c->layout ? c->d_kpos : nullptr,
+                 c->layout ? c->d_fpos : nullptr};
     e = launch_linear(a, c->stream);
   }
   if (e != cudaSuccess) return e;
   c->launches++;
   mark(1);
-  GatherArgs gk{c->Ktot(), c->d_kptr, c->d_kids, c->d_contribK, c->d_K};
-  e = launch_gather_bs(gk, c->gather_bs, c->stream);
+  if (c->layout) {
+    SegSumArgs gk{c->Ktot(), c->d_kptr, c->d_contribK, c->d_K};
+    e = launch_segsum(gk, c->gather_bs, c->stream);
+  } else {
+    GatherArgs gk{c->Ktot(), c->d_kptr, c->d_kids, c->d_contribK, c->d_K};
+    e = launch_gather_bs(gk, c->gather_bs, c->stream);
+  }
   if (e != cudaSuccess) return e;
   c->launches += c->Ktot() ? 1 : 0;
   mark(2);
-  GatherArgs gf{c->Utot(), c->d_fptr, c->d_fids, c->d_contribF, c->d_F};
-  e = launch_gather_bs(gf, c->gather_bs, c->stream);
+  if (c->layout) {
+    SegSumArgs gf{c->Utot(), c->d_fptr, c->d_contribF, c->d_F};
+    e = launch_segsum(gf, c->gather_bs, c->stream);
+  } else {
+    GatherArgs gf{c->Utot(), c->d_fptr, c->d_fids, c->d_contribF, c->d_F};
+    e = launch_gather_bs(gf, c->gather_bs, c->stream);
+  }
   if (e != cudaSuccess) return e;
   c->launches++;
   mark(3);
@@ -458,6 +483,10 @@ int nla3d_init_solution_data(nla3d_ctx* c) {
   }
   kptr[nnz] = (uint32_t)(E * n_kc);
   fptr[ntot] = (uint32_t)(E * n_fc);
+  // slot-order position of every contribution: the inverse of the gather ids
+  std::vector<uint32_t> kpos(E * n_kc), fpos(E * n_fc);
+  for (uint64_t k = 0; k < kids.size(); k++) kpos[kids[k]] = (uint32_t)k;
+  for (uint64_t k = 0; k < fids.size(); k++) fpos[fids[k]] = (uint32_t)k;
 
 #define CK(x)                                           \
   do {                                                  \
@@ -475,8 +504,10 @@ int nla3d_init_solution_data(nla3d_ctx* c) {
   }
   CK(upload(c, &c->d_kptr, kptr.data(), kptr.size()));
   CK(upload(c, &c->d_kids, kids.data(), kids.size()));
+  CK(upload(c, &c->d_kpos, kpos.data(), kpos.size()));
   CK(upload(c, &c->d_fptr, fptr.data(), fptr.size()));
   CK(upload(c, &c->d_fids, fids.data(), fids.size()));
+  CK(upload(c, &c->d_fpos, fpos.data(), fpos.size()));
   CK(dalloc(c, &c->d_U, ntot));
   CK(dalloc(c, &c->d_Ustate, ntot));
   CK(cudaMemsetAsync(c->d_U, 0, sizeof(double) * ntot, c->stream));
@@ -705,7 +736,14 @@ int nla3d_set_launch_shape(nla3d_ctx* c, int warps_per_block, int blocks_per_sm,
   return NLA3D_OK;
 }
 
-int nla3d_autotune(nla3d_ctx* c, int reps, int32_t chosen[3], float* best_ms) {
+int nla3d_set_contrib_layout(nla3d_ctx* c, int layout) {
+  if (!c || (layout != 0 && layout != 1)) return NLA3D_ERR_ARG;
+  c->layout = layout;
+  graph_release(c);
+  return NLA3D_OK;
+}
+
+int nla3d_autotune(nla3d_ctx* c, int reps, int32_t chosen[4], float* best_ms) {
   if (!c || !c->ready) return fail(c, NLA3D_ERR_ARG, "autotune before init");
   if (reps < 1) reps = 1;
   graph_release(c);
@@ -732,24 +770,29 @@ int nla3d_autotune(nla3d_ctx* c, int reps, int32_t chosen[3], float* best_ms) {
     return cudaSuccess;
   };
   Solid81Shape best_shape = c->shape;
-  int best_bs = c->gather_bs;
+  int best_bs = c->gather_bs, best_layout = c->layout;
   float best = 3.4e38f;
   cudaError_t e = cudaSuccess;
   const int wpbs[3] = {2, 4, 8};
-  for (int wi = 0; wi < (solid ? 3 : 1) && e == cudaSuccess; wi++) {
-    const int maxb = solid ? solid81_max_blocks_per_sm(mixed, wpbs[wi]) : 1;
-    for (int b = 1; b <= maxb && e == cudaSuccess; b++) {
-      c->shape.warps_per_block = wpbs[wi];
-      c->shape.blocks_per_sm = b;
-      float ms = 0;
-      e = measure(&ms);
-      if (e == cudaSuccess && ms < best) {
-        best = ms;
-        best_shape = c->shape;
+  for (int layout = 0; layout < 2 && e == cudaSuccess; layout++) {
+    c->layout = layout;
+    for (int wi = 0; wi < (solid ? 3 : 1) && e == cudaSuccess; wi++) {
+      const int maxb = solid ? solid81_max_blocks_per_sm(mixed, wpbs[wi]) : 1;
+      for (int b = 1; b <= maxb && e == cudaSuccess; b++) {
+        c->shape.warps_per_block = wpbs[wi];
+        c->shape.blocks_per_sm = b;
+        float ms = 0;
+        e = measure(&ms);
+        if (e == cudaSuccess && ms < best) {
+          best = ms;
+          best_shape = c->shape;
+          best_layout = layout;
+        }
       }
     }
   }
   c->shape = best_shape;
+  c->layout = best_layout;
   const int bss[4] = {128, 256, 512, 1024};
   best = 3.4e38f;
   for (int i = 0; i < 4 && e == cudaSuccess; i++) {
@@ -770,6 +813,7 @@ int nla3d_autotune(nla3d_ctx* c, int reps, int32_t chosen[3], float* best_ms) {
     chosen[0] = c->shape.warps_per_block;
     chosen[1] = c->shape.blocks_per_sm;
     chosen[2] = c->gather_bs;
+    chosen[3] = c->layout;
   }
   if (best_ms) *best_ms = best;
   return NLA3D_OK;

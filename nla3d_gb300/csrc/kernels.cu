@@ -386,26 +386,28 @@ __global__ void __launch_bounds__(WPB * 32)
     }
 
     // ---------------- write the element contributions ----------------
+    // destination of contribution idx: slot-ordered (kpos) or element-ordered
+    auto kdst = [&](uint64_t idx) -> uint64_t { return a.kpos ? (uint64_t)__ldg(a.kpos + idx) : idx; };
+    auto fdst = [&](uint64_t idx) -> uint64_t { return a.fpos ? (uint64_t)__ldg(a.fpos + idx) : idx; };
 #pragma unroll
     for (int m = 0; m < kOwned; m++) {
       const int x = lane + 32 * m;
       if (x < kEPW * kKuuPerElem) {
         const int qq = x / kKuuPerElem, t = x - qq * kKuuPerElem;
         const uint32_t ee = e0 + qq;
-        if (ee < E) a.contribK[(uint64_t)ee * kSolidKc + t] = (double)acc[m];
+        if (ee < E) a.contribK[kdst((uint64_t)ee * kSolidKc + t)] = (double)acc[m];
       }
     }
     if (valid) {
-      double* ck = a.contribK + (uint64_t)e * kSolidKc;
-      double* cf = a.contribF + (uint64_t)e * kSolidFc;
+      const uint64_t kb = (uint64_t)e * kSolidKc, fb = (uint64_t)e * kSolidFc;
 #pragma unroll
       for (int i = 0; i < 3; i++) {
-        ck[300 + 3 * node + i] = Kup[i];
-        cf[3 * node + i] = Fu[i];
+        a.contribK[kdst(kb + 300 + 3 * node + i)] = Kup[i];
+        a.contribF[fdst(fb + 3 * node + i)] = Fu[i];
       }
       if (node == 0) {
-        ck[324] = Kpp_part;
-        cf[24] = Fp_part;
+        a.contribK[kdst(kb + 324)] = Kpp_part;
+        a.contribF[fdst(fb + 24)] = Fp_part;
       }
     }
     __syncwarp();
@@ -461,12 +463,43 @@ __global__ void solid81_jacobian_kernel(const JacobianArgs a) {
 
 // K[s] = sum of its contributions in ascending contribution order (the
 // reference's element-ascending accumulation order), starting from 0.
+// Up to kBatch loads of a slot are issued before the first add (a hexahedral
+// mesh has at most 8 contributions per K slot); the adds keep the ascending
+// order, so the sum is the same as the plain loop's.
+constexpr int kBatch = 8;
+
 __global__ void gather_kernel(const GatherArgs a) {
   const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= a.n_slots) return;
-  const uint32_t b = a.ptr[s], e = a.ptr[s + 1];
+  const uint32_t b = __ldg(a.ptr + s), e = __ldg(a.ptr + s + 1);
+  const uint32_t n = e - b;
+  uint32_t id[kBatch];
+#pragma unroll
+  for (int j = 0; j < kBatch; j++) id[j] = (uint32_t)j < n ? __ldg(a.ids + b + j) : 0u;
+  double x[kBatch];
+#pragma unroll
+  for (int j = 0; j < kBatch; j++) x[j] = (uint32_t)j < n ? __ldg(a.contrib + id[j]) : 0.0;
   double v = 0.0;
-  for (uint32_t k = b; k < e; k++) v += a.contrib[a.ids[k]];
+#pragma unroll
+  for (int j = 0; j < kBatch; j++)
+    if ((uint32_t)j < n) v += x[j];
+  for (uint32_t k = b + kBatch; k < e; k++) v += a.contrib[a.ids[k]];
+  a.out[s] = v;
+}
+
+__global__ void segsum_kernel(const SegSumArgs a) {
+  const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= a.n_slots) return;
+  const uint32_t b = __ldg(a.ptr + s), e = __ldg(a.ptr + s + 1);
+  const uint32_t n = e - b;
+  double x[kBatch];
+#pragma unroll
+  for (int j = 0; j < kBatch; j++) x[j] = (uint32_t)j < n ? __ldg(a.contrib + b + j) : 0.0;
+  double v = 0.0;
+#pragma unroll
+  for (int j = 0; j < kBatch; j++)
+    if ((uint32_t)j < n) v += x[j];
+  for (uint32_t k = b + kBatch; k < e; k++) v += a.contrib[k];
   a.out[s] = v;
 }
 
@@ -615,7 +648,6 @@ __global__ void linear_kernel(const LinearArgs a) {
       B[5][3 * i + 0] = dd[i] * Af;
       B[5][3 * i + 2] = bb[i] * Af;
     }
-    double* out = a.contribK + (uint64_t)e * 78;
     int idx = 0;
     for (int r = 0; r < 12; r++)
       for (int col = r; col < 12; col++, idx++) {
@@ -625,7 +657,8 @@ __global__ void linear_kernel(const LinearArgs a) {
           for (int l = 0; l < 6; l++) cb += Cm[k][l] * B[l][col];
           v += B[k][r] * cb;
         }
-        out[idx] = v * vol;
+        const uint64_t i = (uint64_t)e * 78 + idx;
+        a.contribK[a.kpos ? a.kpos[i] : i] = v * vol;
       }
   } else {
     // QUADTH: 2x2 Gauss (isoparametric.h:80-85), conduction k (QUADTH.cpp:22-49)
@@ -655,10 +688,14 @@ __global__ void linear_kernel(const LinearArgs a) {
         for (int j = i; j < 4; j++, idx++)
           Ke[idx] += (G[i][0] * kc * G[j][0] + G[i][1] * kc * G[j][1]) * w;
     }
-    double* out = a.contribK + (uint64_t)e * 10;
-    for (int i = 0; i < 10; i++) out[i] = Ke[i];
-    double* f = a.contribF + (uint64_t)e * 4;
-    for (int i = 0; i < 4; i++) f[i] = 0.0;  // volFlux = 0 (QUADTH.cpp:34-36)
+    for (int i = 0; i < 10; i++) {
+      const uint64_t k = (uint64_t)e * 10 + i;
+      a.contribK[a.kpos ? a.kpos[k] : k] = Ke[i];
+    }
+    for (int i = 0; i < 4; i++) {  // volFlux = 0 (QUADTH.cpp:34-36)
+      const uint64_t k = (uint64_t)e * 4 + i;
+      a.contribF[a.fpos ? a.fpos[k] : k] = 0.0;
+    }
   }
 }
 
@@ -823,6 +860,13 @@ cudaError_t launch_gather_bs(const GatherArgs& a, int bs, cudaStream_t s) {
 }
 
 cudaError_t launch_gather(const GatherArgs& a, cudaStream_t s) { return launch_gather_bs(a, 256, s); }
+
+cudaError_t launch_segsum(const SegSumArgs& a, int bs, cudaStream_t s) {
+  if (a.n_slots == 0) return cudaSuccess;
+  if (bs != 128 && bs != 256 && bs != 512 && bs != 1024) bs = 256;
+  segsum_kernel<<<(unsigned)((a.n_slots + bs - 1) / bs), bs, 0, s>>>(a);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_mpc(const MpcArgs& a, cudaStream_t s) {
   if (a.n_mpc == 0) return cudaSuccess;

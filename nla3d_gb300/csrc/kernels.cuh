@@ -32,6 +32,10 @@ struct Solid81Args {
   // (mat_id, c0..c4, K) instead of mat_id / mc / kbulk
   const uint32_t* elem_mesh;
   const double* mesh_mat;
+  // optional slot-ordered output: contribution c of element e goes to
+  // contribK[kpos[e * 325 + c]] (contribF[fpos[e * 25 + c]]); nullptr = e * 325 + c
+  const uint32_t* kpos;
+  const uint32_t* fpos;
   double* contribK;         // [E * 325]
   double* contribF;         // [E * 25]
   ElementStatus* status;
@@ -78,6 +82,17 @@ struct LinearArgs {
   double* contribK;
   double* contribF;
   ElementStatus* status;
+  const uint32_t* kpos;  // optional slot-ordered output (as Solid81Args)
+  const uint32_t* fpos;
+};
+
+// Contiguous segmented sums: out[s] = sum of contrib[ptr[s] .. ptr[s+1]) in
+// ascending order, starting from 0.
+struct SegSumArgs {
+  uint64_t n_slots;
+  const uint32_t* ptr;
+  const double* contrib;
+  double* out;
 };
 
 // Launchers (return cudaError_t of the launch).
@@ -94,6 +109,7 @@ cudaError_t launch_solid81_shaped(const Solid81Args& a, bool mixed, Solid81Shape
                                   cudaStream_t s);
 int solid81_max_blocks_per_sm(bool mixed, int warps_per_block);
 cudaError_t launch_gather_bs(const GatherArgs& a, int block_size, cudaStream_t s);
+cudaError_t launch_segsum(const SegSumArgs& a, int block_size, cudaStream_t s);
 // kernel tables (constant memory) for the current device; call before any
 // stream capture
 cudaError_t prepare_device_tables();

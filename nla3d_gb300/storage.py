@@ -269,6 +269,16 @@ class FEStorage:
             self._check(rc)
         return c.value, f.value
 
+    def set_contrib_layout(self, layout):
+        self._check(self.lib.nla3d_set_contrib_layout(self.h, layout))
+
+    def autotune(self, reps=3):
+        chosen = np.zeros(4, np.int32)
+        ms = ctypes.c_float()
+        self._check(self.lib.nla3d_autotune(self.h, reps, _p(chosen), ctypes.byref(ms)))
+        return {"warps_per_block": int(chosen[0]), "blocks_per_sm": int(chosen[1]),
+                "gather_block": int(chosen[2]), "layout": int(chosen[3]), "ms": float(ms.value)}
+
     def set_timing(self, on=True):
         self._check(self.lib.nla3d_set_timing(self.h, 1 if on else 0))
 

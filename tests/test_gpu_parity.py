@@ -78,6 +78,29 @@ def test_run_to_run_bitwise_reproducible(precision):
             assert np.array_equal(x.view(np.uint64), y.view(np.uint64))
 
 
+@pytest.mark.parametrize("name,precision", [("cube4_nh_clamped", "fp64"),
+                                            ("cube4_nh_clamped", "mixed"),
+                                            ("bar_mpc_2x2x3", "fp64"),
+                                            ("tetra0_3x3x3", "fp64"),
+                                            ("quadth_5x4", "fp64")])
+def test_contribution_layouts_bitwise_equal(name, precision):
+    """Element-ordered and slot-ordered contributions sum each slot in the
+    same order, so K and F agree to the bit."""
+    mesh, u, p, extra, do_update = cases.FULL_CASES[name]()
+    out = []
+    for layout in (0, 1):
+        s = FEStorage(mesh, precision).initSolutionData()
+        s.set_contrib_layout(layout)
+        ne, ee = s.eq_numbers()
+        s.setU(mg.u_to_vector(ne, ee, u, p, s.n_total, extra))
+        if do_update:
+            s.updateResults()
+        s.assembleGlobalEqMatrices()
+        out.append([s.K(b).copy() for b in (1, 12, 2)] + [s.F().copy()])
+    for x, y in zip(*out):
+        assert np.array_equal(x.view(np.uint64), y.view(np.uint64))
+
+
 def test_fresh_state_and_stale_state_semantics():
     """assemble() before any updateResults() uses the Element::pre() state
     (C = I, S = 0); after updateResults(U1), a new U2 changes only the
