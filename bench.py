@@ -33,7 +33,20 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-FLOP_PER_ELEM = 69072          # FP64 structured algorithm, 8 Gauss points x 8634
+# FP64 flop per SOLID81 element of the algorithm the kernel runs (8 Gauss
+# points x 4402: kinematics 189, material + S + wDd 436, -wFS / w cof F 96,
+# tangent tensor A 513, h_a = A^T G_a 1080, F_u + K_up 288, K_uu 1800).  The
+# executed FP64 instruction counters of one ncu capture give the same figure
+# (2 DFMA + DMUL + DADD = 35,216 per element).  The Bh^T D Bh formulation
+# costs 69,072 (8 x 8634) for the same element.
+FLOP_PER_ELEM = 35216
+FLOP_PER_ELEM_BTDB = 69072
+# DRAM bytes per element of solid81_kernel<double> and of the K gather in one
+# ncu capture of a 40^3 block (64,000 elements, 9,675,406 K slots), used to
+# scale the traffic to the measured launch; the element kernel's writes are a
+# lower bound there (L2 still held part of them when the kernel ended).
+DRAM_BYTES_PER_ELEM_SOLID81 = (108.603392e6 + 123.602432e6) / 64000
+DRAM_BYTES_PER_ELEM_GATHER_K = (301.560064e6 + 62.591488e6) / 64000
 BYTES_PER_ELEM_ALGO = 2700     # compulsory HBM traffic per element (connectivity,
                                # X/U, p, slot map, K written once, F)
 METRIC = "SOLID81 assembly Melem/s"  # Newton iterations per load step (plain vs learned) in "newton"
@@ -452,16 +465,22 @@ def run_ours(args):
         "kernel_ms": {"element": elem_ms, "gather_K": float(kt[1]), "gather_F": float(kt[2]),
                       "mpc": float(kt[3]), "assemblies_averaged": int(kcount)},
         "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": fp64_peak / 1e12,
-                     "unit": "TFLOP/s", "frac": achieved / fp64_peak, "traffic": None,
+                     "unit": "TFLOP/s", "frac": achieved / fp64_peak,
+                     "traffic": DRAM_BYTES_PER_ELEM_SOLID81 * mesh.n_elems,
+                     "traffic_source": "ncu dram bytes of a 64,000-element launch, "
+                                       "scaled by elements",
                      "kernel": "solid81_kernel<double>",
                      "algorithmic": f"{FLOP_PER_ELEM} FP64 flop/element x {mesh.n_elems}",
+                     "btdb_equivalent_tflops": FLOP_PER_ELEM_BTDB * mesh.n_elems
+                     / (elem_ms * 1e-3) / 1e12,
                      "peak_source": "FP64 FMA throughput probe in this run "
                                     "(MEASURED_PEAKS.json has no FP64 figure)"},
         "roofline_gather": {"bound": "hbm", "achieved": gather_bytes / (gather_ms * 1e-3) / 1e9,
                             "peak": hbm, "unit": "GB/s",
                             "frac": (gather_bytes / (gather_ms * 1e-3) / 1e9 / hbm) if hbm else None,
-                            "traffic": None,
-                            "kernel": ("segsum_kernel" if layout else "gather_kernel") + " (K + F)",
+                            "traffic": DRAM_BYTES_PER_ELEM_GATHER_K * mesh.n_elems,
+                            "kernel": "gather_sorted_kernel<" + ("false" if layout else "true")
+                                      + "> (K + F)",
                             "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
         "cpu_baseline": cpu,
         "clocks": clk.summary(),

@@ -12,9 +12,16 @@
 //   Fu_a   += -w * (F S G_a)              ( = -w/2 B^T S,  SOLID81.cpp:73 )
 //   Kup_a  +=  w * (cof(F) G_a)           ( = w/2 B^T J C^-1, since J F C^-1 = cof F )
 //   Fp     += -(J - 1 - p/k) w ;  Kpp += -w / k
-// These are the reference's products with the structural zeros of B, B_NL
-// and Omega removed; they agree with the reference to rounding (the tests
-// bound the difference at 1e-12 relative).
+// Writing Bh out, both Kuu terms are one contraction with a symmetric 9x9
+// tensor per Gauss point:
+//   Kuu(a,i; b,k) += sum_{L,N} G_aL A[iL][kN] G_bN,
+//   A[iL][kN] = sum_{J,M} F_iJ wDd'[(JL)][(MN)] F_kM + delta_ik w S_LN,
+// so one Gauss point costs 45 entries of A (about 300 FMA), h_a[ik] = A^T G_a
+// per node (81 FMA) and 3 FMA per Kuu entry, instead of 6 + the geometric term
+// per entry and D Bh per node.  These are the reference's products with the
+// structural zeros of B, B_NL and Omega removed and the sums regrouped; they
+// agree with the reference to rounding (the tests bound the difference at
+// 1e-12 relative).
 #include <cmath>
 #include <cstdio>
 
@@ -37,17 +44,25 @@ template <typename TT>
 struct WarpSmem {
   double wP[9][32];    // per (element q, Gauss point g): -w F S
   double wCof[9][32];  //  w cof(F)
-  TT Ft[9][32];        //  F = I + O in the tangent type
-  TT wSt[6][32];       //  w S (Voigt xx xy xz yy yz zz) in the tangent type
-  TT wD[21][32];       //  w * 2 Dd, packed upper
-  TT Bh[18][32];       // per (element q, node a) of the current Gauss point: Bh[r*3+i]
-  TT DB[18][32];       // (w 2 Dd) Bh
-  TT SG[3][32];        // w S G_a
-  TT Ga[3][32];        // G_a
+  TT A[45][32];        //  symmetric 9x9 tangent tensor A[iL][kN], packed upper
+  TT H[27][32];        // per (element q, node a) at the current Gauss point:
+                       //  h_a[ik][N] = sum_L G_aL A[iL][kN], index (3i+k)*3+N
+  TT G[3][32];         //  G_a
 };
 
 __device__ __forceinline__ int sym6(int r, int s) {  // packed upper index, r <= s
   return 6 * r - ((r - 1) * r) / 2 + (s - r);
+}
+
+__device__ __forceinline__ int sym6u(int r, int s) { return r <= s ? sym6(r, s) : sym6(s, r); }
+
+__device__ __forceinline__ int sym9(int p, int c) {  // packed upper 9x9, any order
+  return p <= c ? 9 * p - ((p - 1) * p) / 2 + (c - p) : 9 * c - ((c - 1) * c) / 2 + (p - c);
+}
+
+// Voigt index of the symmetric pair (J, L): xx xy xz yy yz zz
+__device__ __forceinline__ int voigt(int J, int L) {
+  return J == L ? (J == 0 ? 0 : (J == 1 ? 3 : 5)) : (J + L == 1 ? 1 : (J + L == 2 ? 2 : 4));
 }
 
 __device__ __forceinline__ void flag_element(ElementStatus* st, uint32_t el1) {
@@ -168,18 +183,18 @@ __global__ void __launch_bounds__(WPB * 32)
   const int lane = threadIdx.x & 31;
 
   // Ownership of Kuu entries: lane owns x = lane + 32 m of the 4*300 entries
-  // of its warp's element quad.  Decode once: smem offsets of Bh[.][i, slot a]
-  // and DB[.][k, slot b].
+  // of its warp's element quad.  Decode once: smem offsets of H[ik][.][slot a]
+  // and G[.][slot b].
   for (int v = threadIdx.x; v < kOwned * 32; v += blockDim.x) {
     const int m = v / 32, l = v % 32;
     const int x = l + 32 * m;
     uint32_t word = 0xFFFFFFFFu;
     if (x < kEPW * kKuuPerElem) {
       const int q = x / kKuuPerElem, t = x - q * kKuuPerElem;
-      const uchar4 en = c_kuu_entry[t];
-      const uint32_t bh = en.y * 32 + q * 8 + en.x;
-      const uint32_t db = en.w * 32 + q * 8 + en.z;
-      word = bh | (db << 16);
+      const uchar4 en = c_kuu_entry[t];  // (a, i, b, k)
+      const uint32_t ho = (en.y * 3 + en.w) * 3 * 32 + q * 8 + en.x;
+      const uint32_t go = q * 8 + en.z;
+      word = ho | (go << 16);
     }
     dec[m * 32 + l] = word;
   }
@@ -279,12 +294,34 @@ __global__ void __launch_bounds__(WPB * 32)
                              F[0] * F[4] - F[1] * F[3]};
 #pragma unroll
       for (int c = 0; c < 9; c++) sm->wCof[c][lane] = w * cof[c];
+      // A[iL][kN] = sum_J F_iJ (sum_M wD[(JL)][(MN)] F_kM) + delta_ik w S_LN,
+      // one row (i, L) at a time
+      TT Fm[9], wS[6];
 #pragma unroll
-      for (int c = 0; c < 9; c++) sm->Ft[c][lane] = (TT)F[c];
+      for (int c = 0; c < 9; c++) Fm[c] = (TT)F[c];
 #pragma unroll
-      for (int c = 0; c < 6; c++) sm->wSt[c][lane] = (TT)(w * mo.S[c]);
+      for (int c = 0; c < 6; c++) wS[c] = (TT)(w * mo.S[c]);
 #pragma unroll
-      for (int c = 0; c < 21; c++) sm->wD[c][lane] = wD[c];
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int L = 0; L < 3; L++) {
+          TT T6[6];
+#pragma unroll
+          for (int t = 0; t < 6; t++)
+            T6[t] = Fm[3 * i + 0] * wD[sym6u(voigt(0, L), t)] +
+                    Fm[3 * i + 1] * wD[sym6u(voigt(1, L), t)] +
+                    Fm[3 * i + 2] * wD[sym6u(voigt(2, L), t)];
+#pragma unroll
+          for (int k = 0; k < 3; k++)
+#pragma unroll
+            for (int N = 0; N < 3; N++) {
+              if (3 * k + N < 3 * i + L) continue;
+              TT v = T6[voigt(0, N)] * Fm[3 * k + 0] + T6[voigt(1, N)] * Fm[3 * k + 1] +
+                     T6[voigt(2, N)] * Fm[3 * k + 2];
+              if (i == k) v += wS[voigt(L, N)];
+              sm->A[sym9(3 * i + L, 3 * k + N)][lane] = v;
+            }
+        }
       Fp_part = -(J - 1 - pc * inv_kb) * w;
       Kpp_part = -inv_kb * w;
       // J = sqrt(det C) cannot see an inverted element; det F can
@@ -322,62 +359,34 @@ __global__ void __launch_bounds__(WPB * 32)
           Kup[i] += sm->wCof[3 * i + 0][s1] * G0 + sm->wCof[3 * i + 1][s1] * G1 +
                     sm->wCof[3 * i + 2][s1] * G2;
         }
-        const TT g0 = (TT)G0, g1 = (TT)G1, g2 = (TT)G2;
-        TT Fm[9];
+        const TT gg[3] = {(TT)G0, (TT)G1, (TT)G2};
 #pragma unroll
-        for (int c = 0; c < 9; c++) Fm[c] = sm->Ft[c][s1];
-        TT Bh[18];
+        for (int i = 0; i < 3; i++)
 #pragma unroll
-        for (int i = 0; i < 3; i++) {
-          const TT f0 = Fm[3 * i + 0], f1 = Fm[3 * i + 1], f2 = Fm[3 * i + 2];
-          Bh[0 * 3 + i] = f0 * g0;
-          Bh[1 * 3 + i] = f1 * g0 + f0 * g1;
-          Bh[2 * 3 + i] = f2 * g0 + f0 * g2;
-          Bh[3 * 3 + i] = f1 * g1;
-          Bh[4 * 3 + i] = f2 * g1 + f1 * g2;
-          Bh[5 * 3 + i] = f2 * g2;
-        }
-        TT D[21];
+          for (int k = 0; k < 3; k++)
 #pragma unroll
-        for (int c = 0; c < 21; c++) D[c] = sm->wD[c][s1];
+            for (int N = 0; N < 3; N++)
+              sm->H[(3 * i + k) * 3 + N][lane] =
+                  gg[0] * sm->A[sym9(3 * i + 0, 3 * k + N)][s1] +
+                  gg[1] * sm->A[sym9(3 * i + 1, 3 * k + N)][s1] +
+                  gg[2] * sm->A[sym9(3 * i + 2, 3 * k + N)][s1];
 #pragma unroll
-        for (int r = 0; r < 6; r++)
-#pragma unroll
-          for (int k = 0; k < 3; k++) {
-            TT v = (TT)0;
-#pragma unroll
-            for (int s = 0; s < 6; s++) v += D[r <= s ? sym6(r, s) : sym6(s, r)] * Bh[s * 3 + k];
-            sm->DB[r * 3 + k][lane] = v;
-          }
-#pragma unroll
-        for (int c = 0; c < 18; c++) sm->Bh[c][lane] = Bh[c];
-        const TT sxx = sm->wSt[0][s1], sxy = sm->wSt[1][s1], sxz = sm->wSt[2][s1],
-                 syy = sm->wSt[3][s1], syz = sm->wSt[4][s1], szz = sm->wSt[5][s1];
-        sm->SG[0][lane] = sxx * g0 + sxy * g1 + sxz * g2;
-        sm->SG[1][lane] = sxy * g0 + syy * g1 + syz * g2;
-        sm->SG[2][lane] = sxz * g0 + syz * g1 + szz * g2;
-        sm->Ga[0][lane] = g0;
-        sm->Ga[1][lane] = g1;
-        sm->Ga[2][lane] = g2;
+        for (int c = 0; c < 3; c++) sm->G[c][lane] = gg[c];
       }
       __syncwarp();
       {
-        // phase 3: owned Kuu entries
-        const TT* Bf = &sm->Bh[0][0];
-        const TT* Df = &sm->DB[0][0];
+        // phase 3: owned Kuu entries, K(a,i; b,k) += h_a[ik] . G_b
+        const TT* Hf = &sm->H[0][0];
+        const TT* Gf = &sm->G[0][0];
 #pragma unroll
         for (int m = 0; m < kOwned; m++) {
           const uint32_t word = dec[m * 32 + lane];
           if (word != 0xFFFFFFFFu) {
-            const uint32_t bh = word & 0xFFFFu, db = word >> 16;
+            const uint32_t ho = word & 0xFFFFu, go = word >> 16;
             TT v = acc[m];
-#pragma unroll
-            for (int r = 0; r < 6; r++) v += Bf[bh + r * 96] * Df[db + r * 96];
-            if ((bh >> 5) == (db >> 5)) {
-              const uint32_t sa = bh & 31u, sb = db & 31u;
-              v += sm->Ga[0][sa] * sm->SG[0][sb] + sm->Ga[1][sa] * sm->SG[1][sb] +
-                   sm->Ga[2][sa] * sm->SG[2][sb];
-            }
+            v += Hf[ho] * Gf[go];
+            v += Hf[ho + 32] * Gf[go + 32];
+            v += Hf[ho + 64] * Gf[go + 64];
             acc[m] = v;
           }
         }
@@ -463,44 +472,97 @@ __global__ void solid81_jacobian_kernel(const JacobianArgs a) {
 
 // K[s] = sum of its contributions in ascending contribution order (the
 // reference's element-ascending accumulation order), starting from 0.
-// Up to kBatch loads of a slot are issued before the first add (a hexahedral
-// mesh has at most 8 contributions per K slot); the adds keep the ascending
-// order, so the sum is the same as the plain loop's.
+//
+// The sums are FP64 adds, and on this part the FP64 pipe is the scarce unit:
+// a warp pays for an add whenever any of its lanes needs one.  Slots have
+// 1..8 contributions (a hexahedral mesh: 8 on a node's own diagonal, 4/2/1
+// off it, 1 for every pressure coupling), so a warp of consecutive slots pays
+// for 8 adds where its slots need ~2.2 on average.  Each block therefore
+// first sorts its slots by contribution count (a counting sort in shared
+// memory; which thread sums a slot does not change the slot's sum), so the
+// warps see nearly uniform counts and stop adding at their own maximum.
+// Up to kBatch loads of a slot are issued before the first add; the adds keep
+// the ascending order, and 0 + c1 is taken as c1 with -0 turned into +0, so
+// the result is bitwise the plain sequential loop's.
 constexpr int kBatch = 8;
+constexpr int kCountClasses = kBatch + 2;  // counts 0..kBatch, and more than kBatch
+constexpr int kMaxGatherBlock = 1024;
 
-__global__ void gather_kernel(const GatherArgs a) {
-  const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= a.n_slots) return;
-  const uint32_t b = __ldg(a.ptr + s), e = __ldg(a.ptr + s + 1);
-  const uint32_t n = e - b;
-  uint32_t id[kBatch];
-#pragma unroll
-  for (int j = 0; j < kBatch; j++) id[j] = (uint32_t)j < n ? __ldg(a.ids + b + j) : 0u;
-  double x[kBatch];
-#pragma unroll
-  for (int j = 0; j < kBatch; j++) x[j] = (uint32_t)j < n ? __ldg(a.contrib + id[j]) : 0.0;
-  double v = 0.0;
-#pragma unroll
-  for (int j = 0; j < kBatch; j++)
-    if ((uint32_t)j < n) v += x[j];
-  for (uint32_t k = b + kBatch; k < e; k++) v += a.contrib[a.ids[k]];
-  a.out[s] = v;
+__device__ __forceinline__ double plus_zero_sum(double x) {
+  // 0.0 + x without an FP64 add: x, except -0.0 -> +0.0
+  const long long b = __double_as_longlong(x);
+  return __longlong_as_double(b == (long long)0x8000000000000000ull ? 0ll : b);
 }
 
-__global__ void segsum_kernel(const SegSumArgs a) {
-  const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= a.n_slots) return;
-  const uint32_t b = __ldg(a.ptr + s), e = __ldg(a.ptr + s + 1);
+template <bool kIds>
+__global__ void __launch_bounds__(kMaxGatherBlock)
+    gather_sorted_kernel(const uint64_t n_slots, const uint32_t* __restrict__ ptr,
+                         const uint32_t* __restrict__ ids, const double* __restrict__ contrib,
+                         double* __restrict__ out) {
+  __shared__ uint32_t s_beg[kMaxGatherBlock];
+  __shared__ uint32_t s_end[kMaxGatherBlock];
+  __shared__ uint16_t s_slot[kMaxGatherBlock];
+  __shared__ uint32_t s_wcnt[kMaxGatherBlock / 32][kCountClasses];
+  __shared__ uint32_t s_total[kCountClasses];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int n_warps = blockDim.x >> 5;
+  const uint64_t base = (uint64_t)blockIdx.x * blockDim.x;
+  const uint64_t s = base + tid;
+  uint32_t b = 0, e = 0;
+  if (s < n_slots) {
+    b = __ldg(ptr + s);
+    e = __ldg(ptr + s + 1);
+  }
+  s_beg[tid] = b;
+  s_end[tid] = e;
   const uint32_t n = e - b;
+  const int cls = n > (uint32_t)kBatch ? kBatch + 1 : (int)n;
+  // rank within (warp, class), and per-warp class counts
+  uint32_t rank = 0;
+#pragma unroll
+  for (int c = 0; c < kCountClasses; c++) {
+    const unsigned m = __ballot_sync(0xFFFFFFFFu, cls == c);
+    if (cls == c) rank = __popc(m & ((1u << lane) - 1u));
+    if (lane == 0) s_wcnt[warp][c] = __popc(m);
+  }
+  __syncthreads();
+  // exclusive prefix over warps, per class (one thread per class)
+  if (tid < kCountClasses) {
+    uint32_t run = 0;
+    for (int w = 0; w < n_warps; w++) {
+      const uint32_t t = s_wcnt[w][tid];
+      s_wcnt[w][tid] = run;
+      run += t;
+    }
+    s_total[tid] = run;
+  }
+  __syncthreads();
+  uint32_t pos = s_wcnt[warp][cls] + rank;
+  for (int c = 0; c < cls; c++) pos += s_total[c];
+  s_slot[pos] = (uint16_t)tid;
+  __syncthreads();
+
+  const int lt = s_slot[tid];
+  const uint64_t slot = base + lt;
+  const uint32_t sb = s_beg[lt], se = s_end[lt];
+  const uint32_t sn = se - sb;
+  unsigned nmax = __reduce_max_sync(0xFFFFFFFFu, slot < n_slots ? sn : 0u);
+  if (slot >= n_slots) return;
   double x[kBatch];
 #pragma unroll
-  for (int j = 0; j < kBatch; j++) x[j] = (uint32_t)j < n ? __ldg(a.contrib + b + j) : 0.0;
-  double v = 0.0;
+  for (int j = 0; j < kBatch; j++) {
+    x[j] = 0.0;
+    if ((uint32_t)j < sn) x[j] = kIds ? __ldg(contrib + __ldg(ids + sb + j)) : __ldg(contrib + sb + j);
+  }
+  double v = plus_zero_sum(x[0]);
 #pragma unroll
-  for (int j = 0; j < kBatch; j++)
-    if ((uint32_t)j < n) v += x[j];
-  for (uint32_t k = b + kBatch; k < e; k++) v += a.contrib[k];
-  a.out[s] = v;
+  for (int j = 1; j < kBatch; j++) {
+    if ((unsigned)j >= nmax) break;  // warp-uniform
+    const double t = v + x[j];
+    v = (uint32_t)j < sn ? t : v;
+  }
+  for (uint32_t k = sb + kBatch; k < se; k++) v += kIds ? contrib[ids[k]] : contrib[k];
+  out[slot] = v;
 }
 
 // Rigid-body MPC rows (RigidBodyMpc::update, Mpc.cpp:70-164, and
@@ -855,7 +917,8 @@ cudaError_t probe_fma_peak(bool fp64, double* flops) {
 cudaError_t launch_gather_bs(const GatherArgs& a, int bs, cudaStream_t s) {
   if (a.n_slots == 0) return cudaSuccess;
   if (bs != 128 && bs != 256 && bs != 512 && bs != 1024) bs = 256;
-  gather_kernel<<<(unsigned)((a.n_slots + bs - 1) / bs), bs, 0, s>>>(a);
+  gather_sorted_kernel<true><<<(unsigned)((a.n_slots + bs - 1) / bs), bs, 0, s>>>(
+      a.n_slots, a.ptr, a.ids, a.contrib, a.out);
   return cudaGetLastError();
 }
 
@@ -864,7 +927,8 @@ cudaError_t launch_gather(const GatherArgs& a, cudaStream_t s) { return launch_g
 cudaError_t launch_segsum(const SegSumArgs& a, int bs, cudaStream_t s) {
   if (a.n_slots == 0) return cudaSuccess;
   if (bs != 128 && bs != 256 && bs != 512 && bs != 1024) bs = 256;
-  segsum_kernel<<<(unsigned)((a.n_slots + bs - 1) / bs), bs, 0, s>>>(a);
+  gather_sorted_kernel<false><<<(unsigned)((a.n_slots + bs - 1) / bs), bs, 0, s>>>(
+      a.n_slots, a.ptr, nullptr, a.contrib, a.out);
   return cudaGetLastError();
 }
 
