@@ -78,14 +78,17 @@ def workload(n):
     return mesh, u, p
 
 
-def workload_config(mesh, extra=None):
+def workload_config(mesh=None, extra=None, n=None):
+    """Config of the n^3 workload (from the mesh, or from n alone)."""
+    if mesh is not None:
+        n = round(mesh.n_elems ** (1 / 3))
     cfg = {
-        "workload": f"SOLID81 u/p hex block {round(mesh.n_elems ** (1 / 3))}^3 on the unit cube, "
+        "workload": f"SOLID81 u/p hex block {n}^3 on the unit cube, "
                     "Mooney-Rivlin C10=0.4 C01=0.1 K=2000, 30deg twist + 1.5 stretch, "
                     "+-0.005h noise, p~N(0,0.1); step = updateResults + "
                     "assembleGlobalEqMatrices",
-        "elements": mesh.n_elems,
-        "nodes": mesh.n_nodes,
+        "elements": n ** 3,
+        "nodes": (n + 1) ** 3,
         "l2": "no flush: inputs larger than L2 (element contributions 2.6 GB, gather lists "
               "1.9 GB, K 1.2 GB per step at 1e6 elements)",
     }
@@ -172,14 +175,15 @@ def run_reference(args):
     ne = steps[0][0]
     t = statistics.median(s[1] for s in steps)
     value = ne / t / 1e6
-    mesh = workload(n)[0]
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "impl": "reference",
-        "config": workload_config(mesh, {"note": f"{cores} independent {n}^3 samples, one per "
-                                                 "host core (the reference is single-threaded)"}),
+        "config": workload_config(None, {"sample": f"each step: {cores} independent {n}^3 "
+                                                   "blocks of the same workload, one per host "
+                                                   "core (the reference is single-threaded)",
+                                         "precision": "fp64"}, n=args.n),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"{cores} processes x {n}^3 = {ne // cores} SOLID81 elements, "
                                    "one updateResults+assemble each per step; "

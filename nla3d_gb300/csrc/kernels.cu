@@ -518,13 +518,11 @@ __global__ void __launch_bounds__(kMaxGatherBlock)
   const uint32_t n = e - b;
   const int cls = n > (uint32_t)kBatch ? kBatch + 1 : (int)n;
   // rank within (warp, class), and per-warp class counts
-  uint32_t rank = 0;
-#pragma unroll
-  for (int c = 0; c < kCountClasses; c++) {
-    const unsigned m = __ballot_sync(0xFFFFFFFFu, cls == c);
-    if (cls == c) rank = __popc(m & ((1u << lane) - 1u));
-    if (lane == 0) s_wcnt[warp][c] = __popc(m);
-  }
+  if (lane < kCountClasses) s_wcnt[warp][lane] = 0;
+  __syncwarp();
+  const unsigned same = __match_any_sync(0xFFFFFFFFu, cls);
+  const uint32_t rank = __popc(same & ((1u << lane) - 1u));
+  if (rank == 0) s_wcnt[warp][cls] = __popc(same);
   __syncthreads();
   // exclusive prefix over warps, per class (one thread per class)
   if (tid < kCountClasses) {
