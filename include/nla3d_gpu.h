@@ -172,6 +172,26 @@ int nla3d_get_K(nla3d_ctx* ctx, int block, double* values);
 int nla3d_get_F(nla3d_ctx* ctx, double* F);
 /* All K values of the context (every mesh: block(1) | block(1,2) | block(2)). */
 int nla3d_get_K_all(nla3d_ctx* ctx, double* values);
+/* y += coef * op(K block) x on the device, with the values of the last
+ * nla3d_assemble of mesh `mesh` (0 for a single-mesh context), on the
+ * context's stream (asynchronous, like nla3d_assemble).  Replaces the
+ * reference's sparse products of the Newton iteration (FESolver.cpp:454-466):
+ *   block 1 or 2: matBVprod(SparseSymMatrix&, dVec, coef, dVec&)
+ *       (SparseMatrix.cpp:497-519): both triangles of the symmetric block,
+ *       entries x_j with |x_j| <= 1e-20 skipped as there; trans is ignored;
+ *   block 12, trans 0: matBVprod(SparseMatrix&, ...)  (SparseMatrix.cpp:522-540);
+ *   block 12, trans 1: matBTVprod(SparseMatrix&, ...) (SparseMatrix.cpp:542-558).
+ * Each y entry is accumulated in the reference's order with (K x) coef
+ * rounded before the add, so y is the reference's result bit for bit (the
+ * reference's symmetric product also adds +-0 for structural zeros, which
+ * can only change the sign of a zero result).  x, y: device arrays of the
+ * block's column / row count (transposed for trans 1); a block without stored
+ * entries leaves y unchanged and reads neither pointer.  The first call per
+ * (mesh, block, trans) builds its walk list (about 8 bytes per stored entry,
+ * twice that for a symmetric block) and synchronises the stream once. */
+int nla3d_block_mv(nla3d_ctx* ctx, uint32_t mesh, int block, int trans, const double* x,
+                   double coef, double* y);
+
 /* Device pointers (valid until nla3d_destroy): K values of one block (block 0
  * = all K values of the context), F. */
 int nla3d_device_K(const nla3d_ctx* ctx, int block, double** values, uint64_t* n);

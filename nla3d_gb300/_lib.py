@@ -33,6 +33,7 @@ EXPORTS = [
     "nla3d_set_launch_shape", "nla3d_autotune", "nla3d_graph_capture", "nla3d_graph_launch",
     "nla3d_mlp_gemm", "nla3d_mlp_tanh_backward", "nla3d_mlp_column_sum", "nla3d_mlp_adam",
     "nla3d_mlp_to_bf16", "nla3d_mlp_mse_grad", "nla3d_set_contrib_layout",
+    "nla3d_block_mv",
 ]
 
 NOALLOC_MAX_ELEMS = 15252
@@ -136,6 +137,8 @@ def load(path: str = LIB_PATH):
         "nla3d_set_launch_shape": ([P, ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
         "nla3d_autotune": ([P, ctypes.c_int, P, ctypes.POINTER(ctypes.c_float)], ctypes.c_int),
         "nla3d_set_contrib_layout": ([P, ctypes.c_int], ctypes.c_int),
+        "nla3d_block_mv": ([P, ctypes.c_uint32, ctypes.c_int, ctypes.c_int, P, ctypes.c_double, P],
+                           ctypes.c_int),
         "nla3d_graph_capture": ([P], ctypes.c_int),
         "nla3d_graph_launch": ([P], ctypes.c_int),
         "nla3d_mlp_gemm": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, P, ctypes.c_int, I64, I64, P,

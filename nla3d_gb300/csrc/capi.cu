@@ -83,6 +83,16 @@ struct nla3d_ctx {
   int32_t* d_mpc_dof = nullptr;
   ElementStatus* d_status = nullptr;
   std::vector<void*> allocs;
+  // walk lists of the sparse block products, built on first use:
+  // per mesh, (block 1) (block 2) (block 1,2) (block 1,2 transposed)
+  struct MvList {
+    bool built = false;
+    uint64_t n_out = 0, n_entries = 0;
+    uint32_t* ptr = nullptr;
+    uint32_t* slot = nullptr;
+    uint32_t* xi = nullptr;
+  };
+  std::vector<std::vector<MvList>> mv;
   // launch shape (nla3d_autotune / nla3d_set_launch_shape)
   Solid81Shape shape;
   int gather_bs = 256;
@@ -130,6 +140,54 @@ cudaError_t upload(nla3d_ctx* c, T** p, const T* host, uint64_t n) {
 }
 
 int block_slot(int block) { return block == 1 ? 0 : (block == 2 ? 2 : (block == 12 ? 1 : -1)); }
+
+// Walk lists of y += coef * op(B) x in the reference's order (SparseMatrix.cpp:497-558):
+//   kind 0/1 (symmetric block 1/2, matBVprod(SparseSymMatrix&)): output row i
+//     visits B(j,i) for j <= i ascending (column i of the stored upper
+//     triangle, diagonal last), then B(i,j) for j > i ascending;
+//   kind 2 (block 1,2, matBVprod(SparseMatrix&)): row i's entries in order;
+//   kind 3 (block 1,2, matBTVprod): output column j visits rows i ascending.
+// slot = value index within the block, xi = 0-based index into x.
+void build_walk(const CsrBlock& b, int kind, std::vector<uint32_t>& ptr,
+                std::vector<uint32_t>& slot, std::vector<uint32_t>& xi) {
+  const bool sym = kind <= 1, trans = kind == 3;
+  const uint32_t n_out = trans ? b.cols : b.rows;
+  std::vector<uint32_t> cnt(n_out, 0);
+  for (uint32_t r = 0; r < b.rows; r++)
+    for (uint32_t k = b.iofeir[r] - 1; k < b.iofeir[r + 1] - 1; k++) {
+      const uint32_t c = b.columns[k] - 1;
+      if (sym) {
+        cnt[c]++;
+        if (c > r) cnt[r]++;
+      } else {
+        cnt[trans ? c : r]++;
+      }
+    }
+  ptr.assign(n_out + 1, 0);
+  for (uint32_t i = 0; i < n_out; i++) ptr[i + 1] = ptr[i] + cnt[i];
+  slot.assign(ptr[n_out], 0);
+  xi.assign(ptr[n_out], 0);
+  std::vector<uint32_t> pos(ptr.begin(), ptr.end() - 1);
+  auto put = [&](uint32_t out, uint32_t k, uint32_t x) {
+    slot[pos[out]] = k;
+    xi[pos[out]] = x;
+    pos[out]++;
+  };
+  for (uint32_t r = 0; r < b.rows; r++)
+    for (uint32_t k = b.iofeir[r] - 1; k < b.iofeir[r + 1] - 1; k++) {
+      const uint32_t c = b.columns[k] - 1;
+      if (sym) {
+        // rows are visited in ascending order, so column c's lower part is
+        // complete (diagonal last) before row c appends its upper part
+        put(c, k, r);
+        if (c > r) put(r, k, c);
+      } else if (trans) {
+        put(c, k, r);
+      } else {
+        put(r, k, c);
+      }
+    }
+}
 
 int check_mesh(const nla3d_mesh_desc* mesh) {
   if (!mesh || (mesh->n_elems && (!mesh->conn || !mesh->xyz))) return NLA3D_ERR_ARG;
@@ -681,6 +739,37 @@ int nla3d_get_F(nla3d_ctx* c, double* F) {
                                   c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   return e == cudaSuccess ? NLA3D_OK : cuda_fail(c, e, "get_F");
+}
+
+int nla3d_block_mv(nla3d_ctx* c, uint32_t mesh, int block, int trans, const double* x,
+                   double coef, double* y) {
+  const int b = block_slot(block);
+  if (!c || !c->ready || !valid_mesh(c, mesh) || b < 0 || (trans != 0 && trans != 1))
+    return fail(c, NLA3D_ERR_ARG, "block_mv");
+  const int kind = block == 1 ? 0 : (block == 2 ? 1 : (trans ? 3 : 2));
+  if (c->mv.size() != c->hm.size()) c->mv.assign(c->hm.size(), std::vector<nla3d_ctx::MvList>(4));
+  nla3d_ctx::MvList& L = c->mv[mesh][kind];
+  const CsrBlock& blk = c->hm[mesh].blk[b];
+  if (!L.built) {
+    std::vector<uint32_t> ptr, slot, xi;
+    build_walk(blk, kind, ptr, slot, xi);
+    cudaError_t e = upload(c, &L.ptr, ptr.data(), ptr.size());
+    if (e == cudaSuccess) e = upload(c, &L.slot, slot.data(), slot.size());
+    if (e == cudaSuccess) e = upload(c, &L.xi, xi.data(), xi.size());
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "block_mv lists");
+    L.n_out = ptr.size() - 1;
+    L.n_entries = ptr.back();
+    L.built = true;
+  }
+  if (L.n_entries == 0) return NLA3D_OK;  // y unchanged (no stored entries)
+  if (!x || !y) return fail(c, NLA3D_ERR_ARG, "block_mv: null vector");
+  BlockMvArgs a{L.n_out, L.ptr, L.slot, L.xi, c->d_K + c->k_off[mesh] + c->hm[mesh].val_off[b],
+                x, coef, y, kind <= 1 ? 1 : 0};
+  cudaError_t e = launch_block_mv(a, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "block_mv");
+  c->launches++;
+  return NLA3D_OK;
 }
 
 int nla3d_device_K(const nla3d_ctx* c, int block, double** values, uint64_t* n) {

@@ -563,6 +563,25 @@ __global__ void __launch_bounds__(kMaxGatherBlock)
   out[slot] = v;
 }
 
+// Sparse block products of the Newton iteration (FESolver.cpp:454-466):
+// one thread per output entry walks its precomputed list in the reference's
+// order; explicit _rn operations keep (K x) coef and the running sum from
+// being fused, so each entry is the reference's value bit for bit (structural
+// zeros, which the reference's symmetric product also visits, add +-0 there
+// and are not visited here).
+__global__ void block_mv_kernel(const BlockMvArgs a) {
+  const uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= a.n_out) return;
+  double acc = a.y[r];
+  const uint32_t e = __ldg(a.ptr + r + 1);
+  for (uint32_t k = __ldg(a.ptr + r); k < e; k++) {
+    const double xv = a.x[__ldg(a.xi + k)];
+    if (a.sym && !(fabs(xv) > 1e-20)) continue;
+    acc = __dadd_rn(acc, __dmul_rn(__dmul_rn(__ldg(a.K + __ldg(a.slot + k)), xv), a.coef));
+  }
+  a.y[r] = acc;
+}
+
 // Rigid-body MPC rows (RigidBodyMpc::update, Mpc.cpp:70-164, and
 // FEStorage.cpp:51-61): one thread per MPC equation.
 __global__ void mpc_kernel(const MpcArgs a) {
@@ -927,6 +946,13 @@ cudaError_t launch_segsum(const SegSumArgs& a, int bs, cudaStream_t s) {
   if (bs != 128 && bs != 256 && bs != 512 && bs != 1024) bs = 256;
   gather_sorted_kernel<false><<<(unsigned)((a.n_slots + bs - 1) / bs), bs, 0, s>>>(
       a.n_slots, a.ptr, nullptr, a.contrib, a.out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_block_mv(const BlockMvArgs& a, cudaStream_t s) {
+  if (a.n_out == 0) return cudaSuccess;
+  const int bs = 128;
+  block_mv_kernel<<<(unsigned)((a.n_out + bs - 1) / bs), bs, 0, s>>>(a);
   return cudaGetLastError();
 }
 

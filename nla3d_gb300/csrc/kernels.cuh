@@ -95,6 +95,21 @@ struct SegSumArgs {
   double* out;
 };
 
+// y[r] += sum over the walk list of r of (K[slot] * x[xi]) * coef, in list
+// order (the reference's matBVprod / matBTVprod order, SparseMatrix.cpp:497-558);
+// sym: skip |x| <= 1e-20 as the symmetric product does.
+struct BlockMvArgs {
+  uint64_t n_out;
+  const uint32_t* ptr;   // n_out + 1
+  const uint32_t* slot;  // value index within the block
+  const uint32_t* xi;    // index into x
+  const double* K;       // the block's values
+  const double* x;
+  double coef;
+  double* y;
+  int sym;
+};
+
 // Launchers (return cudaError_t of the launch).
 cudaError_t launch_solid81_jacobian(const JacobianArgs& a, cudaStream_t s);
 cudaError_t launch_solid81(const Solid81Args& a, bool mixed, int blocks_per_sm_hint,
@@ -115,6 +130,7 @@ cudaError_t launch_segsum(const SegSumArgs& a, int block_size, cudaStream_t s);
 cudaError_t prepare_device_tables();
 cudaError_t launch_gather(const GatherArgs& a, cudaStream_t s);
 cudaError_t launch_mpc(const MpcArgs& a, cudaStream_t s);
+cudaError_t launch_block_mv(const BlockMvArgs& a, cudaStream_t s);
 cudaError_t launch_linear(const LinearArgs& a, cudaStream_t s);
 size_t solid81_smem_bytes(bool mixed);
 cudaError_t probe_fma_peak(bool fp64, double* flops);

@@ -75,8 +75,11 @@ class StepRecord:
 
 class NewtonSolver:
     """backend: an object with eq_numbers(), pattern(b), K(b), F(), set_U(U),
-    update(), assemble(), n_con, n_unk, n_mpc, n_total, blocks -- the GPU
-    FEStorage (nla3d_gb300.storage) or the CPU oracle model."""
+    update(), assemble(), block_mv(block, trans, x, coef, y), n_con, n_unk,
+    n_mpc, n_total, blocks -- the GPU FEStorage (nla3d_gb300.storage, whose
+    block_mv runs nla3d_block_mv on the device K) or the CPU oracle model.
+    The right-hand side, residual and reactions go through block_mv (the
+    reference's matBVprod / matBTVprod); only the solve reads K(2) on the host."""
 
     def __init__(self, backend, fixes, n_loadsteps=10, n_iterations=15, kinematic_tol=1e-3,
                  residual_tol=None, loads=()):
@@ -102,14 +105,26 @@ class NewtonSolver:
         self.reactions: list[np.ndarray] = [np.zeros(self.nc)]
 
     # ---- the global system ----
-    def _matrices(self):
-        rows1, cols1, _ = self.b.blocks[1]
-        rows12, cols12, _ = self.b.blocks[12]
+    def _K2(self):
         rows2, cols2, _ = self.b.blocks[2]
-        K1 = csr_full(*self.patterns[1], self.b.K(1), rows1, cols1, True)
-        K12 = csr_full(*self.patterns[12], self.b.K(12), rows12, cols12, False)
-        K2 = csr_full(*self.patterns[2], self.b.K(2), rows2, cols2, True)
-        return K1, K12, K2
+        return csr_full(*self.patterns[2], self.b.K(2), rows2, cols2, True)
+
+    def _rhs(self, F, dUc):
+        """FESolver.cpp:449-454: rhs = F_sl + R_sl - K(1,2)^T dUc, the last
+        term through the backend's matBTVprod."""
+        y = F[self.nc:] + self.R[self.nc:]
+        if self.nc == 0:
+            return y
+        return self.b.block_mv(12, 1, dUc, -1.0, y)
+
+    def _reactions(self, F, dUc, dUsl):
+        """FESolver.cpp:463-466: R_c = K(1) dUc + K(1,2) dUsl - F_c (matBVprod)."""
+        Rc = np.zeros(self.nc)
+        if self.nc == 0:
+            return Rc
+        Rc = self.b.block_mv(1, 0, dUc, 1.0, Rc)
+        Rc = self.b.block_mv(12, 0, dUsl, 1.0, Rc)
+        return Rc - F[: self.nc]
 
     def _apply_bc(self, t):
         """FESolver::applyBoundaryConditions (FESolver.cpp:229-247)."""
@@ -125,14 +140,17 @@ class NewtonSolver:
         self.b.assemble()
         return self.b.F()
 
-    def residual(self, F, K12, K2, dUc):
+    def residual(self, F, dUc):
         """Equilibrium residual of the unknown + MPC rows.  The reference solves
         the Lagrange multipliers as totals (vecUl = deltaUl, FESolver.cpp:461),
         so its right-hand side F_sl + R_sl - K12^T dUc still contains the
         constraint forces; the residual removes them: r = rhs - K2 [0; U_l]."""
+        r = self._rhs(F, dUc)
+        if self.nm == 0:
+            return r
         lam = np.zeros(self.nu + self.nm)
         lam[self.nu:] = self.U[self.nc + self.nu:]
-        return F[self.nc:] + self.R[self.nc:] - K12.T @ dUc - K2 @ lam
+        return self.b.block_mv(2, 0, lam, -1.0, r)
 
     # ---- the load-step loop ----
     def solve(self, predictor=None, on_converged=None):
@@ -151,8 +169,7 @@ class NewtonSolver:
                 if prop is not None:
                     # residual of the plain start: F(U_prev) - K12^T dUc (linearised)
                     F0 = self._assemble(self.U)
-                    _, K12, K2 = self._matrices()
-                    r_plain = self.residual(F0, K12, K2, Uc_new - Ucprev)
+                    r_plain = self.residual(F0, Uc_new - Ucprev)
                     Up = prop.copy()
                     Up[: self.nc] = Uc_new
                     Uold = self.U
@@ -160,8 +177,7 @@ class NewtonSolver:
                     self.b.set_U(Up)
                     self.b.update()
                     Fp = self._assemble(Up)
-                    _, K12p, K2p = self._matrices()
-                    r_pred = float(np.linalg.norm(self.residual(Fp, K12p, K2p, 0.0 * Uc_new)))
+                    r_pred = float(np.linalg.norm(self.residual(Fp, 0.0 * Uc_new)))
                     self.U = Uold
                     rec.prediction_residual, rec.plain_residual = r_pred, float(np.linalg.norm(r_plain))
                     if np.isfinite(r_pred) and r_pred < rec.plain_residual:
@@ -177,25 +193,23 @@ class NewtonSolver:
                 F = self._assemble(self.U)
                 Uc = self._apply_bc(t)
                 dUc = Uc - Ucprev
-                K1, K12, K2 = self._matrices()
-                rhs = F[self.nc:] + self.R[self.nc:] - K12.T @ dUc
-                rnorm = float(np.linalg.norm(self.residual(F, K12, K2, dUc)))
+                rhs = self._rhs(F, dUc)
+                rnorm = float(np.linalg.norm(self.residual(F, dUc)))
                 rec.residuals.append(rnorm)
                 if self.residual_tol is not None and tc.eq_step > 1 and rnorm < self.residual_tol \
                         and not np.any(dUc):
                     # converged without a further solve: reactions for a zero increment
                     sl = np.zeros(self.nu + self.nm)
                     sl[self.nu:] = self.U[self.nc + self.nu:]
-                    self.R[: self.nc] = K12 @ sl - F[: self.nc]
+                    self.R[: self.nc] = self._reactions(F, np.zeros(self.nc), sl)
                     rec.iterations = tc.eq_step - 1
                     converged = True
                     break
-                dUsl = spla.spsolve(K2.tocsc(), rhs, permc_spec="MMD_AT_PLUS_A")
+                dUsl = spla.spsolve(self._K2().tocsc(), rhs, permc_spec="MMD_AT_PLUS_A")
                 self.U[: self.nc] = Uc
                 self.U[self.nc: self.nc + self.nu] += dUsl[: self.nu]
                 self.U[self.nc + self.nu:] = dUsl[self.nu:]
-                Rc = K1 @ dUc + K12 @ dUsl - F[: self.nc]
-                self.R[: self.nc] = Rc
+                self.R[: self.nc] = self._reactions(F, dUc, dUsl)
                 Ucprev = Uc.copy()
                 self.b.set_U(self.U)
                 self.b.update()

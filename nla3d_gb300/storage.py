@@ -249,6 +249,25 @@ class FEStorage:
     def getF(self):
         return self.F()
 
+    def block_mv_device(self, block, trans, x_ptr, coef, y_ptr, mesh=0):
+        """y += coef * op(block) x on device arrays (nla3d_block_mv): the
+        reference's matBVprod / matBTVprod on this context's K, asynchronous
+        on the context's stream."""
+        self._check(self.lib.nla3d_block_mv(self.h, mesh, block, int(trans),
+                                            ctypes.c_void_p(x_ptr), float(coef),
+                                            ctypes.c_void_p(y_ptr)))
+
+    def block_mv(self, block, trans, x, coef, y):
+        """Host-array form of block_mv_device: copies x and y to the device
+        (PyTorch allocations), runs the product, returns the new y."""
+        import torch
+        xd = torch.from_numpy(np.ascontiguousarray(x, dtype=np.float64)).cuda()
+        yd = torch.from_numpy(np.array(y, dtype=np.float64, copy=True)).cuda()
+        torch.cuda.synchronize()
+        self.block_mv_device(block, trans, xd.data_ptr(), coef, yd.data_ptr())
+        self.synchronize()
+        return yd.cpu().numpy()
+
     def device_K(self, block):
         p = ctypes.c_void_p()
         n = ctypes.c_uint64()

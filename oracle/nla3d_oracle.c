@@ -1268,6 +1268,39 @@ int orc_get_K(orc_model* m, int block, double* values) {
   return 0;
 }
 
+/* SparseSymMatrix::value (SparseMatrix.cpp:484-494): 0 for a structural zero */
+static double blk_value(const csr_block* b, uint32_t i, uint32_t j) {
+  const uint32_t k = blk_index(b, i, j);
+  return k == INVALID ? 0.0 : b->values[k];
+}
+
+/* matBVprod(SparseSymMatrix&) SparseMatrix.cpp:497-519, matBVprod(SparseMatrix&)
+ * :522-540, matBTVprod(SparseMatrix&) :542-558 */
+int orc_block_mv(orc_model* m, int block, int trans, const double* x, double coef, double* y) {
+  const csr_block* b = &m->blk[slot_of(block)];
+  const double eps = 1e-20;
+  if (block == 1 || block == 2) {
+    for (uint32_t i = 1; i <= b->rows; i++) {
+      for (uint32_t j = 1; j <= i; j++)
+        if (fabs(x[j - 1]) > eps) y[i - 1] += blk_value(b, j, i) * x[j - 1] * coef;
+      for (uint32_t j = i + 1; j <= b->rows; j++)
+        if (fabs(x[j - 1]) > eps) y[i - 1] += blk_value(b, i, j) * x[j - 1] * coef;
+    }
+    return 0;
+  }
+  for (uint32_t i = 1; i <= b->rows; i++) {
+    if (b->iofeir[i] - b->iofeir[i - 1] == 0) continue;
+    const uint32_t st = b->iofeir[i - 1] - 1, en = b->iofeir[i] - 2;
+    for (uint32_t j = st; j <= en; j++) {
+      if (trans)
+        y[b->columns[j] - 1] += b->values[j] * x[i - 1] * coef;
+      else
+        y[i - 1] += b->values[j] * x[b->columns[j] - 1] * coef;
+    }
+  }
+  return 0;
+}
+
 int orc_get_F(orc_model* m, double* F) {
   memcpy(F, m->F, sizeof(double) * (m->n_dofs + m->n_mpc));
   return 0;

@@ -46,6 +46,11 @@ int orc_update(orc_model* m);
 int orc_assemble(orc_model* m);
 int orc_get_K(orc_model* m, int block, double* values);
 int orc_get_F(orc_model* m, double* F);
+/* y += coef * op(block) x on the assembled K (SparseMatrix.cpp:497-558):
+ * block 1 / 2: matBVprod(SparseSymMatrix&) (both triangles, x_j with
+ * |x_j| <= 1e-20 skipped); block 12: trans 0 matBVprod(SparseMatrix&),
+ * trans 1 matBTVprod(SparseMatrix&). */
+int orc_block_mv(orc_model* m, int block, int trans, const double* x, double coef, double* y);
 
 /* Element-level pieces (for tests against the reference's own fixtures). */
 void orc_hex_jacobian(const double* X /*8x3*/, int int_order, double* NiXj /*np x 8 x 3*/,

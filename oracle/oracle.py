@@ -82,6 +82,12 @@ def _load(kind: str):
         f("update").argtypes = [_P, _P]
         f("assemble").argtypes = [_P, _P]
     f("get_K").argtypes = [_P, ctypes.c_int, _P]
+    if kind == "port":
+        f("block_mv").argtypes = [_P, ctypes.c_int, ctypes.c_int, _P, ctypes.c_double, _P]
+    else:
+        f("block_mv").argtypes = [_P, ctypes.c_int, ctypes.c_int, _P, ctypes.c_uint,
+                                  ctypes.c_double, _P, ctypes.c_uint]
+    f("block_mv").restype = ctypes.c_int
     f("get_F").argtypes = [_P, _P]
     for n in ("add_fix", "add_rigid_body", "setup", "pattern", "eq_numbers", "set_U", "update",
               "assemble", "get_K", "get_F"):
@@ -212,6 +218,18 @@ class OracleModel:
         v = np.zeros(self.n_total)
         self._check(self._f("get_F")(self.h, _ptr(v)))
         return v
+
+    def block_mv(self, block, trans, x, coef, y):
+        """y + coef * op(block) x through the model's own sparse products
+        (matBVprod / matBTVprod, SparseMatrix.cpp:497-558); returns a new y."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        out = np.array(y, dtype=np.float64, copy=True)
+        if self.kind == "port":
+            self._check(self._f("block_mv")(self.h, block, int(trans), _ptr(x), coef, _ptr(out)))
+        else:
+            self._check(self._f("block_mv")(self.h, block, int(trans), _ptr(x), x.size, coef,
+                                            _ptr(out), out.size))
+        return out
 
 
 def solve_state(mesh, u, p, kind="port", extra=None, max_in_row=100):

@@ -242,6 +242,27 @@ int ref_get_K(void* h, int block, double* values) {
   });
 }
 
+// y += coef * op(block) x with the reference's own sparse products
+// (SparseMatrix.cpp:497-558): block 1 / 2 matBVprod(SparseSymMatrix&),
+// block 12 trans 0 matBVprod(SparseMatrix&), trans 1 matBTVprod(SparseMatrix&).
+int ref_block_mv(void* h, int block, int trans, const double* x, unsigned nx, double coef,
+                 double* y, unsigned ny) {
+  RefModel* m = static_cast<RefModel*>(h);
+  return guarded(m, [&] {
+    math::dVec X(nx), Y(ny);
+    for (unsigned i = 0; i < nx; i++) X[i] = x[i];
+    for (unsigned i = 0; i < ny; i++) Y[i] = y[i];
+    auto* K = m->storage.getK();
+    if (block == 1 || block == 2)
+      matBVprod(*K->block(block), X, coef, Y);  // friends: found by ADL
+    else if (trans)
+      matBTVprod(*K->block(1, 2), X, coef, Y);
+    else
+      matBVprod(*K->block(1, 2), X, coef, Y);
+    for (unsigned i = 0; i < ny; i++) y[i] = Y[i];
+  });
+}
+
 int ref_get_F(void* h, double* F) {
   RefModel* m = static_cast<RefModel*>(h);
   return guarded(m, [&] {

@@ -8,7 +8,8 @@ them into oracle/_ref/):
 For every case in cases.FULL_CASES it stores the equation numbers, the CSR
 pattern of the three K blocks (block(1), block(1,2), block(2)), their values
 and F, as produced by the reference's FEStorage::updateResults() +
-assembleGlobalEqMatrices().  For cases.DIGEST_CASES (too large to commit) it
+assembleGlobalEqMatrices(), and seeded vectors through the reference's sparse
+block products matBVprod / matBTVprod (SparseMatrix.cpp:497-558) on that K.  For cases.DIGEST_CASES (too large to commit) it
 stores SHA-256 digests of the exact bytes plus a few norms.
 """
 import hashlib
@@ -44,6 +45,31 @@ def run_reference(case):
         out[f"columns_{b}"] = co
         out[f"K_{b}"] = m.K(b)
         out[f"shape_{b}"] = np.array(m.blocks[b], np.uint32)
+    out.update(block_products(m))
+    return out
+
+
+MV_PRODUCTS = ((1, 0), (2, 0), (12, 0), (12, 1))   # (block, transposed)
+
+
+def block_products(m, seed=5, coef=-1.5):
+    """y0 + coef * op(block) x through the model's sparse products
+    (matBVprod / matBTVprod).  x is seeded N(0,1) with every 7th entry 0 and
+    every 11th entry 1e-21 (below the symmetric product's 1e-20 skip)."""
+    rng = np.random.default_rng(seed)
+    out = {}
+    for blk, trans in MV_PRODUCTS:
+        rows, cols, _ = m.blocks[blk]
+        nx = cols if (blk == 12 and not trans) else rows
+        ny = cols if (blk == 12 and trans) else rows
+        x = rng.standard_normal(nx)
+        x[::7] = 0.0
+        x[3::11] = 1e-21
+        y0 = rng.standard_normal(ny)
+        out[f"mv_{blk}_{trans}_x"] = x
+        out[f"mv_{blk}_{trans}_y0"] = y0
+        out[f"mv_{blk}_{trans}_y"] = m.block_mv(blk, trans, x, coef, y0)
+    out["mv_coef"] = np.array(coef)
     return out
 
 

@@ -53,6 +53,21 @@ def test_port_matches_reference_goldens_bit_exact(name):
     assert np.array_equal(_bits(m.F()), _bits(g["F"]))
 
 
+MV_PRODUCTS = ((1, 0), (2, 0), (12, 0), (12, 1))
+
+
+@pytest.mark.parametrize("name", sorted(cases.FULL_CASES))
+def test_port_block_products_match_reference_goldens(name):
+    """matBVprod / matBTVprod (SparseMatrix.cpp:497-558) on the assembled K:
+    the port gives the compiled reference's vectors bit for bit."""
+    g = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    m = _run("port", cases.FULL_CASES[name])[0]
+    coef = float(g["mv_coef"])
+    for blk, trans in MV_PRODUCTS:
+        y = m.block_mv(blk, trans, g[f"mv_{blk}_{trans}_x"], coef, g[f"mv_{blk}_{trans}_y0"])
+        assert np.array_equal(_bits(y), _bits(g[f"mv_{blk}_{trans}_y"])), (blk, trans)
+
+
 def test_port_matches_reference_digests_cube10():
     want = {}
     with open(os.path.join(GOLDEN, "digests.txt")) as f:
@@ -66,6 +81,18 @@ def test_port_matches_reference_digests_cube10():
         got[f"iofeir_{b}"], got[f"columns_{b}"], got[f"K_{b}"] = io, co, m.K(b)
         got[f"shape_{b}"] = np.array(m.blocks[b], np.uint32)
     got["info"] = np.array([m.n_dofs, m.n_con, m.n_unk, m.n_mpc], np.uint32)
+    rng = np.random.default_rng(5)
+    for blk, trans in MV_PRODUCTS:
+        rows, cols, _ = m.blocks[blk]
+        nx = cols if (blk == 12 and not trans) else rows
+        ny = cols if (blk == 12 and trans) else rows
+        x = rng.standard_normal(nx)
+        x[::7] = 0.0
+        x[3::11] = 1e-21
+        y0 = rng.standard_normal(ny)
+        got[f"mv_{blk}_{trans}_x"], got[f"mv_{blk}_{trans}_y0"] = x, y0
+        got[f"mv_{blk}_{trans}_y"] = m.block_mv(blk, trans, x, -1.5, y0)
+    got["mv_coef"] = np.array(-1.5)
     assert m.blocks[2] == (4993, 4993, 161056)
     for k, v in got.items():
         assert hashlib.sha256(np.ascontiguousarray(v).tobytes()).hexdigest() == \
