@@ -8,6 +8,7 @@
  *                                (+ node positions, the Material instance  FEStorage.h:48)
  *   nla3d_add_fix                FEStorage::setConstrainedNodeDof           FEStorage.h:159
  *   nla3d_add_rigid_body         FEStorage::addMpcCollection(RigidBodyMpc)  FEStorage.h:200, Mpc.h:51
+ *   nla3d_add_mpc                FEStorage::addMpc(Mpc)                     FEStorage.h:198, Mpc.h:31
  *   nla3d_build_pattern          initDofs + assignEquationNumbers + the
  *                                sparsity part of initSolutionData (host)   FEStorage.h:259,263,265
  *   nla3d_init_solution_data     initSolutionData: the above + device
@@ -110,6 +111,8 @@ int nla3d_mesh_add_fix(nla3d_ctx* ctx, uint32_t mesh, uint32_t n, const uint32_t
                        const int32_t* dofs);
 int nla3d_mesh_add_rigid_body(nla3d_ctx* ctx, uint32_t mesh, uint32_t master, uint32_t n_slaves,
                               const uint32_t* slaves, uint32_t n_dofs, const int32_t* dofs);
+int nla3d_mesh_add_mpc(nla3d_ctx* ctx, uint32_t mesh, uint32_t n_terms, const uint32_t* nodes,
+                       const int32_t* dofs, const double* coefs, double b);
 /* out as nla3d_info; offsets[0..4] = the mesh's first element, node, equation
  * (index into vecU / F), K value and MPC equation in the concatenation. */
 int nla3d_mesh_info(const nla3d_ctx* ctx, uint32_t mesh, uint32_t out[16], uint64_t offsets[5]);
@@ -128,6 +131,15 @@ void* nla3d_get_stream(const nla3d_ctx* ctx);
 int nla3d_add_fix(nla3d_ctx* ctx, uint32_t n, const uint32_t* nodes, const int32_t* dofs);
 int nla3d_add_rigid_body(nla3d_ctx* ctx, uint32_t master, uint32_t n_slaves,
                          const uint32_t* slaves, uint32_t n_dofs, const int32_t* dofs);
+/* A linear MPC equation sum_t coefs[t] * u(nodes[t], dofs[t]) = b (an Mpc
+ * with these terms passed to FEStorage::addMpc, as readCdbFile builds it from
+ * a CE record, FEReaders.cpp:549-573).  Its equation comes after the DoFs, in
+ * the order of the calls and before the rigid-body MPC equations; each
+ * assembly writes F[eq] = b and adds every coefficient to K(DoF, eq)
+ * (FEStorage.cpp:49-60).  Every term's DoF must be used by an element or a
+ * rigid body. */
+int nla3d_add_mpc(nla3d_ctx* ctx, uint32_t n_terms, const uint32_t* nodes, const int32_t* dofs,
+                  const double* coefs, double b);
 
 /* Host-only set-up: DoF registration, equation numbering, the CSR pattern
  * (bit-exact with the reference) and the element -> CSR slot maps with their

@@ -51,6 +51,12 @@ class BatchAssembly:
                 n = np.ascontiguousarray(m.fix_nodes, np.uint32)
                 dd = np.ascontiguousarray(m.fix_dofs, np.int32)
                 self._check(self.lib.nla3d_mesh_add_fix(self.h, i, n.size, _p(n), _p(dd)))
+            for q in m.mpcs:
+                qn = np.ascontiguousarray(q.nodes, np.uint32)
+                qd = np.ascontiguousarray(q.dofs, np.int32)
+                qc = np.ascontiguousarray(q.coefs, np.float64)
+                self._check(self.lib.nla3d_mesh_add_mpc(self.h, i, qn.size, _p(qn), _p(qd),
+                                                        _p(qc), float(q.b)))
             for rb in m.rigid_bodies:
                 s = np.ascontiguousarray(rb.slaves, np.uint32)
                 dd = np.ascontiguousarray(np.asarray(rb.dofs, np.int32))

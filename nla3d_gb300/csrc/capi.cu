@@ -81,6 +81,13 @@ struct nla3d_ctx {
   double* d_mesh_mat = nullptr;
   uint32_t* d_mpc_u32 = nullptr;  // master, slave, eq, slave_eq, master_eq6 (6), slot (5)
   int32_t* d_mpc_dof = nullptr;
+  // linear MPC equations of all meshes: eq, ptr (n + 1), slot (terms); b, coef
+  uint64_t n_lmpc = 0;
+  uint32_t* d_lmpc_eq = nullptr;
+  uint32_t* d_lmpc_ptr = nullptr;
+  uint32_t* d_lmpc_slot = nullptr;
+  double* d_lmpc_b = nullptr;
+  double* d_lmpc_coef = nullptr;
   ElementStatus* d_status = nullptr;
   std::vector<void*> allocs;
   // walk lists of the sparse block products, built on first use:
@@ -309,6 +316,13 @@ cudaError_t enqueue_assembly(nla3d_ctx* c) {
     if (e != cudaSuccess) return e;
     c->launches++;
   }
+  if (c->n_lmpc) {
+    LinearMpcArgs a{(uint32_t)c->n_lmpc, c->d_lmpc_eq, c->d_lmpc_b, c->d_lmpc_ptr,
+                    c->d_lmpc_slot, c->d_lmpc_coef, c->d_K, c->d_F};
+    e = launch_linear_mpc(a, c->stream);
+    if (e != cudaSuccess) return e;
+    c->launches++;
+  }
   mark(4);
   if (c->timing) c->timed++;
   return cudaSuccess;
@@ -392,6 +406,24 @@ int nla3d_add_fix(nla3d_ctx* c, uint32_t n, const uint32_t* nodes, const int32_t
   return nla3d_mesh_add_fix(c, 0, n, nodes, dofs);
 }
 
+int nla3d_mesh_add_mpc(nla3d_ctx* c, uint32_t mesh, uint32_t n_terms, const uint32_t* nodes,
+                       const int32_t* dofs, const double* coefs, double b) {
+  if (!valid_mesh(c, mesh) || c->host_ready || n_terms == 0 || !nodes || !dofs || !coefs)
+    return fail(c, NLA3D_ERR_ARG, "add_mpc");
+  LinearMpc q;
+  q.node.assign(nodes, nodes + n_terms);
+  q.dof.assign(dofs, dofs + n_terms);
+  q.coef.assign(coefs, coefs + n_terms);
+  q.b = b;
+  c->hm[mesh].lmpcs.push_back(std::move(q));
+  return NLA3D_OK;
+}
+
+int nla3d_add_mpc(nla3d_ctx* c, uint32_t n_terms, const uint32_t* nodes, const int32_t* dofs,
+                  const double* coefs, double b) {
+  return nla3d_mesh_add_mpc(c, 0, n_terms, nodes, dofs, coefs, b);
+}
+
 int nla3d_mesh_add_rigid_body(nla3d_ctx* c, uint32_t mesh, uint32_t master, uint32_t n_slaves,
                               const uint32_t* slaves, uint32_t n_dofs, const int32_t* dofs) {
   if (!valid_mesh(c, mesh) || c->host_ready || n_dofs > 3 || (n_slaves && !slaves) ||
@@ -459,7 +491,7 @@ int nla3d_build_pattern(nla3d_ctx* c) {
     c->node_off[i + 1] = c->node_off[i] + m.n_nodes;
     c->u_off[i + 1] = c->u_off[i] + m.n_total();
     c->k_off[i + 1] = c->k_off[i] + m.nnz_total;
-    c->mpc_off[i + 1] = c->mpc_off[i] + m.n_mpc;
+    c->mpc_off[i + 1] = c->mpc_off[i] + m.mpcs.size();
   }
   const uint64_t n_kc = c->hm[0].n_kc, n_fc = c->hm[0].n_fc;
   if (c->E() * (n_kc + n_fc) >= 0xFFFFFFF0ull || c->Ktot() >= 0xFFFFFFF0ull ||
@@ -589,7 +621,7 @@ int nla3d_init_solution_data(nla3d_ctx* c) {
       std::sort(sl.begin(), sl.end());
       if (std::adjacent_find(sl.begin(), sl.end()) != sl.end())
         return fail(c, NLA3D_ERR_PATTERN, "two MPC terms share one K slot");
-      for (uint64_t k = 0; k < m.n_mpc; k++) {
+      for (uint64_t k = 0; k < m.mpcs.size(); k++) {
         const uint64_t g = c->mpc_off[i] + k;
         const MpcEq& q = m.mpcs[k];
         w[g] = q.node[1] + no;
@@ -603,6 +635,34 @@ int nla3d_init_solution_data(nla3d_ctx* c) {
     }
     CK(upload(c, &c->d_mpc_u32, w.data(), w.size()));
     CK(upload(c, &c->d_mpc_dof, dof.data(), dof.size()));
+  }
+  {
+    // linear MPC equations, global numbering (eq + u_off, slot + k_off)
+    std::vector<uint32_t> leq, lptr(1, 0), lslot;
+    std::vector<double> lb, lcoef;
+    for (size_t i = 0; i < M; i++) {
+      const HostModel& m = c->hm[i];
+      const uint32_t uo = (uint32_t)c->u_off[i], ko = (uint32_t)c->k_off[i];
+      size_t t0 = 0;
+      for (const LinearMpc& q : m.lmpcs) {
+        leq.push_back(q.eq + uo);
+        lb.push_back(q.b);
+        for (size_t t = 0; t < q.node.size(); t++) {
+          lslot.push_back(m.lmpc_slot[t0 + t] + ko);
+          lcoef.push_back(q.coef[t]);
+        }
+        t0 += q.node.size();
+        lptr.push_back((uint32_t)lslot.size());
+      }
+    }
+    c->n_lmpc = leq.size();
+    if (c->n_lmpc) {
+      CK(upload(c, &c->d_lmpc_eq, leq.data(), leq.size()));
+      CK(upload(c, &c->d_lmpc_b, lb.data(), lb.size()));
+      CK(upload(c, &c->d_lmpc_ptr, lptr.data(), lptr.size()));
+      CK(upload(c, &c->d_lmpc_slot, lslot.data(), lslot.size()));
+      CK(upload(c, &c->d_lmpc_coef, lcoef.data(), lcoef.size()));
+    }
   }
   CK(cudaMemsetAsync(c->d_status, 0, sizeof(ElementStatus), c->stream));
   CK(cudaMemsetAsync(&c->d_status->first, 0xFF, sizeof(uint32_t), c->stream));
@@ -944,7 +1004,7 @@ int nla3d_graph_launch(nla3d_ctx* c) {
   if (!c || !c->graph_exec) return fail(c, NLA3D_ERR_ARG, "graph_launch without a captured graph");
   cudaError_t e = cudaGraphLaunch(c->graph_exec, c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "graph_launch");
-  c->launches += 3 + (c->Mtot() ? 1 : 0);
+  c->launches += 3 + (c->Mtot() ? 1 : 0) + (c->n_lmpc ? 1 : 0);
   return NLA3D_OK;
 }
 

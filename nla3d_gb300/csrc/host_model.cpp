@@ -133,7 +133,16 @@ std::string build_host_model(HostModel& m, int n_threads) {
   for (const MpcEq& q : m.mpcs)
     if (!(m.node_mask[q.node[0] - 1] & (1u << q.dof[0])))
       return "rigid body slave DoF is not registered by any element";
-  m.n_mpc = (uint32_t)m.mpcs.size();
+  for (const LinearMpc& q : m.lmpcs) {
+    if (q.node.empty() || q.node.size() != q.dof.size() || q.node.size() != q.coef.size())
+      return "linear MPC without terms";
+    for (size_t t = 0; t < q.node.size(); t++)
+      if (q.node[t] < 1 || q.node[t] > N || q.dof[t] < 0 || q.dof[t] >= kDofTypes ||
+          !(m.node_mask[q.node[t] - 1] & (1u << q.dof[t])))
+        return "linear MPC term on a DoF that no element or rigid body uses";
+  }
+  if (m.mpcs.size() + m.lmpcs.size() >= 0xFFFFFFFFull) return "too many MPC equations";
+  m.n_mpc = (uint32_t)(m.lmpcs.size() + m.mpcs.size());
   uint64_t nd = 0;
   for (uint32_t n = 0; n < N; n++) nd += popcount8(m.node_mask[n]);
   for (uint32_t e = 0; e < E; e++) nd += popcount8(m.elem_mask[e]);
@@ -169,6 +178,7 @@ std::string build_host_model(HostModel& m, int n_threads) {
       if (m.node_mask[n] & (1u << t))
         m.node_eq[(size_t)n * kDofTypes + t] =
             (m.node_fix[n] & (1u << t)) ? next_const++ : next_solve++;
+  for (LinearMpc& q : m.lmpcs) q.eq = next_solve++;  // FEStorage.cpp:424-426, list order
   for (MpcEq& q : m.mpcs) q.eq = next_solve++;
 
   // ---- node -> element incidence (FEStorage::learnTopology) ----
@@ -202,11 +212,17 @@ std::string build_host_model(HostModel& m, int n_threads) {
     mpc_ptr.assign((size_t)N * kDofTypes + 1, 0);
     for (const MpcEq& q : m.mpcs)
       for (int t = 0; t < 5; t++) mpc_ptr[(size_t)(q.node[t] - 1) * kDofTypes + q.dof[t] + 1]++;
+    for (const LinearMpc& q : m.lmpcs)
+      for (size_t t = 0; t < q.node.size(); t++)
+        mpc_ptr[(size_t)(q.node[t] - 1) * kDofTypes + q.dof[t] + 1]++;
     for (size_t k = 0; k + 1 < mpc_ptr.size(); k++) mpc_ptr[k + 1] += mpc_ptr[k];
     mpc_eqs.resize(mpc_ptr.back());
     std::vector<uint32_t> pos(mpc_ptr.begin(), mpc_ptr.end() - 1);
     for (const MpcEq& q : m.mpcs)
       for (int t = 0; t < 5; t++) mpc_eqs[pos[(size_t)(q.node[t] - 1) * kDofTypes + q.dof[t]]++] = q.eq;
+    for (const LinearMpc& q : m.lmpcs)
+      for (size_t t = 0; t < q.node.size(); t++)
+        mpc_eqs[pos[(size_t)(q.node[t] - 1) * kDofTypes + q.dof[t]]++] = q.eq;
     for (size_t k = 0; k + 1 < mpc_ptr.size(); k++) {
       auto b = mpc_eqs.begin() + mpc_ptr[k], e = mpc_eqs.begin() + mpc_ptr[k + 1];
       std::sort(b, e);  // ascending; duplicates removed at use
@@ -425,8 +441,16 @@ std::string build_host_model(HostModel& m, int n_threads) {
   invert(fslot, ntot, m.n_fc, m.f_ptr, m.f_ids);
 
   // ---- MPC term slots ----
-  m.mpc_slot.assign((size_t)m.n_mpc * 5, 0);
-  for (uint32_t k = 0; k < m.n_mpc; k++)
+  m.lmpc_slot.clear();
+  for (const LinearMpc& q : m.lmpcs)
+    for (size_t t = 0; t < q.node.size(); t++) {
+      uint32_t sl = 0;
+      if (!slot_of(q.eq, m.neq(q.node[t], q.dof[t]), &sl))
+        return "an MPC term has no slot in the CSR pattern";
+      m.lmpc_slot.push_back(sl);
+    }
+  m.mpc_slot.assign(m.mpcs.size() * 5, 0);
+  for (uint32_t k = 0; k < (uint32_t)m.mpcs.size(); k++)
     for (int t = 0; t < 5; t++) {
       const MpcEq& q = m.mpcs[k];
       if (!slot_of(q.eq, m.neq(q.node[t], q.dof[t]), &m.mpc_slot[(size_t)k * 5 + t]))

@@ -32,6 +32,18 @@ struct MpcEq {
   int slave_dof = 0;     // UX/UY/UZ of this equation
 };
 
+// A linear MPC equation added by the caller (Mpc, Mpc.h:31-36, through
+// FEStorage::addMpc, FEStorage.cpp:175-179): sum_t coef_t u(node_t, dof_t) = b.
+// Its equation is numbered after the DoFs and before the rigid-body MPCs
+// (those are registered later, in initDofs, FEStorage.cpp:351-354).
+struct LinearMpc {
+  std::vector<uint32_t> node;
+  std::vector<int> dof;
+  std::vector<double> coef;
+  double b = 0.0;
+  uint32_t eq = 0;
+};
+
 // 1-based 3-array CSR block (SparseMatrix.h:53-69).
 struct CsrBlock {
   uint32_t rows = 0, cols = 0;
@@ -55,7 +67,8 @@ struct HostModel {
   std::vector<uint32_t> fix_node;
   std::vector<int> fix_dof;
   std::vector<RigidBody> rbs;
-  std::vector<MpcEq> mpcs;
+  std::vector<MpcEq> mpcs;        // rigid-body MPC equations
+  std::vector<LinearMpc> lmpcs;   // linear MPC equations (numbered first)
   // DoF tables
   std::vector<uint8_t> node_mask, elem_mask, node_fix;
   std::vector<uint32_t> node_eq, elem_eq;  // (entity, type) -> eq, 0 = unused
@@ -73,8 +86,10 @@ struct HostModel {
   std::vector<uint32_t> kslot, fslot;  // element -> slot maps (freed after upload)
   std::vector<uint32_t> k_ptr, k_ids;
   std::vector<uint32_t> f_ptr, f_ids;
-  // MPC term slots (n_mpc * 5) in the concatenated K values
+  // rigid-body MPC term slots (mpcs.size() * 5) and linear MPC term slots
+  // (all terms, equation by equation) in the concatenated K values
   std::vector<uint32_t> mpc_slot;
+  std::vector<uint32_t> lmpc_slot;
 
   uint32_t n_total() const { return n_dofs + n_mpc; }
   uint32_t neq(uint32_t node, int t) const { return node_eq[(size_t)(node - 1) * kDofTypes + t]; }

@@ -582,6 +582,13 @@ __global__ void block_mv_kernel(const BlockMvArgs a) {
   a.y[r] = acc;
 }
 
+__global__ void linear_mpc_kernel(const LinearMpcArgs a) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= a.n) return;
+  a.F[a.eq[k] - 1] = a.b[k];
+  for (uint32_t t = a.ptr[k]; t < a.ptr[k + 1]; t++) a.K[a.slot[t]] += a.coef[t];
+}
+
 // Rigid-body MPC rows (RigidBodyMpc::update, Mpc.cpp:70-164, and
 // FEStorage.cpp:51-61): one thread per MPC equation.
 __global__ void mpc_kernel(const MpcArgs a) {
@@ -953,6 +960,13 @@ cudaError_t launch_block_mv(const BlockMvArgs& a, cudaStream_t s) {
   if (a.n_out == 0) return cudaSuccess;
   const int bs = 128;
   block_mv_kernel<<<(unsigned)((a.n_out + bs - 1) / bs), bs, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_linear_mpc(const LinearMpcArgs& a, cudaStream_t s) {
+  if (a.n == 0) return cudaSuccess;
+  const int bs = 128;
+  linear_mpc_kernel<<<(a.n + bs - 1) / bs, bs, 0, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -95,6 +95,19 @@ struct SegSumArgs {
   double* out;
 };
 
+// Linear MPC rows (FEStorage.cpp:49-60 for an Mpc added with addMpc): one
+// thread per equation: F[eq] = b, then K[slot_t] += coef_t in term order.
+struct LinearMpcArgs {
+  uint32_t n;
+  const uint32_t* eq;     // per equation (1-based global equation)
+  const double* b;        // per equation
+  const uint32_t* ptr;    // n + 1: its terms
+  const uint32_t* slot;   // per term: K slot
+  const double* coef;     // per term
+  double* K;
+  double* F;
+};
+
 // y[r] += sum over the walk list of r of (K[slot] * x[xi]) * coef, in list
 // order (the reference's matBVprod / matBTVprod order, SparseMatrix.cpp:497-558);
 // sym: skip |x| <= 1e-20 as the symmetric product does.
@@ -131,6 +144,7 @@ cudaError_t prepare_device_tables();
 cudaError_t launch_gather(const GatherArgs& a, cudaStream_t s);
 cudaError_t launch_mpc(const MpcArgs& a, cudaStream_t s);
 cudaError_t launch_block_mv(const BlockMvArgs& a, cudaStream_t s);
+cudaError_t launch_linear_mpc(const LinearMpcArgs& a, cudaStream_t s);
 cudaError_t launch_linear(const LinearArgs& a, cudaStream_t s);
 size_t solid81_smem_bytes(bool mixed);
 cudaError_t probe_fma_peak(bool fp64, double* flops);

@@ -42,6 +42,15 @@ class RigidBody:
 
 
 @dataclasses.dataclass
+class LinearMpc:
+    """An Mpc passed to FEStorage::addMpc (Mpc.h:31-36): sum coefs * u(nodes, dofs) = b."""
+    nodes: np.ndarray           # uint32, 1-based node ids
+    dofs: np.ndarray            # int32 Dof types
+    coefs: np.ndarray           # float64
+    b: float = 0.0
+
+
+@dataclasses.dataclass
 class Mesh:
     elem_type: int
     xyz: np.ndarray             # (n_nodes, 3) float64
@@ -52,6 +61,7 @@ class Mesh:
     fix_nodes: np.ndarray | None = None     # uint32 1-based
     fix_dofs: np.ndarray | None = None      # int32 Dof types
     rigid_bodies: list = dataclasses.field(default_factory=list)
+    mpcs: list = dataclasses.field(default_factory=list)   # LinearMpc, numbered first
     name: str = ""
 
     @property

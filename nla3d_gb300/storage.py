@@ -107,6 +107,8 @@ class FEStorage:
             self._check(self.lib.nla3d_set_stream(self.h, ctypes.c_void_p(stream)))
         if mesh.fix_nodes is not None and len(mesh.fix_nodes):
             self._add_fix(mesh.fix_nodes, mesh.fix_dofs)
+        for q in mesh.mpcs:
+            self.addMpc(q)
         for rb in mesh.rigid_bodies:
             self.addMpcCollection(rb)
 
@@ -135,6 +137,13 @@ class FEStorage:
 
     def setConstrainedNodeDof(self, node, dof):
         self._add_fix([node], [dof])
+
+    def addMpc(self, q: mg.LinearMpc):
+        """FEStorage::addMpc: a linear MPC equation (numbered before rigid-body ones)."""
+        n = np.ascontiguousarray(q.nodes, dtype=np.uint32)
+        d = np.ascontiguousarray(q.dofs, dtype=np.int32)
+        cf = np.ascontiguousarray(q.coefs, dtype=np.float64)
+        self._check(self.lib.nla3d_add_mpc(self.h, n.size, _p(n), _p(d), _p(cf), float(q.b)))
 
     def addMpcCollection(self, rb: mg.RigidBody):
         s = np.ascontiguousarray(rb.slaves, dtype=np.uint32)

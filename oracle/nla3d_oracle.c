@@ -479,7 +479,17 @@ struct orc_model {
   int* fix_dof;
   rigid_body* rbs;
   uint32_t n_rbs;
-  mpc_eq* mpcs;
+  mpc_eq* mpcs;     /* rigid-body MPC equations (n_rmpc) */
+  uint32_t n_rmpc;
+  /* linear MPC equations added with orc_add_mpc (FEStorage::addMpc), numbered
+   * before the rigid-body ones: terms lm_ptr[k] .. lm_ptr[k+1] */
+  uint32_t n_lmpc, lm_terms;
+  uint32_t* lm_ptr;
+  uint32_t* lm_node;
+  int* lm_dof;
+  double* lm_coef;
+  double* lm_b;
+  uint32_t* lm_eq;
   /* global system */
   csr_block blk[3]; /* block(1), block(1,2), block(2) */
   double* U;
@@ -531,6 +541,8 @@ void orc_free(orc_model* m) {
   free(m->fix_node); free(m->fix_dof);
   for (uint32_t i = 0; i < m->n_rbs; i++) free(m->rbs[i].slaves);
   free(m->rbs); free(m->mpcs);
+  free(m->lm_ptr); free(m->lm_node); free(m->lm_dof); free(m->lm_coef); free(m->lm_b);
+  free(m->lm_eq);
   for (int b = 0; b < 3; b++) {
     free(m->blk[b].iofeir); free(m->blk[b].columns); free(m->blk[b].values);
   }
@@ -563,6 +575,31 @@ int orc_add_rigid_body(orc_model* m, uint32_t master, uint32_t n_slaves, const u
   rb->slaves = (uint32_t*)malloc(sizeof(uint32_t) * (n_slaves ? n_slaves : 1));
   memcpy(rb->slaves, slaves, sizeof(uint32_t) * n_slaves);
   for (uint32_t i = 0; i < n_dofs; i++) rb->dofs[i] = dofs[i];
+  return 0;
+}
+
+/* FEStorage::addMpc (FEStorage.cpp:175-179) of an Mpc with these terms */
+int orc_add_mpc(orc_model* m, uint32_t n_terms, const uint32_t* nodes, const int32_t* dofs,
+                const double* coefs, double b) {
+  if (!n_terms) return fail(m, "MPC without terms");
+  const uint32_t k = m->n_lmpc, t0 = m->lm_terms;
+  m->lm_ptr = (uint32_t*)realloc(m->lm_ptr, sizeof(uint32_t) * (k + 2));
+  m->lm_b = (double*)realloc(m->lm_b, sizeof(double) * (k + 1));
+  m->lm_eq = (uint32_t*)realloc(m->lm_eq, sizeof(uint32_t) * (k + 1));
+  m->lm_node = (uint32_t*)realloc(m->lm_node, sizeof(uint32_t) * (t0 + n_terms));
+  m->lm_dof = (int*)realloc(m->lm_dof, sizeof(int) * (t0 + n_terms));
+  m->lm_coef = (double*)realloc(m->lm_coef, sizeof(double) * (t0 + n_terms));
+  if (k == 0) m->lm_ptr[0] = 0;
+  for (uint32_t t = 0; t < n_terms; t++) {
+    m->lm_node[t0 + t] = nodes[t];
+    m->lm_dof[t0 + t] = dofs[t];
+    m->lm_coef[t0 + t] = coefs[t];
+  }
+  m->lm_terms = t0 + n_terms;
+  m->lm_ptr[k + 1] = m->lm_terms;
+  m->lm_b[k] = b;
+  m->lm_eq[k] = 0;
+  m->n_lmpc = k + 1;
   return 0;
 }
 
@@ -735,7 +772,8 @@ int orc_setup(orc_model* m, uint32_t max_in_row) {
   uint32_t total_mpc = 0;
   for (uint32_t r = 0; r < m->n_rbs; r++) total_mpc += m->rbs[r].n_slaves * m->rbs[r].n_dofs;
   m->mpcs = (mpc_eq*)calloc(total_mpc + 1, sizeof(mpc_eq));
-  m->n_mpc = total_mpc;
+  m->n_rmpc = total_mpc;
+  m->n_mpc = m->n_lmpc + total_mpc;
   {
     uint32_t k = 0;
     for (uint32_t r = 0; r < m->n_rbs; r++) {
@@ -784,7 +822,17 @@ int orc_setup(orc_model* m, uint32_t max_in_row) {
       if (m->node_mask[n] & (1u << t))
         m->node_eq[(size_t)n * NDOFT + t] =
             (m->node_fix[n] & (1u << t)) ? next_const++ : next_solve++;
-  for (uint32_t k = 0; k < m->n_mpc; k++) m->mpcs[k].eq = next_solve++;
+  /* mpcs list order: addMpc'd equations, then the collections' (initDofs) */
+  for (uint32_t k = 0; k < m->n_lmpc; k++) {
+    for (uint32_t t = m->lm_ptr[k]; t < m->lm_ptr[k + 1]; t++) {
+      const uint32_t n = m->lm_node[t];
+      const int d = m->lm_dof[t];
+      if (n < 1 || n > N || d < 0 || d >= NDOFT || !(m->node_mask[n - 1] & (1u << d)))
+        return fail(m, "MPC term on an unused DoF");
+    }
+    m->lm_eq[k] = next_solve++;
+  }
+  for (uint32_t k = 0; k < m->n_rmpc; k++) m->mpcs[k].eq = next_solve++;
 
   /* --- initSolutionData (FEStorage.cpp:434-550) --- */
   const uint32_t nc = m->n_con, ns = m->n_unk + m->n_mpc;
@@ -840,7 +888,10 @@ int orc_setup(orc_model* m, uint32_t max_in_row) {
         for (int t2 = 0; t2 < NDOFT; t2++)
           if (me & (1u << t2)) rc |= add_entry(m, eeq(m, en, t1), eeq(m, en, t2));
   }
-  for (uint32_t k = 0; k < m->n_mpc && !rc; k++)
+  for (uint32_t k = 0; k < m->n_lmpc && !rc; k++)
+    for (uint32_t t = m->lm_ptr[k]; t < m->lm_ptr[k + 1]; t++)
+      rc |= add_entry(m, m->lm_eq[k], neq(m, m->lm_node[t], m->lm_dof[t]));
+  for (uint32_t k = 0; k < m->n_rmpc && !rc; k++)
     for (int t = 0; t < 5; t++) {
       uint32_t eqj = neq(m, m->mpcs[k].t[t].node, m->mpcs[k].t[t].dof);
       rc |= add_entry(m, m->mpcs[k].eq, eqj);
@@ -1254,7 +1305,12 @@ int orc_assemble(orc_model* m) {
   }
   if (rc) return 1;
   for (uint32_t r = 0; r < m->n_rbs; r++) rigid_body_update(m, &m->rbs[r]);
-  for (uint32_t k = 0; k < m->n_mpc; k++) {
+  for (uint32_t k = 0; k < m->n_lmpc; k++) {
+    m->F[m->lm_eq[k] - 1] = m->lm_b[k];
+    for (uint32_t t = m->lm_ptr[k]; t < m->lm_ptr[k + 1]; t++)
+      rc |= add_value(m, m->lm_eq[k], neq(m, m->lm_node[t], m->lm_dof[t]), m->lm_coef[t]);
+  }
+  for (uint32_t k = 0; k < m->n_rmpc; k++) {
     mpc_eq* q = &m->mpcs[k];
     m->F[q->eq - 1] = q->b;
     for (int t = 0; t < 5; t++) rc |= add_value(m, q->eq, neq(m, q->t[t].node, q->t[t].dof), q->t[t].coef);
@@ -1268,24 +1324,43 @@ int orc_get_K(orc_model* m, int block, double* values) {
   return 0;
 }
 
-/* SparseSymMatrix::value (SparseMatrix.cpp:484-494): 0 for a structural zero */
-static double blk_value(const csr_block* b, uint32_t i, uint32_t j) {
-  const uint32_t k = blk_index(b, i, j);
-  return k == INVALID ? 0.0 : b->values[k];
-}
-
 /* matBVprod(SparseSymMatrix&) SparseMatrix.cpp:497-519, matBVprod(SparseMatrix&)
  * :522-540, matBTVprod(SparseMatrix&) :542-558 */
 int orc_block_mv(orc_model* m, int block, int trans, const double* x, double coef, double* y) {
   const csr_block* b = &m->blk[slot_of(block)];
   const double eps = 1e-20;
   if (block == 1 || block == 2) {
-    for (uint32_t i = 1; i <= b->rows; i++) {
-      for (uint32_t j = 1; j <= i; j++)
-        if (fabs(x[j - 1]) > eps) y[i - 1] += blk_value(b, j, i) * x[j - 1] * coef;
-      for (uint32_t j = i + 1; j <= b->rows; j++)
-        if (fabs(x[j - 1]) > eps) y[i - 1] += blk_value(b, i, j) * x[j - 1] * coef;
+    /* The reference walks j = 1..n for every row i through value(), which
+     * returns 0 for a structural zero.  Walking only the stored entries in
+     * the same order (column i of the upper triangle by ascending row, then
+     * row i right of the diagonal) gives the same sums, except that the
+     * reference also adds +-0 for each structural zero, which can only change
+     * the sign of a zero result; it costs O(nnz) instead of O(n^2 log). */
+    const uint32_t n = b->rows;
+    uint32_t* cp = (uint32_t*)calloc((size_t)n + 1, sizeof(uint32_t));
+    uint32_t* cr = (uint32_t*)malloc(sizeof(uint32_t) * (b->nnz ? b->nnz : 1));
+    uint32_t* ck = (uint32_t*)malloc(sizeof(uint32_t) * (b->nnz ? b->nnz : 1));
+    for (uint32_t k = 0; k < b->nnz; k++) cp[b->columns[k]]++;
+    for (uint32_t i = 0; i < n; i++) cp[i + 1] += cp[i];
+    uint32_t* pos = (uint32_t*)malloc(sizeof(uint32_t) * ((size_t)n + 1));
+    memcpy(pos, cp, sizeof(uint32_t) * ((size_t)n + 1));
+    for (uint32_t r = 1; r <= n; r++)
+      for (uint32_t k = b->iofeir[r - 1] - 1; k < b->iofeir[r] - 1; k++) {
+        const uint32_t c = b->columns[k];
+        cr[pos[c - 1]] = r;
+        ck[pos[c - 1]++] = k;
+      }
+    for (uint32_t i = 1; i <= n; i++) {
+      for (uint32_t q = cp[i - 1]; q < cp[i]; q++) {   /* j = cr[q] <= i ascending */
+        const uint32_t j = cr[q];
+        if (fabs(x[j - 1]) > eps) y[i - 1] += b->values[ck[q]] * x[j - 1] * coef;
+      }
+      for (uint32_t k = b->iofeir[i - 1] - 1; k < b->iofeir[i] - 1; k++) {
+        const uint32_t j = b->columns[k];
+        if (j > i && fabs(x[j - 1]) > eps) y[i - 1] += b->values[k] * x[j - 1] * coef;
+      }
     }
+    free(cp); free(cr); free(ck); free(pos);
     return 0;
   }
   for (uint32_t i = 1; i <= b->rows; i++) {

@@ -33,6 +33,9 @@ const char* orc_error(orc_model* m);
 int orc_add_fix(orc_model* m, uint32_t n, const uint32_t* nodes, const int32_t* dofs);
 int orc_add_rigid_body(orc_model* m, uint32_t master, uint32_t n_slaves, const uint32_t* slaves,
                        uint32_t n_dofs, const int32_t* dofs);
+/* FEStorage::addMpc of an Mpc (Mpc.h:31-36): sum coefs[t] u(nodes[t], dofs[t]) = b */
+int orc_add_mpc(orc_model* m, uint32_t n_terms, const uint32_t* nodes, const int32_t* dofs,
+                const double* coefs, double b);
 /* max_in_row: the reference's pre-compress row capacity (BlockSparseMatrix.h:42,
  * default 100); overflow is reported as an error like SparseMatrix.cpp:84. */
 int orc_setup(orc_model* m, uint32_t max_in_row);
@@ -48,8 +51,8 @@ int orc_get_K(orc_model* m, int block, double* values);
 int orc_get_F(orc_model* m, double* F);
 /* y += coef * op(block) x on the assembled K (SparseMatrix.cpp:497-558):
  * block 1 / 2: matBVprod(SparseSymMatrix&) (both triangles, x_j with
- * |x_j| <= 1e-20 skipped); block 12: trans 0 matBVprod(SparseMatrix&),
- * trans 1 matBTVprod(SparseMatrix&). */
+ * |x_j| <= 1e-20 skipped; stored entries only, in the reference's order);
+ * block 12: trans 0 matBVprod(SparseMatrix&), trans 1 matBTVprod(SparseMatrix&). */
 int orc_block_mv(orc_model* m, int block, int trans, const double* x, double coef, double* y);
 
 /* Element-level pieces (for tests against the reference's own fixtures). */

@@ -70,6 +70,7 @@ def _load(kind: str):
     f("error").argtypes = [_P]
     f("add_fix").argtypes = [_P, ctypes.c_uint, _P, _P]
     f("add_rigid_body").argtypes = [_P, ctypes.c_uint, ctypes.c_uint, _P, ctypes.c_uint, _P]
+    f("add_mpc").argtypes = [_P, ctypes.c_uint, _P, _P, _P, ctypes.c_double]
     f("setup").argtypes = [_P] + ([ctypes.c_uint] if kind == "port" else [])
     f("info").argtypes = [_P, _P]
     f("pattern").argtypes = [_P, ctypes.c_int, _P, _P]
@@ -89,8 +90,8 @@ def _load(kind: str):
                                   ctypes.c_double, _P, ctypes.c_uint]
     f("block_mv").restype = ctypes.c_int
     f("get_F").argtypes = [_P, _P]
-    for n in ("add_fix", "add_rigid_body", "setup", "pattern", "eq_numbers", "set_U", "update",
-              "assemble", "get_K", "get_F"):
+    for n in ("add_fix", "add_rigid_body", "add_mpc", "setup", "pattern", "eq_numbers", "set_U",
+              "update", "assemble", "get_K", "get_F"):
         f(n).restype = ctypes.c_int
     if kind == "port":
         lib.orc_material_S.argtypes = [ctypes.c_int, _P, _P, ctypes.c_double, _P]
@@ -139,6 +140,12 @@ class OracleModel:
             fn = np.ascontiguousarray(mesh.fix_nodes, dtype=np.uint32)
             fd = np.ascontiguousarray(mesh.fix_dofs, dtype=np.int32)
             self._check(self._f("add_fix")(self.h, fn.size, _ptr(fn), _ptr(fd)))
+        for q in mesh.mpcs:
+            qn = np.ascontiguousarray(q.nodes, dtype=np.uint32)
+            qd = np.ascontiguousarray(q.dofs, dtype=np.int32)
+            qc = np.ascontiguousarray(q.coefs, dtype=np.float64)
+            self._check(self._f("add_mpc")(self.h, qn.size, _ptr(qn), _ptr(qd), _ptr(qc),
+                                           float(q.b)))
         for rb in mesh.rigid_bodies:
             sl = np.ascontiguousarray(rb.slaves, dtype=np.uint32)
             dd = np.ascontiguousarray(np.asarray(rb.dofs, dtype=np.int32))

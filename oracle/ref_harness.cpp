@@ -142,6 +142,20 @@ int ref_add_rigid_body(void* h, unsigned master, unsigned n_slaves, const unsign
   });
 }
 
+// FEStorage::addMpc with an Mpc built the way readCdbFile builds one from a
+// CE record (FEReaders.cpp:549-573).
+int ref_add_mpc(void* h, unsigned n_terms, const unsigned* nodes, const int* dofs,
+                const double* coefs, double b) {
+  RefModel* m = static_cast<RefModel*>(h);
+  return guarded(m, [&] {
+    Mpc* mpc = new Mpc();
+    mpc->b = b;
+    for (unsigned t = 0; t < n_terms; t++)
+      mpc->eq.push_back(MpcTerm(nodes[t], (Dof::dofType)dofs[t], coefs[t]));
+    m->storage.addMpc(mpc);
+  });
+}
+
 int ref_setup(void* h) {
   RefModel* m = static_cast<RefModel*>(h);
   return guarded(m, [&] {

@@ -44,6 +44,44 @@ def bar_mpc_2x2x3():
     return m, u, p, extra, True
 
 
+def ce_block_3x3x2():
+    """Clamped 3x3x2 Neo-Hookean (10, 5000) block with linear MPC equations of
+    the kind readCdbFile builds from CE records (FEReaders.cpp:549-573):
+    UX + UZ = 0 on every free node of the x = 3 face, a three-term equation
+    with a non-zero right-hand side, one that names the same DoF twice (its
+    coefficients accumulate in one K entry), and one on a clamped DoF (its K
+    entry lands in block(1,2))."""
+    m = mg.solid81_block(3, 3, 2, 1.0, mg.MAT_NEO_HOOKEAN, (10.0, 5000.0), clamp_z0=True)
+    x, z = m.xyz[:, 0], m.xyz[:, 2]
+    right = np.nonzero((np.abs(x - 3.0) < 1e-12) & (z > 1e-12))[0] + 1
+    for n in right:
+        m.mpcs.append(mg.LinearMpc(np.array([n, n]), np.array([mg.UX, mg.UZ]),
+                                   np.array([1.0, 1.0]), 0.0))
+    m.mpcs.append(mg.LinearMpc(np.array([6, 22, 30]), np.array([mg.UY, mg.UX, mg.UZ]),
+                               np.array([1.0, -0.5, 0.25]), 0.01))
+    m.mpcs.append(mg.LinearMpc(np.array([23, 23, 27]), np.array([mg.UX, mg.UX, mg.UY]),
+                               np.array([1.0, 0.5, -1.0]), 0.0))
+    m.mpcs.append(mg.LinearMpc(np.array([2]), np.array([mg.UY]), np.array([2.0]), 0.0))
+    u, p = mg.stretch_state(m, 1.2, seed=11)
+    return m, u, p, None, True
+
+
+def bar_mpc_ce_2x2x3():
+    """The rigid-body bar plus UX + UY = 0 on the free nodes of its x = 0
+    face: the CE equations are numbered before the rigid-body ones."""
+    m = mg.solid81_bar_mpc(2, 2, 3, 1.0)
+    x, z = m.xyz[:-1, 0], m.xyz[:-1, 2]
+    side = np.nonzero((np.abs(x) < 1e-12) & (z > 1e-12) & (z < 3.0 - 1e-12))[0] + 1
+    for n in side:
+        m.mpcs.append(mg.LinearMpc(np.array([n, n]), np.array([mg.UX, mg.UY]),
+                                   np.array([1.0, 1.0]), 0.0))
+    u, p = mg.stretch_state(m, 1.1, seed=8)
+    master = m.n_nodes
+    extra = {(master, mg.UZ): 0.3, (master, mg.ROTZ): 0.4, (master, mg.ROTX): 0.05,
+             (master, mg.UX): 0.01}
+    return m, u, p, extra, True
+
+
 def tetra0_3x3x3():
     m = mg.tetra0_block(3, 3, 3, 0.5)
     return m, np.zeros((m.n_nodes, 3)), None, None, False
@@ -61,6 +99,6 @@ def cube10_nh():
 
 
 FULL_CASES = {f.__name__: f for f in (cube3_nh, cube4_nh_clamped, mr_twist_3x2x4,
-                                       biderman_3x3x3_clamped, bar_mpc_2x2x3, tetra0_3x3x3,
-                                       quadth_5x4)}
+                                       biderman_3x3x3_clamped, bar_mpc_2x2x3, ce_block_3x3x2,
+                                       bar_mpc_ce_2x2x3, tetra0_3x3x3, quadth_5x4)}
 DIGEST_CASES = {f.__name__: f for f in (cube10_nh,)}

@@ -14,6 +14,7 @@ stores SHA-256 digests of the exact bytes plus a few norms.
 """
 import hashlib
 import os
+import re
 import sys
 
 import numpy as np
@@ -117,6 +118,154 @@ def read_rigid_body_case(cdb_path, curve_path):
     return nodes, elems, comps, fixes, curve
 
 
+DOF_LABELS = ["UX", "UY", "UZ", "ROTX", "ROTY", "ROTZ", "HYDRO_PRESSURE", "TEMP"]
+
+
+def _widths(fmt):
+    """Field widths of an ANSYS fixed format such as (3i9,6e20.13) or (19i9)."""
+    fmt = fmt.strip().lower()
+    m = re.fullmatch(r"\((\d+)i(\d+)(?:,(\d+)e(\d+)\.[0-9e]+)?\)", fmt)
+    if not m:
+        raise ValueError(f"format {fmt!r}")
+    w = [int(m.group(2))] * int(m.group(1))
+    if m.group(3):
+        w += [int(m.group(4))] * int(m.group(3))
+    return w
+
+
+def _split(line, widths):
+    out, pos = [], 0
+    for w in widths:
+        field = line[pos:pos + w]
+        if not field.strip():
+            break
+        out.append(field)
+        pos += w
+    return out
+
+
+def read_cdb(path):
+    """An ANSYS .cdb as the reference's readCdbFile (FEReaders.cpp:330-729)
+    reads it: NBLOCK nodes, SOLID EBLOCK elements (TYPE attribute kept), D
+    fixed DoFs with numeric node and value, CE equations (terms two per
+    line), CMBLOCK node components (names starting with '_' skipped), then
+    MeshData::compressNumbers (FEReaders.cpp:35-80) if the node numbers are
+    not 1..n."""
+    lines = open(path).read().splitlines()
+    node_ids, xyz, cells, ctype, fixes, mpcs, comps = [], [], [], [], [], [], {}
+    i = 0
+    first = lambda t: t.lstrip()[:1]  # noqa: E731
+    while i < len(lines):
+        tok = [t.strip() for t in lines[i].split(",")]
+        key = tok[0].upper()
+        if key == "NBLOCK":
+            w = _widths(lines[i + 1])
+            i += 2
+            while i < len(lines) and first(lines[i]) not in ("-", "N"):
+                v = _split(lines[i], w)
+                node_ids.append(int(v[0]))
+                pos = [0.0, 0.0, 0.0]
+                for k in range(3):
+                    if len(v) > 3 + k:
+                        pos[k] = float(v[3 + k])
+                xyz.append(pos)
+                i += 1
+            continue
+        if key == "EBLOCK":
+            assert tok[2].upper() == "SOLID"
+            w = _widths(lines[i + 1])
+            i += 2
+            while i < len(lines) and first(lines[i]) not in ("-", "N"):
+                v = [int(f) for f in _split(lines[i], w)]
+                n_nodes = v[8]
+                assert len(v) == 11 + n_nodes
+                cells.append(v[11:11 + n_nodes])
+                ctype.append(v[1])
+                i += 1
+            continue
+        if key == "D":
+            try:
+                fixes.append((int(tok[1]), DOF_LABELS.index(tok[2].upper()), float(tok[3])))
+            except ValueError:
+                pass   # 'ALL' etc.: not a numeric node
+        elif key == "CE":
+            b, n_terms = float(tok[5]), int(tok[3])
+            terms = []
+            while n_terms > 0:
+                i += 1
+                t = [x.strip() for x in lines[i].split(",")]
+                for k in range(max(n_terms, 2)):
+                    terms.append((int(t[3 + 3 * k]), DOF_LABELS.index(t[4 + 3 * k].upper()),
+                                  float(t[5 + 3 * k])))
+                    n_terms -= 1
+            mpcs.append((terms, b))
+        elif key == "CMBLOCK" and not tok[1].startswith("_"):
+            n_ranges = int(tok[3].split("!")[0])
+            w = _widths(lines[i + 1])
+            i += 2
+            vals = []
+            while len(vals) < n_ranges:
+                vals += [int(f) for f in _split(lines[i], w)]
+                i += 1
+            lst = []
+            for k, v in enumerate(vals[:n_ranges]):
+                if v > 0:
+                    lst.append(v)
+                else:
+                    lst.extend(range(vals[k - 1] + 1, -v + 1))
+            comps[tok[1]] = lst
+            continue
+        i += 1
+    # compressNumbers
+    if len(node_ids) != max(node_ids):
+        old2new = {o: k + 1 for k, o in enumerate(node_ids)}
+        cells = [[old2new[n] for n in c] for c in cells]
+        fixes = [(old2new[n], d, v) for n, d, v in fixes]
+        mpcs = [([(old2new[n], d, c) for n, d, c in terms], b) for terms, b in mpcs]
+        comps = {k: [old2new[n] for n in v] for k, v in comps.items()}
+    return {"xyz": np.array(xyz), "cells": cells, "type": ctype, "fixes": fixes,
+            "mpcs": mpcs, "comps": comps}
+
+
+def read_ref_curve(path):
+    """main.cpp readRefCurveData: the third column, consecutive repeats dropped."""
+    out, prev = [], -1.0
+    with open(path) as fh:
+        next(fh)
+        for row in fh:
+            if row.strip():
+                v = float(row.split()[2])
+                if v != prev:
+                    out.append(v)
+                    prev = v
+    return out
+
+
+def write_damper_fixture():
+    """The reference's 3d_damper BENCH input (test/CMakeLists.txt:148-153):
+    SOLID81 on the TYPE 1 elements of model.cdb, its fixed DoFs (with their
+    end values), its 497 CE equations, the TOP_SIDE node component used for
+    the UY reaction, and the ANSYS loading curve (test/3d_damper/ansys/)."""
+    base = "/root/reference/test/3d_damper"
+    md = read_cdb(f"{base}/model.cdb")
+    conn = np.array([c for c, t in zip(md["cells"], md["type"]) if t == 1], dtype=np.uint32)
+    terms = [t for terms, _ in md["mpcs"] for t in terms]
+    np.savez_compressed(
+        os.path.join(HERE, "damper_3d.npz"),
+        xyz=md["xyz"], conn=conn,
+        fix_node=np.array([f[0] for f in md["fixes"]], dtype=np.uint32),
+        fix_dof=np.array([f[1] for f in md["fixes"]], dtype=np.int32),
+        fix_value=np.array([f[2] for f in md["fixes"]], dtype=np.float64),
+        mpc_ptr=np.cumsum([0] + [len(t) for t, _ in md["mpcs"]]).astype(np.uint32),
+        mpc_node=np.array([t[0] for t in terms], dtype=np.uint32),
+        mpc_dof=np.array([t[1] for t in terms], dtype=np.int32),
+        mpc_coef=np.array([t[2] for t in terms], dtype=np.float64),
+        mpc_b=np.array([b for _, b in md["mpcs"]], dtype=np.float64),
+        top_side=np.array(md["comps"]["TOP_SIDE"], dtype=np.uint32),
+        ref_curve=np.array(read_ref_curve(f"{base}/ansys/loading_curve_ansys.txt")))
+    print("wrote damper_3d", conn.shape, len(md["mpcs"]), "CE,", len(md["fixes"]), "D")
+
+
 def write_rigid_body_fixture():
     base = "/root/reference/test/rigid_body_mpc"
     nodes, elems, comps, fixes, curve = read_rigid_body_case(
@@ -138,6 +287,7 @@ def write_rigid_body_fixture():
 
 def main():
     write_rigid_body_fixture()
+    write_damper_fixture()
     if not O.build_ref():
         sys.exit("reference sources not found; cannot regenerate goldens")
     for name, case in cases.FULL_CASES.items():

@@ -2,6 +2,7 @@
 numbering and CSR pattern it gets on its own (one reference FEStorage each)."""
 import numpy as np
 
+import cases
 from nla3d_gb300 import meshgen as mg
 from nla3d_gb300.batch import BatchAssembly
 from nla3d_gb300.storage import FEStorage
@@ -14,6 +15,9 @@ def small_batch():
         mat = [(mg.MAT_NEO_HOOKEAN, (1.0 + i, 900.0)), (mg.MAT_MOONEY_RIVLIN, (0.4, 0.1, 2000.0))][i % 2]
         out.append(mg.solid81_block(*n, 0.5, mat[0], mat[1], clamp_z0=clamp))
     out.append(mg.solid81_bar_mpc(2, 2, 3, 1.0))
+    # meshes with linear (CE) MPC equations, one of them also with a rigid body
+    out.append(cases.ce_block_3x3x2()[0])
+    out.append(cases.bar_mpc_ce_2x2x3()[0])
     return out
 
 
