@@ -184,6 +184,20 @@ int nla3d_get_K(nla3d_ctx* ctx, int block, double* values);
 int nla3d_get_F(nla3d_ctx* ctx, double* F);
 /* All K values of the context (every mesh: block(1) | block(1,2) | block(2)). */
 int nla3d_get_K_all(nla3d_ctx* ctx, double* values);
+/* nla3d_assemble, then the K blocks and F copied into host arrays (what
+ * nla3d_get_K for blocks 1, 12, 2 and nla3d_get_F return), with the copies
+ * overlapping the assembly: the element kernel runs over n_chunks element
+ * ranges (1..64), and after each range the runs of K slots whose last
+ * contributing element is done (and that are at least 65,536 slots long)
+ * are summed and copied while the next range computes; the rest, MPC terms
+ * included, comes after the last range.  Same values as the unchunked path,
+ * bit for bit.  The plan is built on the first call per n_chunks.  Single-mesh
+ * contexts; host arrays should be page-locked for the copies to overlap.
+ * Synchronous.  Replaces FEStorage::assembleGlobalEqMatrices + reading
+ * matK / vecF on the host (FEStorage.cpp:26-78, FEStorage.h:100-105). */
+int nla3d_assemble_to_host(nla3d_ctx* ctx, int n_chunks, double* K1, double* K12, double* K2,
+                           double* F);
+
 /* y += coef * op(K block) x on the device, with the values of the last
  * nla3d_assemble of mesh `mesh` (0 for a single-mesh context), on the
  * context's stream (asynchronous, like nla3d_assemble).  Replaces the

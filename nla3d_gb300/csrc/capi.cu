@@ -100,6 +100,17 @@ struct nla3d_ctx {
     uint32_t* xi = nullptr;
   };
   std::vector<std::vector<MvList>> mv;
+  // nla3d_assemble_to_host: element ranges, and the runs of K slots summed
+  // and copied after each range (range index, first slot, end slot)
+  struct SlotRun {
+    int k;
+    uint64_t s0, s1;
+  };
+  cudaStream_t copy_stream = nullptr;
+  std::vector<cudaEvent_t> chunk_ev;
+  int plan_chunks = 0;
+  std::vector<uint32_t> plan_eb;
+  std::vector<SlotRun> plan_runs;
   // launch shape (nla3d_autotune / nla3d_set_launch_shape)
   Solid81Shape shape;
   int gather_bs = 256;
@@ -236,19 +247,16 @@ void graph_release(nla3d_ctx* c) {
 }
 
 // The kernels of one assembly (everything nla3d_assemble enqueues).
-cudaError_t enqueue_assembly(nla3d_ctx* c) {
+// Element kernel over the element range [e0, e1).
+cudaError_t enqueue_elements(nla3d_ctx* c, uint32_t e0, uint32_t e1) {
   const HostModel& m0 = c->hm[0];
-  const uint64_t slot = (c->timed % nla3d_ctx::kRing) * 5;
-  auto mark = [&](int i) {
-    if (c->timing) cudaEventRecord(c->ev[slot + i], c->stream);
-  };
-  cudaError_t e = cudaMemsetAsync(c->d_status, 0, sizeof(ElementStatus), c->stream);
-  if (e == cudaSuccess) e = cudaMemsetAsync(&c->d_status->first, 0xFF, sizeof(uint32_t), c->stream);
-  if (e != cudaSuccess) return e;
-  mark(0);
+  if (e1 <= e0) return cudaSuccess;
+  cudaError_t e;
   if (m0.etype == NLA3D_SOLID81) {
     Solid81Args a{};
-    a.n_elems = (uint32_t)c->E();
+    a.e_begin = e0;
+    a.n_elems = e1;
+    a.n_total = (uint32_t)c->E();
     a.Gt = c->d_Gt;
     a.wdet = c->d_wdet;
     a.conn = c->d_conn;
@@ -269,24 +277,31 @@ cudaError_t enqueue_assembly(nla3d_ctx* c) {
     a.status = c->d_status;
     e = launch_solid81_shaped(a, c->precision == NLA3D_PREC_MIXED, c->shape, c->stream);
   } else {
-    LinearArgs a{m0.etype, (uint32_t)c->E(), c->d_xyz, c->d_conn, c->d_eparams, c->d_contribK,
+    LinearArgs a{m0.etype, e1, c->d_xyz, c->d_conn, c->d_eparams, c->d_contribK,
                  c->d_contribF, c->d_status, c->layout ? c->d_kpos : nullptr,
-                 c->layout ? c->d_fpos : nullptr};
+                 c->layout ? c->d_fpos : nullptr, e0};
     e = launch_linear(a, c->stream);
   }
-  if (e != cudaSuccess) return e;
-  c->launches++;
-  mark(1);
+  if (e == cudaSuccess && e1 > e0) c->launches++;
+  return e;
+}
+
+// K values of the slot range [s0, s1) (fixed-order sums).
+cudaError_t enqueue_gather_K(nla3d_ctx* c, uint64_t s0, uint64_t s1) {
+  cudaError_t e;
   if (c->layout) {
-    SegSumArgs gk{c->Ktot(), c->d_kptr, c->d_contribK, c->d_K};
+    SegSumArgs gk{s1, c->d_kptr, c->d_contribK, c->d_K, s0};
     e = launch_segsum(gk, c->gather_bs, c->stream);
   } else {
-    GatherArgs gk{c->Ktot(), c->d_kptr, c->d_kids, c->d_contribK, c->d_K};
+    GatherArgs gk{s1, c->d_kptr, c->d_kids, c->d_contribK, c->d_K, s0};
     e = launch_gather_bs(gk, c->gather_bs, c->stream);
   }
-  if (e != cudaSuccess) return e;
-  c->launches += c->Ktot() ? 1 : 0;
-  mark(2);
+  if (e == cudaSuccess && s1 > s0) c->launches++;
+  return e;
+}
+
+cudaError_t enqueue_gather_F(nla3d_ctx* c) {
+  cudaError_t e;
   if (c->layout) {
     SegSumArgs gf{c->Utot(), c->d_fptr, c->d_contribF, c->d_F};
     e = launch_segsum(gf, c->gather_bs, c->stream);
@@ -294,9 +309,13 @@ cudaError_t enqueue_assembly(nla3d_ctx* c) {
     GatherArgs gf{c->Utot(), c->d_fptr, c->d_fids, c->d_contribF, c->d_F};
     e = launch_gather_bs(gf, c->gather_bs, c->stream);
   }
-  if (e != cudaSuccess) return e;
-  c->launches++;
-  mark(3);
+  if (e == cudaSuccess) c->launches++;
+  return e;
+}
+
+// MPC rows after the element sums (FEStorage.cpp:41-61).
+cudaError_t enqueue_mpc(nla3d_ctx* c) {
+  cudaError_t e = cudaSuccess;
   if (c->Mtot()) {
     const uint64_t M = c->Mtot();
     MpcArgs a{};
@@ -323,6 +342,30 @@ cudaError_t enqueue_assembly(nla3d_ctx* c) {
     if (e != cudaSuccess) return e;
     c->launches++;
   }
+  return e;
+}
+
+cudaError_t reset_status(nla3d_ctx* c) {
+  cudaError_t e = cudaMemsetAsync(c->d_status, 0, sizeof(ElementStatus), c->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(&c->d_status->first, 0xFF, sizeof(uint32_t), c->stream);
+  return e;
+}
+
+cudaError_t enqueue_assembly(nla3d_ctx* c) {
+  const uint64_t slot = (c->timed % nla3d_ctx::kRing) * 5;
+  auto mark = [&](int i) {
+    if (c->timing) cudaEventRecord(c->ev[slot + i], c->stream);
+  };
+  cudaError_t e = reset_status(c);
+  if (e != cudaSuccess) return e;
+  mark(0);
+  if ((e = enqueue_elements(c, 0, (uint32_t)c->E())) != cudaSuccess) return e;
+  mark(1);
+  if ((e = enqueue_gather_K(c, 0, c->Ktot())) != cudaSuccess) return e;
+  mark(2);
+  if ((e = enqueue_gather_F(c)) != cudaSuccess) return e;
+  mark(3);
+  if ((e = enqueue_mpc(c)) != cudaSuccess) return e;
   mark(4);
   if (c->timing) c->timed++;
   return cudaSuccess;
@@ -371,6 +414,8 @@ int nla3d_destroy(nla3d_ctx* c) {
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   c->allocs.clear();
   for (auto& v : c->ev) cudaEventDestroy(v);
+  for (auto& v : c->chunk_ev) cudaEventDestroy(v);
+  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   delete c;
   return NLA3D_OK;
 }
@@ -799,6 +844,165 @@ int nla3d_get_F(nla3d_ctx* c, double* F) {
                                   c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   return e == cudaSuccess ? NLA3D_OK : cuda_fail(c, e, "get_F");
+}
+
+namespace {
+
+// Element ranges for n chunks and the K slots to sum and copy after each:
+// slot s is complete once the last element contributing to it is done (its
+// range index r(s)); MPC slots are written after every range (r = n - 1).
+// After range k < n - 1, every run of not yet copied slots with r <= k of at
+// least kMinRun slots is summed and copied; after the last range the rest,
+// with gaps shorter than kMaxGap merged (re-summing a finished slot writes the
+// same value, so copying it again is harmless).
+constexpr uint64_t kMinRun = 1u << 16;
+constexpr uint64_t kMaxGap = 1u << 20;
+
+int make_chunk_plan(nla3d_ctx* c, int n) {
+  const uint64_t E = c->E(), nnz = c->Ktot();
+  const uint32_t align = c->hm[0].etype == NLA3D_SOLID81 ? 4u : 1u;
+  std::vector<uint32_t> eb(n + 1, 0);
+  for (int k = 1; k < n; k++) eb[k] = (uint32_t)((E * (uint64_t)k / n) / align * align);
+  eb[n] = (uint32_t)E;
+  for (int k = 1; k <= n; k++) eb[k] = std::max(eb[k], eb[k - 1]);
+  std::vector<uint8_t> r(nnz, 0);
+  if (nnz) {
+    uint32_t* d_eb = nullptr;
+    uint8_t* d_r = nullptr;
+    cudaError_t e = cudaMalloc((void**)&d_eb, sizeof(uint32_t) * (n + 1));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&d_r, nnz);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(d_eb, eb.data(), sizeof(uint32_t) * (n + 1), cudaMemcpyHostToDevice,
+                          c->stream);
+    if (e == cudaSuccess)
+      e = launch_slot_last_range(nnz, c->d_kptr, c->d_kids, (uint32_t)c->hm[0].n_kc, d_eb, n, d_r,
+                                 c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(r.data(), d_r, nnz, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    const cudaError_t f1 = d_eb ? cudaFree(d_eb) : cudaSuccess;
+    const cudaError_t f2 = d_r ? cudaFree(d_r) : cudaSuccess;
+    if (e == cudaSuccess) e = f1 != cudaSuccess ? f1 : f2;
+    if (e != cudaSuccess) return cuda_fail(c, e, "assemble_to_host plan");
+  }
+  for (uint32_t sl : c->hm[0].mpc_slot) r[sl] = (uint8_t)(n - 1);
+  for (uint32_t sl : c->hm[0].lmpc_slot) r[sl] = (uint8_t)(n - 1);
+  const uint8_t kCopied = 0xFF;  // r values are < n <= 64
+  std::vector<nla3d_ctx::SlotRun> runs;
+  for (int k = 0; k + 1 < n; k++) {
+    uint64_t s = 0;
+    while (s < nnz) {
+      if (r[s] > k) {
+        s++;
+        continue;
+      }
+      uint64_t t = s;
+      while (t < nnz && r[t] <= k) t++;   // copied slots (0xFF) end a run
+      if (t - s >= kMinRun) {
+        runs.push_back({k, s, t});
+        std::fill(r.begin() + s, r.begin() + t, kCopied);
+      }
+      s = t;
+    }
+  }
+  // the rest after the last range, small gaps merged
+  uint64_t s = 0;
+  while (s < nnz) {
+    if (r[s] == kCopied) {
+      s++;
+      continue;
+    }
+    uint64_t t = s + 1, gap = 0;
+    for (uint64_t q = s + 1; q < nnz && gap < kMaxGap; q++) {
+      if (r[q] == kCopied) {
+        gap++;
+      } else {
+        gap = 0;
+        t = q + 1;
+      }
+    }
+    runs.push_back({n - 1, s, t});
+    s = t;
+  }
+  c->plan_eb.swap(eb);
+  c->plan_runs.swap(runs);
+  c->plan_chunks = n;
+  return NLA3D_OK;
+}
+
+}  // namespace
+
+int nla3d_assemble_to_host(nla3d_ctx* c, int n_chunks, double* K1, double* K12, double* K2,
+                           double* F) {
+  if (!c || !c->ready || c->hm.size() != 1 || n_chunks < 1 || n_chunks > 64)
+    return fail(c, NLA3D_ERR_ARG, "assemble_to_host");
+  const HostModel& m = c->hm[0];
+  double* host[3] = {K1, K12, K2};
+  for (int b = 0; b < 3; b++)
+    if (m.blk[b].nnz() && !host[b]) return fail(c, NLA3D_ERR_ARG, "assemble_to_host: null K");
+  if (!F) return fail(c, NLA3D_ERR_ARG, "assemble_to_host: null F");
+  cudaError_t e = cudaGetLastError();  // an error left by an earlier call is reported here
+  if (e != cudaSuccess) return cuda_fail(c, e, "assemble_to_host: pending error");
+  if (c->plan_chunks != n_chunks) {
+    int rc = make_chunk_plan(c, n_chunks);
+    if (rc) return rc;
+  }
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(c, e, "assemble_to_host: after the plan");
+  if (!c->copy_stream) {
+    e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_fail(c, e, "assemble_to_host: stream");
+  }
+  while (c->chunk_ev.size() < 64) {
+    cudaEvent_t ev;
+    e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    if (e != cudaSuccess) return cuda_fail(c, e, "assemble_to_host: event");
+    c->chunk_ev.push_back(ev);
+  }
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(c, e, "assemble_to_host: after stream/events");
+  // copy K values [s0, s1) of the concatenated blocks into the block arrays
+  auto copy_range = [&](uint64_t s0, uint64_t s1) -> cudaError_t {
+    for (int b = 0; b < 3 && s0 < s1; b++) {
+      const uint64_t lo = m.val_off[b], hi = lo + m.blk[b].nnz();
+      const uint64_t a = std::max(s0, lo), z = std::min(s1, hi);
+      if (a >= z) continue;
+      cudaError_t err = cudaMemcpyAsync(host[b] + (a - lo), c->d_K + a, sizeof(double) * (z - a),
+                                        cudaMemcpyDeviceToHost, c->copy_stream);
+      if (err != cudaSuccess) return err;
+    }
+    return cudaSuccess;
+  };
+  const int n = n_chunks;
+  const char* where = "status reset";
+  e = reset_status(c);
+  size_t ri = 0;
+  const auto& runs = c->plan_runs;
+  for (int k = 0; k < n && e == cudaSuccess; k++) {
+    where = "element kernel";
+    e = enqueue_elements(c, c->plan_eb[k], c->plan_eb[k + 1]);
+    const size_t r0 = ri;
+    while (ri < runs.size() && runs[ri].k == k && e == cudaSuccess) {
+      where = "K gather";
+      e = enqueue_gather_K(c, runs[ri].s0, runs[ri].s1);
+      ri++;
+    }
+    if (e == cudaSuccess && k == n - 1) where = "F gather", e = enqueue_gather_F(c);
+    if (e == cudaSuccess && k == n - 1) where = "MPC rows", e = enqueue_mpc(c);
+    if (r0 == ri && k < n - 1) continue;  // nothing to copy after this range
+    if (e == cudaSuccess) where = "event record", e = cudaEventRecord(c->chunk_ev[k], c->stream);
+    if (e == cudaSuccess)
+      where = "stream wait", e = cudaStreamWaitEvent(c->copy_stream, c->chunk_ev[k], 0);
+    for (size_t q = r0; q < ri && e == cudaSuccess; q++) {
+      where = "K copy";
+      e = copy_range(runs[q].s0, runs[q].s1);
+    }
+  }
+  if (e == cudaSuccess)
+    where = "F copy", e = cudaMemcpyAsync(F, c->d_F, sizeof(double) * c->Utot(),
+                                          cudaMemcpyDeviceToHost, c->copy_stream);
+  if (e == cudaSuccess) where = "copy stream sync", e = cudaStreamSynchronize(c->copy_stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, (std::string("assemble_to_host: ") + where).c_str());
+  return NLA3D_OK;
 }
 
 int nla3d_block_mv(nla3d_ctx* c, uint32_t mesh, int block, int trans, const double* x,

@@ -200,13 +200,13 @@ __global__ void __launch_bounds__(WPB * 32)
   }
   __syncthreads();
 
-  const uint32_t E = a.n_elems;
-  const uint64_t E8 = (uint64_t)E * 8;
+  const uint32_t E = a.n_elems;  // end of this launch's element range
+  const uint64_t E8 = (uint64_t)(a.n_total ? a.n_total : E) * 8;
   const uint64_t n_quads = (E + kEPW - 1) / kEPW;
   const uint64_t warp_global = (uint64_t)blockIdx.x * WPB + (threadIdx.x >> 5);
   const uint64_t warp_stride = (uint64_t)gridDim.x * WPB;
 
-  for (uint64_t quad = warp_global; quad < n_quads; quad += warp_stride) {
+  for (uint64_t quad = a.e_begin / kEPW + warp_global; quad < n_quads; quad += warp_stride) {
     const uint32_t e0 = (uint32_t)(quad * kEPW);
     const int q = lane >> 3;
     const int sub = lane & 7;  // Gauss point in phase 1, node in phase 2
@@ -496,9 +496,9 @@ __device__ __forceinline__ double plus_zero_sum(double x) {
 
 template <bool kIds>
 __global__ void __launch_bounds__(kMaxGatherBlock)
-    gather_sorted_kernel(const uint64_t n_slots, const uint32_t* __restrict__ ptr,
-                         const uint32_t* __restrict__ ids, const double* __restrict__ contrib,
-                         double* __restrict__ out) {
+    gather_sorted_kernel(const uint64_t s_begin, const uint64_t n_slots,
+                         const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ ids,
+                         const double* __restrict__ contrib, double* __restrict__ out) {
   __shared__ uint32_t s_beg[kMaxGatherBlock];
   __shared__ uint32_t s_end[kMaxGatherBlock];
   __shared__ uint16_t s_slot[kMaxGatherBlock];
@@ -506,7 +506,7 @@ __global__ void __launch_bounds__(kMaxGatherBlock)
   __shared__ uint32_t s_total[kCountClasses];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int n_warps = blockDim.x >> 5;
-  const uint64_t base = (uint64_t)blockIdx.x * blockDim.x;
+  const uint64_t base = s_begin + (uint64_t)blockIdx.x * blockDim.x;
   const uint64_t s = base + tid;
   uint32_t b = 0, e = 0;
   if (s < n_slots) {
@@ -681,7 +681,7 @@ __device__ double det4_lu(double* m) {
 }
 
 __global__ void linear_kernel(const LinearArgs a) {
-  const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t e = a.e_begin + blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= a.n_elems) return;
   const uint32_t* c = a.conn + (uint64_t)e * 4;
   double P[4][3];
@@ -858,7 +858,7 @@ int solid81_max_blocks_per_sm(bool mixed, int wpb) {
 
 cudaError_t launch_solid81_shaped(const Solid81Args& a, bool mixed, Solid81Shape shape,
                                   cudaStream_t s) {
-  if (a.n_elems == 0) return cudaSuccess;
+  if (a.n_elems <= a.e_begin) return cudaSuccess;  // empty element range
   const int wpb = (shape.warps_per_block == 2 || shape.warps_per_block == 8)
                       ? shape.warps_per_block : 4;
   cudaError_t err = ensure_tables();
@@ -871,7 +871,7 @@ cudaError_t launch_solid81_shaped(const Solid81Args& a, bool mixed, Solid81Shape
   if (max_per_sm < 1) return cudaErrorInvalidConfiguration;
   int per_sm = shape.blocks_per_sm;
   if (per_sm <= 0 || per_sm > max_per_sm) per_sm = max_per_sm;
-  const uint64_t quads = ((uint64_t)a.n_elems + kEPW - 1) / kEPW;
+  const uint64_t quads = ((uint64_t)a.n_elems + kEPW - 1) / kEPW - a.e_begin / kEPW;
   uint64_t blocks = (uint64_t)sms * per_sm;
   const uint64_t need = (quads + wpb - 1) / wpb;
   if (blocks > need) blocks = need;
@@ -939,20 +939,20 @@ cudaError_t probe_fma_peak(bool fp64, double* flops) {
 }
 
 cudaError_t launch_gather_bs(const GatherArgs& a, int bs, cudaStream_t s) {
-  if (a.n_slots == 0) return cudaSuccess;
+  if (a.n_slots <= a.s_begin) return cudaSuccess;
   if (bs != 128 && bs != 256 && bs != 512 && bs != 1024) bs = 256;
-  gather_sorted_kernel<true><<<(unsigned)((a.n_slots + bs - 1) / bs), bs, 0, s>>>(
-      a.n_slots, a.ptr, a.ids, a.contrib, a.out);
+  gather_sorted_kernel<true><<<(unsigned)((a.n_slots - a.s_begin + bs - 1) / bs), bs, 0, s>>>(
+      a.s_begin, a.n_slots, a.ptr, a.ids, a.contrib, a.out);
   return cudaGetLastError();
 }
 
 cudaError_t launch_gather(const GatherArgs& a, cudaStream_t s) { return launch_gather_bs(a, 256, s); }
 
 cudaError_t launch_segsum(const SegSumArgs& a, int bs, cudaStream_t s) {
-  if (a.n_slots == 0) return cudaSuccess;
+  if (a.n_slots <= a.s_begin) return cudaSuccess;
   if (bs != 128 && bs != 256 && bs != 512 && bs != 1024) bs = 256;
-  gather_sorted_kernel<false><<<(unsigned)((a.n_slots + bs - 1) / bs), bs, 0, s>>>(
-      a.n_slots, a.ptr, nullptr, a.contrib, a.out);
+  gather_sorted_kernel<false><<<(unsigned)((a.n_slots - a.s_begin + bs - 1) / bs), bs, 0, s>>>(
+      a.s_begin, a.n_slots, a.ptr, nullptr, a.contrib, a.out);
   return cudaGetLastError();
 }
 
@@ -978,9 +978,32 @@ cudaError_t launch_mpc(const MpcArgs& a, cudaStream_t s) {
 }
 
 cudaError_t launch_linear(const LinearArgs& a, cudaStream_t s) {
-  if (a.n_elems == 0) return cudaSuccess;
+  if (a.n_elems <= a.e_begin) return cudaSuccess;
   const int bs = 128;
-  linear_kernel<<<(a.n_elems + bs - 1) / bs, bs, 0, s>>>(a);
+  linear_kernel<<<(a.n_elems - a.e_begin + bs - 1) / bs, bs, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+__global__ void slot_last_range_kernel(uint64_t n_slots, const uint32_t* ptr, const uint32_t* ids,
+                                       uint32_t n_kc, const uint32_t* eb, int n, uint8_t* out) {
+  const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n_slots) return;
+  const uint32_t b = ptr[s], e = ptr[s + 1];
+  int r = 0;
+  if (e > b) {
+    const uint32_t el = ids[e - 1] / n_kc;  // ids ascend within a slot
+    while (r + 1 < n && el >= eb[r + 1]) r++;
+  }
+  out[s] = (uint8_t)r;
+}
+
+cudaError_t launch_slot_last_range(uint64_t n_slots, const uint32_t* ptr, const uint32_t* ids,
+                                   uint32_t n_kc, const uint32_t* eb, int n, uint8_t* out,
+                                   cudaStream_t s) {
+  if (n_slots == 0) return cudaSuccess;
+  const int bs = 256;
+  slot_last_range_kernel<<<(unsigned)((n_slots + bs - 1) / bs), bs, 0, s>>>(n_slots, ptr, ids,
+                                                                          n_kc, eb, n, out);
   return cudaGetLastError();
 }
 

@@ -39,6 +39,11 @@ struct Solid81Args {
   double* contribK;         // [E * 325]
   double* contribF;         // [E * 25]
   ElementStatus* status;
+  // element range [e_begin, n_elems) of a mesh of n_total elements (the
+  // structure-of-arrays stride of Gt); e_begin a multiple of 4; n_total 0
+  // means n_elems
+  uint32_t e_begin;
+  uint32_t n_total;
 };
 
 struct JacobianArgs {
@@ -56,6 +61,7 @@ struct GatherArgs {
   const uint32_t* ids;   // contribution ids
   const double* contrib;
   double* out;
+  uint64_t s_begin;      // slot range [s_begin, n_slots)
 };
 
 struct MpcArgs {
@@ -84,6 +90,7 @@ struct LinearArgs {
   ElementStatus* status;
   const uint32_t* kpos;  // optional slot-ordered output (as Solid81Args)
   const uint32_t* fpos;
+  uint32_t e_begin;      // element range [e_begin, n_elems)
 };
 
 // Contiguous segmented sums: out[s] = sum of contrib[ptr[s] .. ptr[s+1]) in
@@ -93,6 +100,7 @@ struct SegSumArgs {
   const uint32_t* ptr;
   const double* contrib;
   double* out;
+  uint64_t s_begin;      // slot range [s_begin, n_slots)
 };
 
 // Linear MPC rows (FEStorage.cpp:49-60 for an Mpc added with addMpc): one
@@ -144,6 +152,12 @@ cudaError_t prepare_device_tables();
 cudaError_t launch_gather(const GatherArgs& a, cudaStream_t s);
 cudaError_t launch_mpc(const MpcArgs& a, cudaStream_t s);
 cudaError_t launch_block_mv(const BlockMvArgs& a, cudaStream_t s);
+// per K slot: the index of the element range (bounds eb[0..n], n <= 255) that
+// holds the last element contributing to it (contribution ids e * n_kc + c,
+// ascending within a slot)
+cudaError_t launch_slot_last_range(uint64_t n_slots, const uint32_t* ptr, const uint32_t* ids,
+                                   uint32_t n_kc, const uint32_t* eb, int n, uint8_t* out,
+                                   cudaStream_t s);
 cudaError_t launch_linear_mpc(const LinearMpcArgs& a, cudaStream_t s);
 cudaError_t launch_linear(const LinearArgs& a, cudaStream_t s);
 size_t solid81_smem_bytes(bool mixed);

@@ -73,6 +73,40 @@ class StepRecord:
     plain_residual: float | None = None
 
 
+def nested_dissection(K, pts, leaf=64):
+    """Fill-reducing order of a symmetric sparse pattern with a point per row:
+    split the rows at the median of their longest coordinate extent; the rows
+    of the lower half that couple to the upper half form the separator and
+    come after both halves; recurse down to `leaf` rows.  K: CSR holding both
+    triangles; returns the permutation (new position -> row)."""
+    n = K.shape[0]
+    order = []
+
+    def rec(idx):
+        if len(idx) <= leaf:
+            order.extend(idx.tolist())
+            return
+        P = pts[idx]
+        ax = int(np.argmax(P.max(axis=0) - P.min(axis=0)))
+        lower = P[:, ax] < np.median(P[:, ax])
+        if lower.all() or not lower.any():
+            order.extend(idx.tolist())
+            return
+        li, ri = idx[lower], idx[~lower]
+        upper = np.zeros(n, dtype=bool)
+        upper[ri] = True
+        sub = K[li]
+        row = np.repeat(np.arange(len(li)), np.diff(sub.indptr))
+        touch = np.zeros(len(li), dtype=bool)
+        touch[row[upper[sub.indices]]] = True
+        rec(li[~touch])
+        rec(ri)
+        order.extend(li[touch].tolist())
+
+    rec(np.arange(n))
+    return np.asarray(order, dtype=np.int64)
+
+
 class NewtonSolver:
     """backend: an object with eq_numbers(), pattern(b), K(b), F(), set_U(U),
     update(), assemble(), block_mv(block, trans, x, coef, y), n_con, n_unk,
@@ -82,7 +116,21 @@ class NewtonSolver:
     reference's matBVprod / matBTVprod); only the solve reads K(2) on the host."""
 
     def __init__(self, backend, fixes, n_loadsteps=10, n_iterations=15, kinematic_tol=1e-3,
-                 residual_tol=None, loads=()):
+                 residual_tol=None, loads=(), solver="direct"):
+        """solver: "direct" factors K(2) every iteration (SciPy SuperLU, standing
+        in for the reference's EquationSolver); "nd" does the same after a
+        geometric nested-dissection ordering of K(2) (one point per equation
+        from backend.mesh), several times less fill on 3D meshes; "lu-gmres"
+        keeps the last factorisation as the preconditioner of GMRES and
+        refactors only when GMRES needs more than 30 iterations.  Every
+        non-default solve is checked to a relative residual of 1e-10."""
+        if solver not in ("direct", "nd", "lu-gmres"):
+            raise ValueError(solver)
+        self._perm = None
+        self.solver = solver
+        self._lu = None
+        self.factorizations = 0
+        self.krylov_iterations = 0
         self.b = backend
         self.n_loadsteps = n_loadsteps
         self.n_iterations = n_iterations
@@ -108,6 +156,74 @@ class NewtonSolver:
     def _K2(self):
         rows2, cols2, _ = self.b.blocks[2]
         return csr_full(*self.patterns[2], self.b.K(2), rows2, cols2, True)
+
+    def _row_points(self):
+        """A point per K(2) row: the node of a nodal DoF, the element centroid
+        of an element DoF, the first term's node of an MPC equation."""
+        mesh = self.b.mesh
+        xyz = np.asarray(mesh.xyz, dtype=np.float64)
+        conn = np.asarray(mesh.conn, dtype=np.int64)
+        ne, ee = self.b.eq_numbers()
+        pts = np.zeros((self.nu + self.nm, 3))
+        for d in range(ne.shape[1]):
+            eq = ne[:, d].astype(np.int64)
+            sel = eq > self.nc
+            pts[eq[sel] - self.nc - 1] = xyz[sel]
+        cen = xyz[conn - 1].mean(axis=1)
+        for d in range(ee.shape[1]):
+            eq = ee[:, d].astype(np.int64)
+            sel = eq > self.nc
+            pts[eq[sel] - self.nc - 1] = cen[sel]
+        first = [int(q.nodes[0]) for q in mesh.mpcs]
+        for rb in mesh.rigid_bodies:
+            first += [int(n) for n in rb.slaves for _ in rb.dofs]
+        for k, n in enumerate(first):
+            pts[self.nu + k] = xyz[n - 1]
+        return pts
+
+    def _solve(self, K2, rhs):
+        if self.solver == "direct":
+            self.factorizations += 1
+            return spla.spsolve(K2, rhs, permc_spec="MMD_AT_PLUS_A")
+        if self.solver == "nd":
+            if self._perm is None:
+                self._perm = nested_dissection(K2.tocsr(), self._row_points())
+            p = self._perm
+            lu = spla.splu(K2[p][:, p].tocsc(), permc_spec="NATURAL",
+                           options=dict(SymmetricMode=True, DiagPivotThresh=0.001))
+            self.factorizations += 1
+            x = np.empty_like(rhs)
+            x[p] = lu.solve(rhs[p])
+            tol = 1e-10 * max(np.linalg.norm(rhs), 1e-300)
+            for _ in range(3):          # iterative refinement with the same factors
+                r = rhs - K2 @ x
+                if np.linalg.norm(r) <= tol:
+                    return x
+                dx = np.empty_like(rhs)
+                dx[p] = lu.solve(r[p])
+                x += dx
+            if np.linalg.norm(rhs - K2 @ x) <= tol:
+                return x
+            return spla.spsolve(K2, rhs, permc_spec="MMD_AT_PLUS_A")
+        nrm = float(np.linalg.norm(rhs))
+        if nrm == 0.0:
+            return np.zeros_like(rhs)
+        if self._lu is not None:
+            its = [0]
+
+            def count(_):
+                its[0] += 1
+
+            M = spla.LinearOperator(K2.shape, matvec=self._lu.solve, dtype=np.float64)
+            x, info = spla.gmres(K2, rhs, x0=self._lu.solve(rhs), M=M, rtol=1e-13, atol=0.0,
+                                 restart=30, maxiter=1, callback=count,
+                                 callback_type="pr_norm")
+            self.krylov_iterations += its[0]
+            if info == 0 and np.linalg.norm(K2 @ x - rhs) <= 1e-11 * nrm:
+                return x
+        self._lu = spla.splu(K2, permc_spec="COLAMD")
+        self.factorizations += 1
+        return self._lu.solve(rhs)
 
     def _rhs(self, F, dUc):
         """FESolver.cpp:449-454: rhs = F_sl + R_sl - K(1,2)^T dUc, the last
@@ -205,7 +321,7 @@ class NewtonSolver:
                     rec.iterations = tc.eq_step - 1
                     converged = True
                     break
-                dUsl = spla.spsolve(self._K2().tocsc(), rhs, permc_spec="MMD_AT_PLUS_A")
+                dUsl = self._solve(self._K2().tocsc(), rhs)
                 self.U[: self.nc] = Uc
                 self.U[self.nc: self.nc + self.nu] += dUsl[: self.nu]
                 self.U[self.nc + self.nu:] = dUsl[self.nu:]

@@ -258,6 +258,15 @@ class FEStorage:
     def getF(self):
         return self.F()
 
+    def assemble_to_host(self, K1, K12, K2, F, n_chunks=8):
+        """nla3d_assemble_to_host: assemble and copy the K blocks and F into
+        the given host arrays (float64, contiguous; page-locked for overlap)."""
+        for a in (K1, K12, K2, F):
+            assert a.dtype == np.float64 and a.flags.c_contiguous
+        self._check(self.lib.nla3d_assemble_to_host(self.h, n_chunks, _p(K1) if K1.size else None,
+                                                    _p(K12) if K12.size else None,
+                                                    _p(K2) if K2.size else None, _p(F)))
+
     def block_mv_device(self, block, trans, x_ptr, coef, y_ptr, mesh=0):
         """y += coef * op(block) x on device arrays (nla3d_block_mv): the
         reference's matBVprod / matBTVprod on this context's K, asynchronous

@@ -155,3 +155,33 @@ def test_larger_mesh_properties():
         assert abs(fd.sum()) <= 1e-12 * np.abs(fd).sum() * 10
     _, _, Ko, Fo = O.solve_state(mesh, u, p, "port")
     assert rel(K[2], Ko[2]) <= TOL_FP64 and rel(F, Fo) <= TOL_FP64
+
+
+@pytest.mark.parametrize("name,precision", [("cube4_nh_clamped", "fp64"),
+                                            ("cube4_nh_clamped", "mixed"),
+                                            ("bar_mpc_2x2x3", "fp64"),
+                                            ("ce_block_3x3x2", "fp64"),
+                                            ("tetra0_3x3x3", "fp64"),
+                                            ("twist16", "fp64"), ("twist16", "mixed")])
+def test_assemble_to_host_equals_assemble_then_copy(name, precision):
+    """nla3d_assemble_to_host (element ranges, each finished K prefix copied
+    while the next range computes) gives the blocks and F of nla3d_assemble +
+    nla3d_get_K / nla3d_get_F bit for bit, for any number of ranges."""
+    if name == "twist16":
+        # large enough (632k K slots) for runs to be copied after early ranges
+        mesh, u, p = mg.config_twist(n=16, seed=3)
+        extra, do_update = None, True
+    else:
+        mesh, u, p, extra, do_update = cases.FULL_CASES[name]()
+    s = FEStorage(mesh, precision).initSolutionData()
+    ne, ee = s.eq_numbers()
+    s.setU(mg.u_to_vector(ne, ee, u, p, s.n_total, extra))
+    if do_update:
+        s.updateResults()
+    s.assembleGlobalEqMatrices()
+    want = [s.K(b) for b in (1, 12, 2)] + [s.F()]
+    for n_chunks in (1, 3, 8, 64):
+        got = [np.full(s.blocks[b][2], np.nan) for b in (1, 12, 2)] + [np.full(s.n_total, np.nan)]
+        s.assemble_to_host(*got, n_chunks=n_chunks)
+        for x, y in zip(want, got):
+            assert np.array_equal(x.view(np.uint64), y.view(np.uint64)), n_chunks
