@@ -67,6 +67,9 @@ def parse():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batch-meshes", type=int, default=256)
     ap.add_argument("--no-newton", action="store_true")
+    ap.add_argument("--model", choices=["3d_damper", "a2000"],
+                    help="run one of the reference's BENCH models instead (minutes)")
+    ap.add_argument("--model-backend", default="fp64", choices=["fp64", "mixed", "port"])
     ap.add_argument("--e2e-chunks", type=int, default=8,
                     help="element ranges of nla3d_assemble_to_host in the e2e leg")
     ap.add_argument("--no-tune", action="store_true",
@@ -522,8 +525,83 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
 
 
+def cdb_model(name):
+    """A reference BENCH model from its committed fixture (tests/golden/):
+    3d_damper (test/CMakeLists.txt:148-153): 7016 SOLID81, Neo-Hookean
+    (10, 5000), 497 CE equations, UY reaction of TOP_SIDE, threshold 3.0;
+    a2000 (test/CMakeLists.txt:141-146): 3101 PLANE41, Neo-Hookean (1, 500),
+    UY reaction of DISP_BC, threshold 0.2.  Returns (mesh, fixes, reaction
+    nodes, ANSYS curve, threshold)."""
+    from nla3d_gb300 import meshgen as mg
+    if name == "3d_damper":
+        g = np.load(os.path.join(ROOT, "tests", "golden", "damper_3d.npz"))
+        m = mg.Mesh(mg.ELEM_SOLID81, g["xyz"], g["conn"], mat_id=mg.MAT_NEO_HOOKEAN,
+                    mat_c=(10.0, 5000.0), name=name)
+        ptr = g["mpc_ptr"]
+        for k in range(len(g["mpc_b"])):
+            sl = slice(int(ptr[k]), int(ptr[k + 1]))
+            m.mpcs.append(mg.LinearMpc(g["mpc_node"][sl], g["mpc_dof"][sl], g["mpc_coef"][sl],
+                                       float(g["mpc_b"][k])))
+        nodes, thr = g["top_side"], 3.0
+    else:
+        g = np.load(os.path.join(ROOT, "tests", "golden", "a2000_plane41.npz"))
+        m = mg.Mesh(mg.ELEM_PLANE41, g["xyz"], g["conn"], mat_id=mg.MAT_NEO_HOOKEAN,
+                    mat_c=(1.0, 500.0), name=name)
+        nodes, thr = g["disp_bc"], 0.2
+    m.fix_nodes, m.fix_dofs = g["fix_node"], g["fix_dof"]
+    fixes = list(zip(g["fix_node"].tolist(), g["fix_dof"].tolist(), g["fix_value"].tolist()))
+    return m, fixes, nodes, g["ref_curve"], thr
+
+
+def run_cdb_model(args):
+    """A reference BENCH run (20 load steps, 15 iterations, kinematic
+    criterion 1e-3, UY reaction of the component against the ANSYS curve,
+    mean |difference| against the test's threshold as main.cpp compareCurves
+    does), with the assembly on the GPU (or on the CPU oracle for
+    --model-backend port) and the nested-dissection ordered host solve.
+    Prints one JSON line."""
+    from nla3d_gb300.newton import NewtonSolver
+    mesh, fixes, nodes, ref, thr = cdb_model(args.model)
+    if args.model_backend == "port":
+        from oracle import oracle as O
+        b = O.OracleModel(mesh, "port")
+    else:
+        from nla3d_gb300.storage import FEStorage
+        b = FEStorage(mesh, args.model_backend).initSolutionData()
+    t_asm = [0.0]
+    assemble = b.assemble
+
+    def timed_assemble():
+        t0 = time.perf_counter()
+        assemble()
+        if hasattr(b, "synchronize"):
+            b.synchronize()
+        t_asm[0] += time.perf_counter() - t0
+
+    b.assemble = timed_assemble
+    t0 = time.perf_counter()
+    s = NewtonSolver(b, fixes, n_loadsteps=20, n_iterations=15, kinematic_tol=1e-3,
+                     solver="nd").solve()
+    wall = time.perf_counter() - t0
+    ne = s.ne
+    curve = np.array([sum(r[int(ne[n - 1, 1]) - 1] for n in nodes) for r in s.reactions])
+    err = float(np.abs(curve - ref).mean())
+    print(json.dumps({
+        "metric": f"{args.model} reaction curve error vs ANSYS (mean |dF|)", "value": err,
+        "higher_is_better": False, "threshold": thr, "passed": err < thr,
+        "backend": args.model_backend, "load_steps": 20,
+        "iterations": [r.iterations for r in s.records],
+        "factorizations": s.factorizations, "wall_s": wall, "assembly_s": t_asm[0],
+        "curve": curve.round(4).tolist(), "ansys": ref.tolist(),
+        "model": f"{mesh.n_elems} elements, {mesh.n_nodes} nodes, {len(mesh.mpcs)} CE, "
+                 f"{len(fixes)} fixed DoFs"}), flush=True)
+
+
 def main():
     args = parse()
+    if args.model:
+        run_cdb_model(args)
+        return
     if args.impl == "reference":
         if int(os.environ.get("RANK", "0")) != 0:
             return

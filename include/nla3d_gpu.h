@@ -54,6 +54,7 @@ extern "C" {
 #define NLA3D_ERR_ELEMENT 6  /* an element reported J <= 0 or a non-finite value  */
 
 /* Element types: the reference's ElementType codes (sys.h:151-163). */
+#define NLA3D_PLANE41 1
 #define NLA3D_SOLID81 2
 #define NLA3D_TETRA0 3
 #define NLA3D_QUADTH 5
@@ -82,12 +83,12 @@ extern "C" {
 typedef struct nla3d_ctx nla3d_ctx;
 
 typedef struct {
-  int32_t elem_type;          /* NLA3D_SOLID81 / NLA3D_TETRA0 / NLA3D_QUADTH          */
+  int32_t elem_type;          /* NLA3D_SOLID81 / NLA3D_PLANE41 / NLA3D_TETRA0 / QUADTH */
   uint32_t n_nodes;
   uint32_t n_elems;
   const double* xyz;          /* 3 * n_nodes, host                                    */
   const uint32_t* conn;       /* nodes_per_elem * n_elems, 1-based node ids, host     */
-  int32_t mat_id;             /* NLA3D_MAT_* (SOLID81), 0 otherwise                   */
+  int32_t mat_id;             /* NLA3D_MAT_* (SOLID81, PLANE41), 0 otherwise          */
   double mat_c[5];
   const double* elem_params;  /* 2 * n_elems: TETRA0 (E, my), QUADTH (k, 0); or NULL */
 } nla3d_mesh_desc;

@@ -210,12 +210,12 @@ void build_walk(const CsrBlock& b, int kind, std::vector<uint32_t>& ptr,
 int check_mesh(const nla3d_mesh_desc* mesh) {
   if (!mesh || (mesh->n_elems && (!mesh->conn || !mesh->xyz))) return NLA3D_ERR_ARG;
   if (mesh->elem_type != NLA3D_SOLID81 && mesh->elem_type != NLA3D_TETRA0 &&
-      mesh->elem_type != NLA3D_QUADTH)
+      mesh->elem_type != NLA3D_QUADTH && mesh->elem_type != NLA3D_PLANE41)
     return NLA3D_ERR_ARG;
-  if (mesh->elem_type == NLA3D_SOLID81 &&
-      (mesh->mat_id < NLA3D_MAT_NEO_HOOKEAN || mesh->mat_id > NLA3D_MAT_MOONEY_RIVLIN))
+  const bool hyper = mesh->elem_type == NLA3D_SOLID81 || mesh->elem_type == NLA3D_PLANE41;
+  if (hyper && (mesh->mat_id < NLA3D_MAT_NEO_HOOKEAN || mesh->mat_id > NLA3D_MAT_MOONEY_RIVLIN))
     return NLA3D_ERR_ARG;
-  if (mesh->elem_type != NLA3D_SOLID81 && !mesh->elem_params && mesh->n_elems) return NLA3D_ERR_ARG;
+  if (!hyper && !mesh->elem_params && mesh->n_elems) return NLA3D_ERR_ARG;
   return NLA3D_OK;
 }
 
@@ -276,6 +276,28 @@ cudaError_t enqueue_elements(nla3d_ctx* c, uint32_t e0, uint32_t e1) {
     a.contribF = c->d_contribF;
     a.status = c->d_status;
     e = launch_solid81_shaped(a, c->precision == NLA3D_PREC_MIXED, c->shape, c->stream);
+  } else if (m0.etype == NLA3D_PLANE41) {
+    Plane41Args a{};
+    a.e_begin = e0;
+    a.n_elems = e1;
+    a.xyz = c->d_xyz;
+    a.conn = c->d_conn;
+    a.node_eq3 = c->d_node_eq3;
+    a.p_eq = c->d_p_eq;
+    a.U_state = c->d_Ustate;
+    a.U_cur = c->d_U;
+    a.have_state = c->have_state ? 1 : 0;
+    a.mat_id = m0.mat_id;
+    for (int i = 0; i < 5; i++) a.mc[i] = m0.mat_c[i];
+    a.kbulk = bulk_of(m0);
+    a.elem_mesh = c->uniform_material ? nullptr : c->d_elem_mesh;
+    a.mesh_mat = c->uniform_material ? nullptr : c->d_mesh_mat;
+    a.kpos = c->layout ? c->d_kpos : nullptr;
+    a.fpos = c->layout ? c->d_fpos : nullptr;
+    a.contribK = c->d_contribK;
+    a.contribF = c->d_contribF;
+    a.status = c->d_status;
+    e = launch_plane41(a, c->stream);
   } else {
     LinearArgs a{m0.etype, e1, c->d_xyz, c->d_conn, c->d_eparams, c->d_contribK,
                  c->d_contribF, c->d_status, c->layout ? c->d_kpos : nullptr,

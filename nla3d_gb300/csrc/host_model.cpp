@@ -62,6 +62,20 @@ std::vector<LocalPair> element_k_layout(int etype) {
       for (int di = 0; di < 3; di++)
         L.push_back({(int8_t)i, (int8_t)di, (int8_t)-1, (int8_t)HYDRO_PRESSURE});
     L.push_back({(int8_t)-1, (int8_t)HYDRO_PRESSURE, (int8_t)-1, (int8_t)HYDRO_PRESSURE});
+  } else if (etype == PLANE41) {
+    // ElementPLANE41::assembleK (PLANE41.h:54-95): node pairs j >= i, then the
+    // two DoFs, the diagonal node blocks by their lower triangle (dj <= di)
+    for (int i = 0; i < 4; i++)
+      for (int j = i; j < 4; j++)
+        for (int di = 0; di < 2; di++)
+          for (int dj = 0; dj < 2; dj++) {
+            if (i == j && dj > di) continue;
+            L.push_back({(int8_t)i, (int8_t)di, (int8_t)j, (int8_t)dj});
+          }
+    for (int i = 0; i < 4; i++)
+      for (int di = 0; di < 2; di++)
+        L.push_back({(int8_t)i, (int8_t)di, (int8_t)-1, (int8_t)HYDRO_PRESSURE});
+    L.push_back({(int8_t)-1, (int8_t)HYDRO_PRESSURE, (int8_t)-1, (int8_t)HYDRO_PRESSURE});
   } else {
     // Element::assembleK (element.h:281-303, 356-386)
     const int nn = 4;
@@ -84,6 +98,10 @@ std::vector<LocalPair> element_f_layout(int etype) {
     for (int i = 0; i < 8; i++)
       for (int di = 0; di < 3; di++) L.push_back({(int8_t)i, (int8_t)di, 0, 0});
     L.push_back({(int8_t)-1, (int8_t)HYDRO_PRESSURE, 0, 0});
+  } else if (etype == PLANE41) {
+    for (int i = 0; i < 4; i++)
+      for (int di = 0; di < 2; di++) L.push_back({(int8_t)i, (int8_t)di, 0, 0});
+    L.push_back({(int8_t)-1, (int8_t)HYDRO_PRESSURE, 0, 0});
   } else if (etype == QUADTH) {
     for (int i = 0; i < 4; i++) L.push_back({(int8_t)i, (int8_t)TEMP, 0, 0});
   }
@@ -95,17 +113,18 @@ std::string build_host_model(HostModel& m, int n_threads) {
   const uint32_t N = m.n_nodes, E = m.n_elems;
   if (N < 1 && E < 1) return "No any nodes or elements";
   m.npe = m.etype == SOLID81 ? 8 : 4;
-  m.nodal_dofs = m.etype == QUADTH ? 1 : 3;
+  m.nodal_dofs = m.etype == QUADTH ? 1 : (m.etype == PLANE41 ? 2 : 3);
   for (uint64_t i = 0; i < (uint64_t)E * m.npe; i++)
     if (m.conn[i] < 1 || m.conn[i] > N) return "element connectivity refers to a missing node";
 
   // ---- DoF registration (Element::pre, RigidBodyMpc::pre) ----
   m.node_mask.assign(N, 0);
   m.elem_mask.assign(E, 0);
-  const uint8_t node_bits = m.etype == QUADTH ? (uint8_t)(1u << TEMP)
+  const uint8_t node_bits = m.etype == QUADTH    ? (uint8_t)(1u << TEMP)
+                            : m.etype == PLANE41 ? (uint8_t)((1u << UX) | (1u << UY))
                                               : (uint8_t)((1u << UX) | (1u << UY) | (1u << UZ));
   for (uint64_t i = 0; i < (uint64_t)E * m.npe; i++) m.node_mask[m.conn[i] - 1] |= node_bits;
-  if (m.etype == SOLID81)
+  if (m.etype == SOLID81 || m.etype == PLANE41)
     for (uint32_t e = 0; e < E; e++) m.elem_mask[e] = (uint8_t)(1u << HYDRO_PRESSURE);
   m.mpcs.clear();
   for (uint32_t r = 0; r < m.rbs.size(); r++) {

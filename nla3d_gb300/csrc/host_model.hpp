@@ -13,7 +13,7 @@ namespace nla3d_gpu {
 
 constexpr int kDofTypes = 8;  // Dof::numberOfDofTypes (Dof.h:15-25)
 enum DofType { UX = 0, UY, UZ, ROTX, ROTY, ROTZ, HYDRO_PRESSURE, TEMP };
-enum ElemType { SOLID81 = 2, TETRA0 = 3, QUADTH = 5 };
+enum ElemType { PLANE41 = 1, SOLID81 = 2, TETRA0 = 3, QUADTH = 5 };
 
 struct RigidBody {
   uint32_t master = 0;
@@ -56,7 +56,7 @@ struct HostModel {
   // mesh
   int etype = SOLID81;
   int npe = 8;        // nodes per element
-  int nodal_dofs = 3; // DoFs per node used by the element (3 for solids, 1 for QUADTH)
+  int nodal_dofs = 3; // DoFs per node used by the element (3 solids, 2 PLANE41, 1 QUADTH)
   uint32_t n_nodes = 0, n_elems = 0;
   std::vector<double> xyz;
   std::vector<uint32_t> conn;

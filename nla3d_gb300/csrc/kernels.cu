@@ -984,6 +984,144 @@ cudaError_t launch_linear(const LinearArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// PLANE41 algebra (PLANE41.cpp:29-101): with B = B_L + Omega B_omega (3x8),
+//   Kuu += (2 B^T Dd B + B_omega^T S4 B_omega) w,  Kup += B^T Dp w,
+//   Kpp -= w / k,  Qe += B^T S w,  Fp += (J - 1 - p/k) w,
+// Dd and Dp the (XX, YY, XY) part of getDdDp_UP with C_zz = 1; K and F take
+// -Qe, -Fp and the entries in ElementPLANE41::assembleK order (PLANE41.h:54-95).
+__global__ void plane41_kernel(const Plane41Args a) {
+  const uint32_t e = a.e_begin + blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= a.n_elems) return;
+  const uint32_t* cn = a.conn + (uint64_t)e * 4;
+  double X[4][2];
+  uint32_t eq[4][2];
+  for (int n = 0; n < 4; n++) {
+    X[n][0] = a.xyz[(uint64_t)(cn[n] - 1) * 3 + 0];
+    X[n][1] = a.xyz[(uint64_t)(cn[n] - 1) * 3 + 1];
+    eq[n][0] = a.node_eq3[(uint64_t)(cn[n] - 1) * 4 + 0];
+    eq[n][1] = a.node_eq3[(uint64_t)(cn[n] - 1) * 4 + 1];
+  }
+  const uint32_t peq = a.p_eq[e];
+  const double pc = a.U_cur[peq - 1];
+  const double ps = a.have_state ? a.U_state[peq - 1] : 0.0;
+  int mat_id = a.mat_id;
+  const double* mc = a.mc;
+  double kbulk = a.kbulk;
+  if (a.elem_mesh) {
+    const double* mm = a.mesh_mat + 8 * (uint64_t)a.elem_mesh[e];
+    mat_id = (int)mm[0];
+    mc = mm + 1;
+    kbulk = mm[6];
+  }
+  double Us[8];
+  for (int n = 0; n < 4; n++)
+    for (int d = 0; d < 2; d++) Us[2 * n + d] = a.have_state ? a.U_state[eq[n][d] - 1] : 0.0;
+  const int comp[3] = {0, 3, 1};  // M_XX, M_YY, M_XY in the Voigt order xx xy xz yy yz zz
+  double Kuu[8][8] = {}, Kup[8] = {}, Qe[8] = {};
+  double Kpp = 0.0, Fp = 0.0;
+  bool bad = false;
+  for (int g = 0; g < 4; g++) {
+    // isoparametric quad, 2x2 Gauss (isoparametric.h:80-85, .cpp:13-137)
+    const double r = (g & 1) ? kGaussA : -kGaussA;
+    const double sg = (g & 2) ? kGaussA : -kGaussA;
+    const double dN[4][2] = {{-0.25 * (1.0 - sg), -0.25 * (1.0 - r)},
+                             {+0.25 * (1.0 - sg), -0.25 * (1.0 + r)},
+                             {+0.25 * (1.0 + sg), +0.25 * (1.0 + r)},
+                             {-0.25 * (1.0 + sg), +0.25 * (1.0 - r)}};
+    double Jm[2][2] = {};
+    for (int n = 0; n < 4; n++)
+      for (int i = 0; i < 2; i++)
+        for (int j = 0; j < 2; j++) Jm[i][j] += dN[n][i] * X[n][j];
+    const double det = Jm[0][0] * Jm[1][1] - Jm[0][1] * Jm[1][0];
+    if (!(det >= 1.0e-20)) bad = true;
+    const double id = 1.0 / det;
+    const double Ji[2][2] = {{Jm[1][1] * id, -Jm[0][1] * id}, {-Jm[1][0] * id, Jm[0][0] * id}};
+    double G[4][2];
+    for (int n = 0; n < 4; n++)
+      for (int i = 0; i < 2; i++) G[n][i] = Ji[i][0] * dN[n][0] + Ji[i][1] * dN[n][1];
+    const double w = 1.0 * det;
+    // state: O = B_omega U (dU/dx, dU/dy, dV/dx, dV/dy), C (xx, yy, xy)
+    double O[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int n = 0; n < 4; n++) {
+      O[0] += G[n][0] * Us[2 * n];
+      O[1] += G[n][1] * Us[2 * n];
+      O[2] += G[n][0] * Us[2 * n + 1];
+      O[3] += G[n][1] * Us[2 * n + 1];
+    }
+    const double Cxx = 1.0 + 2 * O[0] + O[0] * O[0] + O[2] * O[2];
+    const double Cyy = 1.0 + 2 * O[3] + O[3] * O[3] + O[1] * O[1];
+    const double Cxy = O[1] + O[2] + O[0] * O[1] + O[2] * O[3];
+    const double C6[6] = {Cxx, Cxy, 0.0, Cyy, 0.0, 1.0};
+    MatOut<double> mo;
+    double wD[21];
+    material<double>(mat_id, mc, C6, ps, pc, 1.0, mo, wD);  // wD = 2 Dd
+    const double S[3] = {a.have_state ? mo.S[0] : 0.0, a.have_state ? mo.S[3] : 0.0,
+                         a.have_state ? mo.S[1] : 0.0};
+    double E[3][3];
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) E[i][j] = 0.5 * wD[sym6u(comp[i], comp[j])];
+    const double det2 = Cxx * Cyy - Cxy * Cxy;  // det C (C_zz = 1)
+    const double J = mo.J;
+    const double Dp[3] = {J * Cyy / det2, J * Cxx / det2, -J * Cxy / det2};
+    if (!(J > 0.0 && isfinite(J))) bad = true;
+    // B = B_L + Omega B_omega, rows (xx, yy, xy), columns (node, dof)
+    double B[3][8];
+    for (int n = 0; n < 4; n++) {
+      const double gx = G[n][0], gy = G[n][1];
+      B[0][2 * n] = gx + O[0] * gx;
+      B[0][2 * n + 1] = O[2] * gx;
+      B[1][2 * n] = O[1] * gy;
+      B[1][2 * n + 1] = gy + O[3] * gy;
+      B[2][2 * n] = gy + O[1] * gx + O[0] * gy;
+      B[2][2 * n + 1] = gx + O[3] * gx + O[2] * gy;
+    }
+    double EB[3][8];
+    for (int i = 0; i < 3; i++)
+      for (int c = 0; c < 8; c++) EB[i][c] = E[i][0] * B[0][c] + E[i][1] * B[1][c] + E[i][2] * B[2][c];
+    for (int r2 = 0; r2 < 8; r2++)
+      for (int c = r2; c < 8; c++) {
+        double v = 2.0 * (B[0][r2] * EB[0][c] + B[1][r2] * EB[1][c] + B[2][r2] * EB[2][c]);
+        // geometric term: B_omega^T S4 B_omega couples equal DoFs only
+        if ((r2 & 1) == (c & 1)) {
+          const int na = r2 >> 1, nb = c >> 1;
+          v += G[na][0] * (S[0] * G[nb][0] + S[2] * G[nb][1]) +
+               G[na][1] * (S[2] * G[nb][0] + S[1] * G[nb][1]);
+        }
+        Kuu[r2][c] += v * w;
+      }
+    for (int c = 0; c < 8; c++) {
+      Kup[c] += (B[0][c] * Dp[0] + B[1][c] * Dp[1] + B[2][c] * Dp[2]) * w;
+      Qe[c] += (B[0][c] * S[0] + B[1][c] * S[1] + B[2][c] * S[2]) * w;
+    }
+    Fp += (J - 1 - pc / kbulk) * w;
+    Kpp -= 1.0 / kbulk * w;
+  }
+  if (bad) flag_element(a.status, e + 1);
+  const uint64_t kb = (uint64_t)e * 45, fb = (uint64_t)e * 9;
+  auto kd = [&](uint64_t i) { return a.kpos ? (uint64_t)a.kpos[i] : i; };
+  auto fd = [&](uint64_t i) { return a.fpos ? (uint64_t)a.fpos[i] : i; };
+  int t = 0;
+  for (int i = 0; i < 4; i++)
+    for (int j = i; j < 4; j++)
+      for (int di = 0; di < 2; di++)
+        for (int dj = 0; dj < 2; dj++) {
+          if (i == j && dj > di) continue;
+          const int r2 = 2 * i + di, c = 2 * j + dj;
+          a.contribK[kd(kb + t++)] = r2 <= c ? Kuu[r2][c] : Kuu[c][r2];
+        }
+  for (int c = 0; c < 8; c++) a.contribK[kd(kb + 36 + c)] = Kup[c];
+  a.contribK[kd(kb + 44)] = Kpp;
+  for (int c = 0; c < 8; c++) a.contribF[fd(fb + c)] = -Qe[c];
+  a.contribF[fd(fb + 8)] = -Fp;
+}
+
+cudaError_t launch_plane41(const Plane41Args& a, cudaStream_t s) {
+  if (a.n_elems <= a.e_begin) return cudaSuccess;
+  const int bs = 128;
+  plane41_kernel<<<(a.n_elems - a.e_begin + bs - 1) / bs, bs, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
 __global__ void slot_last_range_kernel(uint64_t n_slots, const uint32_t* ptr, const uint32_t* ids,
                                        uint32_t n_kc, const uint32_t* eb, int n, uint8_t* out) {
   const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;

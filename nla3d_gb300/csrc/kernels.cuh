@@ -93,6 +93,30 @@ struct LinearArgs {
   uint32_t e_begin;      // element range [e_begin, n_elems)
 };
 
+// PLANE41 (PLANE41.cpp:29-146): 4-node plane-strain u/p quad, one thread per
+// element, FP64; Gauss-point state (O, C, S) recomputed from U_state as
+// updateResults() leaves it, tangent and residual with the current pressure.
+struct Plane41Args {
+  uint32_t e_begin, n_elems;  // element range [e_begin, n_elems)
+  const double* xyz;
+  const uint32_t* conn;       // 4 node ids per element, 1-based
+  const uint32_t* node_eq3;   // per node: equations of UX, UY, UZ (4 per node)
+  const uint32_t* p_eq;
+  const double* U_state;
+  const double* U_cur;
+  int have_state;
+  int mat_id;
+  double mc[5];
+  double kbulk;
+  const uint32_t* elem_mesh;  // optional per-element material, as Solid81Args
+  const double* mesh_mat;
+  const uint32_t* kpos;       // optional slot-ordered output, as Solid81Args
+  const uint32_t* fpos;
+  double* contribK;           // [E * 45]
+  double* contribF;           // [E * 9]
+  ElementStatus* status;
+};
+
 // Contiguous segmented sums: out[s] = sum of contrib[ptr[s] .. ptr[s+1]) in
 // ascending order, starting from 0.
 struct SegSumArgs {
@@ -160,6 +184,7 @@ cudaError_t launch_slot_last_range(uint64_t n_slots, const uint32_t* ptr, const 
                                    cudaStream_t s);
 cudaError_t launch_linear_mpc(const LinearMpcArgs& a, cudaStream_t s);
 cudaError_t launch_linear(const LinearArgs& a, cudaStream_t s);
+cudaError_t launch_plane41(const Plane41Args& a, cudaStream_t s);
 size_t solid81_smem_bytes(bool mixed);
 cudaError_t probe_fma_peak(bool fp64, double* flops);
 

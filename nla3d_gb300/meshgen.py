@@ -22,6 +22,7 @@ import math
 import numpy as np
 
 # Reference enums (sys.h:151-163, MaterialFactory.h:12-18, Dof.h:15-25).
+ELEM_PLANE41 = 1
 ELEM_SOLID81 = 2
 ELEM_TETRA0 = 3
 ELEM_QUADTH = 5
@@ -272,6 +273,35 @@ def batched_meshes(n_meshes=256, lo=4, hi=40, seed=3, max_side=None):
         u, p = stretch_state(mesh, lam, 0.01, 0.1, seed=int(rng.integers(1 << 31)), h=h)
         out.append((mesh, u, p))
     return out
+
+
+def plane41_plate(nx, ny, h=1.0, mat_id=MAT_NEO_HOOKEAN, mat_c=(1.0, 500.0), clamp_y0=False,
+                  name="") -> Mesh:
+    """Regular nx*ny PLANE41 plate (4-node plane-strain u/p quads, UX/UY per
+    node, HYDRO_PRESSURE per element) in the z = 0 plane, nodes numbered
+    x-fastest, element nodes counter-clockwise; optionally clamped on y = 0."""
+    q = quadth_plate(nx, ny, h, fix_x0=False)
+    m = Mesh(ELEM_PLANE41, q.xyz, q.conn, mat_id=mat_id, mat_c=tuple(float(c) for c in mat_c),
+             name=name or f"plane41_{nx}x{ny}")
+    if clamp_y0:
+        edge = np.nonzero(np.abs(q.xyz[:, 1]) < 1e-12)[0].astype(np.uint32) + 1
+        m.fix_nodes = np.repeat(edge, 2)
+        m.fix_dofs = np.tile(np.array([UX, UY], dtype=np.int32), edge.size)
+    return m
+
+
+def plane_state(mesh, stretch=1.2, shear=0.1, noise_frac=0.01, seed=0, p_sigma=0.1):
+    """In-plane stretch along y with a simple shear and seeded noise on UX/UY;
+    UZ stays 0; element pressures ~ N(0, p_sigma)."""
+    rng = np.random.default_rng(seed)
+    x = mesh.xyz
+    h = float(np.min(np.abs(np.diff(np.unique(x[:, 0]))))) if mesh.n_nodes > 1 else 1.0
+    u = np.zeros_like(x)
+    u[:, 0] = shear * x[:, 1]
+    u[:, 1] = (stretch - 1.0) * x[:, 1]
+    u[:, :2] += rng.uniform(-noise_frac * h, noise_frac * h, size=(x.shape[0], 2))
+    p = rng.normal(0.0, p_sigma, size=mesh.n_elems)
+    return u, p
 
 
 def u_to_vector(eq_node: np.ndarray, eq_elem: np.ndarray, u: np.ndarray, p: np.ndarray,

@@ -28,7 +28,7 @@
 
 #define NDOFT 8 /* Dof::numberOfDofTypes (Dof.h:15-25) */
 enum { UX = 0, UY, UZ, ROTX, ROTY, ROTZ, HYDRO_PRESSURE, TEMP };
-enum { ET_SOLID81 = 2, ET_TETRA0 = 3, ET_QUADTH = 5 };
+enum { ET_PLANE41 = 1, ET_SOLID81 = 2, ET_TETRA0 = 3, ET_QUADTH = 5 };
 enum { MAT_NH = 1, MAT_BID = 2, MAT_MR = 3 };
 static const uint32_t INVALID = 0xFFFFFFFFu; /* SparseMatrix.cpp:11 */
 
@@ -369,9 +369,10 @@ void orc_material_S(int mat_id, const double* MC, const double* C, double press,
   }
 }
 
-/* getDdDp_UP, materials_hyperelastic.cpp:65-129 */
-void orc_material_D(int mat_id, const double* MC, const double* C, double press, double* Dd,
-                    double* Dp) {
+/* getDdDp_UP, materials_hyperelastic.cpp:65-129, for the components comps[0..ncomp):
+ * Dd packed upper over (comps[i], comps[j]), j >= i, in that order */
+static void material_D_comps(int mat_id, const double* MC, int ncomp, const int* comps,
+                             const double* C, double press, double* Dd, double* Dp) {
   double alpha[5];
   double IC[3];
   IC_C(C, IC);
@@ -407,8 +408,10 @@ void orc_material_D(int mat_id, const double* MC, const double* C, double press,
       {-c[M_XZ] * c[M_XZ], -c[M_XZ] * c[M_YZ], -c[M_XZ] * c[M_ZZ], -c[M_YZ] * c[M_YZ],
        -c[M_YZ] * c[M_ZZ], -c[M_ZZ] * c[M_ZZ]}};
   int ind = 0;
-  for (int ij = 0; ij < 6; ij++) {
-    for (int kl = ij; kl < 6; kl++) {
+  for (int i = 0; i < ncomp; i++) {
+    const int ij = comps[i];
+    for (int j = i; j < ncomp; j++) {
+      const int kl = comps[j];
       Dd[ind] = 4.0 * alpha[2] * pppp * A[ij] * A[kl] +
                 4.0 * alpha[3] * oo * (B[ij] * A[kl] + A[ij] * B[kl]) +
                 4.0 * alpha[4] * pppp * pppp * B[ij] * B[kl] -
@@ -423,8 +426,14 @@ void orc_material_D(int mat_id, const double* MC, const double* C, double press,
       Dd[ind] = Dd[ind] / 2.0;
       ind++;
     }
-    Dp[ij] = J * C_inv[ij];
+    Dp[i] = J * C_inv[ij];
   }
+}
+
+void orc_material_D(int mat_id, const double* MC, const double* C, double press, double* Dd,
+                    double* Dp) {
+  static const int all[6] = {0, 1, 2, 3, 4, 5};
+  material_D_comps(mat_id, MC, 6, all, C, press, Dd, Dp);
 }
 
 /* ----------------------------------------------------------------------- */
@@ -731,10 +740,13 @@ int orc_setup(orc_model* m, uint32_t max_in_row) {
       if (c[a] < 1 || c[a] > N) return fail(m, "element %u: bad node id", e + 1);
       if (m->etype == ET_QUADTH)
         m->node_mask[c[a] - 1] |= 1u << TEMP;
+      else if (m->etype == ET_PLANE41)  /* PLANE41.cpp:25-27 */
+        m->node_mask[c[a] - 1] |= (1u << UX) | (1u << UY);
       else
         m->node_mask[c[a] - 1] |= (1u << UX) | (1u << UY) | (1u << UZ);
     }
-    if (m->etype == ET_SOLID81) m->elem_mask[e] |= 1u << HYDRO_PRESSURE;
+    if (m->etype == ET_SOLID81 || m->etype == ET_PLANE41)
+      m->elem_mask[e] |= 1u << HYDRO_PRESSURE;
   }
   if (m->etype == ET_SOLID81) {
     m->np = 8;
@@ -754,8 +766,18 @@ int orc_setup(orc_model* m, uint32_t max_in_row) {
         C[0] = 1.0; C[3] = 1.0; C[5] = 1.0;
       }
     }
-  } else if (m->etype == ET_QUADTH) {
+  } else if (m->etype == ET_QUADTH || m->etype == ET_PLANE41) {
     m->np = 4;
+    if (m->etype == ET_PLANE41) {
+      /* PLANE41::pre (PLANE41.cpp:15-24): S = 0, C = (1, 1, 0), O = 0 */
+      m->S = (double*)calloc((size_t)E * 4 * 3 + 1, sizeof(double));
+      m->Cst = (double*)calloc((size_t)E * 4 * 3 + 1, sizeof(double));
+      m->O = (double*)calloc((size_t)E * 4 * 4 + 1, sizeof(double));
+      for (size_t g = 0; g < (size_t)E * 4; g++) {
+        m->Cst[g * 3 + 0] = 1.0;
+        m->Cst[g * 3 + 1] = 1.0;
+      }
+    }
     m->NiXj = (double*)malloc(sizeof(double) * (size_t)E * 4 * 8 + 8);
     m->det = (double*)malloc(sizeof(double) * (size_t)E * 4 + 8);
     m->wts = (double*)malloc(sizeof(double) * 4);
@@ -1215,6 +1237,138 @@ static int quadth_buildK(orc_model* m, uint32_t e) {
 }
 
 /* ----------------------------------------------------------------------- */
+/* PLANE41 (PLANE41.cpp): 4-node plane-strain u/p quad, Mat operator algebra */
+/* ----------------------------------------------------------------------- */
+
+/* Mat::operator*(Mat) (Mat.h:198-212): element = 0, += a_il b_lj in l order */
+static void mat_mul(const double* A, int M, int N, const double* B, int K, double* out) {
+  for (int i = 0; i < M; i++)
+    for (int j = 0; j < K; j++) {
+      double el = 0.0;
+      for (int l = 0; l < N; l++) el += A[i * N + l] * B[l * K + j];
+      out[i * K + j] = el;
+    }
+}
+
+static void mat_T(const double* A, int M, int N, double* out) {
+  for (int i = 0; i < M; i++)
+    for (int j = 0; j < N; j++) out[j * M + i] = A[i * N + j];
+}
+
+/* components of PLANE41 (PLANE41.cpp:11): M_XX, M_YY, M_XY */
+static const int P41_COMPS[3] = {M_XX, M_YY, M_XY};
+
+static void plane41_B(const double* G, double* B /*3x8*/, double* Bw /*4x8*/) {
+  /* make_B, make_Bomega (PLANE41.cpp:103-118); G[2a+d] = dN_a/dx_d */
+  memset(B, 0, sizeof(double) * 24);
+  memset(Bw, 0, sizeof(double) * 32);
+  for (int a = 0; a < 4; a++) {
+    const double gx = G[2 * a], gy = G[2 * a + 1];
+    B[0 * 8 + 2 * a] = gx;
+    B[1 * 8 + 2 * a + 1] = gy;
+    B[2 * 8 + 2 * a] = gy;
+    B[2 * 8 + 2 * a + 1] = gx;
+    Bw[0 * 8 + 2 * a] = gx;
+    Bw[1 * 8 + 2 * a] = gy;
+    Bw[2 * 8 + 2 * a + 1] = gx;
+    Bw[3 * 8 + 2 * a + 1] = gy;
+  }
+}
+
+/* ElementPLANE41::update (PLANE41.cpp:120-146) */
+static void plane41_update(orc_model* m, uint32_t e) {
+  const uint32_t* c = m->conn + (size_t)e * 4;
+  double U[8];
+  for (int a = 0; a < 4; a++) {
+    U[2 * a] = m->U[neq(m, c[a], UX) - 1];
+    U[2 * a + 1] = m->U[neq(m, c[a], UY) - 1];
+  }
+  const double p_e = m->U[eeq(m, e + 1, HYDRO_PRESSURE) - 1];
+  for (int g = 0; g < 4; g++) {
+    double B[24], Bw[32];
+    plane41_B(m->NiXj + ((size_t)e * 4 + g) * 8, B, Bw);
+    double* O = m->O + ((size_t)e * 4 + g) * 4;
+    double* C = m->Cst + ((size_t)e * 4 + g) * 3;
+    mat_mul(Bw, 4, 8, U, 1, O);
+    C[0] = 1.0 + 2 * O[0] + 1.0 * (O[0] * O[0] + O[2] * O[2]);
+    C[1] = 1.0 + 2 * O[3] + 1.0 * (O[3] * O[3] + O[1] * O[1]);
+    C[2] = O[1] + O[2] + O[0] * O[1] + O[2] * O[3];
+    double CV[6] = {C[0], C[2], 0.0, C[1], 0.0, 1.0};
+    double S6[6];
+    orc_material_S(m->mat_id, m->MC, CV, p_e, S6);
+    double* S = m->S + ((size_t)e * 4 + g) * 3;
+    for (int i = 0; i < 3; i++) S[i] = S6[P41_COMPS[i]];
+  }
+}
+
+/* ElementPLANE41::buildK (PLANE41.cpp:31-101) and its assembleK (PLANE41.h:54-95) */
+static int plane41_buildK(orc_model* m, uint32_t e) {
+  double Kuu[64], Kup[8], Qe[8];
+  memset(Kuu, 0, sizeof(Kuu));
+  memset(Kup, 0, sizeof(Kup));
+  memset(Qe, 0, sizeof(Qe));
+  double Kpp = 0.0, Fp = 0.0;
+  const double p_e = m->U[eeq(m, e + 1, HYDRO_PRESSURE) - 1];
+  const double k = mat_K(m->mat_id, m->MC);
+  for (int g = 0; g < 4; g++) {
+    const double dWt = m->wts[g] * m->det[(size_t)e * 4 + g];
+    const double* Cg = m->Cst + ((size_t)e * 4 + g) * 3;
+    const double* S = m->S + ((size_t)e * 4 + g) * 3;
+    const double* O = m->O + ((size_t)e * 4 + g) * 4;
+    double CV[6] = {Cg[0], Cg[2], 0.0, Cg[1], 0.0, 1.0};
+    double Dd[6], Dp[3];
+    material_D_comps(m->mat_id, m->MC, 3, P41_COMPS, CV, p_e, Dd, Dp);
+    const double Ec[9] = {Dd[0], Dd[1], Dd[2], Dd[1], Dd[3], Dd[4], Dd[2], Dd[4], Dd[5]};
+    double IC[3];
+    IC_C(CV, IC);
+    const double J = IC[2];
+    double B[24], Bw[32];
+    plane41_B(m->NiXj + ((size_t)e * 4 + g) * 8, B, Bw);
+    const double S4[16] = {S[0], S[2], 0.0, 0.0, S[2], S[1], 0.0, 0.0,
+                           0.0, 0.0, S[0], S[2], 0.0, 0.0, S[2], S[1]};
+    const double Om[12] = {O[0], 0.0, O[2], 0.0, 0.0, O[1], 0.0, O[3], O[1], O[0], O[3], O[2]};
+    double Bl[24];
+    mat_mul(Om, 3, 4, Bw, 8, Bl);
+    for (int i = 0; i < 24; i++) B[i] += Bl[i];
+    double BT[24], BwT[32], t1[24], t2[64], t3[32], t4[64];
+    mat_T(B, 3, 8, BT);
+    mat_T(Bw, 4, 8, BwT);
+    mat_mul(BT, 8, 3, Ec, 3, t1);   /* B^T E */
+    mat_mul(t1, 8, 3, B, 8, t2);    /* (B^T E) B */
+    mat_mul(BwT, 8, 4, S4, 4, t3);  /* Bw^T S */
+    mat_mul(t3, 8, 4, Bw, 8, t4);   /* (Bw^T S) Bw */
+    for (int i = 0; i < 64; i++) Kuu[i] += (t2[i] * 2.0 + t4[i]) * dWt;
+    Fp += (J - 1 - p_e / k) * dWt;
+    double q[8];
+    mat_mul(BT, 8, 3, S, 1, q);     /* B^T S (Mat * Vec) */
+    for (int i = 0; i < 8; i++) Qe[i] += q[i] * dWt;
+    double kup[8];
+    mat_mul(BT, 8, 3, Dp, 1, kup);
+    for (int i = 0; i < 8; i++) Kup[i] += kup[i] * dWt;
+    Kpp -= 1.0 / k * dWt;
+  }
+  const uint32_t* c = m->conn + (size_t)e * 4;
+  const uint32_t pe = eeq(m, e + 1, HYDRO_PRESSURE);
+  const int dofs[2] = {UX, UY};
+  int rc = 0;
+  for (int i = 0; i < 4; i++)
+    for (int j = i; j < 4; j++)
+      for (int di = 0; di < 2; di++)
+        for (int dj = 0; dj < 2; dj++) {
+          if (i == j && dj > di) continue;
+          rc |= add_value(m, neq(m, c[i], dofs[di]), neq(m, c[j], dofs[dj]),
+                          Kuu[(i * 2 + di) * 8 + j * 2 + dj]);
+        }
+  for (int i = 0; i < 4; i++)
+    for (int di = 0; di < 2; di++) rc |= add_value(m, neq(m, c[i], dofs[di]), pe, Kup[i * 2 + di]);
+  rc |= add_value(m, pe, pe, Kpp);
+  for (int i = 0; i < 4; i++)
+    for (int di = 0; di < 2; di++) m->F[neq(m, c[i], dofs[di]) - 1] += -Qe[i * 2 + di];
+  m->F[pe - 1] += -Fp;
+  return rc;
+}
+
+/* ----------------------------------------------------------------------- */
 /* RigidBodyMpc::update (Mpc.cpp:70-164)                                    */
 /* ----------------------------------------------------------------------- */
 
@@ -1286,6 +1440,8 @@ int orc_update(orc_model* m) {
   if (!m->setup_done) return fail(m, "setup first");
   if (m->etype == ET_SOLID81)
     for (uint32_t e = 0; e < m->n_elems; e++) solid81_update(m, e);
+  else if (m->etype == ET_PLANE41)
+    for (uint32_t e = 0; e < m->n_elems; e++) plane41_update(m, e);
   return 0;
 }
 
@@ -1300,6 +1456,8 @@ int orc_assemble(orc_model* m) {
       rc |= solid81_buildK(m, e);
     else if (m->etype == ET_TETRA0)
       rc |= tetra0_buildK(m, e);
+    else if (m->etype == ET_PLANE41)
+      rc |= plane41_buildK(m, e);
     else
       rc |= quadth_buildK(m, e);
   }

@@ -12,7 +12,7 @@
 // and the per-iteration pair updateResults() -> assembleGlobalEqMatrices()
 // (FESolver.cpp:471 -> :446).
 //
-// Only SOLID81, TETRA0 and QUADTH are instantiated, so ElementFactory is
+// Only SOLID81, TETRA0, QUADTH and PLANE41 are instantiated, so ElementFactory is
 // provided here (the reference's factory also instantiates element types that
 // are outside the assembly path and need the full third-party library).
 #include <cstring>
@@ -22,6 +22,7 @@
 #include "FEStorage.h"
 #include "Mpc.h"
 #include "Node.h"
+#include "elements/PLANE41.h"
 #include "elements/QUADTH.h"
 #include "elements/SOLID81.h"
 #include "elements/TETRA0.h"
@@ -43,6 +44,7 @@ void ElementFactory::createElements(ElementType elId, const uint32 n, std::vecto
       case ElementType::SOLID81: ptr.push_back(new ElementSOLID81()); break;
       case ElementType::TETRA0: ptr.push_back(new ElementTETRA0()); break;
       case ElementType::QUADTH: ptr.push_back(new ElementQUADTH()); break;
+      case ElementType::PLANE41: ptr.push_back(new ElementPLANE41()); break;
       default: LOG(FATAL) << "element type not built into the oracle harness";
     }
   }
@@ -74,7 +76,8 @@ int guarded(RefModel* m, F&& f) {
 
 extern "C" {
 
-// elem_type: reference ElementType code (sys.h:151-163): 2 SOLID81, 3 TETRA0, 5 QUADTH.
+// elem_type: reference ElementType code (sys.h:151-163): 1 PLANE41, 2 SOLID81, 3 TETRA0,
+//            5 QUADTH.
 // mat_id: reference MaterialFactory::matId (MaterialFactory.h:12-18): 1 Neo-Hookean,
 //         2 Biderman, 3 Mooney-Rivlin; 0 = no material (TETRA0 / QUADTH).
 // elem_params: per element, two doubles (TETRA0: E, my; QUADTH: k, unused).

@@ -82,6 +82,21 @@ def bar_mpc_ce_2x2x3():
     return m, u, p, extra, True
 
 
+def plane41_nh_3x2():
+    """PLANE41 (4-node plane-strain u/p quad) Neo-Hookean (1, 500) plate of
+    3x2 elements, free, stretched and sheared with noise."""
+    m = mg.plane41_plate(3, 2, 0.5, mg.MAT_NEO_HOOKEAN, (1.0, 500.0))
+    u, p = mg.plane_state(m, stretch=1.2, shear=0.1, seed=3)
+    return m, u, p, None, True
+
+
+def plane41_mr_4x3_clamped():
+    """PLANE41 Mooney-Rivlin (0.4, 0.1, 2000) plate of 4x3 elements clamped on y = 0."""
+    m = mg.plane41_plate(4, 3, 0.5, mg.MAT_MOONEY_RIVLIN, (0.4, 0.1, 2000.0), clamp_y0=True)
+    u, p = mg.plane_state(m, stretch=1.3, shear=-0.15, seed=4)
+    return m, u, p, None, True
+
+
 def tetra0_3x3x3():
     m = mg.tetra0_block(3, 3, 3, 0.5)
     return m, np.zeros((m.n_nodes, 3)), None, None, False
@@ -100,5 +115,6 @@ def cube10_nh():
 
 FULL_CASES = {f.__name__: f for f in (cube3_nh, cube4_nh_clamped, mr_twist_3x2x4,
                                        biderman_3x3x3_clamped, bar_mpc_2x2x3, ce_block_3x3x2,
-                                       bar_mpc_ce_2x2x3, tetra0_3x3x3, quadth_5x4)}
+                                       bar_mpc_ce_2x2x3, plane41_nh_3x2, plane41_mr_4x3_clamped,
+                                       tetra0_3x3x3, quadth_5x4)}
 DIGEST_CASES = {f.__name__: f for f in (cube10_nh,)}

@@ -266,6 +266,25 @@ def write_damper_fixture():
     print("wrote damper_3d", conn.shape, len(md["mpcs"]), "CE,", len(md["fixes"]), "D")
 
 
+def write_a2000_fixture():
+    """The reference's a2000_damper BENCH input (test/CMakeLists.txt:141-146):
+    PLANE41 on the TYPE 1 elements of a2000.cdb, its fixed DoFs, the DISP_BC
+    node component of the UY reaction, and the ANSYS loading curve."""
+    base = "/root/reference/test/a2000_damper"
+    md = read_cdb(f"{base}/a2000.cdb")
+    conn = np.array([c for c, t in zip(md["cells"], md["type"]) if t == 1], dtype=np.uint32)
+    assert not md["mpcs"]
+    np.savez_compressed(
+        os.path.join(HERE, "a2000_plane41.npz"),
+        xyz=md["xyz"], conn=conn,
+        fix_node=np.array([f[0] for f in md["fixes"]], dtype=np.uint32),
+        fix_dof=np.array([f[1] for f in md["fixes"]], dtype=np.int32),
+        fix_value=np.array([f[2] for f in md["fixes"]], dtype=np.float64),
+        disp_bc=np.array(md["comps"]["DISP_BC"], dtype=np.uint32),
+        ref_curve=np.array(read_ref_curve(f"{base}/ansys/loading_curve_ansys.txt")))
+    print("wrote a2000_plane41", conn.shape, len(md["fixes"]), "D")
+
+
 def write_rigid_body_fixture():
     base = "/root/reference/test/rigid_body_mpc"
     nodes, elems, comps, fixes, curve = read_rigid_body_case(
@@ -288,6 +307,7 @@ def write_rigid_body_fixture():
 def main():
     write_rigid_body_fixture()
     write_damper_fixture()
+    write_a2000_fixture()
     if not O.build_ref():
         sys.exit("reference sources not found; cannot regenerate goldens")
     for name, case in cases.FULL_CASES.items():
