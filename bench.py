@@ -47,8 +47,6 @@ FLOP_PER_ELEM_BTDB = 69072
 # lower bound there (L2 still held part of them when the kernel ended).
 DRAM_BYTES_PER_ELEM_SOLID81 = (108.603392e6 + 123.602432e6) / 64000
 DRAM_BYTES_PER_ELEM_GATHER_K = (301.560064e6 + 62.591488e6) / 64000
-BYTES_PER_ELEM_ALGO = 2700     # compulsory HBM traffic per element (connectivity,
-                               # X/U, p, slot map, K written once, F)
 METRIC = "SOLID81 assembly Melem/s"  # Newton iterations per load step (plain vs learned) in "newton"
 UNIT = "Melem/s"
 
