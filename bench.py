@@ -256,6 +256,22 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def max_over_ranks(x, dist):
+    """The slowest rank's time (replicas: whole-job time = the max)."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(n_units_per_rank, sec, world):
+    """Whole-job throughput of `world` independent replicas, in millions of
+    units per second, from the slowest rank's time per step."""
+    return world * n_units_per_rank / sec / 1e6
+
+
 def time_steps(st, U_dev, n_total, steps, torch, stream):
     """Device-resident steps: U already in HBM; returns seconds per step."""
     ev0 = torch.cuda.Event(enable_timing=True)
@@ -271,7 +287,7 @@ def time_steps(st, U_dev, n_total, steps, torch, stream):
     return ev0.elapsed_time(ev1) / 1e3 / steps
 
 
-def run_batched(args, torch, stream, local):
+def run_batched(args, torch, stream, local, dist=None, world=1):
     """Batched workload: independent hex blocks with per-side edge counts drawn
     log-uniform in [4, 40], C10 ~ U(0.2, 1.0), K = C10 * U(500, 5000), stretch
     ~ U(1.0, 1.8); FP32 tangent / FP64 residual and CSR sums; all meshes in one
@@ -301,9 +317,10 @@ def run_batched(args, torch, stream, local):
         b.graph_launch()
     ev1.record(stream)
     torch.cuda.synchronize()
-    sec = ev0.elapsed_time(ev1) / 1e3 / args.steps
+    sec = max_over_ranks(ev0.elapsed_time(ev1) / 1e3 / args.steps, dist)
     flagged = b.element_status()[0]
-    out = {"value": b.n_elems / sec / 1e6, "unit": UNIT, "ms_per_step": sec * 1e3,
+    out = {"value": replica_throughput(b.n_elems, sec, world), "unit": UNIT,
+           "ms_per_step": sec * 1e3,
            "meshes": len(meshes), "elements": b.n_elems, "equations": b.n_total,
            "nnz_upper": b.nnz_total, "autotuned": tuned, "graph": True,
            "dtype": "f32 tangent / f64 residual, volumetric terms and CSR sums",
@@ -364,11 +381,8 @@ def run_ours(args):
     launches = st.kernel_launches() - launches0
     kt, kcount = st.kernel_times()
     st.set_timing(False)
-    if dist:
-        t = torch.tensor([sec], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        sec = float(t.item())
-    value = world * mesh.n_elems / sec / 1e6
+    sec = max_over_ranks(sec, dist)
+    value = replica_throughput(mesh.n_elems, sec, world)
 
     # e2e through the C ABI with host buffers (pinned): U in, K blocks + F out
     e2e = None
@@ -415,11 +429,8 @@ def run_ours(args):
         K_plain = Kh_np[2].copy()
         e2e_sec = time_it(e2e_step)
         assert np.array_equal(Kh_np[2], K_plain), "chunked copy differs from the plain path"
-        if dist:
-            t = torch.tensor([e2e_sec], dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_sec = float(t.item())
-        e2e = {"value": world * mesh.n_elems / e2e_sec / 1e6, "unit": UNIT,
+        e2e_sec = max_over_ranks(e2e_sec, dist)
+        e2e = {"value": replica_throughput(mesh.n_elems, e2e_sec, world), "unit": UNIT,
                "h2d_bytes_per_step": int(U.nbytes),
                "d2h_bytes_per_step": int(8 * nnz + 8 * st.n_total),
                "ms_per_step": e2e_sec * 1e3,
@@ -446,7 +457,8 @@ def run_ours(args):
         mkt, _ = sm.kernel_times()
         K64, K32 = st.K(2), sm.K(2)
         F64, F32 = st.F(), sm.F()
-        mixed = {"value": world * mesh.n_elems / msec / 1e6, "unit": UNIT,
+        msec = max_over_ranks(msec, dist)
+        mixed = {"value": replica_throughput(mesh.n_elems, msec, world), "unit": UNIT,
                  "ms_per_step": msec * 1e3, "speedup_vs_fp64": sec / msec, "autotuned": mtuned,
                  "kernel_ms": {"element": float(mkt[0]), "gather_K": float(mkt[1]),
                                "gather_F": float(mkt[2])},
@@ -457,7 +469,7 @@ def run_ours(args):
 
     batched = None
     if not args.no_batched:
-        batched = run_batched(args, torch, stream, local)
+        batched = run_batched(args, torch, stream, local, dist, world)
 
     newton = None
     if not args.no_newton and rank == 0:
