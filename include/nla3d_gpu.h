@@ -148,8 +148,19 @@ int nla3d_add_mpc(nla3d_ctx* ctx, uint32_t n_terms, const uint32_t* nodes, const
 int nla3d_build_pattern(nla3d_ctx* ctx);
 /* nla3d_build_pattern (if not done yet), device allocation and upload, and
  * the once-per-mesh Jacobian precompute.  Synchronous.  Selects the device
- * that is current at this call. */
+ * that is current at this call.  For a single mesh, the CSR pattern, slot
+ * maps and gather lists may be built on the device instead (the numbering
+ * stays on the host; same arrays, bit for bit): see nla3d_set_pattern_builder. */
 int nla3d_init_solution_data(nla3d_ctx* ctx);
+/* Where nla3d_init_solution_data builds the pattern of a single-mesh context:
+ * 0 host, 1 device, -1 (default) device for meshes of 65,536 elements or
+ * more.  A mesh beyond the device builder's limits (more than 1024 distinct
+ * columns around one node) is built on the host.  Call before
+ * nla3d_build_pattern / nla3d_init_solution_data.  No counterpart in the
+ * reference (its initSolutionData is host code, FEStorage.cpp:434-550). */
+int nla3d_set_pattern_builder(nla3d_ctx* ctx, int mode);
+/* 1 if this context's pattern was built on the device. */
+int nla3d_pattern_on_device(const nla3d_ctx* ctx);
 /* Element -> slot maps (valid after nla3d_build_pattern and until
  * nla3d_init_solution_data releases them): kslot[e * nk + c] is the index
  * into the concatenated K values (block(1) | block(1,2) | block(2)) of K

@@ -34,6 +34,7 @@ EXPORTS = [
     "nla3d_mlp_gemm", "nla3d_mlp_tanh_backward", "nla3d_mlp_column_sum", "nla3d_mlp_adam",
     "nla3d_mlp_to_bf16", "nla3d_mlp_mse_grad", "nla3d_set_contrib_layout",
     "nla3d_block_mv", "nla3d_add_mpc", "nla3d_mesh_add_mpc", "nla3d_assemble_to_host",
+    "nla3d_set_pattern_builder", "nla3d_pattern_on_device",
 ]
 
 NOALLOC_MAX_ELEMS = 15252
@@ -141,6 +142,8 @@ def load(path: str = LIB_PATH):
         "nla3d_mesh_add_mpc": ([P, ctypes.c_uint32, ctypes.c_uint32, P, P, P, ctypes.c_double],
                                ctypes.c_int),
         "nla3d_assemble_to_host": ([P, ctypes.c_int, P, P, P, P], ctypes.c_int),
+        "nla3d_set_pattern_builder": ([P, ctypes.c_int], ctypes.c_int),
+        "nla3d_pattern_on_device": ([P], ctypes.c_int),
         "nla3d_block_mv": ([P, ctypes.c_uint32, ctypes.c_int, ctypes.c_int, P, ctypes.c_double, P],
                            ctypes.c_int),
         "nla3d_graph_capture": ([P], ctypes.c_int),

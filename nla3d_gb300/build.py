@@ -22,7 +22,7 @@ LIB = os.path.join(HERE, "libnla3d_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O3",
               "-I" + os.path.join(ROOT, "include")]
-SOURCES = ["kernels.cu", "capi.cu", "host_model.cpp", "noalloc.cu", "mlp.cu"]
+SOURCES = ["kernels.cu", "capi.cu", "host_model.cpp", "noalloc.cu", "mlp.cu", "pattern_gpu.cu"]
 
 
 def nvcc() -> str:

@@ -39,6 +39,7 @@
 #include "../../include/nla3d_gpu.h"
 #include "host_model.hpp"
 #include "kernels.cuh"
+#include "pattern_gpu.hpp"
 
 using namespace nla3d_gpu;
 
@@ -90,6 +91,12 @@ struct nla3d_ctx {
   double* d_lmpc_coef = nullptr;
   ElementStatus* d_status = nullptr;
   std::vector<void*> allocs;
+  // pattern builder: 0 host, 1 device, -1 device for single meshes of at
+  // least kDevicePatternElems elements; device_pattern: the gather lists were
+  // built on the device (pd)
+  int pattern_mode = -1;
+  bool device_pattern = false;
+  PatternDevice pd;
   // walk lists of the sparse block products, built on first use:
   // per mesh, (block 1) (block 2) (block 1,2) (block 1,2 transposed)
   struct MvList {
@@ -393,6 +400,8 @@ cudaError_t enqueue_assembly(nla3d_ctx* c) {
   return cudaSuccess;
 }
 
+constexpr uint32_t kDevicePatternElems = 65536;
+
 cudaError_t enqueue_update(nla3d_ctx* c) {
   return cudaMemcpyAsync(c->d_Ustate, c->d_U, sizeof(double) * c->Utot(), cudaMemcpyDeviceToDevice,
                          c->stream);
@@ -509,6 +518,8 @@ int nla3d_add_rigid_body(nla3d_ctx* c, uint32_t master, uint32_t n_slaves, const
   return nla3d_mesh_add_rigid_body(c, 0, master, n_slaves, slaves, n_dofs, dofs);
 }
 
+static int set_offsets(nla3d_ctx* c);
+
 int nla3d_build_pattern(nla3d_ctx* c) {
   if (!c) return NLA3D_ERR_ARG;
   if (c->host_ready) return NLA3D_OK;
@@ -546,6 +557,12 @@ int nla3d_build_pattern(nla3d_ctx* c) {
                          : NLA3D_ERR_PATTERN,
                   msg);
     }
+  return set_offsets(c);
+}
+
+// offsets of the meshes in the concatenation; marks the host model ready
+static int set_offsets(nla3d_ctx* c) {
+  const size_t M = c->hm.size();
   // offsets of the concatenation
   c->elem_off.assign(M + 1, 0);
   c->node_off.assign(M + 1, 0);
@@ -583,10 +600,16 @@ int nla3d_slot_maps(const nla3d_ctx* c, uint32_t* kslot, uint32_t* fslot) {
   return NLA3D_OK;
 }
 
+int nla3d_set_pattern_builder(nla3d_ctx* c, int mode) {
+  if (!c || mode < -1 || mode > 1 || c->host_ready) return fail(c, NLA3D_ERR_ARG, "set_pattern_builder");
+  c->pattern_mode = mode;
+  return NLA3D_OK;
+}
+
+int nla3d_pattern_on_device(const nla3d_ctx* c) { return c && c->device_pattern ? 1 : 0; }
+
 int nla3d_init_solution_data(nla3d_ctx* c) {
   if (!c || c->ready) return fail(c, NLA3D_ERR_ARG, "init_solution_data: bad call order");
-  int rc = nla3d_build_pattern(c);
-  if (rc) return rc;
   cudaError_t e = cudaGetDevice(&c->device);
   if (e != cudaSuccess) return cuda_fail(c, e, "cudaGetDevice");
   if (!c->stream) {
@@ -594,6 +617,32 @@ int nla3d_init_solution_data(nla3d_ctx* c) {
     if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamCreate");
     c->own_stream = true;
   }
+  const bool device_build =
+      !c->host_ready && c->hm.size() == 1 &&
+      (c->pattern_mode == 1 || (c->pattern_mode == -1 && c->hm[0].n_elems >= kDevicePatternElems));
+  if (device_build) {
+    HostModel& m = c->hm[0];
+    std::string msg = build_host_numbering(m);
+    if (msg.empty()) {
+      DeviceAlloc alloc = [c](void** p, size_t bytes) -> cudaError_t {
+        cudaError_t err = cudaMalloc(p, bytes ? bytes : 1);
+        if (err == cudaSuccess) c->allocs.push_back(*p);
+        return err;
+      };
+      msg = build_pattern_gpu(m, c->stream, alloc, &c->pd);
+      if (msg.rfind("fallback:", 0) == 0)
+        msg = build_host_pattern(m, 0);
+      else if (msg.empty())
+        c->device_pattern = true;
+    }
+    if (!msg.empty())
+      return fail(c, msg.find("2^32") != std::string::npos || msg.find("too many") != std::string::npos
+                         ? NLA3D_ERR_RANGE : NLA3D_ERR_PATTERN, msg);
+    int rc = set_offsets(c);
+    if (rc) return rc;
+  }
+  int rc = nla3d_build_pattern(c);
+  if (rc) return rc;
   const size_t M = c->hm.size();
   const uint64_t E = c->E(), N = c->Ntot(), ntot = c->Utot(), nnz = c->Ktot(), NM = c->Mtot();
   const int npe = c->hm[0].npe;
@@ -602,7 +651,9 @@ int nla3d_init_solution_data(nla3d_ctx* c) {
   std::vector<double> xyz(3 * N);
   std::vector<uint32_t> conn(npe * E), neq3(4 * N, 0), peq(E, 0), elem_mesh;
   std::vector<double> eparams, mesh_mat;
-  std::vector<uint32_t> kptr(nnz + 1), kids(E * n_kc), fptr(ntot + 1), fids(E * n_fc);
+  const bool host_lists = !c->device_pattern;
+  std::vector<uint32_t> kptr(host_lists ? nnz + 1 : 0), kids(host_lists ? E * n_kc : 0),
+      fptr(host_lists ? ntot + 1 : 0), fids(host_lists ? E * n_fc : 0);
   if (!c->uniform_material) {
     elem_mesh.resize(E);
     mesh_mat.assign(8 * M, 0.0);
@@ -625,12 +676,14 @@ int nla3d_init_solution_data(nla3d_ctx* c) {
     }
     if (!eparams.empty())
       std::memcpy(&eparams[2 * eo], m.eparams.data(), sizeof(double) * 2 * m.n_elems);
-    for (uint64_t s = 0; s < m.nnz_total; s++) kptr[ko + s] = m.k_ptr[s] + (uint32_t)(eo * n_kc);
-    for (uint64_t k = 0; k < m.k_ids.size(); k++)
-      kids[eo * n_kc + k] = m.k_ids[k] + (uint32_t)(eo * n_kc);
-    for (uint64_t s = 0; s < m.n_total(); s++) fptr[uo + s] = m.f_ptr[s] + (uint32_t)(eo * n_fc);
-    for (uint64_t k = 0; k < m.f_ids.size(); k++)
-      fids[eo * n_fc + k] = m.f_ids[k] + (uint32_t)(eo * n_fc);
+    if (host_lists) {
+      for (uint64_t s = 0; s < m.nnz_total; s++) kptr[ko + s] = m.k_ptr[s] + (uint32_t)(eo * n_kc);
+      for (uint64_t k = 0; k < m.k_ids.size(); k++)
+        kids[eo * n_kc + k] = m.k_ids[k] + (uint32_t)(eo * n_kc);
+      for (uint64_t s = 0; s < m.n_total(); s++) fptr[uo + s] = m.f_ptr[s] + (uint32_t)(eo * n_fc);
+      for (uint64_t k = 0; k < m.f_ids.size(); k++)
+        fids[eo * n_fc + k] = m.f_ids[k] + (uint32_t)(eo * n_fc);
+    }
     if (!c->uniform_material) {
       for (uint64_t el = 0; el < m.n_elems; el++) elem_mesh[eo + el] = (uint32_t)i;
       mesh_mat[8 * i + 0] = m.mat_id;
@@ -638,12 +691,16 @@ int nla3d_init_solution_data(nla3d_ctx* c) {
       mesh_mat[8 * i + 6] = bulk_of(m);
     }
   }
-  kptr[nnz] = (uint32_t)(E * n_kc);
-  fptr[ntot] = (uint32_t)(E * n_fc);
-  // slot-order position of every contribution: the inverse of the gather ids
-  std::vector<uint32_t> kpos(E * n_kc), fpos(E * n_fc);
-  for (uint64_t k = 0; k < kids.size(); k++) kpos[kids[k]] = (uint32_t)k;
-  for (uint64_t k = 0; k < fids.size(); k++) fpos[fids[k]] = (uint32_t)k;
+  std::vector<uint32_t> kpos, fpos;
+  if (host_lists) {
+    kptr[nnz] = (uint32_t)(E * n_kc);
+    fptr[ntot] = (uint32_t)(E * n_fc);
+    // slot-order position of every contribution: the inverse of the gather ids
+    kpos.resize(E * n_kc);
+    fpos.resize(E * n_fc);
+    for (uint64_t k = 0; k < kids.size(); k++) kpos[kids[k]] = (uint32_t)k;
+    for (uint64_t k = 0; k < fids.size(); k++) fpos[fids[k]] = (uint32_t)k;
+  }
 
 #define CK(x)                                           \
   do {                                                  \
@@ -659,12 +716,21 @@ int nla3d_init_solution_data(nla3d_ctx* c) {
     CK(upload(c, &c->d_elem_mesh, elem_mesh.data(), elem_mesh.size()));
     CK(upload(c, &c->d_mesh_mat, mesh_mat.data(), mesh_mat.size()));
   }
-  CK(upload(c, &c->d_kptr, kptr.data(), kptr.size()));
-  CK(upload(c, &c->d_kids, kids.data(), kids.size()));
-  CK(upload(c, &c->d_kpos, kpos.data(), kpos.size()));
-  CK(upload(c, &c->d_fptr, fptr.data(), fptr.size()));
-  CK(upload(c, &c->d_fids, fids.data(), fids.size()));
-  CK(upload(c, &c->d_fpos, fpos.data(), fpos.size()));
+  if (host_lists) {
+    CK(upload(c, &c->d_kptr, kptr.data(), kptr.size()));
+    CK(upload(c, &c->d_kids, kids.data(), kids.size()));
+    CK(upload(c, &c->d_kpos, kpos.data(), kpos.size()));
+    CK(upload(c, &c->d_fptr, fptr.data(), fptr.size()));
+    CK(upload(c, &c->d_fids, fids.data(), fids.size()));
+    CK(upload(c, &c->d_fpos, fpos.data(), fpos.size()));
+  } else {
+    c->d_kptr = c->pd.k_ptr;
+    c->d_kids = c->pd.k_ids;
+    c->d_kpos = c->pd.k_pos;
+    c->d_fptr = c->pd.f_ptr;
+    c->d_fids = c->pd.f_ids;
+    c->d_fpos = c->pd.f_pos;
+  }
   CK(dalloc(c, &c->d_U, ntot));
   CK(dalloc(c, &c->d_Ustate, ntot));
   CK(cudaMemsetAsync(c->d_U, 0, sizeof(double) * ntot, c->stream));

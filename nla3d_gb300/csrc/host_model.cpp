@@ -108,8 +108,7 @@ std::vector<LocalPair> element_f_layout(int etype) {
   return L;  // TETRA0 assembles no F from its fresh state (TETRA0.cpp:45-76)
 }
 
-std::string build_host_model(HostModel& m, int n_threads) {
-  if (n_threads <= 0) n_threads = (int)std::max(1u, std::thread::hardware_concurrency());
+std::string build_host_numbering(HostModel& m) {
   const uint32_t N = m.n_nodes, E = m.n_elems;
   if (N < 1 && E < 1) return "No any nodes or elements";
   m.npe = m.etype == SOLID81 ? 8 : 4;
@@ -199,6 +198,79 @@ std::string build_host_model(HostModel& m, int n_threads) {
             (m.node_fix[n] & (1u << t)) ? next_const++ : next_solve++;
   for (LinearMpc& q : m.lmpcs) q.eq = next_solve++;  // FEStorage.cpp:424-426, list order
   for (MpcEq& q : m.mpcs) q.eq = next_solve++;
+  return "";
+}
+
+void mpc_extras(const HostModel& m, std::vector<uint32_t>& mpc_ptr,
+                std::vector<uint32_t>& mpc_eqs) {
+  mpc_ptr.clear();
+  mpc_eqs.clear();
+  if (!m.n_mpc) return;
+  mpc_ptr.assign((size_t)m.n_nodes * kDofTypes + 1, 0);
+  for (const MpcEq& q : m.mpcs)
+    for (int t = 0; t < 5; t++) mpc_ptr[(size_t)(q.node[t] - 1) * kDofTypes + q.dof[t] + 1]++;
+  for (const LinearMpc& q : m.lmpcs)
+    for (size_t t = 0; t < q.node.size(); t++)
+      mpc_ptr[(size_t)(q.node[t] - 1) * kDofTypes + q.dof[t] + 1]++;
+  for (size_t k = 0; k + 1 < mpc_ptr.size(); k++) mpc_ptr[k + 1] += mpc_ptr[k];
+  mpc_eqs.resize(mpc_ptr.back());
+  std::vector<uint32_t> pos(mpc_ptr.begin(), mpc_ptr.end() - 1);
+  for (const MpcEq& q : m.mpcs)
+    for (int t = 0; t < 5; t++) mpc_eqs[pos[(size_t)(q.node[t] - 1) * kDofTypes + q.dof[t]]++] = q.eq;
+  for (const LinearMpc& q : m.lmpcs)
+    for (size_t t = 0; t < q.node.size(); t++)
+      mpc_eqs[pos[(size_t)(q.node[t] - 1) * kDofTypes + q.dof[t]]++] = q.eq;
+  for (size_t k = 0; k + 1 < mpc_ptr.size(); k++) {
+    auto b = mpc_eqs.begin() + mpc_ptr[k], e = mpc_eqs.begin() + mpc_ptr[k + 1];
+    std::sort(b, e);  // ascending; duplicates removed at use
+  }
+}
+
+bool host_slot_of(const HostModel& m, uint32_t i, uint32_t j, uint32_t* out) {
+  const uint32_t nc = m.n_con;
+  if (i > j) std::swap(i, j);
+  int b;
+  if (j <= nc) {
+    b = 0;
+  } else if (i <= nc) {
+    b = 1;
+    j -= nc;
+  } else {
+    b = 2;
+    i -= nc;
+    j -= nc;
+  }
+  const CsrBlock& B = m.blk[b];
+  const uint32_t* beg = B.columns.data() + (B.iofeir[i - 1] - 1);
+  const uint32_t* end = B.columns.data() + (B.iofeir[i] - 1);
+  const uint32_t* p = std::lower_bound(beg, end, j);
+  if (p == end || *p != j) return false;
+  *out = (uint32_t)(m.val_off[b] + (uint64_t)(p - B.columns.data()));
+  return true;
+}
+
+std::string host_mpc_slots(HostModel& m) {
+  m.lmpc_slot.clear();
+  for (const LinearMpc& q : m.lmpcs)
+    for (size_t t = 0; t < q.node.size(); t++) {
+      uint32_t sl = 0;
+      if (!host_slot_of(m, q.eq, m.neq(q.node[t], q.dof[t]), &sl))
+        return "an MPC term has no slot in the CSR pattern";
+      m.lmpc_slot.push_back(sl);
+    }
+  m.mpc_slot.assign(m.mpcs.size() * 5, 0);
+  for (uint32_t k = 0; k < (uint32_t)m.mpcs.size(); k++)
+    for (int t = 0; t < 5; t++) {
+      const MpcEq& q = m.mpcs[k];
+      if (!host_slot_of(m, q.eq, m.neq(q.node[t], q.dof[t]), &m.mpc_slot[(size_t)k * 5 + t]))
+        return "an MPC term has no slot in the CSR pattern";
+    }
+  return "";
+}
+
+std::string build_host_pattern(HostModel& m, int n_threads) {
+  if (n_threads <= 0) n_threads = (int)std::max(1u, std::thread::hardware_concurrency());
+  const uint32_t N = m.n_nodes, E = m.n_elems;
 
   // ---- node -> element incidence (FEStorage::learnTopology) ----
   std::vector<uint32_t> inc_ptr(N + 1, 0), inc_el;
@@ -227,26 +299,7 @@ std::string build_host_model(HostModel& m, int n_threads) {
 
   // ---- MPC equations per (node, dof) ----
   std::vector<uint32_t> mpc_ptr, mpc_eqs;
-  if (m.n_mpc) {
-    mpc_ptr.assign((size_t)N * kDofTypes + 1, 0);
-    for (const MpcEq& q : m.mpcs)
-      for (int t = 0; t < 5; t++) mpc_ptr[(size_t)(q.node[t] - 1) * kDofTypes + q.dof[t] + 1]++;
-    for (const LinearMpc& q : m.lmpcs)
-      for (size_t t = 0; t < q.node.size(); t++)
-        mpc_ptr[(size_t)(q.node[t] - 1) * kDofTypes + q.dof[t] + 1]++;
-    for (size_t k = 0; k + 1 < mpc_ptr.size(); k++) mpc_ptr[k + 1] += mpc_ptr[k];
-    mpc_eqs.resize(mpc_ptr.back());
-    std::vector<uint32_t> pos(mpc_ptr.begin(), mpc_ptr.end() - 1);
-    for (const MpcEq& q : m.mpcs)
-      for (int t = 0; t < 5; t++) mpc_eqs[pos[(size_t)(q.node[t] - 1) * kDofTypes + q.dof[t]]++] = q.eq;
-    for (const LinearMpc& q : m.lmpcs)
-      for (size_t t = 0; t < q.node.size(); t++)
-        mpc_eqs[pos[(size_t)(q.node[t] - 1) * kDofTypes + q.dof[t]]++] = q.eq;
-    for (size_t k = 0; k + 1 < mpc_ptr.size(); k++) {
-      auto b = mpc_eqs.begin() + mpc_ptr[k], e = mpc_eqs.begin() + mpc_ptr[k + 1];
-      std::sort(b, e);  // ascending; duplicates removed at use
-    }
-  }
+  mpc_extras(m, mpc_ptr, mpc_eqs);
 
   // ---- pattern, row by row ----
   const uint32_t nc = m.n_con, ns = m.n_unk + m.n_mpc, ntot = m.n_total();
@@ -382,27 +435,8 @@ std::string build_host_model(HostModel& m, int n_threads) {
   m.val_off[2] = s0 + s1;
   m.nnz_total = s0 + s1 + s2;
 
-  // ---- slot lookup: (eq_i, eq_j) -> index in the concatenated values ----
   auto slot_of = [&](uint32_t i, uint32_t j, uint32_t* out) -> bool {
-    if (i > j) std::swap(i, j);
-    int b;
-    if (j <= nc) {
-      b = 0;
-    } else if (i <= nc) {
-      b = 1;
-      j -= nc;
-    } else {
-      b = 2;
-      i -= nc;
-      j -= nc;
-    }
-    const CsrBlock& B = m.blk[b];
-    const uint32_t* beg = B.columns.data() + (B.iofeir[i - 1] - 1);
-    const uint32_t* end = B.columns.data() + (B.iofeir[i] - 1);
-    const uint32_t* p = std::lower_bound(beg, end, j);
-    if (p == end || *p != j) return false;
-    *out = (uint32_t)(m.val_off[b] + (uint64_t)(p - B.columns.data()));
-    return true;
+    return host_slot_of(m, i, j, out);
   };
 
   // ---- element -> slot maps ----
@@ -460,22 +494,13 @@ std::string build_host_model(HostModel& m, int n_threads) {
   invert(fslot, ntot, m.n_fc, m.f_ptr, m.f_ids);
 
   // ---- MPC term slots ----
-  m.lmpc_slot.clear();
-  for (const LinearMpc& q : m.lmpcs)
-    for (size_t t = 0; t < q.node.size(); t++) {
-      uint32_t sl = 0;
-      if (!slot_of(q.eq, m.neq(q.node[t], q.dof[t]), &sl))
-        return "an MPC term has no slot in the CSR pattern";
-      m.lmpc_slot.push_back(sl);
-    }
-  m.mpc_slot.assign(m.mpcs.size() * 5, 0);
-  for (uint32_t k = 0; k < (uint32_t)m.mpcs.size(); k++)
-    for (int t = 0; t < 5; t++) {
-      const MpcEq& q = m.mpcs[k];
-      if (!slot_of(q.eq, m.neq(q.node[t], q.dof[t]), &m.mpc_slot[(size_t)k * 5 + t]))
-        return "an MPC term has no slot in the CSR pattern";
-    }
-  return "";
+  return host_mpc_slots(m);
+}
+
+std::string build_host_model(HostModel& m, int n_threads) {
+  std::string msg = build_host_numbering(m);
+  if (!msg.empty()) return msg;
+  return build_host_pattern(m, n_threads);
 }
 
 }  // namespace nla3d_gpu

@@ -99,6 +99,19 @@ struct HostModel {
 // Build DoF tables, numbering, pattern, slot maps.  Returns "" on success,
 // else a message.  n_threads <= 0 means "use the hardware concurrency".
 std::string build_host_model(HostModel& m, int n_threads);
+// The two halves of build_host_model: DoF registration, constraints and
+// equation numbers; then incidence, CSR pattern, slot maps and gather lists
+// (and the MPC term slots).
+std::string build_host_numbering(HostModel& m);
+std::string build_host_pattern(HostModel& m, int n_threads);
+// MPC equations per (node, dof): mpc_eqs[mpc_ptr[k] .. mpc_ptr[k+1]) for
+// k = (node - 1) * kDofTypes + dof, ascending (may repeat).
+void mpc_extras(const HostModel& m, std::vector<uint32_t>& mpc_ptr,
+                std::vector<uint32_t>& mpc_eqs);
+// (eq_i, eq_j) -> index in the concatenated K values of this mesh.
+bool host_slot_of(const HostModel& m, uint32_t i, uint32_t j, uint32_t* out);
+// MPC term slots from the pattern in m.blk.
+std::string host_mpc_slots(HostModel& m);
 
 // Local contribution layout of one element in the reference's assembly order:
 // for contribution c < n_kc, the (row entity dof, col entity dof) pair.

@@ -150,6 +150,16 @@ class FEStorage:
         d = np.ascontiguousarray(np.asarray(rb.dofs, dtype=np.int32))
         self._check(self.lib.nla3d_add_rigid_body(self.h, rb.master, s.size, _p(s), d.size, _p(d)))
 
+    def set_pattern_builder(self, mode):
+        """Where initSolutionData builds the pattern: "host", "device" or
+        "auto" (device for single meshes of >= 65,536 elements)."""
+        self._check(self.lib.nla3d_set_pattern_builder(self.h, {"host": 0, "device": 1,
+                                                                 "auto": -1}[mode]))
+        return self
+
+    def pattern_on_device(self):
+        return bool(self.lib.nla3d_pattern_on_device(self.h))
+
     def buildPattern(self):
         """Host-only: initDofs + assignEquationNumbers + the CSR pattern and slot maps."""
         self._check(self.lib.nla3d_build_pattern(self.h))
