@@ -90,7 +90,9 @@ typedef struct {
   const uint32_t* conn;       /* nodes_per_elem * n_elems, 1-based node ids, host     */
   int32_t mat_id;             /* NLA3D_MAT_* (SOLID81, PLANE41), 0 otherwise          */
   double mat_c[5];
-  const double* elem_params;  /* 2 * n_elems: TETRA0 (E, my), QUADTH (k, 0); or NULL */
+  const double* elem_params;  /* n_elem_params * n_elems: TETRA0 (E, my), QUADTH (k,
+                                 volFlux[, rho, c]); or NULL                          */
+  int32_t n_elem_params;      /* 2 (also when 0) or 4 (QUADTH with rho, c)            */
 } nla3d_mesh_desc;
 
 /* Create a model (FEStorage with nodes, elements and material).  `precision`
@@ -132,6 +134,25 @@ void* nla3d_get_stream(const nla3d_ctx* ctx);
 int nla3d_add_fix(nla3d_ctx* ctx, uint32_t n, const uint32_t* nodes, const int32_t* dofs);
 int nla3d_add_rigid_body(nla3d_ctx* ctx, uint32_t master, uint32_t n_slaves,
                          const uint32_t* slaves, uint32_t n_dofs, const int32_t* dofs);
+/* SurfaceLINETH elements (QUADTH.cpp:70-125) of a single-mesh QUADTH
+ * context: n lines of 2 nodes (conn, 1-based) with convection coefficient
+ * htc, flux and environment temperatures etemp (2 per line; a zero second
+ * value takes the first, as SurfaceLINETH::pre does).  They are numbered
+ * after the QUADTH elements, as when created after them.  Before
+ * nla3d_init_solution_data. */
+int nla3d_add_surface_lines(nla3d_ctx* ctx, uint32_t n, const uint32_t* conn, const double* htc,
+                            const double* flux, const double* etemp);
+/* FEStorage::setTransient (FEStorage.h:127): each assembly also builds the
+ * capacity matrix C and the mass matrix M on K's pattern (FEStorage.cpp:63-76).
+ * Of the element types here only QUADTH builds C (QUADTH.cpp:51-67) and none
+ * builds M, so M is zero; other types abort in the reference and are refused
+ * here (NLA3D_ERR_ELEMENT).  Before nla3d_init_solution_data. */
+int nla3d_set_transient(nla3d_ctx* ctx, int on);
+/* Values of C or M, block 1 / 12 / 2 (as nla3d_get_K), after an assembly of
+ * a transient context. */
+int nla3d_get_C(nla3d_ctx* ctx, int block, double* values);
+int nla3d_get_M(nla3d_ctx* ctx, int block, double* values);
+
 /* A linear MPC equation sum_t coefs[t] * u(nodes[t], dofs[t]) = b (an Mpc
  * with these terms passed to FEStorage::addMpc, as readCdbFile builds it from
  * a CE record, FEReaders.cpp:549-573).  Its equation comes after the DoFs, in

@@ -34,7 +34,8 @@ EXPORTS = [
     "nla3d_mlp_gemm", "nla3d_mlp_tanh_backward", "nla3d_mlp_column_sum", "nla3d_mlp_adam",
     "nla3d_mlp_to_bf16", "nla3d_mlp_mse_grad", "nla3d_set_contrib_layout",
     "nla3d_block_mv", "nla3d_add_mpc", "nla3d_mesh_add_mpc", "nla3d_assemble_to_host",
-    "nla3d_set_pattern_builder", "nla3d_pattern_on_device",
+    "nla3d_set_pattern_builder", "nla3d_pattern_on_device", "nla3d_add_surface_lines",
+    "nla3d_set_transient", "nla3d_get_C", "nla3d_get_M",
 ]
 
 NOALLOC_MAX_ELEMS = 15252
@@ -73,6 +74,7 @@ class MeshDesc(ctypes.Structure):
         ("mat_id", ctypes.c_int32),
         ("mat_c", ctypes.c_double * 5),
         ("elem_params", ctypes.c_void_p),
+        ("n_elem_params", ctypes.c_int32),
     ]
 
 
@@ -143,6 +145,10 @@ def load(path: str = LIB_PATH):
                                ctypes.c_int),
         "nla3d_assemble_to_host": ([P, ctypes.c_int, P, P, P, P], ctypes.c_int),
         "nla3d_set_pattern_builder": ([P, ctypes.c_int], ctypes.c_int),
+        "nla3d_add_surface_lines": ([P, ctypes.c_uint32, P, P, P, P], ctypes.c_int),
+        "nla3d_set_transient": ([P, ctypes.c_int], ctypes.c_int),
+        "nla3d_get_C": ([P, ctypes.c_int, P], ctypes.c_int),
+        "nla3d_get_M": ([P, ctypes.c_int, P], ctypes.c_int),
         "nla3d_pattern_on_device": ([P], ctypes.c_int),
         "nla3d_block_mv": ([P, ctypes.c_uint32, ctypes.c_int, ctypes.c_int, P, ctypes.c_double, P],
                            ctypes.c_int),

@@ -29,9 +29,12 @@ class BatchAssembly:
         self._keep = []
         descs = (_lib.MeshDesc * len(self.meshes))()
         for i, m in enumerate(self.meshes):
+            if (m.lines is not None and m.lines.n) or m.transient:
+                raise ValueError("surface lines and transient C, M are single-mesh (FEStorage) "
+                                 "features")
             xyz = np.ascontiguousarray(m.xyz, dtype=np.float64)
             conn = np.ascontiguousarray(m.conn, dtype=np.uint32)
-            ep = None if m.elem_params is None else np.ascontiguousarray(m.elem_params, np.float64)
+            ep, n_ep = mg.elem_params_array(m)
             self._keep += [xyz, conn, ep]
             d = descs[i]
             d.elem_type, d.n_nodes, d.n_elems = m.elem_type, m.n_nodes, m.n_elems
@@ -39,6 +42,7 @@ class BatchAssembly:
             for k, c in enumerate(m.mat_c[:5]):
                 d.mat_c[k] = c
             d.elem_params = _p(ep)
+            d.n_elem_params = n_ep
         h = ctypes.c_void_p()
         rc = self.lib.nla3d_create_batch(descs, len(self.meshes), prec, ctypes.byref(h))
         if rc:

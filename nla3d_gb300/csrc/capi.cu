@@ -82,6 +82,14 @@ struct nla3d_ctx {
   double* d_mesh_mat = nullptr;
   uint32_t* d_mpc_u32 = nullptr;  // master, slave, eq, slave_eq, master_eq6 (6), slot (5)
   int32_t* d_mpc_dof = nullptr;
+  // SurfaceLINETH lines (single-mesh QUADTH contexts) and transient C / M
+  uint32_t n_lines = 0;
+  uint32_t* d_line_conn = nullptr;
+  double* d_line_par = nullptr;
+  bool transient = false;
+  double* d_contribC = nullptr;
+  double* d_C = nullptr;
+  double* d_M = nullptr;
   // linear MPC equations of all meshes: eq, ptr (n + 1), slot (terms); b, coef
   uint64_t n_lmpc = 0;
   uint32_t* d_lmpc_eq = nullptr;
@@ -223,6 +231,8 @@ int check_mesh(const nla3d_mesh_desc* mesh) {
   if (hyper && (mesh->mat_id < NLA3D_MAT_NEO_HOOKEAN || mesh->mat_id > NLA3D_MAT_MOONEY_RIVLIN))
     return NLA3D_ERR_ARG;
   if (!hyper && !mesh->elem_params && mesh->n_elems) return NLA3D_ERR_ARG;
+  const int np = mesh->n_elem_params ? mesh->n_elem_params : 2;
+  if (np != 2 && !(np == 4 && mesh->elem_type == NLA3D_QUADTH)) return NLA3D_ERR_ARG;
   return NLA3D_OK;
 }
 
@@ -235,8 +245,13 @@ void fill_model(HostModel& m, const nla3d_mesh_desc* mesh) {
   m.conn.assign(mesh->conn, mesh->conn + (size_t)m.npe * mesh->n_elems);
   m.mat_id = mesh->mat_id;
   for (int i = 0; i < 5; i++) m.mat_c[i] = mesh->mat_c[i];
-  if (mesh->elem_params)
-    m.eparams.assign(mesh->elem_params, mesh->elem_params + 2 * (size_t)mesh->n_elems);
+  if (mesh->elem_params) {
+    // stored kElemParams per element, missing trailing values zero
+    const int np = mesh->n_elem_params ? mesh->n_elem_params : 2;
+    m.eparams.assign((size_t)kElemParams * mesh->n_elems, 0.0);
+    for (size_t e = 0; e < mesh->n_elems; e++)
+      for (int i = 0; i < np; i++) m.eparams[kElemParams * e + i] = mesh->elem_params[np * e + i];
+  }
 }
 
 double bulk_of(const HostModel& m) {
@@ -308,10 +323,19 @@ cudaError_t enqueue_elements(nla3d_ctx* c, uint32_t e0, uint32_t e1) {
   } else {
     LinearArgs a{m0.etype, e1, c->d_xyz, c->d_conn, c->d_eparams, c->d_contribK,
                  c->d_contribF, c->d_status, c->layout ? c->d_kpos : nullptr,
-                 c->layout ? c->d_fpos : nullptr, e0};
+                 c->layout ? c->d_fpos : nullptr, e0, c->transient ? c->d_contribC : nullptr};
     e = launch_linear(a, c->stream);
   }
   if (e == cudaSuccess && e1 > e0) c->launches++;
+  if (e == cudaSuccess && c->n_lines && e1 == (uint32_t)c->E()) {
+    // the lines are created after the elements: they go with the last range
+    LineArgs la{c->n_lines, c->d_xyz, c->d_line_conn, c->d_line_par,
+                (uint64_t)c->E() * m0.n_kc, (uint64_t)c->E() * m0.n_fc,
+                c->layout ? c->d_kpos : nullptr, c->layout ? c->d_fpos : nullptr,
+                c->d_contribK, c->d_contribF, c->d_status, (uint32_t)c->E() + 1};
+    e = launch_lines(la, c->stream);
+    if (e == cudaSuccess) c->launches++;
+  }
   return e;
 }
 
@@ -374,6 +398,18 @@ cudaError_t enqueue_mpc(nla3d_ctx* c) {
   return e;
 }
 
+// C of a transient context with the K slots' gather lists (FEStorage.cpp:63-76:
+// zeroC, buildC over the elements); M stays zero (no element here builds it)
+cudaError_t enqueue_gather_C(nla3d_ctx* c) {
+  if (!c->transient) return cudaSuccess;
+  GatherArgs gc{c->Ktot(), c->d_kptr, c->d_kids, c->d_contribC, c->d_C};
+  SegSumArgs sc{c->Ktot(), c->d_kptr, c->d_contribC, c->d_C};
+  cudaError_t e = c->layout ? launch_segsum(sc, c->gather_bs, c->stream)
+                            : launch_gather_bs(gc, c->gather_bs, c->stream);
+  if (e == cudaSuccess) c->launches++;
+  return e;
+}
+
 cudaError_t reset_status(nla3d_ctx* c) {
   cudaError_t e = cudaMemsetAsync(c->d_status, 0, sizeof(ElementStatus), c->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(&c->d_status->first, 0xFF, sizeof(uint32_t), c->stream);
@@ -391,6 +427,7 @@ cudaError_t enqueue_assembly(nla3d_ctx* c) {
   if ((e = enqueue_elements(c, 0, (uint32_t)c->E())) != cudaSuccess) return e;
   mark(1);
   if ((e = enqueue_gather_K(c, 0, c->Ktot())) != cudaSuccess) return e;
+  if ((e = enqueue_gather_C(c)) != cudaSuccess) return e;
   mark(2);
   if ((e = enqueue_gather_F(c)) != cudaSuccess) return e;
   mark(3);
@@ -480,6 +517,54 @@ int nla3d_mesh_add_fix(nla3d_ctx* c, uint32_t mesh, uint32_t n, const uint32_t* 
 
 int nla3d_add_fix(nla3d_ctx* c, uint32_t n, const uint32_t* nodes, const int32_t* dofs) {
   return nla3d_mesh_add_fix(c, 0, n, nodes, dofs);
+}
+
+int nla3d_add_surface_lines(nla3d_ctx* c, uint32_t n, const uint32_t* conn, const double* htc,
+                            const double* flux, const double* etemp) {
+  if (!c || c->host_ready || c->hm.size() != 1 || c->hm[0].etype != NLA3D_QUADTH ||
+      (n && (!conn || !htc || !flux || !etemp)))
+    return fail(c, NLA3D_ERR_ARG, "add_surface_lines: single-mesh QUADTH contexts");
+  HostModel& m = c->hm[0];
+  for (uint32_t l = 0; l < n; l++) {
+    m.line_conn.push_back(conn[2 * l]);
+    m.line_conn.push_back(conn[2 * l + 1]);
+    // SurfaceLINETH::pre (QUADTH.cpp:79-82): etemp[1] = etemp[0] when etemp[1] is 0
+    const double t0 = etemp[2 * l], t1 = etemp[2 * l + 1] == 0.0 ? t0 : etemp[2 * l + 1];
+    const double par[4] = {htc[l], flux[l], t0, t1};
+    m.line_par.insert(m.line_par.end(), par, par + 4);
+  }
+  return NLA3D_OK;
+}
+
+int nla3d_set_transient(nla3d_ctx* c, int on) {
+  if (!c || c->ready) return fail(c, NLA3D_ERR_ARG, "set_transient after init_solution_data");
+  if (on)
+    for (const HostModel& m : c->hm)
+      if (m.etype != NLA3D_QUADTH)
+        return fail(c, NLA3D_ERR_ELEMENT, "transient C, M: only QUADTH builds them "
+                                          "(Element::buildC/buildM abort, element.cpp:63-70)");
+  c->transient = on != 0;
+  return NLA3D_OK;
+}
+
+static int get_CM(nla3d_ctx* c, const double* src, int block, double* values, const char* what) {
+  const int b = block_slot(block);
+  if (!c || !c->ready || b < 0 || !c->transient) return fail(c, NLA3D_ERR_ARG, what);
+  const uint64_t n = c->hm[0].blk[b].nnz();
+  if (!n) return NLA3D_OK;
+  if (!values) return fail(c, NLA3D_ERR_ARG, what);
+  cudaError_t e = cudaMemcpyAsync(values, src + c->hm[0].val_off[b], sizeof(double) * n,
+                                  cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  return e == cudaSuccess ? NLA3D_OK : cuda_fail(c, e, what);
+}
+
+int nla3d_get_C(nla3d_ctx* c, int block, double* values) {
+  return get_CM(c, c ? c->d_C : nullptr, block, values, "get_C");
+}
+
+int nla3d_get_M(nla3d_ctx* c, int block, double* values) {
+  return get_CM(c, c ? c->d_M : nullptr, block, values, "get_M");
 }
 
 int nla3d_mesh_add_mpc(nla3d_ctx* c, uint32_t mesh, uint32_t n_terms, const uint32_t* nodes,
@@ -618,7 +703,7 @@ int nla3d_init_solution_data(nla3d_ctx* c) {
     c->own_stream = true;
   }
   const bool device_build =
-      !c->host_ready && c->hm.size() == 1 &&
+      !c->host_ready && c->hm.size() == 1 && c->hm[0].line_conn.empty() &&
       (c->pattern_mode == 1 || (c->pattern_mode == -1 && c->hm[0].n_elems >= kDevicePatternElems));
   if (device_build) {
     HostModel& m = c->hm[0];
@@ -647,18 +732,21 @@ int nla3d_init_solution_data(nla3d_ctx* c) {
   const uint64_t E = c->E(), N = c->Ntot(), ntot = c->Utot(), nnz = c->Ktot(), NM = c->Mtot();
   const int npe = c->hm[0].npe;
   const uint64_t n_kc = c->hm[0].n_kc, n_fc = c->hm[0].n_fc;
+  // contributions: the elements', then (single-mesh QUADTH) the surface lines'
+  const uint64_t LN = c->hm[0].n_lines();
+  const uint64_t CK_tot = E * n_kc + LN * kLineKc, CF_tot = E * n_fc + LN * kLineFc;
   // concatenated host arrays with global offsets
   std::vector<double> xyz(3 * N);
   std::vector<uint32_t> conn(npe * E), neq3(4 * N, 0), peq(E, 0), elem_mesh;
   std::vector<double> eparams, mesh_mat;
   const bool host_lists = !c->device_pattern;
-  std::vector<uint32_t> kptr(host_lists ? nnz + 1 : 0), kids(host_lists ? E * n_kc : 0),
-      fptr(host_lists ? ntot + 1 : 0), fids(host_lists ? E * n_fc : 0);
+  std::vector<uint32_t> kptr(host_lists ? nnz + 1 : 0), kids(host_lists ? CK_tot : 0),
+      fptr(host_lists ? ntot + 1 : 0), fids(host_lists ? CF_tot : 0);
   if (!c->uniform_material) {
     elem_mesh.resize(E);
     mesh_mat.assign(8 * M, 0.0);
   }
-  if (!c->hm[0].eparams.empty()) eparams.resize(2 * E);
+  if (!c->hm[0].eparams.empty()) eparams.resize((size_t)kElemParams * E);
   for (size_t i = 0; i < M; i++) {
     const HostModel& m = c->hm[i];
     const uint64_t eo = c->elem_off[i], no = c->node_off[i], uo = c->u_off[i], ko = c->k_off[i];
@@ -675,7 +763,8 @@ int nla3d_init_solution_data(nla3d_ctx* c) {
       peq[eo + el] = q ? q + (uint32_t)uo : 0;
     }
     if (!eparams.empty())
-      std::memcpy(&eparams[2 * eo], m.eparams.data(), sizeof(double) * 2 * m.n_elems);
+      std::memcpy(&eparams[kElemParams * eo], m.eparams.data(),
+                  sizeof(double) * kElemParams * m.n_elems);
     if (host_lists) {
       for (uint64_t s = 0; s < m.nnz_total; s++) kptr[ko + s] = m.k_ptr[s] + (uint32_t)(eo * n_kc);
       for (uint64_t k = 0; k < m.k_ids.size(); k++)
@@ -693,11 +782,11 @@ int nla3d_init_solution_data(nla3d_ctx* c) {
   }
   std::vector<uint32_t> kpos, fpos;
   if (host_lists) {
-    kptr[nnz] = (uint32_t)(E * n_kc);
-    fptr[ntot] = (uint32_t)(E * n_fc);
+    kptr[nnz] = (uint32_t)CK_tot;
+    fptr[ntot] = (uint32_t)CF_tot;
     // slot-order position of every contribution: the inverse of the gather ids
-    kpos.resize(E * n_kc);
-    fpos.resize(E * n_fc);
+    kpos.resize(CK_tot);
+    fpos.resize(CF_tot);
     for (uint64_t k = 0; k < kids.size(); k++) kpos[kids[k]] = (uint32_t)k;
     for (uint64_t k = 0; k < fids.size(); k++) fpos[fids[k]] = (uint32_t)k;
   }
@@ -735,11 +824,26 @@ int nla3d_init_solution_data(nla3d_ctx* c) {
   CK(dalloc(c, &c->d_Ustate, ntot));
   CK(cudaMemsetAsync(c->d_U, 0, sizeof(double) * ntot, c->stream));
   CK(cudaMemsetAsync(c->d_Ustate, 0, sizeof(double) * ntot, c->stream));
-  CK(dalloc(c, &c->d_contribK, E * n_kc));
-  CK(dalloc(c, &c->d_contribF, E * (n_fc ? n_fc : 1)));
+  CK(dalloc(c, &c->d_contribK, CK_tot));
+  CK(dalloc(c, &c->d_contribF, CF_tot ? CF_tot : 1));
   CK(dalloc(c, &c->d_K, nnz));
   CK(dalloc(c, &c->d_F, ntot));
   CK(dalloc(c, &c->d_status, 1));
+  if (LN) {
+    c->n_lines = (uint32_t)LN;
+    CK(upload(c, &c->d_line_conn, c->hm[0].line_conn.data(), c->hm[0].line_conn.size()));
+    CK(upload(c, &c->d_line_par, c->hm[0].line_par.data(), c->hm[0].line_par.size()));
+  }
+  if (c->transient) {
+    // C and M share K's pattern (FEStorage.cpp:475-479); no element of this
+    // set builds M, so M stays zero; the lines add nothing to C
+    CK(dalloc(c, &c->d_contribC, CK_tot));
+    CK(cudaMemsetAsync(c->d_contribC, 0, sizeof(double) * CK_tot, c->stream));
+    CK(dalloc(c, &c->d_C, nnz));
+    CK(dalloc(c, &c->d_M, nnz));
+    CK(cudaMemsetAsync(c->d_C, 0, sizeof(double) * (nnz ? nnz : 1), c->stream));
+    CK(cudaMemsetAsync(c->d_M, 0, sizeof(double) * (nnz ? nnz : 1), c->stream));
+  }
   if (NM) {
     // per MPC: master, slave, eq, slave_eq, master_eq6[6], slot[5]  (15 words), global
     std::vector<uint32_t> w(15ull * NM);
@@ -1074,6 +1178,7 @@ int nla3d_assemble_to_host(nla3d_ctx* c, int n_chunks, double* K1, double* K12, 
       e = enqueue_gather_K(c, runs[ri].s0, runs[ri].s1);
       ri++;
     }
+    if (e == cudaSuccess && k == n - 1) where = "C gather", e = enqueue_gather_C(c);
     if (e == cudaSuccess && k == n - 1) where = "F gather", e = enqueue_gather_F(c);
     if (e == cudaSuccess && k == n - 1) where = "MPC rows", e = enqueue_mpc(c);
     if (r0 == ri && k < n - 1) continue;  // nothing to copy after this range

@@ -123,6 +123,12 @@ std::string build_host_numbering(HostModel& m) {
                             : m.etype == PLANE41 ? (uint8_t)((1u << UX) | (1u << UY))
                                               : (uint8_t)((1u << UX) | (1u << UY) | (1u << UZ));
   for (uint64_t i = 0; i < (uint64_t)E * m.npe; i++) m.node_mask[m.conn[i] - 1] |= node_bits;
+  // SurfaceLINETH::pre (QUADTH.cpp:70-83): TEMP on the line's nodes
+  if (m.n_lines() && m.etype != QUADTH) return "surface lines need a QUADTH mesh";
+  for (uint32_t n : m.line_conn) {
+    if (n < 1 || n > N) return "surface line connectivity refers to a missing node";
+    m.node_mask[n - 1] |= (uint8_t)(1u << TEMP);
+  }
   if (m.etype == SOLID81 || m.etype == PLANE41)
     for (uint32_t e = 0; e < E; e++) m.elem_mask[e] = (uint8_t)(1u << HYDRO_PRESSURE);
   m.mpcs.clear();
@@ -306,8 +312,24 @@ std::string build_host_pattern(HostModel& m, int n_threads) {
   // per equation row: counts per destination block
   std::vector<uint32_t> cnt_lo(ntot + 1, 0), cnt_hi(ntot + 1, 0);  // (block1 or block2), block(1,2)
 
+  // node -> surface lines
+  const uint32_t Lc = m.n_lines();
+  std::vector<uint32_t> lptr(Lc ? N + 1 : 0, 0), lel;
+  if (Lc) {
+    for (uint32_t n : m.line_conn) lptr[n]++;
+    for (uint32_t n = 0; n < N; n++) lptr[n + 1] += lptr[n];
+    lel.resize(lptr[N]);
+    std::vector<uint32_t> pos(lptr.begin(), lptr.end() - 1);
+    for (uint32_t l = 0; l < Lc; l++) lel[pos[m.line_conn[2 * l] - 1]++] = l;
+    for (uint32_t l = 0; l < Lc; l++)
+      if (m.line_conn[2 * l + 1] != m.line_conn[2 * l]) lel[pos[m.line_conn[2 * l + 1] - 1]++] = l;
+  }
+
   auto node_row_cols = [&](uint32_t n /*1-based*/, std::vector<uint32_t>& cand) {
     cand.clear();
+    if (Lc)
+      for (uint32_t k = lptr[n - 1]; k < lptr[n]; k++)
+        for (int a = 0; a < 2; a++) cand.push_back(m.neq(m.line_conn[2 * lel[k] + a], TEMP));
     for (uint32_t k = inc_ptr[n - 1]; k < inc_ptr[n]; k++) {
       const uint32_t el = inc_el[k];
       for (int t = 0; t < kDofTypes; t++)
@@ -444,11 +466,13 @@ std::string build_host_pattern(HostModel& m, int n_threads) {
   const std::vector<LocalPair> FL = element_f_layout(m.etype);
   m.n_kc = (int)KL.size();
   m.n_fc = (int)FL.size();
-  if ((uint64_t)E * (m.n_kc + m.n_fc) >= 0xFFFFFFF0ull) return "too many element contributions";
+  if ((uint64_t)E * (m.n_kc + m.n_fc) + (uint64_t)Lc * (kLineKc + kLineFc) >= 0xFFFFFFF0ull)
+    return "too many element contributions";
   std::vector<uint32_t>& kslot = m.kslot;
   std::vector<uint32_t>& fslot = m.fslot;
-  kslot.assign((size_t)E * m.n_kc, 0);
-  fslot.assign((size_t)E * m.n_fc, 0);
+  // contributions of the lines follow the elements' (the lines are created after them)
+  kslot.assign((size_t)E * m.n_kc + (size_t)Lc * kLineKc, 0);
+  fslot.assign((size_t)E * m.n_fc + (size_t)Lc * kLineFc, 0);
   std::atomic<int> bad(0);
   parallel_for(E, n_threads, [&](uint64_t b, uint64_t e) {
     for (uint64_t i = b; i < e; i++) {
@@ -464,6 +488,17 @@ std::string build_host_pattern(HostModel& m, int n_threads) {
       for (int k = 0; k < m.n_fc; k++) fslot[i * m.n_fc + k] = eqof(FL[k].ei, FL[k].ti) - 1;
     }
   });
+  // surface lines: assembleK(MatSym<2>, Vec<2>, {TEMP}) order (element.h:356-386)
+  for (uint32_t l = 0; l < Lc; l++) {
+    const uint32_t qa = m.neq(m.line_conn[2 * l], TEMP), qb = m.neq(m.line_conn[2 * l + 1], TEMP);
+    const uint64_t kb = (uint64_t)E * m.n_kc + (uint64_t)l * kLineKc;
+    if (!slot_of(qa, qa, &kslot[kb]) || !slot_of(qa, qb, &kslot[kb + 1]) ||
+        !slot_of(qb, qb, &kslot[kb + 2]))
+      bad = 1;
+    const uint64_t fb = (uint64_t)E * m.n_fc + (uint64_t)l * kLineFc;
+    fslot[fb] = qa - 1;
+    fslot[fb + 1] = qb - 1;
+  }
   if (bad) return "an element contribution has no slot in the CSR pattern";
 
   // ---- inverse: gather lists in ascending contribution order ----

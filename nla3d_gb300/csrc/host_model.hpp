@@ -12,6 +12,9 @@
 namespace nla3d_gpu {
 
 constexpr int kDofTypes = 8;  // Dof::numberOfDofTypes (Dof.h:15-25)
+constexpr int kElemParams = 4;  // per-element parameters stored per element
+constexpr int kLineKc = 3;      // K contributions of a SurfaceLINETH line
+constexpr int kLineFc = 2;      // F contributions of a SurfaceLINETH line
 enum DofType { UX = 0, UY, UZ, ROTX, ROTY, ROTZ, HYDRO_PRESSURE, TEMP };
 enum ElemType { PLANE41 = 1, SOLID81 = 2, TETRA0 = 3, QUADTH = 5 };
 
@@ -62,7 +65,12 @@ struct HostModel {
   std::vector<uint32_t> conn;
   int mat_id = 0;
   double mat_c[5] = {0, 0, 0, 0, 0};
-  std::vector<double> eparams;
+  std::vector<double> eparams;  // kElemParams per element: TETRA0 (E, my, 0, 0),
+                                // QUADTH (k, volFlux, rho, c)
+  // SurfaceLINETH line elements of a QUADTH mesh (QUADTH.cpp:70-125), created
+  // after the quads: 2 node ids and (htc, flux, etemp0, etemp1) per line
+  std::vector<uint32_t> line_conn;
+  std::vector<double> line_par;
   // constraints and MPC
   std::vector<uint32_t> fix_node;
   std::vector<int> fix_dof;
@@ -92,6 +100,7 @@ struct HostModel {
   std::vector<uint32_t> lmpc_slot;
 
   uint32_t n_total() const { return n_dofs + n_mpc; }
+  uint32_t n_lines() const { return (uint32_t)(line_conn.size() / 2); }
   uint32_t neq(uint32_t node, int t) const { return node_eq[(size_t)(node - 1) * kDofTypes + t]; }
   uint32_t eeq(uint32_t el, int t) const { return elem_eq[(size_t)(el - 1) * kDofTypes + t]; }
 };

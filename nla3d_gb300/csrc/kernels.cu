@@ -697,7 +697,8 @@ __global__ void linear_kernel(const LinearArgs a) {
     }
     const double vol = det4_lu(S) / 6.0;
     if (!(vol > 0.0)) flag_element(a.status, e + 1);
-    const double Em = a.eparams[2 * (uint64_t)e], my = a.eparams[2 * (uint64_t)e + 1];
+    const double Em = a.eparams[kEparamStride * (uint64_t)e];
+    const double my = a.eparams[kEparamStride * (uint64_t)e + 1];
     const double Ac = Em / ((1. + my) * (1. - 2. * my));
     // C (6x6, makeC) as dense
     double Cm[6][6] = {};
@@ -747,9 +748,11 @@ __global__ void linear_kernel(const LinearArgs a) {
         a.contribK[a.kpos ? a.kpos[i] : i] = v * vol;
       }
   } else {
-    // QUADTH: 2x2 Gauss (isoparametric.h:80-85), conduction k (QUADTH.cpp:22-49)
-    const double kc = a.eparams[2 * (uint64_t)e];
-    double Ke[10] = {};
+    // QUADTH: 2x2 Gauss (isoparametric.h:80-85), conduction k and volume flux
+    // (QUADTH.cpp:22-49), capacity rho c for transient analysis (:51-67)
+    const double* ep = a.eparams + kEparamStride * (uint64_t)e;
+    const double kc = ep[0], vflux = ep[1], rho = ep[2], cap = ep[3];
+    double Ke[10] = {}, Ce[10] = {}, Fe[4] = {};
     for (int g = 0; g < 4; g++) {
       const double r = (g & 1) ? kGaussA : -kGaussA;
       const double s = (g & 2) ? kGaussA : -kGaussA;
@@ -757,6 +760,8 @@ __global__ void linear_kernel(const LinearArgs a) {
                                {+0.25 * (1.0 - s), -0.25 * (1.0 + r)},
                                {+0.25 * (1.0 + s), +0.25 * (1.0 + r)},
                                {-0.25 * (1.0 + s), +0.25 * (1.0 - r)}};
+      const double N[4] = {0.25 * (1.0 - r) * (1.0 - s), 0.25 * (1.0 + r) * (1.0 - s),
+                           0.25 * (1.0 + r) * (1.0 + s), 0.25 * (1.0 - r) * (1.0 + s)};
       double J[2][2] = {};
       for (int n = 0; n < 4; n++)
         for (int i = 0; i < 2; i++)
@@ -771,17 +776,72 @@ __global__ void linear_kernel(const LinearArgs a) {
       const double w = 1.0 * det;
       int idx = 0;
       for (int i = 0; i < 4; i++)
-        for (int j = i; j < 4; j++, idx++)
+        for (int j = i; j < 4; j++, idx++) {
           Ke[idx] += (G[i][0] * kc * G[j][0] + G[i][1] * kc * G[j][1]) * w;
+          Ce[idx] = __dadd_rn(Ce[idx], __dmul_rn(N[i] * N[j] * rho * cap, w));
+        }
+      if (vflux != 0.0)
+        for (int i = 0; i < 4; i++) Fe[i] = __dadd_rn(Fe[i], __dmul_rn(N[i], vflux * w));
     }
     for (int i = 0; i < 10; i++) {
       const uint64_t k = (uint64_t)e * 10 + i;
       a.contribK[a.kpos ? a.kpos[k] : k] = Ke[i];
+      if (a.contribC) a.contribC[a.kpos ? a.kpos[k] : k] = Ce[i];
     }
-    for (int i = 0; i < 4; i++) {  // volFlux = 0 (QUADTH.cpp:34-36)
+    for (int i = 0; i < 4; i++) {
       const uint64_t k = (uint64_t)e * 4 + i;
-      a.contribF[a.fpos ? a.fpos[k] : k] = 0.0;
+      a.contribF[a.fpos ? a.fpos[k] : k] = Fe[i];
     }
+  }
+}
+
+// SurfaceLINETH::buildK (QUADTH.cpp:86-121): 2-point Gauss on the line
+// (isoparametric.h:47-50), w = det = length / 2 (isoparametric.cpp:12-26);
+// flux: F += N flux w; convection: K += N N^T htc w and F += (N N^T htc w) T_env.
+__global__ void line_kernel(const LineArgs a) {
+  const uint32_t l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= a.n_lines) return;
+  const uint32_t na = a.conn[2 * (uint64_t)l], nb = a.conn[2 * (uint64_t)l + 1];
+  double d2 = 0.0;
+  for (int k = 0; k < 3; k++) {
+    const double d = a.xyz[(uint64_t)(nb - 1) * 3 + k] - a.xyz[(uint64_t)(na - 1) * 3 + k];
+    d2 += d * d;
+  }
+  const double det = sqrt(d2) * 0.5;
+  if (!(det > 0.0)) flag_element(a.status, a.first_elem + l);
+  const double* par = a.par + 4 * (uint64_t)l;
+  const double htc = par[0], flux = par[1], t0 = par[2], t1 = par[3];
+  double Ke[3] = {0.0, 0.0, 0.0}, Fe[2] = {0.0, 0.0};
+  const double w = 1.0 * det;
+  // the flux loop runs over both points before the convection loop, and F
+  // takes each product separately (matBVprod, Mat.h), as the reference adds
+  if (flux != 0.0)
+    for (int g = 0; g < 2; g++) {
+      const double r = g ? kGaussA : -kGaussA;
+      const double N0 = 0.5 * (1.0 - r), N1 = 0.5 * (1.0 + r);
+      Fe[0] = __dadd_rn(Fe[0], __dmul_rn(N0, flux * w));
+      Fe[1] = __dadd_rn(Fe[1], __dmul_rn(N1, flux * w));
+    }
+  if (htc != 0.0)
+    for (int g = 0; g < 2; g++) {
+      const double r = g ? kGaussA : -kGaussA;
+      const double N0 = 0.5 * (1.0 - r), N1 = 0.5 * (1.0 + r);
+      const double k00 = N0 * N0 * htc * w, k01 = N0 * N1 * htc * w, k11 = N1 * N1 * htc * w;
+      Ke[0] += k00;
+      Ke[1] += k01;
+      Ke[2] += k11;
+      Fe[0] = __dadd_rn(Fe[0], __dmul_rn(k00, t0));
+      Fe[0] = __dadd_rn(Fe[0], __dmul_rn(k01, t1));
+      Fe[1] = __dadd_rn(Fe[1], __dmul_rn(k01, t0));
+      Fe[1] = __dadd_rn(Fe[1], __dmul_rn(k11, t1));
+    }
+  for (int i = 0; i < 3; i++) {
+    const uint64_t k = a.k_off + 3 * (uint64_t)l + i;
+    a.contribK[a.kpos ? a.kpos[k] : k] = Ke[i];
+  }
+  for (int i = 0; i < 2; i++) {
+    const uint64_t k = a.f_off + 2 * (uint64_t)l + i;
+    a.contribF[a.fpos ? a.fpos[k] : k] = Fe[i];
   }
 }
 
@@ -974,6 +1034,13 @@ cudaError_t launch_mpc(const MpcArgs& a, cudaStream_t s) {
   if (a.n_mpc == 0) return cudaSuccess;
   const int bs = 128;
   mpc_kernel<<<(a.n_mpc + bs - 1) / bs, bs, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lines(const LineArgs& a, cudaStream_t s) {
+  if (a.n_lines == 0) return cudaSuccess;
+  const int bs = 128;
+  line_kernel<<<(a.n_lines + bs - 1) / bs, bs, 0, s>>>(a);
   return cudaGetLastError();
 }
 

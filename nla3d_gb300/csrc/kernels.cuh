@@ -79,18 +79,39 @@ struct MpcArgs {
   double* F;
 };
 
+constexpr int kEparamStride = 4;  // per-element parameters: TETRA0 (E, my, -, -),
+                                  // QUADTH (k, volFlux, rho, c)
+
 struct LinearArgs {
   int etype;
   uint32_t n_elems;
   const double* xyz;
   const uint32_t* conn;
-  const double* eparams;
+  const double* eparams;           // kEparamStride per element
   double* contribK;
   double* contribF;
   ElementStatus* status;
   const uint32_t* kpos;  // optional slot-ordered output (as Solid81Args)
   const uint32_t* fpos;
   uint32_t e_begin;      // element range [e_begin, n_elems)
+  double* contribC;      // QUADTH capacity contributions [E * 10] (transient), or null
+};
+
+// SurfaceLINETH (QUADTH.cpp:86-121): convection and flux on 2-node lines,
+// one thread per line; K contributions (0,0), (0,1), (1,1) at contribK[k_off
+// + 3 l + c], F contributions at contribF[f_off + 2 l + c].
+struct LineArgs {
+  uint32_t n_lines;
+  const double* xyz;
+  const uint32_t* conn;    // 2 node ids per line
+  const double* par;       // (htc, flux, etemp0, etemp1) per line
+  uint64_t k_off, f_off;
+  const uint32_t* kpos;
+  const uint32_t* fpos;
+  double* contribK;
+  double* contribF;
+  ElementStatus* status;
+  uint32_t first_elem;     // element number of line 0 (for the status word)
 };
 
 // PLANE41 (PLANE41.cpp:29-146): 4-node plane-strain u/p quad, one thread per
@@ -185,6 +206,7 @@ cudaError_t launch_slot_last_range(uint64_t n_slots, const uint32_t* ptr, const 
 cudaError_t launch_linear_mpc(const LinearMpcArgs& a, cudaStream_t s);
 cudaError_t launch_linear(const LinearArgs& a, cudaStream_t s);
 cudaError_t launch_plane41(const Plane41Args& a, cudaStream_t s);
+cudaError_t launch_lines(const LineArgs& a, cudaStream_t s);
 size_t solid81_smem_bytes(bool mixed);
 cudaError_t probe_fma_peak(bool fp64, double* flops);
 

@@ -52,17 +52,34 @@ class LinearMpc:
 
 
 @dataclasses.dataclass
+class SurfaceLines:
+    """SurfaceLINETH elements (QUADTH.h:38-55) on a QUADTH mesh: convection
+    (htc, environment temperatures etemp) and flux over 2-node lines."""
+    conn: np.ndarray            # (n, 2) uint32, 1-based node ids
+    htc: np.ndarray             # (n,) float64
+    flux: np.ndarray            # (n,) float64
+    etemp: np.ndarray           # (n, 2) float64 (a zero second value takes the first)
+
+    @property
+    def n(self) -> int:
+        return int(self.conn.shape[0])
+
+
+@dataclasses.dataclass
 class Mesh:
     elem_type: int
     xyz: np.ndarray             # (n_nodes, 3) float64
     conn: np.ndarray            # (n_elems, nodes_per_elem) uint32, 1-based
     mat_id: int = 0
     mat_c: tuple = ()
-    elem_params: np.ndarray | None = None   # (n_elems, 2) float64 (TETRA0: E, my; QUADTH: k, 0)
+    # (n_elems, 2..4) float64: TETRA0 (E, my); QUADTH (k[, volFlux, rho, c])
+    elem_params: np.ndarray | None = None
     fix_nodes: np.ndarray | None = None     # uint32 1-based
     fix_dofs: np.ndarray | None = None      # int32 Dof types
     rigid_bodies: list = dataclasses.field(default_factory=list)
     mpcs: list = dataclasses.field(default_factory=list)   # LinearMpc, numbered first
+    lines: SurfaceLines | None = None       # created after the elements
+    transient: bool = False                 # FEStorage::setTransient: assemble C, M too
     name: str = ""
 
     @property
@@ -76,6 +93,24 @@ class Mesh:
     @property
     def bulk_modulus(self) -> float:
         return float(self.mat_c[-1]) if self.mat_c else 0.0
+
+
+def elem_params_array(mesh: "Mesh"):
+    """(contiguous float64 array, columns) of the mesh's element parameters as
+    the library takes them: 2 columns (TETRA0 E, my; QUADTH k, volFlux) or 4
+    (QUADTH k, volFlux, rho, c); other widths are zero-padded to the next."""
+    if mesh.elem_params is None:
+        return None, 0
+    ep = np.asarray(mesh.elem_params, dtype=np.float64)
+    if ep.ndim == 1:
+        ep = ep[:, None]
+    c = ep.shape[1]
+    if c > 4:
+        raise ValueError("at most 4 element parameters")
+    width = 2 if c <= 2 else 4
+    if c < width:
+        ep = np.concatenate([ep, np.zeros((ep.shape[0], width - c))], axis=1)
+    return np.ascontiguousarray(ep), width
 
 
 def hex_block(nx: int, ny: int, nz: int, h=1.0) -> tuple[np.ndarray, np.ndarray]:
@@ -186,6 +221,37 @@ def quadth_plate(nx, ny, h=1.0, k=1.0, fix_x0=True, name="") -> Mesh:
         edge = np.nonzero(np.abs(xyz[:, 0]) < 1e-12)[0].astype(np.uint32) + 1
         m.fix_nodes = edge
         m.fix_dofs = np.full(edge.size, TEMP, dtype=np.int32)
+    return m
+
+
+def quadth_thermal_plate(nx, ny, h=0.1, seed=0, transient=False, name="") -> Mesh:
+    """QUADTH plate with the thermal loads of the reference's heat-transfer
+    model: per-element conductivity k and volume flux (and rho, c when
+    transient), convection lines (htc, etemp) on the top edge and flux lines on
+    the right edge; interior nodes jittered so that no two elements are equal."""
+    m = quadth_plate(nx, ny, h=h, k=1.0, name=name or f"quadth_thermal_{nx}x{ny}")
+    rng = np.random.default_rng(seed)
+    ep = np.zeros((m.n_elems, 4 if transient else 2))
+    ep[:, 0] = 10.0 + 5.0 * rng.random(m.n_elems)
+    ep[:, 1] = np.where(rng.random(m.n_elems) < 0.5, 0.0, 1.0e3 * rng.random(m.n_elems))
+    if transient:
+        ep[:, 2] = 7800.0
+        ep[:, 3] = 460.0 + 10.0 * rng.random(m.n_elems)
+    m.elem_params = ep
+    inner = (m.xyz[:, 0] > 1e-12) & (m.xyz[:, 0] < nx * h - 1e-12) & \
+            (m.xyz[:, 1] > 1e-12) & (m.xyz[:, 1] < ny * h - 1e-12)
+    m.xyz[inner, :2] += rng.uniform(-0.2 * h, 0.2 * h, (int(inner.sum()), 2))
+    top = [1 + i + (nx + 1) * ny for i in range(nx + 1)]
+    right = [1 + nx + (nx + 1) * j for j in range(ny + 1)]
+    conn = [(top[i + 1], top[i]) for i in range(nx)] + [(right[j], right[j + 1])
+                                                        for j in range(ny)]
+    htc = np.r_[25.0 + rng.random(nx), np.zeros(ny)]
+    flux = np.r_[np.zeros(nx), 300.0 + 50.0 * rng.random(ny)]
+    et = np.zeros((nx + ny, 2))
+    et[:nx, 0] = 20.0 + rng.random(nx)
+    et[:nx:2, 1] = 35.0          # every other line: its own second temperature
+    m.lines = SurfaceLines(np.array(conn, np.uint32), htc, flux, et)
+    m.transient = transient
     return m
 
 

@@ -84,9 +84,7 @@ class FEStorage:
         prec = {"fp64": _lib.PREC_FP64, "mixed": _lib.PREC_MIXED}[precision]
         self._xyz = np.ascontiguousarray(mesh.xyz, dtype=np.float64)
         self._conn = np.ascontiguousarray(mesh.conn, dtype=np.uint32)
-        self._ep = None
-        if mesh.elem_params is not None:
-            self._ep = np.ascontiguousarray(mesh.elem_params, dtype=np.float64)
+        self._ep, n_ep = mg.elem_params_array(mesh)
         d = _lib.MeshDesc()
         d.elem_type = mesh.elem_type
         d.n_nodes = mesh.n_nodes
@@ -97,12 +95,14 @@ class FEStorage:
         for i, c in enumerate(mesh.mat_c[:5]):
             d.mat_c[i] = c
         d.elem_params = _p(self._ep)
+        d.n_elem_params = n_ep
         h = ctypes.c_void_p()
         rc = self.lib.nla3d_create(ctypes.byref(d), prec, ctypes.byref(h))
         if rc:
             raise _lib.Nla3dError(rc, "nla3d_create rejected the mesh")
         self.h = h
         self.ready = False
+        self.transient = False
         if stream is not None:
             self._check(self.lib.nla3d_set_stream(self.h, ctypes.c_void_p(stream)))
         if mesh.fix_nodes is not None and len(mesh.fix_nodes):
@@ -111,6 +111,10 @@ class FEStorage:
             self.addMpc(q)
         for rb in mesh.rigid_bodies:
             self.addMpcCollection(rb)
+        if mesh.lines is not None and mesh.lines.n:
+            self.add_surface_lines(mesh.lines)
+        if mesh.transient:
+            self.setTransient(True)
 
     # ---- lifecycle ----
     def _check(self, rc):
@@ -149,6 +153,21 @@ class FEStorage:
         s = np.ascontiguousarray(rb.slaves, dtype=np.uint32)
         d = np.ascontiguousarray(np.asarray(rb.dofs, dtype=np.int32))
         self._check(self.lib.nla3d_add_rigid_body(self.h, rb.master, s.size, _p(s), d.size, _p(d)))
+
+    def add_surface_lines(self, lines: mg.SurfaceLines):
+        """SurfaceLINETH elements (convection htc to etemp, flux) created after
+        the QUADTH elements."""
+        c = np.ascontiguousarray(lines.conn, dtype=np.uint32)
+        h = np.ascontiguousarray(lines.htc, dtype=np.float64)
+        f = np.ascontiguousarray(lines.flux, dtype=np.float64)
+        t = np.ascontiguousarray(lines.etemp, dtype=np.float64)
+        self._check(self.lib.nla3d_add_surface_lines(self.h, lines.n, _p(c), _p(h), _p(f),
+                                                     _p(t)))
+
+    def setTransient(self, on: bool = True):
+        """FEStorage::setTransient: assembly also builds C and M on K's pattern."""
+        self._check(self.lib.nla3d_set_transient(self.h, 1 if on else 0))
+        self.transient = bool(on)
 
     def set_pattern_builder(self, mode):
         """Where initSolutionData builds the pattern: "host", "device" or
@@ -256,6 +275,20 @@ class FEStorage:
     def F(self):
         v = np.zeros(self.n_total)
         self._check(self.lib.nla3d_get_F(self.h, _p(v)))
+        return v
+
+    def C(self, block):
+        """Capacity matrix values of a transient storage (K's pattern)."""
+        v = np.zeros(self.blocks[block][2])
+        if v.size:
+            self._check(self.lib.nla3d_get_C(self.h, block, _p(v)))
+        return v
+
+    def M(self, block):
+        """Mass matrix values of a transient storage (K's pattern)."""
+        v = np.zeros(self.blocks[block][2])
+        if v.size:
+            self._check(self.lib.nla3d_get_M(self.h, block, _p(v)))
         return v
 
     def getK(self):

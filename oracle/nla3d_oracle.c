@@ -30,6 +30,9 @@
 enum { UX = 0, UY, UZ, ROTX, ROTY, ROTZ, HYDRO_PRESSURE, TEMP };
 enum { ET_PLANE41 = 1, ET_SOLID81 = 2, ET_TETRA0 = 3, ET_QUADTH = 5 };
 enum { MAT_NH = 1, MAT_BID = 2, MAT_MR = 3 };
+/* element parameters kept per element: TETRA0 (E, my), QUADTH (k, volFlux,
+ * rho, c) (TETRA0.h, QUADTH.h:29-35) */
+#define EPAR 4
 static const uint32_t INVALID = 0xFFFFFFFFu; /* SparseMatrix.cpp:11 */
 
 /* ----------------------------------------------------------------------- */
@@ -499,6 +502,15 @@ struct orc_model {
   double* lm_coef;
   double* lm_b;
   uint32_t* lm_eq;
+  /* SurfaceLINETH elements (QUADTH.h:38-55), numbered after the n_elems
+   * elements: line_conn 2 per line, line_par (htc, flux, etemp0, etemp1) */
+  uint32_t n_lines;
+  uint32_t* line_conn;
+  double* line_par;
+  /* FEStorage::setTransient: C and M on K's pattern (FEStorage.cpp:475-480) */
+  int transient;
+  double* cval[3];
+  double* mval[3];
   /* global system */
   csr_block blk[3]; /* block(1), block(1,2), block(2) */
   double* U;
@@ -526,7 +538,7 @@ static int fail(orc_model* m, const char* fmt, ...) {
 
 orc_model* orc_new(int elem_type, uint32_t n_nodes, const double* xyz, uint32_t n_elems,
                    const uint32_t* conn, int mat_id, const double* mat_c, int n_mat_c,
-                   const double* elem_params) {
+                   const double* elem_params, int n_elem_params) {
   orc_model* m = (orc_model*)calloc(1, sizeof(orc_model));
   m->etype = elem_type;
   m->npe = elem_type == ET_SOLID81 ? 8 : 4;
@@ -538,14 +550,21 @@ orc_model* orc_new(int elem_type, uint32_t n_nodes, const double* xyz, uint32_t 
   memcpy(m->xyz, xyz, sizeof(double) * 3 * n_nodes);
   m->conn = (uint32_t*)malloc(sizeof(uint32_t) * m->npe * (n_elems ? n_elems : 1));
   memcpy(m->conn, conn, sizeof(uint32_t) * m->npe * n_elems);
-  m->eparams = (double*)calloc(2 * (n_elems ? n_elems : 1), sizeof(double));
-  if (elem_params) memcpy(m->eparams, elem_params, sizeof(double) * 2 * n_elems);
+  m->eparams = (double*)calloc((size_t)EPAR * (n_elems ? n_elems : 1), sizeof(double));
+  if (elem_params && n_elem_params > 0)
+    for (uint32_t e = 0; e < n_elems; e++)
+      for (int k = 0; k < n_elem_params && k < EPAR; k++)
+        m->eparams[(size_t)e * EPAR + k] = elem_params[(size_t)e * n_elem_params + k];
   return m;
 }
 
 void orc_free(orc_model* m) {
   if (!m) return;
   free(m->xyz); free(m->conn); free(m->eparams);
+  free(m->line_conn); free(m->line_par);
+  for (int b = 0; b < 3; b++) {
+    free(m->cval[b]); free(m->mval[b]);
+  }
   free(m->node_mask); free(m->elem_mask); free(m->node_fix); free(m->node_eq); free(m->elem_eq);
   free(m->fix_node); free(m->fix_dof);
   for (uint32_t i = 0; i < m->n_rbs; i++) free(m->rbs[i].slaves);
@@ -708,12 +727,26 @@ static int add_entry(orc_model* m, uint32_t i, uint32_t j) {
   return blk_add_entry(m, &m->blk[b], i, j);
 }
 
-static int add_value(orc_model* m, uint32_t i, uint32_t j, double v) {
+/* value arrays: NULL = K's own; C and M share K's pattern (FEStorage.cpp:475-480) */
+static int add_value_to(orc_model* m, double** vals, uint32_t i, uint32_t j, double v) {
   int b = route(m, &i, &j);
   uint32_t idx = blk_index(&m->blk[b], i, j);
   if (idx == INVALID) return fail(m, "The position(%u, %u) is absent in the matrix", i, j);
-  m->blk[b].values[idx] += v;
+  (vals ? vals[b] : m->blk[b].values)[idx] += v;
   return 0;
+}
+
+static int add_value(orc_model* m, uint32_t i, uint32_t j, double v) {
+  return add_value_to(m, NULL, i, j, v);
+}
+
+/* nodes of element en (1-based): the n_elems elements, then the lines */
+static inline int elem_npe(const orc_model* m, uint32_t en) {
+  return en <= m->n_elems ? m->npe : 2;
+}
+static inline uint32_t elem_node(const orc_model* m, uint32_t en, int a) {
+  if (en <= m->n_elems) return m->conn[(size_t)(en - 1) * m->npe + a];
+  return m->line_conn[2 * (size_t)(en - 1 - m->n_elems) + a];
 }
 
 static inline uint32_t neq(const orc_model* m, uint32_t node, int dof) {
@@ -724,13 +757,15 @@ static inline uint32_t eeq(const orc_model* m, uint32_t el, int dof) {
 }
 
 int orc_setup(orc_model* m, uint32_t max_in_row) {
-  const uint32_t N = m->n_nodes, E = m->n_elems;
+  const uint32_t N = m->n_nodes, E = m->n_elems, L = m->n_lines, EL = E + L;
   if (N < 1 && E < 1) return fail(m, "No any nodes or elements");
+  if (m->transient && m->etype != ET_QUADTH)
+    return fail(m, "transient: only QUADTH builds C and M here");
   m->node_mask = (uint8_t*)calloc(N + 1, 1);
-  m->elem_mask = (uint8_t*)calloc(E + 1, 1);
+  m->elem_mask = (uint8_t*)calloc(EL + 1, 1);
   m->node_fix = (uint8_t*)calloc(N + 1, 1);
   m->node_eq = (uint32_t*)calloc((size_t)(N + 1) * NDOFT, sizeof(uint32_t));
-  m->elem_eq = (uint32_t*)calloc((size_t)(E + 1) * NDOFT, sizeof(uint32_t));
+  m->elem_eq = (uint32_t*)calloc((size_t)(EL + 1) * NDOFT, sizeof(uint32_t));
 
   /* --- Element::pre(): DoF registration and element state (SOLID81.cpp:12-26,
    *     TETRA0.cpp:10-14, QUADTH.cpp:12-20) --- */
@@ -747,6 +782,16 @@ int orc_setup(orc_model* m, uint32_t max_in_row) {
     }
     if (m->etype == ET_SOLID81 || m->etype == ET_PLANE41)
       m->elem_mask[e] |= 1u << HYDRO_PRESSURE;
+  }
+  /* SurfaceLINETH::pre (QUADTH.cpp:73-84): TEMP on both nodes; a zero second
+   * environment temperature takes the first */
+  for (uint32_t l = 0; l < L; l++) {
+    for (int a = 0; a < 2; a++) {
+      const uint32_t n = m->line_conn[2 * l + a];
+      if (n < 1 || n > N) return fail(m, "line %u: bad node id", l + 1);
+      m->node_mask[n - 1] |= 1u << TEMP;
+    }
+    if (m->line_par[4 * l + 3] == 0.0) m->line_par[4 * l + 3] = m->line_par[4 * l + 2];
   }
   if (m->etype == ET_SOLID81) {
     m->np = 8;
@@ -865,17 +910,18 @@ int orc_setup(orc_model* m, uint32_t max_in_row) {
   m->U = (double*)calloc(ntot + 1, sizeof(double));
   m->F = (double*)calloc(ntot + 1, sizeof(double));
 
-  /* learnTopology: node -> ascending element ids (FEStorage.cpp:580-589) */
+  /* learnTopology: node -> ascending element ids (FEStorage.cpp:580-589);
+   * the lines are elements E+1 .. E+L */
   uint32_t* cnt = (uint32_t*)calloc(N + 1, sizeof(uint32_t));
-  for (uint32_t e = 0; e < E; e++)
-    for (int a = 0; a < m->npe; a++) cnt[m->conn[(size_t)e * m->npe + a]]++;
+  for (uint32_t e = 0; e < EL; e++)
+    for (int a = 0; a < elem_npe(m, e + 1); a++) cnt[elem_node(m, e + 1, a)]++;
   for (uint32_t n = 1; n <= N; n++) cnt[n] += cnt[n - 1];
   uint32_t* topo = (uint32_t*)malloc(sizeof(uint32_t) * (cnt[N] + 1));
   uint32_t* fillp = (uint32_t*)malloc(sizeof(uint32_t) * (N + 1));
   memcpy(fillp, cnt, sizeof(uint32_t) * (N + 1));
-  for (uint32_t e = 0; e < E; e++)
-    for (int a = 0; a < m->npe; a++) {
-      uint32_t n = m->conn[(size_t)e * m->npe + a];
+  for (uint32_t e = 0; e < EL; e++)
+    for (int a = 0; a < elem_npe(m, e + 1); a++) {
+      uint32_t n = elem_node(m, e + 1, a);
       uint32_t* beg = topo + cnt[n - 1];
       int dup = 0;
       for (uint32_t* p = beg; p < topo + fillp[n - 1]; p++) dup |= (*p == e + 1);
@@ -891,8 +937,8 @@ int orc_setup(orc_model* m, uint32_t max_in_row) {
         if (me & (1u << t1))
           for (int t2 = 0; t2 < NDOFT; t2++)
             if (mn & (1u << t2)) rc |= add_entry(m, eeq(m, en, t1), neq(m, nn, t2));
-      for (int a = 0; a < m->npe; a++) {
-        uint32_t nn2 = m->conn[(size_t)(en - 1) * m->npe + a];
+      for (int a = 0; a < elem_npe(m, en); a++) {
+        uint32_t nn2 = elem_node(m, en, a);
         if (nn2 < nn) continue;
         const uint8_t m2 = m->node_mask[nn2 - 1];
         for (int t1 = 0; t1 < NDOFT; t1++)
@@ -920,6 +966,11 @@ int orc_setup(orc_model* m, uint32_t max_in_row) {
     }
   if (rc) return 1;
   for (int b = 0; b < 3; b++) blk_compress(&m->blk[b]);
+  if (m->transient)
+    for (int b = 0; b < 3; b++) {
+      m->cval[b] = (double*)calloc(m->blk[b].nnz ? m->blk[b].nnz : 1, sizeof(double));
+      m->mval[b] = (double*)calloc(m->blk[b].nnz ? m->blk[b].nnz : 1, sizeof(double));
+    }
   m->setup_done = 1;
   return 0;
 }
@@ -1145,7 +1196,7 @@ static int tetra0_buildK(orc_model* m, uint32_t e) {
   double Cm[21];
   memset(Cm, 0, sizeof(Cm));
   /* makeC (TETRA0.cpp:186-199); MatSym<6>::comp index = 6*i - (i-1)*i/2 + (j-i) */
-  const double E = m->eparams[2 * e], my = m->eparams[2 * e + 1];
+  const double E = m->eparams[EPAR * e], my = m->eparams[EPAR * e + 1];
   const double A = E / ((1. + my) * (1. - 2. * my));
 #define CIDX(i, j) (6 * (i) - ((i) - 1) * (i) / 2 + ((j) - (i)))
   Cm[CIDX(0, 0)] = (1. - my) * A;
@@ -1209,20 +1260,23 @@ static int tetra0_buildK(orc_model* m, uint32_t e) {
 }
 
 /* ----------------------------------------------------------------------- */
-/* QUADTH (QUADTH.cpp:22-49)                                                */
+/* QUADTH (QUADTH.cpp:22-67), SurfaceLINETH (QUADTH.cpp:70-121)           */
 /* ----------------------------------------------------------------------- */
 
 static int quadth_buildK(orc_model* m, uint32_t e) {
   double Ke[10];
   memset(Ke, 0, sizeof(Ke));
   double Fe[4] = {0, 0, 0, 0};
-  const double kc = m->eparams[2 * e];
+  const double kc = m->eparams[EPAR * e], vflux = m->eparams[EPAR * e + 1];
   const double matk[3] = {kc, 0.0, kc};
   for (int g = 0; g < 4; g++) {
     const double dWt = m->wts[g] * m->det[(size_t)e * 4 + g];
     const double* G = m->NiXj + ((size_t)e * 4 + g) * 8;
     const double Bm[8] = {G[0], G[2], G[4], G[6], G[1], G[3], G[5], G[7]};
     k_matBTDBprod(2, 4, Bm, matk, dWt, Ke);
+    /* volume flux: Fe += N (volFlux dWt) */
+    if (vflux != 0.0)
+      for (int i = 0; i < 4; i++) Fe[i] += m->Nq[g * 4 + i] * (vflux * dWt);
   }
   const uint32_t* c = m->conn + (size_t)e * 4;
   const double* Kp = Ke;
@@ -1233,6 +1287,70 @@ static int quadth_buildK(orc_model* m, uint32_t e) {
       Kp++;
     }
   for (int i = 0; i < 4; i++) m->F[neq(m, c[i], TEMP) - 1] += Fe[i];
+  return rc;
+}
+
+/* ElementQUADTH::buildC (QUADTH.cpp:51-67): Ce_ij += N_i N_j rho c dWt, then
+ * Element::assembleC (element.h:306-329) in assembleK's upper-triangle order */
+static int quadth_buildC(orc_model* m, uint32_t e) {
+  double Ce[10];
+  memset(Ce, 0, sizeof(Ce));
+  const double rho = m->eparams[EPAR * e + 2], cap = m->eparams[EPAR * e + 3];
+  for (int g = 0; g < 4; g++) {
+    const double dWt = m->wts[g] * m->det[(size_t)e * 4 + g];
+    const double* ff = m->Nq + g * 4;
+    int k = 0;
+    for (int i = 0; i < 4; i++)
+      for (int j = i; j < 4; j++, k++) Ce[k] += ff[i] * ff[j] * rho * cap * dWt;
+  }
+  const uint32_t* c = m->conn + (size_t)e * 4;
+  int rc = 0, k = 0;
+  for (int i = 0; i < 4; i++)
+    for (int j = i; j < 4; j++, k++)
+      rc |= add_value_to(m, m->cval, neq(m, c[i], TEMP), neq(m, c[j], TEMP), Ce[k]);
+  return rc;
+}
+
+/* SurfaceLINETH::buildK (QUADTH.cpp:86-121): 2-point Gauss (isoparametric.h:44-48),
+ * dWt = w * |x2 - x1| / 2 (isoparametric.cpp:13-27, Vec::length).  The flux
+ * loop runs before the convection loop; convection adds N N^T htc dWt to Ke
+ * and (N N^T htc dWt) etemp to Fe term by term (matBVprod of a MatSym, Mat.h). */
+static int line_buildK(orc_model* m, uint32_t l) {
+  const uint32_t na = m->line_conn[2 * l], nb = m->line_conn[2 * l + 1];
+  double q = 0.0;
+  for (int d = 0; d < 3; d++) {
+    const double dx = m->xyz[(size_t)(nb - 1) * 3 + d] - m->xyz[(size_t)(na - 1) * 3 + d];
+    q += dx * dx;
+  }
+  const double det = sqrt(q) * 0.5;
+  const double* par = m->line_par + 4 * (size_t)l;
+  const double htc = par[0], flux = par[1], et[2] = {par[2], par[3]};
+  double Ke[3] = {0.0, 0.0, 0.0}, Fe[2] = {0.0, 0.0};
+  const double gr[2] = {-GP_A, GP_A};
+  if (flux != 0.0)
+    for (int g = 0; g < 2; g++) {
+      const double dWt = 1.0 * det;
+      const double Ns[2] = {0.5 * (1.0 - gr[g]), 0.5 * (1.0 + gr[g])};
+      for (int i = 0; i < 2; i++) Fe[i] += Ns[i] * (flux * dWt);
+    }
+  if (htc != 0.0)
+    for (int g = 0; g < 2; g++) {
+      const double dWt = 1.0 * det;
+      const double Ns[2] = {0.5 * (1.0 - gr[g]), 0.5 * (1.0 + gr[g])};
+      const double t00 = Ns[0] * Ns[0] * htc * dWt, t01 = Ns[0] * Ns[1] * htc * dWt,
+                   t11 = Ns[1] * Ns[1] * htc * dWt;
+      Ke[0] += t00;
+      Ke[1] += t01;
+      Ke[2] += t11;
+      const double T[2][2] = {{t00, t01}, {t01, t11}};
+      for (int i = 0; i < 2; i++)
+        for (int j = 0; j < 2; j++) Fe[i] += T[i][j] * et[j] * 1.0;
+    }
+  int rc = add_value(m, neq(m, na, TEMP), neq(m, na, TEMP), Ke[0]);
+  rc |= add_value(m, neq(m, na, TEMP), neq(m, nb, TEMP), Ke[1]);
+  rc |= add_value(m, neq(m, nb, TEMP), neq(m, nb, TEMP), Ke[2]);
+  m->F[neq(m, na, TEMP) - 1] += Fe[0];
+  m->F[neq(m, nb, TEMP) - 1] += Fe[1];
   return rc;
 }
 
@@ -1461,6 +1579,7 @@ int orc_assemble(orc_model* m) {
     else
       rc |= quadth_buildK(m, e);
   }
+  for (uint32_t l = 0; l < m->n_lines && !rc; l++) rc |= line_buildK(m, l);
   if (rc) return 1;
   for (uint32_t r = 0; r < m->n_rbs; r++) rigid_body_update(m, &m->rbs[r]);
   for (uint32_t k = 0; k < m->n_lmpc; k++) {
@@ -1473,8 +1592,54 @@ int orc_assemble(orc_model* m) {
     m->F[q->eq - 1] = q->b;
     for (int t = 0; t < 5; t++) rc |= add_value(m, q->eq, neq(m, q->t[t].node, q->t[t].dof), q->t[t].coef);
   }
+  /* transient: zeroC, zeroM, buildC / buildM over the elements (FEStorage.cpp:63-76);
+   * SurfaceLINETH and buildM of QUADTH add nothing (QUADTH.h:25, :48-49) */
+  if (m->transient && !rc) {
+    for (int b = 0; b < 3; b++)
+      if (m->blk[b].nnz) {
+        memset(m->cval[b], 0, sizeof(double) * m->blk[b].nnz);
+        memset(m->mval[b], 0, sizeof(double) * m->blk[b].nnz);
+      }
+    for (uint32_t e = 0; e < m->n_elems && !rc; e++) rc |= quadth_buildC(m, e);
+  }
   return rc;
 }
+
+int orc_add_surface_lines(orc_model* m, uint32_t n, const uint32_t* conn, const double* htc,
+                          const double* flux, const double* etemp) {
+  if (m->setup_done) return fail(m, "add_surface_lines after setup");
+  if (m->etype != ET_QUADTH) return fail(m, "surface lines need a QUADTH model");
+  const uint32_t L = m->n_lines + n;
+  m->line_conn = (uint32_t*)realloc(m->line_conn, sizeof(uint32_t) * 2 * (L ? L : 1));
+  m->line_par = (double*)realloc(m->line_par, sizeof(double) * 4 * (L ? L : 1));
+  for (uint32_t i = 0; i < n; i++) {
+    const uint32_t l = m->n_lines + i;
+    m->line_conn[2 * l] = conn[2 * i];
+    m->line_conn[2 * l + 1] = conn[2 * i + 1];
+    m->line_par[4 * l + 0] = htc ? htc[i] : 0.0;
+    m->line_par[4 * l + 1] = flux ? flux[i] : 0.0;
+    m->line_par[4 * l + 2] = etemp ? etemp[2 * i] : 0.0;
+    m->line_par[4 * l + 3] = etemp ? etemp[2 * i + 1] : 0.0;
+  }
+  m->n_lines = L;
+  return 0;
+}
+
+int orc_set_transient(orc_model* m, int on) {
+  if (m->setup_done) return fail(m, "set_transient after setup");
+  m->transient = on != 0;
+  return 0;
+}
+
+static int get_cm(orc_model* m, double** vals, int block, double* values) {
+  if (!m->setup_done || !m->transient) return fail(m, "C, M: not a transient model");
+  const int b = slot_of(block);
+  if (m->blk[b].nnz) memcpy(values, vals[b], sizeof(double) * m->blk[b].nnz);
+  return 0;
+}
+
+int orc_get_C(orc_model* m, int block, double* values) { return get_cm(m, m->cval, block, values); }
+int orc_get_M(orc_model* m, int block, double* values) { return get_cm(m, m->mval, block, values); }
 
 int orc_get_K(orc_model* m, int block, double* values) {
   csr_block* b = &m->blk[slot_of(block)];

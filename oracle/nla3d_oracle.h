@@ -24,10 +24,11 @@ typedef struct orc_model orc_model;
  * mat_id: reference MaterialFactory::matId (MaterialFactory.h:12-18):
  *   1 Neo-Hookean (G, K), 2 Biderman (C10, C20, C30, C01, K),
  *   3 Mooney-Rivlin (C10, C01, K); 0 = none.
- * elem_params: two doubles per element (TETRA0: E, my; QUADTH: k, unused). */
+ * elem_params: n_elem_params doubles per element (up to 4; missing ones are 0):
+ *   TETRA0 (E, my), QUADTH (k, volFlux, rho, c) (TETRA0.h, QUADTH.h:29-35). */
 orc_model* orc_new(int elem_type, uint32_t n_nodes, const double* xyz, uint32_t n_elems,
                    const uint32_t* conn, int mat_id, const double* mat_c, int n_mat_c,
-                   const double* elem_params);
+                   const double* elem_params, int n_elem_params);
 void orc_free(orc_model* m);
 const char* orc_error(orc_model* m);
 int orc_add_fix(orc_model* m, uint32_t n, const uint32_t* nodes, const int32_t* dofs);
@@ -36,6 +37,13 @@ int orc_add_rigid_body(orc_model* m, uint32_t master, uint32_t n_slaves, const u
 /* FEStorage::addMpc of an Mpc (Mpc.h:31-36): sum coefs[t] u(nodes[t], dofs[t]) = b */
 int orc_add_mpc(orc_model* m, uint32_t n_terms, const uint32_t* nodes, const int32_t* dofs,
                 const double* coefs, double b);
+/* SurfaceLINETH elements of a QUADTH model (QUADTH.h:38-55), created after
+ * its elements: conn 2 nodes per line, htc, flux (NULL = 0) and etemp
+ * (2 per line; a zero second value takes the first, SurfaceLINETH::pre). */
+int orc_add_surface_lines(orc_model* m, uint32_t n, const uint32_t* conn, const double* htc,
+                          const double* flux, const double* etemp);
+/* FEStorage::setTransient (FEStorage.h:127): assemble C and M too. */
+int orc_set_transient(orc_model* m, int on);
 /* max_in_row: the reference's pre-compress row capacity (BlockSparseMatrix.h:42,
  * default 100); overflow is reported as an error like SparseMatrix.cpp:84. */
 int orc_setup(orc_model* m, uint32_t max_in_row);
@@ -49,6 +57,9 @@ int orc_update(orc_model* m);
 int orc_assemble(orc_model* m);
 int orc_get_K(orc_model* m, int block, double* values);
 int orc_get_F(orc_model* m, double* F);
+/* C and M of a transient model, block 1 / 12 / 2 on K's pattern. */
+int orc_get_C(orc_model* m, int block, double* values);
+int orc_get_M(orc_model* m, int block, double* values);
 /* y += coef * op(block) x on the assembled K (SparseMatrix.cpp:497-558):
  * block 1 / 2: matBVprod(SparseSymMatrix&) (both triangles, x_j with
  * |x_j| <= 1e-20 skipped; stored entries only, in the reference's order);

@@ -64,13 +64,17 @@ def _load(kind: str):
     f = lambda n: getattr(lib, pre + n)  # noqa: E731
     f("new").restype = _P
     f("new").argtypes = [ctypes.c_int, ctypes.c_uint, _P, ctypes.c_uint, _P, ctypes.c_int, _P,
-                         ctypes.c_int, _P]
+                         ctypes.c_int, _P, ctypes.c_int]
     f("free").argtypes = [_P]
     f("error").restype = ctypes.c_char_p
     f("error").argtypes = [_P]
     f("add_fix").argtypes = [_P, ctypes.c_uint, _P, _P]
     f("add_rigid_body").argtypes = [_P, ctypes.c_uint, ctypes.c_uint, _P, ctypes.c_uint, _P]
     f("add_mpc").argtypes = [_P, ctypes.c_uint, _P, _P, _P, ctypes.c_double]
+    f("add_surface_lines").argtypes = [_P, ctypes.c_uint, _P, _P, _P, _P]
+    f("set_transient").argtypes = [_P, ctypes.c_int]
+    f("get_C").argtypes = [_P, ctypes.c_int, _P]
+    f("get_M").argtypes = [_P, ctypes.c_int, _P]
     f("setup").argtypes = [_P] + ([ctypes.c_uint] if kind == "port" else [])
     f("info").argtypes = [_P, _P]
     f("pattern").argtypes = [_P, ctypes.c_int, _P, _P]
@@ -91,7 +95,8 @@ def _load(kind: str):
     f("block_mv").restype = ctypes.c_int
     f("get_F").argtypes = [_P, _P]
     for n in ("add_fix", "add_rigid_body", "add_mpc", "setup", "pattern", "eq_numbers", "set_U",
-              "update", "assemble", "get_K", "get_F"):
+              "update", "assemble", "get_K", "get_F", "add_surface_lines", "set_transient",
+              "get_C", "get_M"):
         f(n).restype = ctypes.c_int
     if kind == "port":
         lib.orc_material_S.argtypes = [ctypes.c_int, _P, _P, ctypes.c_double, _P]
@@ -127,15 +132,28 @@ class OracleModel:
         xyz = np.ascontiguousarray(mesh.xyz, dtype=np.float64)
         conn = np.ascontiguousarray(mesh.conn, dtype=np.uint32)
         mc = np.ascontiguousarray(np.asarray(mesh.mat_c, dtype=np.float64).reshape(-1))
-        ep = None
+        ep, n_ep = None, 0
         if mesh.elem_params is not None:
             ep = np.ascontiguousarray(mesh.elem_params, dtype=np.float64)
+            n_ep = int(ep.shape[1]) if ep.ndim == 2 else 1
         self._keep += [xyz, conn, mc, ep]
         self.h = self._f("new")(mesh.elem_type, mesh.n_nodes, _ptr(xyz), mesh.n_elems,
                                 _ptr(conn), mesh.mat_id, _ptr(mc) if mc.size else None,
-                                int(mc.size), _ptr(ep))
+                                int(mc.size), _ptr(ep), n_ep)
         if not self.h:
             raise OracleError("model creation failed")
+        lines = getattr(mesh, "lines", None)
+        if lines is not None and lines.n:
+            lc = np.ascontiguousarray(lines.conn, dtype=np.uint32)
+            lh = np.ascontiguousarray(lines.htc, dtype=np.float64)
+            lf = np.ascontiguousarray(lines.flux, dtype=np.float64)
+            lt = np.ascontiguousarray(lines.etemp, dtype=np.float64)
+            self._keep += [lc, lh, lf, lt]
+            self._check(self._f("add_surface_lines")(self.h, lines.n, _ptr(lc), _ptr(lh),
+                                                     _ptr(lf), _ptr(lt)))
+        self.transient = bool(getattr(mesh, "transient", False))
+        if self.transient:
+            self._check(self._f("set_transient")(self.h, 1))
         if mesh.fix_nodes is not None and len(mesh.fix_nodes):
             fn = np.ascontiguousarray(mesh.fix_nodes, dtype=np.uint32)
             fd = np.ascontiguousarray(mesh.fix_dofs, dtype=np.int32)
@@ -224,6 +242,20 @@ class OracleModel:
     def F(self):
         v = np.zeros(self.n_total)
         self._check(self._f("get_F")(self.h, _ptr(v)))
+        return v
+
+    def C(self, block):
+        """Capacity matrix block of a transient model (K's pattern)."""
+        v = np.zeros(self.blocks[block][2])
+        if v.size:
+            self._check(self._f("get_C")(self.h, block, _ptr(v)))
+        return v
+
+    def M(self, block):
+        """Mass matrix block of a transient model (K's pattern)."""
+        v = np.zeros(self.blocks[block][2])
+        if v.size:
+            self._check(self._f("get_M")(self.h, block, _ptr(v)))
         return v
 
     def block_mv(self, block, trans, x, coef, y):

@@ -45,6 +45,7 @@ void ElementFactory::createElements(ElementType elId, const uint32 n, std::vecto
       case ElementType::TETRA0: ptr.push_back(new ElementTETRA0()); break;
       case ElementType::QUADTH: ptr.push_back(new ElementQUADTH()); break;
       case ElementType::PLANE41: ptr.push_back(new ElementPLANE41()); break;
+      case ElementType::SurfaceLINETH: ptr.push_back(new SurfaceLINETH()); break;
       default: LOG(FATAL) << "element type not built into the oracle harness";
     }
   }
@@ -56,6 +57,7 @@ namespace {
 struct RefModel {
   FEStorage storage;
   ElementType type = ElementType::UNDEFINED;
+  unsigned n_model_elems = 0;  // the elements of ref_new; lines come after them
   std::vector<std::pair<uint32, int>> fixes;
   std::string err;
   double t_update = 0.0, t_assemble = 0.0;
@@ -80,13 +82,15 @@ extern "C" {
 //            5 QUADTH.
 // mat_id: reference MaterialFactory::matId (MaterialFactory.h:12-18): 1 Neo-Hookean,
 //         2 Biderman, 3 Mooney-Rivlin; 0 = no material (TETRA0 / QUADTH).
-// elem_params: per element, two doubles (TETRA0: E, my; QUADTH: k, unused).
+// elem_params: per element, n_elem_params doubles (missing ones are 0):
+//              TETRA0 (E, my), QUADTH (k, volFlux, rho, c) (QUADTH.h:29-35).
 void* ref_new(int elem_type, unsigned n_nodes, const double* xyz, unsigned n_elems,
               const unsigned* conn, int mat_id, const double* mat_c, int n_mat_c,
-              const double* elem_params) {
+              const double* elem_params, int n_elem_params) {
   RefModel* m = new RefModel();
   int rc = guarded(m, [&] {
     m->type = (ElementType)elem_type;
+    m->n_model_elems = n_elems;
     auto nind = m->storage.createNodes(n_nodes);
     for (unsigned i = 0; i < n_nodes; i++) {
       Node& nd = m->storage.getNode(nind[i]);
@@ -99,13 +103,20 @@ void* ref_new(int elem_type, unsigned n_nodes, const double* xyz, unsigned n_ele
       Element& el = m->storage.getElement(eind[e]);
       const unsigned nn = el.getNNodes();
       for (unsigned j = 0; j < nn; j++) el.getNodeNumber(j) = conn[e * nn + j];
+      auto par = [&](int k) {
+        return (elem_params && k < n_elem_params) ? elem_params[(size_t)e * n_elem_params + k]
+                                                  : 0.0;
+      };
       if (m->type == ElementType::TETRA0) {
         auto& t = dynamic_cast<ElementTETRA0&>(el);
-        t.E = elem_params[2 * e + 0];
-        t.my = elem_params[2 * e + 1];
+        t.E = par(0);
+        t.my = par(1);
       } else if (m->type == ElementType::QUADTH) {
         auto& q = dynamic_cast<ElementQUADTH&>(el);
-        q.k = elem_params[2 * e + 0];
+        q.k = par(0);
+        q.volFlux = par(1);
+        q.rho = par(2);
+        q.c = par(3);
       }
     }
     if (mat_id > 0) {
@@ -159,6 +170,31 @@ int ref_add_mpc(void* h, unsigned n_terms, const unsigned* nodes, const int* dof
   });
 }
 
+// SurfaceLINETH elements created after the model's elements (as a .cdb reader
+// or a test would): conn 2 per line, htc, flux, etemp 2 per line.
+int ref_add_surface_lines(void* h, unsigned n, const unsigned* conn, const double* htc,
+                          const double* flux, const double* etemp) {
+  RefModel* m = static_cast<RefModel*>(h);
+  return guarded(m, [&] {
+    auto ind = m->storage.createElements(n, ElementType::SurfaceLINETH);
+    for (unsigned l = 0; l < n; l++) {
+      auto& el = dynamic_cast<SurfaceLINETH&>(m->storage.getElement(ind[l]));
+      el.getNodeNumber(0) = conn[2 * l];
+      el.getNodeNumber(1) = conn[2 * l + 1];
+      el.htc = htc ? htc[l] : 0.0;
+      el.flux = flux ? flux[l] : 0.0;
+      el.etemp[0] = etemp ? etemp[2 * l] : 0.0;
+      el.etemp[1] = etemp ? etemp[2 * l + 1] : 0.0;
+    }
+  });
+}
+
+int ref_set_transient(void* h, int on) {
+  RefModel* m = static_cast<RefModel*>(h);
+  m->storage.setTransient(on != 0);
+  return 0;
+}
+
 int ref_setup(void* h) {
   RefModel* m = static_cast<RefModel*>(h);
   return guarded(m, [&] {
@@ -205,7 +241,8 @@ int ref_pattern(void* h, int block, unsigned* iofeir, unsigned* columns) {
   });
 }
 
-// Equation numbers per (entity, Dof::dofType) (Dof.h:15-25), 0 = DoF not used.
+// Equation numbers per (entity, Dof::dofType) (Dof.h:15-25), 0 = DoF not used;
+// elem_eq covers the elements of ref_new (surface lines carry no element DoF).
 int ref_eq_numbers(void* h, unsigned* node_eq, unsigned* elem_eq) {
   RefModel* m = static_cast<RefModel*>(h);
   return guarded(m, [&] {
@@ -214,7 +251,7 @@ int ref_eq_numbers(void* h, unsigned* node_eq, unsigned* elem_eq) {
       for (int t = 0; t < Dof::numberOfDofTypes; t++)
         node_eq[(n - 1) * 8 + t] = s.isNodeDofUsed(n, (Dof::dofType)t)
                                        ? s.getNodeDofEqNumber(n, (Dof::dofType)t) : 0;
-    for (uint32 e = 1; e <= s.nElements(); e++)
+    for (uint32 e = 1; e <= s.nElements() && e <= m->n_model_elems; e++)
       for (int t = 0; t < Dof::numberOfDofTypes; t++)
         elem_eq[(e - 1) * 8 + t] = s.isElementDofUsed(e, (Dof::dofType)t)
                                        ? s.getElementDofEqNumber(e, (Dof::dofType)t) : 0;
@@ -278,6 +315,26 @@ int ref_block_mv(void* h, int block, int trans, const double* x, unsigned nx, do
       matBVprod(*K->block(1, 2), X, coef, Y);
     for (unsigned i = 0; i < ny; i++) y[i] = Y[i];
   });
+}
+
+static int get_cm(RefModel* m, bool C, int block, double* values) {
+  return guarded(m, [&] {
+    if (!m->storage.isTransient()) LOG(FATAL) << "not a transient model";
+    auto* X = C ? m->storage.getC() : m->storage.getM();
+    math::BaseSparseMatrix* B = X->block(1, 2);
+    if (block == 1) B = X->block(1);
+    if (block == 2) B = X->block(2);
+    if (B->nValues() == 0) return;
+    std::memcpy(values, B->getValuesArray(), sizeof(double) * B->nValues());
+  });
+}
+
+int ref_get_C(void* h, int block, double* values) {
+  return get_cm(static_cast<RefModel*>(h), true, block, values);
+}
+
+int ref_get_M(void* h, int block, double* values) {
+  return get_cm(static_cast<RefModel*>(h), false, block, values);
 }
 
 int ref_get_F(void* h, double* F) {

@@ -107,6 +107,18 @@ def quadth_5x4():
     return m, np.zeros((m.n_nodes, 3)), None, None, False
 
 
+def quadth_lines_6x5():
+    """QUADTH with volume flux, convection and flux lines (SurfaceLINETH)."""
+    m = mg.quadth_thermal_plate(6, 5, 0.1, seed=2)
+    return m, np.zeros((m.n_nodes, 3)), None, None, False
+
+
+def quadth_transient_5x4():
+    """Transient QUADTH: K, F and the capacity matrix C (M stays zero)."""
+    m = mg.quadth_thermal_plate(5, 4, 0.1, seed=3, transient=True)
+    return m, np.zeros((m.n_nodes, 3)), None, None, False
+
+
 def cube10_nh():
     """The 10^3 unit-cube workload (1000 SOLID81, 4993 equations)."""
     mesh, u, p = mg.config_cube(10, seed=1)
@@ -116,5 +128,6 @@ def cube10_nh():
 FULL_CASES = {f.__name__: f for f in (cube3_nh, cube4_nh_clamped, mr_twist_3x2x4,
                                        biderman_3x3x3_clamped, bar_mpc_2x2x3, ce_block_3x3x2,
                                        bar_mpc_ce_2x2x3, plane41_nh_3x2, plane41_mr_4x3_clamped,
-                                       tetra0_3x3x3, quadth_5x4)}
+                                       tetra0_3x3x3, quadth_5x4, quadth_lines_6x5,
+                                       quadth_transient_5x4)}
 DIGEST_CASES = {f.__name__: f for f in (cube10_nh,)}

@@ -46,6 +46,9 @@ def run_reference(case):
         out[f"columns_{b}"] = co
         out[f"K_{b}"] = m.K(b)
         out[f"shape_{b}"] = np.array(m.blocks[b], np.uint32)
+        if mesh.transient:
+            out[f"C_{b}"] = m.C(b)
+            out[f"M_{b}"] = m.M(b)
     out.update(block_products(m))
     return out
 

@@ -40,6 +40,10 @@ def test_fp64_matches_reference_fixtures(name):
     for b in (1, 12, 2):
         assert rel(K[b], g[f"K_{b}"]) <= TOL_FP64, (b, rel(K[b], g[f"K_{b}"]))
     assert rel(F, g["F"]) <= TOL_FP64, rel(F, g["F"])
+    for b in (1, 12, 2):
+        if f"C_{b}" in g:   # transient: capacity C and mass M on K's pattern
+            assert rel(s.C(b), g[f"C_{b}"]) <= TOL_FP64, (b, rel(s.C(b), g[f"C_{b}"]))
+            assert np.array_equal(s.M(b), g[f"M_{b}"])
     assert s.element_status() == (0, 0)
 
 
@@ -82,7 +86,9 @@ def test_run_to_run_bitwise_reproducible(precision):
                                             ("cube4_nh_clamped", "mixed"),
                                             ("bar_mpc_2x2x3", "fp64"),
                                             ("tetra0_3x3x3", "fp64"),
-                                            ("quadth_5x4", "fp64")])
+                                            ("quadth_5x4", "fp64"),
+                                            ("quadth_lines_6x5", "fp64"),
+                                            ("quadth_transient_5x4", "fp64")])
 def test_contribution_layouts_bitwise_equal(name, precision):
     """Element-ordered and slot-ordered contributions sum each slot in the
     same order, so K and F agree to the bit."""
@@ -96,7 +102,8 @@ def test_contribution_layouts_bitwise_equal(name, precision):
         if do_update:
             s.updateResults()
         s.assembleGlobalEqMatrices()
-        out.append([s.K(b).copy() for b in (1, 12, 2)] + [s.F().copy()])
+        out.append([s.K(b).copy() for b in (1, 12, 2)] + [s.F().copy()] +
+                   ([s.C(b) for b in (1, 12, 2)] if s.transient else []))
     for x, y in zip(*out):
         assert np.array_equal(x.view(np.uint64), y.view(np.uint64))
 
@@ -162,6 +169,7 @@ def test_larger_mesh_properties():
                                             ("bar_mpc_2x2x3", "fp64"),
                                             ("ce_block_3x3x2", "fp64"),
                                             ("tetra0_3x3x3", "fp64"),
+                                            ("quadth_transient_5x4", "fp64"),
                                             ("twist16", "fp64"), ("twist16", "mixed")])
 def test_assemble_to_host_equals_assemble_then_copy(name, precision):
     """nla3d_assemble_to_host (element ranges, each finished K prefix copied
@@ -180,8 +188,35 @@ def test_assemble_to_host_equals_assemble_then_copy(name, precision):
         s.updateResults()
     s.assembleGlobalEqMatrices()
     want = [s.K(b) for b in (1, 12, 2)] + [s.F()]
+    wantC = [s.C(b) for b in (1, 12, 2)] if s.transient else []
     for n_chunks in (1, 3, 8, 64):
         got = [np.full(s.blocks[b][2], np.nan) for b in (1, 12, 2)] + [np.full(s.n_total, np.nan)]
         s.assemble_to_host(*got, n_chunks=n_chunks)
-        for x, y in zip(want, got):
+        gotC = [s.C(b) for b in (1, 12, 2)] if s.transient else []
+        for x, y in zip(want + wantC, got + gotC):
             assert np.array_equal(x.view(np.uint64), y.view(np.uint64)), n_chunks
+
+
+@pytest.mark.parametrize("transient", [False, True])
+def test_thermal_plate_with_lines_vs_oracle(transient):
+    """A 40x30 QUADTH plate with volume flux, convection and flux lines (and
+    the capacity matrix when transient) against the oracle at 1e-12.  A
+    context with surface lines builds its pattern on the host even when the
+    device builder is asked for."""
+    mesh = mg.quadth_thermal_plate(40, 30, 0.05, seed=7, transient=transient)
+    for builder in ("host", "device"):
+        s = FEStorage(mesh).set_pattern_builder(builder).initSolutionData()
+        assert not s.pattern_on_device()
+        o = O.OracleModel(mesh, "port")
+        U = np.random.default_rng(2).standard_normal(s.n_total)
+        s.setU(U)
+        s.assembleGlobalEqMatrices()
+        o.set_U(U)
+        o.assemble()
+        for b in (1, 12, 2):
+            assert np.array_equal(s.pattern(b)[1], o.pattern(b)[1])
+            assert rel(s.K(b), o.K(b)) <= TOL_FP64
+            if transient:
+                assert rel(s.C(b), o.C(b)) <= TOL_FP64
+                assert not np.any(s.M(b))
+        assert rel(s.F(), o.F()) <= TOL_FP64

@@ -39,6 +39,11 @@ def test_device_pattern_equals_host_pattern(name):
     mesh, u, p, extra, do_update = cases.FULL_CASES[name]()
     host = _assemble(mesh, u, p, extra, do_update, "host")
     dev = _assemble(mesh, u, p, extra, do_update, "device")
+    if mesh.lines is not None:
+        # surface lines are handled by the host builder only: the request
+        # for the device builder falls back to it
+        assert not dev.pattern_on_device()
+        return
     assert dev.pattern_on_device()
     _same(host, dev)
 

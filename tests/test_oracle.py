@@ -50,6 +50,9 @@ def test_port_matches_reference_goldens_bit_exact(name):
         assert np.array_equal(io, g[f"iofeir_{b}"])
         assert np.array_equal(co, g[f"columns_{b}"])
         assert np.array_equal(_bits(m.K(b)), _bits(g[f"K_{b}"])), f"K block {b}"
+        if f"C_{b}" in g:
+            assert np.array_equal(_bits(m.C(b)), _bits(g[f"C_{b}"])), f"C block {b}"
+            assert np.array_equal(_bits(m.M(b)), _bits(g[f"M_{b}"])), f"M block {b}"
     assert np.array_equal(_bits(m.F()), _bits(g["F"]))
 
 
@@ -202,3 +205,32 @@ def test_isoparametric_hexahedron_invariants():
             assert abs(float((weights[n] * det).sum()) - 16.0) < th
     for (Ga, da, n), (Gb, db, _) in zip(_hex(arb), _hex(moved)):
         assert np.allclose(da, db, atol=th) and np.allclose(Ga, Gb, atol=th)
+
+
+def test_thermal_goldens_exercise_every_term():
+    """The QUADTH fixtures are not vacuous: volume flux, convection lines
+    (F and K on the line nodes) and the capacity matrix all contribute, and
+    the second environment temperature of a line with etemp[1] = 0 is taken
+    from etemp[0] (SurfaceLINETH::pre)."""
+    mesh = cases.quadth_lines_6x5()[0]
+    assert mesh.lines.n == 11 and (mesh.elem_params[:, 1] != 0).any()
+    g = np.load(os.path.join(GOLDEN, "quadth_lines_6x5.npz"))
+    base = mesh.__class__(**{**mesh.__dict__, "lines": None})
+    m0 = O.OracleModel(base, "port")
+    m0.set_U(np.zeros(m0.n_total))
+    m0.assemble()
+    assert not np.array_equal(m0.F(), g["F"])            # lines load F
+    assert not np.array_equal(m0.K(2), g["K_2"])         # convection adds to K
+    t = cases.quadth_transient_5x4()[0]
+    gt = np.load(os.path.join(GOLDEN, "quadth_transient_5x4.npz"))
+    assert np.abs(gt["C_2"]).max() > 0 and not np.any(gt["M_2"])
+    # a zero second temperature equals giving it explicitly
+    lines = t.lines
+    et = lines.etemp.copy()
+    et[et[:, 1] == 0.0, 1] = et[et[:, 1] == 0.0, 0]
+    t2 = t.__class__(**{**t.__dict__, "lines": lines.__class__(lines.conn, lines.htc, lines.flux,
+                                                                et)})
+    m2 = O.OracleModel(t2, "port")
+    m2.set_U(np.zeros(m2.n_total))
+    m2.assemble()
+    assert np.array_equal(_bits(m2.F()), _bits(gt["F"]))
