@@ -131,3 +131,26 @@ FULL_CASES = {f.__name__: f for f in (cube3_nh, cube4_nh_clamped, mr_twist_3x2x4
                                        tetra0_3x3x3, quadth_5x4, quadth_lines_6x5,
                                        quadth_transient_5x4)}
 DIGEST_CASES = {f.__name__: f for f in (cube10_nh,)}
+
+
+def heat_model(transient=False):
+    """The reference's QUADTH_test / QUADTH_transient model (test/QUADTH/heat.cdb):
+    QUADTH k = 0.018 (rho = 1.1e-3, c = 920 when transient), convection lines
+    htc = 0.0034 to -6 degrees, the HEAT load of the .cdb; returns (mesh,
+    loads, probe node, fixture)."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "heat_quadth.npz"))
+    E = g["quads"].shape[0]
+    ep = np.zeros((E, 4))
+    ep[:, 0] = 0.018
+    if transient:
+        ep[:, 2] = 1.1e-3
+        ep[:, 3] = 920.0
+    L = g["lines"].shape[0]
+    lines = mg.SurfaceLines(g["lines"].astype(np.uint32), np.full(L, 0.0034), np.zeros(L),
+                            np.full((L, 2), -6.0))
+    mesh = mg.Mesh(mg.ELEM_QUADTH, g["xyz"].astype(np.float64), g["quads"].astype(np.uint32),
+                   elem_params=ep, lines=lines, transient=transient, name="heat_quadth")
+    loads = [(int(n), int(d), float(v)) for n, d, v in zip(g["load_node"], g["load_dof"],
+                                                            g["load_value"])]
+    return mesh, loads, int(g["probe"][0]), g

@@ -156,6 +156,7 @@ def read_cdb(path):
     not 1..n."""
     lines = open(path).read().splitlines()
     node_ids, xyz, cells, ctype, fixes, mpcs, comps = [], [], [], [], [], [], {}
+    loads = []
     i = 0
     first = lambda t: t.lstrip()[:1]  # noqa: E731
     while i < len(lines):
@@ -191,6 +192,16 @@ def read_cdb(path):
                 fixes.append((int(tok[1]), DOF_LABELS.index(tok[2].upper()), float(tok[3])))
             except ValueError:
                 pass   # 'ALL' etc.: not a numeric node
+        elif key == "F":
+            # FEReaders.cpp:677-704: HEAT -> TEMP, FX/FY/FZ -> UX/UY/UZ, else a DoF label
+            try:
+                node, val = int(tok[1]), float(tok[3])
+            except ValueError:
+                node = None
+            if node is not None:
+                lab = tok[2].upper()
+                lab = {"HEAT": "TEMP", "FX": "UX", "FY": "UY", "FZ": "UZ"}.get(lab, lab)
+                loads.append((node, DOF_LABELS.index(lab), val))
         elif key == "CE":
             b, n_terms = float(tok[5]), int(tok[3])
             terms = []
@@ -224,10 +235,11 @@ def read_cdb(path):
         old2new = {o: k + 1 for k, o in enumerate(node_ids)}
         cells = [[old2new[n] for n in c] for c in cells]
         fixes = [(old2new[n], d, v) for n, d, v in fixes]
+        loads = [(old2new[n], d, v) for n, d, v in loads]
         mpcs = [([(old2new[n], d, c) for n, d, c in terms], b) for terms, b in mpcs]
         comps = {k: [old2new[n] for n in v] for k, v in comps.items()}
     return {"xyz": np.array(xyz), "cells": cells, "type": ctype, "fixes": fixes,
-            "mpcs": mpcs, "comps": comps}
+            "mpcs": mpcs, "comps": comps, "loads": loads}
 
 
 def read_ref_curve(path):
@@ -288,6 +300,42 @@ def write_a2000_fixture():
     print("wrote a2000_plane41", conn.shape, len(md["fixes"]), "D")
 
 
+def write_heat_fixture():
+    """The reference's QUADTH_test / QUADTH_transient inputs (test/QUADTH):
+    the QUADTH (TYPE 1) and SurfaceLINETH (TYPE 2) cells of heat.cdb, its
+    HEAT loads, the PROBE node, and the ANSYS results the two tests check:
+    every node's steady temperature (temp.txt) and the probe's transient
+    history (temphistory.txt)."""
+    base = "/root/reference/test/QUADTH"
+    md = read_cdb(f"{base}/heat.cdb")
+    quads = np.array([c for c, t in zip(md["cells"], md["type"]) if t == 1], dtype=np.uint32)
+    lines = np.array([c for c, t in zip(md["cells"], md["type"]) if t == 2], dtype=np.uint32)
+    temp = []
+    with open(f"{base}/temp.txt", encoding="latin-1") as fh:
+        next(fh)
+        for row in fh:
+            if row.strip():
+                temp.append(float(row.split()[1]))
+    hist_t, hist_v = [], []
+    with open(f"{base}/temphistory.txt") as fh:
+        next(fh)
+        for row in fh:
+            if row.strip():
+                a, b = row.split(",")
+                hist_t.append(float(a))
+                hist_v.append(float(b))
+    assert len(temp) == md["xyz"].shape[0] and not md["fixes"]
+    np.savez_compressed(
+        os.path.join(HERE, "heat_quadth.npz"),
+        xyz=md["xyz"], quads=quads, lines=lines,
+        load_node=np.array([f[0] for f in md["loads"]], dtype=np.uint32),
+        load_dof=np.array([f[1] for f in md["loads"]], dtype=np.int32),
+        load_value=np.array([f[2] for f in md["loads"]], dtype=np.float64),
+        probe=np.array(md["comps"]["PROBE"], dtype=np.uint32),
+        ansys_temp=np.array(temp), ansys_time=np.array(hist_t), ansys_probe=np.array(hist_v))
+    print("wrote heat_quadth", quads.shape, lines.shape, len(md["loads"]), "F")
+
+
 def write_rigid_body_fixture():
     base = "/root/reference/test/rigid_body_mpc"
     nodes, elems, comps, fixes, curve = read_rigid_body_case(
@@ -311,6 +359,7 @@ def main():
     write_rigid_body_fixture()
     write_damper_fixture()
     write_a2000_fixture()
+    write_heat_fixture()
     if not O.build_ref():
         sys.exit("reference sources not found; cannot regenerate goldens")
     for name, case in cases.FULL_CASES.items():
