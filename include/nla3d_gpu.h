@@ -384,6 +384,48 @@ typedef struct {
 int nla3d_assemble_solid81_noalloc(const nla3d_solid81_noalloc_args* args, void* stream,
                                    uint32_t* flagged);
 
+/* ---- sparse LDL^T of K(2) on the device --------------------------------
+ * Replaces the reference's EquationSolver (EquationSolver.h:19-34:
+ * factorizeEquations / substituteEquations / solveEquations on the
+ * SparseSymMatrix K(2), upper CSR, 1-based) with a supernodal multifrontal
+ * LDL^T whose factor stays on the device next to the assembled K.
+ * iofeir / columns: the upper CSR pattern (nla3d_pattern of block 2); perm:
+ * a fill-reducing order (perm[new] = equation - 1) or NULL; rows with a zero
+ * diagonal (MPC / CE equations) must come after the DoFs they couple to.
+ * There is no pivoting: a pivot below pivot_rel * max|K| (1e-13 FP64, 1e-7
+ * FP32) is replaced by +-that value and counted; the solve refines in FP64. */
+typedef struct nla3d_ldlt nla3d_ldlt;
+/* Symbolic analysis only (host; no GPU needed).  stats[8] = supernodes,
+ * levels, largest front, entries of L (incl. D), factorisation flops, front
+ * buffer entries, most children of a supernode, total supernode rows; each
+ * other output may be NULL: perm_out (n, factor order -> equation - 1),
+ * sn_first_out (supernodes + 1), row_ptr_out (supernodes + 1), rows_out
+ * (stats[7]; each supernode's rows in factor order, its pivots first). */
+int nla3d_ldlt_analyze(int64_t n, const uint32_t* iofeir, const uint32_t* columns,
+                       const int32_t* perm, double* stats, int32_t* perm_out, int32_t* sn_first_out,
+                       int64_t* row_ptr_out, int32_t* rows_out);
+/* precision 0: FP64 fronts; 1: FP32 fronts (half the memory, FP64 refinement).
+ * stream: the stream the values are produced on (NULL: a stream of its own);
+ * a borrowed stream must outlive the handle.
+ * On an error after the handle exists, *out is set: read nla3d_ldlt_last_error
+ * and call nla3d_ldlt_destroy. */
+int nla3d_ldlt_create(int64_t n, const uint32_t* iofeir, const uint32_t* columns,
+                      const int32_t* perm, int precision, void* stream, nla3d_ldlt** out);
+/* EquationSolver::factorizeEquations: values = the device K(2) values
+ * (nla3d_device_K block 2).  NLA3D_ERR_ELEMENT on a non-finite pivot. */
+int nla3d_ldlt_factor(nla3d_ldlt* h, const double* values);
+/* EquationSolver::substituteEquations: x = K(2)^-1 b on device vectors, then
+ * at most max_refine steps x += K^-1 (b - K x) until ||b - K x|| <= tol ||b||
+ * (values: the same K as factored, or a nearby one).  NLA3D_ERR_RANGE when
+ * tol is not reached; steps and rel_residual may be NULL. */
+int nla3d_ldlt_solve(nla3d_ldlt* h, const double* values, const double* b, double* x,
+                     int max_refine, double tol, int* steps, double* rel_residual);
+/* out[8]: supernodes, levels, largest front, entries of L, flops, front bytes,
+ * perturbed pivots and non-finite pivots of the last factorisation. */
+int nla3d_ldlt_info(const nla3d_ldlt* h, double* out);
+const char* nla3d_ldlt_last_error(const nla3d_ldlt* h);
+int nla3d_ldlt_destroy(nla3d_ldlt* h);
+
 #ifdef __cplusplus
 }
 #endif

@@ -6,6 +6,9 @@ Translation units (compiled in parallel, then linked by nvcc):
   csrc/host_model.cpp  DoF numbering, CSR pattern, slot maps (host C++)
   csrc/noalloc.cu      SOLID81 assembly with a fixed, library-owned scratch array
   csrc/mlp.cu          kernels of the learned Newton start (BF16 MLP)
+  csrc/pattern_gpu.cu  CSR pattern, slot maps and gather lists built on the device
+  csrc/ldlt.cu         supernodal multifrontal LDL^T of K(2) on the device (solver)
+  csrc/ldlt_host.cpp   its symbolic analysis (host C++)
 """
 from __future__ import annotations
 
@@ -22,7 +25,8 @@ LIB = os.path.join(HERE, "libnla3d_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O3",
               "-I" + os.path.join(ROOT, "include")]
-SOURCES = ["kernels.cu", "capi.cu", "host_model.cpp", "noalloc.cu", "mlp.cu", "pattern_gpu.cu"]
+SOURCES = ["kernels.cu", "capi.cu", "host_model.cpp", "noalloc.cu", "mlp.cu", "pattern_gpu.cu",
+           "ldlt.cu", "ldlt_host.cpp"]
 
 
 def nvcc() -> str:

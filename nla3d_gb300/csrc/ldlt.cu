@@ -1,0 +1,801 @@
+// Supernodal multifrontal LDL^T on the device for a symmetric K(2) held in
+// the reference's upper CSR layout (SparseSymMatrix, SparseMatrix.h:206-221):
+// the GPU counterpart of EquationSolver::factorizeEquations /
+// substituteEquations (EquationSolver.h:19-34).  No counterpart exists in the
+// reference's own sources for the device; its host PARDISO / dense Gauss
+// solvers are what this replaces.
+//
+// Numeric factorisation, level by level of the supernodal tree (all fronts
+// of a level are independent):
+//   1. every front is zeroed and the matrix values are scattered into it
+//      (one map entry per stored value, computed by the symbolic analysis);
+//   2. extend-add: each child's update matrix is added into its parent's
+//      front; children are taken one ordinal at a time (first children of all
+//      parents of the level, then second children, ...) so that no two
+//      threads add into one entry and the sums keep a fixed order;
+//   3. partial LDL^T of the front's k pivot columns, right-looking, without
+//      pivoting (the u/p blocks are quasi-definite: K_uu > 0, K_pp < 0, and
+//      constraint rows are ordered last by the caller); a pivot below
+//      tau = pivot_rel * max|A| is replaced by +-tau and counted, and the
+//      solve's iterative refinement recovers the accuracy.
+//      Fronts of <= kSmallFront rows: one thread block per front, all fronts
+//      of the level in one launch.  Larger fronts: blocked, 64 columns per
+//      panel (diagonal block, panel rows, then a tiled rank-64 update of the
+//      trailing lower triangle).
+// Solve (multifrontal, vectors): forward by levels with the same extend-add
+// on the update vectors, D^-1, backward by levels top-down gathering the
+// solved ancestor entries; FP64 iterative refinement r = b - A x with A's
+// both-triangle CSR in the input numbering.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "../../include/nla3d_gpu.h"
+#include "ldlt.hpp"
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kSmallFront = 256;   // fronts up to this many rows: one block each
+constexpr int kPanel = 64;         // panel width of the blocked path
+constexpr int kTile = 64;          // trailing-update tile
+
+struct LdltDev {
+  const uint64_t* front_off;
+  const uint64_t* vec_off;
+  const int64_t* row_ptr;
+  const int32_t* rows;
+  const int32_t* sn_first;
+  const int32_t* sn_parent;
+  const int64_t* rel_ptr;
+  const uint32_t* rel;
+};
+
+// ---- factorisation kernels ----
+
+template <typename T>
+__global__ void scatter_values_kernel(uint64_t nnz, const uint64_t* __restrict__ dest,
+                                      const double* __restrict__ values, T* __restrict__ front) {
+  for (uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; q < nnz;
+       q += (uint64_t)gridDim.x * blockDim.x)
+    front[dest[q]] = (T)values[q];
+}
+
+// max |A| over the stored values: per-block maxima, then one block over them
+constexpr int kMaxBlocks = 1024;
+__global__ void maxabs_kernel(uint64_t nnz, const double* __restrict__ values,
+                              double* __restrict__ part) {
+  __shared__ double red[kThreads];
+  double m = 0.0;
+  for (uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; q < nnz;
+       q += (uint64_t)gridDim.x * blockDim.x)
+    m = fmax(m, fabs(values[q]));
+  red[threadIdx.x] = m;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+__global__ void maxabs_final_kernel(int n, const double* __restrict__ part, double* out) {
+  __shared__ double red[kThreads];
+  double m = 0.0;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) m = fmax(m, part[q]);
+  red[threadIdx.x] = m;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[0] = red[0];
+}
+
+// children[blockIdx.x]: add its update matrix into its parent's front
+template <typename T>
+__global__ void extend_add_kernel(const int32_t* __restrict__ children, int n, LdltDev d,
+                                  T* __restrict__ front) {
+  const int c = children[blockIdx.x];
+  const int p = d.sn_parent[c];
+  const int64_t mc = d.row_ptr[c + 1] - d.row_ptr[c];
+  const int64_t kc = d.sn_first[c + 1] - d.sn_first[c];
+  const int64_t mp = d.row_ptr[p + 1] - d.row_ptr[p];
+  const int64_t u = mc - kc;
+  const T* Fc = front + d.front_off[c];
+  T* Fp = front + d.front_off[p];
+  const uint32_t* rel = d.rel + d.rel_ptr[c];
+  for (int64_t j = blockIdx.y; j < u; j += gridDim.y) {
+    const int64_t pj = rel[j];
+    const T* src = Fc + (kc + j) * mc + kc;
+    T* dst = Fp + pj * mp;
+    for (int64_t i = j + threadIdx.x; i < u; i += blockDim.x) dst[rel[i]] += src[i];
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ T guard_pivot(T dv, double tau, int* perturbed) {
+  if (!(fabs((double)dv) >= tau)) {   // also catches NaN
+    if (dv != dv) {
+      atomicAdd(perturbed + 1, 1);
+      return dv;
+    }
+    atomicAdd(perturbed, 1);
+    return dv < T(0) ? T(-tau) : T(tau);
+  }
+  return dv;
+}
+
+// one block per front (m <= kSmallFront): right-looking LDL^T of the k pivot
+// columns, the trailing (m-k)^2 block left as the update matrix
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    factor_small_kernel(const int32_t* __restrict__ list, LdltDev d, T* __restrict__ front,
+                        const double* __restrict__ tau_p, double pivot_rel, int* perturbed) {
+  __shared__ T sl[kSmallFront], sw[kSmallFront];
+  __shared__ T sd;
+  const int s = list[blockIdx.x];
+  const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
+  const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
+  T* F = front + d.front_off[s];
+  const double tau = pivot_rel * tau_p[0];
+  for (int64_t p = 0; p < k; p++) {
+    if (threadIdx.x == 0) {
+      const T dv = guard_pivot(F[p + p * m], tau, perturbed);
+      F[p + p * m] = dv;
+      sd = dv;
+    }
+    __syncthreads();
+    const T dv = sd;
+    for (int64_t i = p + 1 + threadIdx.x; i < m; i += blockDim.x) {
+      const T w = F[i + p * m];
+      const T l = w / dv;
+      sw[i] = w;
+      sl[i] = l;
+      F[i + p * m] = l;
+    }
+    __syncthreads();
+    for (int64_t j = p + 1; j < m; j++) {
+      const T wj = sw[j];
+      T* col = F + j * m;
+      for (int64_t i = j + threadIdx.x; i < m; i += blockDim.x) col[i] -= sl[i] * wj;
+    }
+    __syncthreads();
+  }
+}
+
+// blocked path, step 1: LDL^T of the pb x pb diagonal block at column p0
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    diag_block_kernel(T* __restrict__ F, int64_t m, int64_t p0, int pb,
+                      const double* __restrict__ tau_p, double pivot_rel, int* perturbed) {
+  __shared__ T B[kPanel][kPanel + 1];   // B[col][row]
+  __shared__ T sd;
+  for (int t = threadIdx.x; t < pb * pb; t += blockDim.x) {
+    const int r = t % pb, c = t / pb;
+    B[c][r] = r >= c ? F[(p0 + r) + (p0 + c) * m] : T(0);
+  }
+  __syncthreads();
+  const double tau = pivot_rel * tau_p[0];
+  for (int p = 0; p < pb; p++) {
+    if (threadIdx.x == 0) {
+      const T dv = guard_pivot(B[p][p], tau, perturbed);
+      B[p][p] = dv;
+      sd = dv;
+    }
+    __syncthreads();
+    const T dv = sd;
+    // rank-1 update of the rest with w = column p, then column p becomes l = w / d
+    for (int t = threadIdx.x; t < (pb - p - 1) * (pb - p - 1); t += blockDim.x) {
+      const int r = p + 1 + t % (pb - p - 1), c = p + 1 + t / (pb - p - 1);
+      if (r >= c) B[c][r] -= B[p][r] * (B[p][c] / dv);
+    }
+    __syncthreads();
+    for (int t = p + 1 + threadIdx.x; t < pb; t += blockDim.x) B[p][t] = B[p][t] / dv;
+    __syncthreads();
+  }
+  for (int t = threadIdx.x; t < pb * pb; t += blockDim.x) {
+    const int r = t % pb, c = t / pb;
+    if (r >= c) F[(p0 + r) + (p0 + c) * m] = B[c][r];
+  }
+}
+
+// blocked path, step 2: rows i >= p0+pb of the panel: w = f L11^-T (forward
+// substitution with the unit lower L11), W[i] = w, F[i] = l = w / d
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    panel_rows_kernel(T* __restrict__ F, int64_t m, int64_t p0, int pb, T* __restrict__ W,
+                      int64_t ldw) {
+  __shared__ T L[kPanel][kPanel + 1];   // L[col][row]
+  __shared__ T D[kPanel];
+  for (int t = threadIdx.x; t < pb * pb; t += blockDim.x) {
+    const int r = t % pb, c = t / pb;
+    L[c][r] = r > c ? F[(p0 + r) + (p0 + c) * m] : T(0);
+  }
+  for (int t = threadIdx.x; t < pb; t += blockDim.x) D[t] = F[(p0 + t) + (p0 + t) * m];
+  __syncthreads();
+  const int64_t i = p0 + pb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  T w[kPanel];
+#pragma unroll 4
+  for (int c = 0; c < pb; c++) {
+    T v = F[i + (p0 + c) * m];
+    for (int c2 = 0; c2 < c; c2++) v -= L[c2][c] * w[c2];
+    w[c] = v;
+  }
+  const int64_t r = i - (p0 + pb);
+  for (int c = 0; c < pb; c++) {
+    W[r + c * ldw] = w[c];
+    F[i + (p0 + c) * m] = w[c] / D[c];
+  }
+}
+
+// blocked path, step 3: trailing lower triangle, F[i][j] -= sum_c L[i][c] W[j][c]
+// for i >= j >= q0 = p0+pb; 64x64 tiles, 4x4 outputs per thread
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    trailing_update_kernel(T* __restrict__ F, int64_t m, int64_t p0, int pb,
+                           const T* __restrict__ W, int64_t ldw) {
+  const int ti = blockIdx.x, tj = blockIdx.y;
+  if (tj > ti) return;
+  const int64_t q0 = p0 + pb;
+  __shared__ T As[16][kTile + 1];
+  __shared__ T Bs[16][kTile + 1];
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  const int64_t i0 = q0 + (int64_t)ti * kTile, j0 = q0 + (int64_t)tj * kTile;
+  T acc[4][4] = {};
+  for (int c0 = 0; c0 < pb; c0 += 16) {
+    for (int t = threadIdx.x; t < 16 * kTile; t += blockDim.x) {
+      const int cc = t / kTile, rr = t % kTile;
+      const int c = c0 + cc;
+      const int64_t i = i0 + rr, j = j0 + rr;
+      As[cc][rr] = (c < pb && i < m) ? F[i + (p0 + c) * m] : T(0);
+      Bs[cc][rr] = (c < pb && j < m) ? W[(j - q0) + c * ldw] : T(0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int cc = 0; cc < 16; cc++) {
+      T a[4], b[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) a[u] = As[cc][ty * 4 + u];
+#pragma unroll
+      for (int v = 0; v < 4; v++) b[v] = Bs[cc][tx * 4 + v];
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+#pragma unroll
+        for (int v = 0; v < 4; v++) acc[u][v] += a[u] * b[v];
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int u = 0; u < 4; u++) {
+    const int64_t i = i0 + ty * 4 + u;
+    if (i >= m) continue;
+#pragma unroll
+    for (int v = 0; v < 4; v++) {
+      const int64_t j = j0 + tx * 4 + v;
+      if (j < m && j <= i) F[i + j * m] -= acc[u][v];
+    }
+  }
+}
+
+// ---- solve kernels ----
+
+__global__ void solve_init_kernel(int64_t n, const int32_t* __restrict__ perm,
+                                  const int32_t* __restrict__ col2sn, LdltDev d,
+                                  const double* __restrict__ b, double* __restrict__ vec) {
+  const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const int s = col2sn[j];
+  vec[d.vec_off[s] + (j - d.sn_first[s])] = b[perm[j]];
+}
+
+__global__ void vec_extend_add_kernel(const int32_t* __restrict__ children, LdltDev d,
+                                      double* __restrict__ vec) {
+  const int c = children[blockIdx.x];
+  const int p = d.sn_parent[c];
+  const int64_t mc = d.row_ptr[c + 1] - d.row_ptr[c];
+  const int64_t kc = d.sn_first[c + 1] - d.sn_first[c];
+  const double* src = vec + d.vec_off[c] + kc;
+  double* dst = vec + d.vec_off[p];
+  const uint32_t* rel = d.rel + d.rel_ptr[c];
+  for (int64_t i = threadIdx.x; i < mc - kc; i += blockDim.x) dst[rel[i]] += src[i];
+}
+
+// forward: v[0:k] <- D^-1 L11^-1 v[0:k], v[k:m] <- v[k:m] - L21 (L11^-1 v[0:k])
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    forward_kernel(const int32_t* __restrict__ list, LdltDev d, const T* __restrict__ front,
+                   double* __restrict__ vec) {
+  const int s = list[blockIdx.x];
+  const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
+  const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
+  const T* F = front + d.front_off[s];
+  double* v = vec + d.vec_off[s];
+  for (int64_t c = 0; c < k; c++) {
+    __syncthreads();
+    const double y = v[c];
+    for (int64_t i = c + 1 + threadIdx.x; i < m; i += blockDim.x) v[i] -= (double)F[i + c * m] * y;
+  }
+  __syncthreads();
+  for (int64_t c = threadIdx.x; c < k; c += blockDim.x) v[c] /= (double)F[c + c * m];
+}
+
+// backward: x[0:k] = L11^-T (v[0:k] - L21^T x_rest), x_rest gathered from the
+// solved ancestors (factor order), written to xf
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    backward_kernel(const int32_t* __restrict__ list, LdltDev d, const T* __restrict__ front,
+                    double* __restrict__ vec, double* __restrict__ xf) {
+  const int s = list[blockIdx.x];
+  const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
+  const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
+  const int32_t* rows = d.rows + d.row_ptr[s];
+  const T* F = front + d.front_off[s];
+  double* v = vec + d.vec_off[s];
+  // t_c = v_c - sum_{i >= k} L[i][c] x[rows[i]]: a warp per column
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int64_t c = warp; c < k; c += blockDim.x / 32) {
+    double acc = 0.0;
+    for (int64_t i = k + lane; i < m; i += 32) acc += (double)F[i + c * m] * xf[rows[i]];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) v[c] -= acc;
+  }
+  for (int64_t c = k - 1; c >= 0; c--) {
+    __syncthreads();
+    const double x = v[c];
+    for (int64_t i = threadIdx.x; i < c; i += blockDim.x) v[i] -= (double)F[c + i * m] * x;
+  }
+  __syncthreads();
+  const int32_t f = d.sn_first[s];
+  for (int64_t c = threadIdx.x; c < k; c += blockDim.x) xf[f + c] = v[c];
+}
+
+__global__ void solve_finish_kernel(int64_t n, const int32_t* __restrict__ perm,
+                                    const double* __restrict__ xf, double* __restrict__ x,
+                                    int accumulate) {
+  const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  if (accumulate)
+    x[perm[j]] += xf[j];
+  else
+    x[perm[j]] = xf[j];
+}
+
+// r = b - A x, A by both-triangle rows (a warp per row, fixed order); per-block
+// partial sums of r^2 and b^2 for the norms
+__global__ void residual_kernel(int64_t n, const int64_t* __restrict__ ptr,
+                                const int32_t* __restrict__ col, const uint32_t* __restrict__ slot,
+                                const double* __restrict__ A, const double* __restrict__ x,
+                                const double* __restrict__ b, double* __restrict__ r,
+                                double* __restrict__ part) {
+  __shared__ double red[2][kThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t row = blockIdx.x * (int64_t)(blockDim.x / 32) + warp;
+  double rr = 0.0, bb = 0.0;
+  if (row < n) {
+    double acc = 0.0;
+    for (int64_t q = ptr[row] + lane; q < ptr[row + 1]; q += 32) acc += A[slot[q]] * x[col[q]];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) {
+      const double ri = b[row] - acc;
+      r[row] = ri;
+      rr = ri * ri;
+      bb = b[row] * b[row];
+    }
+  }
+  if (lane == 0) {
+    red[0][warp] = rr;
+    red[1][warp] = bb;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, c = 0.0;
+    for (int w = 0; w < kThreads / 32; w++) {
+      a += red[0][w];
+      c += red[1][w];
+    }
+    part[2 * blockIdx.x] = a;
+    part[2 * blockIdx.x + 1] = c;
+  }
+}
+
+}  // namespace
+
+struct nla3d_ldlt {
+  LdltSymbolic S;
+  int prec = 0;   // 0: FP64 fronts, 1: FP32 fronts (FP64 refinement)
+  double pivot_rel = 1e-13;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::string err;
+  std::vector<void*> allocs;
+  void* d_front = nullptr;
+  double* d_vec = nullptr;
+  double* d_xf = nullptr;
+  double* d_r = nullptr;
+  double* d_dx = nullptr;
+  double* d_part = nullptr;
+  double* d_maxabs = nullptr;
+  double* d_maxpart = nullptr;
+  int* d_perturbed = nullptr;
+  void* d_W = nullptr;
+  int64_t ldw = 0;
+  uint64_t* d_adest = nullptr;
+  int32_t* d_perm = nullptr;
+  int32_t* d_col2sn = nullptr;
+  int32_t* d_lists = nullptr;   // level lists, small lists, extend-add child lists
+  int64_t* d_fptr = nullptr;
+  int32_t* d_fcol = nullptr;
+  uint32_t* d_fslot = nullptr;
+  LdltDev dev{};
+  // host schedule per level
+  struct Level {
+    int64_t all_off = 0, all_cnt = 0;     // every supernode of the level
+    int64_t small_off = 0, small_cnt = 0;
+    std::vector<int32_t> large;
+    std::vector<int64_t> ea_off, ea_cnt;  // children of the level's parents, by ordinal
+  };
+  std::vector<Level> levels;
+  const double* factored_values = nullptr;
+  bool factored = false;
+  int perturbed[2] = {0, 0};
+  uint64_t front_entries = 0;
+};
+
+namespace {
+
+int fail(nla3d_ldlt* h, int code, const std::string& msg) {
+  if (h) h->err = msg;
+  return code;
+}
+
+int cuda_fail(nla3d_ldlt* h, cudaError_t e, const char* where) {
+  return fail(h, NLA3D_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+template <typename X>
+cudaError_t dalloc(nla3d_ldlt* h, X** p, size_t count) {
+  void* q = nullptr;
+  cudaError_t e = cudaMalloc(&q, sizeof(X) * (count ? count : 1));
+  if (e == cudaSuccess) {
+    h->allocs.push_back(q);
+    *p = static_cast<X*>(q);
+  }
+  return e;
+}
+
+template <typename X>
+cudaError_t upload(nla3d_ldlt* h, X** p, const std::vector<X>& v) {
+  cudaError_t e = dalloc(h, p, v.size());
+  if (e == cudaSuccess && !v.empty())
+    e = cudaMemcpyAsync(*p, v.data(), sizeof(X) * v.size(), cudaMemcpyHostToDevice, h->stream);
+  return e;
+}
+
+template <typename T>
+cudaError_t enqueue_factor(nla3d_ldlt* h, const double* values) {
+  const LdltSymbolic& S = h->S;
+  T* front = static_cast<T*>(h->d_front);
+  cudaStream_t st = h->stream;
+  cudaError_t e = cudaMemsetAsync(front, 0, sizeof(T) * h->front_entries, st);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(h->d_perturbed, 0, 2 * sizeof(int), st);
+  if (e != cudaSuccess) return e;
+  {
+    const int blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>(
+        kMaxBlocks, (S.nnz + kThreads - 1) / kThreads));
+    maxabs_kernel<<<blocks, kThreads, 0, st>>>(S.nnz, values, h->d_maxpart);
+    maxabs_final_kernel<<<1, kThreads, 0, st>>>(blocks, h->d_maxpart, h->d_maxabs);
+  }
+  if (S.nnz) {
+    const unsigned blocks = (unsigned)std::min<uint64_t>((S.nnz + kThreads - 1) / kThreads, 152 * 16);
+    scatter_values_kernel<T><<<blocks, kThreads, 0, st>>>(S.nnz, h->d_adest, values, front);
+  }
+  for (const auto& L : h->levels) {
+    for (size_t q = 0; q < L.ea_off.size(); q++) {
+      if (!L.ea_cnt[q]) continue;
+      const dim3 grid((unsigned)L.ea_cnt[q], 16);
+      extend_add_kernel<T><<<grid, kThreads, 0, st>>>(h->d_lists + L.ea_off[q], (int)L.ea_cnt[q],
+                                                      h->dev, front);
+    }
+    if (L.small_cnt)
+      factor_small_kernel<T><<<(unsigned)L.small_cnt, kThreads, 0, st>>>(
+          h->d_lists + L.small_off, h->dev, front, h->d_maxabs, h->pivot_rel, h->d_perturbed);
+    for (int32_t s : L.large) {
+      const int64_t m = S.m(s), k = S.k(s);
+      T* F = front + S.front_off[s];
+      T* W = static_cast<T*>(h->d_W);
+      for (int64_t p0 = 0; p0 < k; p0 += kPanel) {
+        const int pb = (int)std::min<int64_t>(kPanel, k - p0);
+        diag_block_kernel<T><<<1, kThreads, 0, st>>>(F, m, p0, pb, h->d_maxabs, h->pivot_rel,
+                                                     h->d_perturbed);
+        const int64_t rest = m - p0 - pb;
+        if (rest <= 0) continue;
+        panel_rows_kernel<T><<<(unsigned)((rest + kThreads - 1) / kThreads), kThreads, 0, st>>>(
+            F, m, p0, pb, W, h->ldw);
+        const unsigned tiles = (unsigned)((rest + kTile - 1) / kTile);
+        trailing_update_kernel<T><<<dim3(tiles, tiles), kThreads, 0, st>>>(F, m, p0, pb, W, h->ldw);
+      }
+    }
+  }
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t enqueue_solve(nla3d_ldlt* h, const double* b, double* x, int accumulate) {
+  const LdltSymbolic& S = h->S;
+  const T* front = static_cast<const T*>(h->d_front);
+  cudaStream_t st = h->stream;
+  cudaError_t e = cudaMemsetAsync(h->d_vec, 0, sizeof(double) * S.vec_off.back(), st);
+  if (e != cudaSuccess) return e;
+  const unsigned nb = (unsigned)((S.n + kThreads - 1) / kThreads);
+  solve_init_kernel<<<nb, kThreads, 0, st>>>(S.n, h->d_perm, h->d_col2sn, h->dev, b, h->d_vec);
+  for (const auto& L : h->levels) {
+    for (size_t q = 0; q < L.ea_off.size(); q++)
+      if (L.ea_cnt[q])
+        vec_extend_add_kernel<<<(unsigned)L.ea_cnt[q], kThreads, 0, st>>>(h->d_lists + L.ea_off[q],
+                                                                           h->dev, h->d_vec);
+    forward_kernel<T><<<(unsigned)L.all_cnt, kThreads, 0, st>>>(h->d_lists + L.all_off, h->dev,
+                                                                front, h->d_vec);
+  }
+  for (auto it = h->levels.rbegin(); it != h->levels.rend(); ++it)
+    backward_kernel<T><<<(unsigned)it->all_cnt, kThreads, 0, st>>>(h->d_lists + it->all_off,
+                                                                   h->dev, front, h->d_vec, h->d_xf);
+  solve_finish_kernel<<<nb, kThreads, 0, st>>>(S.n, h->d_perm, h->d_xf, x, accumulate);
+  return cudaGetLastError();
+}
+
+cudaError_t enqueue_residual(nla3d_ldlt* h, const double* A, const double* x, const double* b) {
+  const LdltSymbolic& S = h->S;
+  const int64_t rows_per_block = kThreads / 32;
+  const unsigned blocks = (unsigned)((S.n + rows_per_block - 1) / rows_per_block);
+  residual_kernel<<<blocks, kThreads, 0, h->stream>>>(S.n, h->d_fptr, h->d_fcol, h->d_fslot, A, x,
+                                                     b, h->d_r, h->d_part);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+extern "C" {
+
+int nla3d_ldlt_analyze(int64_t n, const uint32_t* iofeir, const uint32_t* columns,
+                       const int32_t* perm, double* stats, int32_t* perm_out, int32_t* sn_first_out,
+                       int64_t* row_ptr_out, int32_t* rows_out) {
+  if (!stats) return NLA3D_ERR_ARG;
+  LdltSymbolic S;
+  const std::string msg = ldlt_analyze(n, iofeir, columns, perm, &S);
+  if (!msg.empty()) return NLA3D_ERR_ARG;
+  stats[0] = (double)S.n_sn();
+  stats[1] = (double)(S.level_ptr.size() - 1);
+  stats[2] = (double)S.max_front;
+  stats[3] = (double)S.nnz_L;
+  stats[4] = S.flops;
+  stats[5] = (double)S.front_off.back();
+  stats[6] = (double)S.max_children;
+  stats[7] = (double)S.rows.size();
+  if (perm_out) std::copy(S.perm.begin(), S.perm.end(), perm_out);
+  if (sn_first_out) std::copy(S.sn_first.begin(), S.sn_first.end(), sn_first_out);
+  if (row_ptr_out) std::copy(S.row_ptr.begin(), S.row_ptr.end(), row_ptr_out);
+  if (rows_out) std::copy(S.rows.begin(), S.rows.end(), rows_out);
+  return NLA3D_OK;
+}
+
+int nla3d_ldlt_create(int64_t n, const uint32_t* iofeir, const uint32_t* columns,
+                      const int32_t* perm, int precision, void* stream, nla3d_ldlt** out) {
+  if (!out || (precision != 0 && precision != 1)) return NLA3D_ERR_ARG;
+  *out = nullptr;
+  nla3d_ldlt* h = new nla3d_ldlt();
+  h->prec = precision;
+  if (precision == 1) h->pivot_rel = 1e-7;
+  const std::string msg = ldlt_analyze(n, iofeir, columns, perm, &h->S);
+  if (!msg.empty()) {
+    delete h;
+    return NLA3D_ERR_ARG;
+  }
+  const LdltSymbolic& S = h->S;
+  h->front_entries = S.front_off.back();
+  // the schedule: per level, all / small / large supernodes, children by ordinal
+  const int64_t ns = S.n_sn();
+  const int nlev = (int)S.level_ptr.size() - 1;
+  std::vector<int32_t> lists;
+  std::vector<int32_t> col2sn(S.n);
+  for (int64_t s = 0; s < ns; s++)
+    for (int32_t t = S.sn_first[s]; t < S.sn_first[s + 1]; t++) col2sn[t] = (int32_t)s;
+  int64_t max_large = 0;
+  h->levels.resize(nlev);
+  for (int L = 0; L < nlev; L++) {
+    auto& lv = h->levels[L];
+    lv.all_off = (int64_t)lists.size();
+    for (int32_t q = S.level_ptr[L]; q < S.level_ptr[L + 1]; q++) lists.push_back(S.level_list[q]);
+    lv.all_cnt = (int64_t)lists.size() - lv.all_off;
+    lv.small_off = (int64_t)lists.size();
+    for (int32_t q = S.level_ptr[L]; q < S.level_ptr[L + 1]; q++) {
+      const int32_t s = S.level_list[q];
+      if (S.m(s) <= kSmallFront)
+        lists.push_back(s);
+      else {
+        lv.large.push_back(s);
+        max_large = std::max<int64_t>(max_large, S.m(s));
+      }
+    }
+    lv.small_cnt = (int64_t)lists.size() - lv.small_off;
+    int maxc = 0;
+    for (int32_t q = S.level_ptr[L]; q < S.level_ptr[L + 1]; q++) {
+      const int32_t s = S.level_list[q];
+      maxc = std::max(maxc, S.child_ptr[s + 1] - S.child_ptr[s]);
+    }
+    for (int o = 0; o < maxc; o++) {
+      lv.ea_off.push_back((int64_t)lists.size());
+      for (int32_t q = S.level_ptr[L]; q < S.level_ptr[L + 1]; q++) {
+        const int32_t s = S.level_list[q];
+        if (S.child_ptr[s + 1] - S.child_ptr[s] > o) lists.push_back(S.child_list[S.child_ptr[s] + o]);
+      }
+      lv.ea_cnt.push_back((int64_t)lists.size() - lv.ea_off.back());
+    }
+  }
+  if (lists.size() >= (size_t)INT32_MAX) {
+    delete h;
+    return NLA3D_ERR_RANGE;
+  }
+  cudaError_t e = cudaSuccess;
+  if (stream) {
+    h->stream = (cudaStream_t)stream;
+  } else {
+    e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+      delete h;
+      return NLA3D_ERR_CUDA;
+    }
+    h->own_stream = true;
+  }
+  size_t free_b = 0, total_b = 0;
+  e = cudaMemGetInfo(&free_b, &total_b);
+  const size_t tsize = precision ? sizeof(float) : sizeof(double);
+  const double need = (double)h->front_entries * tsize + (double)S.nnz * 8 + (double)S.n * 64 +
+                      (double)S.full_col.size() * 8 + (double)S.rows.size() * 8;
+  int rc = NLA3D_OK;
+  if (e != cudaSuccess)
+    rc = cuda_fail(h, e, "cudaMemGetInfo");
+  else if (need > 0.9 * (double)free_b)
+    rc = fail(h, NLA3D_ERR_NOMEM, "fronts need more device memory than is free");
+#define LCK(x)                                  \
+  do {                                          \
+    if (rc == NLA3D_OK) {                       \
+      cudaError_t _e = (x);                     \
+      if (_e != cudaSuccess) rc = cuda_fail(h, _e, #x); \
+    }                                           \
+  } while (0)
+  if (precision)
+    LCK(dalloc(h, reinterpret_cast<float**>(&h->d_front), h->front_entries));
+  else
+    LCK(dalloc(h, reinterpret_cast<double**>(&h->d_front), h->front_entries));
+  h->ldw = std::max<int64_t>(max_large, 1);
+  if (precision)
+    LCK(dalloc(h, reinterpret_cast<float**>(&h->d_W), (size_t)h->ldw * kPanel));
+  else
+    LCK(dalloc(h, reinterpret_cast<double**>(&h->d_W), (size_t)h->ldw * kPanel));
+  LCK(dalloc(h, &h->d_vec, S.vec_off.back()));
+  LCK(dalloc(h, &h->d_xf, S.n));
+  LCK(dalloc(h, &h->d_r, S.n));
+  LCK(dalloc(h, &h->d_dx, S.n));
+  LCK(dalloc(h, &h->d_part, 2 * ((S.n + 7) / 8 + 1)));
+  LCK(dalloc(h, &h->d_maxabs, 1));
+  LCK(dalloc(h, &h->d_maxpart, kMaxBlocks));
+  LCK(dalloc(h, &h->d_perturbed, 2));
+  LCK(upload(h, &h->d_adest, S.a_dest));
+  LCK(upload(h, &h->d_perm, S.perm));
+  LCK(upload(h, &h->d_col2sn, col2sn));
+  LCK(upload(h, &h->d_lists, lists));
+  LCK(upload(h, &h->d_fptr, S.full_ptr));
+  LCK(upload(h, &h->d_fcol, S.full_col));
+  LCK(upload(h, &h->d_fslot, S.full_slot));
+  uint64_t *fo = nullptr, *vo = nullptr;
+  int64_t *rp = nullptr, *relp = nullptr;
+  int32_t *rw = nullptr, *sf = nullptr, *sp = nullptr;
+  uint32_t* rl = nullptr;
+  LCK(upload(h, &fo, S.front_off));
+  LCK(upload(h, &vo, S.vec_off));
+  LCK(upload(h, &rp, S.row_ptr));
+  LCK(upload(h, &rw, S.rows));
+  LCK(upload(h, &sf, S.sn_first));
+  LCK(upload(h, &sp, S.sn_parent));
+  LCK(upload(h, &relp, S.rel_ptr));
+  LCK(upload(h, &rl, S.rel));
+  LCK(cudaStreamSynchronize(h->stream));
+#undef LCK
+  h->dev = LdltDev{fo, vo, rp, rw, sf, sp, relp, rl};
+  if (rc != NLA3D_OK) {
+    // keep the handle so that the caller can read the message, then destroy it
+    *out = h;
+    return rc;
+  }
+  *out = h;
+  return NLA3D_OK;
+}
+
+const char* nla3d_ldlt_last_error(const nla3d_ldlt* h) { return h ? h->err.c_str() : "null handle"; }
+
+int nla3d_ldlt_info(const nla3d_ldlt* h, double* out) {
+  if (!h || !out) return NLA3D_ERR_ARG;
+  const LdltSymbolic& S = h->S;
+  out[0] = (double)S.n_sn();
+  out[1] = (double)h->levels.size();
+  out[2] = (double)S.max_front;
+  out[3] = (double)S.nnz_L;
+  out[4] = S.flops;
+  out[5] = (double)h->front_entries * (h->prec ? 4.0 : 8.0);
+  out[6] = (double)h->perturbed[0];
+  out[7] = (double)h->perturbed[1];
+  return NLA3D_OK;
+}
+
+int nla3d_ldlt_factor(nla3d_ldlt* h, const double* values) {
+  if (!h || !values) return fail(h, NLA3D_ERR_ARG, "ldlt_factor: null argument");
+  if (!h->d_front) return fail(h, NLA3D_ERR_ARG, "ldlt_factor: the handle was not set up");
+  cudaError_t e = h->prec ? enqueue_factor<float>(h, values) : enqueue_factor<double>(h, values);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(h->perturbed, h->d_perturbed, 2 * sizeof(int), cudaMemcpyDeviceToHost,
+                        h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) return cuda_fail(h, e, "ldlt_factor");
+  h->factored = true;
+  h->factored_values = values;
+  if (h->perturbed[1]) return fail(h, NLA3D_ERR_ELEMENT, "ldlt_factor: a non-finite pivot");
+  return NLA3D_OK;
+}
+
+int nla3d_ldlt_solve(nla3d_ldlt* h, const double* values, const double* b, double* x,
+                     int max_refine, double tol, int* steps, double* rel_residual) {
+  if (!h || !values || !b || !x || max_refine < 0)
+    return fail(h, NLA3D_ERR_ARG, "ldlt_solve: bad argument");
+  if (!h->factored) return fail(h, NLA3D_ERR_ARG, "ldlt_solve: factor first");
+  const LdltSymbolic& S = h->S;
+  auto solve = [&](const double* rhs, double* out, int acc) {
+    return h->prec ? enqueue_solve<float>(h, rhs, out, acc) : enqueue_solve<double>(h, rhs, out, acc);
+  };
+  cudaError_t e = solve(b, x, 0);
+  const int64_t nblk = (S.n + 7) / 8;
+  std::vector<double> part(2 * nblk);
+  double rel = 0.0;
+  int it = 0;
+  for (;;) {
+    if (e == cudaSuccess) e = enqueue_residual(h, values, x, b);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(part.data(), h->d_part, sizeof(double) * 2 * nblk, cudaMemcpyDeviceToHost,
+                          h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "ldlt_solve");
+    double rr = 0.0, bb = 0.0;
+    for (int64_t q = 0; q < nblk; q++) {
+      rr += part[2 * q];
+      bb += part[2 * q + 1];
+    }
+    rel = bb > 0.0 ? std::sqrt(rr / bb) : std::sqrt(rr);
+    if (!(rel > tol) || it >= max_refine) break;
+    e = solve(h->d_r, x, 1);   // x += A^-1 r with the same factors
+    it++;
+  }
+  if (steps) *steps = it;
+  if (rel_residual) *rel_residual = rel;
+  if (!(rel <= tol)) return fail(h, NLA3D_ERR_RANGE, "ldlt_solve: refinement did not reach tol");
+  return NLA3D_OK;
+}
+
+int nla3d_ldlt_destroy(nla3d_ldlt* h) {
+  if (!h) return NLA3D_OK;
+  // a borrowed stream may already be gone: only an owned one is synchronised
+  // (cudaFree waits for the device anyway)
+  if (h->own_stream && h->stream) cudaStreamSynchronize(h->stream);
+  for (void* p : h->allocs) cudaFree(p);
+  if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  cudaGetLastError();   // leave no error of this teardown to the next caller
+  return NLA3D_OK;
+}
+
+}  // extern "C"

@@ -122,10 +122,14 @@ class NewtonSolver:
         geometric nested-dissection ordering of K(2) (one point per equation
         from backend.mesh), several times less fill on 3D meshes; "lu-gmres"
         keeps the last factorisation as the preconditioner of GMRES and
-        refactors only when GMRES needs more than 30 iterations.  Every
+        refactors only when GMRES needs more than 30 iterations; "gpu" factors
+        the device K(2) in place with the library's multifrontal LDL^T
+        (nla3d_gb300.ldlt; the same nested-dissection order, the MPC
+        equations and master DoFs last), "gpu-fp32" with FP32 fronts.  Every
         non-default solve is checked to a relative residual of 1e-10."""
-        if solver not in ("direct", "nd", "lu-gmres"):
+        if solver not in ("direct", "nd", "lu-gmres", "gpu", "gpu-fp32"):
             raise ValueError(solver)
+        self._ldlt = None
         self._perm = None
         self.solver = solver
         self._lu = None
@@ -181,7 +185,25 @@ class NewtonSolver:
             pts[self.nu + k] = xyz[n - 1]
         return pts
 
+    def _solve_gpu(self, rhs):
+        from .ldlt import DeviceLDLT, saddle_order
+        if self._ldlt is None:
+            io, co = self.patterns[2]
+            n2 = self.nu + self.nm
+            K = csr_full(io, co, np.ones(co.size), n2, n2, True)
+            order = nested_dissection(K, self._row_points())
+            perm = saddle_order(io, co, order, self.nu)
+            self._ldlt = DeviceLDLT.for_storage(self.b, perm,
+                                                "fp32" if self.solver == "gpu-fp32" else "fp64")
+        self._ldlt.factor(self.b)
+        self.factorizations += 1
+        x = self._ldlt.solve_host(self.b, rhs, max_refine=10, tol=1e-10)
+        self.krylov_iterations += self._ldlt.last_steps
+        return x
+
     def _solve(self, K2, rhs):
+        if self.solver in ("gpu", "gpu-fp32"):
+            return self._solve_gpu(rhs)
         if self.solver == "direct":
             self.factorizations += 1
             return spla.spsolve(K2, rhs, permc_spec="MMD_AT_PLUS_A")
@@ -321,7 +343,8 @@ class NewtonSolver:
                     rec.iterations = tc.eq_step - 1
                     converged = True
                     break
-                dUsl = self._solve(self._K2().tocsc(), rhs)
+                K2 = None if self.solver in ("gpu", "gpu-fp32") else self._K2().tocsc()
+                dUsl = self._solve(K2, rhs)
                 self.U[: self.nc] = Uc
                 self.U[self.nc: self.nc + self.nu] += dUsl[: self.nu]
                 self.U[self.nc + self.nu:] = dUsl[self.nu:]
