@@ -68,6 +68,9 @@ def parse():
     ap.add_argument("--model", choices=["3d_damper", "a2000"],
                     help="run one of the reference's BENCH models instead (minutes)")
     ap.add_argument("--model-backend", default="fp64", choices=["fp64", "mixed", "port"])
+    ap.add_argument("--model-solver", default="nd", choices=["nd", "gpu", "gpu-fp32", "direct"],
+                    help="K(2) solve of --model runs: host SuperLU after nested dissection, "
+                         "or the device LDL^T with FP64 / FP32 fronts")
     ap.add_argument("--e2e-chunks", type=int, default=8,
                     help="element ranges of nla3d_assemble_to_host in the e2e leg")
     ap.add_argument("--no-tune", action="store_true",
@@ -568,7 +571,7 @@ def run_cdb_model(args):
     criterion 1e-3, UY reaction of the component against the ANSYS curve,
     mean |difference| against the test's threshold as main.cpp compareCurves
     does), with the assembly on the GPU (or on the CPU oracle for
-    --model-backend port) and the nested-dissection ordered host solve.
+    --model-backend port) and the K(2) solve of --model-solver.
     Prints one JSON line."""
     from nla3d_gb300.newton import NewtonSolver
     mesh, fixes, nodes, ref, thr = cdb_model(args.model)
@@ -590,9 +593,13 @@ def run_cdb_model(args):
 
     b.assemble = timed_assemble
     t0 = time.perf_counter()
+    solver = args.model_solver
+    if args.model_backend == "port" and solver.startswith("gpu"):
+        raise SystemExit("the device solver needs a GPU backend")
     s = NewtonSolver(b, fixes, n_loadsteps=20, n_iterations=15, kinematic_tol=1e-3,
-                     solver="nd").solve()
+                     solver=solver).solve()
     wall = time.perf_counter() - t0
+    ldlt_info = s._ldlt.info() if s._ldlt is not None else None
     ne = s.ne
     curve = np.array([sum(r[int(ne[n - 1, 1]) - 1] for n in nodes) for r in s.reactions])
     err = float(np.abs(curve - ref).mean())
@@ -601,6 +608,7 @@ def run_cdb_model(args):
         "higher_is_better": False, "threshold": thr, "passed": err < thr,
         "backend": args.model_backend, "load_steps": 20,
         "iterations": [r.iterations for r in s.records],
+        "solver": solver, "ldlt": ldlt_info,
         "factorizations": s.factorizations, "wall_s": wall, "assembly_s": t_asm[0],
         "curve": curve.round(4).tolist(), "ansys": ref.tolist(),
         "model": f"{mesh.n_elems} elements, {mesh.n_nodes} nodes, {len(mesh.mpcs)} CE, "

@@ -40,7 +40,7 @@
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kSmallFront = 256;   // fronts up to this many rows: one block each
+constexpr int kSmallFront = 128;   // fronts up to this many rows: one block each, in smem
 constexpr int kPanel = 64;         // panel width of the blocked path
 constexpr int kTile = 64;          // trailing-update tile
 
@@ -130,55 +130,76 @@ __device__ __forceinline__ T guard_pivot(T dv, double tau, int* perturbed) {
   return dv;
 }
 
-// one block per front (m <= kSmallFront): right-looking LDL^T of the k pivot
-// columns, the trailing (m-k)^2 block left as the update matrix
+// one block per front (m <= kSmallFront), the front held in shared memory
+// (column-major, leading dimension m+1): right-looking LDL^T of the k pivot
+// columns, the trailing (m-k)^2 block left as the update matrix.  Threads
+// cover the trailing triangle as 32 rows x 8 columns.
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
     factor_small_kernel(const int32_t* __restrict__ list, LdltDev d, T* __restrict__ front,
                         const double* __restrict__ tau_p, double pivot_rel, int* perturbed) {
-  __shared__ T sl[kSmallFront], sw[kSmallFront];
+  extern __shared__ unsigned char smem_raw[];
+  T* S = reinterpret_cast<T*>(smem_raw);
   __shared__ T sd;
   const int s = list[blockIdx.x];
-  const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
-  const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
+  const int m = (int)(d.row_ptr[s + 1] - d.row_ptr[s]);
+  const int k = d.sn_first[s + 1] - d.sn_first[s];
+  const int ld = m + 1;
   T* F = front + d.front_off[s];
+  for (int c = 0; c < m; c++)
+    for (int r = c + threadIdx.x; r < m; r += blockDim.x) S[r + c * ld] = F[r + (int64_t)c * m];
+  __syncthreads();
   const double tau = pivot_rel * tau_p[0];
-  for (int64_t p = 0; p < k; p++) {
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int p = 0; p < k; p++) {
     if (threadIdx.x == 0) {
-      const T dv = guard_pivot(F[p + p * m], tau, perturbed);
-      F[p + p * m] = dv;
+      const T dv = guard_pivot(S[p + p * ld], tau, perturbed);
+      S[p + p * ld] = dv;
       sd = dv;
     }
     __syncthreads();
     const T dv = sd;
-    for (int64_t i = p + 1 + threadIdx.x; i < m; i += blockDim.x) {
-      const T w = F[i + p * m];
-      const T l = w / dv;
-      sw[i] = w;
-      sl[i] = l;
-      F[i + p * m] = l;
+    T* colp = S + p * ld;
+    // trailing update with w = column p (unscaled): A_ij -= w_i w_j / d
+    for (int j = p + 1 + ty; j < m; j += 8) {
+      const T lj = colp[j] / dv;
+      T* col = S + j * ld;
+      for (int i = j + tx; i < m; i += 32) col[i] -= colp[i] * lj;
     }
     __syncthreads();
-    for (int64_t j = p + 1; j < m; j++) {
-      const T wj = sw[j];
-      T* col = F + j * m;
-      for (int64_t i = j + threadIdx.x; i < m; i += blockDim.x) col[i] -= sl[i] * wj;
-    }
+    for (int i = p + 1 + threadIdx.x; i < m; i += blockDim.x) colp[i] = colp[i] / dv;
     __syncthreads();
   }
+  for (int c = 0; c < m; c++)
+    for (int r = c + threadIdx.x; r < m; r += blockDim.x) F[r + (int64_t)c * m] = S[r + c * ld];
 }
 
-// blocked path, step 1: LDL^T of the pb x pb diagonal block at column p0
+// Blocked path for the fronts above kSmallFront rows, batched: every launch
+// works on panel p0 of all large fronts of one level (blockIdx.z / .x picks
+// the front; fronts with k <= p0 return).  W: per front an m x kPanel block.
+struct BigBatch {
+  const int32_t* list;
+  const uint64_t* w_off;
+};
+
+// step 1: LDL^T of the pb x pb diagonal block, and the inverse of its unit
+// lower factor (Linv, 64 x 64 column-major per front) for step 2
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
-    diag_block_kernel(T* __restrict__ F, int64_t m, int64_t p0, int pb,
-                      const double* __restrict__ tau_p, double pivot_rel, int* perturbed) {
+    batched_diag_kernel(BigBatch b, LdltDev d, T* __restrict__ front, int64_t p0,
+                        T* __restrict__ Linv, const double* __restrict__ tau_p, double pivot_rel,
+                        int* perturbed) {
   __shared__ T B[kPanel][kPanel + 1];   // B[col][row]
   __shared__ T sd;
-  for (int t = threadIdx.x; t < pb * pb; t += blockDim.x) {
-    const int r = t % pb, c = t / pb;
-    B[c][r] = r >= c ? F[(p0 + r) + (p0 + c) * m] : T(0);
-  }
+  const int s = b.list[blockIdx.x];
+  const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
+  const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
+  if (p0 >= k) return;
+  const int pb = (int)(k - p0 < kPanel ? k - p0 : kPanel);
+  T* F = front + d.front_off[s];
+  const int tc = threadIdx.x % kPanel, tr = threadIdx.x / kPanel;   // 64 columns x 4
+  for (int r = tr; r < pb; r += kThreads / kPanel)
+    if (tc < pb) B[tc][r] = r >= tc ? F[(p0 + r) + (p0 + tc) * m] : T(0);
   __syncthreads();
   const double tau = pivot_rel * tau_p[0];
   for (int p = 0; p < pb; p++) {
@@ -189,64 +210,112 @@ __global__ void __launch_bounds__(kThreads)
     }
     __syncthreads();
     const T dv = sd;
-    // rank-1 update of the rest with w = column p, then column p becomes l = w / d
-    for (int t = threadIdx.x; t < (pb - p - 1) * (pb - p - 1); t += blockDim.x) {
-      const int r = p + 1 + t % (pb - p - 1), c = p + 1 + t / (pb - p - 1);
-      if (r >= c) B[c][r] -= B[p][r] * (B[p][c] / dv);
+    if (tc > p && tc < pb) {
+      const T lc = B[p][tc] / dv;
+      for (int r = tc + tr; r < pb; r += kThreads / kPanel) B[tc][r] -= B[p][r] * lc;
     }
     __syncthreads();
-    for (int t = p + 1 + threadIdx.x; t < pb; t += blockDim.x) B[p][t] = B[p][t] / dv;
+    if (threadIdx.x > p && threadIdx.x < pb) B[p][threadIdx.x] = B[p][threadIdx.x] / dv;
     __syncthreads();
   }
-  for (int t = threadIdx.x; t < pb * pb; t += blockDim.x) {
-    const int r = t % pb, c = t / pb;
-    if (r >= c) F[(p0 + r) + (p0 + c) * m] = B[c][r];
+  for (int r = tr; r < pb; r += kThreads / kPanel)
+    if (tc < pb && r >= tc) F[(p0 + r) + (p0 + tc) * m] = B[tc][r];
+  // inverse of the unit lower L11, column c by thread c
+  T* Li = Linv + (uint64_t)blockIdx.x * kPanel * kPanel;
+  if (threadIdx.x < pb) {
+    const int c = threadIdx.x;
+    for (int r = 0; r < c; r++) Li[r + c * kPanel] = T(0);
+    Li[c + c * kPanel] = T(1);
+    for (int r = c + 1; r < pb; r++) {
+      T acc = -B[c][r];
+      for (int q = c + 1; q < r; q++) acc -= B[q][r] * Li[q + c * kPanel];
+      Li[r + c * kPanel] = acc;
+    }
   }
 }
 
-// blocked path, step 2: rows i >= p0+pb of the panel: w = f L11^-T (forward
-// substitution with the unit lower L11), W[i] = w, F[i] = l = w / d
+// step 2: the panel rows i >= q0 = p0+pb: W = F21 Linv^T (W = L21 D), F21 <- W D^-1;
+// 64-row tiles, 4 rows x 4 columns per thread
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
-    panel_rows_kernel(T* __restrict__ F, int64_t m, int64_t p0, int pb, T* __restrict__ W,
-                      int64_t ldw) {
-  __shared__ T L[kPanel][kPanel + 1];   // L[col][row]
-  __shared__ T D[kPanel];
-  for (int t = threadIdx.x; t < pb * pb; t += blockDim.x) {
-    const int r = t % pb, c = t / pb;
-    L[c][r] = r > c ? F[(p0 + r) + (p0 + c) * m] : T(0);
+    batched_panel_kernel(BigBatch b, LdltDev d, T* __restrict__ front, int64_t p0,
+                         const T* __restrict__ Linv, T* __restrict__ Wbuf) {
+  __shared__ T As[16][kTile + 1];
+  __shared__ T Bs[16][kPanel + 1];
+  __shared__ T Dv[kPanel];
+  const int s = b.list[blockIdx.y];
+  const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
+  const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
+  if (p0 >= k) return;
+  const int pb = (int)(k - p0 < kPanel ? k - p0 : kPanel);
+  const int64_t q0 = p0 + pb;
+  const int64_t i0 = q0 + (int64_t)blockIdx.x * kTile;
+  if (i0 >= m) return;
+  T* F = front + d.front_off[s];
+  T* W = Wbuf + b.w_off[blockIdx.y];
+  const T* Li = Linv + (uint64_t)blockIdx.y * kPanel * kPanel;
+  for (int t = threadIdx.x; t < pb; t += blockDim.x) Dv[t] = F[(p0 + t) + (p0 + t) * m];
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  T acc[4][4] = {};
+  for (int c0 = 0; c0 < pb; c0 += 16) {
+    for (int t = threadIdx.x; t < 16 * kTile; t += blockDim.x) {
+      const int cc = t / kTile, rr = t % kTile;
+      const int c2 = c0 + cc;
+      const int64_t i = i0 + rr;
+      As[cc][rr] = (c2 < pb && i < m) ? F[i + (p0 + c2) * m] : T(0);
+      // Bs[c2][c] = Linv[c][c2]
+      Bs[cc][rr] = (c2 < pb && rr < pb) ? Li[rr + c2 * kPanel] : T(0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int cc = 0; cc < 16; cc++) {
+      T a[4], bb[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) a[u] = As[cc][ty * 4 + u];
+#pragma unroll
+      for (int v = 0; v < 4; v++) bb[v] = Bs[cc][tx * 4 + v];
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+#pragma unroll
+        for (int v = 0; v < 4; v++) acc[u][v] += a[u] * bb[v];
+    }
+    __syncthreads();
   }
-  for (int t = threadIdx.x; t < pb; t += blockDim.x) D[t] = F[(p0 + t) + (p0 + t) * m];
-  __syncthreads();
-  const int64_t i = p0 + pb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= m) return;
-  T w[kPanel];
-#pragma unroll 4
-  for (int c = 0; c < pb; c++) {
-    T v = F[i + (p0 + c) * m];
-    for (int c2 = 0; c2 < c; c2++) v -= L[c2][c] * w[c2];
-    w[c] = v;
-  }
-  const int64_t r = i - (p0 + pb);
-  for (int c = 0; c < pb; c++) {
-    W[r + c * ldw] = w[c];
-    F[i + (p0 + c) * m] = w[c] / D[c];
+#pragma unroll
+  for (int u = 0; u < 4; u++) {
+    const int64_t i = i0 + ty * 4 + u;
+    if (i >= m) continue;
+#pragma unroll
+    for (int v = 0; v < 4; v++) {
+      const int c = tx * 4 + v;
+      if (c >= pb) continue;
+      W[(i - q0) + c * m] = acc[u][v];
+      F[i + (p0 + c) * m] = acc[u][v] / Dv[c];
+    }
   }
 }
 
-// blocked path, step 3: trailing lower triangle, F[i][j] -= sum_c L[i][c] W[j][c]
-// for i >= j >= q0 = p0+pb; 64x64 tiles, 4x4 outputs per thread
+// step 3: trailing lower triangle, F[i][j] -= sum_c L[i][c] W[j][c], i >= j >= q0;
+// 64x64 tiles (blockIdx.x, .y), front blockIdx.z, 4x4 outputs per thread
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
-    trailing_update_kernel(T* __restrict__ F, int64_t m, int64_t p0, int pb,
-                           const T* __restrict__ W, int64_t ldw) {
+    batched_trailing_kernel(BigBatch b, LdltDev d, T* __restrict__ front, int64_t p0,
+                            const T* __restrict__ Wbuf) {
   const int ti = blockIdx.x, tj = blockIdx.y;
   if (tj > ti) return;
+  const int s = b.list[blockIdx.z];
+  const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
+  const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
+  if (p0 >= k) return;
+  const int pb = (int)(k - p0 < kPanel ? k - p0 : kPanel);
   const int64_t q0 = p0 + pb;
+  const int64_t i0 = q0 + (int64_t)ti * kTile, j0 = q0 + (int64_t)tj * kTile;
+  if (i0 >= m) return;
+  T* F = front + d.front_off[s];
+  const T* W = Wbuf + b.w_off[blockIdx.z];
   __shared__ T As[16][kTile + 1];
   __shared__ T Bs[16][kTile + 1];
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-  const int64_t i0 = q0 + (int64_t)ti * kTile, j0 = q0 + (int64_t)tj * kTile;
   T acc[4][4] = {};
   for (int c0 = 0; c0 < pb; c0 += 16) {
     for (int t = threadIdx.x; t < 16 * kTile; t += blockDim.x) {
@@ -254,20 +323,20 @@ __global__ void __launch_bounds__(kThreads)
       const int c = c0 + cc;
       const int64_t i = i0 + rr, j = j0 + rr;
       As[cc][rr] = (c < pb && i < m) ? F[i + (p0 + c) * m] : T(0);
-      Bs[cc][rr] = (c < pb && j < m) ? W[(j - q0) + c * ldw] : T(0);
+      Bs[cc][rr] = (c < pb && j < m) ? W[(j - q0) + c * m] : T(0);
     }
     __syncthreads();
 #pragma unroll
     for (int cc = 0; cc < 16; cc++) {
-      T a[4], b[4];
+      T a[4], bb[4];
 #pragma unroll
       for (int u = 0; u < 4; u++) a[u] = As[cc][ty * 4 + u];
 #pragma unroll
-      for (int v = 0; v < 4; v++) b[v] = Bs[cc][tx * 4 + v];
+      for (int v = 0; v < 4; v++) bb[v] = Bs[cc][tx * 4 + v];
 #pragma unroll
       for (int u = 0; u < 4; u++)
 #pragma unroll
-        for (int v = 0; v < 4; v++) acc[u][v] += a[u] * b[v];
+        for (int v = 0; v < 4; v++) acc[u][v] += a[u] * bb[v];
     }
     __syncthreads();
   }
@@ -306,51 +375,80 @@ __global__ void vec_extend_add_kernel(const int32_t* __restrict__ children, Ldlt
   for (int64_t i = threadIdx.x; i < mc - kc; i += blockDim.x) dst[rel[i]] += src[i];
 }
 
-// forward: v[0:k] <- D^-1 L11^-1 v[0:k], v[k:m] <- v[k:m] - L21 (L11^-1 v[0:k])
+// forward: v[0:k] <- D^-1 L11^-1 v[0:k], v[k:m] <- v[k:m] - L21 (L11^-1 v[0:k]);
+// blocks of 64 pivots: the block's unit triangle in shared memory, then one
+// pass over the rows below it
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
     forward_kernel(const int32_t* __restrict__ list, LdltDev d, const T* __restrict__ front,
                    double* __restrict__ vec) {
+  __shared__ double yb[kPanel];
   const int s = list[blockIdx.x];
   const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
   const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
   const T* F = front + d.front_off[s];
   double* v = vec + d.vec_off[s];
-  for (int64_t c = 0; c < k; c++) {
+  for (int64_t c0 = 0; c0 < k; c0 += kPanel) {
+    const int cb = (int)(k - c0 < kPanel ? k - c0 : kPanel);
+    if (threadIdx.x < cb) yb[threadIdx.x] = v[c0 + threadIdx.x];
     __syncthreads();
-    const double y = v[c];
-    for (int64_t i = c + 1 + threadIdx.x; i < m; i += blockDim.x) v[i] -= (double)F[i + c * m] * y;
+    for (int c = 0; c < cb; c++) {
+      const int t = threadIdx.x;
+      if (t > c && t < cb) yb[t] -= (double)F[(c0 + t) + (c0 + c) * m] * yb[c];
+      __syncthreads();
+    }
+    if (threadIdx.x < cb) v[c0 + threadIdx.x] = yb[threadIdx.x];
+    for (int64_t i = c0 + cb + threadIdx.x; i < m; i += blockDim.x) {
+      double acc = 0.0;
+      for (int c = 0; c < cb; c++) acc += (double)F[i + (c0 + c) * m] * yb[c];
+      v[i] -= acc;
+    }
+    __syncthreads();
   }
-  __syncthreads();
   for (int64_t c = threadIdx.x; c < k; c += blockDim.x) v[c] /= (double)F[c + c * m];
 }
 
 // backward: x[0:k] = L11^-T (v[0:k] - L21^T x_rest), x_rest gathered from the
-// solved ancestors (factor order), written to xf
+// solved ancestors (factor order), written to xf; blocks of 64 pivots from the
+// last: the contributions of the solved pivots below the block (a warp per
+// column), then the block's triangle in shared memory
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
     backward_kernel(const int32_t* __restrict__ list, LdltDev d, const T* __restrict__ front,
                     double* __restrict__ vec, double* __restrict__ xf) {
+  __shared__ double xb[kPanel];
   const int s = list[blockIdx.x];
   const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
   const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
   const int32_t* rows = d.rows + d.row_ptr[s];
   const T* F = front + d.front_off[s];
   double* v = vec + d.vec_off[s];
-  // t_c = v_c - sum_{i >= k} L[i][c] x[rows[i]]: a warp per column
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int64_t c = warp; c < k; c += blockDim.x / 32) {
+  const int nwarps = blockDim.x / 32;
+  for (int64_t c = warp; c < k; c += nwarps) {
     double acc = 0.0;
     for (int64_t i = k + lane; i < m; i += 32) acc += (double)F[i + c * m] * xf[rows[i]];
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
     if (lane == 0) v[c] -= acc;
   }
-  for (int64_t c = k - 1; c >= 0; c--) {
-    __syncthreads();
-    const double x = v[c];
-    for (int64_t i = threadIdx.x; i < c; i += blockDim.x) v[i] -= (double)F[c + i * m] * x;
-  }
   __syncthreads();
+  for (int64_t c0 = ((k - 1) / kPanel) * kPanel; c0 >= 0; c0 -= kPanel) {
+    const int cb = (int)(k - c0 < kPanel ? k - c0 : kPanel);
+    for (int c = warp; c < cb; c += nwarps) {
+      double acc = 0.0;
+      for (int64_t i = c0 + cb + lane; i < k; i += 32) acc += (double)F[i + (c0 + c) * m] * v[i];
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+      if (lane == 0) xb[c] = v[c0 + c] - acc;
+    }
+    __syncthreads();
+    for (int c = cb - 1; c >= 0; c--) {
+      const int t = threadIdx.x;
+      if (t < c) xb[t] -= (double)F[(c0 + c) + (c0 + t) * m] * xb[c];
+      __syncthreads();
+    }
+    if (threadIdx.x < cb) v[c0 + threadIdx.x] = xb[threadIdx.x];
+    __syncthreads();
+  }
   const int32_t f = d.sn_first[s];
   for (int64_t c = threadIdx.x; c < k; c += blockDim.x) xf[f + c] = v[c];
 }
@@ -424,7 +522,8 @@ struct nla3d_ldlt {
   double* d_maxpart = nullptr;
   int* d_perturbed = nullptr;
   void* d_W = nullptr;
-  int64_t ldw = 0;
+  void* d_Linv = nullptr;
+  uint64_t* d_wo = nullptr;
   uint64_t* d_adest = nullptr;
   int32_t* d_perm = nullptr;
   int32_t* d_col2sn = nullptr;
@@ -437,7 +536,10 @@ struct nla3d_ldlt {
   struct Level {
     int64_t all_off = 0, all_cnt = 0;     // every supernode of the level
     int64_t small_off = 0, small_cnt = 0;
-    std::vector<int32_t> large;
+    int32_t small_max_m = 0;
+    int64_t large_off = 0, large_cnt = 0; // fronts above kSmallFront rows
+    int64_t wo_off = 0;                   // their W offsets in d_wo
+    int64_t large_max_m = 0, large_max_k = 0;
     std::vector<int64_t> ea_off, ea_cnt;  // children of the level's parents, by ordinal
   };
   std::vector<Level> levels;
@@ -503,23 +605,25 @@ cudaError_t enqueue_factor(nla3d_ldlt* h, const double* values) {
       extend_add_kernel<T><<<grid, kThreads, 0, st>>>(h->d_lists + L.ea_off[q], (int)L.ea_cnt[q],
                                                       h->dev, front);
     }
-    if (L.small_cnt)
-      factor_small_kernel<T><<<(unsigned)L.small_cnt, kThreads, 0, st>>>(
+    if (L.small_cnt) {
+      const size_t smem = sizeof(T) * (size_t)L.small_max_m * (L.small_max_m + 1);
+      factor_small_kernel<T><<<(unsigned)L.small_cnt, kThreads, smem, st>>>(
           h->d_lists + L.small_off, h->dev, front, h->d_maxabs, h->pivot_rel, h->d_perturbed);
-    for (int32_t s : L.large) {
-      const int64_t m = S.m(s), k = S.k(s);
-      T* F = front + S.front_off[s];
+    }
+    if (L.large_cnt) {
+      const BigBatch bb{h->d_lists + L.large_off, h->d_wo + L.wo_off};
       T* W = static_cast<T*>(h->d_W);
-      for (int64_t p0 = 0; p0 < k; p0 += kPanel) {
-        const int pb = (int)std::min<int64_t>(kPanel, k - p0);
-        diag_block_kernel<T><<<1, kThreads, 0, st>>>(F, m, p0, pb, h->d_maxabs, h->pivot_rel,
-                                                     h->d_perturbed);
-        const int64_t rest = m - p0 - pb;
+      T* Li = static_cast<T*>(h->d_Linv);
+      const unsigned nf = (unsigned)L.large_cnt;
+      for (int64_t p0 = 0; p0 < L.large_max_k; p0 += kPanel) {
+        batched_diag_kernel<T><<<nf, kThreads, 0, st>>>(bb, h->dev, front, p0, Li, h->d_maxabs,
+                                                        h->pivot_rel, h->d_perturbed);
+        const int64_t rest = L.large_max_m - p0 - 1;   // rows past the smallest panel
         if (rest <= 0) continue;
-        panel_rows_kernel<T><<<(unsigned)((rest + kThreads - 1) / kThreads), kThreads, 0, st>>>(
-            F, m, p0, pb, W, h->ldw);
         const unsigned tiles = (unsigned)((rest + kTile - 1) / kTile);
-        trailing_update_kernel<T><<<dim3(tiles, tiles), kThreads, 0, st>>>(F, m, p0, pb, W, h->ldw);
+        batched_panel_kernel<T><<<dim3(tiles, nf), kThreads, 0, st>>>(bb, h->dev, front, p0, Li, W);
+        batched_trailing_kernel<T><<<dim3(tiles, tiles, nf), kThreads, 0, st>>>(bb, h->dev, front,
+                                                                              p0, W);
       }
     }
   }
@@ -606,7 +710,8 @@ int nla3d_ldlt_create(int64_t n, const uint32_t* iofeir, const uint32_t* columns
   std::vector<int32_t> col2sn(S.n);
   for (int64_t s = 0; s < ns; s++)
     for (int32_t t = S.sn_first[s]; t < S.sn_first[s + 1]; t++) col2sn[t] = (int32_t)s;
-  int64_t max_large = 0;
+  std::vector<uint64_t> wo;
+  int64_t max_w = 0, max_large_cnt = 0;
   h->levels.resize(nlev);
   for (int L = 0; L < nlev; L++) {
     auto& lv = h->levels[L];
@@ -616,14 +721,28 @@ int nla3d_ldlt_create(int64_t n, const uint32_t* iofeir, const uint32_t* columns
     lv.small_off = (int64_t)lists.size();
     for (int32_t q = S.level_ptr[L]; q < S.level_ptr[L + 1]; q++) {
       const int32_t s = S.level_list[q];
-      if (S.m(s) <= kSmallFront)
+      if (S.m(s) <= kSmallFront) {
         lists.push_back(s);
-      else {
-        lv.large.push_back(s);
-        max_large = std::max<int64_t>(max_large, S.m(s));
+        lv.small_max_m = std::max(lv.small_max_m, S.m(s));
       }
     }
     lv.small_cnt = (int64_t)lists.size() - lv.small_off;
+    lv.large_off = (int64_t)lists.size();
+    lv.wo_off = (int64_t)wo.size();
+    int64_t w = 0;
+    for (int32_t q = S.level_ptr[L]; q < S.level_ptr[L + 1]; q++) {
+      const int32_t s = S.level_list[q];
+      if (S.m(s) > kSmallFront) {
+        lists.push_back(s);
+        wo.push_back((uint64_t)w);
+        w += (int64_t)S.m(s) * kPanel;
+        lv.large_max_m = std::max<int64_t>(lv.large_max_m, S.m(s));
+        lv.large_max_k = std::max<int64_t>(lv.large_max_k, S.k(s));
+      }
+    }
+    lv.large_cnt = (int64_t)lists.size() - lv.large_off;
+    max_w = std::max(max_w, w);
+    max_large_cnt = std::max(max_large_cnt, lv.large_cnt);
     int maxc = 0;
     for (int32_t q = S.level_ptr[L]; q < S.level_ptr[L + 1]; q++) {
       const int32_t s = S.level_list[q];
@@ -638,7 +757,7 @@ int nla3d_ldlt_create(int64_t n, const uint32_t* iofeir, const uint32_t* columns
       lv.ea_cnt.push_back((int64_t)lists.size() - lv.ea_off.back());
     }
   }
-  if (lists.size() >= (size_t)INT32_MAX) {
+  if (lists.size() >= (size_t)INT32_MAX || max_large_cnt > 65535) {
     delete h;
     return NLA3D_ERR_RANGE;
   }
@@ -674,11 +793,21 @@ int nla3d_ldlt_create(int64_t n, const uint32_t* iofeir, const uint32_t* columns
     LCK(dalloc(h, reinterpret_cast<float**>(&h->d_front), h->front_entries));
   else
     LCK(dalloc(h, reinterpret_cast<double**>(&h->d_front), h->front_entries));
-  h->ldw = std::max<int64_t>(max_large, 1);
-  if (precision)
-    LCK(dalloc(h, reinterpret_cast<float**>(&h->d_W), (size_t)h->ldw * kPanel));
-  else
-    LCK(dalloc(h, reinterpret_cast<double**>(&h->d_W), (size_t)h->ldw * kPanel));
+  const size_t nlinv = (size_t)std::max<int64_t>(max_large_cnt, 1) * kPanel * kPanel;
+  if (precision) {
+    LCK(dalloc(h, reinterpret_cast<float**>(&h->d_W), (size_t)max_w));
+    LCK(dalloc(h, reinterpret_cast<float**>(&h->d_Linv), nlinv));
+    LCK(cudaFuncSetAttribute(factor_small_kernel<float>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(sizeof(float) * kSmallFront * (kSmallFront + 1))));
+  } else {
+    LCK(dalloc(h, reinterpret_cast<double**>(&h->d_W), (size_t)max_w));
+    LCK(dalloc(h, reinterpret_cast<double**>(&h->d_Linv), nlinv));
+    LCK(cudaFuncSetAttribute(factor_small_kernel<double>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(sizeof(double) * kSmallFront * (kSmallFront + 1))));
+  }
+  LCK(upload(h, &h->d_wo, wo));
   LCK(dalloc(h, &h->d_vec, S.vec_off.back()));
   LCK(dalloc(h, &h->d_xf, S.n));
   LCK(dalloc(h, &h->d_r, S.n));
