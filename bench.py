@@ -68,6 +68,15 @@ def parse():
     ap.add_argument("--model", choices=["3d_damper", "a2000"],
                     help="run one of the reference's BENCH models instead (minutes)")
     ap.add_argument("--model-backend", default="fp64", choices=["fp64", "mixed", "port"])
+    ap.add_argument("--solver-bench", type=int, default=0, metavar="NX",
+                    help="time the device LDL^T of K(2) on the NX x NX x 4NX rigid-body bar "
+                         "(40: the 1.07M-equation Newton bar) and exit")
+    ap.add_argument("--solver-precisions", default="fp32,fp64")
+    ap.add_argument("--newton-bar", type=int, default=0, metavar="NX",
+                    help="Newton study on the NX x NX x 4NX torsion + stretch bar (40: the "
+                         "256k-element bar): plain vs learned start, FP64 vs mixed assembly, "
+                         "K(2) factored on the device; prints one JSON line and exits")
+    ap.add_argument("--newton-starts", default="plain,learned")
     ap.add_argument("--model-solver", default="nd", choices=["nd", "gpu", "gpu-fp32", "direct"],
                     help="K(2) solve of --model runs: host SuperLU after nested dissection, "
                          "or the device LDL^T with FP64 / FP32 fronts")
@@ -615,8 +624,115 @@ def run_cdb_model(args):
                  f"{len(fixes)} fixed DoFs"}), flush=True)
 
 
+def run_solver_bench(args):
+    """The EquationSolver consumer of the assembled K(2) on the device: the
+    nx x nx x 4nx bar of the Newton study (rigid-body MPC end, Neo-Hookean
+    G = 1, K = 1000) assembled on the GPU at its initial state, a geometric
+    nested-dissection order (MPC equations last), the symbolic analysis on
+    the host, then the timed factorisation (CUDA events around
+    nla3d_ldlt_factor) and one refined solve.  Prints one JSON line per
+    front precision."""
+    import math
+    import torch
+    from nla3d_gb300 import learned as L, ldlt
+    from nla3d_gb300.newton import NewtonSolver, csr_full, nested_dissection
+    from nla3d_gb300.storage import FEStorage
+    nx = args.solver_bench
+    pb = L.bar_problem(nx, 4 * nx, 0.5, 1000.0, 2.0, math.pi / 2)
+    t0 = time.perf_counter()
+    s = FEStorage(pb.mesh).initSolutionData()
+    ns = NewtonSolver(s, pb.fixes, solver="gpu")
+    s.set_U(np.zeros(s.n_total))
+    s.assemble()
+    s.synchronize()
+    io, co = s.pattern(2)
+    n2 = io.size - 1
+    K = csr_full(io, co, np.ones(co.size), n2, n2, True)
+    perm = ldlt.saddle_order(io, co, nested_dissection(K, ns._row_points()), s.n_unk)
+    t_order = time.perf_counter() - t0
+    rhs = np.random.default_rng(0).standard_normal(n2)
+    for prec in args.solver_precisions.split(","):
+        t1 = time.perf_counter()
+        solver = ldlt.DeviceLDLT.for_storage(s, perm, prec)
+        t_create = time.perf_counter() - t1
+        info = solver.info()
+        vals = s.device_K(2)[0]
+        times = []
+        for _ in range(2):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            solver.factor_device(vals)
+            e1.record()
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+        t2 = time.perf_counter()
+        x = solver.solve_host(s, rhs, max_refine=20, tol=1e-10)
+        t_solve = time.perf_counter() - t2
+        fac = times[-1]
+        print(json.dumps({
+            "metric": "K(2) LDL^T factorisation on the device", "precision": prec,
+            "value": fac, "unit": "s", "higher_is_better": False,
+            "workload": f"rigid-body bar {nx}x{nx}x{4 * nx}, n={n2}, nnz(upper)={co.size}",
+            "flops": info["flops"], "gflops": info["flops"] / fac / 1e9,
+            "nnz_L": info["nnz_L"], "front_GB": info["front_bytes"] / 1e9,
+            "supernodes": info["supernodes"], "levels": info["levels"],
+            "max_front": info["max_front"], "perturbed_pivots": info["perturbed"],
+            "factor_s_first": times[0], "solve_s": t_solve, "refine_steps": solver.last_steps,
+            "rel_residual": solver.last_residual, "order_s": t_order, "symbolic_s": t_create,
+            "x_norm": float(np.linalg.norm(x))}), flush=True)
+        solver.close()
+        del solver
+        torch.cuda.empty_cache()
+
+
+def run_newton_bar(args):
+    """Newton-Raphson on the nx x nx x 4nx bar (Neo-Hookean C10 = 0.5, K =
+    1000, z = 0 clamped, z = L slaved to a master driven to stretch 2.0 and
+    90 deg over 50 load steps, residual tolerance 1e-8) with the assembly on
+    the GPU and K(2) factored on the device (FP32 fronts, FP64 refinement).
+    The learned start's MLP is trained on small bars (3 x 3 x 12, C10, K,
+    stretch and twist drawn around the target) by the library's kernels, then
+    used on the large bar through its coarse modes.  Mean Newton iterations
+    per load step for each start, and for FP64 vs mixed assembly."""
+    import math
+    from nla3d_gb300 import learned as L
+    nx = args.newton_bar
+    log = lambda m: print(m, file=sys.stderr, flush=True)  # noqa: E731
+    t0 = time.perf_counter()
+    starts = tuple(args.newton_starts.split(","))
+    mlp = None
+    train = {}
+    if "learned" in starts:
+        Xb, Yb, _ = L.generate(L.sample_bar_problems(12, nx=3, nz=12, seed=5, n_loadsteps=50))
+        mlp = L.MLP(seed=1)
+        hist = mlp.fit(Xb, Yb, epochs=300, batch=128, lr=2e-3)
+        train = {"train_samples": int(Xb.shape[0]), "final_loss": hist[-1][1],
+                 "train_s": time.perf_counter() - t0}
+        log(f"trained: {train}")
+    cfg = L.bar_problem(nx, 4 * nx, 0.5, 1000.0, 2.0, math.pi / 2, 50)
+    res = {}
+    res["fp64_assembly"] = L.evaluate([cfg], mlp, precision="fp64", linear_solver="gpu-fp32",
+                                      starts=starts, log=log)
+    res["mixed_assembly"] = L.evaluate([cfg], mlp, precision="mixed", linear_solver="gpu-fp32",
+                                       starts=("plain",), log=log)
+    print(json.dumps({
+        "metric": "Newton iterations per load step (residual 1e-8)", "unit": "iterations",
+        "higher_is_better": False,
+        "workload": f"torsion + stretch bar {nx}x{nx}x{4 * nx} ({cfg.mesh.n_elems} SOLID81), "
+                    "rigid-body MPC end, 50 load steps",
+        "linear_solver": "device LDL^T, FP32 fronts + FP64 refinement",
+        "results": res, "training": train, "wall_s": time.perf_counter() - t0}), flush=True)
+
+
 def main():
     args = parse()
+    if args.newton_bar:
+        run_newton_bar(args)
+        return
+    if args.solver_bench:
+        run_solver_bench(args)
+        return
     if args.model:
         run_cdb_model(args)
         return

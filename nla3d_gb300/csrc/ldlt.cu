@@ -180,10 +180,11 @@ __global__ void __launch_bounds__(kThreads)
 struct BigBatch {
   const int32_t* list;
   const uint64_t* w_off;
+  const uint64_t* li_off;   // the front's inverted diagonal blocks, 64 x 64 per panel
 };
 
 // step 1: LDL^T of the pb x pb diagonal block, and the inverse of its unit
-// lower factor (Linv, 64 x 64 column-major per front) for step 2
+// lower factor (64 x 64 column-major, kept per panel for step 2 and the solves)
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
     batched_diag_kernel(BigBatch b, LdltDev d, T* __restrict__ front, int64_t p0,
@@ -221,7 +222,7 @@ __global__ void __launch_bounds__(kThreads)
   for (int r = tr; r < pb; r += kThreads / kPanel)
     if (tc < pb && r >= tc) F[(p0 + r) + (p0 + tc) * m] = B[tc][r];
   // inverse of the unit lower L11, column c by thread c
-  T* Li = Linv + (uint64_t)blockIdx.x * kPanel * kPanel;
+  T* Li = Linv + b.li_off[blockIdx.x] + (uint64_t)(p0 / kPanel) * kPanel * kPanel;
   if (threadIdx.x < pb) {
     const int c = threadIdx.x;
     for (int r = 0; r < c; r++) Li[r + c * kPanel] = T(0);
@@ -253,7 +254,7 @@ __global__ void __launch_bounds__(kThreads)
   if (i0 >= m) return;
   T* F = front + d.front_off[s];
   T* W = Wbuf + b.w_off[blockIdx.y];
-  const T* Li = Linv + (uint64_t)blockIdx.y * kPanel * kPanel;
+  const T* Li = Linv + b.li_off[blockIdx.y] + (uint64_t)(p0 / kPanel) * kPanel * kPanel;
   for (int t = threadIdx.x; t < pb; t += blockDim.x) Dv[t] = F[(p0 + t) + (p0 + t) * m];
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
   T acc[4][4] = {};
@@ -296,11 +297,14 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // step 3: trailing lower triangle, F[i][j] -= sum_c L[i][c] W[j][c], i >= j >= q0;
-// 64x64 tiles (blockIdx.x, .y), front blockIdx.z, 4x4 outputs per thread
-template <typename T>
+// BT x BT tiles (blockIdx.x, .y), front blockIdx.z, RT x RT outputs per thread
+// (64 / 4 for FP64, whose FMA pipe bounds it anyway; 128 / 8 for FP32)
+template <typename T, int BT, int RT>
 __global__ void __launch_bounds__(kThreads)
     batched_trailing_kernel(BigBatch b, LdltDev d, T* __restrict__ front, int64_t p0,
                             const T* __restrict__ Wbuf) {
+  static_assert((BT / RT) * (BT / RT) == kThreads, "one output block per thread");
+  constexpr int TD = BT / RT;
   const int ti = blockIdx.x, tj = blockIdx.y;
   if (tj > ti) return;
   const int s = b.list[blockIdx.z];
@@ -309,17 +313,17 @@ __global__ void __launch_bounds__(kThreads)
   if (p0 >= k) return;
   const int pb = (int)(k - p0 < kPanel ? k - p0 : kPanel);
   const int64_t q0 = p0 + pb;
-  const int64_t i0 = q0 + (int64_t)ti * kTile, j0 = q0 + (int64_t)tj * kTile;
+  const int64_t i0 = q0 + (int64_t)ti * BT, j0 = q0 + (int64_t)tj * BT;
   if (i0 >= m) return;
   T* F = front + d.front_off[s];
   const T* W = Wbuf + b.w_off[blockIdx.z];
-  __shared__ T As[16][kTile + 1];
-  __shared__ T Bs[16][kTile + 1];
-  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-  T acc[4][4] = {};
+  __shared__ T As[16][BT + 1];
+  __shared__ T Bs[16][BT + 1];
+  const int tx = threadIdx.x % TD, ty = threadIdx.x / TD;
+  T acc[RT][RT] = {};
   for (int c0 = 0; c0 < pb; c0 += 16) {
-    for (int t = threadIdx.x; t < 16 * kTile; t += blockDim.x) {
-      const int cc = t / kTile, rr = t % kTile;
+    for (int t = threadIdx.x; t < 16 * BT; t += blockDim.x) {
+      const int cc = t / BT, rr = t % BT;
       const int c = c0 + cc;
       const int64_t i = i0 + rr, j = j0 + rr;
       As[cc][rr] = (c < pb && i < m) ? F[i + (p0 + c) * m] : T(0);
@@ -328,29 +332,38 @@ __global__ void __launch_bounds__(kThreads)
     __syncthreads();
 #pragma unroll
     for (int cc = 0; cc < 16; cc++) {
-      T a[4], bb[4];
+      T a[RT], bb[RT];
 #pragma unroll
-      for (int u = 0; u < 4; u++) a[u] = As[cc][ty * 4 + u];
+      for (int u = 0; u < RT; u++) a[u] = As[cc][ty * RT + u];
 #pragma unroll
-      for (int v = 0; v < 4; v++) bb[v] = Bs[cc][tx * 4 + v];
+      for (int v = 0; v < RT; v++) bb[v] = Bs[cc][tx * RT + v];
 #pragma unroll
-      for (int u = 0; u < 4; u++)
+      for (int u = 0; u < RT; u++)
 #pragma unroll
-        for (int v = 0; v < 4; v++) acc[u][v] += a[u] * bb[v];
+        for (int v = 0; v < RT; v++) acc[u][v] += a[u] * bb[v];
     }
     __syncthreads();
   }
 #pragma unroll
-  for (int u = 0; u < 4; u++) {
-    const int64_t i = i0 + ty * 4 + u;
+  for (int u = 0; u < RT; u++) {
+    const int64_t i = i0 + ty * RT + u;
     if (i >= m) continue;
 #pragma unroll
-    for (int v = 0; v < 4; v++) {
-      const int64_t j = j0 + tx * 4 + v;
+    for (int v = 0; v < RT; v++) {
+      const int64_t j = j0 + tx * RT + v;
       if (j < m && j <= i) F[i + j * m] -= acc[u][v];
     }
   }
 }
+
+template <typename T>
+struct TrailingShape {
+  static constexpr int BT = 64, RT = 4;
+};
+template <>
+struct TrailingShape<float> {
+  static constexpr int BT = 128, RT = 8;
+};
 
 // ---- solve kernels ----
 
@@ -453,6 +466,149 @@ __global__ void __launch_bounds__(kThreads)
   for (int64_t c = threadIdx.x; c < k; c += blockDim.x) xf[f + c] = v[c];
 }
 
+// Solves of the large supernodes, batched per level like their factorisation
+// (blockIdx picks the supernode in the level's large list; panels of 64
+// pivots, each diagonal block applied through its stored inverse).
+
+// forward, panel c0: y_B = Linv_B v_B
+template <typename T>
+__global__ void fwd_diag_kernel(BigBatch b, LdltDev d, const T* __restrict__ Linv, int64_t c0,
+                                double* __restrict__ vec) {
+  __shared__ double vb[kPanel];
+  const int s = b.list[blockIdx.x];
+  const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
+  if (c0 >= k) return;
+  const int cb = (int)(k - c0 < kPanel ? k - c0 : kPanel);
+  double* v = vec + d.vec_off[s];
+  if (threadIdx.x < cb) vb[threadIdx.x] = v[c0 + threadIdx.x];
+  __syncthreads();
+  const T* Li = Linv + b.li_off[blockIdx.x] + (uint64_t)(c0 / kPanel) * kPanel * kPanel;
+  const int t = threadIdx.x;
+  if (t < cb) {
+    double acc = 0.0;
+    for (int c = 0; c <= t; c++) acc += (double)Li[t + c * kPanel] * vb[c];
+    v[c0 + t] = acc;
+  }
+}
+
+// forward, panel c0: v[i] -= sum_c L[i][c0+c] y_c for the rows below the panel
+template <typename T>
+__global__ void fwd_rows_kernel(BigBatch b, LdltDev d, const T* __restrict__ front, int64_t c0,
+                                double* __restrict__ vec) {
+  __shared__ double yb[kPanel];
+  const int s = b.list[blockIdx.y];
+  const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
+  const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
+  if (c0 >= k) return;
+  const int cb = (int)(k - c0 < kPanel ? k - c0 : kPanel);
+  const int64_t r0 = c0 + cb + (int64_t)blockIdx.x * blockDim.x;
+  if (r0 >= m) return;
+  const T* F = front + d.front_off[s];
+  double* v = vec + d.vec_off[s];
+  if (threadIdx.x < cb) yb[threadIdx.x] = v[c0 + threadIdx.x];
+  __syncthreads();
+  const int64_t i = r0 + threadIdx.x;
+  if (i < m) {
+    double acc = 0.0;
+    for (int c = 0; c < cb; c++) acc += (double)F[i + (c0 + c) * m] * yb[c];
+    v[i] -= acc;
+  }
+}
+
+// after the forward panels: v[0:k] <- D^-1 v[0:k]
+template <typename T>
+__global__ void scale_pivots_kernel(BigBatch b, LdltDev d, const T* __restrict__ front,
+                                    double* __restrict__ vec) {
+  const int s = b.list[blockIdx.y];
+  const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
+  const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= k) return;
+  const T* F = front + d.front_off[s];
+  vec[d.vec_off[s] + c] /= (double)F[c + c * m];
+}
+
+// backward: t_c = v_c - sum_{i >= k} L[i][c] x[rows[i]], 32 columns per block
+// (a warp per column)
+template <typename T>
+__global__ void bwd_rest_kernel(BigBatch b, LdltDev d, const T* __restrict__ front,
+                                double* __restrict__ vec, const double* __restrict__ xf) {
+  const int s = b.list[blockIdx.y];
+  const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
+  const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
+  const int64_t cbeg = (int64_t)blockIdx.x * 32;
+  if (cbeg >= k) return;
+  const int32_t* rows = d.rows + d.row_ptr[s];
+  const T* F = front + d.front_off[s];
+  double* v = vec + d.vec_off[s];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t cend = cbeg + 32 < k ? cbeg + 32 : k;
+  for (int64_t c = cbeg + warp; c < cend; c += blockDim.x / 32) {
+    double acc = 0.0;
+    for (int64_t i = k + lane; i < m; i += 32) acc += (double)F[i + c * m] * xf[rows[i]];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) v[c] -= acc;
+  }
+}
+
+// backward, panel c0: x_B = Linv_B^T t_B
+template <typename T>
+__global__ void bwd_diag_kernel(BigBatch b, LdltDev d, const T* __restrict__ Linv, int64_t c0,
+                                double* __restrict__ vec) {
+  __shared__ double tb[kPanel];
+  const int s = b.list[blockIdx.x];
+  const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
+  if (c0 >= k) return;
+  const int cb = (int)(k - c0 < kPanel ? k - c0 : kPanel);
+  double* v = vec + d.vec_off[s];
+  if (threadIdx.x < cb) tb[threadIdx.x] = v[c0 + threadIdx.x];
+  __syncthreads();
+  const T* Li = Linv + b.li_off[blockIdx.x] + (uint64_t)(c0 / kPanel) * kPanel * kPanel;
+  const int t = threadIdx.x;
+  if (t < cb) {
+    double acc = 0.0;
+    for (int c = t; c < cb; c++) acc += (double)Li[c + t * kPanel] * tb[c];
+    v[c0 + t] = acc;
+  }
+}
+
+// backward, panel c0: t[j] -= sum_c L[c0+c][j] x_B[c] for the pivots j < c0
+// (a warp per column j, lanes over the panel's 64 rows)
+template <typename T>
+__global__ void bwd_cols_kernel(BigBatch b, LdltDev d, const T* __restrict__ front, int64_t c0,
+                                double* __restrict__ vec) {
+  __shared__ double xb[kPanel];
+  const int s = b.list[blockIdx.y];
+  const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
+  const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
+  if (c0 >= k) return;
+  const int64_t jbeg = (int64_t)blockIdx.x * (blockDim.x / 32) * 4;
+  if (jbeg >= c0) return;
+  const int cb = (int)(k - c0 < kPanel ? k - c0 : kPanel);
+  const T* F = front + d.front_off[s];
+  double* v = vec + d.vec_off[s];
+  if (threadIdx.x < cb) xb[threadIdx.x] = v[c0 + threadIdx.x];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t jend = jbeg + (blockDim.x / 32) * 4 < c0 ? jbeg + (blockDim.x / 32) * 4 : c0;
+  for (int64_t j = jbeg + warp; j < jend; j += blockDim.x / 32) {
+    double acc = 0.0;
+    for (int c = lane; c < cb; c += 32) acc += (double)F[(c0 + c) + j * m] * xb[c];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) v[j] -= acc;
+  }
+}
+
+// the solved pivots of the large supernodes into xf (factor order)
+__global__ void store_pivots_kernel(BigBatch b, LdltDev d, const double* __restrict__ vec,
+                                    double* __restrict__ xf) {
+  const int s = b.list[blockIdx.y];
+  const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= k) return;
+  xf[d.sn_first[s] + c] = vec[d.vec_off[s] + c];
+}
+
 __global__ void solve_finish_kernel(int64_t n, const int32_t* __restrict__ perm,
                                     const double* __restrict__ xf, double* __restrict__ x,
                                     int accumulate) {
@@ -524,6 +680,7 @@ struct nla3d_ldlt {
   void* d_W = nullptr;
   void* d_Linv = nullptr;
   uint64_t* d_wo = nullptr;
+  uint64_t* d_lio = nullptr;
   uint64_t* d_adest = nullptr;
   int32_t* d_perm = nullptr;
   int32_t* d_col2sn = nullptr;
@@ -611,7 +768,7 @@ cudaError_t enqueue_factor(nla3d_ldlt* h, const double* values) {
           h->d_lists + L.small_off, h->dev, front, h->d_maxabs, h->pivot_rel, h->d_perturbed);
     }
     if (L.large_cnt) {
-      const BigBatch bb{h->d_lists + L.large_off, h->d_wo + L.wo_off};
+      const BigBatch bb{h->d_lists + L.large_off, h->d_wo + L.wo_off, h->d_lio + L.wo_off};
       T* W = static_cast<T*>(h->d_W);
       T* Li = static_cast<T*>(h->d_Linv);
       const unsigned nf = (unsigned)L.large_cnt;
@@ -622,8 +779,10 @@ cudaError_t enqueue_factor(nla3d_ldlt* h, const double* values) {
         if (rest <= 0) continue;
         const unsigned tiles = (unsigned)((rest + kTile - 1) / kTile);
         batched_panel_kernel<T><<<dim3(tiles, nf), kThreads, 0, st>>>(bb, h->dev, front, p0, Li, W);
-        batched_trailing_kernel<T><<<dim3(tiles, tiles, nf), kThreads, 0, st>>>(bb, h->dev, front,
-                                                                              p0, W);
+        constexpr int BT = TrailingShape<T>::BT, RT = TrailingShape<T>::RT;
+        const unsigned ttiles = (unsigned)((rest + BT - 1) / BT);
+        batched_trailing_kernel<T, BT, RT><<<dim3(ttiles, ttiles, nf), kThreads, 0, st>>>(
+            bb, h->dev, front, p0, W);
       }
     }
   }
@@ -639,17 +798,50 @@ cudaError_t enqueue_solve(nla3d_ldlt* h, const double* b, double* x, int accumul
   if (e != cudaSuccess) return e;
   const unsigned nb = (unsigned)((S.n + kThreads - 1) / kThreads);
   solve_init_kernel<<<nb, kThreads, 0, st>>>(S.n, h->d_perm, h->d_col2sn, h->dev, b, h->d_vec);
+  const T* Li = static_cast<const T*>(h->d_Linv);
   for (const auto& L : h->levels) {
     for (size_t q = 0; q < L.ea_off.size(); q++)
       if (L.ea_cnt[q])
         vec_extend_add_kernel<<<(unsigned)L.ea_cnt[q], kThreads, 0, st>>>(h->d_lists + L.ea_off[q],
                                                                            h->dev, h->d_vec);
-    forward_kernel<T><<<(unsigned)L.all_cnt, kThreads, 0, st>>>(h->d_lists + L.all_off, h->dev,
-                                                                front, h->d_vec);
+    if (L.small_cnt)
+      forward_kernel<T><<<(unsigned)L.small_cnt, kThreads, 0, st>>>(h->d_lists + L.small_off,
+                                                                    h->dev, front, h->d_vec);
+    if (L.large_cnt) {
+      const BigBatch bb{h->d_lists + L.large_off, h->d_wo + L.wo_off, h->d_lio + L.wo_off};
+      const unsigned nf = (unsigned)L.large_cnt;
+      for (int64_t c0 = 0; c0 < L.large_max_k; c0 += kPanel) {
+        fwd_diag_kernel<T><<<nf, kPanel, 0, st>>>(bb, h->dev, Li, c0, h->d_vec);
+        const int64_t rest = L.large_max_m - c0 - 1;
+        if (rest > 0)
+          fwd_rows_kernel<T><<<dim3((unsigned)((rest + kThreads - 1) / kThreads), nf), kThreads, 0,
+                               st>>>(bb, h->dev, front, c0, h->d_vec);
+      }
+      scale_pivots_kernel<T><<<dim3((unsigned)((L.large_max_k + kThreads - 1) / kThreads), nf),
+                               kThreads, 0, st>>>(bb, h->dev, front, h->d_vec);
+    }
   }
-  for (auto it = h->levels.rbegin(); it != h->levels.rend(); ++it)
-    backward_kernel<T><<<(unsigned)it->all_cnt, kThreads, 0, st>>>(h->d_lists + it->all_off,
-                                                                   h->dev, front, h->d_vec, h->d_xf);
+  for (auto it = h->levels.rbegin(); it != h->levels.rend(); ++it) {
+    const auto& L = *it;
+    if (L.small_cnt)
+      backward_kernel<T><<<(unsigned)L.small_cnt, kThreads, 0, st>>>(h->d_lists + L.small_off,
+                                                                     h->dev, front, h->d_vec,
+                                                                     h->d_xf);
+    if (L.large_cnt) {
+      const BigBatch bb{h->d_lists + L.large_off, h->d_wo + L.wo_off, h->d_lio + L.wo_off};
+      const unsigned nf = (unsigned)L.large_cnt;
+      bwd_rest_kernel<T><<<dim3((unsigned)((L.large_max_k + 31) / 32), nf), kThreads, 0, st>>>(
+          bb, h->dev, front, h->d_vec, h->d_xf);
+      for (int64_t c0 = ((L.large_max_k - 1) / kPanel) * kPanel; c0 >= 0; c0 -= kPanel) {
+        bwd_diag_kernel<T><<<nf, kPanel, 0, st>>>(bb, h->dev, Li, c0, h->d_vec);
+        if (c0 > 0)
+          bwd_cols_kernel<T><<<dim3((unsigned)((c0 + 31) / 32), nf), kThreads, 0, st>>>(
+              bb, h->dev, front, c0, h->d_vec);
+      }
+      store_pivots_kernel<<<dim3((unsigned)((L.large_max_k + kThreads - 1) / kThreads), nf),
+                            kThreads, 0, st>>>(bb, h->dev, h->d_vec, h->d_xf);
+    }
+  }
   solve_finish_kernel<<<nb, kThreads, 0, st>>>(S.n, h->d_perm, h->d_xf, x, accumulate);
   return cudaGetLastError();
 }
@@ -710,8 +902,9 @@ int nla3d_ldlt_create(int64_t n, const uint32_t* iofeir, const uint32_t* columns
   std::vector<int32_t> col2sn(S.n);
   for (int64_t s = 0; s < ns; s++)
     for (int32_t t = S.sn_first[s]; t < S.sn_first[s + 1]; t++) col2sn[t] = (int32_t)s;
-  std::vector<uint64_t> wo;
+  std::vector<uint64_t> wo, lio;
   int64_t max_w = 0, max_large_cnt = 0;
+  uint64_t li_total = 0;
   h->levels.resize(nlev);
   for (int L = 0; L < nlev; L++) {
     auto& lv = h->levels[L];
@@ -736,6 +929,8 @@ int nla3d_ldlt_create(int64_t n, const uint32_t* iofeir, const uint32_t* columns
         lists.push_back(s);
         wo.push_back((uint64_t)w);
         w += (int64_t)S.m(s) * kPanel;
+        lio.push_back(li_total);
+        li_total += (uint64_t)((S.k(s) + kPanel - 1) / kPanel) * kPanel * kPanel;
         lv.large_max_m = std::max<int64_t>(lv.large_max_m, S.m(s));
         lv.large_max_k = std::max<int64_t>(lv.large_max_k, S.k(s));
       }
@@ -793,7 +988,7 @@ int nla3d_ldlt_create(int64_t n, const uint32_t* iofeir, const uint32_t* columns
     LCK(dalloc(h, reinterpret_cast<float**>(&h->d_front), h->front_entries));
   else
     LCK(dalloc(h, reinterpret_cast<double**>(&h->d_front), h->front_entries));
-  const size_t nlinv = (size_t)std::max<int64_t>(max_large_cnt, 1) * kPanel * kPanel;
+  const size_t nlinv = (size_t)std::max<uint64_t>(li_total, 1);
   if (precision) {
     LCK(dalloc(h, reinterpret_cast<float**>(&h->d_W), (size_t)max_w));
     LCK(dalloc(h, reinterpret_cast<float**>(&h->d_Linv), nlinv));
@@ -808,6 +1003,7 @@ int nla3d_ldlt_create(int64_t n, const uint32_t* iofeir, const uint32_t* columns
                              (int)(sizeof(double) * kSmallFront * (kSmallFront + 1))));
   }
   LCK(upload(h, &h->d_wo, wo));
+  LCK(upload(h, &h->d_lio, lio));
   LCK(dalloc(h, &h->d_vec, S.vec_off.back()));
   LCK(dalloc(h, &h->d_xf, S.n));
   LCK(dalloc(h, &h->d_r, S.n));

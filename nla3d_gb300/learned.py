@@ -338,11 +338,13 @@ def sample_bar_problems(count, nx=3, nz=12, seed=0, n_loadsteps=50):
 # data generation, training and evaluation
 # ---------------------------------------------------------------------------
 
-def solve(problem: Problem, backend, predictor_factory=None, residual_tol=1e-8, n_iterations=25):
+def solve(problem: Problem, backend, predictor_factory=None, residual_tol=1e-8, n_iterations=25,
+          linear_solver="direct"):
     """Run the Newton driver; returns (solver, history)."""
     from .newton import NewtonSolver
     solver = NewtonSolver(backend, problem.fixes, n_loadsteps=problem.n_loadsteps,
-                          n_iterations=n_iterations, residual_tol=residual_tol)
+                          n_iterations=n_iterations, residual_tol=residual_tol,
+                          solver=linear_solver)
     hist = History(backend.n_total)
     pred = predictor_factory(solver, hist) if predictor_factory else None
     solver.solve(predictor=pred, on_converged=hist)
@@ -388,23 +390,36 @@ def generate(problems, kind="gpu", precision="fp64"):
     return np.array(X), np.array(Y), iters
 
 
-def evaluate(problems, mlp, kind="gpu", precision="fp64"):
+def evaluate(problems, mlp, kind="gpu", precision="fp64", linear_solver="direct",
+             starts=("plain", "extrapolation", "learned"), log=None):
     """Mean Newton iterations per load step: plain start, secant extrapolation
     and the learned start (with the plain-start fallback)."""
-    out = {"plain": [], "extrapolation": [], "learned": [], "learned_used": []}
+    import time
+    out = {k: [] for k in starts}
+    out["learned_used"] = []
+    wall = {}
     for pb in problems:
         be = make_backend(pb, kind, precision)
         basis = basis_for(pb, be)
-        s, _ = solve(pb, be)
-        out["plain"] += [r.iterations for r in s.records]
-        be = make_backend(pb, kind, precision)
-        s, _ = solve(pb, be, lambda sv, h: ExtrapolationPredictor(h))
-        out["extrapolation"] += [r.iterations for r in s.records]
-        be = make_backend(pb, kind, precision)
-        s, _ = solve(pb, be, lambda sv, h: MLPPredictor(mlp, basis, h, pb.c10, pb.kbulk))
-        out["learned"] += [r.iterations for r in s.records]
-        out["learned_used"] += [r.predicted for r in s.records]
-    return {k: float(np.mean(v)) for k, v in out.items()} | {"steps": len(out["plain"])}
+        for start in starts:
+            if start != "plain":
+                be = make_backend(pb, kind, precision)
+            factory = None
+            if start == "extrapolation":
+                factory = lambda sv, h: ExtrapolationPredictor(h)  # noqa: E731
+            elif start == "learned":
+                factory = lambda sv, h: MLPPredictor(mlp, basis, h, pb.c10, pb.kbulk)  # noqa: E731
+            t0 = time.perf_counter()
+            s, _ = solve(pb, be, factory, linear_solver=linear_solver)
+            wall[start] = wall.get(start, 0.0) + time.perf_counter() - t0
+            out[start] += [r.iterations for r in s.records]
+            if start == "learned":
+                out["learned_used"] += [r.predicted for r in s.records]
+            if log:
+                log(f"{pb.label} {start}: {np.mean(out[start]):.3f} it/step, "
+                    f"{wall[start]:.1f} s, {s.factorizations} factorisations")
+    res = {k: float(np.mean(v)) for k, v in out.items() if v}
+    return res | {"steps": len(out[starts[0]]), "wall_s": wall}
 
 
 def benchmark(n_block_train=40, n_block_eval=8, n_bar_train=12, log=None):
