@@ -98,6 +98,11 @@ def _load(kind: str):
               "update", "assemble", "get_K", "get_F", "add_surface_lines", "set_transient",
               "get_C", "get_M"):
         f(n).restype = ctypes.c_int
+    if kind != "port":
+        lib.ref_set_R.argtypes = [_P, _P, ctypes.c_uint]
+        lib.ref_set_R.restype = ctypes.c_int
+        lib.ref_write_vtk.argtypes = [_P, ctypes.c_char_p, ctypes.c_int]
+        lib.ref_write_vtk.restype = ctypes.c_int
     if kind == "port":
         lib.orc_material_S.argtypes = [ctypes.c_int, _P, _P, ctypes.c_double, _P]
         lib.orc_material_D.argtypes = [ctypes.c_int, _P, _P, ctypes.c_double, _P, _P]
@@ -243,6 +248,16 @@ class OracleModel:
         v = np.zeros(self.n_total)
         self._check(self._f("get_F")(self.h, _ptr(v)))
         return v
+
+    def write_vtk(self, prefix, step, U, R):
+        """Compiled reference only: its VtkProcessor writes <prefix>0.vtk (and
+        <prefix><step>.vtk for step > 0) from vecU = U, vecR = R."""
+        if self.kind == "port":
+            raise OracleError("the VTK writer is the compiled reference's")
+        self.set_U(U)
+        R = np.ascontiguousarray(R, dtype=np.float64)
+        self._check(self.lib.ref_set_R(self.h, _ptr(R), R.size))
+        self._check(self.lib.ref_write_vtk(self.h, prefix.encode(), int(step)))
 
     def C(self, block):
         """Capacity matrix block of a transient model (K's pattern)."""

@@ -2,7 +2,8 @@
 // the reference checkout by oracle/Makefile into oracle/_ref/).  Test
 // infrastructure only: it lets the tests and the golden-fixture script drive
 // the reference's own FEStorage / SOLID81 / TETRA0 / QUADTH / RigidBodyMpc code
-// on synthetic meshes and read back its DoF numbering, CSR pattern, K and F.
+// on synthetic meshes and read back its DoF numbering, CSR pattern, K and F,
+// and have its VtkProcessor write the legacy VTK files of a state.
 //
 // It follows the reference's own set-up sequence:
 //   createNodes / createElements        (main.cpp:189-205)
@@ -22,6 +23,7 @@
 #include "FEStorage.h"
 #include "Mpc.h"
 #include "Node.h"
+#include "VtkProcessor.h"
 #include "elements/PLANE41.h"
 #include "elements/QUADTH.h"
 #include "elements/SOLID81.h"
@@ -335,6 +337,26 @@ int ref_get_C(void* h, int block, double* values) {
 
 int ref_get_M(void* h, int block, double* values) {
   return get_cm(static_cast<RefModel*>(h), false, block, values);
+}
+
+int ref_set_R(void* h, const double* R, unsigned n) {
+  RefModel* m = static_cast<RefModel*>(h);
+  return guarded(m, [&] {
+    math::dVec* v = m->storage.getR();
+    if (v->size() != n) LOG(FATAL) << "R size mismatch";
+    for (unsigned i = 0; i < n; i++) (*v)[i] = R[i];
+  });
+}
+
+// The reference's VtkProcessor (VtkProcessor.cpp): pre() writes <prefix>0.vtk,
+// process(step) writes <prefix><step>.vtk (step > 0), from the current vecU / vecR.
+int ref_write_vtk(void* h, const char* prefix, int step) {
+  RefModel* m = static_cast<RefModel*>(h);
+  return guarded(m, [&] {
+    VtkProcessor vtk(&m->storage, prefix);
+    vtk.pre();
+    if (step > 0) vtk.process((uint16)step);
+  });
 }
 
 int ref_get_F(void* h, double* F) {

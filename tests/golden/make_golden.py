@@ -336,6 +336,37 @@ def write_heat_fixture():
     print("wrote heat_quadth", quads.shape, lines.shape, len(md["loads"]), "F")
 
 
+VTK_CASES = ("bar_mpc_2x2x3", "quadth_lines_6x5", "plane41_nh_3x2", "tetra0_3x3x3")
+
+
+def vtk_state(name):
+    """The state the VTK fixtures are written from: the case's vecU and a
+    deterministic vecR."""
+    mesh, u, p, extra, do_update = cases.FULL_CASES[name]()
+    m = O.OracleModel(mesh, "port")
+    ne, ee = m.eq_numbers()
+    U = mg.u_to_vector(ne, ee, u, p, m.n_total, extra)
+    R = np.linspace(-1.5, 2.5, m.n_total) ** 3
+    return mesh, U, R
+
+
+def write_vtk_fixtures():
+    """The reference's own VtkProcessor output (pre() + process(7)) for a few
+    cases, as text fixtures vtk_<case>_<0|7>.vtk."""
+    import tempfile
+    for name in VTK_CASES:
+        mesh, U, R = vtk_state(name)
+        m = O.OracleModel(mesh, "ref")
+        with tempfile.TemporaryDirectory() as d:
+            prefix = os.path.join(d, "out")
+            m.write_vtk(prefix, 7, U, R)
+            for step in (0, 7):
+                with open(f"{prefix}{step}.vtk") as fh, \
+                        open(os.path.join(HERE, f"vtk_{name}_{step}.vtk"), "w") as out:
+                    out.write(fh.read())
+        print("wrote vtk", name)
+
+
 def write_rigid_body_fixture():
     base = "/root/reference/test/rigid_body_mpc"
     nodes, elems, comps, fixes, curve = read_rigid_body_case(
@@ -362,6 +393,7 @@ def main():
     write_heat_fixture()
     if not O.build_ref():
         sys.exit("reference sources not found; cannot regenerate goldens")
+    write_vtk_fixtures()
     for name, case in cases.FULL_CASES.items():
         out = run_reference(case)
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
