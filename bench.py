@@ -65,6 +65,8 @@ def parse():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batch-meshes", type=int, default=256)
     ap.add_argument("--no-newton", action="store_true")
+    ap.add_argument("--no-solver", action="store_true",
+                    help="skip the device LDL^T leg (K(2) of the 20x20x80 bar)")
     ap.add_argument("--model", choices=["3d_damper", "a2000"],
                     help="run one of the reference's BENCH models instead (minutes)")
     ap.add_argument("--model-backend", default="fp64", choices=["fp64", "mixed", "port"])
@@ -488,6 +490,11 @@ def run_ours(args):
         from nla3d_gb300 import learned
         newton = learned.benchmark()
 
+    ldlt_leg = None
+    if not args.no_solver and rank == 0:
+        # the consumer of the assembled K(2): its device LDL^T on the 139k-equation bar
+        ldlt_leg = solver_bench(20)
+
     if rank != 0:
         return
     fp64_peak = probe_fma_peak(True)
@@ -541,6 +548,7 @@ def run_ours(args):
         "mixed": mixed,
         "batched": batched,
         "newton": newton,
+        "ldlt": ldlt_leg,
         "setup_s": setup_s,
         "element_status": {"flagged": int(count)},
     }
@@ -624,20 +632,18 @@ def run_cdb_model(args):
                  f"{len(fixes)} fixed DoFs"}), flush=True)
 
 
-def run_solver_bench(args):
+def solver_bench(nx, precisions=("fp32", "fp64")):
     """The EquationSolver consumer of the assembled K(2) on the device: the
     nx x nx x 4nx bar of the Newton study (rigid-body MPC end, Neo-Hookean
     G = 1, K = 1000) assembled on the GPU at its initial state, a geometric
     nested-dissection order (MPC equations last), the symbolic analysis on
     the host, then the timed factorisation (CUDA events around
-    nla3d_ldlt_factor) and one refined solve.  Prints one JSON line per
-    front precision."""
+    nla3d_ldlt_factor) and one refined solve.  One dict per front precision."""
     import math
     import torch
     from nla3d_gb300 import learned as L, ldlt
     from nla3d_gb300.newton import NewtonSolver, csr_full, nested_dissection
     from nla3d_gb300.storage import FEStorage
-    nx = args.solver_bench
     pb = L.bar_problem(nx, 4 * nx, 0.5, 1000.0, 2.0, math.pi / 2)
     t0 = time.perf_counter()
     s = FEStorage(pb.mesh).initSolutionData()
@@ -651,7 +657,8 @@ def run_solver_bench(args):
     perm = ldlt.saddle_order(io, co, nested_dissection(K, ns._row_points()), s.n_unk)
     t_order = time.perf_counter() - t0
     rhs = np.random.default_rng(0).standard_normal(n2)
-    for prec in args.solver_precisions.split(","):
+    out = []
+    for prec in precisions:
         t1 = time.perf_counter()
         solver = ldlt.DeviceLDLT.for_storage(s, perm, prec)
         t_create = time.perf_counter() - t1
@@ -670,7 +677,7 @@ def run_solver_bench(args):
         x = solver.solve_host(s, rhs, max_refine=20, tol=1e-10)
         t_solve = time.perf_counter() - t2
         fac = times[-1]
-        print(json.dumps({
+        out.append({
             "metric": "K(2) LDL^T factorisation on the device", "precision": prec,
             "value": fac, "unit": "s", "higher_is_better": False,
             "workload": f"rigid-body bar {nx}x{nx}x{4 * nx}, n={n2}, nnz(upper)={co.size}",
@@ -680,10 +687,17 @@ def run_solver_bench(args):
             "max_front": info["max_front"], "perturbed_pivots": info["perturbed"],
             "factor_s_first": times[0], "solve_s": t_solve, "refine_steps": solver.last_steps,
             "rel_residual": solver.last_residual, "order_s": t_order, "symbolic_s": t_create,
-            "x_norm": float(np.linalg.norm(x))}), flush=True)
+            "x_norm": float(np.linalg.norm(x))})
         solver.close()
         del solver
         torch.cuda.empty_cache()
+    s.close()
+    return out
+
+
+def run_solver_bench(args):
+    for rec in solver_bench(args.solver_bench, tuple(args.solver_precisions.split(","))):
+        print(json.dumps(rec), flush=True)
 
 
 def run_newton_bar(args):

@@ -415,7 +415,9 @@ int nla3d_ldlt_create(int64_t n, const uint32_t* iofeir, const uint32_t* columns
  * (nla3d_device_K block 2).  NLA3D_ERR_ELEMENT on a non-finite pivot. */
 int nla3d_ldlt_factor(nla3d_ldlt* h, const double* values);
 /* EquationSolver::substituteEquations: x = K(2)^-1 b on device vectors, then
- * at most max_refine steps x += K^-1 (b - K x) until ||b - K x|| <= tol ||b||
+ * refinement until ||b - K x|| <= tol ||b|| with at most max_refine further
+ * applications of the factor: steps x += K^-1 (b - K x) while each cuts the
+ * residual tenfold, then restarted GMRES(30) preconditioned by the factor
  * (values: the same K as factored, or a nearby one).  NLA3D_ERR_RANGE when
  * tol is not reached; steps and rel_residual may be NULL. */
 int nla3d_ldlt_solve(nla3d_ldlt* h, const double* values, const double* b, double* x,

@@ -117,6 +117,13 @@ __global__ void extend_add_kernel(const int32_t* __restrict__ children, int n, L
   }
 }
 
+// the guarded pivot without counting it
+template <typename T>
+__device__ __forceinline__ T guard_value(T dv, double tau) {
+  if (!(fabs((double)dv) >= tau) && dv == dv) return dv < T(0) ? T(-tau) : T(tau);
+  return dv;
+}
+
 template <typename T>
 __device__ __forceinline__ T guard_pivot(T dv, double tau, int* perturbed) {
   if (!(fabs((double)dv) >= tau)) {   // also catches NaN
@@ -140,7 +147,6 @@ __global__ void __launch_bounds__(kThreads)
                         const double* __restrict__ tau_p, double pivot_rel, int* perturbed) {
   extern __shared__ unsigned char smem_raw[];
   T* S = reinterpret_cast<T*>(smem_raw);
-  __shared__ T sd;
   const int s = list[blockIdx.x];
   const int m = (int)(d.row_ptr[s + 1] - d.row_ptr[s]);
   const int k = d.sn_first[s + 1] - d.sn_first[s];
@@ -152,13 +158,9 @@ __global__ void __launch_bounds__(kThreads)
   const double tau = pivot_rel * tau_p[0];
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   for (int p = 0; p < k; p++) {
-    if (threadIdx.x == 0) {
-      const T dv = guard_pivot(S[p + p * ld], tau, perturbed);
-      S[p + p * ld] = dv;
-      sd = dv;
-    }
-    __syncthreads();
-    const T dv = sd;
+    // every thread guards the pivot itself (thread 0 counts)
+    const T raw = S[p + p * ld];
+    const T dv = threadIdx.x == 0 ? guard_pivot(raw, tau, perturbed) : guard_value(raw, tau);
     T* colp = S + p * ld;
     // trailing update with w = column p (unscaled): A_ij -= w_i w_j / d
     for (int j = p + 1 + ty; j < m; j += 8) {
@@ -167,6 +169,7 @@ __global__ void __launch_bounds__(kThreads)
       for (int i = j + tx; i < m; i += 32) col[i] -= colp[i] * lj;
     }
     __syncthreads();
+    if (threadIdx.x == 0) colp[p] = dv;
     for (int i = p + 1 + threadIdx.x; i < m; i += blockDim.x) colp[i] = colp[i] / dv;
     __syncthreads();
   }
@@ -190,8 +193,9 @@ __global__ void __launch_bounds__(kThreads)
     batched_diag_kernel(BigBatch b, LdltDev d, T* __restrict__ front, int64_t p0,
                         T* __restrict__ Linv, const double* __restrict__ tau_p, double pivot_rel,
                         int* perturbed) {
-  __shared__ T B[kPanel][kPanel + 1];   // B[col][row]
-  __shared__ T sd;
+  extern __shared__ unsigned char diag_smem_raw[];
+  T(*B)[kPanel + 1] = reinterpret_cast<T(*)[kPanel + 1]>(diag_smem_raw);   // B[col][row]
+  unsigned char* diag_smem = diag_smem_raw + sizeof(T) * kPanel * (kPanel + 1);
   const int s = b.list[blockIdx.x];
   const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
   const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
@@ -203,35 +207,40 @@ __global__ void __launch_bounds__(kThreads)
     if (tc < pb) B[tc][r] = r >= tc ? F[(p0 + r) + (p0 + tc) * m] : T(0);
   __syncthreads();
   const double tau = pivot_rel * tau_p[0];
+  // one barrier per pivot: every thread guards the pivot itself (only thread
+  // 0 counts), column p is scaled by its own threads while the others update
   for (int p = 0; p < pb; p++) {
-    if (threadIdx.x == 0) {
-      const T dv = guard_pivot(B[p][p], tau, perturbed);
-      B[p][p] = dv;
-      sd = dv;
-    }
-    __syncthreads();
-    const T dv = sd;
+    const T raw = B[p][p];
+    const T dv = threadIdx.x == 0 ? guard_pivot(raw, tau, perturbed) : guard_value(raw, tau);
     if (tc > p && tc < pb) {
       const T lc = B[p][tc] / dv;
       for (int r = tc + tr; r < pb; r += kThreads / kPanel) B[tc][r] -= B[p][r] * lc;
     }
     __syncthreads();
+    if (threadIdx.x == p) B[p][p] = dv;
     if (threadIdx.x > p && threadIdx.x < pb) B[p][threadIdx.x] = B[p][threadIdx.x] / dv;
     __syncthreads();
   }
   for (int r = tr; r < pb; r += kThreads / kPanel)
     if (tc < pb && r >= tc) F[(p0 + r) + (p0 + tc) * m] = B[tc][r];
-  // inverse of the unit lower L11, column c by thread c
-  T* Li = Linv + b.li_off[blockIdx.x] + (uint64_t)(p0 / kPanel) * kPanel * kPanel;
+  // inverse of the unit lower L11 in shared memory (X[col][row]), column c by
+  // thread c, then stored for step 2 and the solves
+  T(*X)[kPanel + 1] = reinterpret_cast<T(*)[kPanel + 1]>(diag_smem);
   if (threadIdx.x < pb) {
     const int c = threadIdx.x;
-    for (int r = 0; r < c; r++) Li[r + c * kPanel] = T(0);
-    Li[c + c * kPanel] = T(1);
+    for (int r = 0; r < c; r++) X[c][r] = T(0);
+    X[c][c] = T(1);
     for (int r = c + 1; r < pb; r++) {
       T acc = -B[c][r];
-      for (int q = c + 1; q < r; q++) acc -= B[q][r] * Li[q + c * kPanel];
-      Li[r + c * kPanel] = acc;
+      for (int q = c + 1; q < r; q++) acc -= B[q][r] * X[c][q];
+      X[c][r] = acc;
     }
+  }
+  __syncthreads();
+  T* Li = Linv + b.li_off[blockIdx.x] + (uint64_t)(p0 / kPanel) * kPanel * kPanel;
+  for (int t = threadIdx.x; t < pb * kPanel; t += blockDim.x) {
+    const int r = t % kPanel, c = t / kPanel;
+    if (r < pb) Li[r + c * kPanel] = X[c][r];
   }
 }
 
@@ -658,6 +667,55 @@ __global__ void residual_kernel(int64_t n, const int64_t* __restrict__ ptr,
   }
 }
 
+// ---- vector kernels of the GMRES refinement (fixed-order reductions) ----
+constexpr int kDotBlocks = 1024;
+
+__global__ void dot_kernel(int64_t n, const double* __restrict__ a, const double* __restrict__ b,
+                           double* __restrict__ part) {
+  __shared__ double red[kThreads];
+  double acc = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    acc += a[i] * b[i];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+// y += alpha x
+__global__ void axpy_kernel(int64_t n, double alpha, const double* __restrict__ x,
+                            double* __restrict__ y) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    y[i] += alpha * x[i];
+}
+
+// y = alpha x
+__global__ void scale_kernel(int64_t n, double alpha, const double* __restrict__ x,
+                             double* __restrict__ y) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = alpha * x[i];
+}
+
+// y = A x, A by both-triangle rows, a warp per row
+__global__ void spmv_kernel(int64_t n, const int64_t* __restrict__ ptr,
+                            const int32_t* __restrict__ col, const uint32_t* __restrict__ slot,
+                            const double* __restrict__ A, const double* __restrict__ x,
+                            double* __restrict__ y) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t row = blockIdx.x * (int64_t)(blockDim.x / 32) + warp;
+  if (row >= n) return;
+  double acc = 0.0;
+  for (int64_t q = ptr[row] + lane; q < ptr[row + 1]; q += 32) acc += A[slot[q]] * x[col[q]];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if (lane == 0) y[row] = acc;
+}
+
 }  // namespace
 
 struct nla3d_ldlt {
@@ -674,6 +732,8 @@ struct nla3d_ldlt {
   double* d_r = nullptr;
   double* d_dx = nullptr;
   double* d_part = nullptr;
+  double* d_V = nullptr;        // GMRES basis, (kRestart + 1) x n, allocated on first use
+  double* d_dot = nullptr;
   double* d_maxabs = nullptr;
   double* d_maxpart = nullptr;
   int* d_perturbed = nullptr;
@@ -773,8 +833,8 @@ cudaError_t enqueue_factor(nla3d_ldlt* h, const double* values) {
       T* Li = static_cast<T*>(h->d_Linv);
       const unsigned nf = (unsigned)L.large_cnt;
       for (int64_t p0 = 0; p0 < L.large_max_k; p0 += kPanel) {
-        batched_diag_kernel<T><<<nf, kThreads, 0, st>>>(bb, h->dev, front, p0, Li, h->d_maxabs,
-                                                        h->pivot_rel, h->d_perturbed);
+        batched_diag_kernel<T><<<nf, kThreads, 2 * sizeof(T) * kPanel * (kPanel + 1), st>>>(
+            bb, h->dev, front, p0, Li, h->d_maxabs, h->pivot_rel, h->d_perturbed);
         const int64_t rest = L.large_max_m - p0 - 1;   // rows past the smallest panel
         if (rest <= 0) continue;
         const unsigned tiles = (unsigned)((rest + kTile - 1) / kTile);
@@ -992,12 +1052,18 @@ int nla3d_ldlt_create(int64_t n, const uint32_t* iofeir, const uint32_t* columns
   if (precision) {
     LCK(dalloc(h, reinterpret_cast<float**>(&h->d_W), (size_t)max_w));
     LCK(dalloc(h, reinterpret_cast<float**>(&h->d_Linv), nlinv));
+    LCK(cudaFuncSetAttribute(batched_diag_kernel<float>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(2 * sizeof(float) * kPanel * (kPanel + 1))));
     LCK(cudaFuncSetAttribute(factor_small_kernel<float>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)(sizeof(float) * kSmallFront * (kSmallFront + 1))));
   } else {
     LCK(dalloc(h, reinterpret_cast<double**>(&h->d_W), (size_t)max_w));
     LCK(dalloc(h, reinterpret_cast<double**>(&h->d_Linv), nlinv));
+    LCK(cudaFuncSetAttribute(batched_diag_kernel<double>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(2 * sizeof(double) * kPanel * (kPanel + 1))));
     LCK(cudaFuncSetAttribute(factor_small_kernel<double>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)(sizeof(double) * kSmallFront * (kSmallFront + 1))));
@@ -1009,6 +1075,7 @@ int nla3d_ldlt_create(int64_t n, const uint32_t* iofeir, const uint32_t* columns
   LCK(dalloc(h, &h->d_r, S.n));
   LCK(dalloc(h, &h->d_dx, S.n));
   LCK(dalloc(h, &h->d_part, 2 * ((S.n + 7) / 8 + 1)));
+  LCK(dalloc(h, &h->d_dot, kDotBlocks));
   LCK(dalloc(h, &h->d_maxabs, 1));
   LCK(dalloc(h, &h->d_maxpart, kMaxBlocks));
   LCK(dalloc(h, &h->d_perturbed, 2));
@@ -1074,35 +1141,160 @@ int nla3d_ldlt_factor(nla3d_ldlt* h, const double* values) {
   return NLA3D_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+constexpr int kRestart = 30;
+
+unsigned vec_blocks(int64_t n) {
+  return (unsigned)std::min<int64_t>((n + kThreads - 1) / kThreads, 152 * 8);
+}
+
+cudaError_t enqueue_solve_any(nla3d_ldlt* h, const double* rhs, double* out, int acc) {
+  return h->prec ? enqueue_solve<float>(h, rhs, out, acc) : enqueue_solve<double>(h, rhs, out, acc);
+}
+
+// <a, b> with a fixed reduction order (per-block partial sums, summed on the host)
+cudaError_t dot(nla3d_ldlt* h, const double* a, const double* b, double* out) {
+  double part[kDotBlocks];
+  dot_kernel<<<kDotBlocks, kThreads, 0, h->stream>>>(h->S.n, a, b, h->d_dot);
+  cudaError_t e = cudaMemcpyAsync(part, h->d_dot, sizeof(part), cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  double acc = 0.0;
+  for (int q = 0; q < kDotBlocks; q++) acc += part[q];
+  *out = acc;
+  return e;
+}
+
+// ||b - A x|| and ||b|| (the residual kernel leaves b - A x in d_r)
+cudaError_t residual_norms(nla3d_ldlt* h, const double* values, const double* x, const double* b,
+                           double* rnorm, double* bnorm) {
+  const int64_t nblk = (h->S.n + 7) / 8;
+  std::vector<double> part(2 * nblk);
+  cudaError_t e = enqueue_residual(h, values, x, b);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(part.data(), h->d_part, sizeof(double) * 2 * nblk, cudaMemcpyDeviceToHost,
+                        h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  double rr = 0.0, bb = 0.0;
+  for (int64_t q = 0; q < nblk; q++) {
+    rr += part[2 * q];
+    bb += part[2 * q + 1];
+  }
+  *rnorm = std::sqrt(rr);
+  *bnorm = std::sqrt(bb);
+  return e;
+}
+
+// Right-preconditioned restarted GMRES with the factor as the preconditioner
+// (GMRES-based iterative refinement), modified Gram-Schmidt, Givens rotations;
+// x is improved in place until ||b - A x|| <= tol ||b|| or `budget`
+// preconditioner applications are spent.
+cudaError_t gmres_refine(nla3d_ldlt* h, const double* values, const double* b, double* x,
+                         double tol, int budget, int* apps, double* rel) {
+  const LdltSymbolic& S = h->S;
+  const int64_t n = S.n;
+  cudaStream_t st = h->stream;
+  cudaError_t e = cudaSuccess;
+  if (!h->d_V) {
+    e = dalloc(h, &h->d_V, (size_t)(kRestart + 1) * n);
+    if (e != cudaSuccess) return e;
+  }
+  const unsigned vb = vec_blocks(n);
+  const unsigned mb = (unsigned)((n + kThreads / 32 - 1) / (kThreads / 32));
+  double rnorm = 0.0, bnorm = 0.0;
+  while (true) {
+    e = residual_norms(h, values, x, b, &rnorm, &bnorm);
+    if (e != cudaSuccess) return e;
+    const double scale = bnorm > 0.0 ? bnorm : 1.0;
+    *rel = rnorm / scale;
+    if (!(*rel > tol) || *apps >= budget) return cudaSuccess;
+    double H[kRestart + 1][kRestart] = {};
+    double cs[kRestart] = {}, sn[kRestart] = {}, g[kRestart + 1] = {};
+    g[0] = rnorm;
+    scale_kernel<<<vb, kThreads, 0, st>>>(n, 1.0 / rnorm, h->d_r, h->d_V);
+    int j = 0;
+    for (; j < kRestart && *apps < budget; j++) {
+      double* vj = h->d_V + (size_t)j * n;
+      double* w = h->d_V + (size_t)(j + 1) * n;
+      e = enqueue_solve_any(h, vj, h->d_dx, 0);   // z = M^-1 v_j
+      (*apps)++;
+      if (e != cudaSuccess) return e;
+      spmv_kernel<<<mb, kThreads, 0, st>>>(n, h->d_fptr, h->d_fcol, h->d_fslot, values, h->d_dx, w);
+      for (int i = 0; i <= j; i++) {
+        double hij = 0.0;
+        e = dot(h, w, h->d_V + (size_t)i * n, &hij);
+        if (e != cudaSuccess) return e;
+        H[i][j] = hij;
+        axpy_kernel<<<vb, kThreads, 0, st>>>(n, -hij, h->d_V + (size_t)i * n, w);
+      }
+      double ww = 0.0;
+      e = dot(h, w, w, &ww);
+      if (e != cudaSuccess) return e;
+      const double hn = std::sqrt(ww);
+      H[j + 1][j] = hn;
+      if (hn > 0.0) scale_kernel<<<vb, kThreads, 0, st>>>(n, 1.0 / hn, w, w);
+      for (int i = 0; i < j; i++) {
+        const double t = cs[i] * H[i][j] + sn[i] * H[i + 1][j];
+        H[i + 1][j] = -sn[i] * H[i][j] + cs[i] * H[i + 1][j];
+        H[i][j] = t;
+      }
+      const double a = H[j][j], c = H[j + 1][j];
+      const double rho = std::sqrt(a * a + c * c);
+      cs[j] = rho > 0.0 ? a / rho : 1.0;
+      sn[j] = rho > 0.0 ? c / rho : 0.0;
+      H[j][j] = rho;
+      H[j + 1][j] = 0.0;
+      g[j + 1] = -sn[j] * g[j];
+      g[j] = cs[j] * g[j];
+      if (std::fabs(g[j + 1]) <= 0.5 * tol * scale || hn == 0.0) {
+        j++;
+        break;
+      }
+    }
+    // y = H^-1 g, t = V y, x += M^-1 t
+    double y[kRestart] = {};
+    for (int i = j - 1; i >= 0; i--) {
+      double acc = g[i];
+      for (int q = i + 1; q < j; q++) acc -= H[i][q] * y[q];
+      y[i] = H[i][i] != 0.0 ? acc / H[i][i] : 0.0;
+    }
+    e = cudaMemsetAsync(h->d_r, 0, sizeof(double) * n, st);
+    if (e != cudaSuccess) return e;
+    for (int i = 0; i < j; i++)
+      axpy_kernel<<<vb, kThreads, 0, st>>>(n, y[i], h->d_V + (size_t)i * n, h->d_r);
+    e = enqueue_solve_any(h, h->d_r, x, 1);
+    (*apps)++;
+    if (e != cudaSuccess) return e;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
 int nla3d_ldlt_solve(nla3d_ldlt* h, const double* values, const double* b, double* x,
                      int max_refine, double tol, int* steps, double* rel_residual) {
   if (!h || !values || !b || !x || max_refine < 0)
     return fail(h, NLA3D_ERR_ARG, "ldlt_solve: bad argument");
   if (!h->factored) return fail(h, NLA3D_ERR_ARG, "ldlt_solve: factor first");
-  const LdltSymbolic& S = h->S;
-  auto solve = [&](const double* rhs, double* out, int acc) {
-    return h->prec ? enqueue_solve<float>(h, rhs, out, acc) : enqueue_solve<double>(h, rhs, out, acc);
-  };
-  cudaError_t e = solve(b, x, 0);
-  const int64_t nblk = (S.n + 7) / 8;
-  std::vector<double> part(2 * nblk);
-  double rel = 0.0;
+  cudaError_t e = enqueue_solve_any(h, b, x, 0);
+  double rel = 0.0, prev = 0.0, rnorm = 0.0, bnorm = 0.0;
   int it = 0;
+  // plain refinement while it converges fast; GMRES with the same factor after
   for (;;) {
-    if (e == cudaSuccess) e = enqueue_residual(h, values, x, b);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(part.data(), h->d_part, sizeof(double) * 2 * nblk, cudaMemcpyDeviceToHost,
-                          h->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e == cudaSuccess) e = residual_norms(h, values, x, b, &rnorm, &bnorm);
     if (e != cudaSuccess) return cuda_fail(h, e, "ldlt_solve");
-    double rr = 0.0, bb = 0.0;
-    for (int64_t q = 0; q < nblk; q++) {
-      rr += part[2 * q];
-      bb += part[2 * q + 1];
-    }
-    rel = bb > 0.0 ? std::sqrt(rr / bb) : std::sqrt(rr);
+    rel = rnorm / (bnorm > 0.0 ? bnorm : 1.0);
     if (!(rel > tol) || it >= max_refine) break;
-    e = solve(h->d_r, x, 1);   // x += A^-1 r with the same factors
+    if (it > 0 && !(rel < 0.1 * prev)) {
+      e = gmres_refine(h, values, b, x, tol, max_refine, &it, &rel);
+      if (e != cudaSuccess) return cuda_fail(h, e, "ldlt_solve (GMRES)");
+      break;
+    }
+    prev = rel;
+    e = enqueue_solve_any(h, h->d_r, x, 1);   // x += A^-1 r with the same factors
     it++;
   }
   if (steps) *steps = it;

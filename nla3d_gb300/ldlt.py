@@ -145,7 +145,7 @@ class DeviceLDLT:
         """factorizeEquations on the storage's device K(2)."""
         self.factor_device(storage.device_K(2)[0])
 
-    def solve_device(self, values_ptr, b_ptr, x_ptr, max_refine=10, tol=1e-13):
+    def solve_device(self, values_ptr, b_ptr, x_ptr, max_refine=50, tol=1e-13):
         steps = ctypes.c_int()
         rel = ctypes.c_double()
         self._check(self.lib.nla3d_ldlt_solve(self.h, ctypes.c_void_p(values_ptr),
@@ -155,7 +155,7 @@ class DeviceLDLT:
         self.last_steps, self.last_residual = steps.value, rel.value
         return steps.value, rel.value
 
-    def solve_host(self, storage, rhs, max_refine=10, tol=1e-13):
+    def solve_host(self, storage, rhs, max_refine=50, tol=1e-13):
         """x = K(2)^-1 rhs for a host vector (PyTorch device buffers as plumbing)."""
         import torch
         b = torch.from_numpy(np.ascontiguousarray(rhs, dtype=np.float64)).cuda()

@@ -197,7 +197,7 @@ class NewtonSolver:
                                                 "fp32" if self.solver == "gpu-fp32" else "fp64")
         self._ldlt.factor(self.b)
         self.factorizations += 1
-        x = self._ldlt.solve_host(self.b, rhs, max_refine=10, tol=1e-10)
+        x = self._ldlt.solve_host(self.b, rhs, max_refine=100, tol=1e-10)
         self.krylov_iterations += self._ldlt.last_steps
         return x
 

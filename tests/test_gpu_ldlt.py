@@ -93,3 +93,14 @@ def test_newton_rigid_body_with_device_solver():
         curves[solver] = np.concatenate([r for r in n.reactions])
     for k in ("gpu", "gpu-fp32"):
         assert np.abs(curves[k] - curves["direct"]).max() <= 1e-8 * np.abs(curves["direct"]).max()
+
+
+def test_fp32_fronts_on_a_nearly_incompressible_block():
+    """K/G = 1e6 (Neo-Hookean), twisted: the FP32 factor alone is far from
+    1e-12; the refinement (steps, then GMRES preconditioned by the factor)
+    reaches it and agrees with SciPy."""
+    mesh = mg.solid81_block(6, 6, 6, 1.0 / 6, mg.MAT_NEO_HOOKEAN, (1.0, 1.0e6), clamp_z0=True)
+    u, p = mg.twist_state(mesh, angle_deg=30.0, stretch=1.2, noise_frac=0.01, seed=4)
+    s = _storage(mesh, u, p, None, True)
+    solver, x = _check(s, "fp32", 1e-12)
+    assert solver.last_steps >= 2
