@@ -79,6 +79,8 @@ def parse():
                          "256k-element bar): plain vs learned start, FP64 vs mixed assembly, "
                          "K(2) factored on the device; prints one JSON line and exits")
     ap.add_argument("--newton-starts", default="plain,learned")
+    ap.add_argument("--newton-assembly", default="fp64,mixed",
+                    help="assembly precisions of --newton-bar (the mixed run uses the plain start)")
     ap.add_argument("--model-solver", default="nd", choices=["nd", "gpu", "gpu-fp32", "direct"],
                     help="K(2) solve of --model runs: host SuperLU after nested dissection, "
                          "or the device LDL^T with FP64 / FP32 fronts")
@@ -717,7 +719,7 @@ def run_newton_bar(args):
     starts = tuple(args.newton_starts.split(","))
     mlp = None
     train = {}
-    if "learned" in starts:
+    if "learned" in starts and "fp64" in args.newton_assembly.split(","):
         Xb, Yb, _ = L.generate(L.sample_bar_problems(12, nx=3, nz=12, seed=5, n_loadsteps=50))
         mlp = L.MLP(seed=1)
         hist = mlp.fit(Xb, Yb, epochs=300, batch=128, lr=2e-3)
@@ -726,10 +728,13 @@ def run_newton_bar(args):
         log(f"trained: {train}")
     cfg = L.bar_problem(nx, 4 * nx, 0.5, 1000.0, 2.0, math.pi / 2, 50)
     res = {}
-    res["fp64_assembly"] = L.evaluate([cfg], mlp, precision="fp64", linear_solver="gpu-fp32",
-                                      starts=starts, log=log)
-    res["mixed_assembly"] = L.evaluate([cfg], mlp, precision="mixed", linear_solver="gpu-fp32",
-                                       starts=("plain",), log=log)
+    precisions = args.newton_assembly.split(",")
+    if "fp64" in precisions:
+        res["fp64_assembly"] = L.evaluate([cfg], mlp, precision="fp64", linear_solver="gpu-fp32",
+                                          starts=starts, log=log)
+    if "mixed" in precisions:
+        res["mixed_assembly"] = L.evaluate([cfg], mlp, precision="mixed",
+                                           linear_solver="gpu-fp32", starts=("plain",), log=log)
     print(json.dumps({
         "metric": "Newton iterations per load step (residual 1e-8)", "unit": "iterations",
         "higher_is_better": False,

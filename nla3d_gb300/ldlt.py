@@ -145,21 +145,25 @@ class DeviceLDLT:
         """factorizeEquations on the storage's device K(2)."""
         self.factor_device(storage.device_K(2)[0])
 
-    def solve_device(self, values_ptr, b_ptr, x_ptr, max_refine=50, tol=1e-13):
+    def solve_device(self, values_ptr, b_ptr, x_ptr, max_refine=50, tol=1e-13, strict=True):
+        """strict=False returns the refined x and its residual even when tol
+        was not reached (NLA3D_ERR_RANGE); other errors always raise."""
         steps = ctypes.c_int()
         rel = ctypes.c_double()
-        self._check(self.lib.nla3d_ldlt_solve(self.h, ctypes.c_void_p(values_ptr),
-                                              ctypes.c_void_p(b_ptr), ctypes.c_void_p(x_ptr),
-                                              int(max_refine), float(tol), ctypes.byref(steps),
-                                              ctypes.byref(rel)))
+        rc = self.lib.nla3d_ldlt_solve(self.h, ctypes.c_void_p(values_ptr), ctypes.c_void_p(b_ptr),
+                                       ctypes.c_void_p(x_ptr), int(max_refine), float(tol),
+                                       ctypes.byref(steps), ctypes.byref(rel))
         self.last_steps, self.last_residual = steps.value, rel.value
+        if rc and (strict or rc != 5):
+            self._check(rc)
         return steps.value, rel.value
 
-    def solve_host(self, storage, rhs, max_refine=50, tol=1e-13):
+    def solve_host(self, storage, rhs, max_refine=50, tol=1e-13, strict=True):
         """x = K(2)^-1 rhs for a host vector (PyTorch device buffers as plumbing)."""
         import torch
         b = torch.from_numpy(np.ascontiguousarray(rhs, dtype=np.float64)).cuda()
         x = torch.empty_like(b)
         torch.cuda.synchronize()
-        self.solve_device(storage.device_K(2)[0], b.data_ptr(), x.data_ptr(), max_refine, tol)
+        self.solve_device(storage.device_K(2)[0], b.data_ptr(), x.data_ptr(), max_refine, tol,
+                          strict)
         return x.cpu().numpy()

@@ -417,7 +417,8 @@ def evaluate(problems, mlp, kind="gpu", precision="fp64", linear_solver="direct"
                 out["learned_used"] += [r.predicted for r in s.records]
             if log:
                 log(f"{pb.label} {start}: {np.mean(out[start]):.3f} it/step, "
-                    f"{wall[start]:.1f} s, {s.factorizations} factorisations")
+                    f"{wall[start]:.1f} s, {s.factorizations} factorisations, "
+                    f"{s.inexact_solves} inexact solves, {s.fp64_refactorizations} FP64 refactors")
     res = {k: float(np.mean(v)) for k, v in out.items() if v}
     return res | {"steps": len(out[starts[0]]), "wall_s": wall}
 
