@@ -79,6 +79,11 @@ def parse():
                          "256k-element bar): plain vs learned start, FP64 vs mixed assembly, "
                          "K(2) factored on the device; prints one JSON line and exits")
     ap.add_argument("--newton-starts", default="plain,learned")
+    ap.add_argument("--learned-blocks", type=int, default=0, metavar="N",
+                    help="learned-start study on N^3 blocks (20: the configured size) with "
+                         "K(2) factored on the device; prints one JSON line and exits")
+    ap.add_argument("--learned-train", type=int, default=120)
+    ap.add_argument("--learned-eval", type=int, default=16)
     ap.add_argument("--newton-assembly", default="fp64,mixed",
                     help="assembly precisions of --newton-bar (the mixed run uses the plain start)")
     ap.add_argument("--model-solver", default="nd", choices=["nd", "gpu", "gpu-fp32", "direct"],
@@ -744,8 +749,44 @@ def run_newton_bar(args):
         "results": res, "training": train, "wall_s": time.perf_counter() - t0}), flush=True)
 
 
+def run_learned_blocks(args):
+    """The learned Newton start on n^3 blocks (Neo-Hookean, C10 ~ U(0.2, 1),
+    K ~ U(500, 5000), target stretch ~ U(1, 2), 20 load steps, residual
+    1e-8), K(2) factored on the device (FP32 fronts, FP64 refinement): the
+    MLP (4 x 256, BF16 weights, FP32 accumulation) is trained by the
+    library's kernels on the converged increments of `--learned-train`
+    solves and evaluated on `--learned-eval` held-out ones against the plain
+    and the secant-extrapolation starts."""
+    from nla3d_gb300 import learned as L
+    n = args.learned_blocks
+    log = lambda m: print(m, file=sys.stderr, flush=True)  # noqa: E731
+    t0 = time.perf_counter()
+    X, Y, its = L.generate(L.sample_block_problems(args.learned_train, n=n, seed=11),
+                           linear_solver="gpu-fp32")
+    t_gen = time.perf_counter() - t0
+    log(f"generated {X.shape[0]} samples from {args.learned_train} solves in {t_gen:.1f} s")
+    mlp = L.MLP(seed=0)
+    hist = mlp.fit(X, Y, epochs=300, batch=128, lr=2e-3)
+    t_fit = time.perf_counter() - t0 - t_gen
+    res = L.evaluate(L.sample_block_problems(args.learned_eval, n=n, seed=99), mlp,
+                     linear_solver="gpu-fp32", log=None)
+    print(json.dumps({
+        "metric": "Newton iterations per load step (residual 1e-8), learned vs plain start",
+        "unit": "iterations", "higher_is_better": False,
+        "workload": f"{n}^3 SOLID81 blocks (C10 ~ U(0.2,1), K ~ U(500,5000), stretch ~ U(1,2)), "
+                    "20 load steps",
+        "train_solves": args.learned_train, "train_samples": int(X.shape[0]),
+        "train_plain_iterations": float(np.mean([np.mean(i) for i in its])),
+        "final_loss": hist[-1][1], "eval_solves": args.learned_eval, "results": res,
+        "generate_s": t_gen, "fit_s": t_fit, "wall_s": time.perf_counter() - t0,
+        "linear_solver": "device LDL^T, FP32 fronts + FP64 refinement"}), flush=True)
+
+
 def main():
     args = parse()
+    if args.learned_blocks:
+        run_learned_blocks(args)
+        return
     if args.newton_bar:
         run_newton_bar(args)
         return

@@ -378,11 +378,11 @@ def basis_for(problem: Problem, backend):
     return CoarseBasis(problem.mesh, ne, ee, backend.n_con, backend.n_total)
 
 
-def generate(problems, kind="gpu", precision="fp64"):
+def generate(problems, kind="gpu", precision="fp64", linear_solver="direct"):
     X, Y, iters = [], [], []
     for pb in problems:
         be = make_backend(pb, kind, precision)
-        solver, hist = solve(pb, be)
+        solver, hist = solve(pb, be, linear_solver=linear_solver)
         x, y = samples_from_history(basis_for(pb, be), hist, pb.c10, pb.kbulk)
         X += x
         Y += y
