@@ -307,13 +307,18 @@ __global__ void __launch_bounds__(kThreads)
 
 // step 3: trailing lower triangle, F[i][j] -= sum_c L[i][c] W[j][c], i >= j >= q0;
 // BT x BT tiles (blockIdx.x, .y), front blockIdx.z, RT x RT outputs per thread
-// (64 / 4 for FP64, whose FMA pipe bounds it anyway; 128 / 8 for FP32)
+// (64 / 4 for FP64, whose FMA pipe bounds it anyway; 128 / 8 for FP32).  A
+// thread owns rows tx + 16u and columns ty + 16v: shared-memory reads are
+// conflict-free or broadcast and the stores run down the columns.  The next
+// 16-wide slice of the panel is loaded into registers while the current one
+// is multiplied.
 template <typename T, int BT, int RT>
 __global__ void __launch_bounds__(kThreads)
     batched_trailing_kernel(BigBatch b, LdltDev d, T* __restrict__ front, int64_t p0,
                             const T* __restrict__ Wbuf) {
   static_assert((BT / RT) * (BT / RT) == kThreads, "one output block per thread");
-  constexpr int TD = BT / RT;
+  static_assert(BT / RT == 16, "16 x 16 threads");
+  constexpr int LPT = 16 * BT / kThreads;   // slice elements each thread loads per operand
   const int ti = blockIdx.x, tj = blockIdx.y;
   if (tj > ti) return;
   const int s = b.list[blockIdx.z];
@@ -326,26 +331,39 @@ __global__ void __launch_bounds__(kThreads)
   if (i0 >= m) return;
   T* F = front + d.front_off[s];
   const T* W = Wbuf + b.w_off[blockIdx.z];
-  __shared__ T As[16][BT + 1];
-  __shared__ T Bs[16][BT + 1];
-  const int tx = threadIdx.x % TD, ty = threadIdx.x / TD;
+  __shared__ T As[16][BT];
+  __shared__ T Bs[16][BT];
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
   T acc[RT][RT] = {};
-  for (int c0 = 0; c0 < pb; c0 += 16) {
-    for (int t = threadIdx.x; t < 16 * BT; t += blockDim.x) {
+  T ra[LPT], rb[LPT];
+  auto load = [&](int c0) {
+#pragma unroll
+    for (int q = 0; q < LPT; q++) {
+      const int t = threadIdx.x + q * kThreads;
       const int cc = t / BT, rr = t % BT;
       const int c = c0 + cc;
       const int64_t i = i0 + rr, j = j0 + rr;
-      As[cc][rr] = (c < pb && i < m) ? F[i + (p0 + c) * m] : T(0);
-      Bs[cc][rr] = (c < pb && j < m) ? W[(j - q0) + c * m] : T(0);
+      ra[q] = (c < pb && i < m) ? F[i + (p0 + c) * m] : T(0);
+      rb[q] = (c < pb && j < m) ? W[(j - q0) + c * m] : T(0);
+    }
+  };
+  load(0);
+  for (int c0 = 0; c0 < pb; c0 += 16) {
+#pragma unroll
+    for (int q = 0; q < LPT; q++) {
+      const int t = threadIdx.x + q * kThreads;
+      As[t / BT][t % BT] = ra[q];
+      Bs[t / BT][t % BT] = rb[q];
     }
     __syncthreads();
+    if (c0 + 16 < pb) load(c0 + 16);
 #pragma unroll
     for (int cc = 0; cc < 16; cc++) {
       T a[RT], bb[RT];
 #pragma unroll
-      for (int u = 0; u < RT; u++) a[u] = As[cc][ty * RT + u];
+      for (int u = 0; u < RT; u++) a[u] = As[cc][tx + 16 * u];
 #pragma unroll
-      for (int v = 0; v < RT; v++) bb[v] = Bs[cc][tx * RT + v];
+      for (int v = 0; v < RT; v++) bb[v] = Bs[cc][ty + 16 * v];
 #pragma unroll
       for (int u = 0; u < RT; u++)
 #pragma unroll
@@ -354,13 +372,13 @@ __global__ void __launch_bounds__(kThreads)
     __syncthreads();
   }
 #pragma unroll
-  for (int u = 0; u < RT; u++) {
-    const int64_t i = i0 + ty * RT + u;
-    if (i >= m) continue;
+  for (int v = 0; v < RT; v++) {
+    const int64_t j = j0 + ty + 16 * v;
+    if (j >= m) continue;
 #pragma unroll
-    for (int v = 0; v < RT; v++) {
-      const int64_t j = j0 + tx * RT + v;
-      if (j < m && j <= i) F[i + j * m] -= acc[u][v];
+    for (int u = 0; u < RT; u++) {
+      const int64_t i = i0 + tx + 16 * u;
+      if (i < m && j <= i) F[i + j * m] -= acc[u][v];
     }
   }
 }
