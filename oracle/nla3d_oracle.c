@@ -1177,7 +1177,10 @@ static double det4_lu(const double* M) {
   return det;
 }
 
-static int tetra0_buildK(orc_model* m, uint32_t e) {
+/* the element strain matrix B (6x12, makeB TETRA0.cpp:110-184), the elastic
+ * matrix C (packed MatSym<6>, makeC :186-199) and the volume (det[1 X] / 6) */
+static void tetra0_B_C(const orc_model* m, uint32_t e, double* B, double* Cm,
+                       double* vol_out) {
   const uint32_t* c = m->conn + (size_t)e * 4;
   const double* P[4];
   for (int a = 0; a < 4; a++) P[a] = m->xyz + (size_t)(c[a] - 1) * 3;
@@ -1189,12 +1192,9 @@ static int tetra0_buildK(orc_model* m, uint32_t e) {
     S[a * 4 + 3] = P[a][2];
   }
   const double vol = det4_lu(S) / 6.;
-  double Ke[78];
-  memset(Ke, 0, sizeof(Ke));
-  double B[6 * 12];
-  memset(B, 0, sizeof(B));
-  double Cm[21];
-  memset(Cm, 0, sizeof(Cm));
+  *vol_out = vol;
+  memset(B, 0, sizeof(double) * 72);
+  memset(Cm, 0, sizeof(double) * 21);
   /* makeC (TETRA0.cpp:186-199); MatSym<6>::comp index = 6*i - (i-1)*i/2 + (j-i) */
   const double E = m->eparams[EPAR * e], my = m->eparams[EPAR * e + 1];
   const double A = E / ((1. + my) * (1. - 2. * my));
@@ -1244,6 +1244,14 @@ static int tetra0_buildK(orc_model* m, uint32_t e) {
     B[60 + 3 * i] = d[i] * Af;
     B[62 + 3 * i] = b[i] * Af;
   }
+}
+
+static int tetra0_buildK(orc_model* m, uint32_t e) {
+  double Ke[78];
+  memset(Ke, 0, sizeof(Ke));
+  double B[6 * 12], Cm[21], vol;
+  tetra0_B_C(m, e, B, Cm, &vol);
+  const uint32_t* c = m->conn + (size_t)e * 4;
   k_matBTDBprod(6, 12, B, Cm, vol, Ke);
   /* Element::assembleK(Ke, {UX,UY,UZ}) (element.h:281-303) */
   const double* Kp = Ke;
@@ -1257,6 +1265,35 @@ static int tetra0_buildK(orc_model* m, uint32_t e) {
           Kp++;
         }
   return rc;
+}
+
+/* ElementTETRA0::update (TETRA0.cpp:79-108): strains = -B U (matBVprod with
+ * coefficient -1), stress = C strains (matBVprod of the MatSym C); out: six
+ * stress components per element in the element's order (xx, yy, zz, xy, yz,
+ * xz), from the model's current U. */
+int orc_tetra0_stress(orc_model* m, double* out) {
+  if (!m->setup_done || m->etype != ET_TETRA0) return fail(m, "tetra0_stress: a set-up TETRA0 model");
+  for (uint32_t e = 0; e < m->n_elems; e++) {
+    double B[72], Cm[21], vol, U[12], strain[6] = {0, 0, 0, 0, 0, 0}, C[36];
+    tetra0_B_C(m, e, B, Cm, &vol);
+    const uint32_t* c = m->conn + (size_t)e * 4;
+    for (int a = 0; a < 4; a++)
+      for (int d = 0; d < 3; d++) U[3 * a + d] = m->U[neq(m, c[a], d) - 1];
+    for (int i = 0; i < 6; i++)
+      for (int j = 0; j < 12; j++) strain[i] += B[i * 12 + j] * U[j] * -1.0;
+    /* MatSym<6>::toMat: both triangles from the packed upper storage */
+    for (int i = 0; i < 6; i++)
+      for (int j = 0; j < 6; j++) {
+        const int a = i < j ? i : j, b = i < j ? j : i;
+        C[i * 6 + j] = Cm[6 * a - (a - 1) * a / 2 + (b - a)];
+      }
+    double* st = out + (size_t)e * 6;
+    for (int i = 0; i < 6; i++) {
+      st[i] = 0.0;
+      for (int j = 0; j < 6; j++) st[i] += C[i * 6 + j] * strain[j] * 1.0;
+    }
+  }
+  return 0;
 }
 
 /* ----------------------------------------------------------------------- */

@@ -57,6 +57,9 @@ int orc_update(orc_model* m);
 int orc_assemble(orc_model* m);
 int orc_get_K(orc_model* m, int block, double* values);
 int orc_get_F(orc_model* m, double* F);
+/* TETRA0 stresses from the current U (ElementTETRA0::update, TETRA0.cpp:79-108):
+ * 6 per element (xx, yy, zz, xy, yz, xz). */
+int orc_tetra0_stress(orc_model* m, double* out);
 /* C and M of a transient model, block 1 / 12 / 2 on K's pattern. */
 int orc_get_C(orc_model* m, int block, double* values);
 int orc_get_M(orc_model* m, int block, double* values);

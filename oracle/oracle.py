@@ -104,6 +104,8 @@ def _load(kind: str):
         lib.ref_write_vtk.argtypes = [_P, ctypes.c_char_p, ctypes.c_int]
         lib.ref_write_vtk.restype = ctypes.c_int
     if kind == "port":
+        lib.orc_tetra0_stress.argtypes = [_P, _P]
+        lib.orc_tetra0_stress.restype = ctypes.c_int
         lib.orc_material_S.argtypes = [ctypes.c_int, _P, _P, ctypes.c_double, _P]
         lib.orc_material_D.argtypes = [ctypes.c_int, _P, _P, ctypes.c_double, _P, _P]
         lib.orc_hex_jacobian.argtypes = [_P, ctypes.c_int, _P, _P]
@@ -248,6 +250,12 @@ class OracleModel:
         v = np.zeros(self.n_total)
         self._check(self._f("get_F")(self.h, _ptr(v)))
         return v
+
+    def tetra0_stress(self):
+        """Port only: TETRA0 element stresses from the current U (TETRA0.cpp:79-108)."""
+        out = np.zeros((self.mesh.n_elems, 6))
+        self._check(self.lib.orc_tetra0_stress(self.h, _ptr(out)))
+        return out
 
     def write_vtk(self, prefix, step, U, R):
         """Compiled reference only: its VtkProcessor writes <prefix>0.vtk (and

@@ -154,3 +154,22 @@ def heat_model(transient=False):
     loads = [(int(n), int(d), float(v)) for n, d, v in zip(g["load_node"], g["load_dof"],
                                                             g["load_value"])]
     return mesh, loads, int(g["probe"][0]), g
+
+
+def tetra0_ansys_model():
+    """The reference's TETRA0_test model (test/TETRA0/tetra.cdb): 883 TETRA0,
+    E = 1e8, my = 0.3, the .cdb's D fixes and F loads; returns (mesh, fixes,
+    loads, fixture with the ANSYS displacements and stresses)."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "tetra0_ansys.npz"))
+    E = g["conn"].shape[0]
+    ep = np.zeros((E, 2))
+    ep[:, 0], ep[:, 1] = 1.0e8, 0.3
+    mesh = mg.Mesh(mg.ELEM_TETRA0, g["xyz"].astype(np.float64), g["conn"].astype(np.uint32),
+                   elem_params=ep, name="tetra0_ansys")
+    mesh.fix_nodes, mesh.fix_dofs = g["fix_node"], g["fix_dof"]
+    fixes = [(int(n), int(d), float(v)) for n, d, v in zip(g["fix_node"], g["fix_dof"],
+                                                            g["fix_value"])]
+    loads = [(int(n), int(d), float(v)) for n, d, v in zip(g["load_node"], g["load_dof"],
+                                                            g["load_value"])]
+    return mesh, fixes, loads, g

@@ -367,6 +367,38 @@ def write_vtk_fixtures():
         print("wrote vtk", name)
 
 
+def write_tetra0_fixture():
+    """The reference's TETRA0_test input (test/TETRA0): the TYPE 1 cells of
+    tetra.cdb as TETRA0 (nodes 0, 1, 2, 4 of the degenerate 8-node cell, as
+    TETRA0_test.cpp takes them), its D fixes and F loads, and the ANSYS
+    results the test checks: nodal displacements (disp.res, 1e-10) and
+    element stresses (stress.res, 1e-3)."""
+    base = "/root/reference/test/TETRA0"
+    md = read_cdb(f"{base}/tetra.cdb")
+    conn = np.array([[c[0], c[1], c[2], c[4]] for c, t in zip(md["cells"], md["type"]) if t == 1],
+                    dtype=np.uint32)
+
+    def table(path, cols):
+        rows = []
+        with open(path) as fh:
+            next(fh)
+            for row in fh:
+                if row.strip():
+                    rows.append([float(v) for v in row.split()[1:1 + cols]])
+        return np.array(rows)
+    np.savez_compressed(
+        os.path.join(HERE, "tetra0_ansys.npz"),
+        xyz=md["xyz"], conn=conn,
+        fix_node=np.array([f[0] for f in md["fixes"]], dtype=np.uint32),
+        fix_dof=np.array([f[1] for f in md["fixes"]], dtype=np.int32),
+        fix_value=np.array([f[2] for f in md["fixes"]], dtype=np.float64),
+        load_node=np.array([f[0] for f in md["loads"]], dtype=np.uint32),
+        load_dof=np.array([f[1] for f in md["loads"]], dtype=np.int32),
+        load_value=np.array([f[2] for f in md["loads"]], dtype=np.float64),
+        ansys_disp=table(f"{base}/disp.res", 3), ansys_stress=table(f"{base}/stress.res", 6))
+    print("wrote tetra0_ansys", conn.shape, len(md["fixes"]), "D", len(md["loads"]), "F")
+
+
 def write_rigid_body_fixture():
     base = "/root/reference/test/rigid_body_mpc"
     nodes, elems, comps, fixes, curve = read_rigid_body_case(
@@ -391,6 +423,7 @@ def main():
     write_damper_fixture()
     write_a2000_fixture()
     write_heat_fixture()
+    write_tetra0_fixture()
     if not O.build_ref():
         sys.exit("reference sources not found; cannot regenerate goldens")
     write_vtk_fixtures()
