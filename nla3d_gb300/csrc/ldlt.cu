@@ -42,7 +42,7 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kSmallFront = 128;   // fronts up to this many rows: one block each, in smem
 constexpr int kPanel = 64;         // panel width of the blocked path
-constexpr int kTile = 64;          // trailing-update tile
+constexpr int kTile = 64;          // panel-row tile of the blocked path
 
 struct LdltDev {
   const uint64_t* front_off;
@@ -778,7 +778,6 @@ struct nla3d_ldlt {
     std::vector<int64_t> ea_off, ea_cnt;  // children of the level's parents, by ordinal
   };
   std::vector<Level> levels;
-  const double* factored_values = nullptr;
   bool factored = false;
   int perturbed[2] = {0, 0};
   uint64_t front_entries = 0;
@@ -1154,7 +1153,6 @@ int nla3d_ldlt_factor(nla3d_ldlt* h, const double* values) {
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
   if (e != cudaSuccess) return cuda_fail(h, e, "ldlt_factor");
   h->factored = true;
-  h->factored_values = values;
   if (h->perturbed[1]) return fail(h, NLA3D_ERR_ELEMENT, "ldlt_factor: a non-finite pivot");
   return NLA3D_OK;
 }
