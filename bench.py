@@ -86,7 +86,8 @@ def parse():
     ap.add_argument("--learned-eval", type=int, default=16)
     ap.add_argument("--newton-assembly", default="fp64,mixed",
                     help="assembly precisions of --newton-bar (the mixed run uses the plain start)")
-    ap.add_argument("--model-solver", default="nd", choices=["nd", "gpu", "gpu-fp32", "direct"],
+    ap.add_argument("--model-solver", default="nd",
+                    choices=["nd", "gpu", "gpu-fp32", "gpu-tc", "direct"],
                     help="K(2) solve of --model runs: host SuperLU after nested dissection, "
                          "or the device LDL^T with FP64 / FP32 fronts")
     ap.add_argument("--e2e-chunks", type=int, default=8,

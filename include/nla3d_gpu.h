@@ -404,7 +404,9 @@ typedef struct nla3d_ldlt nla3d_ldlt;
 int nla3d_ldlt_analyze(int64_t n, const uint32_t* iofeir, const uint32_t* columns,
                        const int32_t* perm, double* stats, int32_t* perm_out, int32_t* sn_first_out,
                        int64_t* row_ptr_out, int32_t* rows_out);
-/* precision 0: FP64 fronts; 1: FP32 fronts (half the memory, FP64 refinement).
+/* precision 0: FP64 fronts; 1: FP32 fronts (half the memory, FP64 refinement);
+ * 2: FP32 fronts whose trailing updates run on the tensor cores (tcgen05,
+ * TF32 split in high and low parts: hi.hi + hi.lo + lo.hi, FP32 accumulation).
  * stream: the stream the values are produced on (NULL: a stream of its own);
  * a borrowed stream must outlive the handle.
  * On an error after the handle exists, *out is set: read nla3d_ldlt_last_error
@@ -426,6 +428,12 @@ int nla3d_ldlt_solve(nla3d_ldlt* h, const double* values, const double* b, doubl
  * perturbed pivots and non-finite pivots of the last factorisation. */
 int nla3d_ldlt_info(const nla3d_ldlt* h, double* out);
 const char* nla3d_ldlt_last_error(const nla3d_ldlt* h);
+/* Self-check of the tensor-core trailing update (precision 2): one front of m
+ * rows (65 .. 4096) after its first 64-column panel, updated from the same
+ * random data by the FMA kernel and by the tcgen05 kernel; out[0] = max
+ * |difference|, out[1] = max |update|.  NLA3D_ERR_RANGE if an MMA wait timed
+ * out.  Synchronises the device. */
+int nla3d_ldlt_tc_check(int m, double* out);
 int nla3d_ldlt_destroy(nla3d_ldlt* h);
 
 #ifdef __cplusplus

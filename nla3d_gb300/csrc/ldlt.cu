@@ -31,6 +31,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <type_traits>
 #include <string>
 #include <vector>
 
@@ -392,6 +393,179 @@ struct TrailingShape<float> {
   static constexpr int BT = 128, RT = 8;
 };
 
+// ---- the FP32 trailing update on the tensor cores (tcgen05, kind::tf32) ----
+//
+// One CTA (128 threads) per 128 x 128 tile of the trailing lower triangle:
+// the panel slices L[i0:i0+128, p0:p0+64] and W[j0:j0+128, 0:64] are split
+// into TF32 high and low parts (x = hi + lo, hi = x rounded to TF32) and
+// staged in shared memory in the canonical K-major layout without swizzle
+// (8-row x 16-byte core matrices; K-adjacent cores 128 B apart, 8-row groups
+// 2 KB apart); one thread issues 8 k-steps x 3 MMAs (hi.hi + hi.lo + lo.hi,
+// FP32 accumulation in 128 TMEM columns), whose completion it commits to an
+// mbarrier; then each warp reads its 32 TMEM lanes (rows) and subtracts them
+// from the front.  Every wait on the mbarrier is bounded: on a timeout the
+// tile is left unchanged and err[0] is set.
+constexpr int kTcM = 128, kTcN = 128, kTcK = 64;
+constexpr int kTcThreads = 128;
+constexpr uint32_t kTcTileFloats = kTcM * kTcK;                 // one 128 x 64 operand
+constexpr size_t kTcSmem = 4 * kTcTileFloats * sizeof(float) + 64;
+// instruction descriptor: D F32 (bit 4), A and B TF32 (bits 7, 10), both
+// K-major, N / 8 at bit 17, M / 16 at bit 24
+constexpr uint32_t kTcIdesc =
+    (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kTcN >> 3) << 17) | ((uint32_t)(kTcM >> 4) << 24);
+constexpr long long kTcSpinLimit = 1ll << 26;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// shared-memory matrix descriptor: start, leading (K) and stride (8-row) byte
+// offsets, descriptor version 1, no swizzle
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+__device__ __forceinline__ float tf32_hi(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+// offset (floats) of element (row r, k) of a 128 x 64 K-major operand
+__device__ __forceinline__ uint32_t tc_off(int r, int k) {
+  return (uint32_t)(((r >> 3) * (kTcK / 4) + (k >> 2)) * 32 + (r & 7) * 4 + (k & 3));
+}
+
+__device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t phase) {
+  for (long long it = 0; it < kTcSpinLimit; it++) {
+    uint32_t done;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(mbar), "r"(phase)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__global__ void __launch_bounds__(kTcThreads)
+    tc_trailing_kernel(BigBatch b, LdltDev d, float* __restrict__ front, int64_t p0,
+                       const float* __restrict__ Wbuf, int* __restrict__ err) {
+  const int ti = blockIdx.x, tj = blockIdx.y;
+  if (tj > ti) return;
+  const int s = b.list[blockIdx.z];
+  const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
+  const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
+  if (p0 >= k) return;
+  const int pb = (int)(k - p0 < kPanel ? k - p0 : kPanel);
+  const int64_t q0 = p0 + pb;
+  const int64_t i0 = q0 + (int64_t)ti * kTcM, j0 = q0 + (int64_t)tj * kTcN;
+  if (i0 >= m) return;
+  float* F = front + d.front_off[s];
+  const float* W = Wbuf + b.w_off[blockIdx.z];
+  extern __shared__ __align__(1024) unsigned char tc_smem[];
+  float* Ahi = reinterpret_cast<float*>(tc_smem);
+  float* Alo = Ahi + kTcTileFloats;
+  float* Bhi = Alo + kTcTileFloats;
+  float* Blo = Bhi + kTcTileFloats;
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(Blo + kTcTileFloats);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_addr(tmem_slot)),
+                 "r"(kTcN));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(mbar)), "r"(1));
+    asm volatile("fence.mbarrier_init.release.cluster;");
+  }
+  // stage the operands: thread r holds row r of each tile (coalesced column reads)
+  {
+    const int r = threadIdx.x;
+    const int64_t i = i0 + r, j = j0 + r;
+    for (int c = 0; c < kTcK; c++) {
+      const float a = (c < pb && i < m) ? F[i + (p0 + c) * m] : 0.0f;
+      const float w = (c < pb && j < m) ? W[(j - q0) + c * m] : 0.0f;
+      const float ah = tf32_hi(a), wh = tf32_hi(w);
+      const uint32_t o = tc_off(r, c);
+      Ahi[o] = ah;
+      Alo[o] = a - ah;
+      Bhi[o] = wh;
+      Blo[o] = w - wh;
+    }
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+  if (threadIdx.x == 0) {
+    const uint32_t lbo = 128, sbo = (kTcK / 4) * 128;
+    const uint32_t ahi = smem_addr(Ahi), alo = smem_addr(Alo);
+    const uint32_t bhi = smem_addr(Bhi), blo = smem_addr(Blo);
+    for (int st = 0; st < kTcK / 8; st++) {
+      const uint32_t koff = st * 256;   // 8 K values = two core matrices
+      const uint64_t dah = tc_desc(ahi + koff, lbo, sbo), dal = tc_desc(alo + koff, lbo, sbo);
+      const uint64_t dbh = tc_desc(bhi + koff, lbo, sbo), dbl = tc_desc(blo + koff, lbo, sbo);
+      const uint32_t acc = st > 0 ? 1u : 0u;
+      asm volatile(
+          "{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\n"
+          "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+          "l"(dah), "l"(dbh), "r"(kTcIdesc), "r"(acc));
+      asm volatile(
+          "{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\n"
+          "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+          "l"(dah), "l"(dbl), "r"(kTcIdesc), "r"(1u));
+      asm volatile(
+          "{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\n"
+          "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+          "l"(dal), "l"(dbh), "r"(kTcIdesc), "r"(1u));
+    }
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+            smem_addr(mbar))
+        : "memory");
+  }
+  const bool ok = tc_wait(smem_addr(mbar), 0);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (!ok) {
+    if (lane == 0) atomicExch(err, 1);
+  } else {
+    // warp w: TMEM lanes 32w .. 32w+31 = tile rows; 16 columns per load
+    const int r = warp * 32 + lane;
+    const int64_t i = i0 + r;
+    for (int c0 = 0; c0 < kTcN; c0 += 16) {
+      uint32_t v[16];
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+          "%11, %12, %13, %14, %15}, [%16];"
+          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+            "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
+            "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+          : "r"(taddr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (i < m)
+        for (int q = 0; q < 16; q++) {
+          const int64_t j = j0 + c0 + q;
+          if (j < m && j <= i) F[i + j * m] -= __uint_as_float(v[q]);
+        }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    // after a timeout the MMAs may still run: give them another bounded wait
+    if (!ok) tc_wait(smem_addr(mbar), 0);
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcN));
+  }
+}
+
 // ---- solve kernels ----
 
 __global__ void solve_init_kernel(int64_t n, const int32_t* __restrict__ perm,
@@ -739,6 +913,8 @@ __global__ void spmv_kernel(int64_t n, const int64_t* __restrict__ ptr,
 struct nla3d_ldlt {
   LdltSymbolic S;
   int prec = 0;   // 0: FP64 fronts, 1: FP32 fronts (FP64 refinement)
+  bool tc = false;   // FP32 fronts with the trailing updates on the tensor cores
+  int* d_err = nullptr;
   double pivot_rel = 1e-13;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
@@ -858,8 +1034,13 @@ cudaError_t enqueue_factor(nla3d_ldlt* h, const double* values) {
         batched_panel_kernel<T><<<dim3(tiles, nf), kThreads, 0, st>>>(bb, h->dev, front, p0, Li, W);
         constexpr int BT = TrailingShape<T>::BT, RT = TrailingShape<T>::RT;
         const unsigned ttiles = (unsigned)((rest + BT - 1) / BT);
-        batched_trailing_kernel<T, BT, RT><<<dim3(ttiles, ttiles, nf), kThreads, 0, st>>>(
-            bb, h->dev, front, p0, W);
+        if (std::is_same<T, float>::value && h->tc)
+          tc_trailing_kernel<<<dim3(ttiles, ttiles, nf), kTcThreads, kTcSmem, st>>>(
+              bb, h->dev, reinterpret_cast<float*>(front), p0,
+              reinterpret_cast<const float*>(W), h->d_err);
+        else
+          batched_trailing_kernel<T, BT, RT><<<dim3(ttiles, ttiles, nf), kThreads, 0, st>>>(
+              bb, h->dev, front, p0, W);
       }
     }
   }
@@ -960,9 +1141,11 @@ int nla3d_ldlt_analyze(int64_t n, const uint32_t* iofeir, const uint32_t* column
 
 int nla3d_ldlt_create(int64_t n, const uint32_t* iofeir, const uint32_t* columns,
                       const int32_t* perm, int precision, void* stream, nla3d_ldlt** out) {
-  if (!out || (precision != 0 && precision != 1)) return NLA3D_ERR_ARG;
+  if (!out || precision < 0 || precision > 2) return NLA3D_ERR_ARG;
   *out = nullptr;
   nla3d_ldlt* h = new nla3d_ldlt();
+  h->tc = precision == 2;
+  if (precision == 2) precision = 1;
   h->prec = precision;
   if (precision == 1) h->pivot_rel = 1e-7;
   const std::string msg = ldlt_analyze(n, iofeir, columns, perm, &h->S);
@@ -1096,6 +1279,11 @@ int nla3d_ldlt_create(int64_t n, const uint32_t* iofeir, const uint32_t* columns
   LCK(dalloc(h, &h->d_maxabs, 1));
   LCK(dalloc(h, &h->d_maxpart, kMaxBlocks));
   LCK(dalloc(h, &h->d_perturbed, 2));
+  LCK(dalloc(h, &h->d_err, 1));
+  LCK(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
+  if (h->tc)
+    LCK(cudaFuncSetAttribute(tc_trailing_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)kTcSmem));
   LCK(upload(h, &h->d_adest, S.a_dest));
   LCK(upload(h, &h->d_perm, S.perm));
   LCK(upload(h, &h->d_col2sn, col2sn));
@@ -1150,8 +1338,15 @@ int nla3d_ldlt_factor(nla3d_ldlt* h, const double* values) {
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(h->perturbed, h->d_perturbed, 2 * sizeof(int), cudaMemcpyDeviceToHost,
                         h->stream);
+  int tc_err = 0;
+  if (e == cudaSuccess && h->tc)
+    e = cudaMemcpyAsync(&tc_err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
   if (e != cudaSuccess) return cuda_fail(h, e, "ldlt_factor");
+  if (tc_err) {
+    h->factored = false;
+    return fail(h, NLA3D_ERR_CUDA, "ldlt_factor: a tensor-core tile timed out waiting for its MMAs");
+  }
   h->factored = true;
   if (h->perturbed[1]) return fail(h, NLA3D_ERR_ELEMENT, "ldlt_factor: a non-finite pivot");
   return NLA3D_OK;
@@ -1316,6 +1511,93 @@ int nla3d_ldlt_solve(nla3d_ldlt* h, const double* values, const double* b, doubl
   if (steps) *steps = it;
   if (rel_residual) *rel_residual = rel;
   if (!(rel <= tol)) return fail(h, NLA3D_ERR_RANGE, "ldlt_solve: refinement did not reach tol");
+  return NLA3D_OK;
+}
+
+int nla3d_ldlt_tc_check(int m, double* out) {
+  // one front of m rows whose first panel (64 pivots) is done: the trailing
+  // update of rows / columns 64 .. m-1 by the FMA kernel and by the tensor
+  // cores from the same random data; out[0] = max |difference|, out[1] =
+  // max |update|
+  if (m < kPanel + 1 || m > 4096 || !out) return NLA3D_ERR_ARG;
+  const size_t mm = (size_t)m * m, mw = (size_t)m * kPanel;
+  std::vector<float> F0(mm), W(mw);
+  uint64_t x = 88172645463325252ull;   // xorshift, fixed seed
+  auto rnd = [&]() {
+    x ^= x << 13;
+    x ^= x >> 7;
+    x ^= x << 17;
+    return (float)((double)(x >> 11) / 9007199254740992.0 * 2.0 - 1.0);
+  };
+  for (auto& v : F0) v = rnd();
+  for (auto& v : W) v = rnd();
+  std::vector<void*> allocs;
+  auto dal = [&](void** p, size_t bytes) {
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e == cudaSuccess) allocs.push_back(*p);
+    return e;
+  };
+  float *F1 = nullptr, *F2 = nullptr, *dW = nullptr;
+  int* err = nullptr;
+  int32_t* list = nullptr;
+  uint64_t *woff = nullptr, *foff = nullptr;
+  int64_t* rowp = nullptr;
+  int32_t* snf = nullptr;
+  cudaError_t e = dal((void**)&F1, mm * 4);
+  if (e == cudaSuccess) e = dal((void**)&F2, mm * 4);
+  if (e == cudaSuccess) e = dal((void**)&dW, mw * 4);
+  if (e == cudaSuccess) e = dal((void**)&err, 4);
+  if (e == cudaSuccess) e = dal((void**)&list, 4);
+  if (e == cudaSuccess) e = dal((void**)&woff, 8);
+  if (e == cudaSuccess) e = dal((void**)&foff, 16);
+  if (e == cudaSuccess) e = dal((void**)&rowp, 16);
+  if (e == cudaSuccess) e = dal((void**)&snf, 8);
+  const int32_t zero32 = 0;
+  const uint64_t zero64[2] = {0, (uint64_t)mm};
+  const int64_t rp[2] = {0, m};
+  const int32_t sf[2] = {0, kPanel};
+  if (e == cudaSuccess) e = cudaMemcpy(F1, F0.data(), mm * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(F2, F0.data(), mm * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dW, W.data(), mw * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(err, 0, 4);
+  if (e == cudaSuccess) e = cudaMemcpy(list, &zero32, 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(woff, zero64, 8, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(foff, zero64, 16, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(rowp, rp, 16, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(snf, sf, 8, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(tc_trailing_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)kTcSmem);
+  int tc_err = 0;
+  if (e == cudaSuccess) {
+    LdltDev d{};
+    d.front_off = foff;
+    d.row_ptr = rowp;
+    d.sn_first = snf;
+    const BigBatch bb{list, woff, woff};
+    const int64_t rest = m - kPanel;
+    const unsigned t128 = (unsigned)((rest + 127) / 128);
+    batched_trailing_kernel<float, 128, 8><<<dim3(t128, t128, 1), kThreads>>>(bb, d, F1, 0, dW);
+    tc_trailing_kernel<<<dim3(t128, t128, 1), kTcThreads, kTcSmem>>>(bb, d, F2, 0, dW, err);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(&tc_err, err, 4, cudaMemcpyDeviceToHost);
+  }
+  std::vector<float> R1(mm), R2(mm);
+  if (e == cudaSuccess) e = cudaMemcpy(R1.data(), F1, mm * 4, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(R2.data(), F2, mm * 4, cudaMemcpyDeviceToHost);
+  for (void* p : allocs) cudaFree(p);
+  if (e != cudaSuccess) return NLA3D_ERR_CUDA;
+  if (tc_err) return NLA3D_ERR_RANGE;
+  double dmax = 0.0, umax = 0.0;
+  for (int j = kPanel; j < m; j++)
+    for (int i = j; i < m; i++) {
+      const size_t q = (size_t)i + (size_t)j * m;
+      dmax = std::max(dmax, (double)std::fabs(R1[q] - R2[q]));
+      umax = std::max(umax, (double)std::fabs(R1[q] - F0[q]));
+    }
+  out[0] = dmax;
+  out[1] = umax;
   return NLA3D_OK;
 }
 

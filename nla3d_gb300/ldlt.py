@@ -93,7 +93,7 @@ class DeviceLDLT:
         co = np.ascontiguousarray(columns, dtype=np.uint32)
         self.n = io.size - 1
         pa = _perm_array(perm, self.n)
-        prec = {"fp64": 0, "fp32": 1}[precision]
+        prec = {"fp64": 0, "fp32": 1, "fp32-tc": 2}[precision]
         h = ctypes.c_void_p()
         rc = self.lib.nla3d_ldlt_create(self.n, _p(io), _p(co), _p(pa), prec,
                                         ctypes.c_void_p(stream) if stream else None,

@@ -125,9 +125,10 @@ class NewtonSolver:
         refactors only when GMRES needs more than 30 iterations; "gpu" factors
         the device K(2) in place with the library's multifrontal LDL^T
         (nla3d_gb300.ldlt; the same nested-dissection order, the MPC
-        equations and master DoFs last), "gpu-fp32" with FP32 fronts.  Every
+        equations and master DoFs last), "gpu-fp32" with FP32 fronts, "gpu-tc"
+        with FP32 fronts updated on the tensor cores.  Every
         non-default solve is checked to a relative residual of 1e-10."""
-        if solver not in ("direct", "nd", "lu-gmres", "gpu", "gpu-fp32"):
+        if solver not in ("direct", "nd", "lu-gmres", "gpu", "gpu-fp32", "gpu-tc"):
             raise ValueError(solver)
         self._ldlt = None
         self._ldlt64 = None
@@ -201,8 +202,8 @@ class NewtonSolver:
             K = csr_full(io, co, np.ones(co.size), n2, n2, True)
             order = nested_dissection(K, self._row_points())
             self._perm = saddle_order(io, co, order, self.nu)
-            self._ldlt = DeviceLDLT.for_storage(self.b, self._perm,
-                                                "fp32" if self.solver == "gpu-fp32" else "fp64")
+            self._ldlt = DeviceLDLT.for_storage(
+                self.b, self._perm, {"gpu": "fp64", "gpu-fp32": "fp32", "gpu-tc": "fp32-tc"}[self.solver])
         self._ldlt.factor(self.b)
         self.factorizations += 1
         x = self._ldlt.solve_host(self.b, rhs, max_refine=100, tol=1e-10, strict=False)
@@ -220,7 +221,7 @@ class NewtonSolver:
         return self._ldlt64.solve_host(self.b, rhs, max_refine=100, tol=1e-10)
 
     def _solve(self, K2, rhs):
-        if self.solver in ("gpu", "gpu-fp32"):
+        if self.solver.startswith("gpu"):
             return self._solve_gpu(rhs)
         if self.solver == "direct":
             self.factorizations += 1
@@ -361,7 +362,7 @@ class NewtonSolver:
                     rec.iterations = tc.eq_step - 1
                     converged = True
                     break
-                K2 = None if self.solver in ("gpu", "gpu-fp32") else self._K2().tocsc()
+                K2 = None if self.solver.startswith("gpu") else self._K2().tocsc()
                 dUsl = self._solve(K2, rhs)
                 self.U[: self.nc] = Uc
                 self.U[self.nc: self.nc + self.nu] += dUsl[: self.nu]

@@ -104,3 +104,28 @@ def test_fp32_fronts_on_a_nearly_incompressible_block():
     s = _storage(mesh, u, p, None, True)
     solver, x = _check(s, "fp32", 1e-12)
     assert solver.last_steps >= 2
+
+
+@pytest.mark.parametrize("m", [200, 700])
+def test_tensor_core_trailing_update_matches_fma(m):
+    """The tcgen05 trailing update (split TF32, FP32 accumulation) against the
+    FMA kernel on the same random front: FP32-level agreement."""
+    from nla3d_gb300 import _lib
+    out = np.zeros(2)
+    assert _lib.load().nla3d_ldlt_tc_check(m, out.ctypes.data) == 0
+    assert out[0] <= 1e-5 * out[1]
+
+
+@pytest.mark.parametrize("name", ["cube4_nh_clamped", "bar_mpc_2x2x3", "quadth_lines_6x5"])
+def test_tensor_core_fronts_small_cases(name):
+    s = _storage(*cases.FULL_CASES[name]())
+    _check(s, "fp32-tc", 1e-12)
+
+
+def test_tensor_core_fronts_twisted_block():
+    mesh = mg.solid81_block(12, 12, 12, 1.0 / 12, mg.MAT_MOONEY_RIVLIN, (0.4, 0.1, 2000.0),
+                            clamp_z0=True)
+    u, p = mg.twist_state(mesh, angle_deg=20.0, stretch=1.3, noise_frac=0.005, seed=2)
+    s = _storage(mesh, u, p, None, True)
+    solver, x = _check(s, "fp32-tc", 1e-12)
+    assert solver.info()["max_front"] > 256
