@@ -395,19 +395,23 @@ struct TrailingShape<float> {
 
 // ---- the FP32 trailing update on the tensor cores (tcgen05, kind::tf32) ----
 //
-// One CTA (128 threads) per 128 x 128 tile of the trailing lower triangle:
-// the panel slices L[i0:i0+128, p0:p0+64] and W[j0:j0+128, 0:64] are split
-// into TF32 high and low parts (x = hi + lo, hi = x rounded to TF32) and
-// staged in shared memory in the canonical K-major layout without swizzle
-// (8-row x 16-byte core matrices; K-adjacent cores 128 B apart, 8-row groups
-// 2 KB apart); one thread issues 8 k-steps x 3 MMAs (hi.hi + hi.lo + lo.hi,
-// FP32 accumulation in 128 TMEM columns), whose completion it commits to an
-// mbarrier; then each warp reads its 32 TMEM lanes (rows) and subtracts them
-// from the front.  Every wait on the mbarrier is bounded: on a timeout the
-// tile is left unchanged and err[0] is set.
-constexpr int kTcM = 128, kTcN = 128, kTcK = 64;
-constexpr int kTcThreads = 128;
-constexpr uint32_t kTcTileFloats = kTcM * kTcK;                 // one 128 x 64 operand
+// One CTA (256 threads) per 128 x 128 tile of the trailing lower triangle.
+// The panel slices L[i0:i0+128, p0:p0+64] and W[j0:j0+128, 0:64] are taken
+// in two halves of 32 columns; each half is split into TF32 high and low
+// parts (x = hi + lo, hi = x rounded to TF32) and staged in shared memory in
+// the canonical K-major layout without swizzle (8-row x 16-byte core
+// matrices; K-adjacent cores 128 B apart, 8-row groups 1 KB apart).  One
+// thread issues 4 k-steps x 3 MMAs per half (hi.hi + hi.lo + lo.hi, FP32
+// accumulation in 128 TMEM columns) and commits them to an mbarrier; the
+// second half is staged once the first half's MMAs are done with the
+// buffers.  Then each warp reads 32 TMEM lanes (rows) x 64 columns and
+// subtracts them from the front.  64 KB of shared memory and 128 TMEM
+// columns per CTA, so that three CTAs share an SM and one's loads overlap
+// another's MMAs and epilogue.  Every wait on the mbarrier is bounded: on a
+// timeout the tile is left unchanged and err[0] is set.
+constexpr int kTcM = 128, kTcN = 128, kTcKH = 32;   // tile rows, columns, K per half
+constexpr int kTcThreads = 256;
+constexpr uint32_t kTcTileFloats = kTcM * kTcKH;     // one 128 x 32 operand half
 constexpr size_t kTcSmem = 4 * kTcTileFloats * sizeof(float) + 64;
 // instruction descriptor: D F32 (bit 4), A and B TF32 (bits 7, 10), both
 // K-major, N / 8 at bit 17, M / 16 at bit 24
@@ -432,9 +436,9 @@ __device__ __forceinline__ float tf32_hi(float x) {
   return __uint_as_float(r);
 }
 
-// offset (floats) of element (row r, k) of a 128 x 64 K-major operand
+// offset (floats) of element (row r, k) of a 128 x 32 K-major operand half
 __device__ __forceinline__ uint32_t tc_off(int r, int k) {
-  return (uint32_t)(((r >> 3) * (kTcK / 4) + (k >> 2)) * 32 + (r & 7) * 4 + (k & 3));
+  return (uint32_t)(((r >> 3) * (kTcKH / 4) + (k >> 2)) * 32 + (r & 7) * 4 + (k & 3));
 }
 
 __device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t phase) {
@@ -449,6 +453,13 @@ __device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t phase) {
     if (done) return true;
   }
   return false;
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t a, uint64_t b, uint32_t acc) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+      "l"(a), "l"(b), "r"(kTcIdesc), "r"(acc));
 }
 
 __global__ void __launch_bounds__(kTcThreads)
@@ -484,64 +495,62 @@ __global__ void __launch_bounds__(kTcThreads)
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(mbar)), "r"(1));
     asm volatile("fence.mbarrier_init.release.cluster;");
   }
-  // stage the operands: thread r holds row r of each tile (coalesced column reads)
-  {
-    const int r = threadIdx.x;
-    const int64_t i = i0 + r, j = j0 + r;
-    for (int c = 0; c < kTcK; c++) {
-      const float a = (c < pb && i < m) ? F[i + (p0 + c) * m] : 0.0f;
-      const float w = (c < pb && j < m) ? W[(j - q0) + c * m] : 0.0f;
-      const float ah = tf32_hi(a), wh = tf32_hi(w);
-      const uint32_t o = tc_off(r, c);
-      Ahi[o] = ah;
-      Alo[o] = a - ah;
-      Bhi[o] = wh;
-      Blo[o] = w - wh;
+  const int r = threadIdx.x % kTcM, kq = threadIdx.x / kTcM;   // row, which 16 of the 32
+  const int64_t ia = i0 + r, jb = j0 + r;
+  const uint32_t lbo = 128, sbo = (kTcKH / 4) * 128;
+  bool ok = true;
+  uint32_t tmem = 0;
+  for (int h = 0; h < 2 && ok; h++) {
+    if (h == 1) ok = tc_wait(smem_addr(mbar), 0);   // half 0's MMAs are done with the buffers
+    if (ok) {
+#pragma unroll 4
+      for (int q = 0; q < 16; q++) {
+        const int kk = kq * 16 + q, c = h * kTcKH + kk;
+        const float a = (c < pb && ia < m) ? F[ia + (p0 + c) * m] : 0.0f;
+        const float w = (c < pb && jb < m) ? W[(jb - q0) + c * m] : 0.0f;
+        const float ah = tf32_hi(a), wh = tf32_hi(w);
+        const uint32_t o = tc_off(r, kk);
+        Ahi[o] = ah;
+        Alo[o] = a - ah;
+        Bhi[o] = wh;
+        Blo[o] = w - wh;
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    tmem = *tmem_slot;
+    ok = __syncthreads_and(ok ? 1 : 0) != 0;
+    if (ok && threadIdx.x == 0) {
+      const uint32_t ahi = smem_addr(Ahi), alo = smem_addr(Alo);
+      const uint32_t bhi = smem_addr(Bhi), blo = smem_addr(Blo);
+      for (int st = 0; st < kTcKH / 8; st++) {
+        const uint32_t koff = st * 256;   // 8 K values = two core matrices
+        const uint64_t dah = tc_desc(ahi + koff, lbo, sbo), dal = tc_desc(alo + koff, lbo, sbo);
+        const uint64_t dbh = tc_desc(bhi + koff, lbo, sbo), dbl = tc_desc(blo + koff, lbo, sbo);
+        tc_mma(tmem, dah, dbh, (h > 0 || st > 0) ? 1u : 0u);
+        tc_mma(tmem, dah, dbl, 1u);
+        tc_mma(tmem, dal, dbh, 1u);
+      }
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+              smem_addr(mbar))
+          : "memory");
     }
   }
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  __syncthreads();
+  if (ok) ok = tc_wait(smem_addr(mbar), 1);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  const uint32_t tmem = *tmem_slot;
-  if (threadIdx.x == 0) {
-    const uint32_t lbo = 128, sbo = (kTcK / 4) * 128;
-    const uint32_t ahi = smem_addr(Ahi), alo = smem_addr(Alo);
-    const uint32_t bhi = smem_addr(Bhi), blo = smem_addr(Blo);
-    for (int st = 0; st < kTcK / 8; st++) {
-      const uint32_t koff = st * 256;   // 8 K values = two core matrices
-      const uint64_t dah = tc_desc(ahi + koff, lbo, sbo), dal = tc_desc(alo + koff, lbo, sbo);
-      const uint64_t dbh = tc_desc(bhi + koff, lbo, sbo), dbl = tc_desc(blo + koff, lbo, sbo);
-      const uint32_t acc = st > 0 ? 1u : 0u;
-      asm volatile(
-          "{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\n"
-          "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-          "l"(dah), "l"(dbh), "r"(kTcIdesc), "r"(acc));
-      asm volatile(
-          "{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\n"
-          "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-          "l"(dah), "l"(dbl), "r"(kTcIdesc), "r"(1u));
-      asm volatile(
-          "{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\n"
-          "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-          "l"(dal), "l"(dbh), "r"(kTcIdesc), "r"(1u));
-    }
-    asm volatile(
-        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-            smem_addr(mbar))
-        : "memory");
-  }
-  const bool ok = tc_wait(smem_addr(mbar), 0);
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  ok = __syncthreads_and(ok ? 1 : 0) != 0;
   if (!ok) {
-    if (lane == 0) atomicExch(err, 1);
+    if (threadIdx.x == 0) atomicExch(err, 1);
   } else {
-    // warp w: TMEM lanes 32w .. 32w+31 = tile rows; 16 columns per load
-    const int r = warp * 32 + lane;
-    const int64_t i = i0 + r;
-    for (int c0 = 0; c0 < kTcN; c0 += 16) {
+    // warp w: TMEM lanes 32 (w % 4) .. +31 = tile rows, columns 64 (w / 4) .. +63
+    const int row = (warp & 3) * 32 + lane;
+    const int64_t i = i0 + row;
+    for (int c0 = (warp >> 2) * 64; c0 < (warp >> 2) * 64 + 64; c0 += 16) {
       uint32_t v[16];
-      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+      const uint32_t taddr = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)c0;
       asm volatile(
           "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
           "%11, %12, %13, %14, %15}, [%16];"
@@ -551,6 +560,7 @@ __global__ void __launch_bounds__(kTcThreads)
           : "r"(taddr));
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
       if (i < m)
+#pragma unroll
         for (int q = 0; q < 16; q++) {
           const int64_t j = j0 + c0 + q;
           if (j < m && j <= i) F[i + j * m] -= __uint_as_float(v[q]);
@@ -561,7 +571,10 @@ __global__ void __launch_bounds__(kTcThreads)
   __syncthreads();
   if (warp == 0) {
     // after a timeout the MMAs may still run: give them another bounded wait
-    if (!ok) tc_wait(smem_addr(mbar), 0);
+    if (!ok) {
+      tc_wait(smem_addr(mbar), 0);
+      tc_wait(smem_addr(mbar), 1);
+    }
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcN));
   }
 }
