@@ -84,6 +84,8 @@ def parse():
                          "K(2) factored on the device; prints one JSON line and exits")
     ap.add_argument("--learned-train", type=int, default=120)
     ap.add_argument("--learned-eval", type=int, default=16)
+    ap.add_argument("--newton-solver", default="gpu-fp32", choices=["gpu", "gpu-fp32", "gpu-tc"],
+                    help="K(2) solve of --newton-bar and --learned-blocks")
     ap.add_argument("--newton-assembly", default="fp64,mixed",
                     help="assembly precisions of --newton-bar (the mixed run uses the plain start)")
     ap.add_argument("--model-solver", default="nd",
@@ -736,17 +738,18 @@ def run_newton_bar(args):
     res = {}
     precisions = args.newton_assembly.split(",")
     if "fp64" in precisions:
-        res["fp64_assembly"] = L.evaluate([cfg], mlp, precision="fp64", linear_solver="gpu-fp32",
-                                          starts=starts, log=log)
+        res["fp64_assembly"] = L.evaluate([cfg], mlp, precision="fp64",
+                                          linear_solver=args.newton_solver, starts=starts, log=log)
     if "mixed" in precisions:
         res["mixed_assembly"] = L.evaluate([cfg], mlp, precision="mixed",
-                                           linear_solver="gpu-fp32", starts=("plain",), log=log)
+                                           linear_solver=args.newton_solver, starts=("plain",),
+                                           log=log)
     print(json.dumps({
         "metric": "Newton iterations per load step (residual 1e-8)", "unit": "iterations",
         "higher_is_better": False,
         "workload": f"torsion + stretch bar {nx}x{nx}x{4 * nx} ({cfg.mesh.n_elems} SOLID81), "
                     "rigid-body MPC end, 50 load steps",
-        "linear_solver": "device LDL^T, FP32 fronts + FP64 refinement",
+        "linear_solver": f"device LDL^T ({args.newton_solver}), FP64 refinement",
         "results": res, "training": train, "wall_s": time.perf_counter() - t0}), flush=True)
 
 
@@ -763,14 +766,14 @@ def run_learned_blocks(args):
     log = lambda m: print(m, file=sys.stderr, flush=True)  # noqa: E731
     t0 = time.perf_counter()
     X, Y, its = L.generate(L.sample_block_problems(args.learned_train, n=n, seed=11),
-                           linear_solver="gpu-fp32")
+                           linear_solver=args.newton_solver)
     t_gen = time.perf_counter() - t0
     log(f"generated {X.shape[0]} samples from {args.learned_train} solves in {t_gen:.1f} s")
     mlp = L.MLP(seed=0)
     hist = mlp.fit(X, Y, epochs=300, batch=128, lr=2e-3)
     t_fit = time.perf_counter() - t0 - t_gen
     res = L.evaluate(L.sample_block_problems(args.learned_eval, n=n, seed=99), mlp,
-                     linear_solver="gpu-fp32", log=None)
+                     linear_solver=args.newton_solver, log=None)
     print(json.dumps({
         "metric": "Newton iterations per load step (residual 1e-8), learned vs plain start",
         "unit": "iterations", "higher_is_better": False,
@@ -780,7 +783,7 @@ def run_learned_blocks(args):
         "train_plain_iterations": float(np.mean([np.mean(i) for i in its])),
         "final_loss": hist[-1][1], "eval_solves": args.learned_eval, "results": res,
         "generate_s": t_gen, "fit_s": t_fit, "wall_s": time.perf_counter() - t0,
-        "linear_solver": "device LDL^T, FP32 fronts + FP64 refinement"}), flush=True)
+        "linear_solver": f"device LDL^T ({args.newton_solver}), FP64 refinement"}), flush=True)
 
 
 def main():

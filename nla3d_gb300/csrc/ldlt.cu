@@ -946,6 +946,9 @@ struct nla3d_ldlt {
   int* d_perturbed = nullptr;
   void* d_W = nullptr;
   void* d_Linv = nullptr;
+  double* d_rhs = nullptr;      // the solve graph's right-hand side
+  cudaGraphExec_t factor_exec = nullptr, solve_exec = nullptr;
+  const double* factor_graph_values = nullptr;
   uint64_t* d_wo = nullptr;
   uint64_t* d_lio = nullptr;
   uint64_t* d_adest = nullptr;
@@ -1061,7 +1064,7 @@ cudaError_t enqueue_factor(nla3d_ldlt* h, const double* values) {
 }
 
 template <typename T>
-cudaError_t enqueue_solve(nla3d_ldlt* h, const double* b, double* x, int accumulate) {
+cudaError_t enqueue_solve_core(nla3d_ldlt* h, const double* b) {
   const LdltSymbolic& S = h->S;
   const T* front = static_cast<const T*>(h->d_front);
   cudaStream_t st = h->stream;
@@ -1113,7 +1116,6 @@ cudaError_t enqueue_solve(nla3d_ldlt* h, const double* b, double* x, int accumul
                             kThreads, 0, st>>>(bb, h->dev, h->d_vec, h->d_xf);
     }
   }
-  solve_finish_kernel<<<nb, kThreads, 0, st>>>(S.n, h->d_perm, h->d_xf, x, accumulate);
   return cudaGetLastError();
 }
 
@@ -1285,6 +1287,7 @@ int nla3d_ldlt_create(int64_t n, const uint32_t* iofeir, const uint32_t* columns
   LCK(upload(h, &h->d_lio, lio));
   LCK(dalloc(h, &h->d_vec, S.vec_off.back()));
   LCK(dalloc(h, &h->d_xf, S.n));
+  LCK(dalloc(h, &h->d_rhs, S.n));
   LCK(dalloc(h, &h->d_r, S.n));
   LCK(dalloc(h, &h->d_dx, S.n));
   LCK(dalloc(h, &h->d_part, 2 * ((S.n + 7) / 8 + 1)));
@@ -1347,7 +1350,26 @@ int nla3d_ldlt_info(const nla3d_ldlt* h, double* out) {
 int nla3d_ldlt_factor(nla3d_ldlt* h, const double* values) {
   if (!h || !values) return fail(h, NLA3D_ERR_ARG, "ldlt_factor: null argument");
   if (!h->d_front) return fail(h, NLA3D_ERR_ARG, "ldlt_factor: the handle was not set up");
-  cudaError_t e = h->prec ? enqueue_factor<float>(h, values) : enqueue_factor<double>(h, values);
+  // the factorisation's kernel sequence is captured once per values array
+  // into a CUDA graph and replayed
+  cudaError_t e = cudaSuccess;
+  if (!h->factor_exec || h->factor_graph_values != values) {
+    if (h->factor_exec) cudaGraphExecDestroy(h->factor_exec);
+    h->factor_exec = nullptr;
+    cudaGraph_t g = nullptr;
+    e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      const cudaError_t ec = h->prec ? enqueue_factor<float>(h, values)
+                                     : enqueue_factor<double>(h, values);
+      e = cudaStreamEndCapture(h->stream, &g);
+      if (ec != cudaSuccess) e = ec;
+      if (e == cudaSuccess) e = cudaGraphInstantiate(&h->factor_exec, g, 0);
+      if (g) cudaGraphDestroy(g);
+      if (e != cudaSuccess) h->factor_exec = nullptr;
+      h->factor_graph_values = values;
+    }
+  }
+  if (e == cudaSuccess) e = cudaGraphLaunch(h->factor_exec, h->stream);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(h->perturbed, h->d_perturbed, 2 * sizeof(int), cudaMemcpyDeviceToHost,
                         h->stream);
@@ -1375,8 +1397,35 @@ unsigned vec_blocks(int64_t n) {
   return (unsigned)std::min<int64_t>((n + kThreads - 1) / kThreads, 152 * 8);
 }
 
+// the solve's kernel sequence (a few thousand launches on large models) is
+// captured once into a CUDA graph reading d_rhs and leaving the factor-order
+// solution in d_xf; each solve copies its right-hand side in, replays the
+// graph and scatters (or adds) the result into `out`
 cudaError_t enqueue_solve_any(nla3d_ldlt* h, const double* rhs, double* out, int acc) {
-  return h->prec ? enqueue_solve<float>(h, rhs, out, acc) : enqueue_solve<double>(h, rhs, out, acc);
+  cudaError_t e = cudaSuccess;
+  if (!h->solve_exec) {
+    cudaGraph_t g = nullptr;
+    e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    const cudaError_t ec =
+        h->prec ? enqueue_solve_core<float>(h, h->d_rhs) : enqueue_solve_core<double>(h, h->d_rhs);
+    e = cudaStreamEndCapture(h->stream, &g);
+    if (ec != cudaSuccess) e = ec;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&h->solve_exec, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      h->solve_exec = nullptr;
+      return e;
+    }
+  }
+  if (rhs != h->d_rhs)
+    e = cudaMemcpyAsync(h->d_rhs, rhs, sizeof(double) * h->S.n, cudaMemcpyDeviceToDevice,
+                        h->stream);
+  if (e == cudaSuccess) e = cudaGraphLaunch(h->solve_exec, h->stream);
+  if (e != cudaSuccess) return e;
+  const unsigned nb = (unsigned)((h->S.n + kThreads - 1) / kThreads);
+  solve_finish_kernel<<<nb, kThreads, 0, h->stream>>>(h->S.n, h->d_perm, h->d_xf, out, acc);
+  return cudaGetLastError();
 }
 
 // <a, b> with a fixed reduction order (per-block partial sums, summed on the host)
@@ -1619,6 +1668,8 @@ int nla3d_ldlt_destroy(nla3d_ldlt* h) {
   // a borrowed stream may already be gone: only an owned one is synchronised
   // (cudaFree waits for the device anyway)
   if (h->own_stream && h->stream) cudaStreamSynchronize(h->stream);
+  if (h->factor_exec) cudaGraphExecDestroy(h->factor_exec);
+  if (h->solve_exec) cudaGraphExecDestroy(h->solve_exec);
   for (void* p : h->allocs) cudaFree(p);
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
   delete h;
