@@ -18,14 +18,18 @@
 //      constraint rows are ordered last by the caller); a pivot below
 //      tau = pivot_rel * max|A| is replaced by +-tau and counted, and the
 //      solve's iterative refinement recovers the accuracy.
-//      Fronts of <= kSmallFront rows: one thread block per front, all fronts
-//      of the level in one launch.  Larger fronts: blocked, 64 columns per
-//      panel (diagonal block, panel rows, then a tiled rank-64 update of the
-//      trailing lower triangle).
+//      Fronts of <= kSmallFront rows: one thread block per front, the front
+//      in shared memory, all fronts of the level in one launch.  Larger
+//      fronts: all of the level's together, blocked, 64 columns per panel
+//      (diagonal block and its inverse, panel rows, then a tiled rank-64
+//      update of the trailing lower triangle: FMA tiles, or tcgen05 TF32
+//      split MMAs for FP32 fronts with precision 2).
 // Solve (multifrontal, vectors): forward by levels with the same extend-add
 // on the update vectors, D^-1, backward by levels top-down gathering the
-// solved ancestor entries; FP64 iterative refinement r = b - A x with A's
-// both-triangle CSR in the input numbering.
+// solved ancestor entries; FP64 refinement r = b - A x with A's
+// both-triangle CSR in the input numbering (plain steps, then GMRES
+// preconditioned by the factor).  Factorisation and solve are captured once
+// into CUDA graphs and replayed.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
