@@ -228,17 +228,24 @@ __global__ void __launch_bounds__(kThreads)
   }
   for (int r = tr; r < pb; r += kThreads / kPanel)
     if (tc < pb && r >= tc) F[(p0 + r) + (p0 + tc) * m] = B[tc][r];
-  // inverse of the unit lower L11 in shared memory (X[col][row]), column c by
-  // thread c, then stored for step 2 and the solves
+  // inverse of the unit lower L11 in shared memory (X[col][row]): column c by
+  // the four consecutive lanes 4c .. 4c+3, row after row, each row's dot
+  // product split over the four lanes and summed by shuffles, so that only
+  // warp-level barriers separate the rows; then stored for step 2 and the solves
   T(*X)[kPanel + 1] = reinterpret_cast<T(*)[kPanel + 1]>(diag_smem);
-  if (threadIdx.x < pb) {
-    const int c = threadIdx.x;
-    for (int r = 0; r < c; r++) X[c][r] = T(0);
-    X[c][c] = T(1);
-    for (int r = c + 1; r < pb; r++) {
-      T acc = -B[c][r];
-      for (int q = c + 1; q < r; q++) acc -= B[q][r] * X[c][q];
-      X[c][r] = acc;
+  {
+    const int c = threadIdx.x >> 2, sub = threadIdx.x & 3;
+    if (c < pb)
+      for (int r = sub; r <= c; r += 4) X[c][r] = r == c ? T(1) : T(0);
+    __syncwarp();
+    for (int r = 1; r < pb; r++) {
+      T part = T(0);
+      if (c < r)
+        for (int q = c + sub; q < r; q += 4) part += B[q][r] * X[c][q];
+      part += __shfl_xor_sync(0xffffffffu, part, 1);
+      part += __shfl_xor_sync(0xffffffffu, part, 2);
+      if (sub == 0 && c < r) X[c][r] = -part;
+      __syncwarp();
     }
   }
   __syncthreads();
