@@ -514,17 +514,22 @@ __global__ void __launch_bounds__(kTcThreads)
   for (int h = 0; h < 2 && ok; h++) {
     if (h == 1) ok = tc_wait(smem_addr(mbar), 0);   // half 0's MMAs are done with the buffers
     if (ok) {
-#pragma unroll 4
+      // all 32 loads of this thread in flight first, then split and store
+      float av[16], wv[16];
+#pragma unroll
       for (int q = 0; q < 16; q++) {
-        const int kk = kq * 16 + q, c = h * kTcKH + kk;
-        const float a = (c < pb && ia < m) ? F[ia + (p0 + c) * m] : 0.0f;
-        const float w = (c < pb && jb < m) ? W[(jb - q0) + c * m] : 0.0f;
-        const float ah = tf32_hi(a), wh = tf32_hi(w);
-        const uint32_t o = tc_off(r, kk);
+        const int c = h * kTcKH + kq * 16 + q;
+        av[q] = (c < pb && ia < m) ? F[ia + (p0 + c) * m] : 0.0f;
+        wv[q] = (c < pb && jb < m) ? W[(jb - q0) + c * m] : 0.0f;
+      }
+#pragma unroll
+      for (int q = 0; q < 16; q++) {
+        const float ah = tf32_hi(av[q]), wh = tf32_hi(wv[q]);
+        const uint32_t o = tc_off(r, kq * 16 + q);
         Ahi[o] = ah;
-        Alo[o] = a - ah;
+        Alo[o] = av[q] - ah;
         Bhi[o] = wh;
-        Blo[o] = w - wh;
+        Blo[o] = wv[q] - wh;
       }
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
