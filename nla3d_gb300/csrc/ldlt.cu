@@ -984,6 +984,7 @@ struct nla3d_ldlt {
     int64_t wo_off = 0;                   // their W offsets in d_wo
     int64_t large_max_m = 0, large_max_k = 0;
     std::vector<int64_t> ea_off, ea_cnt;  // children of the level's parents, by ordinal
+    std::vector<uint32_t> ea_gy;          // column blocks per child (its update's size)
   };
   std::vector<Level> levels;
   bool factored = false;
@@ -1043,7 +1044,7 @@ cudaError_t enqueue_factor(nla3d_ldlt* h, const double* values) {
   for (const auto& L : h->levels) {
     for (size_t q = 0; q < L.ea_off.size(); q++) {
       if (!L.ea_cnt[q]) continue;
-      const dim3 grid((unsigned)L.ea_cnt[q], 16);
+      const dim3 grid((unsigned)L.ea_cnt[q], L.ea_gy[q]);
       extend_add_kernel<T><<<grid, kThreads, 0, st>>>(h->d_lists + L.ea_off[q], (int)L.ea_cnt[q],
                                                       h->dev, front);
     }
@@ -1236,11 +1237,18 @@ int nla3d_ldlt_create(int64_t n, const uint32_t* iofeir, const uint32_t* columns
     }
     for (int o = 0; o < maxc; o++) {
       lv.ea_off.push_back((int64_t)lists.size());
+      int64_t umax = 0;
       for (int32_t q = S.level_ptr[L]; q < S.level_ptr[L + 1]; q++) {
         const int32_t s = S.level_list[q];
-        if (S.child_ptr[s + 1] - S.child_ptr[s] > o) lists.push_back(S.child_list[S.child_ptr[s] + o]);
+        if (S.child_ptr[s + 1] - S.child_ptr[s] > o) {
+          const int32_t c = S.child_list[S.child_ptr[s] + o];
+          lists.push_back(c);
+          umax = std::max<int64_t>(umax, S.m(c) - S.k(c));
+        }
       }
       lv.ea_cnt.push_back((int64_t)lists.size() - lv.ea_off.back());
+      // about 32 update columns per block, 16 .. 1024 blocks per child
+      lv.ea_gy.push_back((uint32_t)std::min<int64_t>(1024, std::max<int64_t>(16, (umax + 31) / 32)));
     }
   }
   if (lists.size() >= (size_t)INT32_MAX || max_large_cnt > 65535) {
