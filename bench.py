@@ -503,7 +503,7 @@ def run_ours(args):
     ldlt_leg = None
     if not args.no_solver and rank == 0:
         # the consumer of the assembled K(2): its device LDL^T on the 139k-equation bar
-        ldlt_leg = solver_bench(20)
+        ldlt_leg = solver_bench(20, ("fp32-tc", "fp32", "fp64"))
 
     if rank != 0:
         return

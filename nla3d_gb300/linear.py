@@ -24,9 +24,13 @@ with U'_c = U_c, as the reference writes them (FESolver.cpp:604-625).
 The backend is the GPU FEStorage (nla3d_gb300.storage) or the CPU oracle
 model: eq_numbers(), pattern(b), K(b), C(b), M(b), F(), set_U(U), update(),
 assemble(), block_mv(...), n_con / n_unk / n_mpc / n_total, blocks.  The
-K(1,2) and K(1) products go through block_mv (matBVprod / matBTVprod); the
-sparse solves and the C / M products run on the host (SciPy), standing in for
-the reference's EquationSolver.
+K(1,2) and K(1) products go through block_mv (matBVprod / matBTVprod).  The
+linear solve of K(2) runs on the host (SciPy, standing in for the reference's
+EquationSolver) or, with solver="gpu" / "gpu-fp32", through the device LDL^T
+(nla3d_ldlt_*) on the K(2) values the assembly left in HBM.  The transient
+driver factors Kmod by SciPy or, with the same options, by the device LDL^T
+(Kmod's values uploaded on K(2)'s pattern); its C / M products run on the
+host.
 """
 from __future__ import annotations
 
@@ -73,12 +77,41 @@ class _Driver:
         rows2, cols2, _ = self.b.blocks[2]
         return csr_full(*self.b.pattern(2), values, rows2, cols2, True)
 
+    def _device_ldlt(self):
+        """The device LDL^T on K(2)'s pattern: nested dissection of the rows'
+        points, MPC equations after the DoFs (saddle_order)."""
+        from .ldlt import DeviceLDLT, saddle_order
+        from .newton import nested_dissection, row_points
+        io, co = self.b.pattern(2)
+        pts = row_points(self.b, self.nc, self.nu, self.nm)
+        order = nested_dissection(self._block2(np.ones(co.size)), pts)
+        return DeviceLDLT.for_storage(self.b, saddle_order(io, co, order, self.nu),
+                                      "fp64" if self.solver == "gpu" else "fp32")
+
     def node_solution(self, node, dof):
         """FEStorage::getNodeDofSolution: vecU at the DoF's equation."""
         return float(self.U[int(self.ne[node - 1, dof]) - 1])
 
 
 class LinearFESolver(_Driver):
+    def __init__(self, backend, fixes=(), loads=(), solver="host"):
+        """solver: "host" (SciPy sparse LU) or "gpu" / "gpu-fp32" (the
+        library's LDL^T of the device K(2), with a geometric nested-dissection
+        order; GPU FEStorage backends only)."""
+        super().__init__(backend, fixes, loads)
+        if solver not in ("host", "gpu", "gpu-fp32"):
+            raise ValueError(solver)
+        self.solver = solver
+
+    def _solve_K2(self, rhs):
+        if self.solver == "host":
+            return spla.spsolve(self._block2(self.b.K(2)).tocsc(), rhs)
+        ldlt = self._device_ldlt()
+        ldlt.factor(self.b)
+        x = ldlt.solve_host(self.b, rhs, max_refine=50, tol=1e-12)
+        ldlt.close()
+        return x
+
     def solve(self):
         self.R[:] = 0.0
         self.b.set_U(self.U)
@@ -90,7 +123,7 @@ class LinearFESolver(_Driver):
         rhs = F[nc:] + self.R[nc:]
         if nc:
             rhs = self.b.block_mv(12, 1, Uc, -1.0, rhs)
-        self.U[nc:] = spla.spsolve(self._block2(self.b.K(2)).tocsc(), rhs)
+        self.U[nc:] = self._solve_K2(rhs)
         Rc = np.zeros(nc)
         if nc:
             Rc = self.b.block_mv(1, 0, Uc, 1.0, Rc)
@@ -109,6 +142,15 @@ class LinearTransientFESolver(_Driver):
     initValue = 0.0
     alpha = 0.25     # trapezoidal rule
     delta = 0.5
+
+    def __init__(self, backend, fixes=(), loads=(), solver="host"):
+        """solver: "host" (SciPy sparse LU of Kmod) or "gpu" / "gpu-fp32"
+        (Kmod's values, on K(2)'s pattern, factored once by the device LDL^T
+        and every step solved on the device with FP64 refinement)."""
+        super().__init__(backend, fixes, loads)
+        if solver not in ("host", "gpu", "gpu-fp32"):
+            raise ValueError(solver)
+        self.solver = solver
 
     def solve(self, probes=()):
         """Runs the time steps; returns (times, U at the probes per step) for
@@ -137,7 +179,25 @@ class LinearTransientFESolver(_Driver):
         self._apply_bc(1.0)
         F = self.b.F()
         K2, C2, M2 = self.b.K(2), self.b.C(2), self.b.M(2)
-        lu = spla.splu(self._block2(a0 * M2 + a1 * C2 + K2).tocsc(), permc_spec="COLAMD")
+        kmod = a0 * M2 + a1 * C2 + K2
+        if self.solver == "host":
+            lu = spla.splu(self._block2(kmod).tocsc(), permc_spec="COLAMD")
+            solve = lu.solve
+        else:
+            import torch
+            ldlt = self._device_ldlt()
+            kmod_d = torch.from_numpy(np.ascontiguousarray(kmod)).cuda()
+            b_d = torch.empty(self.nu + self.nm, dtype=torch.float64, device="cuda")
+            x_d = torch.empty_like(b_d)
+            torch.cuda.synchronize()
+            ldlt.factor_device(kmod_d.data_ptr())
+
+            def solve(rhs):
+                b_d.copy_(torch.from_numpy(rhs))
+                torch.cuda.synchronize()
+                ldlt.solve_device(kmod_d.data_ptr(), b_d.data_ptr(), x_d.data_ptr(),
+                                  max_refine=50, tol=1e-12)
+                return x_d.cpu().numpy()
         Cs, Ms = self._block2(C2), self._block2(M2)
         times, values = [], []
         t = self.time0 + dt
@@ -147,7 +207,7 @@ class LinearTransientFESolver(_Driver):
             rhs = rhs + Cs @ (a1 * self.U[nc:] + a4 * dU[nc:] + a5 * ddU[nc:])
             Un = np.empty(self.n)
             Un[:nc] = self.U[:nc]
-            Un[nc:] = lu.solve(rhs)
+            Un[nc:] = solve(rhs)
             ddUn = a0 * (Un - self.U) - a2 * dU - a3 * ddU
             dUn = dU + a6 * ddUn + a7 * ddU
             self.U, dU, ddU = Un, dUn, ddUn
@@ -157,4 +217,6 @@ class LinearTransientFESolver(_Driver):
             values.append([self.node_solution(n, d) for n, d in probes])
             t += dt
         self.dU, self.ddU = dU, ddU
+        if self.solver != "host":
+            ldlt.close()
         return np.array(times), np.array(values)

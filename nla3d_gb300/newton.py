@@ -73,6 +73,32 @@ class StepRecord:
     plain_residual: float | None = None
 
 
+def row_points(backend, nc, n_unk, n_mpc):
+    """A point per K(2) row, for nested_dissection: the node of a nodal DoF,
+    the element centroid of an element DoF, the first term's node of an MPC
+    equation."""
+    mesh = backend.mesh
+    xyz = np.asarray(mesh.xyz, dtype=np.float64)
+    conn = np.asarray(mesh.conn, dtype=np.int64)
+    ne, ee = backend.eq_numbers()
+    pts = np.zeros((n_unk + n_mpc, 3))
+    for d in range(ne.shape[1]):
+        eq = ne[:, d].astype(np.int64)
+        sel = eq > nc
+        pts[eq[sel] - nc - 1] = xyz[sel]
+    cen = xyz[conn - 1].mean(axis=1)
+    for d in range(ee.shape[1]):
+        eq = ee[:, d].astype(np.int64)
+        sel = eq > nc
+        pts[eq[sel] - nc - 1] = cen[sel]
+    first = [int(q.nodes[0]) for q in mesh.mpcs]
+    for rb in mesh.rigid_bodies:
+        first += [int(n) for n in rb.slaves for _ in rb.dofs]
+    for k, n in enumerate(first):
+        pts[n_unk + k] = xyz[n - 1]
+    return pts
+
+
 def nested_dissection(K, pts, leaf=64):
     """Fill-reducing order of a symmetric sparse pattern with a point per row:
     split the rows at the median of their longest coordinate extent; the rows
@@ -166,28 +192,7 @@ class NewtonSolver:
         return csr_full(*self.patterns[2], self.b.K(2), rows2, cols2, True)
 
     def _row_points(self):
-        """A point per K(2) row: the node of a nodal DoF, the element centroid
-        of an element DoF, the first term's node of an MPC equation."""
-        mesh = self.b.mesh
-        xyz = np.asarray(mesh.xyz, dtype=np.float64)
-        conn = np.asarray(mesh.conn, dtype=np.int64)
-        ne, ee = self.b.eq_numbers()
-        pts = np.zeros((self.nu + self.nm, 3))
-        for d in range(ne.shape[1]):
-            eq = ne[:, d].astype(np.int64)
-            sel = eq > self.nc
-            pts[eq[sel] - self.nc - 1] = xyz[sel]
-        cen = xyz[conn - 1].mean(axis=1)
-        for d in range(ee.shape[1]):
-            eq = ee[:, d].astype(np.int64)
-            sel = eq > self.nc
-            pts[eq[sel] - self.nc - 1] = cen[sel]
-        first = [int(q.nodes[0]) for q in mesh.mpcs]
-        for rb in mesh.rigid_bodies:
-            first += [int(n) for n in rb.slaves for _ in rb.dofs]
-        for k, n in enumerate(first):
-            pts[self.nu + k] = xyz[n - 1]
-        return pts
+        return row_points(self.b, self.nc, self.nu, self.nm)
 
     def _solve_gpu(self, rhs):
         """The device LDL^T: a solve refined to 1e-10 is used as is; one that

@@ -11,8 +11,8 @@ from nla3d_gb300.linear import LinearFESolver
 from oracle import oracle as O
 
 
-def _solve(backend, fixes, loads):
-    s = LinearFESolver(backend, fixes=fixes, loads=loads)
+def _solve(backend, fixes, loads, solver="host"):
+    s = LinearFESolver(backend, fixes=fixes, loads=loads, solver=solver)
     s.solve()
     ne, _ = backend.eq_numbers()
     U = s.U
@@ -38,5 +38,16 @@ def test_tetra0_matches_ansys_with_gpu_assembly():
     from nla3d_gb300.storage import FEStorage
     mesh, fixes, loads, g = cases.tetra0_ansys_model()
     U, disp = _solve(FEStorage(mesh).initSolutionData(), fixes, loads)
+    assert np.abs(disp - g["ansys_disp"]).max() < 1e-10
+    assert np.abs(_stress(mesh, U) - g["ansys_stress"]).max() < 1e-3
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("solver", ["gpu", "gpu-fp32"])
+def test_tetra0_matches_ansys_with_the_device_solve(solver):
+    """The same test with K(2) factored on the device (LinearFESolver(solver=...))."""
+    from nla3d_gb300.storage import FEStorage
+    mesh, fixes, loads, g = cases.tetra0_ansys_model()
+    U, disp = _solve(FEStorage(mesh).initSolutionData(), fixes, loads, solver)
     assert np.abs(disp - g["ansys_disp"]).max() < 1e-10
     assert np.abs(_stress(mesh, U) - g["ansys_stress"]).max() < 1e-3
