@@ -80,6 +80,10 @@ struct nla3d_ctx {
   double* d_F = nullptr;
   uint32_t* d_elem_mesh = nullptr;
   double* d_mesh_mat = nullptr;
+  // mixed precision: dN/dX, w det J and the materials as float pairs
+  float2* d_Gdf = nullptr;
+  float2* d_wdf = nullptr;
+  float2* d_mesh_mat_df = nullptr;
   uint32_t* d_mpc_u32 = nullptr;  // master, slave, eq, slave_eq, master_eq6 (6), slot (5)
   int32_t* d_mpc_dof = nullptr;
   // SurfaceLINETH lines (single-mesh QUADTH contexts) and transient C / M
@@ -170,6 +174,12 @@ cudaError_t upload(nla3d_ctx* c, T** p, const T* host, uint64_t n) {
   cudaError_t e = dalloc(c, p, n);
   if (e != cudaSuccess || n == 0) return e;
   return cudaMemcpyAsync(*p, host, sizeof(T) * n, cudaMemcpyHostToDevice, c->stream);
+}
+
+// hi + lo = v to 2^-48: the mixed kernel's float-pair form of a double
+float2 split_pair(double v) {
+  const float h = (float)v;
+  return make_float2(h, (float)(v - (double)h));
 }
 
 int block_slot(int block) { return block == 1 ? 0 : (block == 2 ? 2 : (block == 12 ? 1 : -1)); }
@@ -297,6 +307,13 @@ cudaError_t enqueue_elements(nla3d_ctx* c, uint32_t e0, uint32_t e1) {
     a.contribK = c->d_contribK;
     a.contribF = c->d_contribF;
     a.status = c->d_status;
+    if (c->precision == NLA3D_PREC_MIXED) {
+      a.Gdf = c->d_Gdf;
+      a.wdf = c->d_wdf;
+      for (int i = 0; i < 5; i++) a.mcd[i] = split_pair(m0.mat_c[i]);
+      a.inv_kbd = split_pair(1.0 / a.kbulk);
+      a.mesh_mat_df = c->uniform_material ? nullptr : c->d_mesh_mat_df;
+    }
     e = launch_solid81_shaped(a, c->precision == NLA3D_PREC_MIXED, c->shape, c->stream);
   } else if (m0.etype == NLA3D_PLANE41) {
     Plane41Args a{};
@@ -732,6 +749,7 @@ int nla3d_init_solution_data(nla3d_ctx* c) {
   const uint64_t E = c->E(), N = c->Ntot(), ntot = c->Utot(), nnz = c->Ktot(), NM = c->Mtot();
   const int npe = c->hm[0].npe;
   const uint64_t n_kc = c->hm[0].n_kc, n_fc = c->hm[0].n_fc;
+  const bool mixed_solid = c->precision == NLA3D_PREC_MIXED && c->hm[0].etype == NLA3D_SOLID81;
   // contributions: the elements', then (single-mesh QUADTH) the surface lines'
   const uint64_t LN = c->hm[0].n_lines();
   const uint64_t CK_tot = E * n_kc + LN * kLineKc, CF_tot = E * n_fc + LN * kLineFc;
@@ -804,6 +822,13 @@ int nla3d_init_solution_data(nla3d_ctx* c) {
   if (!c->uniform_material) {
     CK(upload(c, &c->d_elem_mesh, elem_mesh.data(), elem_mesh.size()));
     CK(upload(c, &c->d_mesh_mat, mesh_mat.data(), mesh_mat.size()));
+  }
+  std::vector<float2> mesh_mat_df;
+  if (!c->uniform_material && mixed_solid) {
+    mesh_mat_df.resize(mesh_mat.size());
+    for (size_t i = 0; i < mesh_mat.size(); i++) mesh_mat_df[i] = split_pair(mesh_mat[i]);
+    for (size_t i = 0; i < M; i++) mesh_mat_df[8 * i + 7] = split_pair(1.0 / mesh_mat[8 * i + 6]);
+    CK(upload(c, &c->d_mesh_mat_df, mesh_mat_df.data(), mesh_mat_df.size()));
   }
   if (host_lists) {
     CK(upload(c, &c->d_kptr, kptr.data(), kptr.size()));
@@ -904,9 +929,16 @@ int nla3d_init_solution_data(nla3d_ctx* c) {
   CK(cudaMemsetAsync(c->d_status, 0, sizeof(ElementStatus), c->stream));
   CK(cudaMemsetAsync(&c->d_status->first, 0xFF, sizeof(uint32_t), c->stream));
   if (c->hm[0].etype == NLA3D_SOLID81) {
-    CK(dalloc(c, &c->d_Gt, 24 * 8 * E));
+    // FP64 contexts keep dN/dX as doubles, mixed ones as float pairs only
+    if (mixed_solid) {
+      CK(dalloc(c, &c->d_Gdf, 24 * 8 * E));
+      CK(dalloc(c, &c->d_wdf, 8 * E));
+    } else {
+      CK(dalloc(c, &c->d_Gt, 24 * 8 * E));
+    }
     CK(dalloc(c, &c->d_wdet, 8 * E));
-    JacobianArgs ja{(uint32_t)E, c->d_xyz, c->d_conn, c->d_Gt, c->d_wdet, c->d_status};
+    JacobianArgs ja{(uint32_t)E, c->d_xyz, c->d_conn, c->d_Gt, c->d_wdet, c->d_status,
+                    c->d_Gdf, c->d_wdf};
     CK(launch_solid81_jacobian(ja, c->stream));
     c->launches++;
   }

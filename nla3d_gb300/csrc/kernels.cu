@@ -24,6 +24,7 @@
 // 1e-12 relative).
 #include <cmath>
 #include <cstdio>
+#include <type_traits>
 
 #include "kernels.cuh"
 
@@ -40,13 +41,36 @@ constexpr double kGaussA = 0.5773502691896258;        // isoparametric.h:127
 // Kuu entry t (assemble3 order, SOLID81.h:62-74) -> (a, i, b, k) packed.
 __constant__ uchar4 c_kuu_entry[kKuuPerElem];
 
+// -w F S: FP64, or a float pair (hi, lo) in the mixed kernel
+template <typename TT>
+struct ResidualType {
+  using type = double;
+};
+template <>
+struct ResidualType<float> {
+  using type = float2;
+};
+
+// Stride of one (i, k) block of h in the warp scratch.  In the mixed kernel
+// a warp's Kuu loads read h at up to six (i, k) blocks with the same slot a;
+// a stride of 97 floats puts them in different banks (96 made them a 3-way
+// bank conflict that bounded the kernel).  The FP64 kernel keeps 96.
+template <typename TT>
+struct HStride {
+  static constexpr int value = 96;
+};
+template <>
+struct HStride<float> {
+  static constexpr int value = 97;
+};
+
 template <typename TT>
 struct WarpSmem {
-  double wP[9][32];    // per (element q, Gauss point g): -w F S
-  double wCof[9][32];  //  w cof(F)
+  typename ResidualType<TT>::type wP[9][32];  // per (element q, Gauss point g): -w F S
+  TT wCof[9][32];      //  w cof(F)
   TT A[45][32];        //  symmetric 9x9 tangent tensor A[iL][kN], packed upper
-  TT H[27][32];        // per (element q, node a) at the current Gauss point:
-                       //  h_a[ik][N] = sum_L G_aL A[iL][kN], index (3i+k)*3+N
+  TT H[9 * HStride<TT>::value];  // per (element q, node a) at the current Gauss point:
+                       //  h_a[ik][N] at (3i+k) * HStride + 32 N + slot
   TT G[3][32];         //  G_a
 };
 
@@ -69,6 +93,12 @@ __device__ __forceinline__ void flag_element(ElementStatus* st, uint32_t el1) {
   atomicAdd(&st->count, 1u);
   atomicMin(&st->first, el1);
 }
+
+template <typename TT>
+__device__ __forceinline__ void tangent_from_coefficients(const TT At[6], const TT Bt[6],
+                                                          const TT Ct[6], TT wk11, TT wk1,
+                                                          TT wk2, TT wc0, TT sIIt, TT sI,
+                                                          TT wD[21]);
 
 // Material response at one Gauss point (materials_hyperelastic.cpp:30-129).
 // Inputs: C (Voigt), p_state (for S), p_cur (for Dd).  Outputs: S, J and the
@@ -134,12 +164,28 @@ __device__ __forceinline__ void material(int mat_id, const double* mc, const dou
   const TT sI = (TT)(w * 1.5 * k2);
   // scalar coefficients in FP64, the 6-vectors P, Q, R in the tangent type
   const TT wk11 = (TT)(w * k11), wk1 = (TT)(w * k1), wk2 = (TT)(w * k2), wc0 = (TT)(w * c0);
-  TT P[6], Q[6], R[6], At[6], Bt[6], Ct[6];
+  TT At[6], Bt[6], Ct[6];
 #pragma unroll
   for (int i = 0; i < 6; i++) {
     At[i] = (TT)A[i];
     Bt[i] = (TT)B[i];
     Ct[i] = (TT)Ci[i];
+  }
+  tangent_from_coefficients<TT>(At, Bt, Ct, wk11, wk1, wk2, wc0, sIIt, sI, wD);
+}
+
+// w * 2 Dd, packed upper Voigt, from the coefficient form
+//   A (x) P + B (x) Q + Ci (x) R + sIIt * IIt + sI * (I (x) I - II)
+// with P = wk11 A - wk1 Ci, Q = -wk2 Ci, R = -wk1 A - wk2 B + wc0 Ci
+// (materials_hyperelastic.cpp:64-129 with the reference's /2 taken out).
+template <typename TT>
+__device__ __forceinline__ void tangent_from_coefficients(const TT At[6], const TT Bt[6],
+                                                          const TT Ct[6], TT wk11, TT wk1,
+                                                          TT wk2, TT wc0, TT sIIt, TT sI,
+                                                          TT wD[21]) {
+  TT P[6], Q[6], R[6];
+#pragma unroll
+  for (int i = 0; i < 6; i++) {
     P[i] = wk11 * At[i] - wk1 * Ct[i];
     Q[i] = -wk2 * Ct[i];
     R[i] = -wk1 * At[i] - wk2 * Bt[i] + wc0 * Ct[i];
@@ -169,7 +215,253 @@ __device__ __forceinline__ void material(int mat_id, const double* mc, const dou
       if (minus) v -= h * sI;
       wD[idx] = v;
     }
-  (void)B;
+}
+
+// ---------------------------------------------------------------------------
+// Float-pair ("double-word") arithmetic for the mixed path's residual.
+//
+// On this part the FP64 pipe runs at 1/64 of the FP32 rate, so the mixed
+// kernel computes the residual chain (displacement gradient, C, the
+// material's S and J, -w F S G_a, the pressure terms) with pairs of floats
+// x = h + l, |l| <= ulp(h) / 2, instead of doubles.  The building blocks are
+// the error-free transformations TwoSum (Knuth) and TwoProd by FMA, and the
+// compensated dot product Dot2 (Ogita, Rump, Oishi, "Accurate sum and dot
+// product", SIAM J. Sci. Comput. 26, 2005); the pair operations follow the
+// double-word algorithms analysed by Joldes, Muller and Popescu ("Tight and
+// rigorous error bounds for basic building blocks of double-word
+// arithmetic", ACM TOMS 44, 2017).  Each operation's error is a few units of
+// 2^-48 relative to its operands, so the residual agrees with the FP64 path
+// to ~1e-14 relative (the tests bound it at 1e-12).  The float exponent range
+// applies: the mixed path needs |values| well inside 1e-30 .. 1e30.
+// The intrinsics (__fadd_rn, __fmul_rn, __fmaf_rn) keep the compiler from
+// contracting the transformations' separate roundings into FMAs.
+struct dw {
+  float h, l;
+};
+
+__device__ __forceinline__ dw two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return {s, e};
+}
+
+__device__ __forceinline__ dw fast_two_sum(float a, float b) {  // |a| >= |b| (or a == 0)
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+__device__ __forceinline__ dw two_prod(float a, float b) {
+  const float p = __fmul_rn(a, b);
+  return {p, __fmaf_rn(a, b, -p)};
+}
+
+__device__ __forceinline__ dw dw_neg(dw x) { return {-x.h, -x.l}; }
+__device__ __forceinline__ dw dw_scale2(dw x, float p2) {  // p2 a power of two: exact
+  return {x.h * p2, x.l * p2};
+}
+
+// x + y with error ~2^-47 (|x| + |y|)
+__device__ __forceinline__ dw dw_add(dw x, dw y) {
+  const dw s = two_sum(x.h, y.h);
+  return fast_two_sum(s.h, __fadd_rn(s.l, __fadd_rn(x.l, y.l)));
+}
+
+__device__ __forceinline__ dw dw_addf(dw x, float y) {
+  const dw s = two_sum(x.h, y);
+  return fast_two_sum(s.h, __fadd_rn(s.l, x.l));
+}
+
+__device__ __forceinline__ dw dw_mul(dw x, dw y) {
+  const dw p = two_prod(x.h, y.h);
+  return fast_two_sum(p.h, __fmaf_rn(x.h, y.l, __fmaf_rn(x.l, y.h, p.l)));
+}
+
+__device__ __forceinline__ dw dw_mulf(dw x, float y) {
+  const dw p = two_prod(x.h, y);
+  return fast_two_sum(p.h, __fmaf_rn(x.l, y, p.l));
+}
+
+// Dot2 accumulator: value s + c, c collects the rounding errors unnormalised
+struct dacc {
+  float s, c;
+};
+
+__device__ __forceinline__ void acc_prod(dacc& a, dw x, dw y) {
+  const dw p = two_prod(x.h, y.h);
+  const float e = __fmaf_rn(x.h, y.l, __fmaf_rn(x.l, y.h, p.l));
+  const dw t = two_sum(a.s, p.h);
+  a.s = t.h;
+  a.c = __fadd_rn(a.c, __fadd_rn(t.l, e));
+}
+
+__device__ __forceinline__ void acc_add(dacc& a, dw x) {
+  const dw t = two_sum(a.s, x.h);
+  a.s = t.h;
+  a.c = __fadd_rn(a.c, __fadd_rn(t.l, x.l));
+}
+
+__device__ __forceinline__ dw acc_val(dacc a) { return two_sum(a.s, a.c); }
+
+__device__ __forceinline__ dw dw_of(float2 v) { return {v.x, v.y}; }
+
+__device__ __forceinline__ dw dw_from_double(double v) {
+  const float h = __double2float_rn(v);
+  return {h, __double2float_rn(v - (double)h)};
+}
+
+__device__ __forceinline__ double dw_to_double(dw x) { return (double)x.h + (double)x.l; }
+
+// sqrt(d): the float root refined by one Newton step on the pair
+__device__ __forceinline__ dw dw_sqrt(dw d) {
+  const float y = __fsqrt_rn(d.h);
+  const dw yy = two_prod(y, y);
+  const float r = __fadd_rn(__fsub_rn(__fsub_rn(d.h, yy.h), yy.l), d.l);  // d - y^2
+  return fast_two_sum(y, __fdiv_rn(r, 2.0f * y));
+}
+
+// 1 / d: the float reciprocal refined by one Newton step
+__device__ __forceinline__ dw dw_rcp(dw d) {
+  const float y = __frcp_rn(d.h);
+  const dw p = two_prod(d.h, y);
+  const float r = __fsub_rn(__fsub_rn(1.0f, p.h), __fmaf_rn(d.l, y, p.l));  // 1 - d y
+  return fast_two_sum(y, __fmul_rn(y, r));
+}
+
+// x^(-1/3): the float estimate refined by Newton steps on f(x) = x^-3 - J,
+//   x' = x + x (1 - J x^3) / 3,   relative error e -> 2 e^2,
+// two steps, since one leaves 2 (2^-23)^2 ~ 3e-14 from a 1-ulp estimate.
+__device__ __forceinline__ dw dw_rcbrt(dw J) {
+  const float x0 = rcbrtf(J.h);
+  const dw t0 = dw_mul(J, dw_mulf(two_prod(x0, x0), x0));
+  const float u0 = __fsub_rn(__fsub_rn(1.0f, t0.h), t0.l);  // 1 - J x^3 (t.h ~ 1: exact)
+  const dw x1 = fast_two_sum(x0, __fmul_rn(x0, __fmul_rn(u0, 1.0f / 3.0f)));
+  const dw t1 = dw_mul(J, dw_mul(dw_mul(x1, x1), x1));
+  const float u1 = __fsub_rn(__fsub_rn(1.0f, t1.h), t1.l);
+  return dw_add(x1, dw_mulf(x1, __fmul_rn(u1, 1.0f / 3.0f)));
+}
+
+// constants as pairs (the low parts folded at compile time)
+#define NLA3D_DW_CONST(name, value) \
+  constexpr float name##_h = (float)(value); \
+  constexpr float name##_l = (float)((value) - (double)name##_h);
+NLA3D_DW_CONST(kThird, 1.0 / 3.0)
+NLA3D_DW_CONST(kTwoThirds, 2.0 / 3.0)
+NLA3D_DW_CONST(kFourThirds, 4.0 / 3.0)
+NLA3D_DW_CONST(kEightThirds, 8.0 / 3.0)
+#undef NLA3D_DW_CONST
+
+// a b - c d
+__device__ __forceinline__ dw dw_diff_prod(dw a, dw b, dw c, dw d) {
+  dacc t{0.0f, 0.0f};
+  acc_prod(t, a, b);
+  acc_prod(t, dw_neg(c), d);
+  return acc_val(t);
+}
+
+// The material response of material<TT> with the state (S, J) in pairs and
+// the tangent coefficients rounded to float (materials_hyperelastic.cpp:30-129,
+// 135-204).
+__device__ __forceinline__ void material_mixed(int mat_id, const float2* mcd, const dw C[6],
+                                               dw p_state, dw p_cur, dw w, dw S[6], dw& Jout,
+                                               float wD[21]) {
+  const dw I1 = dw_add(dw_add(C[0], C[3]), C[5]);
+  dacc t2{0.0f, 0.0f};
+  acc_prod(t2, C[0], C[3]);
+  acc_prod(t2, C[3], C[5]);
+  acc_prod(t2, C[0], C[5]);
+  acc_prod(t2, dw_neg(C[1]), C[1]);
+  acc_prod(t2, dw_neg(C[4]), C[4]);
+  acc_prod(t2, dw_neg(C[2]), C[2]);
+  const dw I2 = acc_val(t2);
+  // cofactors of the symmetric C: Ci = cof / det C
+  dw cf[6];
+  cf[0] = dw_diff_prod(C[3], C[5], C[4], C[4]);
+  cf[1] = dw_diff_prod(C[2], C[4], C[1], C[5]);
+  cf[2] = dw_diff_prod(C[1], C[4], C[2], C[3]);
+  cf[3] = dw_diff_prod(C[0], C[5], C[2], C[2]);
+  cf[4] = dw_diff_prod(C[1], C[2], C[0], C[4]);
+  cf[5] = dw_diff_prod(C[0], C[3], C[1], C[1]);
+  dacc td{0.0f, 0.0f};
+  acc_prod(td, C[0], cf[0]);
+  acc_prod(td, C[1], cf[1]);
+  acc_prod(td, C[2], cf[2]);
+  const dw detC = acc_val(td);
+  const dw J = dw_sqrt(detC);
+  const dw rc = dw_rcbrt(J);
+  const dw pp = dw_mul(rc, rc);      // J^(-2/3)
+  const dw pppp = dw_mul(pp, pp);    // J^(-4/3)
+  const dw oo = dw_rcp(detC);        // 1 / J^2
+  dw Ci[6];
+#pragma unroll
+  for (int i = 0; i < 6; i++) Ci[i] = dw_mul(oo, cf[i]);
+  const dw t13 = dw_mul(I1, dw{kThird_h, kThird_l});
+  const dw t23 = dw_mul(I2, dw{kTwoThirds_h, kTwoThirds_l});
+  dw a1, a2{0.0f, 0.0f}, a11{0.0f, 0.0f};
+  if (mat_id == 1) {
+    a1 = dw_scale2(dw_of(mcd[0]), 0.5f);
+  } else if (mat_id == 2) {
+    const dw d = dw_addf(dw_mul(I1, pp), -3.0f);
+    const dw m1 = dw_of(mcd[1]), m2 = dw_of(mcd[2]);
+    dacc ta{0.0f, 0.0f};
+    acc_add(ta, dw_of(mcd[0]));
+    acc_prod(ta, dw_scale2(m1, 2.0f), d);
+    acc_prod(ta, dw_mulf(m2, 3.0f), dw_mul(d, d));
+    a1 = acc_val(ta);
+    a2 = dw_of(mcd[3]);
+    a11 = dw_add(dw_scale2(m1, 2.0f), dw_mul(dw_mulf(m2, 6.0f), d));
+  } else {
+    a1 = dw_of(mcd[0]);
+    a2 = dw_of(mcd[1]);
+  }
+  const float I6[6] = {1.0f, 0.0f, 0.0f, 1.0f, 0.0f, 1.0f};
+  dw A[6], B[6];
+#pragma unroll
+  for (int i = 0; i < 6; i++) {
+    A[i] = dw_addf(dw_neg(dw_mul(t13, Ci[i])), I6[i]);
+    dacc tb{0.0f, 0.0f};
+    acc_add(tb, dw_neg(C[i]));
+    acc_prod(tb, dw_neg(t23), Ci[i]);
+    if (I6[i] != 0.0f) acc_add(tb, I1);
+    B[i] = acc_val(tb);
+  }
+  const dw ko1 = dw_scale2(dw_mul(a1, pp), 2.0f), ko2 = dw_scale2(dw_mul(a2, pppp), 2.0f);
+  const dw pJs = dw_mul(p_state, J);
+#pragma unroll
+  for (int i = 0; i < 6; i++) {
+    dacc ts{0.0f, 0.0f};
+    acc_prod(ts, ko1, A[i]);
+    acc_prod(ts, ko2, B[i]);
+    acc_prod(ts, pJs, Ci[i]);
+    S[i] = acc_val(ts);
+  }
+  Jout = J;
+  // tangent coefficients (Dd before the reference's /2, times w), in float
+  const dw k11 = dw_scale2(dw_mul(a11, pppp), 4.0f);
+  const dw k1 = dw_mul(dw_mul(a1, pp), dw{kFourThirds_h, kFourThirds_l});
+  const dw k2 = dw_mul(dw_mul(a2, pppp), dw{kEightThirds_h, kEightThirds_l});
+  const dw pj = dw_mul(p_cur, J);
+  dacc tc0{0.0f, 0.0f};
+  acc_add(tc0, pj);
+  acc_prod(tc0, dw_neg(k1), t13);
+  acc_prod(tc0, dw_neg(k2), t23);
+  const dw c0 = acc_val(tc0);
+  dacc tst{0.0f, 0.0f};
+  acc_add(tst, dw_scale2(pj, 2.0f));
+  acc_prod(tst, dw_neg(k1), I1);
+  acc_prod(tst, dw_neg(k2), I2);
+  const float wf = w.h;
+  const float sIIt = wf * acc_val(tst).h;
+  const float sI = wf * 1.5f * k2.h;
+  float At[6], Bt[6], Ct[6];
+#pragma unroll
+  for (int i = 0; i < 6; i++) {
+    At[i] = A[i].h;
+    Bt[i] = B[i].h;
+    Ct[i] = Ci[i].h;
+  }
+  tangent_from_coefficients<float>(At, Bt, Ct, wf * k11.h, wf * k1.h, wf * k2.h, wf * c0.h, sIIt,
+                                   sI, wD);
 }
 
 template <typename TT, int WPB>
@@ -192,7 +484,7 @@ __global__ void __launch_bounds__(WPB * 32)
     if (x < kEPW * kKuuPerElem) {
       const int q = x / kKuuPerElem, t = x - q * kKuuPerElem;
       const uchar4 en = c_kuu_entry[t];  // (a, i, b, k)
-      const uint32_t ho = (en.y * 3 + en.w) * 3 * 32 + q * 8 + en.x;
+      const uint32_t ho = (en.y * 3 + en.w) * HStride<TT>::value + q * 8 + en.x;
       const uint32_t go = q * 8 + en.z;
       word = ho | (go << 16);
     }
@@ -215,92 +507,210 @@ __global__ void __launch_bounds__(WPB * 32)
     const uint32_t ec = valid ? e : E - 1;
 
     // ---------------- phase 1: lane = (element q, Gauss point g) ----------------
-    double Fp_part, Kpp_part;
+    constexpr bool kMixed = std::is_same<TT, float>::value;
+    double Fp_part = 0.0, Kpp_part = 0.0;  // FP64 kernel
+    dw Fp_dw{0.0f, 0.0f}, Kpp_dw{0.0f, 0.0f};  // mixed kernel
     {
       const int g = sub;
       const uint64_t tg = (uint64_t)ec * 8 + g;
-      const double w = a.wdet[tg];
-      const double pc = a.U_cur[a.p_eq[ec] - 1];
-      double O[9];
-      double C[6];
-      double ps = 0.0;
-      if (a.have_state) {
-        double G[24];
+      TT Fm[9], wS[6], wD[21];
+      bool bad;
+      if constexpr (kMixed) {
+        // the residual chain in float pairs, the tangent inputs rounded to float
+        const dw w = dw_of(__ldg(a.wdf + tg));
+        const dw pc = dw_from_double(a.U_cur[a.p_eq[ec] - 1]);
+        dw O[9];
+        dw C[6];
+        dw ps{0.0f, 0.0f};
+        if (a.have_state) {
+          // O = sum_n (u_n - u_0) G_n (the shape gradients sum to zero): the
+          // displacements relative to the element's node 0 are formed in FP64,
+          // so the pairs carry the small differences, not |u| (which can be
+          // ~1/h times larger, and would cost that factor in accuracy).
+          // Lane (q, g) forms node g's difference; the others read it by shuffle.
+          const uint32_t* cn = a.conn + (uint64_t)ec * 8;
+          const uint4 eq0 = __ldg(reinterpret_cast<const uint4*>(a.node_eq3) + (__ldg(cn) - 1));
+          const uint4 eqg = __ldg(reinterpret_cast<const uint4*>(a.node_eq3) + (__ldg(cn + g) - 1));
+          const dw dx = dw_from_double(a.U_state[eqg.x - 1] - a.U_state[eq0.x - 1]);
+          const dw dy = dw_from_double(a.U_state[eqg.y - 1] - a.U_state[eq0.y - 1]);
+          const dw dz = dw_from_double(a.U_state[eqg.z - 1] - a.U_state[eq0.z - 1]);
+          dw G[24];
 #pragma unroll
-        for (int c = 0; c < 24; c++) G[c] = __ldg(a.Gt + c * E8 + tg);
+          for (int c = 0; c < 24; c++) G[c] = dw_of(__ldg(a.Gdf + c * E8 + tg));
+          dacc Oa[9];
 #pragma unroll
-        for (int c = 0; c < 9; c++) O[c] = 0.0;
+          for (int c = 0; c < 9; c++) Oa[c] = dacc{0.0f, 0.0f};
+          const int base = lane & ~7;
 #pragma unroll
-        for (int n = 0; n < 8; n++) {
-          const uint32_t nid = __ldg(a.conn + (uint64_t)ec * 8 + n);
-          const uint4 eq = __ldg(reinterpret_cast<const uint4*>(a.node_eq3) + (nid - 1));
-          const double ux = a.U_state[eq.x - 1], uy = a.U_state[eq.y - 1],
-                       uz = a.U_state[eq.z - 1];
+          for (int n = 1; n < 8; n++) {
+            const dw ux{__shfl_sync(0xFFFFFFFFu, dx.h, base + n), __shfl_sync(0xFFFFFFFFu, dx.l, base + n)};
+            const dw uy{__shfl_sync(0xFFFFFFFFu, dy.h, base + n), __shfl_sync(0xFFFFFFFFu, dy.l, base + n)};
+            const dw uz{__shfl_sync(0xFFFFFFFFu, dz.h, base + n), __shfl_sync(0xFFFFFFFFu, dz.l, base + n)};
 #pragma unroll
-          for (int j = 0; j < 3; j++) {
-            O[0 + j] = fma(ux, G[3 * n + j], O[0 + j]);
-            O[3 + j] = fma(uy, G[3 * n + j], O[3 + j]);
-            O[6 + j] = fma(uz, G[3 * n + j], O[6 + j]);
+            for (int j = 0; j < 3; j++) {
+              acc_prod(Oa[0 + j], ux, G[3 * n + j]);
+              acc_prod(Oa[3 + j], uy, G[3 * n + j]);
+              acc_prod(Oa[6 + j], uz, G[3 * n + j]);
+            }
           }
+#pragma unroll
+          for (int c = 0; c < 9; c++) O[c] = acc_val(Oa[c]);
+          ps = dw_from_double(a.U_state[a.p_eq[ec] - 1]);
+          // C = F^T F = I + O + O^T + O^T O (SOLID81.cpp:105-110)
+          const int dg[3] = {0, 4, 8};
+          const int cj[6] = {0, 0, 0, 1, 1, 2}, cl[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+          for (int v = 0; v < 6; v++) {
+            const int J = cj[v], L = cl[v];
+            dacc t{J == L ? 1.0f : 0.0f, 0.0f};
+            if (J == L) {
+              acc_add(t, dw_scale2(O[dg[J]], 2.0f));
+            } else {
+              acc_add(t, O[3 * J + L]);
+              acc_add(t, O[3 * L + J]);
+            }
+#pragma unroll
+            for (int i = 0; i < 3; i++) acc_prod(t, O[3 * i + J], O[3 * i + L]);
+            C[v] = acc_val(t);
+          }
+        } else {
+#pragma unroll
+          for (int c = 0; c < 9; c++) O[c] = dw{0.0f, 0.0f};
+          C[0] = C[3] = C[5] = dw{1.0f, 0.0f};
+          C[1] = C[2] = C[4] = dw{0.0f, 0.0f};
         }
-        ps = a.U_state[a.p_eq[ec] - 1];
-        // C = F^T F from O (SOLID81.cpp:105-110)
-        C[0] = 1.0 + 2 * O[0] + O[0] * O[0] + O[3] * O[3] + O[6] * O[6];
-        C[3] = 1.0 + 2 * O[4] + O[1] * O[1] + O[4] * O[4] + O[7] * O[7];
-        C[5] = 1.0 + 2 * O[8] + O[2] * O[2] + O[5] * O[5] + O[8] * O[8];
-        C[1] = O[1] + O[3] + O[0] * O[1] + O[3] * O[4] + O[6] * O[7];
-        C[4] = O[5] + O[7] + O[1] * O[2] + O[4] * O[5] + O[7] * O[8];
-        C[2] = O[2] + O[6] + O[0] * O[2] + O[3] * O[5] + O[6] * O[8];
+        int mat_id = a.mat_id;
+        const float2* mcd = a.mcd;
+        dw inv_kb = dw_of(a.inv_kbd);
+        if (a.elem_mesh) {
+          const uint32_t mi = __ldg(a.elem_mesh + ec);
+          mat_id = (int)a.mesh_mat[8 * (uint64_t)mi];
+          mcd = a.mesh_mat_df + 8 * (uint64_t)mi + 1;
+          inv_kb = dw_of(a.mesh_mat_df[8 * (uint64_t)mi + 7]);
+        }
+        dw S[6], J;
+        material_mixed(mat_id, mcd, C, ps, pc, w, S, J, wD);
+        if (!a.have_state) {
+#pragma unroll
+          for (int i = 0; i < 6; i++) S[i] = dw{0.0f, 0.0f};
+        }
+        dw F[9];
+#pragma unroll
+        for (int c = 0; c < 9; c++) F[c] = (c == 0 || c == 4 || c == 8) ? dw_addf(O[c], 1.0f) : O[c];
+        const int sv[9] = {0, 1, 2, 1, 3, 4, 2, 4, 5};
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+          for (int k = 0; k < 3; k++) {
+            dacc t{0.0f, 0.0f};
+#pragma unroll
+            for (int J2 = 0; J2 < 3; J2++) acc_prod(t, F[3 * i + J2], S[sv[3 * J2 + k]]);
+            const dw wp = dw_mul(w, acc_val(t));
+            sm->wP[3 * i + k][lane] = make_float2(-wp.h, -wp.l);
+          }
+#pragma unroll
+        for (int c = 0; c < 9; c++) Fm[c] = F[c].h;
+        const float cof[9] = {Fm[4] * Fm[8] - Fm[5] * Fm[7], Fm[5] * Fm[6] - Fm[3] * Fm[8],
+                              Fm[3] * Fm[7] - Fm[4] * Fm[6], Fm[2] * Fm[7] - Fm[1] * Fm[8],
+                              Fm[0] * Fm[8] - Fm[2] * Fm[6], Fm[1] * Fm[6] - Fm[0] * Fm[7],
+                              Fm[1] * Fm[5] - Fm[2] * Fm[4], Fm[2] * Fm[3] - Fm[0] * Fm[5],
+                              Fm[0] * Fm[4] - Fm[1] * Fm[3]};
+#pragma unroll
+        for (int c = 0; c < 9; c++) sm->wCof[c][lane] = w.h * cof[c];
+#pragma unroll
+        for (int c = 0; c < 6; c++) wS[c] = w.h * S[c].h;
+        // Fp = -(J - 1 - p / K) w, Kpp = -w / K
+        Fp_dw = dw_neg(dw_mul(dw_add(dw_addf(J, -1.0f), dw_neg(dw_mul(pc, inv_kb))), w));
+        Kpp_dw = dw_neg(dw_mul(inv_kb, w));
+        const float detF = Fm[0] * cof[0] + Fm[1] * cof[1] + Fm[2] * cof[2];
+        bad = valid && !(J.h > 0.0f && isfinite(J.h) && detF > 0.0f && w.h > 0.0f);
       } else {
-        // state right after Element::pre(): C = I, S = 0, O = 0 (SOLID81.cpp:17-19)
+        const double w = a.wdet[tg];
+        const double pc = a.U_cur[a.p_eq[ec] - 1];
+        double O[9];
+        double C[6];
+        double ps = 0.0;
+        if (a.have_state) {
+          double G[24];
 #pragma unroll
-        for (int c = 0; c < 9; c++) O[c] = 0.0;
-        C[0] = C[3] = C[5] = 1.0;
-        C[1] = C[2] = C[4] = 0.0;
-      }
-      int mat_id = a.mat_id;
-      const double* mc = a.mc;
-      double kbulk = a.kbulk;
-      if (a.elem_mesh) {
-        const double* mm = a.mesh_mat + 8 * (uint64_t)__ldg(a.elem_mesh + ec);
-        mat_id = (int)mm[0];
-        mc = mm + 1;
-        kbulk = mm[6];
-      }
-      const double inv_kb = 1.0 / kbulk;
-      MatOut<TT> mo;
-      TT wD[21];
-      material<TT>(mat_id, mc, C, ps, pc, w, mo, wD);
-      if (!a.have_state) {
+          for (int c = 0; c < 24; c++) G[c] = __ldg(a.Gt + c * E8 + tg);
 #pragma unroll
-        for (int i = 0; i < 6; i++) mo.S[i] = 0.0;
-      }
-      const double J = mo.J;
-      const double F[9] = {1.0 + O[0], O[1], O[2], O[3], 1.0 + O[4], O[5], O[6], O[7], 1.0 + O[8]};
-      const double S3[9] = {mo.S[0], mo.S[1], mo.S[2], mo.S[1], mo.S[3], mo.S[4],
-                            mo.S[2], mo.S[4], mo.S[5]};
+          for (int c = 0; c < 9; c++) O[c] = 0.0;
 #pragma unroll
-      for (int i = 0; i < 3; i++)
+          for (int n = 0; n < 8; n++) {
+            const uint32_t nid = __ldg(a.conn + (uint64_t)ec * 8 + n);
+            const uint4 eq = __ldg(reinterpret_cast<const uint4*>(a.node_eq3) + (nid - 1));
+            const double ux = a.U_state[eq.x - 1], uy = a.U_state[eq.y - 1],
+                         uz = a.U_state[eq.z - 1];
 #pragma unroll
-        for (int k = 0; k < 3; k++) {
-          const double fs = F[3 * i + 0] * S3[0 + k] + F[3 * i + 1] * S3[3 + k] +
-                            F[3 * i + 2] * S3[6 + k];
-          sm->wP[3 * i + k][lane] = -w * fs;
+            for (int j = 0; j < 3; j++) {
+              O[0 + j] = fma(ux, G[3 * n + j], O[0 + j]);
+              O[3 + j] = fma(uy, G[3 * n + j], O[3 + j]);
+              O[6 + j] = fma(uz, G[3 * n + j], O[6 + j]);
+            }
+          }
+          ps = a.U_state[a.p_eq[ec] - 1];
+          // C = F^T F from O (SOLID81.cpp:105-110)
+          C[0] = 1.0 + 2 * O[0] + O[0] * O[0] + O[3] * O[3] + O[6] * O[6];
+          C[3] = 1.0 + 2 * O[4] + O[1] * O[1] + O[4] * O[4] + O[7] * O[7];
+          C[5] = 1.0 + 2 * O[8] + O[2] * O[2] + O[5] * O[5] + O[8] * O[8];
+          C[1] = O[1] + O[3] + O[0] * O[1] + O[3] * O[4] + O[6] * O[7];
+          C[4] = O[5] + O[7] + O[1] * O[2] + O[4] * O[5] + O[7] * O[8];
+          C[2] = O[2] + O[6] + O[0] * O[2] + O[3] * O[5] + O[6] * O[8];
+        } else {
+          // state right after Element::pre(): C = I, S = 0, O = 0 (SOLID81.cpp:17-19)
+#pragma unroll
+          for (int c = 0; c < 9; c++) O[c] = 0.0;
+          C[0] = C[3] = C[5] = 1.0;
+          C[1] = C[2] = C[4] = 0.0;
         }
-      const double cof[9] = {F[4] * F[8] - F[5] * F[7], F[5] * F[6] - F[3] * F[8],
-                             F[3] * F[7] - F[4] * F[6], F[2] * F[7] - F[1] * F[8],
-                             F[0] * F[8] - F[2] * F[6], F[1] * F[6] - F[0] * F[7],
-                             F[1] * F[5] - F[2] * F[4], F[2] * F[3] - F[0] * F[5],
-                             F[0] * F[4] - F[1] * F[3]};
+        int mat_id = a.mat_id;
+        const double* mc = a.mc;
+        double kbulk = a.kbulk;
+        if (a.elem_mesh) {
+          const double* mm = a.mesh_mat + 8 * (uint64_t)__ldg(a.elem_mesh + ec);
+          mat_id = (int)mm[0];
+          mc = mm + 1;
+          kbulk = mm[6];
+        }
+        const double inv_kb = 1.0 / kbulk;
+        MatOut<TT> mo;
+        material<TT>(mat_id, mc, C, ps, pc, w, mo, wD);
+        if (!a.have_state) {
 #pragma unroll
-      for (int c = 0; c < 9; c++) sm->wCof[c][lane] = w * cof[c];
+          for (int i = 0; i < 6; i++) mo.S[i] = 0.0;
+        }
+        const double J = mo.J;
+        const double F[9] = {1.0 + O[0], O[1], O[2], O[3], 1.0 + O[4], O[5], O[6], O[7], 1.0 + O[8]};
+        const double S3[9] = {mo.S[0], mo.S[1], mo.S[2], mo.S[1], mo.S[3], mo.S[4],
+                              mo.S[2], mo.S[4], mo.S[5]};
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+          for (int k = 0; k < 3; k++) {
+            const double fs = F[3 * i + 0] * S3[0 + k] + F[3 * i + 1] * S3[3 + k] +
+                              F[3 * i + 2] * S3[6 + k];
+            sm->wP[3 * i + k][lane] = -w * fs;
+          }
+        const double cof[9] = {F[4] * F[8] - F[5] * F[7], F[5] * F[6] - F[3] * F[8],
+                               F[3] * F[7] - F[4] * F[6], F[2] * F[7] - F[1] * F[8],
+                               F[0] * F[8] - F[2] * F[6], F[1] * F[6] - F[0] * F[7],
+                               F[1] * F[5] - F[2] * F[4], F[2] * F[3] - F[0] * F[5],
+                               F[0] * F[4] - F[1] * F[3]};
+#pragma unroll
+        for (int c = 0; c < 9; c++) sm->wCof[c][lane] = w * cof[c];
+#pragma unroll
+        for (int c = 0; c < 9; c++) Fm[c] = (TT)F[c];
+#pragma unroll
+        for (int c = 0; c < 6; c++) wS[c] = (TT)(w * mo.S[c]);
+        Fp_part = -(J - 1 - pc * inv_kb) * w;
+        Kpp_part = -inv_kb * w;
+        // J = sqrt(det C) cannot see an inverted element; det F can
+        const double detF = F[0] * cof[0] + F[1] * cof[1] + F[2] * cof[2];
+        bad = valid && !(J > 0.0 && isfinite(J) && detF > 0.0 && w > 0.0);
+      }
       // A[iL][kN] = sum_J F_iJ (sum_M wD[(JL)][(MN)] F_kM) + delta_ik w S_LN,
       // one row (i, L) at a time
-      TT Fm[9], wS[6];
-#pragma unroll
-      for (int c = 0; c < 9; c++) Fm[c] = (TT)F[c];
-#pragma unroll
-      for (int c = 0; c < 6; c++) wS[c] = (TT)(w * mo.S[c]);
 #pragma unroll
       for (int i = 0; i < 3; i++)
 #pragma unroll
@@ -322,18 +732,22 @@ __global__ void __launch_bounds__(WPB * 32)
               sm->A[sym9(3 * i + L, 3 * k + N)][lane] = v;
             }
         }
-      Fp_part = -(J - 1 - pc * inv_kb) * w;
-      Kpp_part = -inv_kb * w;
-      // J = sqrt(det C) cannot see an inverted element; det F can
-      const double detF = F[0] * cof[0] + F[1] * cof[1] + F[2] * cof[2];
-      const bool bad = valid && !(J > 0.0 && isfinite(J) && detF > 0.0 && w > 0.0);
       const unsigned ballot = __ballot_sync(0xFFFFFFFFu, bad);
       if (sub == 0 && ((ballot >> (q * 8)) & 0xFFu)) flag_element(a.status, e + 1);
     }
 #pragma unroll
     for (int off = 1; off < 8; off <<= 1) {
-      Fp_part += __shfl_xor_sync(0xFFFFFFFFu, Fp_part, off);
-      Kpp_part += __shfl_xor_sync(0xFFFFFFFFu, Kpp_part, off);
+      if constexpr (kMixed) {
+        const dw fo{__shfl_xor_sync(0xFFFFFFFFu, Fp_dw.h, off),
+                    __shfl_xor_sync(0xFFFFFFFFu, Fp_dw.l, off)};
+        const dw ko{__shfl_xor_sync(0xFFFFFFFFu, Kpp_dw.h, off),
+                    __shfl_xor_sync(0xFFFFFFFFu, Kpp_dw.l, off)};
+        Fp_dw = dw_add(Fp_dw, fo);
+        Kpp_dw = dw_add(Kpp_dw, ko);
+      } else {
+        Fp_part += __shfl_xor_sync(0xFFFFFFFFu, Fp_part, off);
+        Kpp_part += __shfl_xor_sync(0xFFFFFFFFu, Kpp_part, off);
+      }
     }
     __syncwarp();
 
@@ -341,32 +755,55 @@ __global__ void __launch_bounds__(WPB * 32)
     TT acc[kOwned];
 #pragma unroll
     for (int m = 0; m < kOwned; m++) acc[m] = (TT)0;
-    double Fu[3] = {0.0, 0.0, 0.0}, Kup[3] = {0.0, 0.0, 0.0};
+    double Fu[3] = {0.0, 0.0, 0.0};
+    TT Kup[3] = {(TT)0, (TT)0, (TT)0};
+    dacc Fua[3] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};  // mixed: Fu in pairs
     const int node = sub;
     for (int g = 0; g < 8; g++) {
       const int s1 = q * 8 + g;
       {
         // phase 2: lane = (element q, node a)
         const uint64_t tg = (uint64_t)ec * 8 + g;
-        const double G0 = __ldg(a.Gt + (3 * node + 0) * E8 + tg);
-        const double G1 = __ldg(a.Gt + (3 * node + 1) * E8 + tg);
-        const double G2 = __ldg(a.Gt + (3 * node + 2) * E8 + tg);
-        // residual and pressure coupling in FP64
+        TT gg[3];
+        if constexpr (kMixed) {
+          // residual in float pairs, pressure coupling in float
+          const dw G0 = dw_of(__ldg(a.Gdf + (3 * node + 0) * E8 + tg));
+          const dw G1 = dw_of(__ldg(a.Gdf + (3 * node + 1) * E8 + tg));
+          const dw G2 = dw_of(__ldg(a.Gdf + (3 * node + 2) * E8 + tg));
 #pragma unroll
-        for (int i = 0; i < 3; i++) {
-          Fu[i] += sm->wP[3 * i + 0][s1] * G0 + sm->wP[3 * i + 1][s1] * G1 +
-                   sm->wP[3 * i + 2][s1] * G2;
-          Kup[i] += sm->wCof[3 * i + 0][s1] * G0 + sm->wCof[3 * i + 1][s1] * G1 +
-                    sm->wCof[3 * i + 2][s1] * G2;
+          for (int i = 0; i < 3; i++) {
+            acc_prod(Fua[i], dw_of(sm->wP[3 * i + 0][s1]), G0);
+            acc_prod(Fua[i], dw_of(sm->wP[3 * i + 1][s1]), G1);
+            acc_prod(Fua[i], dw_of(sm->wP[3 * i + 2][s1]), G2);
+            Kup[i] += sm->wCof[3 * i + 0][s1] * G0.h + sm->wCof[3 * i + 1][s1] * G1.h +
+                      sm->wCof[3 * i + 2][s1] * G2.h;
+          }
+          gg[0] = G0.h;
+          gg[1] = G1.h;
+          gg[2] = G2.h;
+        } else {
+          const double G0 = __ldg(a.Gt + (3 * node + 0) * E8 + tg);
+          const double G1 = __ldg(a.Gt + (3 * node + 1) * E8 + tg);
+          const double G2 = __ldg(a.Gt + (3 * node + 2) * E8 + tg);
+          // residual and pressure coupling in FP64
+#pragma unroll
+          for (int i = 0; i < 3; i++) {
+            Fu[i] += sm->wP[3 * i + 0][s1] * G0 + sm->wP[3 * i + 1][s1] * G1 +
+                     sm->wP[3 * i + 2][s1] * G2;
+            Kup[i] += sm->wCof[3 * i + 0][s1] * G0 + sm->wCof[3 * i + 1][s1] * G1 +
+                      sm->wCof[3 * i + 2][s1] * G2;
+          }
+          gg[0] = (TT)G0;
+          gg[1] = (TT)G1;
+          gg[2] = (TT)G2;
         }
-        const TT gg[3] = {(TT)G0, (TT)G1, (TT)G2};
 #pragma unroll
         for (int i = 0; i < 3; i++)
 #pragma unroll
           for (int k = 0; k < 3; k++)
 #pragma unroll
             for (int N = 0; N < 3; N++)
-              sm->H[(3 * i + k) * 3 + N][lane] =
+              sm->H[(3 * i + k) * HStride<TT>::value + 32 * N + lane] =
                   gg[0] * sm->A[sym9(3 * i + 0, 3 * k + N)][s1] +
                   gg[1] * sm->A[sym9(3 * i + 1, 3 * k + N)][s1] +
                   gg[2] * sm->A[sym9(3 * i + 2, 3 * k + N)][s1];
@@ -376,7 +813,7 @@ __global__ void __launch_bounds__(WPB * 32)
       __syncwarp();
       {
         // phase 3: owned Kuu entries, K(a,i; b,k) += h_a[ik] . G_b
-        const TT* Hf = &sm->H[0][0];
+        const TT* Hf = sm->H;
         const TT* Gf = &sm->G[0][0];
 #pragma unroll
         for (int m = 0; m < kOwned; m++) {
@@ -407,11 +844,17 @@ __global__ void __launch_bounds__(WPB * 32)
         if (ee < E) a.contribK[kdst((uint64_t)ee * kSolidKc + t)] = (double)acc[m];
       }
     }
+    if constexpr (kMixed) {
+#pragma unroll
+      for (int i = 0; i < 3; i++) Fu[i] = dw_to_double(acc_val(Fua[i]));
+      Fp_part = dw_to_double(Fp_dw);
+      Kpp_part = dw_to_double(Kpp_dw);
+    }
     if (valid) {
       const uint64_t kb = (uint64_t)e * kSolidKc, fb = (uint64_t)e * kSolidFc;
 #pragma unroll
       for (int i = 0; i < 3; i++) {
-        a.contribK[kdst(kb + 300 + 3 * node + i)] = Kup[i];
+        a.contribK[kdst(kb + 300 + 3 * node + i)] = (double)Kup[i];
         a.contribF[fdst(fb + 3 * node + i)] = Fu[i];
       }
       if (node == 0) {
@@ -463,9 +906,17 @@ __global__ void solid81_jacobian_kernel(const JacobianArgs a) {
     for (int i = 0; i < 3; i++) {
       double v = 0.0;
       for (int j = 0; j < 3; j++) v += Ji[3 * i + j] * dN[3 * n + j];
-      a.Gt[(uint64_t)(3 * n + i) * E8 + t] = v;
+      if (a.Gt) a.Gt[(uint64_t)(3 * n + i) * E8 + t] = v;
+      if (a.Gdf) {
+        const dw p = dw_from_double(v);
+        a.Gdf[(uint64_t)(3 * n + i) * E8 + t] = make_float2(p.h, p.l);
+      }
     }
   a.wdet[t] = 1.0 * det;
+  if (a.wdf) {
+    const dw p = dw_from_double(1.0 * det);
+    a.wdf[t] = make_float2(p.h, p.l);
+  }
   // isoparametric.cpp:177 logs det < 1e-20; here it is an element status
   if (!(det >= 1.0e-20) && g == 0) flag_element(a.status, e + 1);
 }

@@ -44,15 +44,25 @@ struct Solid81Args {
   // means n_elems
   uint32_t e_begin;
   uint32_t n_total;
+  // mixed precision only: inputs of the residual as float pairs (hi, lo)
+  // with hi + lo = the double to 2^-48 (Gdf replaces Gt, same layout); the
+  // residual is computed in float-pair arithmetic
+  const float2* Gdf;
+  const float2* wdf;        // w det J
+  float2 mcd[5];            // material constants
+  float2 inv_kbd;           // 1 / K
+  const float2* mesh_mat_df;  // per mesh: 8 pairs (-, c0..c4, K, 1/K) when elem_mesh != nullptr
 };
 
 struct JacobianArgs {
   uint32_t n_elems;
   const double* xyz;
   const uint32_t* conn;
-  double* Gt;
+  double* Gt;               // FP64 dN/dX, or nullptr
   double* wdet;
   ElementStatus* status;
+  float2* Gdf;              // the same as float pairs (mixed precision), or nullptr
+  float2* wdf;
 };
 
 struct GatherArgs {
