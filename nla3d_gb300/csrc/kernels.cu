@@ -606,7 +606,9 @@ __global__ void __launch_bounds__(WPB * 32)
 #pragma unroll
             for (int J2 = 0; J2 < 3; J2++) acc_prod(t, F[3 * i + J2], S[sv[3 * J2 + k]]);
             const dw wp = dw_mul(w, acc_val(t));
-            sm->wP[3 * i + k][lane] = make_float2(-wp.h, -wp.l);
+            // slot g * 4 + q: the four elements' pairs of one Gauss point
+            // fall in different bank pairs when phase 2 reads them
+            sm->wP[3 * i + k][g * 4 + q] = make_float2(-wp.h, -wp.l);
           }
 #pragma unroll
         for (int c = 0; c < 9; c++) Fm[c] = F[c].h;
@@ -772,9 +774,10 @@ __global__ void __launch_bounds__(WPB * 32)
           const dw G2 = dw_of(__ldg(a.Gdf + (3 * node + 2) * E8 + tg));
 #pragma unroll
           for (int i = 0; i < 3; i++) {
-            acc_prod(Fua[i], dw_of(sm->wP[3 * i + 0][s1]), G0);
-            acc_prod(Fua[i], dw_of(sm->wP[3 * i + 1][s1]), G1);
-            acc_prod(Fua[i], dw_of(sm->wP[3 * i + 2][s1]), G2);
+            const int sp = g * 4 + q;
+            acc_prod(Fua[i], dw_of(sm->wP[3 * i + 0][sp]), G0);
+            acc_prod(Fua[i], dw_of(sm->wP[3 * i + 1][sp]), G1);
+            acc_prod(Fua[i], dw_of(sm->wP[3 * i + 2][sp]), G2);
             Kup[i] += sm->wCof[3 * i + 0][s1] * G0.h + sm->wCof[3 * i + 1][s1] * G1.h +
                       sm->wCof[3 * i + 2][s1] * G2.h;
           }
