@@ -347,7 +347,7 @@ def run_batched(args, torch, stream, local, dist=None, world=1):
            "ms_per_step": sec * 1e3,
            "meshes": len(meshes), "elements": b.n_elems, "equations": b.n_total,
            "nnz_upper": b.nnz_total, "autotuned": tuned, "graph": True,
-           "dtype": "f32 tangent / f64 residual, volumetric terms and CSR sums",
+           "dtype": "f32 tangent / float-pair (2^-48) residual chain / f64 CSR sums",
            "setup_s": setup_s, "element_status": {"flagged": int(flagged)},
            "workload": f"{len(meshes)} hex blocks, sides log-uniform in [4, 40] (seed 3), "
                        "Neo-Hookean C10~U(0.2,1.0), K/C10~U(500,5000), stretch~U(1.0,1.8)"}
@@ -488,7 +488,7 @@ def run_ours(args):
                                "gather_F": float(mkt[2])},
                  "K_rel_err_vs_fp64": float(np.abs(K32 - K64).max() / np.abs(K64).max()),
                  "F_rel_err_vs_fp64": float(np.abs(F32 - F64).max() / np.abs(F64).max()),
-                 "dtype": "f32 tangent / f64 residual, volumetric terms and CSR sums"}
+                 "dtype": "f32 tangent / float-pair (2^-48) residual chain / f64 CSR sums"}
         sm.close()
 
     batched = None

@@ -77,8 +77,9 @@ extern "C" {
 
 /* Arithmetic of the SOLID81 element kernel. */
 #define NLA3D_PREC_FP64 0  /* everything in FP64 (parity path, <=1e-12 vs the reference) */
-#define NLA3D_PREC_MIXED 1 /* FP32 tangent (B^T.D.B, geometric term); FP64 for F, J,
-                              J-1, the pressure coupling, the residual and CSR sums */
+#define NLA3D_PREC_MIXED 1 /* FP32 tangent (B^T.D.B, geometric term, pressure coupling);
+                              the residual chain (gradient, C, S, J, J-1, F) in float-pair
+                              arithmetic (~2^-48 per operation); FP64 CSR sums */
 
 typedef struct nla3d_ctx nla3d_ctx;
 
