@@ -3,7 +3,8 @@
 Tolerance (FP64 path): max |K_gpu - K_ref| / max |K_ref| <= 1e-12 per K block
 and the same for F, against (a) the committed fixtures produced by the
 reference's own compiled sources and (b) the bit-exact CPU oracle.  The mixed
-path keeps F in FP64 (same 1e-12 bound) and its FP32 tangent within 2e-5.
+path computes F in float-pair arithmetic (held to the same 1e-12 bound) and
+its tangent in FP32 (within 2e-5).
 """
 import os
 
@@ -64,6 +65,25 @@ def test_mixed_precision_bounds():
     assert rel(F32, F64) <= TOL_FP64       # residual stays FP64
     assert rel(K32[2], K64[2]) <= TOL_MIXED_K
     assert rel(K32[2], K64[2]) > 0.0       # the tangent really ran in FP32
+
+
+SOLID81_CASES = ["cube3_nh", "cube4_nh_clamped", "mr_twist_3x2x4", "biderman_3x3x3_clamped",
+                 "bar_mpc_2x2x3", "ce_block_3x3x2", "bar_mpc_ce_2x2x3"]
+
+
+@pytest.mark.parametrize("name", SOLID81_CASES)
+def test_mixed_matches_reference_fixtures(name):
+    """The mixed path against the reference's own dumps, per material
+    (Neo-Hookean, Mooney-Rivlin, Biderman), with rigid-body and linear MPCs:
+    the float-pair residual within the FP64 bound, the FP32 tangent within
+    TOL_MIXED_K."""
+    g = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    s, U, K, F = _gpu(cases.FULL_CASES[name], "mixed")
+    assert np.array_equal(U, g["U"])
+    assert rel(F, g["F"]) <= TOL_FP64, rel(F, g["F"])
+    for b in (1, 12, 2):
+        assert rel(K[b], g[f"K_{b}"]) <= TOL_MIXED_K, (b, rel(K[b], g[f"K_{b}"]))
+    assert s.element_status() == (0, 0)
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
