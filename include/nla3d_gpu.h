@@ -79,7 +79,10 @@ extern "C" {
 #define NLA3D_PREC_FP64 0  /* everything in FP64 (parity path, <=1e-12 vs the reference) */
 #define NLA3D_PREC_MIXED 1 /* FP32 tangent (B^T.D.B, geometric term, pressure coupling);
                               the residual chain (gradient, C, S, J, J-1, F) in float-pair
-                              arithmetic (~2^-48 per operation); FP64 CSR sums */
+                              arithmetic (~2^-48 per operation); FP64 CSR sums.  SOLID81
+                              meshes whose material constants are outside 1e-20 .. 1e20 in
+                              magnitude, or whose extent is outside 1e-6 .. 1e6, are
+                              rejected by nla3d_create(_batch) with NLA3D_ERR_RANGE */
 
 typedef struct nla3d_ctx nla3d_ctx;
 

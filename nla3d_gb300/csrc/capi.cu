@@ -29,6 +29,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <mutex>
 #include <new>
@@ -269,6 +270,32 @@ double bulk_of(const HostModel& m) {
                                            : (m.mat_id == NLA3D_MAT_BIDERMAN ? m.mat_c[4] : m.mat_c[2]);
 }
 
+// The mixed SOLID81 kernel computes in floats and float pairs: its inputs
+// must sit well inside the float exponent range.  Material constants (and
+// the bulk modulus) are 0 or of magnitude 1e-20 .. 1e20; the coordinates'
+// extent is 1e-6 .. 1e6.
+bool mixed_range_ok(const HostModel& m) {
+  auto in_range = [](double v, double lo, double hi) {
+    const double a = std::fabs(v);
+    return std::isfinite(v) && (a == 0.0 || (a >= lo && a <= hi));
+  };
+  for (int k = 0; k < 5; k++)
+    if (!in_range(m.mat_c[k], 1e-20, 1e20)) return false;
+  if (!in_range(bulk_of(m), 1e-20, 1e20) || bulk_of(m) == 0.0) return false;
+  double ext = 0.0;
+  for (int d = 0; d < 3; d++) {
+    double lo = 0.0, hi = 0.0;
+    for (uint64_t n = 0; n < m.n_nodes; n++) {
+      const double x = m.xyz[3 * n + d];
+      if (!std::isfinite(x)) return false;
+      if (n == 0 || x < lo) lo = x;
+      if (n == 0 || x > hi) hi = x;
+    }
+    ext = std::max(ext, hi - lo);
+  }
+  return m.n_nodes == 0 || in_range(ext, 1e-6, 1e6);
+}
+
 bool valid_mesh(const nla3d_ctx* c, uint32_t mesh) { return c && mesh < c->hm.size(); }
 
 void graph_release(nla3d_ctx* c) {
@@ -485,6 +512,13 @@ int nla3d_create_batch(const nla3d_mesh_desc* meshes, uint32_t n_meshes, int pre
   c->hm.resize(n_meshes);
   for (uint32_t i = 0; i < n_meshes; i++) fill_model(c->hm[i], &meshes[i]);
   c->precision = precision;
+  if (precision == NLA3D_PREC_MIXED && meshes[0].elem_type == NLA3D_SOLID81) {
+    for (const HostModel& m : c->hm)
+      if (!mixed_range_ok(m)) {
+        delete c;
+        return NLA3D_ERR_RANGE;
+      }
+  }
   *out = c;
   return NLA3D_OK;
 }

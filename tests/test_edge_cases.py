@@ -74,3 +74,17 @@ def test_uneven_batch_keeps_each_mesh_pattern():
             io, co = b.pattern(i, blk)
             rio, rco = r.pattern(blk)
             assert np.array_equal(io, rio) and np.array_equal(co, rco)
+
+
+def test_mixed_precision_rejects_inputs_outside_the_float_range():
+    """The mixed SOLID81 kernel computes in floats and float pairs: a mesh
+    whose material constants or extent leave the range it supports is
+    rejected at nla3d_create (NLA3D_ERR_RANGE); FP64 takes the same mesh."""
+    big = mg.solid81_block(1, 1, 1, 1.0, mg.MAT_MOONEY_RIVLIN, (4e22, 1e22, 2e24))
+    tiny = mg.solid81_block(1, 1, 1, 1e-8, mg.MAT_NEO_HOOKEAN, (1.0, 100.0))
+    for m in (big, tiny):
+        with pytest.raises(_lib.Nla3dError) as ei:
+            FEStorage(m, "mixed")
+        assert ei.value.code == 5
+        FEStorage(m, "fp64").buildPattern()
+    FEStorage(mg.solid81_block(1, 1, 1, 1.0), "mixed").buildPattern()
