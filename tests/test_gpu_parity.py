@@ -169,6 +169,9 @@ def test_element_status_flags_inverted_element():
     s, _, K, F = assemble_state(mesh, u, p, "fp64")
     count, first = s.element_status()
     assert count > 0 and 1 <= first <= mesh.n_elems
+    # the mixed kernel (float-pair J, float det F) flags the same elements
+    sm, _, _, _ = assemble_state(mesh, u, p, "mixed")
+    assert sm.element_status() == (count, first)
 
 
 def test_larger_mesh_properties():
@@ -182,6 +185,10 @@ def test_larger_mesh_properties():
         assert abs(fd.sum()) <= 1e-12 * np.abs(fd).sum() * 10
     _, _, Ko, Fo = O.solve_state(mesh, u, p, "port")
     assert rel(K[2], Ko[2]) <= TOL_FP64 and rel(F, Fo) <= TOL_FP64
+    # mixed: the float-pair residual on the same twisted block (the gradient
+    # from relative displacements keeps it within the FP64 bound)
+    _, _, Km, Fm = assemble_state(mesh, u, p, "mixed")
+    assert rel(Fm, Fo) <= TOL_FP64 and rel(Km[2], Ko[2]) <= TOL_MIXED_K
 
 
 @pytest.mark.parametrize("name,precision", [("cube4_nh_clamped", "fp64"),
