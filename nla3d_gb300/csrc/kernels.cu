@@ -480,7 +480,8 @@ __global__ void __launch_bounds__(WPB * 32)
   for (int v = threadIdx.x; v < kOwned * 32; v += blockDim.x) {
     const int m = v / 32, l = v % 32;
     const int x = l + 32 * m;
-    uint32_t word = 0xFFFFFFFFu;
+    // entries past the quad's 1200 read slot 0 (in bounds) and are never written
+    uint32_t word = 0u;
     if (x < kEPW * kKuuPerElem) {
       const int q = x / kKuuPerElem, t = x - q * kKuuPerElem;
       const uchar4 en = c_kuu_entry[t];  // (a, i, b, k)
@@ -821,14 +822,12 @@ __global__ void __launch_bounds__(WPB * 32)
 #pragma unroll
         for (int m = 0; m < kOwned; m++) {
           const uint32_t word = dec[m * 32 + lane];
-          if (word != 0xFFFFFFFFu) {
-            const uint32_t ho = word & 0xFFFFu, go = word >> 16;
-            TT v = acc[m];
-            v += Hf[ho] * Gf[go];
-            v += Hf[ho + 32] * Gf[go + 32];
-            v += Hf[ho + 64] * Gf[go + 64];
-            acc[m] = v;
-          }
+          const uint32_t ho = word & 0xFFFFu, go = word >> 16;
+          TT v = acc[m];
+          v += Hf[ho] * Gf[go];
+          v += Hf[ho + 32] * Gf[go + 32];
+          v += Hf[ho + 64] * Gf[go + 64];
+          acc[m] = v;
         }
       }
       __syncwarp();
