@@ -20,6 +20,8 @@
 #include <initializer_list>
 #include <stdexcept>
 #include <string>
+#include <algorithm>
+#include <functional>
 #include <vector>
 
 #include "nla3d_gpu.h"
@@ -202,6 +204,8 @@ class FEStorage {
     return {count, first};
   }
   nla3d_ctx* ctx() { return ctx_; }
+  const std::vector<Mpc>& mpcs() const { return mpcs_; }
+  const std::vector<RigidBodyMpc>& rigidBodies() const { return rigid_; }
 
  private:
   void check(int rc) const {
@@ -295,6 +299,194 @@ class FEStorage {
   std::vector<uint32_t> node_eq_, elem_eq_;
   std::vector<double> U_, F_;
   BlockSparseSymMatrix K_;
+};
+
+// ---- the equation solver on the device (EquationSolver.h:19-34) ----
+
+// A fill-reducing order of K(2) for DeviceEquationSolver (order[new] = K(2)
+// row, 0-based): a point per row (the node of a nodal DoF, the element's
+// centroid for an element DoF, the first node of an MPC equation), geometric
+// nested dissection (split at the median of the longest extent; the rows of
+// the lower half that couple to the upper half are the separator, ordered
+// after both halves; leaves of 64 rows); then the DoFs with a stored diagonal,
+// the MPC equations, the DoFs without a diagonal (a rigid-body master), so
+// that the factorisation needs no pivoting.
+inline std::vector<int32_t> fillReducingOrder(FEStorage& s) {
+  SparseBlock* K2 = s.getK()->block(2);
+  const uint32_t n = K2->nRows();
+  const uint32_t nc = s.nConstrainedDofs(), nu = s.nUnknownDofs();
+  const uint32_t* io = K2->getIofeirArray();
+  const uint32_t* co = K2->getColumnsArray();
+  std::vector<double> pts(3 * (size_t)n, 0.0);
+  auto place = [&](uint32_t eq, const double* p) {
+    if (eq > nc && eq - nc - 1 < n)
+      for (int d = 0; d < 3; d++) pts[3 * (size_t)(eq - nc - 1) + d] = p[d];
+  };
+  for (uint32_t v = 1; v <= s.nNodes(); v++)
+    for (int32_t d = 0; d < 8; d++) place(s.getNodeDofEqNumber(v, (Dof::dofType)d), s.getNode(v).pos);
+  for (uint32_t e = 1; e <= s.nElements(); e++) {
+    Element& el = s.getElement(e);
+    double c[3] = {0.0, 0.0, 0.0};
+    for (uint32_t v : el.nodes)
+      for (int d = 0; d < 3; d++) c[d] += s.getNode(v).pos[d] / (double)el.nodes.size();
+    for (int32_t d = 0; d < 8; d++) place(s.getElementDofEqNumber(e, (Dof::dofType)d), c);
+  }
+  uint32_t k = 0;
+  auto place_row = [&](uint32_t node) {
+    if (nu + k < n)
+      for (int d = 0; d < 3; d++) pts[3 * (size_t)(nu + k) + d] = s.getNode(node).pos[d];
+    k++;
+  };
+  for (const Mpc& m : s.mpcs()) place_row(m.eq.at(0).node);
+  for (const RigidBodyMpc& rb : s.rigidBodies())
+    for (uint32_t v : rb.slaveNodes)
+      for (size_t q = 0; q < rb.dofs.size(); q++) place_row(v);
+  // both triangles of the pattern
+  std::vector<uint32_t> deg(n + 1, 0);
+  for (uint32_t r = 0; r < n; r++)
+    for (uint32_t q = io[r] - 1; q < io[r + 1] - 1; q++) {
+      const uint32_t c = co[q] - 1;
+      if (c != r) {
+        deg[r + 1]++;
+        deg[c + 1]++;
+      }
+    }
+  for (uint32_t r = 0; r < n; r++) deg[r + 1] += deg[r];
+  std::vector<uint32_t> adj(deg[n]), fill(deg.begin(), deg.end() - 1);
+  for (uint32_t r = 0; r < n; r++)
+    for (uint32_t q = io[r] - 1; q < io[r + 1] - 1; q++) {
+      const uint32_t c = co[q] - 1;
+      if (c != r) {
+        adj[fill[r]++] = c;
+        adj[fill[c]++] = r;
+      }
+    }
+  std::vector<int32_t> nd;
+  nd.reserve(n);
+  std::vector<uint8_t> upper(n, 0);
+  std::vector<uint32_t> all(n);
+  for (uint32_t r = 0; r < n; r++) all[r] = r;
+  std::function<void(std::vector<uint32_t>&)> rec = [&](std::vector<uint32_t>& idx) {
+    if (idx.size() <= 64) {
+      nd.insert(nd.end(), idx.begin(), idx.end());
+      return;
+    }
+    int ax = 0;
+    double best = -1.0;
+    for (int d = 0; d < 3; d++) {
+      double lo = pts[3 * (size_t)idx[0] + d], hi = lo;
+      for (uint32_t r : idx) {
+        lo = std::min(lo, pts[3 * (size_t)r + d]);
+        hi = std::max(hi, pts[3 * (size_t)r + d]);
+      }
+      if (hi - lo > best) {
+        best = hi - lo;
+        ax = d;
+      }
+    }
+    std::vector<double> x(idx.size());
+    for (size_t i = 0; i < idx.size(); i++) x[i] = pts[3 * (size_t)idx[i] + ax];
+    std::vector<double> sorted = x;
+    const size_t mid = sorted.size() / 2;
+    std::nth_element(sorted.begin(), sorted.begin() + mid, sorted.end());
+    double med = sorted[mid];
+    if (sorted.size() % 2 == 0) {
+      const double below = *std::max_element(sorted.begin(), sorted.begin() + mid);
+      med = 0.5 * (below + med);
+    }
+    std::vector<uint32_t> lower, up;
+    for (size_t i = 0; i < idx.size(); i++) (x[i] < med ? lower : up).push_back(idx[i]);
+    if (lower.empty() || up.empty()) {
+      nd.insert(nd.end(), idx.begin(), idx.end());
+      return;
+    }
+    for (uint32_t r : up) upper[r] = 1;
+    std::vector<uint32_t> inner, sep;
+    for (uint32_t r : lower) {
+      bool touch = false;
+      for (uint32_t q = deg[r]; q < deg[r + 1] && !touch; q++) touch = upper[adj[q]] != 0;
+      (touch ? sep : inner).push_back(r);
+    }
+    for (uint32_t r : up) upper[r] = 0;
+    rec(inner);
+    rec(up);
+    nd.insert(nd.end(), sep.begin(), sep.end());
+  };
+  rec(all);
+  std::vector<int32_t> order;
+  order.reserve(n);
+  auto has_diag = [&](uint32_t r) { return io[r + 1] > io[r] && co[io[r] - 1] == r + 1; };
+  for (int32_t r : nd)
+    if ((uint32_t)r < nu && has_diag((uint32_t)r)) order.push_back(r);
+  for (uint32_t r = nu; r < n; r++) order.push_back((int32_t)r);
+  for (int32_t r : nd)
+    if ((uint32_t)r < nu && !has_diag((uint32_t)r)) order.push_back(r);
+  return order;
+}
+
+// EquationSolver (EquationSolver.h:19-34) on the device: the sparse LDL^T of
+// K(2) (nla3d_ldlt_*) factored from the K values the last assembly left in
+// HBM, solved with host vectors and refined in FP64.
+class DeviceEquationSolver {
+ public:
+  enum Precision : int { FP64 = 0, FP32 = 1, FP32_TENSOR_CORES = 2 };
+  // after s.initSolutionData(); order: K(2) rows in factor order (default
+  // fillReducingOrder(s))
+  explicit DeviceEquationSolver(FEStorage& s, int precision = FP64,
+                                std::vector<int32_t> order = {})
+      : s_(s) {
+    SparseBlock* K2 = s.getK()->block(2);
+    n_ = K2->nRows();
+    if (order.empty()) order = fillReducingOrder(s);
+    const int rc = nla3d_ldlt_create(n_, K2->getIofeirArray(), K2->getColumnsArray(), order.data(),
+                                     precision, nullptr, &h_);
+    if (rc != NLA3D_OK) {
+      const std::string msg = h_ ? nla3d_ldlt_last_error(h_) : "";
+      if (h_) nla3d_ldlt_destroy(h_);
+      h_ = nullptr;
+      throw Error(rc, "nla3d_ldlt_create: " + msg);
+    }
+  }
+  ~DeviceEquationSolver() {
+    if (h_) nla3d_ldlt_destroy(h_);
+  }
+  DeviceEquationSolver(const DeviceEquationSolver&) = delete;
+  DeviceEquationSolver& operator=(const DeviceEquationSolver&) = delete;
+
+  // factorizeEquations: the device K(2) of the storage's last assembly
+  void factorizeEquations() { check(nla3d_ldlt_factor(h_, deviceK2())); }
+  // substituteEquations: x = K(2)^-1 rhs (host vectors of nRows() doubles),
+  // refined until ||rhs - K x|| <= tol ||rhs||
+  void substituteEquations(const double* rhs, double* x, double tol = 1e-12, int max_refine = 50) {
+    check(nla3d_ldlt_solve_host(h_, deviceK2(), rhs, x, max_refine, tol, &steps_, &residual_));
+  }
+  // solveEquations: both
+  void solveEquations(const double* rhs, double* x) {
+    factorizeEquations();
+    substituteEquations(rhs, x);
+  }
+  uint32_t nRows() const { return (uint32_t)n_; }
+  int refinementSteps() const { return steps_; }
+  double relativeResidual() const { return residual_; }
+
+ private:
+  const double* deviceK2() {
+    double* v = nullptr;
+    uint64_t cnt = 0;
+    check(nla3d_device_K(s_.ctx(), 2, &v, &cnt));
+    return v;
+  }
+  void check(int rc) const {
+    if (rc != NLA3D_OK) {
+      const char* msg = h_ ? nla3d_ldlt_last_error(h_) : "";
+      throw Error(rc, std::string("nla3d_gb300 equation solver: ") + (msg && *msg ? msg : "call failed"));
+    }
+  }
+  FEStorage& s_;
+  nla3d_ldlt* h_ = nullptr;
+  int64_t n_ = 0;
+  int steps_ = 0;
+  double residual_ = 0.0;
 };
 
 }  // namespace nla3d_gb300

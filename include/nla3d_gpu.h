@@ -428,6 +428,14 @@ int nla3d_ldlt_factor(nla3d_ldlt* h, const double* values);
  * tol is not reached; steps and rel_residual may be NULL. */
 int nla3d_ldlt_solve(nla3d_ldlt* h, const double* values, const double* b, double* x,
                      int max_refine, double tol, int* steps, double* rel_residual);
+/* EquationSolver::solveEquations(K(2), rhs, x) with host vectors: b_host and
+ * x_host hold n doubles (pageable or pinned); they go through device buffers
+ * the handle owns, then as nla3d_ldlt_solve.  x_host is written also on
+ * NLA3D_ERR_RANGE (the refined x, tol not reached).  Synchronises the
+ * handle's stream. */
+int nla3d_ldlt_solve_host(nla3d_ldlt* h, const double* values, const double* b_host,
+                          double* x_host, int max_refine, double tol, int* steps,
+                          double* rel_residual);
 /* out[8]: supernodes, levels, largest front, entries of L, flops, front bytes,
  * perturbed pivots and non-finite pivots of the last factorisation. */
 int nla3d_ldlt_info(const nla3d_ldlt* h, double* out);

@@ -963,6 +963,8 @@ struct nla3d_ldlt {
   void* d_W = nullptr;
   void* d_Linv = nullptr;
   double* d_rhs = nullptr;      // the solve graph's right-hand side
+  double* d_hb = nullptr;       // nla3d_ldlt_solve_host: b and x on the device
+  double* d_hx = nullptr;
   cudaGraphExec_t factor_exec = nullptr, solve_exec = nullptr;
   const double* factor_graph_values = nullptr;
   uint64_t* d_wo = nullptr;
@@ -1598,6 +1600,26 @@ int nla3d_ldlt_solve(nla3d_ldlt* h, const double* values, const double* b, doubl
   if (rel_residual) *rel_residual = rel;
   if (!(rel <= tol)) return fail(h, NLA3D_ERR_RANGE, "ldlt_solve: refinement did not reach tol");
   return NLA3D_OK;
+}
+
+int nla3d_ldlt_solve_host(nla3d_ldlt* h, const double* values, const double* b_host,
+                          double* x_host, int max_refine, double tol, int* steps,
+                          double* rel_residual) {
+  if (!h || !values || !b_host || !x_host) return fail(h, NLA3D_ERR_ARG, "ldlt_solve_host: bad argument");
+  const size_t n = (size_t)h->S.n;
+  cudaError_t e = cudaSuccess;
+  if (!h->d_hb) e = dalloc(h, &h->d_hb, n);
+  if (e == cudaSuccess && !h->d_hx) e = dalloc(h, &h->d_hx, n);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(h->d_hb, b_host, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream);
+  if (e != cudaSuccess) return cuda_fail(h, e, "ldlt_solve_host");
+  const int rc = nla3d_ldlt_solve(h, values, h->d_hb, h->d_hx, max_refine, tol, steps, rel_residual);
+  if (rc != NLA3D_OK && rc != NLA3D_ERR_RANGE) return rc;
+  // the refined x also when tol was not reached (the caller reads the residual)
+  e = cudaMemcpyAsync(x_host, h->d_hx, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) return cuda_fail(h, e, "ldlt_solve_host");
+  return rc;
 }
 
 int nla3d_ldlt_tc_check(int m, double* out) {

@@ -5,7 +5,9 @@
 // updateResults and assembleGlobalEqMatrices, and prints the numbering, the
 // three CSR blocks of getK() and getF() (%.17g, so the values read back
 // exactly).  With "pattern" as the third argument it stops after the host
-// set-up (no GPU needed) and prints zero values.
+// set-up (no GPU needed) and prints zero values; with "order" it also prints
+// fillReducingOrder (host only); with "solve" it then solves K(2) x = F(2)
+// with DeviceEquationSolver (EquationSolver::solveEquations) and prints x.
 //
 // Input (whitespace separated):
 //   elem_type n_nodes n_elems mat_id c0 c1 c2 c3 c4 n_params
@@ -26,7 +28,8 @@ int main(int argc, char** argv) {
     std::fprintf(stderr, "usage: %s model.txt out.txt [pattern]\n", argv[0]);
     return 2;
   }
-  const bool pattern_only = argc > 3 && std::string(argv[3]) == "pattern";
+  const std::string mode = argc > 3 ? argv[3] : "";
+  const bool pattern_only = mode == "pattern" || mode == "order";
   std::ifstream in(argv[1]);
   int etype, mat_id, n_params;
   uint32_t n_nodes, n_elems;
@@ -128,6 +131,28 @@ int main(int argc, char** argv) {
   std::fprintf(out, "%zu\n", storage.getF().size());
   for (double v : storage.getF()) std::fprintf(out, "%.17g ", v);
   std::fprintf(out, "\n");
+  try {
+    if (mode == "order") {
+      const std::vector<int32_t> order = fillReducingOrder(storage);
+      std::fprintf(out, "%zu\n", order.size());
+      for (int32_t r : order) std::fprintf(out, "%d ", r);
+      std::fprintf(out, "\n");
+    } else if (mode == "solve") {
+      DeviceEquationSolver solver(storage, DeviceEquationSolver::FP64);
+      const uint32_t nc = storage.nConstrainedDofs();
+      const std::vector<double>& F = storage.getF();
+      std::vector<double> x(solver.nRows());
+      solver.solveEquations(F.data() + nc, x.data());
+      std::fprintf(out, "%zu %d %.3e\n", x.size(), solver.refinementSteps(),
+                   solver.relativeResidual());
+      for (double v : x) std::fprintf(out, "%.17g ", v);
+      std::fprintf(out, "\n");
+    }
+  } catch (const Error& e) {
+    std::fprintf(stderr, "%s\n", e.what());
+    std::fclose(out);
+    return 1;
+  }
   std::fclose(out);
   return 0;
 }

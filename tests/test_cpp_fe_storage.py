@@ -14,6 +14,7 @@ import numpy as np
 import pytest
 
 import cases
+from nla3d_gb300 import meshgen as mg
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
@@ -112,3 +113,83 @@ def test_cpp_assembly_matches_reference_fixtures(example, tmp_path, name):
         K, want = blocks[b][3], g[f"K_{b}"]
         assert np.abs(K - want).max(initial=0.0) <= 1e-12 * max(np.abs(want).max(initial=0.0), 1e-300)
     assert np.abs(F - g["F"]).max() <= 1e-12 * np.abs(g["F"]).max()
+
+
+def _order(example, tmp_path, mesh):
+    model, out = tmp_path / "model.txt", tmp_path / "out.txt"
+    n_total = None
+    from nla3d_gb300.storage import FEStorage
+    s = FEStorage(mesh).buildPattern()
+    n_total = s.n_total
+    _write_model(model, mesh, np.zeros(n_total), False)
+    subprocess.run([example, str(model), str(out), "order"], check=True)
+    lines = open(out).read().split("\n")
+    order = np.array(lines[-2].split(), dtype=np.int64)
+    assert int(lines[-3]) == order.size
+    return s, order
+
+
+@pytest.mark.parametrize("case", ["bar_mpc_2x2x3", "bar_mpc_4x4x16", "block_12"])
+def test_cpp_fill_reducing_order(example, tmp_path, case):
+    """fillReducingOrder (the C++ DeviceEquationSolver's default order): a
+    permutation of K(2)'s rows with the DoFs that have a diagonal first, the
+    MPC equations next and diagonal-less DoFs last, and a fill within 15% of
+    the Python driver's nested dissection (same algorithm), well below the
+    natural order's on a cube (host symbolic analysis, no GPU)."""
+    from nla3d_gb300 import ldlt
+    from nla3d_gb300.newton import csr_full, nested_dissection, row_points
+    if case == "bar_mpc_4x4x16":
+        mesh = mg.solid81_bar_mpc(4, 4, 16, 1.0)
+    elif case == "block_12":
+        mesh = mg.solid81_block(12, 12, 12, 1.0 / 12, clamp_z0=True)
+    else:
+        mesh = cases.FULL_CASES[case]()[0]
+    s, order = _order(example, tmp_path, mesh)
+    io, co = s.pattern(2)
+    n = io.size - 1
+    assert np.array_equal(np.sort(order), np.arange(n))
+    diag = ldlt.has_diagonal(io, co)
+    pos = np.empty(n, np.int64)
+    pos[order] = np.arange(n)
+    rows = np.arange(n)
+    dofs_d = rows[(rows < s.n_unk) & diag]
+    mpc = rows[rows >= s.n_unk]
+    dofs_nd = rows[(rows < s.n_unk) & ~diag]
+    if mpc.size:
+        assert pos[dofs_d].max(initial=-1) < pos[mpc].min()
+    if dofs_nd.size:
+        assert pos[mpc].max(initial=-1) < pos[dofs_nd].min()
+    K = csr_full(io, co, np.ones(co.size), n, n, True)
+    py = ldlt.saddle_order(io, co, nested_dissection(K, row_points(s, s.n_con, s.n_unk, s.n_mpc)),
+                           s.n_unk)
+    fill_cpp = ldlt.analyze(io, co, order)["nnz_L"]
+    fill_py = ldlt.analyze(io, co, py)["nnz_L"]
+    fill_nat = ldlt.analyze(io, co, ldlt.saddle_order(io, co, np.arange(n), s.n_unk))["nnz_L"]
+    assert fill_cpp <= 1.15 * fill_py
+    if case == "block_12":   # (a thin bar's natural order is already banded)
+        assert fill_cpp < 0.7 * fill_nat
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["bar_mpc_2x2x3", "cube4_nh_clamped", "biderman_3x3x3_clamped",
+                                  "bar_mpc_ce_2x2x3"])
+def test_cpp_device_equation_solver(example, tmp_path, name):
+    """DeviceEquationSolver::solveEquations(F(2)) after the C++ assembly: the
+    solution of the reference's K(2) fixture (SciPy, FP64) within 1e-9, on
+    the constrained cases (an unconstrained body's K(2) is singular)."""
+    import scipy.sparse.linalg as spla
+    from nla3d_gb300.newton import csr_full
+    mesh, u, p, extra, do_update = cases.FULL_CASES[name]()
+    g = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    model, out = tmp_path / "model.txt", tmp_path / "out.txt"
+    _write_model(model, mesh, g["U"], do_update)
+    subprocess.run([example, str(model), str(out), "solve"], check=True)
+    lines = open(out).read().split("\n")
+    head = lines[-3].split()
+    x = np.array(lines[-2].split(), dtype=np.float64)
+    assert int(head[0]) == x.size
+    nc = int(g["info"][1])
+    n2 = x.size
+    K2 = csr_full(g["iofeir_2"], g["columns_2"], g["K_2"], n2, n2, True).tocsc()
+    want = spla.spsolve(K2, g["F"][nc:])
+    assert np.abs(x - want).max() <= 1e-9 * np.abs(want).max()
