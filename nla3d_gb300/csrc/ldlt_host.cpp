@@ -14,7 +14,9 @@
 #include "ldlt.hpp"
 
 #include <algorithm>
+#include <atomic>
 #include <climits>
+#include <thread>
 
 std::string ldlt_analyze(int64_t n, const uint32_t* iofeir, const uint32_t* columns,
                          const int32_t* perm_in, LdltSymbolic* out) {
@@ -103,18 +105,70 @@ std::string ldlt_analyze(int64_t n, const uint32_t* iofeir, const uint32_t* colu
     if (t != n) return "elimination tree is not a forest";
     for (int32_t i = 0; i < n; i++) ipost[post[i]] = i;
   }
-  // ---- column counts (row subtrees), incl. the diagonal ----
+  // ---- column counts, incl. the diagonal ----
+  // c(j) = number of row subtrees T(i) (rows i > j of L) that contain j, plus
+  // one.  As in Gilbert, Ng and Peyton ("An efficient algorithm to compute row
+  // and column counts for sparse Cholesky factorization", 1994) each count is
+  // a subtree sum of weights: +1 at every leaf of a row subtree, -1 at the
+  // least common ancestor of consecutive leaves (in postorder) and at the
+  // subtree's root i, and 1 - (number of children) for the diagonal.  A
+  // column j is a leaf of T(i) when no earlier neighbour of row i lies in j's
+  // subtree (first(j) > the last neighbour seen); the ancestors come from a
+  // disjoint-set forest merged along the postorder.  Cost O(nnz(A)), where
+  // walking every row subtree costs O(nnz(L)).
   std::vector<int64_t> cc(n, 1);
   {
-    std::vector<int32_t> mark(n, -1);
-    for (int32_t k = 0; k < n; k++) {
-      mark[k] = k;
-      for (int64_t q = lp[k]; q < lp[k + 1]; q++)
-        for (int32_t j = li[q]; j != -1 && mark[j] != k; j = parent[j]) {
-          cc[j]++;
-          mark[j] = k;
-        }
+    // upper neighbours of each column (order 0): k > j with A(k, j) != 0
+    std::vector<int64_t> up(n + 1, 0);
+    for (int32_t k = 0; k < n; k++)
+      for (int64_t q = lp[k]; q < lp[k + 1]; q++) up[li[q] + 1]++;
+    for (int64_t i = 0; i < n; i++) up[i + 1] += up[i];
+    std::vector<int32_t> ui(up[n]);
+    {
+      std::vector<int64_t> fill(up.begin(), up.end() - 1);
+      for (int32_t k = 0; k < n; k++)
+        for (int64_t q = lp[k]; q < lp[k + 1]; q++) ui[fill[li[q]]++] = k;
     }
+    // everything below in postorder positions
+    std::vector<int32_t> pp(n), first(n, -1), prevnbr(n, -1), prevleaf(n, -1), anc(n);
+    std::vector<int64_t> w(n, 1);
+    for (int32_t t = 0; t < n; t++) {
+      const int32_t p = parent[post[t]];
+      pp[t] = p == -1 ? -1 : ipost[p];
+      anc[t] = t;
+    }
+    for (int32_t t = 0; t < n; t++)
+      if (pp[t] != -1) w[pp[t]]--;
+    for (int32_t t = 0; t < n; t++)
+      for (int32_t r = t; r != -1 && first[r] == -1; r = pp[r]) first[r] = t;
+    for (int32_t t = 0; t < n; t++) {
+      const int32_t j = post[t];
+      for (int64_t q = up[j]; q < up[j + 1]; q++) {
+        const int32_t ip = ipost[ui[q]];
+        if (first[t] > prevnbr[ip]) {   // t is a leaf of row ip's subtree
+          w[t]++;
+          const int32_t pl = prevleaf[ip];
+          if (pl == -1) {
+            w[ip]--;
+          } else {
+            int32_t r = pl;
+            while (anc[r] != r) r = anc[r];
+            for (int32_t x = pl; anc[x] != r;) {
+              const int32_t nx = anc[x];
+              anc[x] = r;
+              x = nx;
+            }
+            w[r]--;   // the least common ancestor of the previous leaf and t
+          }
+          prevleaf[ip] = t;
+        }
+        prevnbr[ip] = t;
+      }
+      if (pp[t] != -1) anc[t] = pp[t];
+    }
+    for (int32_t t = 0; t < n; t++)
+      if (pp[t] != -1) w[pp[t]] += w[t];
+    for (int32_t t = 0; t < n; t++) cc[post[t]] = w[t];
   }
   // ---- order 1: postorder labels ----
   std::vector<int32_t> par1(n), nch1(n, 0);
@@ -291,25 +345,45 @@ std::string ldlt_analyze(int64_t n, const uint32_t* iofeir, const uint32_t* colu
     for (int32_t s = 0; s < ns; s++) S.level_list[fill[S.level[s]]++] = s;
   }
   // ---- where each stored value lands: front of the lower column's supernode ----
+  // (rows split over the host threads; every entry is independent)
   S.a_dest.resize(nnz);
-  for (int64_t r = 0; r < n; r++)
-    for (uint64_t q = iofeir[r] - 1; q < (uint64_t)iofeir[r + 1] - 1; q++) {
-      const int32_t a = o1(r), b = o1(columns[q] - 1);
-      const int32_t hi = std::max(a, b), lo = std::min(a, b);
-      const int32_t s = col2sn[lo];
-      const int32_t f = S.sn_first[s], l = S.sn_first[s + 1] - 1;
-      int64_t lrow;
-      if (hi <= l) {
-        lrow = hi - f;
-      } else {
-        const int32_t* b0 = S.rows.data() + S.row_ptr[s] + S.k(s);
-        const int32_t* b1 = S.rows.data() + S.row_ptr[s + 1];
-        const int32_t* it = std::lower_bound(b0, b1, hi);
-        if (it == b1 || *it != hi) return "entry outside its front";
-        lrow = (int64_t)(it - (S.rows.data() + S.row_ptr[s]));
-      }
-      S.a_dest[q] = S.front_off[s] + (uint64_t)lrow + (uint64_t)(lo - f) * (uint64_t)S.m(s);
+  {
+    std::atomic<bool> outside{false};
+    auto dest_rows = [&](int64_t r0, int64_t r1) {
+      for (int64_t r = r0; r < r1; r++)
+        for (uint64_t q = iofeir[r] - 1; q < (uint64_t)iofeir[r + 1] - 1; q++) {
+          const int32_t a = o1(r), b = o1(columns[q] - 1);
+          const int32_t hi = std::max(a, b), lo = std::min(a, b);
+          const int32_t s = col2sn[lo];
+          const int32_t f = S.sn_first[s], l = S.sn_first[s + 1] - 1;
+          int64_t lrow;
+          if (hi <= l) {
+            lrow = hi - f;
+          } else {
+            const int32_t* b0 = S.rows.data() + S.row_ptr[s] + S.k(s);
+            const int32_t* b1 = S.rows.data() + S.row_ptr[s + 1];
+            const int32_t* it = std::lower_bound(b0, b1, hi);
+            if (it == b1 || *it != hi) {
+              outside = true;
+              return;
+            }
+            lrow = (int64_t)(it - (S.rows.data() + S.row_ptr[s]));
+          }
+          S.a_dest[q] = S.front_off[s] + (uint64_t)lrow + (uint64_t)(lo - f) * (uint64_t)S.m(s);
+        }
+    };
+    const int nt = (int)std::min<int64_t>(std::max(1u, std::thread::hardware_concurrency()),
+                                          std::max<int64_t>(1, n / 4096));
+    std::vector<std::thread> th;
+    const int64_t chunk = (n + nt - 1) / nt;
+    for (int t = 1; t < nt; t++) {
+      const int64_t r0 = t * chunk, r1 = std::min<int64_t>(n, r0 + chunk);
+      if (r0 < r1) th.emplace_back(dest_rows, r0, r1);
     }
+    dest_rows(0, std::min<int64_t>(n, chunk));
+    for (auto& x : th) x.join();
+    if (outside) return "entry outside its front";
+  }
   // ---- both triangles in input numbering (refinement SpMV) ----
   S.full_ptr.assign(n + 1, 0);
   for (int64_t r = 0; r < n; r++)
