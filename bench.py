@@ -656,7 +656,7 @@ def solver_bench(nx, precisions=("fp32", "fp64")):
     import math
     import torch
     from nla3d_gb300 import learned as L, ldlt
-    from nla3d_gb300.newton import NewtonSolver, csr_full, nested_dissection
+    from nla3d_gb300.newton import NewtonSolver
     from nla3d_gb300.storage import FEStorage
     pb = L.bar_problem(nx, 4 * nx, 0.5, 1000.0, 2.0, math.pi / 2)
     t0 = time.perf_counter()
@@ -667,8 +667,7 @@ def solver_bench(nx, precisions=("fp32", "fp64")):
     s.synchronize()
     io, co = s.pattern(2)
     n2 = io.size - 1
-    K = csr_full(io, co, np.ones(co.size), n2, n2, True)
-    perm = ldlt.saddle_order(io, co, nested_dissection(K, ns._row_points()), s.n_unk)
+    perm = ldlt.fill_reducing_order(io, co, ns._row_points(), s.n_unk)
     t_order = time.perf_counter() - t0
     rhs = np.random.default_rng(0).standard_normal(n2)
     out = []

@@ -21,7 +21,6 @@
 #include <stdexcept>
 #include <string>
 #include <algorithm>
-#include <functional>
 #include <vector>
 
 #include "nla3d_gpu.h"
@@ -305,12 +304,10 @@ class FEStorage {
 
 // A fill-reducing order of K(2) for DeviceEquationSolver (order[new] = K(2)
 // row, 0-based): a point per row (the node of a nodal DoF, the element's
-// centroid for an element DoF, the first node of an MPC equation), geometric
-// nested dissection (split at the median of the longest extent; the rows of
-// the lower half that couple to the upper half are the separator, ordered
-// after both halves; leaves of 64 rows); then the DoFs with a stored diagonal,
-// the MPC equations, the DoFs without a diagonal (a rigid-body master), so
-// that the factorisation needs no pivoting.
+// centroid for an element DoF, the first node of an MPC equation), then
+// nla3d_ldlt_order: geometric nested dissection, the DoFs with a stored
+// diagonal first, the MPC equations next, the DoFs without a diagonal (a
+// rigid-body master) last, so that the factorisation needs no pivoting.
 inline std::vector<int32_t> fillReducingOrder(FEStorage& s) {
   SparseBlock* K2 = s.getK()->block(2);
   const uint32_t n = K2->nRows();
@@ -341,86 +338,9 @@ inline std::vector<int32_t> fillReducingOrder(FEStorage& s) {
   for (const RigidBodyMpc& rb : s.rigidBodies())
     for (uint32_t v : rb.slaveNodes)
       for (size_t q = 0; q < rb.dofs.size(); q++) place_row(v);
-  // both triangles of the pattern
-  std::vector<uint32_t> deg(n + 1, 0);
-  for (uint32_t r = 0; r < n; r++)
-    for (uint32_t q = io[r] - 1; q < io[r + 1] - 1; q++) {
-      const uint32_t c = co[q] - 1;
-      if (c != r) {
-        deg[r + 1]++;
-        deg[c + 1]++;
-      }
-    }
-  for (uint32_t r = 0; r < n; r++) deg[r + 1] += deg[r];
-  std::vector<uint32_t> adj(deg[n]), fill(deg.begin(), deg.end() - 1);
-  for (uint32_t r = 0; r < n; r++)
-    for (uint32_t q = io[r] - 1; q < io[r + 1] - 1; q++) {
-      const uint32_t c = co[q] - 1;
-      if (c != r) {
-        adj[fill[r]++] = c;
-        adj[fill[c]++] = r;
-      }
-    }
-  std::vector<int32_t> nd;
-  nd.reserve(n);
-  std::vector<uint8_t> upper(n, 0);
-  std::vector<uint32_t> all(n);
-  for (uint32_t r = 0; r < n; r++) all[r] = r;
-  std::function<void(std::vector<uint32_t>&)> rec = [&](std::vector<uint32_t>& idx) {
-    if (idx.size() <= 64) {
-      nd.insert(nd.end(), idx.begin(), idx.end());
-      return;
-    }
-    int ax = 0;
-    double best = -1.0;
-    for (int d = 0; d < 3; d++) {
-      double lo = pts[3 * (size_t)idx[0] + d], hi = lo;
-      for (uint32_t r : idx) {
-        lo = std::min(lo, pts[3 * (size_t)r + d]);
-        hi = std::max(hi, pts[3 * (size_t)r + d]);
-      }
-      if (hi - lo > best) {
-        best = hi - lo;
-        ax = d;
-      }
-    }
-    std::vector<double> x(idx.size());
-    for (size_t i = 0; i < idx.size(); i++) x[i] = pts[3 * (size_t)idx[i] + ax];
-    std::vector<double> sorted = x;
-    const size_t mid = sorted.size() / 2;
-    std::nth_element(sorted.begin(), sorted.begin() + mid, sorted.end());
-    double med = sorted[mid];
-    if (sorted.size() % 2 == 0) {
-      const double below = *std::max_element(sorted.begin(), sorted.begin() + mid);
-      med = 0.5 * (below + med);
-    }
-    std::vector<uint32_t> lower, up;
-    for (size_t i = 0; i < idx.size(); i++) (x[i] < med ? lower : up).push_back(idx[i]);
-    if (lower.empty() || up.empty()) {
-      nd.insert(nd.end(), idx.begin(), idx.end());
-      return;
-    }
-    for (uint32_t r : up) upper[r] = 1;
-    std::vector<uint32_t> inner, sep;
-    for (uint32_t r : lower) {
-      bool touch = false;
-      for (uint32_t q = deg[r]; q < deg[r + 1] && !touch; q++) touch = upper[adj[q]] != 0;
-      (touch ? sep : inner).push_back(r);
-    }
-    for (uint32_t r : up) upper[r] = 0;
-    rec(inner);
-    rec(up);
-    nd.insert(nd.end(), sep.begin(), sep.end());
-  };
-  rec(all);
-  std::vector<int32_t> order;
-  order.reserve(n);
-  auto has_diag = [&](uint32_t r) { return io[r + 1] > io[r] && co[io[r] - 1] == r + 1; };
-  for (int32_t r : nd)
-    if ((uint32_t)r < nu && has_diag((uint32_t)r)) order.push_back(r);
-  for (uint32_t r = nu; r < n; r++) order.push_back((int32_t)r);
-  for (int32_t r : nd)
-    if ((uint32_t)r < nu && !has_diag((uint32_t)r)) order.push_back(r);
+  std::vector<int32_t> order(n);
+  const int rc = nla3d_ldlt_order(n, io, co, pts.data(), nu, order.data());
+  if (rc != NLA3D_OK) throw Error(rc, "nla3d_ldlt_order rejected the pattern");
   return order;
 }
 

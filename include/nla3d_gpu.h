@@ -399,6 +399,16 @@ int nla3d_assemble_solid81_noalloc(const nla3d_solid81_noalloc_args* args, void*
  * There is no pivoting: a pivot below pivot_rel * max|K| (1e-13 FP64, 1e-7
  * FP32) is replaced by +-that value and counted; the solve refines in FP64. */
 typedef struct nla3d_ldlt nla3d_ldlt;
+/* A fill-reducing order for nla3d_ldlt_create (host; no GPU needed): points
+ * holds a point per row (n x 3: the node of a nodal DoF, an element's
+ * centroid, an MPC equation's first node); geometric nested dissection (split
+ * at the median of the longest extent, the lower half's rows that couple to
+ * the upper half as separator after both halves, leaves of 64 rows), then the
+ * rows below n_dofs with a stored diagonal, the rows from n_dofs on (MPC / CE
+ * equations), the rows below n_dofs without a diagonal.  order: n entries
+ * (order[new] = row, 0-based). */
+int nla3d_ldlt_order(int64_t n, const uint32_t* iofeir, const uint32_t* columns,
+                     const double* points, int64_t n_dofs, int32_t* order);
 /* Symbolic analysis only (host; no GPU needed).  stats[8] = supernodes,
  * levels, largest front, entries of L (incl. D), factorisation flops, front
  * buffer entries, most children of a supernode, total supernode rows; each

@@ -37,7 +37,7 @@ EXPORTS = [
     "nla3d_set_pattern_builder", "nla3d_pattern_on_device", "nla3d_add_surface_lines",
     "nla3d_set_transient", "nla3d_get_C", "nla3d_get_M",
     "nla3d_ldlt_analyze", "nla3d_ldlt_create", "nla3d_ldlt_factor", "nla3d_ldlt_solve",
-    "nla3d_ldlt_solve_host",
+    "nla3d_ldlt_solve_host", "nla3d_ldlt_order",
     "nla3d_ldlt_info", "nla3d_ldlt_last_error", "nla3d_ldlt_destroy", "nla3d_ldlt_tc_check",
 ]
 
@@ -158,6 +158,7 @@ def load(path: str = LIB_PATH):
         "nla3d_ldlt_solve": ([P, P, P, P, ctypes.c_int, ctypes.c_double, P, P], ctypes.c_int),
         "nla3d_ldlt_solve_host": ([P, P, P, P, ctypes.c_int, ctypes.c_double, P, P],
                                   ctypes.c_int),
+        "nla3d_ldlt_order": ([ctypes.c_int64, P, P, P, ctypes.c_int64, P], ctypes.c_int),
         "nla3d_ldlt_info": ([P, P], ctypes.c_int),
         "nla3d_ldlt_last_error": ([P], ctypes.c_char_p),
         "nla3d_ldlt_destroy": ([P], ctypes.c_int),

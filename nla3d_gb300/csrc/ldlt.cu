@@ -1151,6 +1151,12 @@ cudaError_t enqueue_residual(nla3d_ldlt* h, const double* A, const double* x, co
 
 extern "C" {
 
+int nla3d_ldlt_order(int64_t n, const uint32_t* iofeir, const uint32_t* columns,
+                     const double* points, int64_t n_dofs, int32_t* order) {
+  const std::string msg = ldlt_nd_order(n, iofeir, columns, points, n_dofs, order);
+  return msg.empty() ? NLA3D_OK : NLA3D_ERR_ARG;
+}
+
 int nla3d_ldlt_analyze(int64_t n, const uint32_t* iofeir, const uint32_t* columns,
                        const int32_t* perm, double* stats, int32_t* perm_out, int32_t* sn_first_out,
                        int64_t* row_ptr_out, int32_t* rows_out) {

@@ -48,5 +48,11 @@ struct LdltSymbolic {
 // iofeir (n+1) / columns: upper CSR, 1-based, sorted per row, diagonal
 // present or not; perm (n): a fill-reducing order, perm[new] = input index,
 // or null for the identity.  Returns "" or an error message.
+// Fill-reducing order for the factorisation without pivoting (order[new] =
+// row): geometric nested dissection of the rows' points, then the rows below
+// n_dofs that have a stored diagonal, the rows from n_dofs on (MPC / CE
+// equations), the rows below n_dofs without a diagonal.
+std::string ldlt_nd_order(int64_t n, const uint32_t* iofeir, const uint32_t* columns,
+                          const double* points, int64_t n_dofs, int32_t* order);
 std::string ldlt_analyze(int64_t n, const uint32_t* iofeir, const uint32_t* columns,
                          const int32_t* perm, LdltSymbolic* out);

@@ -18,6 +18,117 @@
 #include <climits>
 #include <thread>
 
+namespace {
+
+// Nested dissection of the rows idx: split at the median of the points'
+// longest extent; the rows of the lower half that couple to the upper half
+// form the separator, ordered after both halves; leaves of 64 rows.
+struct NdState {
+  const double* pts;
+  const std::vector<int64_t>* ptr;
+  const std::vector<int32_t>* adj;
+  std::vector<uint8_t> upper;
+  std::vector<int32_t> out;
+};
+
+void nd_split(NdState& st, std::vector<int32_t>& idx) {
+  if (idx.size() <= 64) {
+    st.out.insert(st.out.end(), idx.begin(), idx.end());
+    return;
+  }
+  int ax = 0;
+  double best = -1.0;
+  for (int d = 0; d < 3; d++) {
+    double lo = st.pts[3 * (size_t)idx[0] + d], hi = lo;
+    for (int32_t r : idx) {
+      lo = std::min(lo, st.pts[3 * (size_t)r + d]);
+      hi = std::max(hi, st.pts[3 * (size_t)r + d]);
+    }
+    if (hi - lo > best) {
+      best = hi - lo;
+      ax = d;
+    }
+  }
+  std::vector<double> x(idx.size());
+  for (size_t i = 0; i < idx.size(); i++) x[i] = st.pts[3 * (size_t)idx[i] + ax];
+  std::vector<double> sorted = x;
+  const size_t mid = sorted.size() / 2;
+  std::nth_element(sorted.begin(), sorted.begin() + mid, sorted.end());
+  double med = sorted[mid];
+  if (sorted.size() % 2 == 0)
+    med = 0.5 * (*std::max_element(sorted.begin(), sorted.begin() + mid) + med);
+  std::vector<int32_t> lower, up;
+  for (size_t i = 0; i < idx.size(); i++) (x[i] < med ? lower : up).push_back(idx[i]);
+  if (lower.empty() || up.empty()) {
+    st.out.insert(st.out.end(), idx.begin(), idx.end());
+    return;
+  }
+  std::vector<int32_t>().swap(idx);   // the halves hold the rows now
+  for (int32_t r : up) st.upper[r] = 1;
+  std::vector<int32_t> inner, sep;
+  const std::vector<int64_t>& P = *st.ptr;
+  const std::vector<int32_t>& A = *st.adj;
+  for (int32_t r : lower) {
+    bool touch = false;
+    for (int64_t q = P[r]; q < P[r + 1] && !touch; q++) touch = st.upper[A[q]] != 0;
+    (touch ? sep : inner).push_back(r);
+  }
+  for (int32_t r : up) st.upper[r] = 0;
+  std::vector<int32_t>().swap(lower);
+  nd_split(st, inner);
+  nd_split(st, up);
+  st.out.insert(st.out.end(), sep.begin(), sep.end());
+}
+
+}  // namespace
+
+std::string ldlt_nd_order(int64_t n, const uint32_t* iofeir, const uint32_t* columns,
+                          const double* points, int64_t n_dofs, int32_t* order) {
+  if (n <= 0 || n >= INT32_MAX / 2) return "bad size";
+  if (!iofeir || !points || !order || iofeir[0] != 1) return "bad argument";
+  // both triangles, diagonal excluded
+  std::vector<int64_t> ptr(n + 1, 0);
+  for (int64_t r = 0; r < n; r++) {
+    if (iofeir[r + 1] < iofeir[r]) return "iofeir is not monotone";
+    for (uint64_t q = iofeir[r] - 1; q < (uint64_t)iofeir[r + 1] - 1; q++) {
+      const int64_t c = (int64_t)columns[q] - 1;
+      if (c < r || c >= n) return "not an upper-triangle CSR";
+      if (c != r) {
+        ptr[r + 1]++;
+        ptr[c + 1]++;
+      }
+    }
+  }
+  for (int64_t i = 0; i < n; i++) ptr[i + 1] += ptr[i];
+  std::vector<int32_t> adj(ptr[n]);
+  {
+    std::vector<int64_t> fill(ptr.begin(), ptr.end() - 1);
+    for (int64_t r = 0; r < n; r++)
+      for (uint64_t q = iofeir[r] - 1; q < (uint64_t)iofeir[r + 1] - 1; q++) {
+        const int64_t c = (int64_t)columns[q] - 1;
+        if (c != r) {
+          adj[fill[r]++] = (int32_t)c;
+          adj[fill[c]++] = (int32_t)r;
+        }
+      }
+  }
+  NdState st{points, &ptr, &adj, std::vector<uint8_t>(n, 0), {}};
+  st.out.reserve(n);
+  std::vector<int32_t> all(n);
+  for (int64_t r = 0; r < n; r++) all[r] = (int32_t)r;
+  nd_split(st, all);
+  auto has_diag = [&](int64_t r) {
+    return iofeir[r + 1] > iofeir[r] && (int64_t)columns[iofeir[r] - 1] == r + 1;
+  };
+  int64_t k = 0;
+  for (int32_t r : st.out)
+    if (r < n_dofs && has_diag(r)) order[k++] = r;
+  for (int64_t r = std::max<int64_t>(n_dofs, 0); r < n; r++) order[k++] = (int32_t)r;
+  for (int32_t r : st.out)
+    if (r < n_dofs && !has_diag(r)) order[k++] = r;
+  return k == n ? "" : "order is not a permutation";
+}
+
 std::string ldlt_analyze(int64_t n, const uint32_t* iofeir, const uint32_t* columns,
                          const int32_t* perm_in, LdltSymbolic* out) {
   LdltSymbolic& S = *out;

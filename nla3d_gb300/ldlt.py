@@ -85,6 +85,26 @@ def saddle_order(iofeir, columns, order, n_unknown):
     return np.concatenate([first, np.arange(n_unknown, n), last]).astype(np.int32)
 
 
+def fill_reducing_order(iofeir, columns, points, n_unknown):
+    """nla3d_ldlt_order: geometric nested dissection of K(2)'s rows (a point
+    per row), then saddle_order's grouping (DoFs with a diagonal, MPC / CE
+    equations, DoFs without a diagonal); the same order as
+    saddle_order(iofeir, columns, newton.nested_dissection(K, points),
+    n_unknown), computed in the library."""
+    lib = _lib.load()
+    io = np.ascontiguousarray(iofeir, dtype=np.uint32)
+    co = np.ascontiguousarray(columns, dtype=np.uint32)
+    n = io.size - 1
+    pts = np.ascontiguousarray(points, dtype=np.float64)
+    if pts.shape != (n, 3):
+        raise ValueError("points must be n x 3")
+    order = np.zeros(n, np.int32)
+    rc = lib.nla3d_ldlt_order(n, _p(io), _p(co), _p(pts), int(n_unknown), _p(order))
+    if rc:
+        raise _lib.Nla3dError(rc, "nla3d_ldlt_order rejected the pattern")
+    return order
+
+
 class DeviceLDLT:
     def __init__(self, iofeir, columns, perm=None, precision="fp64", stream=None):
         self.lib = _lib.load()

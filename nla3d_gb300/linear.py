@@ -80,13 +80,11 @@ class _Driver:
     def _device_ldlt(self):
         """The device LDL^T on K(2)'s pattern: nested dissection of the rows'
         points, MPC equations after the DoFs (saddle_order)."""
-        from .ldlt import DeviceLDLT, saddle_order
-        from .newton import nested_dissection, row_points
+        from .ldlt import DeviceLDLT, fill_reducing_order
+        from .newton import row_points
         io, co = self.b.pattern(2)
-        pts = row_points(self.b, self.nc, self.nu, self.nm)
-        order = nested_dissection(self._block2(np.ones(co.size)), pts)
-        return DeviceLDLT.for_storage(self.b, saddle_order(io, co, order, self.nu),
-                                      "fp64" if self.solver == "gpu" else "fp32")
+        order = fill_reducing_order(io, co, row_points(self.b, self.nc, self.nu, self.nm), self.nu)
+        return DeviceLDLT.for_storage(self.b, order, "fp64" if self.solver == "gpu" else "fp32")
 
     def node_solution(self, node, dof):
         """FEStorage::getNodeDofSolution: vecU at the DoF's equation."""

@@ -200,13 +200,10 @@ class NewtonSolver:
         used when its residual is below 1e-6 (an inexact Newton step, counted
         in `inexact_solves`); otherwise this iteration is refactored with FP64
         fronts."""
-        from .ldlt import DeviceLDLT, saddle_order
+        from .ldlt import DeviceLDLT, fill_reducing_order
         if self._ldlt is None:
             io, co = self.patterns[2]
-            n2 = self.nu + self.nm
-            K = csr_full(io, co, np.ones(co.size), n2, n2, True)
-            order = nested_dissection(K, self._row_points())
-            self._perm = saddle_order(io, co, order, self.nu)
+            self._perm = fill_reducing_order(io, co, self._row_points(), self.nu)
             self._ldlt = DeviceLDLT.for_storage(
                 self.b, self._perm, {"gpu": "fp64", "gpu-fp32": "fp32", "gpu-tc": "fp32-tc"}[self.solver])
         self._ldlt.factor(self.b)

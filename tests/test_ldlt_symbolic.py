@@ -125,3 +125,21 @@ def test_sizes_of_a_larger_mesh():
     nat = ldlt.analyze(io, co)
     assert nd["nnz_L"] < 0.8 * nat["nnz_L"] and nd["flops"] < 0.6 * nat["flops"]
     assert nd["levels"] > 3 and nd["supernodes"] < n
+
+
+@pytest.mark.parametrize("name", ["bar_mpc_2x2x3", "bar_mpc_ce_2x2x3", "cube4_nh_clamped",
+                                  "plane41_nh_3x2", "quadth_5x4", "block_14"])
+def test_library_order_equals_the_python_nested_dissection(name):
+    """nla3d_ldlt_order (the drivers' order, computed in the library) is
+    exactly saddle_order(nested_dissection(...)) of the Python restatement."""
+    from nla3d_gb300.newton import row_points
+    from nla3d_gb300.storage import FEStorage
+    mesh = (mg.solid81_block(14, 14, 14, 1.0 / 14, clamp_z0=True) if name == "block_14"
+            else cases.FULL_CASES[name]()[0])
+    s = FEStorage(mesh).buildPattern()
+    io, co = s.pattern(2)
+    n = io.size - 1
+    pts = row_points(s, s.n_con, s.n_unk, s.n_mpc)
+    K = csr_full(io, co, np.ones(co.size), n, n, True)
+    want = ldlt.saddle_order(io, co, nested_dissection(K, pts), s.n_unk)
+    assert np.array_equal(ldlt.fill_reducing_order(io, co, pts, s.n_unk), want)
