@@ -143,3 +143,27 @@ def test_library_order_equals_the_python_nested_dissection(name):
     K = csr_full(io, co, np.ones(co.size), n, n, True)
     want = ldlt.saddle_order(io, co, nested_dissection(K, pts), s.n_unk)
     assert np.array_equal(ldlt.fill_reducing_order(io, co, pts, s.n_unk), want)
+
+
+def test_order_and_host_solve_reject_bad_input():
+    """nla3d_ldlt_order and nla3d_ldlt_solve_host return NLA3D_ERR_ARG on
+    bad arguments (no GPU needed)."""
+    import ctypes
+    from nla3d_gb300 import _lib
+    lib = _lib.load()
+    ERR_ARG = 1
+    io = np.array([1, 2, 3], np.uint32)
+    co = np.array([1, 2], np.uint32)
+    pts = np.zeros((2, 3))
+    out = np.zeros(2, np.int32)
+    p = lambda a: a.ctypes.data  # noqa: E731
+    assert lib.nla3d_ldlt_order(2, p(io), p(co), None, 2, p(out)) == ERR_ARG
+    assert lib.nla3d_ldlt_order(0, p(io), p(co), p(pts), 2, p(out)) == ERR_ARG
+    bad = np.array([2, 1], np.uint32)   # row 2 names column 1: not upper
+    assert lib.nla3d_ldlt_order(2, p(io), p(bad), p(pts), 2, p(out)) == ERR_ARG
+    assert lib.nla3d_ldlt_order(2, p(io), p(co), p(pts), 2, p(out)) == 0
+    assert sorted(out.tolist()) == [0, 1]
+    assert lib.nla3d_ldlt_solve_host(None, None, None, None, 1, 1e-10, None, None) == \
+        ERR_ARG
+    with pytest.raises(ValueError):
+        ldlt.fill_reducing_order(io, co, np.zeros((3, 3)), 2)
