@@ -496,28 +496,63 @@ std::string ldlt_analyze(int64_t n, const uint32_t* iofeir, const uint32_t* colu
     if (outside) return "entry outside its front";
   }
   // ---- both triangles in input numbering (refinement SpMV) ----
-  S.full_ptr.assign(n + 1, 0);
-  for (int64_t r = 0; r < n; r++)
-    for (uint64_t q = iofeir[r] - 1; q < (uint64_t)iofeir[r + 1] - 1; q++) {
-      const int64_t c = columns[q] - 1;
-      S.full_ptr[r + 1]++;
-      if (c != r) S.full_ptr[c + 1]++;
-    }
-  for (int64_t i = 0; i < n; i++) S.full_ptr[i + 1] += S.full_ptr[i];
-  S.full_col.resize(S.full_ptr[n]);
-  S.full_slot.resize(S.full_ptr[n]);
+  // Row c holds the transposed upper entries (r, c), r < c, in ascending r,
+  // then its own upper entries.  The rows are split in chunks over the host
+  // threads; each chunk's count per column gives its write offsets, so the
+  // layout is the sequential one whatever the thread count.
   {
-    std::vector<int64_t> fill(S.full_ptr.begin(), S.full_ptr.end() - 1);
-    for (int64_t r = 0; r < n; r++)
-      for (uint64_t q = iofeir[r] - 1; q < (uint64_t)iofeir[r + 1] - 1; q++) {
-        const int64_t c = columns[q] - 1;
-        S.full_col[fill[r]] = (int32_t)c;
-        S.full_slot[fill[r]++] = (uint32_t)q;
-        if (c != r) {
-          S.full_col[fill[c]] = (int32_t)r;
-          S.full_slot[fill[c]++] = (uint32_t)q;
+    const int nt = (int)std::min<int64_t>(
+        std::min(16u, std::max(1u, std::thread::hardware_concurrency())),
+        std::max<int64_t>(1, n / 65536));
+    const int64_t chunk = (n + nt - 1) / nt;
+    std::vector<std::vector<int64_t>> cnt(nt, std::vector<int64_t>(n, 0));
+    auto run = [&](auto&& body) {
+      std::vector<std::thread> th;
+      for (int t = 1; t < nt; t++) th.emplace_back(body, t);
+      body(0);
+      for (auto& x : th) x.join();
+    };
+    run([&](int t) {
+      const int64_t r0 = t * chunk, r1 = std::min<int64_t>(n, r0 + chunk);
+      for (int64_t r = r0; r < r1; r++)
+        for (uint64_t q = iofeir[r] - 1; q < (uint64_t)iofeir[r + 1] - 1; q++) {
+          const int64_t c = columns[q] - 1;
+          if (c != r) cnt[t][c]++;
+        }
+    });
+    S.full_ptr.assign(n + 1, 0);
+    for (int64_t r = 0; r < n; r++) {
+      int64_t tr = 0;
+      for (int t = 0; t < nt; t++) tr += cnt[t][r];
+      S.full_ptr[r + 1] = S.full_ptr[r] + tr + (int64_t)(iofeir[r + 1] - iofeir[r]);
+    }
+    // cnt[t][c] becomes chunk t's first write position in row c
+    for (int64_t c = 0; c < n; c++) {
+      int64_t at = S.full_ptr[c];
+      for (int t = 0; t < nt; t++) {
+        const int64_t k = cnt[t][c];
+        cnt[t][c] = at;
+        at += k;
+      }
+    }
+    S.full_col.resize(S.full_ptr[n]);
+    S.full_slot.resize(S.full_ptr[n]);
+    run([&](int t) {
+      const int64_t r0 = t * chunk, r1 = std::min<int64_t>(n, r0 + chunk);
+      for (int64_t r = r0; r < r1; r++) {
+        int64_t own = S.full_ptr[r + 1] - (int64_t)(iofeir[r + 1] - iofeir[r]);
+        for (uint64_t q = iofeir[r] - 1; q < (uint64_t)iofeir[r + 1] - 1; q++) {
+          const int64_t c = columns[q] - 1;
+          S.full_col[own] = (int32_t)c;
+          S.full_slot[own++] = (uint32_t)q;
+          if (c != r) {
+            const int64_t w = cnt[t][c]++;
+            S.full_col[w] = (int32_t)r;
+            S.full_slot[w] = (uint32_t)q;
+          }
         }
       }
+    });
   }
   S.perm.resize(n);
   for (int32_t t = 0; t < n; t++) S.perm[t] = p0[post[t]];
