@@ -48,6 +48,8 @@ FLOP_PER_ELEM_BTDB = 69072
 DRAM_BYTES_PER_ELEM_SOLID81 = (108.603392e6 + 123.602432e6) / 64000
 DRAM_BYTES_PER_ELEM_GATHER_K = (301.560064e6 + 62.591488e6) / 64000
 METRIC = "SOLID81 assembly Melem/s"  # Newton iterations per load step (plain vs learned) in "newton"
+MIXED_DTYPE = ("f32 K_uu / f64 volumetric terms (J, J-1, p/K, K_up, K_pp, F_p) / "
+               "float-pair (2^-48) F_u chain / f64 CSR sums")
 UNIT = "Melem/s"
 
 
@@ -347,7 +349,7 @@ def run_batched(args, torch, stream, local, dist=None, world=1):
            "ms_per_step": sec * 1e3,
            "meshes": len(meshes), "elements": b.n_elems, "equations": b.n_total,
            "nnz_upper": b.nnz_total, "autotuned": tuned, "graph": True,
-           "dtype": "f32 tangent / float-pair (2^-48) residual chain / f64 CSR sums",
+           "dtype": MIXED_DTYPE,
            "setup_s": setup_s, "element_status": {"flagged": int(flagged)},
            "workload": f"{len(meshes)} hex blocks, sides log-uniform in [4, 40] (seed 3), "
                        "Neo-Hookean C10~U(0.2,1.0), K/C10~U(500,5000), stretch~U(1.0,1.8)"}
@@ -488,7 +490,7 @@ def run_ours(args):
                                "gather_F": float(mkt[2])},
                  "K_rel_err_vs_fp64": float(np.abs(K32 - K64).max() / np.abs(K64).max()),
                  "F_rel_err_vs_fp64": float(np.abs(F32 - F64).max() / np.abs(F64).max()),
-                 "dtype": "f32 tangent / float-pair (2^-48) residual chain / f64 CSR sums",
+                 "dtype": MIXED_DTYPE,
                  "bound": "instruction issue and the shared-memory LSU path of the element "
                           "kernel (ncu at 64,000 elements: issue 49%, LSU 53%, shared "
                           "wavefronts 57%, FP64 pipe 20%, DRAM 8%)",

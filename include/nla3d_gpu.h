@@ -77,9 +77,12 @@ extern "C" {
 
 /* Arithmetic of the SOLID81 element kernel. */
 #define NLA3D_PREC_FP64 0  /* everything in FP64 (parity path, <=1e-12 vs the reference) */
-#define NLA3D_PREC_MIXED 1 /* FP32 tangent (B^T.D.B, geometric term, pressure coupling);
-                              the residual chain (gradient, C, S, J, J-1, F) in float-pair
-                              arithmetic (~2^-48 per operation); FP64 CSR sums.  SOLID81
+#define NLA3D_PREC_MIXED 1 /* FP32 tangent K_uu (B^T.D.B and the geometric term); FP64
+                              volumetric terms (J = det F, J-1, p/K, the pressure
+                              coupling K_up = w J C^-1 B, K_pp, F_p) and MPC rows; the
+                              rest of the residual chain (gradient, C, S, F_u) in
+                              float-pair arithmetic (~2^-48 per operation); FP64 CSR
+                              sums.  SOLID81
                               meshes whose material constants are outside 1e-20 .. 1e20 in
                               magnitude, or whose extent is outside 1e-6 .. 1e6, are
                               rejected by nla3d_create(_batch) with NLA3D_ERR_RANGE */
@@ -348,7 +351,19 @@ int nla3d_mlp_to_bf16(const float* x, uint16_t* y, int64_t n, void* stream);
  * All calls share that array: calls whose kernels overlap on the GPU (other
  * streams or threads without ordering) race and corrupt each other.  The
  * first call on a device looks up the array's device address with that
- * device current; make that first call before any stream capture.
+ * device current, and uploads a constant table; make that first call before
+ * any stream capture.  The looked-up address is cached per device ordinal
+ * for the device's primary context: after cudaDeviceReset(), or under
+ * another driver-API context on that device, it no longer applies.
+ *
+ * Preconditions, checked on the device by the first kernel of every call:
+ * conn in 1..n_nodes; node_eq[4 (node - 1) + 0..2] of every node that conn
+ * names, and p_eq, in 1..n_eq; k_ptr non-decreasing with
+ * k_ptr[nnz] <= 325 n_elems and every k_ids < 325 n_elems; f_ptr
+ * non-decreasing with f_ptr[n_eq] <= 25 n_elems and every f_ids <
+ * 25 n_elems.  If any fails, nothing is assembled (K and F keep their
+ * contents, no out-of-bounds access) and, when `flagged` is non-NULL, the
+ * call returns NLA3D_ERR_ARG.
  *
  * Semantics: updateResults() followed by assembleGlobalEqMatrices() on the
  * same U, SOLID81 elements only (no MPC rows), FP64.  Inputs:

@@ -339,6 +339,7 @@ cudaError_t enqueue_elements(nla3d_ctx* c, uint32_t e0, uint32_t e1) {
       a.wdf = c->d_wdf;
       for (int i = 0; i < 5; i++) a.mcd[i] = split_pair(m0.mat_c[i]);
       a.inv_kbd = split_pair(1.0 / a.kbulk);
+      a.inv_kb = 1.0 / a.kbulk;
       a.mesh_mat_df = c->uniform_material ? nullptr : c->d_mesh_mat_df;
     }
     e = launch_solid81_shaped(a, c->precision == NLA3D_PREC_MIXED, c->shape, c->stream);
@@ -830,6 +831,7 @@ int nla3d_init_solution_data(nla3d_ctx* c) {
       mesh_mat[8 * i + 0] = m.mat_id;
       for (int k = 0; k < 5; k++) mesh_mat[8 * i + 1 + k] = m.mat_c[k];
       mesh_mat[8 * i + 6] = bulk_of(m);
+      mesh_mat[8 * i + 7] = 1.0 / bulk_of(m);
     }
   }
   std::vector<uint32_t> kpos, fpos;

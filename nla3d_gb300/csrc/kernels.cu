@@ -22,8 +22,10 @@
 // structural zeros of B, B_NL and Omega removed and the sums regrouped; they
 // agree with the reference to rounding (the tests bound the difference at
 // 1e-12 relative).
+#include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <mutex>
 #include <type_traits>
 
 #include "kernels.cuh"
@@ -72,6 +74,26 @@ struct WarpSmem {
   TT H[9 * HStride<TT>::value];  // per (element q, node a) at the current Gauss point:
                        //  h_a[ik][N] at (3i+k) * HStride + 32 N + slot
   TT G[3][32];         //  G_a
+};
+
+// Mixed kernel: -w F S (float pairs) and w cof F (FP64: the pressure
+// coupling K_up keeps FP64) are only needed between phase 1 and the residual
+// / coupling pass that precedes the Gauss point loop, so they share their
+// bytes with h, which that loop writes later.  Per (element q, Gauss point g)
+// they sit at slot g * 4 + q, so the pass's broadcast reads of one Gauss
+// point hit four consecutive words.
+template <>
+struct WarpSmem<float> {
+  float A[45][32];
+  union {
+    float H[9 * HStride<float>::value];
+    struct {
+      float2 wP[9][32];     // -w F S, float pairs
+      double wCof[9][32];   // w cof F, FP64
+      float wCofF[9][32];   // the same from the float F (for G's low part)
+    };
+  };
+  float G[3][32];
 };
 
 __device__ __forceinline__ int sym6(int r, int s) {  // packed upper index, r <= s
@@ -310,7 +332,23 @@ __device__ __forceinline__ dw dw_from_double(double v) {
   return {h, __double2float_rn(v - (double)h)};
 }
 
-__device__ __forceinline__ double dw_to_double(dw x) { return (double)x.h + (double)x.l; }
+// float -> double, exact, with integer operations: on this part the
+// conversion instruction runs on the FP64 pipe, at its 1/64 rate, while a
+// normal float widens by re-biasing the exponent (127 -> 1023) and shifting
+// the mantissa, both on the integer pipe.  Zero is a select; subnormals,
+// infinities and NaNs (none on the assembly's paths) take the conversion.
+__device__ __forceinline__ double f2d(float f) {
+  const uint32_t b = __float_as_uint(f);
+  const uint32_t mag = b & 0x7FFFFFFFu;
+  const uint32_t e = b & 0x7F800000u;
+  if (mag != 0u && (e == 0u || e == 0x7F800000u)) return (double)f;
+  const uint32_t sign = b & 0x80000000u;
+  const uint32_t hi = mag ? (sign | ((mag >> 3) + (896u << 20))) : sign;
+  const uint32_t lo = mag ? (b << 29) : 0u;
+  return __hiloint2double((int)hi, (int)lo);
+}
+
+__device__ __forceinline__ double dw_to_double(dw x) { return f2d(x.h) + f2d(x.l); }
 
 // sqrt(d): the float root refined by one Newton step on the pair
 __device__ __forceinline__ dw dw_sqrt(dw d) {
@@ -467,6 +505,7 @@ __device__ __forceinline__ void material_mixed(int mat_id, const float2* mcd, co
 template <typename TT, int WPB>
 __global__ void __launch_bounds__(WPB * 32)
     solid81_kernel(const Solid81Args a) {
+  if (a.skip && *a.skip) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   uint32_t* dec = reinterpret_cast<uint32_t*>(smem_raw);  // [kOwned][32]
   WarpSmem<TT>* sm =
@@ -509,8 +548,7 @@ __global__ void __launch_bounds__(WPB * 32)
 
     // ---------------- phase 1: lane = (element q, Gauss point g) ----------------
     constexpr bool kMixed = std::is_same<TT, float>::value;
-    double Fp_part = 0.0, Kpp_part = 0.0;  // FP64 kernel
-    dw Fp_dw{0.0f, 0.0f}, Kpp_dw{0.0f, 0.0f};  // mixed kernel
+    double Fp_part = 0.0, Kpp_part = 0.0;  // FP64 in both kernels
     {
       const int g = sub;
       const uint64_t tg = (uint64_t)ec * 8 + g;
@@ -582,12 +620,10 @@ __global__ void __launch_bounds__(WPB * 32)
         }
         int mat_id = a.mat_id;
         const float2* mcd = a.mcd;
-        dw inv_kb = dw_of(a.inv_kbd);
         if (a.elem_mesh) {
           const uint32_t mi = __ldg(a.elem_mesh + ec);
           mat_id = (int)a.mesh_mat[8 * (uint64_t)mi];
           mcd = a.mesh_mat_df + 8 * (uint64_t)mi + 1;
-          inv_kb = dw_of(a.mesh_mat_df[8 * (uint64_t)mi + 7]);
         }
         dw S[6], J;
         material_mixed(mat_id, mcd, C, ps, pc, w, S, J, wD);
@@ -613,20 +649,42 @@ __global__ void __launch_bounds__(WPB * 32)
           }
 #pragma unroll
         for (int c = 0; c < 9; c++) Fm[c] = F[c].h;
-        const float cof[9] = {Fm[4] * Fm[8] - Fm[5] * Fm[7], Fm[5] * Fm[6] - Fm[3] * Fm[8],
-                              Fm[3] * Fm[7] - Fm[4] * Fm[6], Fm[2] * Fm[7] - Fm[1] * Fm[8],
-                              Fm[0] * Fm[8] - Fm[2] * Fm[6], Fm[1] * Fm[6] - Fm[0] * Fm[7],
-                              Fm[1] * Fm[5] - Fm[2] * Fm[4], Fm[2] * Fm[3] - Fm[0] * Fm[5],
-                              Fm[0] * Fm[4] - Fm[1] * Fm[3]};
-#pragma unroll
-        for (int c = 0; c < 9; c++) sm->wCof[c][lane] = w.h * cof[c];
 #pragma unroll
         for (int c = 0; c < 6; c++) wS[c] = w.h * S[c].h;
-        // Fp = -(J - 1 - p / K) w, Kpp = -w / K
-        Fp_dw = dw_neg(dw_mul(dw_add(dw_addf(J, -1.0f), dw_neg(dw_mul(pc, inv_kb))), w));
-        Kpp_dw = dw_neg(dw_mul(inv_kb, w));
-        const float detF = Fm[0] * cof[0] + Fm[1] * cof[1] + Fm[2] * cof[2];
-        bad = valid && !(J.h > 0.0f && isfinite(J.h) && detF > 0.0f && w.h > 0.0f);
+        // The volumetric terms in FP64: F (the pair O widened exactly, plus
+        // I), cof F, J = det F, and from them Fp = -(J - 1 - p / K) w,
+        // Kpp = -w / K (SOLID81.cpp:78-79) and w cof F = w J F^-T, whose
+        // products with G_a are K_up (D_p = J C^-1, materials_hyperelastic.cpp:127).
+        double Fd[9];
+#pragma unroll
+        for (int c = 0; c < 9; c++) {
+          const double o = dw_to_double(O[c]);
+          Fd[c] = (c == 0 || c == 4 || c == 8) ? 1.0 + o : o;
+        }
+        const double cofd[9] = {Fd[4] * Fd[8] - Fd[5] * Fd[7], Fd[5] * Fd[6] - Fd[3] * Fd[8],
+                                Fd[3] * Fd[7] - Fd[4] * Fd[6], Fd[2] * Fd[7] - Fd[1] * Fd[8],
+                                Fd[0] * Fd[8] - Fd[2] * Fd[6], Fd[1] * Fd[6] - Fd[0] * Fd[7],
+                                Fd[1] * Fd[5] - Fd[2] * Fd[4], Fd[2] * Fd[3] - Fd[0] * Fd[5],
+                                Fd[0] * Fd[4] - Fd[1] * Fd[3]};
+        const double wd = a.wdet[tg];
+#pragma unroll
+        for (int c = 0; c < 9; c++) sm->wCof[c][g * 4 + q] = wd * cofd[c];
+        {
+          const float cf[9] = {Fm[4] * Fm[8] - Fm[5] * Fm[7], Fm[5] * Fm[6] - Fm[3] * Fm[8],
+                               Fm[3] * Fm[7] - Fm[4] * Fm[6], Fm[2] * Fm[7] - Fm[1] * Fm[8],
+                               Fm[0] * Fm[8] - Fm[2] * Fm[6], Fm[1] * Fm[6] - Fm[0] * Fm[7],
+                               Fm[1] * Fm[5] - Fm[2] * Fm[4], Fm[2] * Fm[3] - Fm[0] * Fm[5],
+                               Fm[0] * Fm[4] - Fm[1] * Fm[3]};
+#pragma unroll
+          for (int c = 0; c < 9; c++) sm->wCofF[c][g * 4 + q] = w.h * cf[c];
+        }
+        const double Jd = Fd[0] * cofd[0] + Fd[1] * cofd[1] + Fd[2] * cofd[2];
+        const double inv_kbd =
+            a.elem_mesh ? a.mesh_mat[8 * (uint64_t)__ldg(a.elem_mesh + ec) + 7] : a.inv_kb;
+        const double pcd = a.U_cur[a.p_eq[ec] - 1];
+        Fp_part = -(Jd - 1 - pcd * inv_kbd) * wd;
+        Kpp_part = -inv_kbd * wd;
+        bad = valid && !(Jd > 0.0 && isfinite(Jd) && J.h > 0.0f && isfinite(J.h) && wd > 0.0);
       } else {
         const double w = a.wdet[tg];
         const double pc = a.U_cur[a.p_eq[ec] - 1];
@@ -740,27 +798,72 @@ __global__ void __launch_bounds__(WPB * 32)
     }
 #pragma unroll
     for (int off = 1; off < 8; off <<= 1) {
-      if constexpr (kMixed) {
-        const dw fo{__shfl_xor_sync(0xFFFFFFFFu, Fp_dw.h, off),
-                    __shfl_xor_sync(0xFFFFFFFFu, Fp_dw.l, off)};
-        const dw ko{__shfl_xor_sync(0xFFFFFFFFu, Kpp_dw.h, off),
-                    __shfl_xor_sync(0xFFFFFFFFu, Kpp_dw.l, off)};
-        Fp_dw = dw_add(Fp_dw, fo);
-        Kpp_dw = dw_add(Kpp_dw, ko);
-      } else {
-        Fp_part += __shfl_xor_sync(0xFFFFFFFFu, Fp_part, off);
-        Kpp_part += __shfl_xor_sync(0xFFFFFFFFu, Kpp_part, off);
-      }
+      Fp_part += __shfl_xor_sync(0xFFFFFFFFu, Fp_part, off);
+      Kpp_part += __shfl_xor_sync(0xFFFFFFFFu, Kpp_part, off);
     }
     __syncwarp();
+
+    // destination of contribution idx: slot-ordered (kpos) or element-ordered
+    auto kdst = [&](uint64_t idx) -> uint64_t { return a.kpos ? (uint64_t)__ldg(a.kpos + idx) : idx; };
+    auto fdst = [&](uint64_t idx) -> uint64_t { return a.fpos ? (uint64_t)__ldg(a.fpos + idx) : idx; };
+
+    if constexpr (kMixed) {
+      // Residual and pressure coupling, lane = (element q, node a), before the
+      // Gauss point loop reuses the scratch that holds -w F S and w cof F:
+      //   F_u(a, i) = sum_g sum_L (-w F S)_g[iL] G_g[aL]   (float pairs),
+      //   K_up(a, i) = sum_g sum_L (w cof F)_g[iL] G_g[aL]  (FP64),
+      // G = G_hi + G_lo its pair.  The K_up products with G_hi are FP64 FMAs
+      // (two accumulators, even and odd Gauss points, to halve the dependent
+      // chain); the products with G_lo, 2^-24 of the total, are summed in
+      // FP32 (their error, 2^-48 of the total, is that of the pair itself)
+      // and added in FP64 at the end.  The pair arithmetic of F_u keeps the
+      // FP32 pipes busy while the FP64 FMAs drain.  Kpp and Fp are written
+      // here too.
+      double Kupd[2][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
+      float Kupl[3] = {0.0f, 0.0f, 0.0f};
+      dacc Fua[3] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};
+#pragma unroll 2
+      for (int g = 0; g < 8; g++) {
+        const uint64_t tg = (uint64_t)ec * 8 + g;
+        const float2 p0 = __ldg(a.Gdf + (3 * sub + 0) * E8 + tg);
+        const float2 p1 = __ldg(a.Gdf + (3 * sub + 1) * E8 + tg);
+        const float2 p2 = __ldg(a.Gdf + (3 * sub + 2) * E8 + tg);
+        const double G0 = f2d(p0.x), G1 = f2d(p1.x), G2 = f2d(p2.x);
+        const int sp = g * 4 + q;
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+          double& kd = Kupd[g & 1][i];
+          kd = fma(sm->wCof[3 * i + 0][sp], G0, kd);
+          kd = fma(sm->wCof[3 * i + 1][sp], G1, kd);
+          kd = fma(sm->wCof[3 * i + 2][sp], G2, kd);
+          Kupl[i] += sm->wCofF[3 * i + 0][sp] * p0.y + sm->wCofF[3 * i + 1][sp] * p1.y +
+                     sm->wCofF[3 * i + 2][sp] * p2.y;
+          acc_prod(Fua[i], dw_of(sm->wP[3 * i + 0][sp]), dw_of(p0));
+          acc_prod(Fua[i], dw_of(sm->wP[3 * i + 1][sp]), dw_of(p1));
+          acc_prod(Fua[i], dw_of(sm->wP[3 * i + 2][sp]), dw_of(p2));
+        }
+      }
+      if (valid) {
+        const uint64_t kb = (uint64_t)e * kSolidKc, fb = (uint64_t)e * kSolidFc;
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+          a.contribK[kdst(kb + 300 + 3 * sub + i)] = (Kupd[0][i] + Kupd[1][i]) + f2d(Kupl[i]);
+          a.contribF[fdst(fb + 3 * sub + i)] = dw_to_double(acc_val(Fua[i]));
+        }
+        if (sub == 0) {
+          a.contribK[kdst(kb + 324)] = Kpp_part;
+          a.contribF[fdst(fb + 24)] = Fp_part;
+        }
+      }
+      __syncwarp();
+    }
 
     // ---------------- phases 2 + 3 per Gauss point ----------------
     TT acc[kOwned];
 #pragma unroll
     for (int m = 0; m < kOwned; m++) acc[m] = (TT)0;
-    double Fu[3] = {0.0, 0.0, 0.0};
-    TT Kup[3] = {(TT)0, (TT)0, (TT)0};
-    dacc Fua[3] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};  // mixed: Fu in pairs
+    double Fu[3] = {0.0, 0.0, 0.0};   // FP64 kernel (the mixed one wrote F_u and
+    double Kup[3] = {0.0, 0.0, 0.0};  // K_up above)
     const int node = sub;
     for (int g = 0; g < 8; g++) {
       const int s1 = q * 8 + g;
@@ -769,22 +872,10 @@ __global__ void __launch_bounds__(WPB * 32)
         const uint64_t tg = (uint64_t)ec * 8 + g;
         TT gg[3];
         if constexpr (kMixed) {
-          // residual in float pairs, pressure coupling in float
-          const dw G0 = dw_of(__ldg(a.Gdf + (3 * node + 0) * E8 + tg));
-          const dw G1 = dw_of(__ldg(a.Gdf + (3 * node + 1) * E8 + tg));
-          const dw G2 = dw_of(__ldg(a.Gdf + (3 * node + 2) * E8 + tg));
-#pragma unroll
-          for (int i = 0; i < 3; i++) {
-            const int sp = g * 4 + q;
-            acc_prod(Fua[i], dw_of(sm->wP[3 * i + 0][sp]), G0);
-            acc_prod(Fua[i], dw_of(sm->wP[3 * i + 1][sp]), G1);
-            acc_prod(Fua[i], dw_of(sm->wP[3 * i + 2][sp]), G2);
-            Kup[i] += sm->wCof[3 * i + 0][s1] * G0.h + sm->wCof[3 * i + 1][s1] * G1.h +
-                      sm->wCof[3 * i + 2][s1] * G2.h;
-          }
-          gg[0] = G0.h;
-          gg[1] = G1.h;
-          gg[2] = G2.h;
+          // the tangent uses the high parts
+          gg[0] = __ldg(a.Gdf + (3 * node + 0) * E8 + tg).x;
+          gg[1] = __ldg(a.Gdf + (3 * node + 1) * E8 + tg).x;
+          gg[2] = __ldg(a.Gdf + (3 * node + 2) * E8 + tg).x;
         } else {
           const double G0 = __ldg(a.Gt + (3 * node + 0) * E8 + tg);
           const double G1 = __ldg(a.Gt + (3 * node + 1) * E8 + tg);
@@ -834,29 +925,23 @@ __global__ void __launch_bounds__(WPB * 32)
     }
 
     // ---------------- write the element contributions ----------------
-    // destination of contribution idx: slot-ordered (kpos) or element-ordered
-    auto kdst = [&](uint64_t idx) -> uint64_t { return a.kpos ? (uint64_t)__ldg(a.kpos + idx) : idx; };
-    auto fdst = [&](uint64_t idx) -> uint64_t { return a.fpos ? (uint64_t)__ldg(a.fpos + idx) : idx; };
 #pragma unroll
     for (int m = 0; m < kOwned; m++) {
       const int x = lane + 32 * m;
       if (x < kEPW * kKuuPerElem) {
         const int qq = x / kKuuPerElem, t = x - qq * kKuuPerElem;
         const uint32_t ee = e0 + qq;
-        if (ee < E) a.contribK[kdst((uint64_t)ee * kSolidKc + t)] = (double)acc[m];
+        if (ee < E) {
+          if constexpr (kMixed) a.contribK[kdst((uint64_t)ee * kSolidKc + t)] = f2d(acc[m]);
+          else a.contribK[kdst((uint64_t)ee * kSolidKc + t)] = (double)acc[m];
+        }
       }
     }
-    if constexpr (kMixed) {
-#pragma unroll
-      for (int i = 0; i < 3; i++) Fu[i] = dw_to_double(acc_val(Fua[i]));
-      Fp_part = dw_to_double(Fp_dw);
-      Kpp_part = dw_to_double(Kpp_dw);
-    }
-    if (valid) {
+    if (!kMixed && valid) {
       const uint64_t kb = (uint64_t)e * kSolidKc, fb = (uint64_t)e * kSolidFc;
 #pragma unroll
       for (int i = 0; i < 3; i++) {
-        a.contribK[kdst(kb + 300 + 3 * node + i)] = (double)Kup[i];
+        a.contribK[kdst(kb + 300 + 3 * node + i)] = Kup[i];
         a.contribF[fdst(fb + 3 * node + i)] = Fu[i];
       }
       if (node == 0) {
@@ -869,6 +954,7 @@ __global__ void __launch_bounds__(WPB * 32)
 }
 
 __global__ void solid81_jacobian_kernel(const JacobianArgs a) {
+  if (a.skip && *a.skip) return;
   const uint64_t E8 = (uint64_t)a.n_elems * 8;
   const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= E8) return;
@@ -951,7 +1037,9 @@ template <bool kIds>
 __global__ void __launch_bounds__(kMaxGatherBlock)
     gather_sorted_kernel(const uint64_t s_begin, const uint64_t n_slots,
                          const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ ids,
-                         const double* __restrict__ contrib, double* __restrict__ out) {
+                         const double* __restrict__ contrib, double* __restrict__ out,
+                         const uint32_t* __restrict__ skip) {
+  if (skip && *skip) return;  // the same word for every thread: a uniform exit
   __shared__ uint32_t s_beg[kMaxGatherBlock];
   __shared__ uint32_t s_end[kMaxGatherBlock];
   __shared__ uint16_t s_slot[kMaxGatherBlock];
@@ -1315,13 +1403,21 @@ __global__ void fma_probe_kernel(T* out, int iters, T a, T b) {
   if (s == (T)-12345.0) out[0] = s;
 }
 
-int g_tables_ready_device = -1;
+// One ready flag per device: the table is uploaded once per device (a
+// synchronous copy), under a lock so that threads on different devices
+// neither race on the flags nor repeat the upload.
+constexpr int kMaxTableDevices = 64;
+std::atomic<bool> g_tables_ready[kMaxTableDevices];
+std::mutex g_tables_mutex;
 
 cudaError_t ensure_tables() {
   int dev = 0;
   cudaError_t err = cudaGetDevice(&dev);
   if (err != cudaSuccess) return err;
-  if (g_tables_ready_device == dev) return cudaSuccess;
+  if (dev < 0 || dev >= kMaxTableDevices) return cudaErrorInvalidDevice;
+  if (g_tables_ready[dev].load(std::memory_order_acquire)) return cudaSuccess;
+  std::lock_guard<std::mutex> lock(g_tables_mutex);
+  if (g_tables_ready[dev].load(std::memory_order_relaxed)) return cudaSuccess;
   uchar4 h[kKuuPerElem];
   int t = 0;
   for (int i = 0; i < 8; i++)
@@ -1333,7 +1429,7 @@ cudaError_t ensure_tables() {
                                (unsigned char)dj);
         }
   err = cudaMemcpyToSymbol(c_kuu_entry, h, sizeof(h));
-  if (err == cudaSuccess) g_tables_ready_device = dev;
+  if (err == cudaSuccess) g_tables_ready[dev].store(true, std::memory_order_release);
   return err;
 }
 
@@ -1455,7 +1551,7 @@ cudaError_t launch_gather_bs(const GatherArgs& a, int bs, cudaStream_t s) {
   if (a.n_slots <= a.s_begin) return cudaSuccess;
   if (bs != 128 && bs != 256 && bs != 512 && bs != 1024) bs = 256;
   gather_sorted_kernel<true><<<(unsigned)((a.n_slots - a.s_begin + bs - 1) / bs), bs, 0, s>>>(
-      a.s_begin, a.n_slots, a.ptr, a.ids, a.contrib, a.out);
+      a.s_begin, a.n_slots, a.ptr, a.ids, a.contrib, a.out, a.skip);
   return cudaGetLastError();
 }
 
@@ -1465,7 +1561,7 @@ cudaError_t launch_segsum(const SegSumArgs& a, int bs, cudaStream_t s) {
   if (a.n_slots <= a.s_begin) return cudaSuccess;
   if (bs != 128 && bs != 256 && bs != 512 && bs != 1024) bs = 256;
   gather_sorted_kernel<false><<<(unsigned)((a.n_slots - a.s_begin + bs - 1) / bs), bs, 0, s>>>(
-      a.s_begin, a.n_slots, a.ptr, nullptr, a.contrib, a.out);
+      a.s_begin, a.n_slots, a.ptr, nullptr, a.contrib, a.out, nullptr);
   return cudaGetLastError();
 }
 

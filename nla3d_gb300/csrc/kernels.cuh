@@ -29,7 +29,7 @@ struct Solid81Args {
   double kbulk;
   // optional per-element material (several meshes in one launch): when
   // elem_mesh != nullptr, element e uses mesh_mat[8 * elem_mesh[e] + ...] =
-  // (mat_id, c0..c4, K) instead of mat_id / mc / kbulk
+  // (mat_id, c0..c4, K, 1/K) instead of mat_id / mc / kbulk
   const uint32_t* elem_mesh;
   const double* mesh_mat;
   // optional slot-ordered output: contribution c of element e goes to
@@ -51,7 +51,11 @@ struct Solid81Args {
   const float2* wdf;        // w det J
   float2 mcd[5];            // material constants
   float2 inv_kbd;           // 1 / K
+  double inv_kb;            // 1 / K in FP64 (the mixed kernel's volumetric terms)
   const float2* mesh_mat_df;  // per mesh: 8 pairs (-, c0..c4, K, 1/K) when elem_mesh != nullptr
+  // optional: a device word; when non-null and non-zero the launch does
+  // nothing (set by a kernel that found invalid indices in the inputs)
+  const uint32_t* skip;
 };
 
 struct JacobianArgs {
@@ -63,6 +67,9 @@ struct JacobianArgs {
   ElementStatus* status;
   float2* Gdf;              // the same as float pairs (mixed precision), or nullptr
   float2* wdf;
+  // optional: a device word; when non-null and non-zero the launch does
+  // nothing (set by a kernel that found invalid indices in the inputs)
+  const uint32_t* skip;
 };
 
 struct GatherArgs {
@@ -72,6 +79,9 @@ struct GatherArgs {
   const double* contrib;
   double* out;
   uint64_t s_begin;      // slot range [s_begin, n_slots)
+  // optional: a device word; when non-null and non-zero the launch does
+  // nothing (set by a kernel that found invalid indices in the inputs)
+  const uint32_t* skip;
 };
 
 struct MpcArgs {
@@ -156,6 +166,9 @@ struct SegSumArgs {
   const double* contrib;
   double* out;
   uint64_t s_begin;      // slot range [s_begin, n_slots)
+  // optional: a device word; when non-null and non-zero the launch does
+  // nothing (set by a kernel that found invalid indices in the inputs)
+  const uint32_t* skip;
 };
 
 // Linear MPC rows (FEStorage.cpp:49-60 for an Mpc added with addMpc): one

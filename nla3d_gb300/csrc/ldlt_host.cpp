@@ -505,7 +505,9 @@ std::string ldlt_analyze(int64_t n, const uint32_t* iofeir, const uint32_t* colu
         std::min(16u, std::max(1u, std::thread::hardware_concurrency())),
         std::max<int64_t>(1, n / 65536));
     const int64_t chunk = (n + nt - 1) / nt;
-    std::vector<std::vector<int64_t>> cnt(nt, std::vector<int64_t>(n, 0));
+    // per chunk and column: a count, then a write offset within the column's
+    // row of the full pattern (both bounded by one row's length: 32 bits)
+    std::vector<std::vector<uint32_t>> cnt(nt, std::vector<uint32_t>(n, 0));
     auto run = [&](auto&& body) {
       std::vector<std::thread> th;
       for (int t = 1; t < nt; t++) th.emplace_back(body, t);
@@ -526,11 +528,11 @@ std::string ldlt_analyze(int64_t n, const uint32_t* iofeir, const uint32_t* colu
       for (int t = 0; t < nt; t++) tr += cnt[t][r];
       S.full_ptr[r + 1] = S.full_ptr[r] + tr + (int64_t)(iofeir[r + 1] - iofeir[r]);
     }
-    // cnt[t][c] becomes chunk t's first write position in row c
+    // cnt[t][c] becomes chunk t's first write offset in row c
     for (int64_t c = 0; c < n; c++) {
-      int64_t at = S.full_ptr[c];
+      uint32_t at = 0;
       for (int t = 0; t < nt; t++) {
-        const int64_t k = cnt[t][c];
+        const uint32_t k = cnt[t][c];
         cnt[t][c] = at;
         at += k;
       }
@@ -546,7 +548,7 @@ std::string ldlt_analyze(int64_t n, const uint32_t* iofeir, const uint32_t* colu
           S.full_col[own] = (int32_t)c;
           S.full_slot[own++] = (uint32_t)q;
           if (c != r) {
-            const int64_t w = cnt[t][c]++;
+            const int64_t w = S.full_ptr[c] + (int64_t)cnt[t][c]++;
             S.full_col[w] = (int32_t)r;
             S.full_slot[w] = (uint32_t)q;
           }

@@ -365,12 +365,13 @@ def samples_from_history(basis, hist, c10, kbulk):
     return X, Y
 
 
-def make_backend(problem: Problem, kind="gpu", precision="fp64"):
-    if kind == "gpu":
-        from .storage import FEStorage
-        return FEStorage(problem.mesh, precision).initSolutionData()
-    from oracle import oracle as O  # CPU oracle backend (tests only)
-    return O.OracleModel(problem.mesh, "port")
+def make_backend(problem: Problem, precision="fp64", factory=None):
+    """The assembly backend of one solve: the GPU FEStorage, or what
+    `factory(mesh)` returns (any object with the FEStorage driver API)."""
+    if factory is not None:
+        return factory(problem.mesh)
+    from .storage import FEStorage
+    return FEStorage(problem.mesh, precision).initSolutionData()
 
 
 def basis_for(problem: Problem, backend):
@@ -378,10 +379,10 @@ def basis_for(problem: Problem, backend):
     return CoarseBasis(problem.mesh, ne, ee, backend.n_con, backend.n_total)
 
 
-def generate(problems, kind="gpu", precision="fp64", linear_solver="direct"):
+def generate(problems, precision="fp64", linear_solver="direct", backend_factory=None):
     X, Y, iters = [], [], []
     for pb in problems:
-        be = make_backend(pb, kind, precision)
+        be = make_backend(pb, precision, backend_factory)
         solver, hist = solve(pb, be, linear_solver=linear_solver)
         x, y = samples_from_history(basis_for(pb, be), hist, pb.c10, pb.kbulk)
         X += x
@@ -390,8 +391,8 @@ def generate(problems, kind="gpu", precision="fp64", linear_solver="direct"):
     return np.array(X), np.array(Y), iters
 
 
-def evaluate(problems, mlp, kind="gpu", precision="fp64", linear_solver="direct",
-             starts=("plain", "extrapolation", "learned"), log=None):
+def evaluate(problems, mlp, precision="fp64", linear_solver="direct",
+             starts=("plain", "extrapolation", "learned"), log=None, backend_factory=None):
     """Mean Newton iterations per load step: plain start, secant extrapolation
     and the learned start (with the plain-start fallback)."""
     import time
@@ -399,11 +400,11 @@ def evaluate(problems, mlp, kind="gpu", precision="fp64", linear_solver="direct"
     out["learned_used"] = []
     wall = {}
     for pb in problems:
-        be = make_backend(pb, kind, precision)
+        be = make_backend(pb, precision, backend_factory)
         basis = basis_for(pb, be)
         for start in starts:
             if start != "plain":
-                be = make_backend(pb, kind, precision)
+                be = make_backend(pb, precision, backend_factory)
             factory = None
             if start == "extrapolation":
                 factory = lambda sv, h: ExtrapolationPredictor(h)  # noqa: E731
@@ -454,7 +455,7 @@ def benchmark(n_block_train=40, n_block_eval=8, n_bar_train=12, log=None):
                        "mesh": "3x3x12 SOLID81 + rigid-body MPC end", "load_steps": 50})
     its = {}
     for precision in ("fp64", "mixed"):
-        be = make_backend(cfg, "gpu", precision)
+        be = make_backend(cfg, precision)
         s, _ = solve(cfg, be)
         its[precision] = float(np.mean([r.iterations for r in s.records]))
     out["bar"]["iterations_fp64_assembly"] = its["fp64"]

@@ -23,7 +23,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "liborc.so")
 REF_SO = os.path.join(HERE, "_ref", "libnla3d_ref.so")
 REF_WIDE_SO = os.path.join(HERE, "_ref", "libnla3d_ref_wide.so")
-REF_SRC = "/root/reference/src/lib"
+# the reference checkout (read-only); NLA3D_REFERENCE overrides the default
+REF_ROOT = os.environ.get("NLA3D_REFERENCE", "/root/reference")
+REF_SRC = os.path.join(REF_ROOT, "src", "lib")
+REF_TEST = os.path.join(REF_ROOT, "test")
 
 _P = ctypes.c_void_p
 _libs: dict = {}

@@ -261,7 +261,7 @@ def write_damper_fixture():
     SOLID81 on the TYPE 1 elements of model.cdb, its fixed DoFs (with their
     end values), its 497 CE equations, the TOP_SIDE node component used for
     the UY reaction, and the ANSYS loading curve (test/3d_damper/ansys/)."""
-    base = "/root/reference/test/3d_damper"
+    base = os.path.join(O.REF_TEST, "3d_damper")
     md = read_cdb(f"{base}/model.cdb")
     conn = np.array([c for c, t in zip(md["cells"], md["type"]) if t == 1], dtype=np.uint32)
     terms = [t for terms, _ in md["mpcs"] for t in terms]
@@ -285,7 +285,7 @@ def write_a2000_fixture():
     """The reference's a2000_damper BENCH input (test/CMakeLists.txt:141-146):
     PLANE41 on the TYPE 1 elements of a2000.cdb, its fixed DoFs, the DISP_BC
     node component of the UY reaction, and the ANSYS loading curve."""
-    base = "/root/reference/test/a2000_damper"
+    base = os.path.join(O.REF_TEST, "a2000_damper")
     md = read_cdb(f"{base}/a2000.cdb")
     conn = np.array([c for c, t in zip(md["cells"], md["type"]) if t == 1], dtype=np.uint32)
     assert not md["mpcs"]
@@ -306,7 +306,7 @@ def write_heat_fixture():
     HEAT loads, the PROBE node, and the ANSYS results the two tests check:
     every node's steady temperature (temp.txt) and the probe's transient
     history (temphistory.txt)."""
-    base = "/root/reference/test/QUADTH"
+    base = os.path.join(O.REF_TEST, "QUADTH")
     md = read_cdb(f"{base}/heat.cdb")
     quads = np.array([c for c, t in zip(md["cells"], md["type"]) if t == 1], dtype=np.uint32)
     lines = np.array([c for c, t in zip(md["cells"], md["type"]) if t == 2], dtype=np.uint32)
@@ -373,7 +373,7 @@ def write_tetra0_fixture():
     TETRA0_test.cpp takes them), its D fixes and F loads, and the ANSYS
     results the test checks: nodal displacements (disp.res, 1e-10) and
     element stresses (stress.res, 1e-3)."""
-    base = "/root/reference/test/TETRA0"
+    base = os.path.join(O.REF_TEST, "TETRA0")
     md = read_cdb(f"{base}/tetra.cdb")
     conn = np.array([[c[0], c[1], c[2], c[4]] for c, t in zip(md["cells"], md["type"]) if t == 1],
                     dtype=np.uint32)
@@ -400,7 +400,7 @@ def write_tetra0_fixture():
 
 
 def write_rigid_body_fixture():
-    base = "/root/reference/test/rigid_body_mpc"
+    base = os.path.join(O.REF_TEST, "rigid_body_mpc")
     nodes, elems, comps, fixes, curve = read_rigid_body_case(
         f"{base}/block_ROTX.cdb", f"{base}/reference_MOMZ_reaction.txt")
     labels = ["UX", "UY", "UZ", "ROTX", "ROTY", "ROTZ", "HYDRO_PRESSURE", "TEMP"]

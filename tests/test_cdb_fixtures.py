@@ -10,7 +10,7 @@ import pytest
 import make_golden as mgd
 
 GOLDEN = os.path.dirname(mgd.__file__)
-REF_TEST = "/root/reference/test"
+from oracle.oracle import REF_TEST  # noqa: E402
 
 
 @pytest.mark.skipif(not os.path.isdir(REF_TEST), reason="reference tests not present")

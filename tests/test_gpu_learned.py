@@ -37,10 +37,10 @@ def test_learned_start_reduces_newton_iterations():
     pytest.importorskip("torch")
     from nla3d_gb300 import learned as L
     train = L.sample_block_problems(24, n=3, seed=11)
-    X, Y, _ = L.generate(train, kind="gpu")
+    X, Y, _ = L.generate(train)
     mlp = L.MLP(seed=0)
     hist = mlp.fit(X, Y, epochs=300, batch=128, lr=2e-3)
     assert hist[-1][1] < hist[0][1]
     held_out = L.sample_block_problems(4, n=3, seed=99)
-    res = L.evaluate(held_out, mlp, kind="gpu")
+    res = L.evaluate(held_out, mlp)
     assert res["learned"] < res["plain"], res

@@ -3,8 +3,9 @@
 Tolerance (FP64 path): max |K_gpu - K_ref| / max |K_ref| <= 1e-12 per K block
 and the same for F, against (a) the committed fixtures produced by the
 reference's own compiled sources and (b) the bit-exact CPU oracle.  The mixed
-path computes F in float-pair arithmetic (held to the same 1e-12 bound) and
-its tangent in FP32 (within 2e-5).
+path computes F_u in float-pair arithmetic and the volumetric terms (J, K_up,
+K_pp, F_p) in FP64, all held to the same 1e-12 bound, and K_uu in FP32
+(within 2e-5).
 """
 import os
 
@@ -84,6 +85,57 @@ def test_mixed_matches_reference_fixtures(name):
     for b in (1, 12, 2):
         assert rel(K[b], g[f"K_{b}"]) <= TOL_MIXED_K, (b, rel(K[b], g[f"K_{b}"]))
     assert s.element_status() == (0, 0)
+
+
+def _entry_classes(s):
+    """Per K block: a class per stored entry, 0 = displacement-displacement
+    (K_uu), 1 = pressure-displacement (K_up), 2 = pressure-pressure (K_pp),
+    3 = a row or column of an MPC equation.  Block-local indices are mapped
+    back to equations (block(1): constrained, block(1,2): constrained x the
+    rest, block(2): the rest; BlockSparseMatrix.h:126-168)."""
+    ne, ee = s.eq_numbers()
+    pres = np.zeros(s.n_total + 1, bool)
+    pe = ee[:, mg.HYDRO_PRESSURE].astype(np.int64)
+    pres[pe[pe > 0]] = True
+    mpc = np.zeros(s.n_total + 1, bool)
+    mpc[s.n_dofs + 1:] = True
+    out = {}
+    for b, (ro, co) in {1: (0, 0), 12: (0, s.n_con), 2: (s.n_con, s.n_con)}.items():
+        io, cols = s.pattern(b)
+        rows = np.repeat(np.arange(1, io.size, dtype=np.int64), np.diff(io.astype(np.int64)))
+        r = rows + ro
+        c = cols.astype(np.int64) + co
+        cls = pres[r].astype(np.int8) + pres[c].astype(np.int8)
+        cls[mpc[r] | mpc[c]] = 3
+        out[b] = cls
+    return out, pres
+
+
+def _rel_masked(a, b, m):
+    return rel(a[m], b[m]) if m.any() else 0.0
+
+
+@pytest.mark.parametrize("name", SOLID81_CASES)
+def test_mixed_volumetric_terms_fp64(name):
+    """The mixed path keeps FP64 for the volumetric terms: the pressure
+    coupling K_up (D_p = J C^-1), K_pp and the pressure rows F_p of F
+    (J - 1 - p/K) within the FP64 bound of the reference's dumps, K_uu within
+    TOL_MIXED_K; the MPC rows are FP64 in both precisions."""
+    g = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    s, U, K, F = _gpu(cases.FULL_CASES[name], "mixed")
+    cls, pres = _entry_classes(s)
+    seen = set()
+    for b in (1, 12, 2):
+        ref = g[f"K_{b}"]
+        for c, tol in ((0, TOL_MIXED_K), (1, TOL_FP64), (2, TOL_FP64), (3, TOL_FP64)):
+            m = cls[b] == c
+            if m.any():
+                seen.add(c)
+            assert _rel_masked(K[b], ref, m) <= tol, (b, c, _rel_masked(K[b], ref, m))
+    assert {0, 1, 2} <= seen
+    fp = pres[1:F.size + 1]
+    assert fp.any()
+    assert _rel_masked(F, g["F"], fp) <= TOL_FP64, _rel_masked(F, g["F"], fp)
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])

@@ -19,7 +19,7 @@ from nla3d_gb300 import meshgen as mg
 from oracle import oracle as O
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
-REF_TEST = "/root/reference/test"
+from oracle.oracle import REF_TEST  # noqa: E402
 
 
 def _run(kind, case):
