@@ -47,6 +47,12 @@ FLOP_PER_ELEM_BTDB = 69072
 # lower bound there (L2 still held part of them when the kernel ended).
 DRAM_BYTES_PER_ELEM_SOLID81 = (108.603392e6 + 123.602432e6) / 64000
 DRAM_BYTES_PER_ELEM_GATHER_K = (301.560064e6 + 62.591488e6) / 64000
+# Executed arithmetic per element of solid81_kernel<float> (mixed), from the
+# instruction counters of one ncu capture of a 40^3 block (64,000 elements):
+# FP32 2 FFMA + FADD + FMUL and FP64 2 DFMA + DADD + DMUL per element.
+MIXED_FP32_FLOP_PER_ELEM = 66084
+MIXED_FP64_FLOP_PER_ELEM = 1800
+MIXED_WARP_INSTR_PER_ELEM = 3530
 METRIC = "SOLID81 assembly Melem/s"  # Newton iterations per load step (plain vs learned) in "newton"
 MIXED_DTYPE = ("f32 K_uu / f64 volumetric terms (J, J-1, p/K, K_up, K_pp, F_p) / "
                "float-pair (2^-48) F_u chain / f64 CSR sums")
@@ -96,6 +102,8 @@ def parse():
                          "or the device LDL^T with FP64 / FP32 fronts")
     ap.add_argument("--e2e-chunks", type=int, default=8,
                     help="element ranges of nla3d_assemble_to_host in the e2e leg")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the full-size parity check against the oracle port")
     ap.add_argument("--no-tune", action="store_true",
                     help="keep the default launch shape and contribution layout")
     return ap.parse_args()
@@ -220,6 +228,91 @@ def run_reference(args):
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# Parity at full size: the oracle port on the bench's own state, in a spawned
+# process that runs on one host core while the GPU legs run.
+# ---------------------------------------------------------------------------
+
+def _parity_oracle_worker(n, outdir):
+    sys.path.insert(0, ROOT)
+    from oracle import oracle as O
+    from nla3d_gb300 import meshgen as mg
+    t0 = time.perf_counter()
+    mesh, u, p = mg.config_twist(n=n, seed=2)
+    m = O.OracleModel(mesh, "port")
+    ne, ee = m.eq_numbers()
+    m.set_U(mg.u_to_vector(ne, ee, u, p, m.n_total))
+    m.update()
+    m.assemble()
+    np.save(os.path.join(outdir, "ne.npy"), ne)
+    np.save(os.path.join(outdir, "ee.npy"), ee)
+    for b in (1, 12, 2):
+        io, co = m.pattern(b)
+        np.save(os.path.join(outdir, f"io{b}.npy"), io)
+        np.save(os.path.join(outdir, f"co{b}.npy"), co)
+        np.save(os.path.join(outdir, f"K{b}.npy"), m.K(b))
+    np.save(os.path.join(outdir, "F.npy"), m.F())
+    m.close()
+    with open(os.path.join(outdir, "seconds"), "w") as f:
+        f.write(str(time.perf_counter() - t0))
+
+
+def start_parity(n):
+    import multiprocessing as mp
+    import tempfile
+    outdir = tempfile.mkdtemp(prefix="nla3d_parity_")
+    proc = mp.get_context("spawn").Process(target=_parity_oracle_worker, args=(n, outdir))
+    proc.start()
+    return proc, outdir
+
+
+def _rel(a, b, m=None):
+    if m is not None:
+        a, b = a[m], b[m]
+    if b.size == 0:
+        return 0.0
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def finish_parity(proc, outdir, gpu64, gpu_mixed):
+    """Compare the GPU results kept on the host with the oracle's arrays.
+    gpu64 = (ne, ee, n_con, {b: (io, co)}, {b: K}, F); gpu_mixed = (K2, F) or None."""
+    import shutil
+    proc.join()
+    try:
+        if proc.exitcode != 0:
+            return {"error": f"oracle process exit code {proc.exitcode}"}
+        ld = lambda nm: np.load(os.path.join(outdir, nm + ".npy"), mmap_mode="r")  # noqa: E731
+        ne, ee, n_con, pat, K, F = gpu64
+        out = {"vs": "oracle port (oracle/nla3d_oracle.c) on the same state, one host core",
+               "numbering_equal": bool(np.array_equal(ne, ld("ne")) and np.array_equal(ee, ld("ee"))),
+               "pattern_equal": all(np.array_equal(pat[b][0], ld(f"io{b}")) and
+                                    np.array_equal(pat[b][1], ld(f"co{b}")) for b in (1, 12, 2)),
+               "fp64": {"K_rel": max(_rel(K[b], np.asarray(ld(f"K{b}"))) for b in (1, 12, 2)),
+                        "F_rel": _rel(F, np.asarray(ld("F")))},
+               "tolerance": 1e-12}
+        if gpu_mixed is not None:
+            K2m, Fm = gpu_mixed
+            Kr, Fr = np.asarray(ld("K2")), np.asarray(ld("F"))
+            # entry classes of K(2): u-u, u-p, p-p (pressure equations from ee)
+            pres = np.zeros(len(Fr) + 1, bool)
+            pe = ee[:, 6].astype(np.int64)
+            pres[pe[pe > 0]] = True
+            io, co = pat[2]
+            rows = np.repeat(np.arange(1, io.size, dtype=np.int64), np.diff(io.astype(np.int64)))
+            cls = pres[rows + n_con].astype(np.int8) + pres[co.astype(np.int64) + n_con].astype(np.int8)
+            fp = pres[1:len(Fr) + 1]
+            out["mixed"] = {"K_uu": _rel(K2m, Kr, cls == 0), "K_up": _rel(K2m, Kr, cls == 1),
+                            "K_pp": _rel(K2m, Kr, cls == 2), "F_u": _rel(Fm, Fr, ~fp),
+                            "F_p": _rel(Fm, Fr, fp)}
+        out["oracle_s"] = float(open(os.path.join(outdir, "seconds")).read())
+        out["ok"] = bool(out["numbering_equal"] and out["pattern_equal"] and
+                         out["fp64"]["K_rel"] <= 1e-12 and out["fp64"]["F_rel"] <= 1e-12)
+        return out
+    finally:
+        shutil.rmtree(outdir, ignore_errors=True)
 
 
 # ---------------------------------------------------------------------------
@@ -370,6 +463,12 @@ def run_ours(args):
     from nla3d_gb300 import meshgen as mg
     from nla3d_gb300.storage import FEStorage, probe_fma_peak
 
+    # full-size parity against the oracle port: started (spawned) before any
+    # GPU work, it runs on one host core while the GPU legs run
+    parity_job = None
+    if rank == 0 and world == 1 and not args.no_parity:
+        parity_job = start_parity(args.n)
+
     # CPU baseline first (rank 0, N=1 only), before any GPU work
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -409,6 +508,10 @@ def run_ours(args):
     st.set_timing(False)
     sec = max_over_ranks(sec, dist)
     value = replica_throughput(mesh.n_elems, sec, world)
+    gpu64 = None
+    if parity_job:
+        gpu64 = (ne, ee, st.n_con, {b: st.pattern(b) for b in (1, 12, 2)},
+                 {b: st.K(b).copy() for b in (1, 12, 2)}, st.F().copy())
 
     # e2e through the C ABI with host buffers (pinned): U in, K blocks + F out
     e2e = None
@@ -469,6 +572,7 @@ def run_ours(args):
 
     # mixed precision path on the same workload
     mixed = None
+    gpu_mixed = None
     if not args.no_mixed:
         sm = FEStorage(mesh, "mixed", stream=stream.cuda_stream).initSolutionData()
         sm.setU_device(U_dev.data_ptr(), sm.n_total)
@@ -483,6 +587,7 @@ def run_ours(args):
         mkt, _ = sm.kernel_times()
         K64, K32 = st.K(2), sm.K(2)
         F64, F32 = st.F(), sm.F()
+        gpu_mixed = (K32, F32) if parity_job else None
         msec = max_over_ranks(msec, dist)
         mixed = {"value": replica_throughput(mesh.n_elems, msec, world), "unit": UNIT,
                  "ms_per_step": msec * 1e3, "speedup_vs_fp64": sec / msec, "autotuned": mtuned,
@@ -491,10 +596,10 @@ def run_ours(args):
                  "K_rel_err_vs_fp64": float(np.abs(K32 - K64).max() / np.abs(K64).max()),
                  "F_rel_err_vs_fp64": float(np.abs(F32 - F64).max() / np.abs(F64).max()),
                  "dtype": MIXED_DTYPE,
-                 "bound": "instruction issue and the shared-memory LSU path of the element "
-                          "kernel (ncu at 64,000 elements: issue 49%, LSU 53%, shared "
-                          "wavefronts 57%, FP64 pipe 20%, DRAM 8%)",
-                 "profile": "profiles/solid81_mixed_floatpair_block40_ncu.md"}
+                 "bound": "issue / latency of the element kernel: neither pipe nor DRAM "
+                          "saturates (see roofline; ncu at 64,000 elements: issue 42%, LSU "
+                          "44%, shared wavefronts 46%, FP64 pipe 50%, FP32 FMA 19%, DRAM 7%)",
+                 "profile": "profiles/solid81_mixed_fp64vol_block40_ncu.md"}
         sm.close()
 
     batched = None
@@ -511,9 +616,41 @@ def run_ours(args):
         # the consumer of the assembled K(2): its device LDL^T on the 139k-equation bar
         ldlt_leg = solver_bench(20, ("fp32-tc", "fp32", "fp64"))
 
+    parity = None
+    if parity_job:
+        parity = finish_parity(*parity_job, gpu64, gpu_mixed)
+
     if rank != 0:
         return
     fp64_peak = probe_fma_peak(True)
+    fp32_peak = probe_fma_peak(False)
+    if mixed:
+        # executed arithmetic of the mixed element kernel against the FMA
+        # probes of both pipes, and its warp-instruction issue rate against
+        # one instruction per cycle per scheduler
+        mel = mixed["kernel_ms"]["element"] * 1e-3
+        a32 = MIXED_FP32_FLOP_PER_ELEM * mesh.n_elems / mel
+        a64 = MIXED_FP64_FLOP_PER_ELEM * mesh.n_elems / mel
+        import torch as _t
+        sms = _t.cuda.get_device_properties(local).multi_processor_count
+        clk_mhz = (clk.summary().get("sm_mhz") or peaks_sm_mhz())
+        issue_peak = sms * 4 * clk_mhz * 1e6
+        ai = MIXED_WARP_INSTR_PER_ELEM * mesh.n_elems / mel
+        mixed["roofline"] = {
+            "bound": "issue", "kernel": "solid81_kernel<float>",
+            "achieved": ai / 1e9, "peak": issue_peak / 1e9, "unit": "G warp-instr/s",
+            "frac": ai / issue_peak,
+            "fp32": {"achieved": a32 / 1e12, "peak": fp32_peak / 1e12, "unit": "TFLOP/s",
+                     "frac": a32 / fp32_peak},
+            "fp64": {"achieved": a64 / 1e12, "peak": fp64_peak / 1e12, "unit": "TFLOP/s",
+                     "frac": a64 / fp64_peak},
+            "algorithmic": f"executed per element: {MIXED_FP32_FLOP_PER_ELEM} FP32 flop, "
+                           f"{MIXED_FP64_FLOP_PER_ELEM} FP64 flop, {MIXED_WARP_INSTR_PER_ELEM} "
+                           "warp instructions (ncu counters of a 64,000-element launch)",
+            "peak_source": "FP32 / FP64 FMA throughput probes in this run; issue: SMs x 4 "
+                           "schedulers x median SM clock during the timed region",
+            "traffic": (112.792064e6 + 123.714304e6) / 64000 * mesh.n_elems,
+            "traffic_source": "ncu dram bytes of a 64,000-element launch, scaled by elements"}
     elem_ms = float(kt[0])
     achieved = FLOP_PER_ELEM * mesh.n_elems / (elem_ms * 1e-3)
     peaks = {}
@@ -561,14 +698,57 @@ def run_ours(args):
                             "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
+        "ldlt": ldlt_leg,
+        "newton": newton,
         "mixed": mixed,
         "batched": batched,
-        "newton": newton,
-        "ldlt": ldlt_leg,
+        "parity": parity,
         "setup_s": setup_s,
         "element_status": {"flagged": int(count)},
     }
+    line["summary"] = compact_summary(line)
     print(json.dumps(line), flush=True)
+
+
+def peaks_sm_mhz():
+    try:
+        return float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["sm_max_mhz"])
+    except Exception:
+        return 2070.0
+
+
+def compact_summary(line):
+    """The headline numbers of every leg in a few hundred bytes, last in the
+    line (a reader of the line's tail sees them)."""
+    def r(x, d=3):
+        return None if x is None else round(float(x), d)
+    s = {"fp64_melem_s": r(line["value"], 2), "fp64_roofline_frac": r(line["roofline"]["frac"]),
+         "e2e_melem_s": r(line["e2e"]["value"], 2) if line.get("e2e") else None}
+    m = line.get("mixed")
+    if m:
+        s["mixed_melem_s"] = r(m["value"], 2)
+        s["mixed_speedup"] = r(m["speedup_vs_fp64"], 2)
+        if m.get("roofline"):
+            s["mixed_issue_frac"] = r(m["roofline"]["frac"])
+    b = line.get("batched")
+    if b:
+        s["batched_melem_s"] = r(b["value"], 2)
+    p = line.get("parity")
+    if p and "fp64" in p:
+        s["parity_fp64"] = {"K": p["fp64"]["K_rel"], "F": p["fp64"]["F_rel"],
+                            "pattern_equal": p["pattern_equal"]}
+        if "mixed" in p:
+            s["parity_mixed"] = {k: float(f"{v:.2e}") for k, v in p["mixed"].items()}
+    n = line.get("newton")
+    if n:
+        for fam in ("blocks", "bar"):
+            if fam in n:
+                s[f"newton_{fam}"] = {k: r(n[fam].get(k)) for k in ("plain", "learned")} | \
+                    {"mesh": n[fam].get("mesh")}
+    ld = line.get("ldlt")
+    if ld:
+        s["ldlt_s"] = {x["precision"]: r(x["value"], 4) for x in ld}
+    return s
 
 
 def cdb_model(name):

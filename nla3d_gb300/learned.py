@@ -424,43 +424,53 @@ def evaluate(problems, mlp, precision="fp64", linear_solver="direct",
     return res | {"steps": len(out[starts[0]]), "wall_s": wall}
 
 
-def benchmark(n_block_train=40, n_block_eval=8, n_bar_train=12, log=None):
+def benchmark(n_block_train=40, n_block_eval=8, n_bar_train=12, block_n=10, bar_nx=10,
+              linear_solver="gpu-fp32", log=None):
     """Newton iterations per load step, plain vs learned start, at a 1e-8
-    residual tolerance, on the two problem families (shrunk so that a run takes
-    about a minute on one GPU):
-      blocks: 4^3 SOLID81 on the unit cube, C10 ~ U(0.2, 1), K ~ U(500, 5000),
-              stretch ~ U(1, 2), 20 load steps (held-out seeds);
-      bar:    3x3x12 torsion + stretch bar (rigid-body MPC end) at C10 = 0.5,
-              K = 1000, stretch 2.0, 90 deg, 50 load steps, trained on bars with
-              C10 ~ U(0.3, 0.7), K ~ U(500, 2000), stretch ~ U(1.5, 2), twist
-              ~ U(45, 90) deg.
+    residual tolerance, on the two problem families, with K(2) factored on the
+    device (sized so that a run takes a minute or two on one GPU):
+      blocks: block_n^3 SOLID81 on the unit cube, C10 ~ U(0.2, 1), K ~ U(500,
+              5000), stretch ~ U(1, 2), 20 load steps; trained on n_block_train
+              solves, evaluated on n_block_eval held-out seeds;
+      bar:    bar_nx x bar_nx x 4 bar_nx torsion + stretch bar (rigid-body MPC
+              end) at C10 = 0.5, K = 1000, stretch 2.0, 90 deg, 50 load steps;
+              the network is trained on 3x3x12 bars with C10 ~ U(0.3, 0.7),
+              K ~ U(500, 2000), stretch ~ U(1.5, 2), twist ~ U(45, 90) deg (its
+              coarse modes live on the normalised geometry, so it carries over).
     Also FP64 vs mixed assembly iteration counts on that bar."""
     import time
     out = {}
     t0 = time.perf_counter()
-    X, Y, _ = generate(sample_block_problems(n_block_train, n=4, seed=11))
+    X, Y, _ = generate(sample_block_problems(n_block_train, n=block_n, seed=11),
+                       linear_solver=linear_solver)
     mlp = MLP(seed=0)
     h = mlp.fit(X, Y, epochs=300, batch=128, lr=2e-3)
-    out["blocks"] = evaluate(sample_block_problems(n_block_eval, n=4, seed=99), mlp)
+    out["blocks"] = evaluate(sample_block_problems(n_block_eval, n=block_n, seed=99), mlp,
+                             linear_solver=linear_solver)
     out["blocks"].update({"train_samples": int(X.shape[0]), "final_loss": h[-1][1],
-                          "mesh": "4x4x4 SOLID81", "load_steps": 20})
+                          "mesh": f"{block_n}x{block_n}x{block_n} SOLID81", "load_steps": 20,
+                          "train_solves": n_block_train})
     if log:
         log(f"blocks: {out['blocks']}")
-    Xb, Yb, _ = generate(sample_bar_problems(n_bar_train, nx=3, nz=12, seed=5, n_loadsteps=50))
+    Xb, Yb, _ = generate(sample_bar_problems(n_bar_train, nx=3, nz=12, seed=5, n_loadsteps=50),
+                         linear_solver=linear_solver)
     mlpb = MLP(seed=1)
     hb = mlpb.fit(Xb, Yb, epochs=300, batch=128, lr=2e-3)
-    cfg = bar_problem(3, 12, 0.5, 1000.0, 2.0, math.pi / 2, 50)
-    out["bar"] = evaluate([cfg], mlpb)
+    cfg = bar_problem(bar_nx, 4 * bar_nx, 0.5, 1000.0, 2.0, math.pi / 2, 50)
+    out["bar"] = evaluate([cfg], mlpb, linear_solver=linear_solver)
     out["bar"].update({"train_samples": int(Xb.shape[0]), "final_loss": hb[-1][1],
-                       "mesh": "3x3x12 SOLID81 + rigid-body MPC end", "load_steps": 50})
+                       "mesh": f"{bar_nx}x{bar_nx}x{4 * bar_nx} SOLID81 "
+                               f"({bar_nx * bar_nx * 4 * bar_nx} elements) + rigid-body MPC end",
+                       "load_steps": 50, "trained_on": "3x3x12 bars"})
     its = {}
     for precision in ("fp64", "mixed"):
         be = make_backend(cfg, precision)
-        s, _ = solve(cfg, be)
+        s, _ = solve(cfg, be, linear_solver=linear_solver)
         its[precision] = float(np.mean([r.iterations for r in s.records]))
     out["bar"]["iterations_fp64_assembly"] = its["fp64"]
     out["bar"]["iterations_mixed_assembly"] = its["mixed"]
     out["residual_tol"] = 1e-8
+    out["linear_solver"] = linear_solver
     out["seconds"] = time.perf_counter() - t0
     if log:
         log(f"bar: {out['bar']}")
