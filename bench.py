@@ -78,6 +78,10 @@ def parse():
     ap.add_argument("--model", choices=["3d_damper", "a2000"],
                     help="run one of the reference's BENCH models instead (minutes)")
     ap.add_argument("--model-backend", default="fp64", choices=["fp64", "mixed", "port"])
+    ap.add_argument("--cdb", metavar="PATH",
+                    help="read the --model mesh from this .cdb file (the reference's "
+                         "test/3d_damper/model.cdb or test/a2000_damper/a2000.cdb) with the "
+                         "library's reader instead of the committed fixture")
     ap.add_argument("--solver-bench", type=int, default=0, metavar="NX",
                     help="time the device LDL^T of K(2) on the NX x NX x 4NX rigid-body bar "
                          "(40: the 1.07M-equation Newton bar) and exit")
@@ -751,14 +755,28 @@ def compact_summary(line):
     return s
 
 
-def cdb_model(name):
-    """A reference BENCH model from its committed fixture (tests/golden/):
+def cdb_model(name, cdb_path=None):
+    """A reference BENCH model, from a .cdb file read by the library's reader
+    (nla3d_gb300.cdb, as main.cpp:167-225 builds it) or from its committed
+    fixture (tests/golden/, written from the same file):
     3d_damper (test/CMakeLists.txt:148-153): 7016 SOLID81, Neo-Hookean
     (10, 5000), 497 CE equations, UY reaction of TOP_SIDE, threshold 3.0;
     a2000 (test/CMakeLists.txt:141-146): 3101 PLANE41, Neo-Hookean (1, 500),
     UY reaction of DISP_BC, threshold 0.2.  Returns (mesh, fixes, reaction
-    nodes, ANSYS curve, threshold)."""
+    nodes, ANSYS curve, threshold).  The ANSYS curve always comes from the
+    fixture."""
     from nla3d_gb300 import meshgen as mg
+    if cdb_path:
+        from nla3d_gb300 import cdb
+        md = cdb.read_cdb(cdb_path)
+        fx = "damper_3d.npz" if name == "3d_damper" else "a2000_plane41.npz"
+        curve = np.load(os.path.join(ROOT, "tests", "golden", fx))["ref_curve"]
+        if name == "3d_damper":
+            m, fixes, _ = cdb.to_mesh(md, mg.ELEM_SOLID81, mg.MAT_NEO_HOOKEAN, (10.0, 5000.0),
+                                      name=name)
+            return m, fixes, np.array(md.feComps["TOP_SIDE"].list, np.uint32), curve, 3.0
+        m, fixes, _ = cdb.to_mesh(md, mg.ELEM_PLANE41, mg.MAT_NEO_HOOKEAN, (1.0, 500.0), name=name)
+        return m, fixes, np.array(md.feComps["DISP_BC"].list, np.uint32), curve, 0.2
     if name == "3d_damper":
         g = np.load(os.path.join(ROOT, "tests", "golden", "damper_3d.npz"))
         m = mg.Mesh(mg.ELEM_SOLID81, g["xyz"], g["conn"], mat_id=mg.MAT_NEO_HOOKEAN,
@@ -787,7 +805,7 @@ def run_cdb_model(args):
     --model-backend port) and the K(2) solve of --model-solver.
     Prints one JSON line."""
     from nla3d_gb300.newton import NewtonSolver
-    mesh, fixes, nodes, ref, thr = cdb_model(args.model)
+    mesh, fixes, nodes, ref, thr = cdb_model(args.model, args.cdb)
     if args.model_backend == "port":
         from oracle import oracle as O
         b = O.OracleModel(mesh, "port")

@@ -14,7 +14,6 @@ stores SHA-256 digests of the exact bytes plus a few norms.
 """
 import hashlib
 import os
-import re
 import sys
 
 import numpy as np
@@ -121,125 +120,18 @@ def read_rigid_body_case(cdb_path, curve_path):
     return nodes, elems, comps, fixes, curve
 
 
-DOF_LABELS = ["UX", "UY", "UZ", "ROTX", "ROTY", "ROTZ", "HYDRO_PRESSURE", "TEMP"]
-
-
-def _widths(fmt):
-    """Field widths of an ANSYS fixed format such as (3i9,6e20.13) or (19i9)."""
-    fmt = fmt.strip().lower()
-    m = re.fullmatch(r"\((\d+)i(\d+)(?:,(\d+)e(\d+)\.[0-9e]+)?\)", fmt)
-    if not m:
-        raise ValueError(f"format {fmt!r}")
-    w = [int(m.group(2))] * int(m.group(1))
-    if m.group(3):
-        w += [int(m.group(4))] * int(m.group(3))
-    return w
-
-
-def _split(line, widths):
-    out, pos = [], 0
-    for w in widths:
-        field = line[pos:pos + w]
-        if not field.strip():
-            break
-        out.append(field)
-        pos += w
-    return out
-
-
 def read_cdb(path):
-    """An ANSYS .cdb as the reference's readCdbFile (FEReaders.cpp:330-729)
-    reads it: NBLOCK nodes, SOLID EBLOCK elements (TYPE attribute kept), D
-    fixed DoFs with numeric node and value, CE equations (terms two per
-    line), CMBLOCK node components (names starting with '_' skipped), then
-    MeshData::compressNumbers (FEReaders.cpp:35-80) if the node numbers are
-    not 1..n."""
-    lines = open(path).read().splitlines()
-    node_ids, xyz, cells, ctype, fixes, mpcs, comps = [], [], [], [], [], [], {}
-    loads = []
-    i = 0
-    first = lambda t: t.lstrip()[:1]  # noqa: E731
-    while i < len(lines):
-        tok = [t.strip() for t in lines[i].split(",")]
-        key = tok[0].upper()
-        if key == "NBLOCK":
-            w = _widths(lines[i + 1])
-            i += 2
-            while i < len(lines) and first(lines[i]) not in ("-", "N"):
-                v = _split(lines[i], w)
-                node_ids.append(int(v[0]))
-                pos = [0.0, 0.0, 0.0]
-                for k in range(3):
-                    if len(v) > 3 + k:
-                        pos[k] = float(v[3 + k])
-                xyz.append(pos)
-                i += 1
-            continue
-        if key == "EBLOCK":
-            assert tok[2].upper() == "SOLID"
-            w = _widths(lines[i + 1])
-            i += 2
-            while i < len(lines) and first(lines[i]) not in ("-", "N"):
-                v = [int(f) for f in _split(lines[i], w)]
-                n_nodes = v[8]
-                assert len(v) == 11 + n_nodes
-                cells.append(v[11:11 + n_nodes])
-                ctype.append(v[1])
-                i += 1
-            continue
-        if key == "D":
-            try:
-                fixes.append((int(tok[1]), DOF_LABELS.index(tok[2].upper()), float(tok[3])))
-            except ValueError:
-                pass   # 'ALL' etc.: not a numeric node
-        elif key == "F":
-            # FEReaders.cpp:677-704: HEAT -> TEMP, FX/FY/FZ -> UX/UY/UZ, else a DoF label
-            try:
-                node, val = int(tok[1]), float(tok[3])
-            except ValueError:
-                node = None
-            if node is not None:
-                lab = tok[2].upper()
-                lab = {"HEAT": "TEMP", "FX": "UX", "FY": "UY", "FZ": "UZ"}.get(lab, lab)
-                loads.append((node, DOF_LABELS.index(lab), val))
-        elif key == "CE":
-            b, n_terms = float(tok[5]), int(tok[3])
-            terms = []
-            while n_terms > 0:
-                i += 1
-                t = [x.strip() for x in lines[i].split(",")]
-                for k in range(max(n_terms, 2)):
-                    terms.append((int(t[3 + 3 * k]), DOF_LABELS.index(t[4 + 3 * k].upper()),
-                                  float(t[5 + 3 * k])))
-                    n_terms -= 1
-            mpcs.append((terms, b))
-        elif key == "CMBLOCK" and not tok[1].startswith("_"):
-            n_ranges = int(tok[3].split("!")[0])
-            w = _widths(lines[i + 1])
-            i += 2
-            vals = []
-            while len(vals) < n_ranges:
-                vals += [int(f) for f in _split(lines[i], w)]
-                i += 1
-            lst = []
-            for k, v in enumerate(vals[:n_ranges]):
-                if v > 0:
-                    lst.append(v)
-                else:
-                    lst.extend(range(vals[k - 1] + 1, -v + 1))
-            comps[tok[1]] = lst
-            continue
-        i += 1
-    # compressNumbers
-    if len(node_ids) != max(node_ids):
-        old2new = {o: k + 1 for k, o in enumerate(node_ids)}
-        cells = [[old2new[n] for n in c] for c in cells]
-        fixes = [(old2new[n], d, v) for n, d, v in fixes]
-        loads = [(old2new[n], d, v) for n, d, v in loads]
-        mpcs = [([(old2new[n], d, c) for n, d, c in terms], b) for terms, b in mpcs]
-        comps = {k: [old2new[n] for n in v] for k, v in comps.items()}
-    return {"xyz": np.array(xyz), "cells": cells, "type": ctype, "fixes": fixes,
-            "mpcs": mpcs, "comps": comps, "loads": loads}
+    """An ANSYS .cdb through the library's reader (nla3d_gb300.cdb, which
+    follows readCdbFile, FEReaders.cpp:321-729, and compressNumbers,
+    FEReaders.cpp:35-80), as plain lists: node positions, cells with their
+    TYPE attribute, fixed DoFs, loads, CE equations and node components."""
+    from nla3d_gb300 import cdb
+    md = cdb.read_cdb(path)
+    return {"xyz": md.nodes_array(), "cells": md.cellNodes, "type": md.cellIntData["TYPE"],
+            "fixes": [(f.node, f.node_dof, f.value) for f in md.fixBcs],
+            "loads": [(f.node, f.node_dof, f.value) for f in md.loadBcs],
+            "mpcs": [([(t.node, t.node_dof, t.coef) for t in m.eq], m.b) for m in md.mpcs],
+            "comps": {k: list(v.list) for k, v in md.feComps.items()}}
 
 
 def read_ref_curve(path):
