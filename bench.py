@@ -34,12 +34,12 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 # FP64 flop per SOLID81 element of the algorithm the kernel runs (8 Gauss
-# points x 4402: kinematics 189, material + S + wDd 436, -wFS / w cof F 96,
-# tangent tensor A 513, h_a = A^T G_a 1080, F_u + K_up 288, K_uu 1800).  The
-# executed FP64 instruction counters of one ncu capture give the same figure
-# (2 DFMA + DMUL + DADD = 35,216 per element).  The Bh^T D Bh formulation
-# costs 69,072 (8 x 8634) for the same element.
-FLOP_PER_ELEM = 35216
+# points x 4042: kinematics 189, material + S + wDd 436, -wFS / w cof F 96,
+# tangent tensor A 513, h_a = A^T G_a for the 6 blocks i <= k 720, F_u + K_up
+# 288, K_uu 1800).  The executed FP64 instruction counters of one ncu capture
+# give 32,432 per element (2 DFMA + DMUL + DADD); that figure is used.  The
+# Bh^T D Bh formulation costs 69,072 (8 x 8634) for the same element.
+FLOP_PER_ELEM = 32432
 FLOP_PER_ELEM_BTDB = 69072
 # DRAM bytes per element of solid81_kernel<double> and of the K gather in one
 # ncu capture of a 40^3 block (64,000 elements, 9,675,406 K slots), used to

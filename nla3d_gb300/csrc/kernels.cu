@@ -17,8 +17,11 @@
 //   Kuu(a,i; b,k) += sum_{L,N} G_aL A[iL][kN] G_bN,
 //   A[iL][kN] = sum_{J,M} F_iJ wDd'[(JL)][(MN)] F_kM + delta_ik w S_LN,
 // so one Gauss point costs 45 entries of A (about 300 FMA), h_a[ik] = A^T G_a
-// per node (81 FMA) and 3 FMA per Kuu entry, instead of 6 + the geometric term
-// per entry and D Bh per node.  These are the reference's products with the
+// per node and 3 FMA per Kuu entry, instead of 6 + the geometric term per
+// entry and D Bh per node.  Since A is symmetric, K(a,i; b,k) = h_b[ki] . G_a
+// as well, so h is formed only for i <= k (6 of the 9 blocks, 54 FMA per
+// node) and the entries with i > k (off-diagonal node blocks only) read
+// h_b[ki] and G_a.  These are the reference's products with the
 // structural zeros of B, B_NL and Omega removed and the sums regrouped; they
 // agree with the reference to rounding (the tests bound the difference at
 // 1e-12 relative).
@@ -53,26 +56,39 @@ struct ResidualType<float> {
   using type = float2;
 };
 
-// Stride of one (i, k) block of h in the warp scratch.  In the mixed kernel
-// a warp's Kuu loads read h at up to six (i, k) blocks with the same slot a;
-// a stride of 97 floats puts them in different banks (96 made them a 3-way
-// bank conflict that bounded the kernel).  The FP64 kernel keeps 96.
+// Offset of (i, k) block number hb of h in the warp scratch (each block is
+// 3 N x 32 slots).  One warp-wide Kuu load reads 32 consecutive entries of
+// the assemble3 order, which touch up to six blocks at several node slots;
+// in the mixed kernel the block offsets below (found by enumerating that
+// access pattern) put those reads in distinct banks: 39 shared-memory
+// wavefronts for the 38 loads of a lane's entries, against 120 with a plain
+// stride of 97 floats and 187 with 96.  The FP64 kernel, bound by its FP64
+// pipe, keeps a stride of 96 doubles.
 template <typename TT>
-struct HStride {
-  static constexpr int value = 96;
+struct HLayout {
+  __device__ __host__ static constexpr int offset(int hb) { return 96 * hb; }
+  static constexpr int size = 96 * 6;
 };
 template <>
-struct HStride<float> {
-  static constexpr int value = 97;
+struct HLayout<float> {
+  __device__ __host__ static constexpr int offset(int hb) {
+    return hb == 0 ? 0 : hb == 1 ? 115 : hb == 2 ? 236 : hb == 3 ? 348 : hb == 4 ? 451 : 574;
+  }
+  static constexpr int size = 574 + 96;
 };
+
+// the (i, k) blocks of h that are formed: i <= k, packed (6 blocks)
+__host__ __device__ constexpr int hblock(int i, int k) {  // i <= k
+  return 3 * i - (i * (i - 1)) / 2 + (k - i);
+}
 
 template <typename TT>
 struct WarpSmem {
   typename ResidualType<TT>::type wP[9][32];  // per (element q, Gauss point g): -w F S
   TT wCof[9][32];      //  w cof(F)
   TT A[45][32];        //  symmetric 9x9 tangent tensor A[iL][kN], packed upper
-  TT H[9 * HStride<TT>::value];  // per (element q, node a) at the current Gauss point:
-                       //  h_a[ik][N] at (3i+k) * HStride + 32 N + slot
+  TT H[HLayout<TT>::size];  // per (element q, node a) at the current Gauss point:
+                       //  h_a[ik][N], i <= k, at HLayout::offset(hblock(i,k)) + 32 N + slot
   TT G[3][32];         //  G_a
 };
 
@@ -86,7 +102,7 @@ template <>
 struct WarpSmem<float> {
   float A[45][32];
   union {
-    float H[9 * HStride<float>::value];
+    float H[HLayout<float>::size];
     struct {
       float2 wP[9][32];     // -w F S, float pairs
       double wCof[9][32];   // w cof F, FP64
@@ -524,8 +540,11 @@ __global__ void __launch_bounds__(WPB * 32)
     if (x < kEPW * kKuuPerElem) {
       const int q = x / kKuuPerElem, t = x - q * kKuuPerElem;
       const uchar4 en = c_kuu_entry[t];  // (a, i, b, k)
-      const uint32_t ho = (en.y * 3 + en.w) * HStride<TT>::value + q * 8 + en.x;
-      const uint32_t go = q * 8 + en.z;
+      // i <= k: h_a[ik] . G_b;  i > k: h_b[ki] . G_a (A symmetric)
+      const bool up = en.y <= en.w;
+      const uint32_t hb = up ? hblock(en.y, en.w) : hblock(en.w, en.y);
+      const uint32_t ho = HLayout<TT>::offset(hb) + q * 8 + (up ? en.x : en.z);
+      const uint32_t go = q * 8 + (up ? en.z : en.x);
       word = ho | (go << 16);
     }
     dec[m * 32 + l] = word;
@@ -895,10 +914,10 @@ __global__ void __launch_bounds__(WPB * 32)
 #pragma unroll
         for (int i = 0; i < 3; i++)
 #pragma unroll
-          for (int k = 0; k < 3; k++)
+          for (int k = i; k < 3; k++)
 #pragma unroll
             for (int N = 0; N < 3; N++)
-              sm->H[(3 * i + k) * HStride<TT>::value + 32 * N + lane] =
+              sm->H[HLayout<TT>::offset(hblock(i, k)) + 32 * N + lane] =
                   gg[0] * sm->A[sym9(3 * i + 0, 3 * k + N)][s1] +
                   gg[1] * sm->A[sym9(3 * i + 1, 3 * k + N)][s1] +
                   gg[2] * sm->A[sym9(3 * i + 2, 3 * k + N)][s1];
