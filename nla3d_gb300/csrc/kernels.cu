@@ -46,6 +46,14 @@ constexpr double kGaussA = 0.5773502691896258;        // isoparametric.h:127
 // Kuu entry t (assemble3 order, SOLID81.h:62-74) -> (a, i, b, k) packed.
 __constant__ uchar4 c_kuu_entry[kKuuPerElem];
 
+// Mixed kernel: position in assemble3 order of the Kuu entry that
+// D[(i,k), a, b] = sum h_a[ik] . G_b (i <= k) stands for, at [(a * 6 +
+// hblock(i,k)) * 8 + b]: K(a,i; b,k) when a <= b, K(b,k; a,i) when a > b;
+// 0xFFFF where a > b and i == k (the same entry as D[(i,i), b, a]).
+constexpr int kDpos = 8 * 6 * 8;
+constexpr size_t kDposBytes = kDpos * sizeof(uint16_t);
+__constant__ uint16_t c_dpos[kDpos];
+
 // -w F S: FP64, or a float pair (hi, lo) in the mixed kernel
 template <typename TT>
 struct ResidualType {
@@ -56,26 +64,9 @@ struct ResidualType<float> {
   using type = float2;
 };
 
-// Offset of (i, k) block number hb of h in the warp scratch (each block is
-// 3 N x 32 slots).  One warp-wide Kuu load reads 32 consecutive entries of
-// the assemble3 order, which touch up to six blocks at several node slots;
-// in the mixed kernel the block offsets below (found by enumerating that
-// access pattern) put those reads in distinct banks: 39 shared-memory
-// wavefronts for the 38 loads of a lane's entries, against 120 with a plain
-// stride of 97 floats and 187 with 96.  The FP64 kernel, bound by its FP64
-// pipe, keeps a stride of 96 doubles.
-template <typename TT>
-struct HLayout {
-  __device__ __host__ static constexpr int offset(int hb) { return 96 * hb; }
-  static constexpr int size = 96 * 6;
-};
-template <>
-struct HLayout<float> {
-  __device__ __host__ static constexpr int offset(int hb) {
-    return hb == 0 ? 0 : hb == 1 ? 115 : hb == 2 ? 236 : hb == 3 ? 348 : hb == 4 ? 451 : 574;
-  }
-  static constexpr int size = 574 + 96;
-};
+// FP64 kernel: stride of one (i, k) block of h (3 N x 32 slots) in the warp
+// scratch.
+constexpr int kHStride = 96;
 
 // the (i, k) blocks of h that are formed: i <= k, packed (6 blocks)
 __host__ __device__ constexpr int hblock(int i, int k) {  // i <= k
@@ -87,22 +78,23 @@ struct WarpSmem {
   typename ResidualType<TT>::type wP[9][32];  // per (element q, Gauss point g): -w F S
   TT wCof[9][32];      //  w cof(F)
   TT A[45][32];        //  symmetric 9x9 tangent tensor A[iL][kN], packed upper
-  TT H[HLayout<TT>::size];  // per (element q, node a) at the current Gauss point:
-                       //  h_a[ik][N], i <= k, at HLayout::offset(hblock(i,k)) + 32 N + slot
+  TT H[6 * kHStride];  // per (element q, node a) at the current Gauss point:
+                       //  h_a[ik][N], i <= k, at hblock(i,k) * kHStride + 32 N + slot
   TT G[3][32];         //  G_a
 };
 
 // Mixed kernel: -w F S (float pairs) and w cof F (FP64: the pressure
 // coupling K_up keeps FP64) are only needed between phase 1 and the residual
 // / coupling pass that precedes the Gauss point loop, so they share their
-// bytes with h, which that loop writes later.  Per (element q, Gauss point g)
-// they sit at slot g * 4 + q, so the pass's broadcast reads of one Gauss
-// point hit four consecutive words.
+// bytes with the staging buffer of the Kuu write after that loop.  Per
+// (element q, Gauss point g) they sit at slot g * 4 + q, so the pass's
+// broadcast reads of one Gauss point hit four consecutive words.  h stays in
+// registers (each lane keeps its own node's).
 template <>
 struct WarpSmem<float> {
   float A[45][32];
   union {
-    float H[HLayout<float>::size];
+    float stage[4 * 300];   // the quad's Kuu entries in assemble3 order, for the write
     struct {
       float2 wP[9][32];     // -w F S, float pairs
       double wCof[9][32];   // w cof F, FP64
@@ -522,13 +514,19 @@ template <typename TT, int WPB>
 __global__ void __launch_bounds__(WPB * 32)
     solid81_kernel(const Solid81Args a) {
   if (a.skip && *a.skip) return;
+  constexpr bool kMixed = std::is_same<TT, float>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  // block header: the FP64 kernel's Kuu ownership words, the mixed kernel's
+  // D -> assemble3 position table
   uint32_t* dec = reinterpret_cast<uint32_t*>(smem_raw);  // [kOwned][32]
-  WarpSmem<TT>* sm =
-      reinterpret_cast<WarpSmem<TT>*>(smem_raw + sizeof(uint32_t) * kOwned * 32) +
-      (threadIdx.x >> 5);
+  uint16_t* dpos = reinterpret_cast<uint16_t*>(smem_raw);  // [kDpos]
+  constexpr size_t kHead = kMixed ? kDposBytes : sizeof(uint32_t) * kOwned * 32;
+  WarpSmem<TT>* sm = reinterpret_cast<WarpSmem<TT>*>(smem_raw + kHead) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
 
+  if constexpr (kMixed) {
+    for (int v = threadIdx.x; v < kDpos; v += blockDim.x) dpos[v] = c_dpos[v];
+  } else
   // Ownership of Kuu entries: lane owns x = lane + 32 m of the 4*300 entries
   // of its warp's element quad.  Decode once: smem offsets of H[ik][.][slot a]
   // and G[.][slot b].
@@ -543,7 +541,7 @@ __global__ void __launch_bounds__(WPB * 32)
       // i <= k: h_a[ik] . G_b;  i > k: h_b[ki] . G_a (A symmetric)
       const bool up = en.y <= en.w;
       const uint32_t hb = up ? hblock(en.y, en.w) : hblock(en.w, en.y);
-      const uint32_t ho = HLayout<TT>::offset(hb) + q * 8 + (up ? en.x : en.z);
+      const uint32_t ho = hb * kHStride + q * 8 + (up ? en.x : en.z);
       const uint32_t go = q * 8 + (up ? en.z : en.x);
       word = ho | (go << 16);
     }
@@ -566,7 +564,6 @@ __global__ void __launch_bounds__(WPB * 32)
     const uint32_t ec = valid ? e : E - 1;
 
     // ---------------- phase 1: lane = (element q, Gauss point g) ----------------
-    constexpr bool kMixed = std::is_same<TT, float>::value;
     double Fp_part = 0.0, Kpp_part = 0.0;  // FP64 in both kernels
     {
       const int g = sub;
@@ -878,6 +875,75 @@ __global__ void __launch_bounds__(WPB * 32)
     }
 
     // ---------------- phases 2 + 3 per Gauss point ----------------
+    if constexpr (kMixed) {
+      // Lane (q, a) keeps h_a[ik] (i <= k, its own node) in registers and
+      // accumulates D[(ik), a, b] = sum_g h_a[ik] . G_b for all 8 nodes b:
+      // 48 sums of 3 FMA per Gauss point from 3 shared loads per node b.
+      // The 48 cover the element's 300 Kuu entries (the 84 D[(ii), a, b],
+      // a > b, repeat D[(ii), b, a] and are not written).
+      float acc[6][8];
+#pragma unroll
+      for (int c = 0; c < 6; c++)
+#pragma unroll
+        for (int b = 0; b < 8; b++) acc[c][b] = 0.0f;
+      for (int g = 0; g < 8; g++) {
+        const int s1 = q * 8 + g;
+        const uint64_t tg = (uint64_t)ec * 8 + g;
+        // phase 2: the tangent uses the high parts of G
+        const float g0 = __ldg(a.Gdf + (3 * sub + 0) * E8 + tg).x;
+        const float g1 = __ldg(a.Gdf + (3 * sub + 1) * E8 + tg).x;
+        const float g2 = __ldg(a.Gdf + (3 * sub + 2) * E8 + tg).x;
+        float h[6][3];
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+          for (int k = i; k < 3; k++)
+#pragma unroll
+            for (int N = 0; N < 3; N++)
+              h[hblock(i, k)][N] = g0 * sm->A[sym9(3 * i + 0, 3 * k + N)][s1] +
+                                   g1 * sm->A[sym9(3 * i + 1, 3 * k + N)][s1] +
+                                   g2 * sm->A[sym9(3 * i + 2, 3 * k + N)][s1];
+        sm->G[0][lane] = g0;
+        sm->G[1][lane] = g1;
+        sm->G[2][lane] = g2;
+        __syncwarp();
+        // phase 3
+#pragma unroll
+        for (int b = 0; b < 8; b++) {
+          const float b0 = sm->G[0][q * 8 + b], b1 = sm->G[1][q * 8 + b],
+                      b2 = sm->G[2][q * 8 + b];
+#pragma unroll
+          for (int c = 0; c < 6; c++) {
+            float v = acc[c][b];
+            v = fmaf(h[c][0], b0, v);
+            v = fmaf(h[c][1], b1, v);
+            v = fmaf(h[c][2], b2, v);
+            acc[c][b] = v;
+          }
+        }
+        __syncwarp();
+      }
+      // stage the quad's 4 x 300 entries in assemble3 order, then write them
+      // coalesced (the stage shares its bytes with -w F S / w cof F, dead now)
+#pragma unroll
+      for (int c = 0; c < 6; c++)
+#pragma unroll
+        for (int b = 0; b < 8; b++) {
+          const uint32_t pos = dpos[(sub * 6 + c) * 8 + b];
+          if (pos != 0xFFFFu) sm->stage[q * kKuuPerElem + pos] = acc[c][b];
+        }
+      __syncwarp();
+#pragma unroll 4
+      for (int m = 0; m < kOwned; m++) {
+        const int x = lane + 32 * m;
+        if (x < kEPW * kKuuPerElem) {
+          const int qq = x / kKuuPerElem, t = x - qq * kKuuPerElem;
+          const uint32_t ee = e0 + qq;
+          if (ee < E) a.contribK[kdst((uint64_t)ee * kSolidKc + t)] = f2d(sm->stage[x]);
+        }
+      }
+      __syncwarp();
+    } else {
     TT acc[kOwned];
 #pragma unroll
     for (int m = 0; m < kOwned; m++) acc[m] = (TT)0;
@@ -917,7 +983,7 @@ __global__ void __launch_bounds__(WPB * 32)
           for (int k = i; k < 3; k++)
 #pragma unroll
             for (int N = 0; N < 3; N++)
-              sm->H[HLayout<TT>::offset(hblock(i, k)) + 32 * N + lane] =
+              sm->H[hblock(i, k) * kHStride + 32 * N + lane] =
                   gg[0] * sm->A[sym9(3 * i + 0, 3 * k + N)][s1] +
                   gg[1] * sm->A[sym9(3 * i + 1, 3 * k + N)][s1] +
                   gg[2] * sm->A[sym9(3 * i + 2, 3 * k + N)][s1];
@@ -950,13 +1016,10 @@ __global__ void __launch_bounds__(WPB * 32)
       if (x < kEPW * kKuuPerElem) {
         const int qq = x / kKuuPerElem, t = x - qq * kKuuPerElem;
         const uint32_t ee = e0 + qq;
-        if (ee < E) {
-          if constexpr (kMixed) a.contribK[kdst((uint64_t)ee * kSolidKc + t)] = f2d(acc[m]);
-          else a.contribK[kdst((uint64_t)ee * kSolidKc + t)] = (double)acc[m];
-        }
+        if (ee < E) a.contribK[kdst((uint64_t)ee * kSolidKc + t)] = acc[m];
       }
     }
-    if (!kMixed && valid) {
+    if (valid) {
       const uint64_t kb = (uint64_t)e * kSolidKc, fb = (uint64_t)e * kSolidFc;
 #pragma unroll
       for (int i = 0; i < 3; i++) {
@@ -969,6 +1032,7 @@ __global__ void __launch_bounds__(WPB * 32)
       }
     }
     __syncwarp();
+    }  // FP64 kernel
   }
 }
 
@@ -1448,6 +1512,20 @@ cudaError_t ensure_tables() {
                                (unsigned char)dj);
         }
   err = cudaMemcpyToSymbol(c_kuu_entry, h, sizeof(h));
+  if (err != cudaSuccess) return err;
+  // D[(i,k), a, b] -> assemble3 position (see c_dpos)
+  int tpos[8][3][8][3];
+  for (int u = 0; u < kKuuPerElem; u++) tpos[h[u].x][h[u].y][h[u].z][h[u].w] = u;
+  uint16_t dp[kDpos];
+  for (int a = 0; a < 8; a++)
+    for (int i = 0; i < 3; i++)
+      for (int k = i; k < 3; k++)
+        for (int b = 0; b < 8; b++) {
+          const int at = (a * 6 + hblock(i, k)) * 8 + b;
+          if (a <= b) dp[at] = (uint16_t)tpos[a][i][b][k];
+          else dp[at] = i == k ? (uint16_t)0xFFFF : (uint16_t)tpos[b][k][a][i];
+        }
+  err = cudaMemcpyToSymbol(c_dpos, dp, sizeof(dp));
   if (err == cudaSuccess) g_tables_ready[dev].store(true, std::memory_order_release);
   return err;
 }
@@ -1455,8 +1533,8 @@ cudaError_t ensure_tables() {
 }  // namespace
 
 size_t solid81_smem_bytes_wpb(bool mixed, int wpb) {
-  const size_t dec = sizeof(uint32_t) * kOwned * 32;
-  return dec + wpb * (mixed ? sizeof(WarpSmem<float>) : sizeof(WarpSmem<double>));
+  const size_t head = mixed ? kDposBytes : sizeof(uint32_t) * kOwned * 32;
+  return head + wpb * (mixed ? sizeof(WarpSmem<float>) : sizeof(WarpSmem<double>));
 }
 
 size_t solid81_smem_bytes(bool mixed) { return solid81_smem_bytes_wpb(mixed, kWarpsPerBlock); }
