@@ -94,8 +94,13 @@ def parse():
     ap.add_argument("--learned-blocks", type=int, default=0, metavar="N",
                     help="learned-start study on N^3 blocks (20: the configured size) with "
                          "K(2) factored on the device; prints one JSON line and exits")
-    ap.add_argument("--learned-train", type=int, default=120)
-    ap.add_argument("--learned-eval", type=int, default=16)
+    ap.add_argument("--learned-train", type=int, default=2000)
+    ap.add_argument("--learned-eval", type=int, default=100)
+    ap.add_argument("--learned-batch", type=int, default=100,
+                    help="solves advanced in lock step by one batched Newton driver")
+    ap.add_argument("--learned-curve", default="50,200,500,1000",
+                    help="training-set sizes (solves) for the iterations-saved curve")
+    ap.add_argument("--learned-epochs", type=int, default=150)
     ap.add_argument("--newton-solver", default="gpu-fp32", choices=["gpu", "gpu-fp32", "gpu-tc"],
                     help="K(2) solve of --newton-bar and --learned-blocks")
     ap.add_argument("--newton-assembly", default="fp64,mixed",
@@ -959,34 +964,62 @@ def run_newton_bar(args):
 def run_learned_blocks(args):
     """The learned Newton start on n^3 blocks (Neo-Hookean, C10 ~ U(0.2, 1),
     K ~ U(500, 5000), target stretch ~ U(1, 2), 20 load steps, residual
-    1e-8), K(2) factored on the device (FP32 fronts, FP64 refinement): the
-    MLP (4 x 256, BF16 weights, FP32 accumulation) is trained by the
-    library's kernels on the converged increments of `--learned-train`
-    solves and evaluated on `--learned-eval` held-out ones against the plain
-    and the secant-extrapolation starts."""
+    1e-8), K(2) factored on the device.  Solves run `--learned-batch` at a
+    time in lock step (nla3d_gb300.batch_newton: one batched assembly, one
+    block-diagonal LDL^T per Newton iteration).  The MLP (4 x 256, BF16
+    weights, FP32 accumulation) is trained by the library's kernels on the
+    converged increments of the first N of `--learned-train` plain-start
+    solves, for each N of `--learned-curve`, and evaluated on
+    `--learned-eval` held-out solves against the plain and the
+    secant-extrapolation starts."""
     from nla3d_gb300 import learned as L
     n = args.learned_blocks
+    fronts = {"gpu": "fp64", "gpu-fp32": "fp32", "gpu-tc": "fp32-tc"}[args.newton_solver]
     log = lambda m: print(m, file=sys.stderr, flush=True)  # noqa: E731
+    solvers = {}
     t0 = time.perf_counter()
-    X, Y, its = L.generate(L.sample_block_problems(args.learned_train, n=n, seed=11),
-                           linear_solver=args.newton_solver)
+    X, Y, its, failed, owner = L.generate_batched(
+        L.sample_block_problems(args.learned_train, n=n, seed=11), fronts=fronts,
+        batch_size=args.learned_batch, log=log, solvers=solvers)
     t_gen = time.perf_counter() - t0
     log(f"generated {X.shape[0]} samples from {args.learned_train} solves in {t_gen:.1f} s")
-    mlp = L.MLP(seed=0)
-    hist = mlp.fit(X, Y, epochs=300, batch=128, lr=2e-3)
-    t_fit = time.perf_counter() - t0 - t_gen
-    res = L.evaluate(L.sample_block_problems(args.learned_eval, n=n, seed=99), mlp,
-                     linear_solver=args.newton_solver, log=None)
+    held_out = L.sample_block_problems(args.learned_eval, n=n, seed=99)
+    base = L.evaluate_batched(held_out, None, fronts=fronts, batch_size=args.learned_batch,
+                              starts=("plain", "extrapolation"), log=log, solvers=solvers)
+    sizes = sorted({int(v) for v in args.learned_curve.split(",") if v and
+                    int(v) < args.learned_train} | {args.learned_train})
+    curve = []
+    for size in sizes:
+        sel = owner < size
+        t1 = time.perf_counter()
+        mlp = L.MLP(seed=0)
+        hist = mlp.fit(X[sel], Y[sel], epochs=args.learned_epochs, batch=128, lr=2e-3)
+        t_fit = time.perf_counter() - t1
+        res = L.evaluate_batched(held_out, mlp, fronts=fronts, batch_size=args.learned_batch,
+                                 starts=("learned",), log=log, solvers=solvers)
+        curve.append({"train_solves": size, "train_samples": int(sel.sum()),
+                      "learned": res["learned"], "learned_used": res["learned_used"],
+                      "saved_vs_plain": base["plain"] - res["learned"],
+                      "failed": res["failed"]["learned"], "final_loss": hist[-1][1],
+                      "fit_s": t_fit, "eval_s": res["wall_s"]["learned"]})
+        log(f"trained on {size} solves: {curve[-1]}")
+    full = curve[-1]
     print(json.dumps({
         "metric": "Newton iterations per load step (residual 1e-8), learned vs plain start",
         "unit": "iterations", "higher_is_better": False,
         "workload": f"{n}^3 SOLID81 blocks (C10 ~ U(0.2,1), K ~ U(500,5000), stretch ~ U(1,2)), "
                     "20 load steps",
         "train_solves": args.learned_train, "train_samples": int(X.shape[0]),
-        "train_plain_iterations": float(np.mean([np.mean(i) for i in its])),
-        "final_loss": hist[-1][1], "eval_solves": args.learned_eval, "results": res,
-        "generate_s": t_gen, "fit_s": t_fit, "wall_s": time.perf_counter() - t0,
-        "linear_solver": f"device LDL^T ({args.newton_solver}), FP64 refinement"}), flush=True)
+        "train_failed": failed, "train_plain_iterations": float(np.mean(its)),
+        "eval_solves": args.learned_eval,
+        "plain": base["plain"], "extrapolation": base["extrapolation"],
+        "learned": full["learned"], "learned_used": full["learned_used"],
+        "saved_vs_plain": full["saved_vs_plain"], "eval_failed": base["failed"],
+        "curve": curve, "eval_wall_s": base["wall_s"],
+        "generate_s": t_gen, "wall_s": time.perf_counter() - t0,
+        "batch": args.learned_batch, "epochs": args.learned_epochs,
+        "linear_solver": f"block-diagonal device LDL^T ({fronts} fronts), FP64 refinement"}),
+        flush=True)
 
 
 def main():

@@ -108,7 +108,6 @@ class MLP:
         self.lib = _lib.load()
         self.sizes = tuple(sizes)
         self.dev = torch.device(device)
-        self.stream = torch.cuda.current_stream(self.dev).cuda_stream
         rng = np.random.default_rng(seed)
         self.W, self.Wb, self.b, self.state = [], [], [], []
         for fan_in, fan_out in zip(self.sizes[:-1], self.sizes[1:]):
@@ -124,6 +123,12 @@ class MLP:
             self._ck(self.lib.nla3d_mlp_to_bf16(W.data_ptr(), Wb.data_ptr(), W.numel(), self.stream))
         self.step_count = 0
         self.x_mean = self.x_std = self.y_mean = self.y_std = None
+
+    @property
+    def stream(self):
+        """The caller's current stream: the kernels run in order with the
+        PyTorch work around them, whichever stream that is on."""
+        return self.torch.cuda.current_stream(self.dev).cuda_stream
 
     def _ck(self, rc):
         if rc:
@@ -475,3 +480,200 @@ def benchmark(n_block_train=40, n_block_eval=8, n_bar_train=12, block_n=10, bar_
     if log:
         log(f"bar: {out['bar']}")
     return out
+
+
+# ---------------------------------------------------------------------------
+# batched studies: many problems on one mesh, solved in lock step
+# (nla3d_gb300.batch_newton.BatchNewton)
+# ---------------------------------------------------------------------------
+
+def batch_features(basis: CoarseBasis, dU1, dU2, t, ratio, c10, kbulk):
+    """features() for B problems at once (dU1, dU2: B x n; c10, kbulk: B)."""
+    nc = basis.nc
+    P1 = dU1[:, nc:] @ basis.Q
+    P2 = dU2[:, nc:] @ basis.Q
+    s = np.linalg.norm(P1, axis=1) + 1e-300
+    B = dU1.shape[0]
+    X = np.concatenate([P1 / s[:, None], P2 / s[:, None], np.full((B, 1), t),
+                        np.full((B, 1), ratio), np.asarray(c10, np.float64)[:, None],
+                        (np.log10(np.asarray(kbulk, np.float64)) / 4.0)[:, None]], axis=1)
+    return X, s
+
+
+def batch_target(basis: CoarseBasis, dU1, dU2, dU, s):
+    """target() for B problems: the least-squares coefficients of dU on
+    [dU1, dU2, s Q].  Q is orthonormal, so for any (a1, a2) the Q part is
+    fitted exactly by c = (Q^T dU - a1 Q^T dU1 - a2 Q^T dU2) / s, which leaves
+    a two-column least-squares problem on the parts of dU1, dU2 and dU
+    orthogonal to Q: the same minimiser as the full problem whenever that
+    one is unique, at O(n) cost per problem instead of O(n 66^2)."""
+    nc, Q = basis.nc, basis.Q
+    d1, d2, d = dU1[:, nc:], dU2[:, nc:], dU[:, nc:]
+    p1, p2, p = d1 @ Q, d2 @ Q, d @ Q
+    r1, r2, r = d1 - p1 @ Q.T, d2 - p2 @ Q.T, d - p @ Q.T
+    Y = np.zeros((d.shape[0], 2 + Q.shape[1]))
+    for j in range(d.shape[0]):
+        a, *_ = np.linalg.lstsq(np.stack([r1[j], r2[j]], axis=1), r[j], rcond=None)
+        Y[j, :2] = a
+        Y[j, 2:] = (p[j] - a[0] * p1[j] - a[1] * p2[j]) / s[j]
+    return Y
+
+
+def batch_compose(basis: CoarseBasis, dU1, dU2, s, Y):
+    """compose() for B problems."""
+    nc = basis.nc
+    out = np.zeros_like(dU1)
+    out[:, nc:] = (Y[:, 0:1] * dU1[:, nc:] + Y[:, 1:2] * dU2[:, nc:]
+                   + s[:, None] * (Y[:, 2:] @ basis.Q.T))
+    return out
+
+
+class BatchHistory:
+    """on_converged hook of BatchNewton: the last four converged states (host
+    copies, B x n) and, with `collect`, the training samples of every load
+    step from the third on (rows of problems that have failed are left out;
+    `owner` gives each row's problem index, counted from `offset`)."""
+
+    def __init__(self, B, n, basis=None, c10=None, kbulk=None, collect=False, offset=0):
+        self.U = [np.zeros((B, n))]
+        self.t = [0.0]
+        self.basis, self.c10, self.kbulk = basis, c10, kbulk
+        self.collect = collect
+        self.offset = offset
+        self.X, self.Y, self.owner = [], [], []
+
+    def __call__(self, driver, t):
+        self.U.append(driver.U.cpu().numpy())
+        self.t.append(t)
+        if self.collect and len(self.U) >= 4:
+            U0, U1, U2, U3 = self.U[-1], self.U[-2], self.U[-3], self.U[-4]
+            keep = ~driver.failed
+            dU, dU1, dU2 = (U0 - U1)[keep], (U1 - U2)[keep], (U2 - U3)[keep]
+            ratio = (self.t[-1] - self.t[-2]) / (self.t[-2] - self.t[-3])
+            X, s = batch_features(self.basis, dU1, dU2, self.t[-1], ratio, self.c10[keep],
+                                  self.kbulk[keep])
+            self.X.append(X)
+            self.Y.append(batch_target(self.basis, dU1, dU2, dU, s))
+            self.owner.append(np.nonzero(keep)[0] + self.offset)
+        del self.U[:-4]
+
+
+class BatchExtrapolationPredictor:
+    """ExtrapolationPredictor for every problem of a BatchNewton."""
+
+    def __init__(self, history: BatchHistory):
+        self.h = history
+
+    def propose(self, driver, t):
+        h = self.h
+        if len(h.t) < 3:
+            return None, None
+        r = (t - h.t[-1]) / (h.t[-1] - h.t[-2])
+        prop = h.U[-1] + r * (h.U[-1] - h.U[-2])
+        return driver.torch.from_numpy(prop).to(driver.U.device), np.ones(driver.B, bool)
+
+
+class BatchMLPPredictor:
+    """MLPPredictor for every problem of a BatchNewton (one forward pass of
+    the network for the whole batch)."""
+
+    def __init__(self, mlp: MLP, basis: CoarseBasis, history: BatchHistory, c10, kbulk):
+        self.mlp, self.basis, self.h = mlp, basis, history
+        self.c10, self.kbulk = np.asarray(c10, np.float64), np.asarray(kbulk, np.float64)
+
+    def propose(self, driver, t):
+        h = self.h
+        if len(h.t) < 3:
+            return None, None
+        dU1, dU2 = h.U[-1] - h.U[-2], h.U[-2] - h.U[-3]
+        ratio = (t - h.t[-1]) / (h.t[-1] - h.t[-2])
+        X, s = batch_features(self.basis, dU1, dU2, t, ratio, self.c10, self.kbulk)
+        Y = self.mlp.predict(X)
+        prop = h.U[-1] + batch_compose(self.basis, dU1, dU2, s, Y)
+        return driver.torch.from_numpy(prop).to(driver.U.device), np.ones(driver.B, bool)
+
+
+def _batches(problems, batch_size):
+    for i in range(0, len(problems), batch_size):
+        yield problems[i:i + batch_size]
+
+
+def _batch_driver(group, precision, fronts, solvers):
+    from .batch_newton import BatchNewton
+    drv = BatchNewton(group, precision=precision, fronts=fronts,
+                      block_solver=solvers.get(len(group)))
+    solvers[len(group)] = drv.bs
+    return drv
+
+
+def generate_batched(problems, precision="fp64", fronts="fp32", batch_size=100, log=None,
+                     solvers=None):
+    """generate() with BatchNewton: the plain-start solves of `problems` (one
+    mesh), batch_size at a time.  Returns X, Y, the iterations per load step
+    (solves x load steps), the number of failed solves and, per sample row,
+    the index of the solve it comes from.  `solvers` (a dict) keeps the
+    block-diagonal factorisations' symbolic analyses for reuse by later
+    calls."""
+    import time
+    solvers = {} if solvers is None else solvers
+    X, Y, owner, iters, failed = [], [], [], [], 0
+    t0 = time.perf_counter()
+    for k, group in enumerate(_batches(problems, batch_size)):
+        drv = _batch_driver(group, precision, fronts, solvers)
+        basis = CoarseBasis(group[0].mesh, drv.ne, drv.ee, drv.nc, drv.n)
+        hist = BatchHistory(drv.B, drv.n, basis, np.array([pb.c10 for pb in group]),
+                            np.array([pb.kbulk for pb in group]), collect=True,
+                            offset=k * batch_size)
+        drv.solve(on_converged=hist)
+        X += hist.X
+        Y += hist.Y
+        owner += hist.owner
+        iters.append(drv.iterations[~drv.failed])
+        failed += int(drv.failed.sum())
+        drv.close()
+        if log:
+            log(f"batch {k}: {drv.B} solves, {np.mean(drv.iterations[~drv.failed]):.3f} it/step, "
+                f"{drv.factorizations} factorisations, {time.perf_counter() - t0:.1f} s")
+    return (np.concatenate(X), np.concatenate(Y), np.concatenate(iters), failed,
+            np.concatenate(owner))
+
+
+def evaluate_batched(problems, mlp, precision="fp64", fronts="fp32", batch_size=100,
+                     starts=("plain", "extrapolation", "learned"), log=None, solvers=None):
+    """evaluate() with BatchNewton: mean Newton iterations per load step of
+    each start on `problems` (one mesh), failed solves left out and counted."""
+    import time
+    solvers = {} if solvers is None else solvers
+    out = {k: [] for k in starts}
+    used, wall, failed = [], {}, {k: 0 for k in starts}
+    for group in _batches(problems, batch_size):
+        c10 = np.array([pb.c10 for pb in group])
+        kb = np.array([pb.kbulk for pb in group])
+        for start in starts:
+            drv = _batch_driver(group, precision, fronts, solvers)
+            basis = CoarseBasis(group[0].mesh, drv.ne, drv.ee, drv.nc, drv.n)
+            hist = BatchHistory(drv.B, drv.n)
+            pred = None
+            if start == "extrapolation":
+                pred = BatchExtrapolationPredictor(hist)
+            elif start == "learned":
+                pred = BatchMLPPredictor(mlp, basis, hist, c10, kb)
+            t0 = time.perf_counter()
+            drv.solve(predictor=pred, on_converged=hist)
+            wall[start] = wall.get(start, 0.0) + time.perf_counter() - t0
+            ok = ~drv.failed
+            out[start].append(drv.iterations[ok])
+            failed[start] += int(drv.failed.sum())
+            if start == "learned":
+                used.append(drv.predicted[ok])
+            drv.close()
+            if log:
+                log(f"{start}: {np.mean(drv.iterations[ok]):.3f} it/step over {int(ok.sum())} "
+                    f"solves, {wall[start]:.1f} s")
+    res = {k: float(np.mean(np.concatenate(v))) for k, v in out.items() if v}
+    if used:
+        res["learned_used"] = float(np.mean(np.concatenate(used)))
+    res["steps"] = int(np.concatenate(out[starts[0]]).size)
+    res["failed"] = failed
+    res["wall_s"] = wall
+    return res
