@@ -313,7 +313,14 @@ int nla3d_probe_fma_peak(int fp64, double* flops);
  * All pointers are device memory; calls are asynchronous on `stream`.
  *   nla3d_mlp_gemm    C[m,n] = act(sum_k A[m,k] B[k,n] + bias[n]); A[m,k] is at
  *                     A + m*lda_m + k*lda_k (B likewise), a_bf16 / b_bf16 select
- *                     BF16 inputs; act 0 = identity, 1 = tanh; bias may be NULL.
+ *                     BF16 inputs; act 0 = identity, 1 = tanh; bias may be NULL
+ *                     (A and B too when K = 0: C = act(bias)).
+ *                     Runs on the tensor cores (tcgen05.mma, BF16 operands,
+ *                     FP32 accumulation in TMEM); an FP32 operand enters as a
+ *                     BF16 pair hi + lo (|x - hi - lo| <= 2^-16 |x|).  A bounded
+ *                     wait that runs out sets the tile to NaN and is counted.
+ *   nla3d_mlp_status  *timeouts = GEMM tiles whose MMA wait ran out since the
+ *                     last call (then reset; synchronous)
  *   nla3d_mlp_tanh_backward   dY *= 1 - Y*Y (in place)
  *   nla3d_mlp_column_sum      out[c] = sum_r X[r, c] (row-major rows x cols)
  *   nla3d_mlp_adam    Adam step on FP32 master weights (step >= 1), refreshing
@@ -330,6 +337,7 @@ int nla3d_mlp_adam(float* w, const float* g, float* m, float* v, int64_t n, floa
 int nla3d_mlp_mse_grad(const float* Y, const float* T, float* dY, int64_t n, float scale,
                        void* stream);
 int nla3d_mlp_to_bf16(const float* x, uint16_t* y, int64_t n, void* stream);
+int nla3d_mlp_status(uint32_t* timeouts);
 
 /* ---------------------------------------------------------------------------
  * SOLID81 assembly without device allocation.  No counterpart in the

@@ -32,7 +32,7 @@ EXPORTS = [
     "nla3d_mesh_info", "nla3d_mesh_pattern", "nla3d_mesh_eq_numbers", "nla3d_get_K_all",
     "nla3d_set_launch_shape", "nla3d_autotune", "nla3d_graph_capture", "nla3d_graph_launch",
     "nla3d_mlp_gemm", "nla3d_mlp_tanh_backward", "nla3d_mlp_column_sum", "nla3d_mlp_adam",
-    "nla3d_mlp_to_bf16", "nla3d_mlp_mse_grad", "nla3d_set_contrib_layout",
+    "nla3d_mlp_to_bf16", "nla3d_mlp_mse_grad", "nla3d_mlp_status", "nla3d_set_contrib_layout",
     "nla3d_block_mv", "nla3d_add_mpc", "nla3d_mesh_add_mpc", "nla3d_assemble_to_host",
     "nla3d_set_pattern_builder", "nla3d_pattern_on_device", "nla3d_add_surface_lines",
     "nla3d_set_transient", "nla3d_get_C", "nla3d_get_M",
@@ -176,6 +176,7 @@ def load(path: str = LIB_PATH):
                             ctypes.c_float, ctypes.c_int, P, P], ctypes.c_int),
         "nla3d_mlp_to_bf16": ([P, P, I64, P], ctypes.c_int),
         "nla3d_mlp_mse_grad": ([P, P, P, I64, ctypes.c_float, P], ctypes.c_int),
+        "nla3d_mlp_status": ([P], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

@@ -134,6 +134,14 @@ class MLP:
         if rc:
             raise _lib.Nla3dError(rc, "MLP kernel launch failed")
 
+    def check(self):
+        """Raise if a tensor-core GEMM tile's bounded MMA wait ran out (its
+        outputs were set to NaN) since the last check (synchronises)."""
+        t = ctypes.c_uint32()
+        self._ck(self.lib.nla3d_mlp_status(ctypes.byref(t)))
+        if t.value:
+            raise _lib.Nla3dError(5, f"{t.value} MLP GEMM tiles timed out waiting for their MMAs")
+
     def forward(self, X):
         """X: float32 cuda tensor (B, in).  Returns activations [X, h1, ..., out]."""
         acts = [X]
@@ -221,6 +229,7 @@ class MLP:
                 history.append((ep, loss))
                 if log:
                     log(f"epoch {ep} loss {loss:.4e}")
+        self.check()
         return history
 
     def predict(self, X):
