@@ -50,9 +50,9 @@ DRAM_BYTES_PER_ELEM_GATHER_K = (301.560064e6 + 62.591488e6) / 64000
 # Executed arithmetic per element of solid81_kernel<float> (mixed), from the
 # instruction counters of one ncu capture of a 40^3 block (64,000 elements):
 # FP32 2 FFMA + FADD + FMUL and FP64 2 DFMA + DADD + DMUL per element.
-MIXED_FP32_FLOP_PER_ELEM = 66084
+MIXED_FP32_FLOP_PER_ELEM = 67044
 MIXED_FP64_FLOP_PER_ELEM = 1800
-MIXED_WARP_INSTR_PER_ELEM = 3530
+MIXED_WARP_INSTR_PER_ELEM = 2601
 METRIC = "SOLID81 assembly Melem/s"  # Newton iterations per load step (plain vs learned) in "newton"
 MIXED_DTYPE = ("f32 K_uu / f64 volumetric terms (J, J-1, p/K, K_up, K_pp, F_p) / "
                "float-pair (2^-48) F_u chain / f64 CSR sums")
@@ -605,9 +605,10 @@ def run_ours(args):
                  "K_rel_err_vs_fp64": float(np.abs(K32 - K64).max() / np.abs(K64).max()),
                  "F_rel_err_vs_fp64": float(np.abs(F32 - F64).max() / np.abs(F64).max()),
                  "dtype": MIXED_DTYPE,
-                 "bound": "issue / latency of the element kernel: neither pipe nor DRAM "
-                          "saturates (see roofline; ncu at 64,000 elements: issue 42%, LSU "
-                          "44%, shared wavefronts 46%, FP64 pipe 50%, FP32 FMA 19%, DRAM 7%)",
+                 "bound": "latency of the element kernel (short-scoreboard stalls first), "
+                          "the FP64 pipe of its volumetric terms the busiest unit (ncu at "
+                          "64,000 elements: FP64 pipe 65%, FP32 FMA 25%, issue 43%, LSU 17%, "
+                          "shared wavefronts 18%, DRAM 9%)",
                  "profile": "profiles/solid81_mixed_fp64vol_block40_ncu.md"}
         sm.close()
 
@@ -658,7 +659,7 @@ def run_ours(args):
                            "warp instructions (ncu counters of a 64,000-element launch)",
             "peak_source": "FP32 / FP64 FMA throughput probes in this run; issue: SMs x 4 "
                            "schedulers x median SM clock during the timed region",
-            "traffic": (112.792064e6 + 123.714304e6) / 64000 * mesh.n_elems,
+            "traffic": (112.787712e6 + 122.929664e6) / 64000 * mesh.n_elems,
             "traffic_source": "ncu dram bytes of a 64,000-element launch, scaled by elements"}
     elem_ms = float(kt[0])
     achieved = FLOP_PER_ELEM * mesh.n_elems / (elem_ms * 1e-3)
