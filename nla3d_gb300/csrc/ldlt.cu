@@ -21,9 +21,12 @@
 //      Fronts of <= kSmallFront rows: one thread block per front, the front
 //      in shared memory, all fronts of the level in one launch.  Larger
 //      fronts: all of the level's together, blocked, 64 columns per panel
-//      (diagonal block and its inverse, panel rows, then a tiled rank-64
-//      update of the trailing lower triangle: FMA tiles, or tcgen05 TF32
-//      split MMAs for FP32 fronts with precision 2).
+//      (diagonal block and its inverse, panel rows) in outer blocks of 256
+//      columns: each panel's rank-64 update reaches only the rest of its
+//      outer block; the columns after the block take one rank-256 update
+//      per block, so each trailing tile is read and written once per 256
+//      pivots instead of once per 64 (FMA tiles, or tcgen05 TF32 split MMAs
+//      for FP32 fronts with precision 2).
 // Solve (multifrontal, vectors): forward by levels with the same extend-add
 // on the update vectors, D^-1, backward by levels top-down gathering the
 // solved ancestor entries; FP64 refinement r = b - A x with A's
@@ -47,6 +50,7 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kSmallFront = 128;   // fronts up to this many rows: one block each, in smem
 constexpr int kPanel = 64;         // panel width of the blocked path
+constexpr int kOuter = 256;        // outer block of the blocked path (4 panels)
 constexpr int kTile = 64;          // panel-row tile of the blocked path
 
 struct LdltDev {
@@ -184,7 +188,9 @@ __global__ void __launch_bounds__(kThreads)
 
 // Blocked path for the fronts above kSmallFront rows, batched: every launch
 // works on panel p0 of all large fronts of one level (blockIdx.z / .x picks
-// the front; fronts with k <= p0 return).  W: per front an m x kPanel block.
+// the front; fronts with k <= p0 return).  W: per front an m x min(kOuter,
+// k rounded up to kPanel) block, W[i + c m] = (L D)[i][o0 + c] for the rows
+// i past the panel of column o0 + c (o0: the current outer block).
 struct BigBatch {
   const int32_t* list;
   const uint64_t* w_off;
@@ -311,22 +317,54 @@ __global__ void __launch_bounds__(kThreads)
     for (int v = 0; v < 4; v++) {
       const int c = tx * 4 + v;
       if (c >= pb) continue;
-      W[(i - q0) + c * m] = acc[u][v];
+      W[i + (int64_t)(p0 % kOuter + c) * m] = acc[u][v];
       F[i + (p0 + c) * m] = acc[u][v] / Dv[c];
     }
   }
 }
 
-// step 3: trailing lower triangle, F[i][j] -= sum_c L[i][c] W[j][c], i >= j >= q0;
-// BT x BT tiles (blockIdx.x, .y), front blockIdx.z, RT x RT outputs per thread
-// (64 / 4 for FP64, whose FMA pipe bounds it anyway; 128 / 8 for FP32).  A
-// thread owns rows tx + 16u and columns ty + 16v: shared-memory reads are
-// conflict-free or broadcast and the stores run down the columns.  The next
-// 16-wide slice of the panel is loaded into registers while the current one
-// is multiplied.
+// step 3: update of the lower triangle, F[i][j] -= sum_c L[i][lc0 + c] W[j][wc0 + c]
+// for jb <= j < je, i >= j:
+//   inner (outer == 0, after panel p0): the panel's kw = pb columns into the
+//     rest of its outer block, jb = p0 + pb, je = min(o0 + kOuter, k);
+//   outer (outer == 1, p0 = o0): the whole outer block, kw = min(k, o0 +
+//     kOuter) - o0 columns, into everything after it, jb = o0 + kw, je = m.
+// Every front's (lc0, wc0, kw, jb, je) follow from its own k and m.
+struct UpdateRange {
+  int64_t lc0, wc0, kw, jb, je;
+};
+
+__device__ __forceinline__ bool update_range(int64_t p0, int outer, int64_t k, int64_t m,
+                                             UpdateRange& u) {
+  if (p0 >= k) return false;
+  if (!outer) {
+    const int64_t pb = k - p0 < kPanel ? k - p0 : kPanel;
+    const int64_t o0 = p0 - p0 % kOuter;
+    u.lc0 = p0;
+    u.wc0 = p0 % kOuter;
+    u.kw = pb;
+    u.jb = p0 + pb;
+    u.je = o0 + kOuter < k ? o0 + kOuter : k;
+  } else {
+    const int64_t oe = p0 + kOuter < k ? p0 + kOuter : k;
+    u.lc0 = p0;
+    u.wc0 = 0;
+    u.kw = oe - p0;
+    u.jb = oe;
+    u.je = m;
+  }
+  return u.jb < u.je;
+}
+
+// BT x BT tiles (blockIdx.x rows, .y columns, both from jb), front
+// blockIdx.z, RT x RT outputs per thread (64 / 4 for FP64, whose FMA pipe
+// bounds it anyway; 128 / 8 for FP32).  A thread owns rows tx + 16u and
+// columns ty + 16v: shared-memory reads are conflict-free or broadcast and
+// the stores run down the columns.  The next 16-wide slice of the operands
+// is loaded into registers while the current one is multiplied.
 template <typename T, int BT, int RT>
 __global__ void __launch_bounds__(kThreads)
-    batched_trailing_kernel(BigBatch b, LdltDev d, T* __restrict__ front, int64_t p0,
+    batched_trailing_kernel(BigBatch b, LdltDev d, T* __restrict__ front, int64_t p0, int outer,
                             const T* __restrict__ Wbuf) {
   static_assert((BT / RT) * (BT / RT) == kThreads, "one output block per thread");
   static_assert(BT / RT == 16, "16 x 16 threads");
@@ -336,13 +374,13 @@ __global__ void __launch_bounds__(kThreads)
   const int s = b.list[blockIdx.z];
   const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
   const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
-  if (p0 >= k) return;
-  const int pb = (int)(k - p0 < kPanel ? k - p0 : kPanel);
-  const int64_t q0 = p0 + pb;
-  const int64_t i0 = q0 + (int64_t)ti * BT, j0 = q0 + (int64_t)tj * BT;
-  if (i0 >= m) return;
+  UpdateRange ur;
+  if (!update_range(p0, outer, k, m, ur)) return;
+  const int64_t i0 = ur.jb + (int64_t)ti * BT, j0 = ur.jb + (int64_t)tj * BT;
+  if (i0 >= m || j0 >= ur.je) return;
   T* F = front + d.front_off[s];
   const T* W = Wbuf + b.w_off[blockIdx.z];
+  const int kw = (int)ur.kw;
   __shared__ T As[16][BT];
   __shared__ T Bs[16][BT];
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
@@ -355,12 +393,12 @@ __global__ void __launch_bounds__(kThreads)
       const int cc = t / BT, rr = t % BT;
       const int c = c0 + cc;
       const int64_t i = i0 + rr, j = j0 + rr;
-      ra[q] = (c < pb && i < m) ? F[i + (p0 + c) * m] : T(0);
-      rb[q] = (c < pb && j < m) ? W[(j - q0) + c * m] : T(0);
+      ra[q] = (c < kw && i < m) ? F[i + (ur.lc0 + c) * m] : T(0);
+      rb[q] = (c < kw && j < ur.je) ? W[j + (ur.wc0 + c) * m] : T(0);
     }
   };
   load(0);
-  for (int c0 = 0; c0 < pb; c0 += 16) {
+  for (int c0 = 0; c0 < kw; c0 += 16) {
 #pragma unroll
     for (int q = 0; q < LPT; q++) {
       const int t = threadIdx.x + q * kThreads;
@@ -368,7 +406,7 @@ __global__ void __launch_bounds__(kThreads)
       Bs[t / BT][t % BT] = rb[q];
     }
     __syncthreads();
-    if (c0 + 16 < pb) load(c0 + 16);
+    if (c0 + 16 < kw) load(c0 + 16);
 #pragma unroll
     for (int cc = 0; cc < 16; cc++) {
       T a[RT], bb[RT];
@@ -386,7 +424,7 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
   for (int v = 0; v < RT; v++) {
     const int64_t j = j0 + ty + 16 * v;
-    if (j >= m) continue;
+    if (j >= ur.je) continue;
 #pragma unroll
     for (int u = 0; u < RT; u++) {
       const int64_t i = i0 + tx + 16 * u;
@@ -404,22 +442,23 @@ struct TrailingShape<float> {
   static constexpr int BT = 128, RT = 8;
 };
 
-// ---- the FP32 trailing update on the tensor cores (tcgen05, kind::tf32) ----
+// ---- the FP32 updates on the tensor cores (tcgen05, kind::tf32) ----
 //
-// One CTA (256 threads) per 128 x 128 tile of the trailing lower triangle.
-// The panel slices L[i0:i0+128, p0:p0+64] and W[j0:j0+128, 0:64] are taken
-// in two halves of 32 columns; each half is split into TF32 high and low
-// parts (x = hi + lo, hi = x rounded to TF32) and staged in shared memory in
-// the canonical K-major layout without swizzle (8-row x 16-byte core
-// matrices; K-adjacent cores 128 B apart, 8-row groups 1 KB apart).  One
-// thread issues 4 k-steps x 3 MMAs per half (hi.hi + hi.lo + lo.hi, FP32
-// accumulation in 128 TMEM columns) and commits them to an mbarrier; the
-// second half is staged once the first half's MMAs are done with the
-// buffers.  Then each warp reads 32 TMEM lanes (rows) x 64 columns and
-// subtracts them from the front.  64 KB of shared memory and 128 TMEM
-// columns per CTA, so that three CTAs share an SM and one's loads overlap
-// another's MMAs and epilogue.  Every wait on the mbarrier is bounded: on a
-// timeout the tile is left unchanged and err[0] is set.
+// One CTA (256 threads) per 128 x 128 tile of an update (batched_trailing_
+// kernel's inner and outer ranges), over kw <= 256 operand columns in chunks
+// of 32.  Each chunk of L[i0:i0+128, lc0+c] and W[j0:j0+128, wc0+c] is split
+// into TF32 high and low parts (x = hi + lo, hi = x rounded to TF32) and
+// staged in shared memory in the canonical K-major layout without swizzle
+// (8-row x 16-byte core matrices; K-adjacent cores 128 B apart, 8-row groups
+// 1 KB apart).  One thread issues 4 k-steps x 3 MMAs per chunk (hi.hi +
+// hi.lo + lo.hi, FP32 accumulation in 128 TMEM columns) and commits them to
+// an mbarrier; the next chunk is staged once they have released the
+// buffers.  After the last chunk each warp reads 32 TMEM lanes (rows) x 64
+// columns and subtracts them from the front: the tile is read and written
+// once per outer block.  64 KB of shared memory and 128 TMEM columns per
+// CTA, so that three CTAs share an SM and one's loads overlap another's
+// MMAs and epilogue.  Every wait on the mbarrier is bounded: on a timeout
+// the tile is left unchanged and err[0] is set.
 constexpr int kTcM = 128, kTcN = 128, kTcKH = 32;   // tile rows, columns, K per half
 constexpr int kTcThreads = 256;
 constexpr uint32_t kTcTileFloats = kTcM * kTcKH;     // one 128 x 32 operand half
@@ -474,20 +513,21 @@ __device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t a, uint64_t b, ui
 }
 
 __global__ void __launch_bounds__(kTcThreads)
-    tc_trailing_kernel(BigBatch b, LdltDev d, float* __restrict__ front, int64_t p0,
+    tc_trailing_kernel(BigBatch b, LdltDev d, float* __restrict__ front, int64_t p0, int outer,
                        const float* __restrict__ Wbuf, int* __restrict__ err) {
   const int ti = blockIdx.x, tj = blockIdx.y;
   if (tj > ti) return;
   const int s = b.list[blockIdx.z];
   const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
   const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
-  if (p0 >= k) return;
-  const int pb = (int)(k - p0 < kPanel ? k - p0 : kPanel);
-  const int64_t q0 = p0 + pb;
-  const int64_t i0 = q0 + (int64_t)ti * kTcM, j0 = q0 + (int64_t)tj * kTcN;
-  if (i0 >= m) return;
+  UpdateRange ur;
+  if (!update_range(p0, outer, k, m, ur)) return;
+  const int64_t i0 = ur.jb + (int64_t)ti * kTcM, j0 = ur.jb + (int64_t)tj * kTcN;
+  if (i0 >= m || j0 >= ur.je) return;
   float* F = front + d.front_off[s];
   const float* W = Wbuf + b.w_off[blockIdx.z];
+  const int kw = (int)ur.kw;
+  const int n_chunks = (kw + kTcKH - 1) / kTcKH;
   extern __shared__ __align__(1024) unsigned char tc_smem[];
   float* Ahi = reinterpret_cast<float*>(tc_smem);
   float* Alo = Ahi + kTcTileFloats;
@@ -506,21 +546,24 @@ __global__ void __launch_bounds__(kTcThreads)
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(mbar)), "r"(1));
     asm volatile("fence.mbarrier_init.release.cluster;");
   }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
   const int r = threadIdx.x % kTcM, kq = threadIdx.x / kTcM;   // row, which 16 of the 32
-  const int64_t ia = i0 + r, jb = j0 + r;
+  const int64_t ia = i0 + r, jr = j0 + r;
   const uint32_t lbo = 128, sbo = (kTcKH / 4) * 128;
   bool ok = true;
-  uint32_t tmem = 0;
-  for (int h = 0; h < 2 && ok; h++) {
-    if (h == 1) ok = tc_wait(smem_addr(mbar), 0);   // half 0's MMAs are done with the buffers
+  for (int h = 0; h < n_chunks && ok; h++) {
+    if (h > 0) ok = tc_wait(smem_addr(mbar), (uint32_t)(h - 1) & 1u);   // buffers released
     if (ok) {
       // all 32 loads of this thread in flight first, then split and store
       float av[16], wv[16];
 #pragma unroll
       for (int q = 0; q < 16; q++) {
         const int c = h * kTcKH + kq * 16 + q;
-        av[q] = (c < pb && ia < m) ? F[ia + (p0 + c) * m] : 0.0f;
-        wv[q] = (c < pb && jb < m) ? W[(jb - q0) + c * m] : 0.0f;
+        av[q] = (c < kw && ia < m) ? F[ia + (ur.lc0 + c) * m] : 0.0f;
+        wv[q] = (c < kw && jr < ur.je) ? W[jr + (ur.wc0 + c) * m] : 0.0f;
       }
 #pragma unroll
       for (int q = 0; q < 16; q++) {
@@ -536,7 +579,6 @@ __global__ void __launch_bounds__(kTcThreads)
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    tmem = *tmem_slot;
     ok = __syncthreads_and(ok ? 1 : 0) != 0;
     if (ok && threadIdx.x == 0) {
       const uint32_t ahi = smem_addr(Ahi), alo = smem_addr(Alo);
@@ -555,7 +597,7 @@ __global__ void __launch_bounds__(kTcThreads)
           : "memory");
     }
   }
-  if (ok) ok = tc_wait(smem_addr(mbar), 1);
+  if (ok) ok = tc_wait(smem_addr(mbar), (uint32_t)(n_chunks - 1) & 1u);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   ok = __syncthreads_and(ok ? 1 : 0) != 0;
   if (!ok) {
@@ -579,7 +621,7 @@ __global__ void __launch_bounds__(kTcThreads)
 #pragma unroll
         for (int q = 0; q < 16; q++) {
           const int64_t j = j0 + c0 + q;
-          if (j < m && j <= i) F[i + j * m] -= __uint_as_float(v[q]);
+          if (j < ur.je && j <= i) F[i + j * m] -= __uint_as_float(v[q]);
         }
     }
   }
@@ -1060,22 +1102,39 @@ cudaError_t enqueue_factor(nla3d_ldlt* h, const double* values) {
       T* W = static_cast<T*>(h->d_W);
       T* Li = static_cast<T*>(h->d_Linv);
       const unsigned nf = (unsigned)L.large_cnt;
-      for (int64_t p0 = 0; p0 < L.large_max_k; p0 += kPanel) {
-        batched_diag_kernel<T><<<nf, kThreads, 2 * sizeof(T) * kPanel * (kPanel + 1), st>>>(
-            bb, h->dev, front, p0, Li, h->d_maxabs, h->pivot_rel, h->d_perturbed);
-        const int64_t rest = L.large_max_m - p0 - 1;   // rows past the smallest panel
-        if (rest <= 0) continue;
-        const unsigned tiles = (unsigned)((rest + kTile - 1) / kTile);
-        batched_panel_kernel<T><<<dim3(tiles, nf), kThreads, 0, st>>>(bb, h->dev, front, p0, Li, W);
-        constexpr int BT = TrailingShape<T>::BT, RT = TrailingShape<T>::RT;
-        const unsigned ttiles = (unsigned)((rest + BT - 1) / BT);
-        if (std::is_same<T, float>::value && h->tc)
-          tc_trailing_kernel<<<dim3(ttiles, ttiles, nf), kTcThreads, kTcSmem, st>>>(
-              bb, h->dev, reinterpret_cast<float*>(front), p0,
+      constexpr int BT = TrailingShape<T>::BT, RT = TrailingShape<T>::RT;
+      const bool tc = std::is_same<T, float>::value && h->tc;
+      // one update launch: rows from its range's first column to the largest
+      // front's last row, `col_tiles` tiles of columns
+      auto update = [&](int64_t p, int outer, int64_t rows, unsigned col_tiles) {
+        const unsigned rt = (unsigned)((rows + BT - 1) / BT);
+        const dim3 grid(rt, std::min(rt, col_tiles), nf);
+        if (tc)
+          tc_trailing_kernel<<<grid, kTcThreads, kTcSmem, st>>>(
+              bb, h->dev, reinterpret_cast<float*>(front), p, outer,
               reinterpret_cast<const float*>(W), h->d_err);
         else
-          batched_trailing_kernel<T, BT, RT><<<dim3(ttiles, ttiles, nf), kThreads, 0, st>>>(
-              bb, h->dev, front, p0, W);
+          batched_trailing_kernel<T, BT, RT><<<grid, kThreads, 0, st>>>(bb, h->dev, front, p,
+                                                                         outer, W);
+      };
+      for (int64_t o0 = 0; o0 < L.large_max_k; o0 += kOuter) {
+        const int64_t o_end = std::min<int64_t>(o0 + kOuter, L.large_max_k);
+        for (int64_t p0 = o0; p0 < o_end; p0 += kPanel) {
+          batched_diag_kernel<T><<<nf, kThreads, 2 * sizeof(T) * kPanel * (kPanel + 1), st>>>(
+              bb, h->dev, front, p0, Li, h->d_maxabs, h->pivot_rel, h->d_perturbed);
+          const int64_t rest = L.large_max_m - p0 - 1;   // rows past the smallest panel
+          if (rest <= 0) continue;
+          const unsigned tiles = (unsigned)((rest + kTile - 1) / kTile);
+          batched_panel_kernel<T><<<dim3(tiles, nf), kThreads, 0, st>>>(bb, h->dev, front, p0,
+                                                                         Li, W);
+          // the panel's columns into the rest of its outer block (at most
+          // kOuter - kPanel columns)
+          if (p0 + kPanel < o_end)
+            update(p0, 0, rest, (unsigned)((kOuter - kPanel + BT - 1) / BT));
+        }
+        // the outer block into every column after it
+        const int64_t rest = L.large_max_m - o0 - 1;
+        if (rest > 0) update(o0, 1, rest, ~0u);
       }
     }
   }
@@ -1228,7 +1287,8 @@ int nla3d_ldlt_create(int64_t n, const uint32_t* iofeir, const uint32_t* columns
       if (S.m(s) > kSmallFront) {
         lists.push_back(s);
         wo.push_back((uint64_t)w);
-        w += (int64_t)S.m(s) * kPanel;
+        w += (int64_t)S.m(s) *
+             std::min<int64_t>(kOuter, ((int64_t)S.k(s) + kPanel - 1) / kPanel * kPanel);
         lio.push_back(li_total);
         li_total += (uint64_t)((S.k(s) + kPanel - 1) / kPanel) * kPanel * kPanel;
         lv.large_max_m = std::max<int64_t>(lv.large_max_m, S.m(s));
@@ -1629,12 +1689,13 @@ int nla3d_ldlt_solve_host(nla3d_ldlt* h, const double* values, const double* b_h
 }
 
 int nla3d_ldlt_tc_check(int m, double* out) {
-  // one front of m rows whose first panel (64 pivots) is done: the trailing
-  // update of rows / columns 64 .. m-1 by the FMA kernel and by the tensor
-  // cores from the same random data; out[0] = max |difference|, out[1] =
-  // max |update|
+  // one front of m rows whose first kb pivots (one outer block: 256 when
+  // m > 512, else 64) are done: the update of rows / columns kb .. m-1 by the
+  // FMA kernel and by the tensor cores from the same random data; out[0] =
+  // max |difference|, out[1] = max |update|
   if (m < kPanel + 1 || m > 4096 || !out) return NLA3D_ERR_ARG;
-  const size_t mm = (size_t)m * m, mw = (size_t)m * kPanel;
+  const int kb = m > 2 * kOuter ? kOuter : kPanel;
+  const size_t mm = (size_t)m * m, mw = (size_t)m * kb;
   std::vector<float> F0(mm), W(mw);
   uint64_t x = 88172645463325252ull;   // xorshift, fixed seed
   auto rnd = [&]() {
@@ -1669,7 +1730,7 @@ int nla3d_ldlt_tc_check(int m, double* out) {
   const int32_t zero32 = 0;
   const uint64_t zero64[2] = {0, (uint64_t)mm};
   const int64_t rp[2] = {0, m};
-  const int32_t sf[2] = {0, kPanel};
+  const int32_t sf[2] = {0, kb};
   if (e == cudaSuccess) e = cudaMemcpy(F1, F0.data(), mm * 4, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(F2, F0.data(), mm * 4, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(dW, W.data(), mw * 4, cudaMemcpyHostToDevice);
@@ -1689,10 +1750,11 @@ int nla3d_ldlt_tc_check(int m, double* out) {
     d.row_ptr = rowp;
     d.sn_first = snf;
     const BigBatch bb{list, woff, woff};
-    const int64_t rest = m - kPanel;
+    const int64_t rest = m - kb;
     const unsigned t128 = (unsigned)((rest + 127) / 128);
-    batched_trailing_kernel<float, 128, 8><<<dim3(t128, t128, 1), kThreads>>>(bb, d, F1, 0, dW);
-    tc_trailing_kernel<<<dim3(t128, t128, 1), kTcThreads, kTcSmem>>>(bb, d, F2, 0, dW, err);
+    batched_trailing_kernel<float, 128, 8><<<dim3(t128, t128, 1), kThreads>>>(bb, d, F1, 0, 1,
+                                                                               dW);
+    tc_trailing_kernel<<<dim3(t128, t128, 1), kTcThreads, kTcSmem>>>(bb, d, F2, 0, 1, dW, err);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e == cudaSuccess) e = cudaMemcpy(&tc_err, err, 4, cudaMemcpyDeviceToHost);
@@ -1704,7 +1766,7 @@ int nla3d_ldlt_tc_check(int m, double* out) {
   if (e != cudaSuccess) return NLA3D_ERR_CUDA;
   if (tc_err) return NLA3D_ERR_RANGE;
   double dmax = 0.0, umax = 0.0;
-  for (int j = kPanel; j < m; j++)
+  for (int j = kb; j < m; j++)
     for (int i = j; i < m; i++) {
       const size_t q = (size_t)i + (size_t)j * m;
       dmax = std::max(dmax, (double)std::fabs(R1[q] - R2[q]));
