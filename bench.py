@@ -41,6 +41,10 @@ sys.path.insert(0, ROOT)
 # Bh^T D Bh formulation costs 69,072 (8 x 8634) for the same element.
 FLOP_PER_ELEM = 32432
 FLOP_PER_ELEM_BTDB = 69072
+# FP64 instructions per element in the same capture (14,088 DFMA + 3,472
+# DMUL + 784 DADD): a DMUL or DADD takes the pipe as long as a DFMA for half
+# the flops, so the pipe's instruction rate is the tighter ceiling.
+FP64_INSTR_PER_ELEM = 18344
 # DRAM bytes per element of solid81_kernel<double> and of the K gather in one
 # ncu capture of a 40^3 block (64,000 elements, 9,675,406 K slots), used to
 # scale the traffic to the measured launch; the element kernel's writes are a
@@ -698,6 +702,10 @@ def run_ours(args):
                      "algorithmic": f"{FLOP_PER_ELEM} FP64 flop/element x {mesh.n_elems}",
                      "btdb_equivalent_tflops": FLOP_PER_ELEM_BTDB * mesh.n_elems
                      / (elem_ms * 1e-3) / 1e12,
+                     "fp64_instr_frac": FP64_INSTR_PER_ELEM * mesh.n_elems / (elem_ms * 1e-3)
+                     / (fp64_peak / 2),
+                     "fp64_instr_note": "executed FP64 instructions per second against the "
+                                        "probe's DFMA rate (FMA probe flops / 2)",
                      "peak_source": "FP64 FMA throughput probe in this run "
                                     "(MEASURED_PEAKS.json has no FP64 figure)"},
         "roofline_gather": {"bound": "hbm", "achieved": gather_bytes / (gather_ms * 1e-3) / 1e9,
