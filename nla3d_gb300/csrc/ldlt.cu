@@ -195,6 +195,7 @@ struct BigBatch {
   const int32_t* list;
   const uint64_t* w_off;
   const uint64_t* li_off;   // the front's inverted diagonal blocks, 64 x 64 per panel
+  const uint64_t* pk_off;   // tensor-core fronts: the front's packed outer-block operands
 };
 
 // step 1: LDL^T of the pb x pb diagonal block, and the inverse of its unit
@@ -637,6 +638,303 @@ __global__ void __launch_bounds__(kTcThreads)
   }
 }
 
+// ---- the outer-block update from packed operands (tensor-core fronts) ----
+//
+// The rank-256 update after an outer block reads the same operands from
+// every tile of a row or column: L[jb + 128 r .. +127][o0 .. o0 + kw) and
+// W[jb + 128 r .. +127][0 .. kw).  pack_outer_kernel splits them into TF32
+// high and low parts once per outer block and stores them, per 128-row block
+// r and 32-column chunk c, as four 16 KB tiles (A hi, A lo, B hi, B lo) in
+// the MMA's shared-memory layout (tc_off).  tc_outer_kernel is persistent
+// (one CTA per SM walking a host-built list of the level's tiles) and
+// warp-specialised:
+//   warp 0 (one lane): copies each chunk's four tiles into a ring of
+//     kPkStages shared-memory stages with asynchronous bulk copies
+//     (cp.async.bulk, completion counted on the stage's `full` mbarrier);
+//   warp 1 (one lane): waits for a stage, issues its 12 MMAs (hi.hi, hi.lo,
+//     lo.hi per 8-wide k step) into one of two 128-column TMEM
+//     accumulators and commits them to the stage's `empty` mbarrier (the
+//     stage is refilled once they have read it) and, after a tile's last
+//     chunk, to the accumulator's `acc_full` mbarrier;
+//   warps 2-9: load their 32 rows x 64 columns of the front tile into
+//     registers while the tile's MMAs run, then read the same part of the
+//     finished accumulator from TMEM, release it (`acc_empty`, one arrival
+//     per warp) and store the difference, while the MMAs of the next tile
+//     run into the other accumulator.
+// Every wait is bounded: on a timeout the role stops, err[0] is set and the
+// copies and MMAs still in flight get one more bounded wait each before the
+// CTA releases its shared memory and TMEM.
+constexpr int kPkChunks = kOuter / kTcKH;                  // 8 chunks of 32 columns
+constexpr uint32_t kPkTile = kTcTileFloats;                // floats per 128 x 32 tile
+constexpr uint32_t kPkBlock = 4 * kPkTile * kPkChunks;    // floats per 128-row block
+constexpr int kPkStages = 3;
+constexpr size_t kPkSmem = (size_t)kPkStages * 4 * kPkTile * sizeof(float) + 256;
+constexpr int kOuterThreads = 320;   // producer, MMA, 8 epilogue warps
+
+__global__ void __launch_bounds__(kTcThreads)
+    pack_outer_kernel(BigBatch b, LdltDev d, const float* __restrict__ front, int64_t o0,
+                      const float* __restrict__ Wbuf, float* __restrict__ packed) {
+  const int s = b.list[blockIdx.z];
+  const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
+  const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
+  UpdateRange ur;
+  if (!update_range(o0, 1, k, m, ur)) return;
+  const int rb = blockIdx.x, ch = blockIdx.y;
+  const int64_t r0 = ur.jb + (int64_t)rb * kTcM;
+  if (r0 >= m || ch * kTcKH >= ur.kw) return;
+  const float* F = front + d.front_off[s];
+  const float* W = Wbuf + b.w_off[blockIdx.z];
+  float* P = packed + b.pk_off[blockIdx.z] + (uint64_t)(rb * kPkChunks + ch) * 4 * kPkTile;
+  const int r = threadIdx.x % kTcM, kq = threadIdx.x / kTcM;
+  const int64_t i = r0 + r;
+#pragma unroll 4
+  for (int q = 0; q < 16; q++) {
+    const int c = ch * kTcKH + kq * 16 + q;
+    const bool in = c < ur.kw && i < m;
+    const float av = in ? F[i + (ur.lc0 + c) * m] : 0.0f;
+    const float wv = in ? W[i + (ur.wc0 + c) * m] : 0.0f;
+    const float ah = tf32_hi(av), wh = tf32_hi(wv);
+    const uint32_t o = tc_off(r, kq * 16 + q);
+    P[o] = ah;
+    P[kPkTile + o] = av - ah;
+    P[2 * kPkTile + o] = wh;
+    P[3 * kPkTile + o] = wv - wh;
+  }
+}
+
+__device__ __forceinline__ void bulk_copy(uint32_t dst, const void* src, uint32_t bytes,
+                                          uint32_t mbar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(dst), "l"(src), "r"(bytes), "r"(mbar)
+      : "memory");
+}
+
+__device__ __forceinline__ void expect_tx(uint32_t mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes)
+               : "memory");
+}
+
+// one update tile of the level's outer-block list: large front z (index in
+// the level's list), tile row ti >= tile column tj
+struct OuterTile {
+  uint32_t z, tij;   // tij = ti << 16 | tj
+};
+
+__global__ void __launch_bounds__(kOuterThreads, 1)
+    tc_outer_kernel(BigBatch b, LdltDev d, float* __restrict__ front, int64_t o0,
+                    const float* __restrict__ packed, const OuterTile* __restrict__ tiles,
+                    int n_tiles, int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char pk_smem[];
+  float* stage0 = reinterpret_cast<float*>(pk_smem);
+  uint64_t* full = reinterpret_cast<uint64_t*>(stage0 + (size_t)kPkStages * 4 * kPkTile);
+  uint64_t* empty = full + kPkStages;
+  uint64_t* acc_full = empty + kPkStages;
+  uint64_t* acc_empty = acc_full + 2;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acc_empty + 2);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_addr(tmem_slot)),
+                 "r"(2 * kTcN));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (threadIdx.x == 32) {
+    for (int q = 0; q < kPkStages; q++) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(full + q)), "r"(1));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(empty + q)), "r"(1));
+    }
+    for (int q = 0; q < 2; q++) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(acc_full + q)),
+                   "r"(1));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(acc_empty + q)),
+                   "r"(8));
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+  constexpr uint32_t kTileBytes = kPkTile * sizeof(float);
+  auto stage_addr = [&](int q, int t) {   // t: 0 A hi, 1 A lo, 2 B hi, 3 B lo
+    return smem_addr(stage0 + (size_t)(q * 4 + t) * kPkTile);
+  };
+  // the front of a tile: rows m, update range, chunks
+  struct TileInfo {
+    int64_t m, i0, j0;
+    int nch;
+    const float* pa;
+    const float* pb;
+    float* F;
+  };
+  auto info = [&](int t, TileInfo& ti) {
+    const OuterTile ot = tiles[t];
+    const int s = b.list[ot.z];
+    const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
+    const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
+    UpdateRange ur;
+    update_range(o0, 1, k, m, ur);   // the host listed only fronts whose range is not empty
+    const uint32_t rI = ot.tij >> 16, rJ = ot.tij & 0xFFFFu;
+    ti.m = m;
+    ti.i0 = ur.jb + (int64_t)rI * kTcM;
+    ti.j0 = ur.jb + (int64_t)rJ * kTcN;
+    ti.nch = (int)((ur.kw + kTcKH - 1) / kTcKH);
+    ti.pa = packed + b.pk_off[ot.z] + (uint64_t)rI * kPkBlock;
+    ti.pb = packed + b.pk_off[ot.z] + (uint64_t)rJ * kPkBlock;
+    ti.F = front + d.front_off[s];
+  };
+  bool ok = true;
+  if (warp == 0) {
+    if (lane == 0) {
+      // producer: the ring of stages, in the MMA warp's order
+      uint32_t g = 0, issued = 0;
+      for (int t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
+        TileInfo ti;
+        info(t, ti);
+        for (int c = 0; c < ti.nch && ok; c++, g++) {
+          const int q = g % kPkStages;
+          if (g >= kPkStages) ok = tc_wait(smem_addr(empty + q), (g / kPkStages - 1) & 1u);
+          if (!ok) break;
+          const uint32_t fb = smem_addr(full + q);
+          expect_tx(fb, 4 * kTileBytes);
+          const float* a = ti.pa + (size_t)c * 4 * kPkTile;
+          const float* bb = ti.pb + (size_t)c * 4 * kPkTile;
+          bulk_copy(stage_addr(q, 0), a, kTileBytes, fb);
+          bulk_copy(stage_addr(q, 1), a + kPkTile, kTileBytes, fb);
+          bulk_copy(stage_addr(q, 2), bb + 2 * kPkTile, kTileBytes, fb);
+          bulk_copy(stage_addr(q, 3), bb + 3 * kPkTile, kTileBytes, fb);
+          issued = g + 1;
+        }
+      }
+      if (!ok) {
+        atomicExch(err, 1);
+        // the copies of the last kPkStages chunks may still be in flight
+        for (uint32_t h = issued > kPkStages ? issued - kPkStages : 0; h < issued; h++)
+          tc_wait(smem_addr(full + h % kPkStages), (h / kPkStages) & 1u);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // MMA issuer
+      const uint32_t lbo = 128, sbo = (kTcKH / 4) * 128;
+      uint32_t g = 0, it = 0, committed_acc = 0;
+      for (int t = blockIdx.x; t < n_tiles && ok; t += gridDim.x, it++) {
+        TileInfo ti;
+        info(t, ti);
+        const uint32_t a = it & 1u;
+        if (it >= 2) ok = tc_wait(smem_addr(acc_empty + a), (it / 2 - 1) & 1u);
+        if (!ok) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t acc = tmem + a * kTcN;
+        for (int c = 0; c < ti.nch && ok; c++, g++) {
+          const int q = g % kPkStages;
+          ok = tc_wait(smem_addr(full + q), (g / kPkStages) & 1u);
+          if (!ok) break;
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          for (int st = 0; st < kTcKH / 8; st++) {
+            const uint32_t koff = st * 256;   // 8 K values = two core matrices
+            const uint64_t dah = tc_desc(stage_addr(q, 0) + koff, lbo, sbo);
+            const uint64_t dal = tc_desc(stage_addr(q, 1) + koff, lbo, sbo);
+            const uint64_t dbh = tc_desc(stage_addr(q, 2) + koff, lbo, sbo);
+            const uint64_t dbl = tc_desc(stage_addr(q, 3) + koff, lbo, sbo);
+            tc_mma(acc, dah, dbh, (c > 0 || st > 0) ? 1u : 0u);
+            tc_mma(acc, dah, dbl, 1u);
+            tc_mma(acc, dal, dbh, 1u);
+          }
+          asm volatile(
+              "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                  smem_addr(empty + q))
+              : "memory");
+        }
+        if (!ok) break;
+        asm volatile(
+            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                smem_addr(acc_full + a))
+            : "memory");
+        committed_acc = it + 1;
+      }
+      if (!ok) {
+        atomicExch(err, 1);
+        // MMAs complete in order: the last chunk commit covers every MMA issued
+        if (g > 0) tc_wait(smem_addr(empty + (g - 1) % kPkStages), ((g - 1) / kPkStages) & 1u);
+      } else if (committed_acc > 0) {
+        tc_wait(smem_addr(acc_full + ((committed_acc - 1) & 1u)), ((committed_acc - 1) / 2) & 1u);
+      }
+    }
+  } else {
+    // epilogue warp (warps 2-9): TMEM lanes 32 (warp % 4) .. +31 = tile rows
+    // (a warp reaches only its own lane quarter), columns 64 ((warp - 2) / 4)
+    // .. +63
+    const int lq = warp & 3, cb = ((warp - 2) >> 2) * 64;
+    const int row = lq * 32 + lane;
+    uint32_t it = 0;
+    for (int t = blockIdx.x; t < n_tiles && ok; t += gridDim.x, it++) {
+      TileInfo ti;
+      info(t, ti);
+      const uint32_t a = it & 1u;
+      const int64_t i = ti.i0 + row;
+      const bool row_in = i < ti.m;
+      // the front's values of the first 32 columns first: their loads overlap
+      // the tile's MMAs; the second 32 load while the first are stored
+      float* fp = ti.F + i + (ti.j0 + cb) * ti.m;   // (i, j0 + cb); column stride m
+      const int64_t jlim = (row_in ? (i < ti.m - 1 ? i : ti.m - 1) : -1) - (ti.j0 + cb);
+      float cv[32];
+#pragma unroll
+      for (int q = 0; q < 32; q++) cv[q] = q <= jlim ? fp[q * ti.m] : 0.0f;
+      ok = tc_wait(smem_addr(acc_full + a), (it / 2) & 1u);
+      if (!ok) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        uint32_t v[32];
+#pragma unroll
+        for (int c2 = 0; c2 < 2; c2++) {
+          const uint32_t taddr = tmem + ((uint32_t)(lq * 32) << 16) + a * kTcN +
+                                 (uint32_t)(cb + h * 32 + c2 * 16);
+          asm volatile(
+              "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, "
+              "%10, %11, %12, %13, %14, %15}, [%16];"
+              : "=r"(v[c2 * 16 + 0]), "=r"(v[c2 * 16 + 1]), "=r"(v[c2 * 16 + 2]),
+                "=r"(v[c2 * 16 + 3]), "=r"(v[c2 * 16 + 4]), "=r"(v[c2 * 16 + 5]),
+                "=r"(v[c2 * 16 + 6]), "=r"(v[c2 * 16 + 7]), "=r"(v[c2 * 16 + 8]),
+                "=r"(v[c2 * 16 + 9]), "=r"(v[c2 * 16 + 10]), "=r"(v[c2 * 16 + 11]),
+                "=r"(v[c2 * 16 + 12]), "=r"(v[c2 * 16 + 13]), "=r"(v[c2 * 16 + 14]),
+                "=r"(v[c2 * 16 + 15])
+              : "r"(taddr));
+        }
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (h == 1) {
+          // the accumulator is in registers: the MMAs of the tile after next may reuse it
+          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+          __syncwarp();
+          if (lane == 0)
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(acc_empty + a))
+                         : "memory");
+        }
+        float nv[32];
+        if (h == 0) {
+#pragma unroll
+          for (int q = 0; q < 32; q++) nv[q] = 32 + q <= jlim ? fp[(32 + q) * ti.m] : 0.0f;
+        }
+#pragma unroll
+        for (int q = 0; q < 32; q++)
+          if (h * 32 + q <= jlim) fp[(h * 32 + q) * ti.m] = cv[q] - __uint_as_float(v[q]);
+        if (h == 0) {
+#pragma unroll
+          for (int q = 0; q < 32; q++) cv[q] = nv[q];
+        }
+      }
+    }
+    if (!ok && lane == 0) atomicExch(err, 1);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(2 * kTcN));
+}
+
 // ---- solve kernels ----
 
 __global__ void solve_init_kernel(int64_t n, const int32_t* __restrict__ perm,
@@ -1011,6 +1309,10 @@ struct nla3d_ldlt {
   const double* factor_graph_values = nullptr;
   uint64_t* d_wo = nullptr;
   uint64_t* d_lio = nullptr;
+  uint64_t* d_pko = nullptr;    // tensor-core fronts: packed outer-block operand offsets
+  float* d_pk = nullptr;
+  OuterTile* d_tiles = nullptr; // tensor-core fronts: every level's outer-block tile lists
+  int n_sm = 0;
   uint64_t* d_adest = nullptr;
   int32_t* d_perm = nullptr;
   int32_t* d_col2sn = nullptr;
@@ -1027,6 +1329,7 @@ struct nla3d_ldlt {
     int64_t large_off = 0, large_cnt = 0; // fronts above kSmallFront rows
     int64_t wo_off = 0;                   // their W offsets in d_wo
     int64_t large_max_m = 0, large_max_k = 0;
+    std::vector<int64_t> tile_off, tile_cnt;  // tensor-core fronts: per outer block, its tiles
     std::vector<int64_t> ea_off, ea_cnt;  // children of the level's parents, by ordinal
     std::vector<uint32_t> ea_gy;          // column blocks per child (its update's size)
   };
@@ -1098,7 +1401,8 @@ cudaError_t enqueue_factor(nla3d_ldlt* h, const double* values) {
           h->d_lists + L.small_off, h->dev, front, h->d_maxabs, h->pivot_rel, h->d_perturbed);
     }
     if (L.large_cnt) {
-      const BigBatch bb{h->d_lists + L.large_off, h->d_wo + L.wo_off, h->d_lio + L.wo_off};
+      const BigBatch bb{h->d_lists + L.large_off, h->d_wo + L.wo_off, h->d_lio + L.wo_off,
+                        h->d_pko ? h->d_pko + L.wo_off : nullptr};
       T* W = static_cast<T*>(h->d_W);
       T* Li = static_cast<T*>(h->d_Linv);
       const unsigned nf = (unsigned)L.large_cnt;
@@ -1132,9 +1436,23 @@ cudaError_t enqueue_factor(nla3d_ldlt* h, const double* values) {
           if (p0 + kPanel < o_end)
             update(p0, 0, rest, (unsigned)((kOuter - kPanel + BT - 1) / BT));
         }
-        // the outer block into every column after it
+        // the outer block into every column after it (tensor-core fronts:
+        // its operands packed once, then the tiles with bulk copies)
         const int64_t rest = L.large_max_m - o0 - 1;
-        if (rest > 0) update(o0, 1, rest, ~0u);
+        if (rest > 0 && tc) {
+          const unsigned rb = (unsigned)((rest + kTcM - 1) / kTcM);
+          pack_outer_kernel<<<dim3(rb, kPkChunks, nf), kTcThreads, 0, st>>>(
+              bb, h->dev, reinterpret_cast<const float*>(front), o0,
+              reinterpret_cast<const float*>(W), h->d_pk);
+          const int64_t ob = o0 / kOuter;
+          const int nt = (int)L.tile_cnt[ob];
+          if (nt > 0)
+            tc_outer_kernel<<<(unsigned)std::min(nt, h->n_sm), kOuterThreads, kPkSmem, st>>>(
+                bb, h->dev, reinterpret_cast<float*>(front), o0, h->d_pk,
+                h->d_tiles + L.tile_off[ob], nt, h->d_err);
+        } else if (rest > 0) {
+          update(o0, 1, rest, ~0u);
+        }
       }
     }
   }
@@ -1261,8 +1579,9 @@ int nla3d_ldlt_create(int64_t n, const uint32_t* iofeir, const uint32_t* columns
   std::vector<int32_t> col2sn(S.n);
   for (int64_t s = 0; s < ns; s++)
     for (int32_t t = S.sn_first[s]; t < S.sn_first[s + 1]; t++) col2sn[t] = (int32_t)s;
-  std::vector<uint64_t> wo, lio;
-  int64_t max_w = 0, max_large_cnt = 0;
+  std::vector<uint64_t> wo, lio, pko;
+  std::vector<OuterTile> tiles;
+  int64_t max_w = 0, max_large_cnt = 0, max_pk = 0;
   uint64_t li_total = 0;
   h->levels.resize(nlev);
   for (int L = 0; L < nlev; L++) {
@@ -1281,7 +1600,7 @@ int nla3d_ldlt_create(int64_t n, const uint32_t* iofeir, const uint32_t* columns
     lv.small_cnt = (int64_t)lists.size() - lv.small_off;
     lv.large_off = (int64_t)lists.size();
     lv.wo_off = (int64_t)wo.size();
-    int64_t w = 0;
+    int64_t w = 0, pk = 0;
     for (int32_t q = S.level_ptr[L]; q < S.level_ptr[L + 1]; q++) {
       const int32_t s = S.level_list[q];
       if (S.m(s) > kSmallFront) {
@@ -1290,13 +1609,35 @@ int nla3d_ldlt_create(int64_t n, const uint32_t* iofeir, const uint32_t* columns
         w += (int64_t)S.m(s) *
              std::min<int64_t>(kOuter, ((int64_t)S.k(s) + kPanel - 1) / kPanel * kPanel);
         lio.push_back(li_total);
+        pko.push_back((uint64_t)pk);
+        pk += ((int64_t)S.m(s) + kTcM - 1) / kTcM * (int64_t)kPkBlock;
         li_total += (uint64_t)((S.k(s) + kPanel - 1) / kPanel) * kPanel * kPanel;
         lv.large_max_m = std::max<int64_t>(lv.large_max_m, S.m(s));
         lv.large_max_k = std::max<int64_t>(lv.large_max_k, S.k(s));
       }
     }
     lv.large_cnt = (int64_t)lists.size() - lv.large_off;
+    if (h->tc) {
+      // every outer block's update tiles (the rule of update_range, outer):
+      // per front with k > o0, rows and columns from jb = min(o0 + kOuter, k)
+      for (int64_t o0 = 0; o0 < lv.large_max_k; o0 += kOuter) {
+        lv.tile_off.push_back((int64_t)tiles.size());
+        for (int64_t z = 0; z < lv.large_cnt; z++) {
+          const int32_t s = lists[lv.large_off + z];
+          const int64_t k = S.k(s), m = S.m(s);
+          if (o0 >= k) continue;
+          const int64_t jb = std::min<int64_t>(o0 + kOuter, k);
+          if (jb >= m) continue;
+          const int64_t rb = (m - jb + kTcM - 1) / kTcM;
+          for (int64_t ti = 0; ti < rb; ti++)
+            for (int64_t tj = 0; tj <= ti; tj++)
+              tiles.push_back(OuterTile{(uint32_t)z, (uint32_t)(ti << 16 | tj)});
+        }
+        lv.tile_cnt.push_back((int64_t)tiles.size() - lv.tile_off.back());
+      }
+    }
     max_w = std::max(max_w, w);
+    max_pk = std::max(max_pk, pk);
     max_large_cnt = std::max(max_large_cnt, lv.large_cnt);
     int maxc = 0;
     for (int32_t q = S.level_ptr[L]; q < S.level_ptr[L + 1]; q++) {
@@ -1389,9 +1730,18 @@ int nla3d_ldlt_create(int64_t n, const uint32_t* iofeir, const uint32_t* columns
   LCK(dalloc(h, &h->d_perturbed, 2));
   LCK(dalloc(h, &h->d_err, 1));
   LCK(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
-  if (h->tc)
+  if (h->tc) {
     LCK(cudaFuncSetAttribute(tc_trailing_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)kTcSmem));
+    LCK(cudaFuncSetAttribute(tc_outer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)kPkSmem));
+    LCK(upload(h, &h->d_pko, pko));
+    LCK(dalloc(h, &h->d_pk, (size_t)std::max<int64_t>(max_pk, 1)));
+    LCK(upload(h, &h->d_tiles, tiles));
+    int dev = 0;
+    LCK(cudaGetDevice(&dev));
+    LCK(cudaDeviceGetAttribute(&h->n_sm, cudaDevAttrMultiProcessorCount, dev));
+  }
   LCK(upload(h, &h->d_adest, S.a_dest));
   LCK(upload(h, &h->d_perm, S.perm));
   LCK(upload(h, &h->d_col2sn, col2sn));
@@ -1691,8 +2041,9 @@ int nla3d_ldlt_solve_host(nla3d_ldlt* h, const double* values, const double* b_h
 int nla3d_ldlt_tc_check(int m, double* out) {
   // one front of m rows whose first kb pivots (one outer block: 256 when
   // m > 512, else 64) are done: the update of rows / columns kb .. m-1 by the
-  // FMA kernel and by the tensor cores from the same random data; out[0] =
-  // max |difference|, out[1] = max |update|
+  // FMA kernel and by both tensor-core kernels (operands staged through
+  // registers; operands packed, then bulk-copied) from the same random data;
+  // out[0] = max |difference| to the FMA result, out[1] = max |update|
   if (m < kPanel + 1 || m > 4096 || !out) return NLA3D_ERR_ARG;
   const int kb = m > 2 * kOuter ? kOuter : kPanel;
   const size_t mm = (size_t)m * m, mw = (size_t)m * kb;
@@ -1712,7 +2063,14 @@ int nla3d_ldlt_tc_check(int m, double* out) {
     if (e == cudaSuccess) allocs.push_back(*p);
     return e;
   };
-  float *F1 = nullptr, *F2 = nullptr, *dW = nullptr;
+  float *F1 = nullptr, *F2 = nullptr, *F3 = nullptr, *dW = nullptr, *dP = nullptr;
+  const size_t mp = (size_t)((m + kTcM - 1) / kTcM) * kPkBlock;
+  std::vector<OuterTile> tl;   // the outer update's tiles, as the factorisation lists them
+  const int rbk = (m - kb + kTcM - 1) / kTcM;
+  for (int ti = 0; ti < rbk; ti++)
+    for (int tj = 0; tj <= ti; tj++) tl.push_back(OuterTile{0u, (uint32_t)(ti << 16 | tj)});
+  OuterTile* dT = nullptr;
+  int n_sm = 1, dev = 0;
   int* err = nullptr;
   int32_t* list = nullptr;
   uint64_t *woff = nullptr, *foff = nullptr;
@@ -1720,6 +2078,13 @@ int nla3d_ldlt_tc_check(int m, double* out) {
   int32_t* snf = nullptr;
   cudaError_t e = dal((void**)&F1, mm * 4);
   if (e == cudaSuccess) e = dal((void**)&F2, mm * 4);
+  if (e == cudaSuccess) e = dal((void**)&F3, mm * 4);
+  if (e == cudaSuccess) e = dal((void**)&dP, mp * 4);
+  if (e == cudaSuccess) e = dal((void**)&dT, tl.size() * sizeof(OuterTile));
+  if (e == cudaSuccess)
+    e = cudaMemcpy(dT, tl.data(), tl.size() * sizeof(OuterTile), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
   if (e == cudaSuccess) e = dal((void**)&dW, mw * 4);
   if (e == cudaSuccess) e = dal((void**)&err, 4);
   if (e == cudaSuccess) e = dal((void**)&list, 4);
@@ -1733,6 +2098,7 @@ int nla3d_ldlt_tc_check(int m, double* out) {
   const int32_t sf[2] = {0, kb};
   if (e == cudaSuccess) e = cudaMemcpy(F1, F0.data(), mm * 4, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(F2, F0.data(), mm * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(F3, F0.data(), mm * 4, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(dW, W.data(), mw * 4, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(err, 0, 4);
   if (e == cudaSuccess) e = cudaMemcpy(list, &zero32, 4, cudaMemcpyHostToDevice);
@@ -1743,25 +2109,32 @@ int nla3d_ldlt_tc_check(int m, double* out) {
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(tc_trailing_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)kTcSmem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(tc_outer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)kPkSmem);
   int tc_err = 0;
   if (e == cudaSuccess) {
     LdltDev d{};
     d.front_off = foff;
     d.row_ptr = rowp;
     d.sn_first = snf;
-    const BigBatch bb{list, woff, woff};
+    const BigBatch bb{list, woff, woff, woff};
     const int64_t rest = m - kb;
     const unsigned t128 = (unsigned)((rest + 127) / 128);
     batched_trailing_kernel<float, 128, 8><<<dim3(t128, t128, 1), kThreads>>>(bb, d, F1, 0, 1,
                                                                                dW);
     tc_trailing_kernel<<<dim3(t128, t128, 1), kTcThreads, kTcSmem>>>(bb, d, F2, 0, 1, dW, err);
+    pack_outer_kernel<<<dim3(t128, kPkChunks, 1), kTcThreads>>>(bb, d, F3, 0, dW, dP);
+    tc_outer_kernel<<<(unsigned)std::min<int>((int)tl.size(), n_sm), kOuterThreads, kPkSmem>>>(
+        bb, d, F3, 0, dP, dT, (int)tl.size(), err);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e == cudaSuccess) e = cudaMemcpy(&tc_err, err, 4, cudaMemcpyDeviceToHost);
   }
-  std::vector<float> R1(mm), R2(mm);
+  std::vector<float> R1(mm), R2(mm), R3(mm);
   if (e == cudaSuccess) e = cudaMemcpy(R1.data(), F1, mm * 4, cudaMemcpyDeviceToHost);
   if (e == cudaSuccess) e = cudaMemcpy(R2.data(), F2, mm * 4, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(R3.data(), F3, mm * 4, cudaMemcpyDeviceToHost);
   for (void* p : allocs) cudaFree(p);
   if (e != cudaSuccess) return NLA3D_ERR_CUDA;
   if (tc_err) return NLA3D_ERR_RANGE;
@@ -1770,6 +2143,7 @@ int nla3d_ldlt_tc_check(int m, double* out) {
     for (int i = j; i < m; i++) {
       const size_t q = (size_t)i + (size_t)j * m;
       dmax = std::max(dmax, (double)std::fabs(R1[q] - R2[q]));
+      dmax = std::max(dmax, (double)std::fabs(R1[q] - R3[q]));
       umax = std::max(umax, (double)std::fabs(R1[q] - F0[q]));
     }
   out[0] = dmax;
