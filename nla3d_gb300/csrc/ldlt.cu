@@ -128,20 +128,20 @@ __global__ void extend_add_kernel(const int32_t* __restrict__ children, int n, L
 
 // the guarded pivot without counting it
 template <typename T>
-__device__ __forceinline__ T guard_value(T dv, double tau) {
-  if (!(fabs((double)dv) >= tau) && dv == dv) return dv < T(0) ? T(-tau) : T(tau);
+__device__ __forceinline__ T guard_value(T dv, T tau) {
+  if (!(fabs(dv) >= tau) && dv == dv) return dv < T(0) ? -tau : tau;
   return dv;
 }
 
 template <typename T>
-__device__ __forceinline__ T guard_pivot(T dv, double tau, int* perturbed) {
-  if (!(fabs((double)dv) >= tau)) {   // also catches NaN
+__device__ __forceinline__ T guard_pivot(T dv, T tau, int* perturbed) {
+  if (!(fabs(dv) >= tau)) {   // also catches NaN
     if (dv != dv) {
       atomicAdd(perturbed + 1, 1);
       return dv;
     }
     atomicAdd(perturbed, 1);
-    return dv < T(0) ? T(-tau) : T(tau);
+    return dv < T(0) ? -tau : tau;
   }
   return dv;
 }
@@ -164,24 +164,34 @@ __global__ void __launch_bounds__(kThreads)
   for (int c = 0; c < m; c++)
     for (int r = c + threadIdx.x; r < m; r += blockDim.x) S[r + c * ld] = F[r + (int64_t)c * m];
   __syncthreads();
-  const double tau = pivot_rel * tau_p[0];
+  // the pivot bound in the front's precision (the guards compare in it)
+  const T tau = (T)(pivot_rel * tau_p[0]);
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  // one barrier per pivot: the columns right of p are updated with the
+  // unscaled column p (A_ij -= w_i w_j / d), which no later step writes; the
+  // pivot columns are scaled after the loop
   for (int p = 0; p < k; p++) {
     // every thread guards the pivot itself (thread 0 counts)
     const T raw = S[p + p * ld];
     const T dv = threadIdx.x == 0 ? guard_pivot(raw, tau, perturbed) : guard_value(raw, tau);
-    T* colp = S + p * ld;
-    // trailing update with w = column p (unscaled): A_ij -= w_i w_j / d
+    const T* colp = S + p * ld;
     for (int j = p + 1 + ty; j < m; j += 8) {
       const T lj = colp[j] / dv;
       T* col = S + j * ld;
       for (int i = j + tx; i < m; i += 32) col[i] -= colp[i] * lj;
     }
     __syncthreads();
-    if (threadIdx.x == 0) colp[p] = dv;
-    for (int i = p + 1 + threadIdx.x; i < m; i += blockDim.x) colp[i] = colp[i] / dv;
-    __syncthreads();
   }
+  // scale column p by its guarded pivot (its diagonal is unchanged since
+  // step p), one warp per column
+  for (int p = ty; p < k; p += 8) {
+    T* colp = S + p * ld;
+    const T dv = guard_value(colp[p], tau);
+    for (int i = p + 1 + tx; i < m; i += 32) colp[i] = colp[i] / dv;
+    __syncwarp();
+    if (tx == 0) colp[p] = dv;
+  }
+  __syncthreads();
   for (int c = 0; c < m; c++)
     for (int r = c + threadIdx.x; r < m; r += blockDim.x) F[r + (int64_t)c * m] = S[r + c * ld];
 }
@@ -218,9 +228,12 @@ __global__ void __launch_bounds__(kThreads)
   for (int r = tr; r < pb; r += kThreads / kPanel)
     if (tc < pb) B[tc][r] = r >= tc ? F[(p0 + r) + (p0 + tc) * m] : T(0);
   __syncthreads();
-  const double tau = pivot_rel * tau_p[0];
+  // the pivot bound in the front's precision (the guards compare in it)
+  const T tau = (T)(pivot_rel * tau_p[0]);
   // one barrier per pivot: every thread guards the pivot itself (only thread
-  // 0 counts), column p is scaled by its own threads while the others update
+  // 0 counts); the columns right of p are updated with the unscaled column p
+  // (A_rc -= w_r w_c / d), which no later step writes, and every column is
+  // scaled by its pivot after the loop
   for (int p = 0; p < pb; p++) {
     const T raw = B[p][p];
     const T dv = threadIdx.x == 0 ? guard_pivot(raw, tau, perturbed) : guard_value(raw, tau);
@@ -229,10 +242,15 @@ __global__ void __launch_bounds__(kThreads)
       for (int r = tc + tr; r < pb; r += kThreads / kPanel) B[tc][r] -= B[p][r] * lc;
     }
     __syncthreads();
-    if (threadIdx.x == p) B[p][p] = dv;
-    if (threadIdx.x > p && threadIdx.x < pb) B[p][threadIdx.x] = B[p][threadIdx.x] / dv;
-    __syncthreads();
   }
+  if (tc < pb) {
+    // column tc's diagonal is unchanged since its own step
+    const T dc = guard_value(B[tc][tc], tau);
+    for (int r = tc + 1 + tr; r < pb; r += kThreads / kPanel) B[tc][r] = B[tc][r] / dc;
+  }
+  __syncthreads();
+  if (threadIdx.x < pb) B[threadIdx.x][threadIdx.x] = guard_value(B[threadIdx.x][threadIdx.x], tau);
+  __syncthreads();
   for (int r = tr; r < pb; r += kThreads / kPanel)
     if (tc < pb && r >= tc) F[(p0 + r) + (p0 + tc) * m] = B[tc][r];
   // inverse of the unit lower L11 in shared memory (X[col][row]): column c by
@@ -685,20 +703,32 @@ __global__ void __launch_bounds__(kTcThreads)
   const float* F = front + d.front_off[s];
   const float* W = Wbuf + b.w_off[blockIdx.z];
   float* P = packed + b.pk_off[blockIdx.z] + (uint64_t)(rb * kPkChunks + ch) * 4 * kPkTile;
-  const int r = threadIdx.x % kTcM, kq = threadIdx.x / kTcM;
+  // thread: row r, four groups of 4 consecutive columns (16-byte stores)
+  const int r = threadIdx.x % kTcM, g0 = (threadIdx.x / kTcM) * 4;
   const int64_t i = r0 + r;
-#pragma unroll 4
-  for (int q = 0; q < 16; q++) {
-    const int c = ch * kTcKH + kq * 16 + q;
-    const bool in = c < ur.kw && i < m;
-    const float av = in ? F[i + (ur.lc0 + c) * m] : 0.0f;
-    const float wv = in ? W[i + (ur.wc0 + c) * m] : 0.0f;
-    const float ah = tf32_hi(av), wh = tf32_hi(wv);
-    const uint32_t o = tc_off(r, kq * 16 + q);
-    P[o] = ah;
-    P[kPkTile + o] = av - ah;
-    P[2 * kPkTile + o] = wh;
-    P[3 * kPkTile + o] = wv - wh;
+#pragma unroll
+  for (int g = g0; g < g0 + 4; g++) {
+    float4 ah, al, wh, wl;
+    float* ahp = &ah.x;
+    float* alp = &al.x;
+    float* whp = &wh.x;
+    float* wlp = &wl.x;
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      const int c = ch * kTcKH + g * 4 + e;
+      const bool in = c < ur.kw && i < m;
+      const float av = in ? F[i + (ur.lc0 + c) * m] : 0.0f;
+      const float wv = in ? W[i + (ur.wc0 + c) * m] : 0.0f;
+      ahp[e] = tf32_hi(av);
+      alp[e] = av - ahp[e];
+      whp[e] = tf32_hi(wv);
+      wlp[e] = wv - whp[e];
+    }
+    const uint32_t o = tc_off(r, g * 4);
+    *reinterpret_cast<float4*>(P + o) = ah;
+    *reinterpret_cast<float4*>(P + kPkTile + o) = al;
+    *reinterpret_cast<float4*>(P + 2 * kPkTile + o) = wh;
+    *reinterpret_cast<float4*>(P + 3 * kPkTile + o) = wl;
   }
 }
 
