@@ -1067,53 +1067,8 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // Solves of the large supernodes, batched per level like their factorisation
-// (blockIdx picks the supernode in the level's large list; panels of 64
-// pivots, each diagonal block applied through its stored inverse).
-
-// forward, panel c0: y_B = Linv_B v_B
-template <typename T>
-__global__ void fwd_diag_kernel(BigBatch b, LdltDev d, const T* __restrict__ Linv, int64_t c0,
-                                double* __restrict__ vec) {
-  __shared__ double vb[kPanel];
-  const int s = b.list[blockIdx.x];
-  const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
-  if (c0 >= k) return;
-  const int cb = (int)(k - c0 < kPanel ? k - c0 : kPanel);
-  double* v = vec + d.vec_off[s];
-  if (threadIdx.x < cb) vb[threadIdx.x] = v[c0 + threadIdx.x];
-  __syncthreads();
-  const T* Li = Linv + b.li_off[blockIdx.x] + (uint64_t)(c0 / kPanel) * kPanel * kPanel;
-  const int t = threadIdx.x;
-  if (t < cb) {
-    double acc = 0.0;
-    for (int c = 0; c <= t; c++) acc += (double)Li[t + c * kPanel] * vb[c];
-    v[c0 + t] = acc;
-  }
-}
-
-// forward, panel c0: v[i] -= sum_c L[i][c0+c] y_c for the rows below the panel
-template <typename T>
-__global__ void fwd_rows_kernel(BigBatch b, LdltDev d, const T* __restrict__ front, int64_t c0,
-                                double* __restrict__ vec) {
-  __shared__ double yb[kPanel];
-  const int s = b.list[blockIdx.y];
-  const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
-  const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
-  if (c0 >= k) return;
-  const int cb = (int)(k - c0 < kPanel ? k - c0 : kPanel);
-  const int64_t r0 = c0 + cb + (int64_t)blockIdx.x * blockDim.x;
-  if (r0 >= m) return;
-  const T* F = front + d.front_off[s];
-  double* v = vec + d.vec_off[s];
-  if (threadIdx.x < cb) yb[threadIdx.x] = v[c0 + threadIdx.x];
-  __syncthreads();
-  const int64_t i = r0 + threadIdx.x;
-  if (i < m) {
-    double acc = 0.0;
-    for (int c = 0; c < cb; c++) acc += (double)F[i + (c0 + c) * m] * yb[c];
-    v[i] -= acc;
-  }
-}
+// (blockIdx picks the supernode in the level's large list; each 64-pivot
+// diagonal block applied through its stored inverse).
 
 // after the forward panels: v[0:k] <- D^-1 v[0:k]
 template <typename T>
@@ -1151,49 +1106,134 @@ __global__ void bwd_rest_kernel(BigBatch b, LdltDev d, const T* __restrict__ fro
   }
 }
 
-// backward, panel c0: x_B = Linv_B^T t_B
+// The forward and backward passes go by outer blocks of kOuter pivots (four
+// panels), two launches per outer block and level: the block's own triangle
+// by one CTA per supernode (panel by panel through the stored inverses, the
+// rows / columns inside the block updated in shared memory), then the rows
+// below it (forward) or the pivots before it (backward) with up to kOuter
+// products per entry.
+
+// forward, outer block o0: v_B <- L_BB^-1 v_B for the block's ob pivots
 template <typename T>
-__global__ void bwd_diag_kernel(BigBatch b, LdltDev d, const T* __restrict__ Linv, int64_t c0,
-                                double* __restrict__ vec) {
-  __shared__ double tb[kPanel];
+__global__ void __launch_bounds__(kThreads)
+    fwd_block_kernel(BigBatch b, LdltDev d, const T* __restrict__ front,
+                     const T* __restrict__ Linv, int64_t o0, double* __restrict__ vec) {
+  __shared__ double vb[kOuter];
   const int s = b.list[blockIdx.x];
+  const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
   const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
-  if (c0 >= k) return;
-  const int cb = (int)(k - c0 < kPanel ? k - c0 : kPanel);
+  if (o0 >= k) return;
+  const int ob = (int)(k - o0 < kOuter ? k - o0 : kOuter);
+  const T* F = front + d.front_off[s];
   double* v = vec + d.vec_off[s];
-  if (threadIdx.x < cb) tb[threadIdx.x] = v[c0 + threadIdx.x];
-  __syncthreads();
-  const T* Li = Linv + b.li_off[blockIdx.x] + (uint64_t)(c0 / kPanel) * kPanel * kPanel;
   const int t = threadIdx.x;
-  if (t < cb) {
-    double acc = 0.0;
-    for (int c = t; c < cb; c++) acc += (double)Li[c + t * kPanel] * tb[c];
-    v[c0 + t] = acc;
+  if (t < ob) vb[t] = v[o0 + t];
+  __syncthreads();
+  for (int p = 0; p < ob; p += kPanel) {
+    const int cb = ob - p < kPanel ? ob - p : kPanel;
+    const T* Li = Linv + b.li_off[blockIdx.x] + (uint64_t)((o0 + p) / kPanel) * kPanel * kPanel;
+    double y = 0.0;
+    if (t < cb)
+      for (int c = 0; c <= t; c++) y += (double)Li[t + c * kPanel] * vb[p + c];
+    __syncthreads();
+    if (t < cb) vb[p + t] = y;
+    __syncthreads();
+    for (int i = p + cb + t; i < ob; i += blockDim.x) {
+      double acc = 0.0;
+      for (int c = 0; c < cb; c++) acc += (double)F[(o0 + i) + (o0 + p + c) * m] * vb[p + c];
+      vb[i] -= acc;
+    }
+    __syncthreads();
   }
+  if (t < ob) v[o0 + t] = vb[t];
 }
 
-// backward, panel c0: t[j] -= sum_c L[c0+c][j] x_B[c] for the pivots j < c0
-// (a warp per column j, lanes over the panel's 64 rows)
+// forward, outer block o0: v[i] -= sum_c L[i][o0+c] y_c for the rows below the block
 template <typename T>
-__global__ void bwd_cols_kernel(BigBatch b, LdltDev d, const T* __restrict__ front, int64_t c0,
-                                double* __restrict__ vec) {
-  __shared__ double xb[kPanel];
+__global__ void __launch_bounds__(kThreads)
+    fwd_rows_block_kernel(BigBatch b, LdltDev d, const T* __restrict__ front, int64_t o0,
+                          double* __restrict__ vec) {
+  __shared__ double yb[kOuter];
   const int s = b.list[blockIdx.y];
   const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
   const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
-  if (c0 >= k) return;
-  const int64_t jbeg = (int64_t)blockIdx.x * (blockDim.x / 32) * 4;
-  if (jbeg >= c0) return;
-  const int cb = (int)(k - c0 < kPanel ? k - c0 : kPanel);
+  if (o0 >= k) return;
+  const int ob = (int)(k - o0 < kOuter ? k - o0 : kOuter);
+  const int64_t r0 = o0 + ob + (int64_t)blockIdx.x * blockDim.x;
+  if (r0 >= m) return;
   const T* F = front + d.front_off[s];
   double* v = vec + d.vec_off[s];
-  if (threadIdx.x < cb) xb[threadIdx.x] = v[c0 + threadIdx.x];
+  if (threadIdx.x < ob) yb[threadIdx.x] = v[o0 + threadIdx.x];
+  __syncthreads();
+  const int64_t i = r0 + threadIdx.x;
+  if (i < m) {
+    const T* Fi = F + i + o0 * m;
+    double acc = 0.0;
+    for (int c = 0; c < ob; c++) acc += (double)Fi[(int64_t)c * m] * yb[c];
+    v[i] -= acc;
+  }
+}
+
+// backward, outer block o0: x_B = L_BB^-T t_B for the block's pivots
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    bwd_block_kernel(BigBatch b, LdltDev d, const T* __restrict__ front,
+                     const T* __restrict__ Linv, int64_t o0, double* __restrict__ vec) {
+  __shared__ double tb[kOuter];
+  const int s = b.list[blockIdx.x];
+  const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
+  const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
+  if (o0 >= k) return;
+  const int ob = (int)(k - o0 < kOuter ? k - o0 : kOuter);
+  const T* F = front + d.front_off[s];
+  double* v = vec + d.vec_off[s];
+  const int t = threadIdx.x;
+  if (t < ob) tb[t] = v[o0 + t];
+  __syncthreads();
+  for (int p = ((ob - 1) / kPanel) * kPanel; p >= 0; p -= kPanel) {
+    const int cb = ob - p < kPanel ? ob - p : kPanel;
+    const T* Li = Linv + b.li_off[blockIdx.x] + (uint64_t)((o0 + p) / kPanel) * kPanel * kPanel;
+    double x = 0.0;
+    if (t < cb)
+      for (int c = t; c < cb; c++) x += (double)Li[c + t * kPanel] * tb[p + c];
+    __syncthreads();
+    if (t < cb) tb[p + t] = x;
+    __syncthreads();
+    for (int j = t; j < p; j += blockDim.x) {
+      const T* Fj = F + (o0 + p) + (o0 + j) * m;
+      double acc = 0.0;
+      for (int c = 0; c < cb; c++) acc += (double)Fj[c] * tb[p + c];
+      tb[j] -= acc;
+    }
+    __syncthreads();
+  }
+  if (t < ob) v[o0 + t] = tb[t];
+}
+
+// backward, outer block o0: t[j] -= sum_c L[o0+c][j] x_c for the pivots j < o0
+// (a warp per column j, lanes over the block's rows)
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    bwd_cols_block_kernel(BigBatch b, LdltDev d, const T* __restrict__ front, int64_t o0,
+                          double* __restrict__ vec) {
+  __shared__ double xb[kOuter];
+  const int s = b.list[blockIdx.y];
+  const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
+  const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
+  if (o0 >= k) return;
+  const int64_t jbeg = (int64_t)blockIdx.x * 32;
+  if (jbeg >= o0) return;
+  const int ob = (int)(k - o0 < kOuter ? k - o0 : kOuter);
+  const T* F = front + d.front_off[s];
+  double* v = vec + d.vec_off[s];
+  if (threadIdx.x < ob) xb[threadIdx.x] = v[o0 + threadIdx.x];
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t jend = jbeg + (blockDim.x / 32) * 4 < c0 ? jbeg + (blockDim.x / 32) * 4 : c0;
+  const int64_t jend = jbeg + 32 < o0 ? jbeg + 32 : o0;
   for (int64_t j = jbeg + warp; j < jend; j += blockDim.x / 32) {
+    const T* Fj = F + o0 + j * m;
     double acc = 0.0;
-    for (int c = lane; c < cb; c += 32) acc += (double)F[(c0 + c) + j * m] * xb[c];
+    for (int c = lane; c < ob; c += 32) acc += (double)Fj[c] * xb[c];
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
     if (lane == 0) v[j] -= acc;
   }
@@ -1510,12 +1550,12 @@ cudaError_t enqueue_solve_core(nla3d_ldlt* h, const double* b) {
     if (L.large_cnt) {
       const BigBatch bb{h->d_lists + L.large_off, h->d_wo + L.wo_off, h->d_lio + L.wo_off};
       const unsigned nf = (unsigned)L.large_cnt;
-      for (int64_t c0 = 0; c0 < L.large_max_k; c0 += kPanel) {
-        fwd_diag_kernel<T><<<nf, kPanel, 0, st>>>(bb, h->dev, Li, c0, h->d_vec);
-        const int64_t rest = L.large_max_m - c0 - 1;
+      for (int64_t o0 = 0; o0 < L.large_max_k; o0 += kOuter) {
+        fwd_block_kernel<T><<<nf, kThreads, 0, st>>>(bb, h->dev, front, Li, o0, h->d_vec);
+        const int64_t rest = L.large_max_m - o0 - 1;
         if (rest > 0)
-          fwd_rows_kernel<T><<<dim3((unsigned)((rest + kThreads - 1) / kThreads), nf), kThreads, 0,
-                               st>>>(bb, h->dev, front, c0, h->d_vec);
+          fwd_rows_block_kernel<T><<<dim3((unsigned)((rest + kThreads - 1) / kThreads), nf),
+                                     kThreads, 0, st>>>(bb, h->dev, front, o0, h->d_vec);
       }
       scale_pivots_kernel<T><<<dim3((unsigned)((L.large_max_k + kThreads - 1) / kThreads), nf),
                                kThreads, 0, st>>>(bb, h->dev, front, h->d_vec);
@@ -1532,11 +1572,11 @@ cudaError_t enqueue_solve_core(nla3d_ldlt* h, const double* b) {
       const unsigned nf = (unsigned)L.large_cnt;
       bwd_rest_kernel<T><<<dim3((unsigned)((L.large_max_k + 31) / 32), nf), kThreads, 0, st>>>(
           bb, h->dev, front, h->d_vec, h->d_xf);
-      for (int64_t c0 = ((L.large_max_k - 1) / kPanel) * kPanel; c0 >= 0; c0 -= kPanel) {
-        bwd_diag_kernel<T><<<nf, kPanel, 0, st>>>(bb, h->dev, Li, c0, h->d_vec);
-        if (c0 > 0)
-          bwd_cols_kernel<T><<<dim3((unsigned)((c0 + 31) / 32), nf), kThreads, 0, st>>>(
-              bb, h->dev, front, c0, h->d_vec);
+      for (int64_t o0 = ((L.large_max_k - 1) / kOuter) * kOuter; o0 >= 0; o0 -= kOuter) {
+        bwd_block_kernel<T><<<nf, kThreads, 0, st>>>(bb, h->dev, front, Li, o0, h->d_vec);
+        if (o0 > 0)
+          bwd_cols_block_kernel<T><<<dim3((unsigned)((o0 + 31) / 32), nf), kThreads, 0, st>>>(
+              bb, h->dev, front, o0, h->d_vec);
       }
       store_pivots_kernel<<<dim3((unsigned)((L.large_max_k + kThreads - 1) / kThreads), nf),
                             kThreads, 0, st>>>(bb, h->dev, h->d_vec, h->d_xf);

@@ -157,7 +157,6 @@ class NewtonSolver:
         if solver not in ("direct", "nd", "lu-gmres", "gpu", "gpu-fp32", "gpu-tc"):
             raise ValueError(solver)
         self._ldlt = None
-        self._ldlt64 = None
         self.inexact_solves = 0
         self.fp64_refactorizations = 0
         self._perm = None
@@ -185,6 +184,12 @@ class NewtonSolver:
         self.R = np.zeros(self.n)
         self.records: list[StepRecord] = []
         self.reactions: list[np.ndarray] = [np.zeros(self.nc)]
+
+    def close(self):
+        """Release the device factorisation (its fronts can take most of HBM)."""
+        if self._ldlt is not None:
+            self._ldlt.close()
+            self._ldlt = None
 
     # ---- the global system ----
     def _K2(self):
@@ -216,11 +221,15 @@ class NewtonSolver:
         if rel <= 1e-6:
             self.inexact_solves += 1
             return x
-        if self._ldlt64 is None:
-            self._ldlt64 = DeviceLDLT.for_storage(self.b, self._perm, "fp64")
-        self._ldlt64.factor(self.b)
-        self.fp64_refactorizations += 1
-        return self._ldlt64.solve_host(self.b, rhs, max_refine=100, tol=1e-10)
+        # FP64 fronts for this iteration only: their memory (twice the FP32
+        # fronts') is released right after the solve
+        ld64 = DeviceLDLT.for_storage(self.b, self._perm, "fp64")
+        try:
+            ld64.factor(self.b)
+            self.fp64_refactorizations += 1
+            return ld64.solve_host(self.b, rhs, max_refine=100, tol=1e-10)
+        finally:
+            ld64.close()
 
     def _solve(self, K2, rhs):
         if self.solver.startswith("gpu"):
