@@ -440,14 +440,15 @@ def evaluate(problems, mlp, precision="fp64", linear_solver="direct",
     return res | {"steps": len(out[starts[0]]), "wall_s": wall}
 
 
-def benchmark(n_block_train=40, n_block_eval=8, n_bar_train=12, block_n=10, bar_nx=10,
-              linear_solver="gpu-fp32", log=None):
+def benchmark(n_block_train=100, n_block_eval=50, block_batch=50, n_bar_train=12, block_n=10,
+              bar_nx=20, linear_solver="gpu-tc", log=None):
     """Newton iterations per load step, plain vs learned start, at a 1e-8
     residual tolerance, on the two problem families, with K(2) factored on the
     device (sized so that a run takes a minute or two on one GPU):
       blocks: block_n^3 SOLID81 on the unit cube, C10 ~ U(0.2, 1), K ~ U(500,
-              5000), stretch ~ U(1, 2), 20 load steps; trained on n_block_train
-              solves, evaluated on n_block_eval held-out seeds;
+              5000), stretch ~ U(1, 2), 20 load steps, solved block_batch at a
+              time in lock step (batch_newton.BatchNewton); trained on
+              n_block_train solves, evaluated on n_block_eval held-out seeds;
       bar:    bar_nx x bar_nx x 4 bar_nx torsion + stretch bar (rigid-body MPC
               end) at C10 = 0.5, K = 1000, stretch 2.0, 90 deg, 50 load steps;
               the network is trained on 3x3x12 bars with C10 ~ U(0.3, 0.7),
@@ -455,17 +456,23 @@ def benchmark(n_block_train=40, n_block_eval=8, n_bar_train=12, block_n=10, bar_
               coarse modes live on the normalised geometry, so it carries over).
     Also FP64 vs mixed assembly iteration counts on that bar."""
     import time
+    fronts = {"gpu": "fp64", "gpu-fp32": "fp32", "gpu-tc": "fp32-tc"}[linear_solver]
     out = {}
     t0 = time.perf_counter()
-    X, Y, _ = generate(sample_block_problems(n_block_train, n=block_n, seed=11),
-                       linear_solver=linear_solver)
+    solvers = {}
+    X, Y, train_its, failed, _ = generate_batched(
+        sample_block_problems(n_block_train, n=block_n, seed=11), fronts=fronts,
+        batch_size=block_batch, solvers=solvers)
     mlp = MLP(seed=0)
     h = mlp.fit(X, Y, epochs=300, batch=128, lr=2e-3)
-    out["blocks"] = evaluate(sample_block_problems(n_block_eval, n=block_n, seed=99), mlp,
-                             linear_solver=linear_solver)
+    out["blocks"] = evaluate_batched(sample_block_problems(n_block_eval, n=block_n, seed=99), mlp,
+                                     fronts=fronts, batch_size=block_batch, solvers=solvers)
     out["blocks"].update({"train_samples": int(X.shape[0]), "final_loss": h[-1][1],
                           "mesh": f"{block_n}x{block_n}x{block_n} SOLID81", "load_steps": 20,
-                          "train_solves": n_block_train})
+                          "train_solves": n_block_train, "train_failed": failed,
+                          "train_plain_iterations": float(np.mean(train_its)),
+                          "driver": f"batched lock-step Newton, {block_batch} solves per batch"})
+    solvers.clear()
     if log:
         log(f"blocks: {out['blocks']}")
     Xb, Yb, _ = generate(sample_bar_problems(n_bar_train, nx=3, nz=12, seed=5, n_loadsteps=50),
