@@ -1039,8 +1039,14 @@ __global__ void __launch_bounds__(kThreads)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nwarps = blockDim.x / 32;
   for (int64_t c = warp; c < k; c += nwarps) {
-    double acc = 0.0;
-    for (int64_t i = k + lane; i < m; i += 32) acc += (double)F[i + c * m] * xf[rows[i]];
+    double acc = 0.0, acc2 = 0.0;
+    int64_t i = k + lane;
+    for (; i + 32 < m; i += 64) {
+      acc += (double)F[i + c * m] * xf[rows[i]];
+      acc2 += (double)F[i + 32 + c * m] * xf[rows[i + 32]];
+    }
+    if (i < m) acc += (double)F[i + c * m] * xf[rows[i]];
+    acc += acc2;
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
     if (lane == 0) v[c] -= acc;
   }
@@ -1099,8 +1105,14 @@ __global__ void bwd_rest_kernel(BigBatch b, LdltDev d, const T* __restrict__ fro
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t cend = cbeg + 32 < k ? cbeg + 32 : k;
   for (int64_t c = cbeg + warp; c < cend; c += blockDim.x / 32) {
-    double acc = 0.0;
-    for (int64_t i = k + lane; i < m; i += 32) acc += (double)F[i + c * m] * xf[rows[i]];
+    double acc = 0.0, acc2 = 0.0;
+    int64_t i = k + lane;
+    for (; i + 32 < m; i += 64) {
+      acc += (double)F[i + c * m] * xf[rows[i]];
+      acc2 += (double)F[i + 32 + c * m] * xf[rows[i + 32]];
+    }
+    if (i < m) acc += (double)F[i + c * m] * xf[rows[i]];
+    acc += acc2;
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
     if (lane == 0) v[c] -= acc;
   }
@@ -1168,9 +1180,18 @@ __global__ void __launch_bounds__(kThreads)
   const int64_t i = r0 + threadIdx.x;
   if (i < m) {
     const T* Fi = F + i + o0 * m;
-    double acc = 0.0;
-    for (int c = 0; c < ob; c++) acc += (double)Fi[(int64_t)c * m] * yb[c];
-    v[i] -= acc;
+    // four independent partial sums (the FP64 FMA latency, not its rate,
+    // bounds one long chain)
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    int c = 0;
+    for (; c + 3 < ob; c += 4) {
+      a0 += (double)Fi[(int64_t)c * m] * yb[c];
+      a1 += (double)Fi[(int64_t)(c + 1) * m] * yb[c + 1];
+      a2 += (double)Fi[(int64_t)(c + 2) * m] * yb[c + 2];
+      a3 += (double)Fi[(int64_t)(c + 3) * m] * yb[c + 3];
+    }
+    for (; c < ob; c++) a0 += (double)Fi[(int64_t)c * m] * yb[c];
+    v[i] -= (a0 + a1) + (a2 + a3);
   }
 }
 
