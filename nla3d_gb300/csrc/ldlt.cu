@@ -1144,16 +1144,36 @@ __global__ void __launch_bounds__(kThreads)
   for (int p = 0; p < ob; p += kPanel) {
     const int cb = ob - p < kPanel ? ob - p : kPanel;
     const T* Li = Linv + b.li_off[blockIdx.x] + (uint64_t)((o0 + p) / kPanel) * kPanel * kPanel;
+    // the dot products in four independent partial sums (latency, not rate,
+    // bounds one chain)
     double y = 0.0;
-    if (t < cb)
-      for (int c = 0; c <= t; c++) y += (double)Li[t + c * kPanel] * vb[p + c];
+    if (t < cb) {
+      double y1 = 0.0, y2 = 0.0, y3 = 0.0;
+      int c = 0;
+      for (; c + 3 <= t; c += 4) {
+        y += (double)Li[t + c * kPanel] * vb[p + c];
+        y1 += (double)Li[t + (c + 1) * kPanel] * vb[p + c + 1];
+        y2 += (double)Li[t + (c + 2) * kPanel] * vb[p + c + 2];
+        y3 += (double)Li[t + (c + 3) * kPanel] * vb[p + c + 3];
+      }
+      for (; c <= t; c++) y += (double)Li[t + c * kPanel] * vb[p + c];
+      y = (y + y1) + (y2 + y3);
+    }
     __syncthreads();
     if (t < cb) vb[p + t] = y;
     __syncthreads();
     for (int i = p + cb + t; i < ob; i += blockDim.x) {
-      double acc = 0.0;
-      for (int c = 0; c < cb; c++) acc += (double)F[(o0 + i) + (o0 + p + c) * m] * vb[p + c];
-      vb[i] -= acc;
+      const T* Fi = F + (o0 + i) + (o0 + p) * m;
+      double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+      int c = 0;
+      for (; c + 3 < cb; c += 4) {
+        a0 += (double)Fi[(int64_t)c * m] * vb[p + c];
+        a1 += (double)Fi[(int64_t)(c + 1) * m] * vb[p + c + 1];
+        a2 += (double)Fi[(int64_t)(c + 2) * m] * vb[p + c + 2];
+        a3 += (double)Fi[(int64_t)(c + 3) * m] * vb[p + c + 3];
+      }
+      for (; c < cb; c++) a0 += (double)Fi[(int64_t)c * m] * vb[p + c];
+      vb[i] -= (a0 + a1) + (a2 + a3);
     }
     __syncthreads();
   }
@@ -1215,16 +1235,34 @@ __global__ void __launch_bounds__(kThreads)
     const int cb = ob - p < kPanel ? ob - p : kPanel;
     const T* Li = Linv + b.li_off[blockIdx.x] + (uint64_t)((o0 + p) / kPanel) * kPanel * kPanel;
     double x = 0.0;
-    if (t < cb)
-      for (int c = t; c < cb; c++) x += (double)Li[c + t * kPanel] * tb[p + c];
+    if (t < cb) {
+      const T* Lt = Li + (int64_t)t * kPanel;
+      double x1 = 0.0, x2 = 0.0, x3 = 0.0;
+      int c = t;
+      for (; c + 3 < cb; c += 4) {
+        x += (double)Lt[c] * tb[p + c];
+        x1 += (double)Lt[c + 1] * tb[p + c + 1];
+        x2 += (double)Lt[c + 2] * tb[p + c + 2];
+        x3 += (double)Lt[c + 3] * tb[p + c + 3];
+      }
+      for (; c < cb; c++) x += (double)Lt[c] * tb[p + c];
+      x = (x + x1) + (x2 + x3);
+    }
     __syncthreads();
     if (t < cb) tb[p + t] = x;
     __syncthreads();
     for (int j = t; j < p; j += blockDim.x) {
       const T* Fj = F + (o0 + p) + (o0 + j) * m;
-      double acc = 0.0;
-      for (int c = 0; c < cb; c++) acc += (double)Fj[c] * tb[p + c];
-      tb[j] -= acc;
+      double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+      int c = 0;
+      for (; c + 3 < cb; c += 4) {
+        a0 += (double)Fj[c] * tb[p + c];
+        a1 += (double)Fj[c + 1] * tb[p + c + 1];
+        a2 += (double)Fj[c + 2] * tb[p + c + 2];
+        a3 += (double)Fj[c + 3] * tb[p + c + 3];
+      }
+      for (; c < cb; c++) a0 += (double)Fj[c] * tb[p + c];
+      tb[j] -= (a0 + a1) + (a2 + a3);
     }
     __syncthreads();
   }
