@@ -56,3 +56,28 @@ def test_batched_learned_start_reduces_newton_iterations():
                              solvers=solvers)
     assert res["failed"] == {"plain": 0, "extrapolation": 0, "learned": 0}
     assert res["learned"] < res["plain"], res
+
+
+def test_batch_matches_single_problem_driver_with_mpc_rows():
+    """Torsion bars with a rigid-body MPC end (Lagrange multiplier rows in
+    K(2)): the batched residual removes the multipliers' forces per problem
+    as the one-problem driver does, so the iteration counts agree."""
+    pytest.importorskip("torch")
+    import math
+    from nla3d_gb300 import learned as L
+    from nla3d_gb300.batch_newton import BatchNewton
+    from nla3d_gb300.storage import FEStorage
+    problems = [L.bar_problem(2, 6, c10, 1000.0, st, math.radians(tw), n_loadsteps=10)
+                for c10, st, tw in ((0.4, 1.3, 30.0), (0.6, 1.5, 45.0))]
+    drv = BatchNewton(problems, precision="fp64", fronts="fp64")
+    assert drv.nm > 0
+    drv.solve()
+    assert not drv.failed.any()
+    U = drv.U.cpu().numpy()
+    for j, pb in enumerate(problems):
+        be = FEStorage(pb.mesh, "fp64").initSolutionData()
+        s, _ = L.solve(pb, be, linear_solver="gpu")
+        s.close()
+        assert drv.iterations[j].tolist() == [r.iterations for r in s.records], j
+        assert np.abs(U[j] - s.U).max() <= 1e-8 * np.abs(s.U).max()
+    drv.close()
