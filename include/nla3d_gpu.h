@@ -227,7 +227,8 @@ int nla3d_get_K_all(nla3d_ctx* ctx, double* values);
 /* nla3d_assemble, then the K blocks and F copied into host arrays (what
  * nla3d_get_K for blocks 1, 12, 2 and nla3d_get_F return), with the copies
  * overlapping the assembly: the element kernel runs over n_chunks element
- * ranges (1..64), and after each range the runs of K slots whose last
+ * ranges (1..64; range k holds n_chunks - k parts of n_chunks (n_chunks + 1)
+ * / 2, the shortest last), and after each range the runs of K slots whose last
  * contributing element is done (and that are at least 65,536 slots long)
  * are summed and copied while the next range computes; the rest, MPC terms
  * included, comes after the last range.  Same values as the unchunked path,

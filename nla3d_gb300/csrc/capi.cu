@@ -1121,8 +1121,16 @@ constexpr uint64_t kMaxGap = 1u << 20;
 int make_chunk_plan(nla3d_ctx* c, int n) {
   const uint64_t E = c->E(), nnz = c->Ktot();
   const uint32_t align = c->hm[0].etype == NLA3D_SOLID81 ? 4u : 1u;
+  // range k holds a share n - k of n (n + 1) / 2 of the elements: long
+  // ranges first, while their finished slots stream to the host behind
+  // them; short ranges last, so that little is left to sum and copy after
+  // the last one
   std::vector<uint32_t> eb(n + 1, 0);
-  for (int k = 1; k < n; k++) eb[k] = (uint32_t)((E * (uint64_t)k / n) / align * align);
+  const uint64_t total_w = (uint64_t)n * (n + 1) / 2;
+  for (int k = 1; k < n; k++) {
+    const uint64_t w = (uint64_t)k * n - (uint64_t)k * (k - 1) / 2;
+    eb[k] = (uint32_t)((E * w / total_w) / align * align);
+  }
   eb[n] = (uint32_t)E;
   for (int k = 1; k <= n; k++) eb[k] = std::max(eb[k], eb[k - 1]);
   std::vector<uint8_t> r(nnz, 0);
