@@ -476,11 +476,11 @@ int nla3d_ldlt_info(const nla3d_ldlt* h, double* out);
 const char* nla3d_ldlt_last_error(const nla3d_ldlt* h);
 /* Self-check of the tensor-core updates (precision 2): one front of m rows
  * (65 .. 4096) after its first outer block (256 columns when m > 512, else
- * 64), updated from the same random data by the FMA kernel and by both
- * tcgen05 kernels (operands staged through registers; operands packed once,
- * then bulk-copied); out[0] = max |difference| to the FMA result, out[1] =
- * max |update|.  NLA3D_ERR_RANGE if an MMA or copy wait timed out.
- * Synchronises the device. */
+ * 64), updated from the same random data by the FMA kernel and by the
+ * tcgen05 path (operands packed once, then bulk-copied by the persistent
+ * kernel); out[0] = max |difference|, out[1] = max |update|.
+ * NLA3D_ERR_RANGE if an MMA or copy wait timed out.  Synchronises the
+ * device. */
 int nla3d_ldlt_tc_check(int m, double* out);
 int nla3d_ldlt_destroy(nla3d_ldlt* h);
 

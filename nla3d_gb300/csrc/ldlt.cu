@@ -461,27 +461,17 @@ struct TrailingShape<float> {
   static constexpr int BT = 128, RT = 8;
 };
 
-// ---- the FP32 updates on the tensor cores (tcgen05, kind::tf32) ----
+// ---- tensor-core helpers (tcgen05, kind::tf32) ----
 //
-// One CTA (256 threads) per 128 x 128 tile of an update (batched_trailing_
-// kernel's inner and outer ranges), over kw <= 256 operand columns in chunks
-// of 32.  Each chunk of L[i0:i0+128, lc0+c] and W[j0:j0+128, wc0+c] is split
-// into TF32 high and low parts (x = hi + lo, hi = x rounded to TF32) and
-// staged in shared memory in the canonical K-major layout without swizzle
-// (8-row x 16-byte core matrices; K-adjacent cores 128 B apart, 8-row groups
-// 1 KB apart).  One thread issues 4 k-steps x 3 MMAs per chunk (hi.hi +
-// hi.lo + lo.hi, FP32 accumulation in 128 TMEM columns) and commits them to
-// an mbarrier; the next chunk is staged once they have released the
-// buffers.  After the last chunk each warp reads 32 TMEM lanes (rows) x 64
-// columns and subtracts them from the front: the tile is read and written
-// once per outer block.  64 KB of shared memory and 128 TMEM columns per
-// CTA, so that three CTAs share an SM and one's loads overlap another's
-// MMAs and epilogue.  Every wait on the mbarrier is bounded: on a timeout
-// the tile is left unchanged and err[0] is set.
-constexpr int kTcM = 128, kTcN = 128, kTcKH = 32;   // tile rows, columns, K per half
-constexpr int kTcThreads = 256;
-constexpr uint32_t kTcTileFloats = kTcM * kTcKH;     // one 128 x 32 operand half
-constexpr size_t kTcSmem = 4 * kTcTileFloats * sizeof(float) + 64;
+// Operands are split into TF32 high and low parts (x = hi + lo, hi = x
+// rounded to TF32) and staged in shared memory in the canonical K-major
+// layout without swizzle (8-row x 16-byte core matrices; K-adjacent cores
+// 128 B apart, 8-row groups 1 KB apart); an update tile is 128 x 128, its
+// operands taken in chunks of 32 columns, each chunk 4 k-steps x 3 MMAs
+// (hi.hi + hi.lo + lo.hi, FP32 accumulation in TMEM).
+constexpr int kTcM = 128, kTcN = 128, kTcKH = 32;   // tile rows, columns, K per chunk
+constexpr int kTcThreads = 256;                      // the packing kernel's block
+constexpr uint32_t kTcTileFloats = kTcM * kTcKH;     // one 128 x 32 operand chunk
 // instruction descriptor: D F32 (bit 4), A and B TF32 (bits 7, 10), both
 // K-major, N / 8 at bit 17, M / 16 at bit 24
 constexpr uint32_t kTcIdesc =
@@ -505,7 +495,7 @@ __device__ __forceinline__ float tf32_hi(float x) {
   return __uint_as_float(r);
 }
 
-// offset (floats) of element (row r, k) of a 128 x 32 K-major operand half
+// offset (floats) of element (row r, k) of a 128 x 32 K-major operand chunk
 __device__ __forceinline__ uint32_t tc_off(int r, int k) {
   return (uint32_t)(((r >> 3) * (kTcKH / 4) + (k >> 2)) * 32 + (r & 7) * 4 + (k & 3));
 }
@@ -531,139 +521,15 @@ __device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t a, uint64_t b, ui
       "l"(a), "l"(b), "r"(kTcIdesc), "r"(acc));
 }
 
-__global__ void __launch_bounds__(kTcThreads)
-    tc_trailing_kernel(BigBatch b, LdltDev d, float* __restrict__ front, int64_t p0, int outer,
-                       const float* __restrict__ Wbuf, int* __restrict__ err) {
-  const int ti = blockIdx.x, tj = blockIdx.y;
-  if (tj > ti) return;
-  const int s = b.list[blockIdx.z];
-  const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
-  const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
-  UpdateRange ur;
-  if (!update_range(p0, outer, k, m, ur)) return;
-  const int64_t i0 = ur.jb + (int64_t)ti * kTcM, j0 = ur.jb + (int64_t)tj * kTcN;
-  if (i0 >= m || j0 >= ur.je) return;
-  float* F = front + d.front_off[s];
-  const float* W = Wbuf + b.w_off[blockIdx.z];
-  const int kw = (int)ur.kw;
-  const int n_chunks = (kw + kTcKH - 1) / kTcKH;
-  extern __shared__ __align__(1024) unsigned char tc_smem[];
-  float* Ahi = reinterpret_cast<float*>(tc_smem);
-  float* Alo = Ahi + kTcTileFloats;
-  float* Bhi = Alo + kTcTileFloats;
-  float* Blo = Bhi + kTcTileFloats;
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(Blo + kTcTileFloats);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + 1);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
-                     smem_addr(tmem_slot)),
-                 "r"(kTcN));
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-  }
-  if (threadIdx.x == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(mbar)), "r"(1));
-    asm volatile("fence.mbarrier_init.release.cluster;");
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  const uint32_t tmem = *tmem_slot;
-  const int r = threadIdx.x % kTcM, kq = threadIdx.x / kTcM;   // row, which 16 of the 32
-  const int64_t ia = i0 + r, jr = j0 + r;
-  const uint32_t lbo = 128, sbo = (kTcKH / 4) * 128;
-  bool ok = true;
-  for (int h = 0; h < n_chunks && ok; h++) {
-    if (h > 0) ok = tc_wait(smem_addr(mbar), (uint32_t)(h - 1) & 1u);   // buffers released
-    if (ok) {
-      // all 32 loads of this thread in flight first, then split and store
-      float av[16], wv[16];
-#pragma unroll
-      for (int q = 0; q < 16; q++) {
-        const int c = h * kTcKH + kq * 16 + q;
-        av[q] = (c < kw && ia < m) ? F[ia + (ur.lc0 + c) * m] : 0.0f;
-        wv[q] = (c < kw && jr < ur.je) ? W[jr + (ur.wc0 + c) * m] : 0.0f;
-      }
-#pragma unroll
-      for (int q = 0; q < 16; q++) {
-        const float ah = tf32_hi(av[q]), wh = tf32_hi(wv[q]);
-        const uint32_t o = tc_off(r, kq * 16 + q);
-        Ahi[o] = ah;
-        Alo[o] = av[q] - ah;
-        Bhi[o] = wh;
-        Blo[o] = wv[q] - wh;
-      }
-    }
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    ok = __syncthreads_and(ok ? 1 : 0) != 0;
-    if (ok && threadIdx.x == 0) {
-      const uint32_t ahi = smem_addr(Ahi), alo = smem_addr(Alo);
-      const uint32_t bhi = smem_addr(Bhi), blo = smem_addr(Blo);
-      for (int st = 0; st < kTcKH / 8; st++) {
-        const uint32_t koff = st * 256;   // 8 K values = two core matrices
-        const uint64_t dah = tc_desc(ahi + koff, lbo, sbo), dal = tc_desc(alo + koff, lbo, sbo);
-        const uint64_t dbh = tc_desc(bhi + koff, lbo, sbo), dbl = tc_desc(blo + koff, lbo, sbo);
-        tc_mma(tmem, dah, dbh, (h > 0 || st > 0) ? 1u : 0u);
-        tc_mma(tmem, dah, dbl, 1u);
-        tc_mma(tmem, dal, dbh, 1u);
-      }
-      asm volatile(
-          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-              smem_addr(mbar))
-          : "memory");
-    }
-  }
-  if (ok) ok = tc_wait(smem_addr(mbar), (uint32_t)(n_chunks - 1) & 1u);
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  ok = __syncthreads_and(ok ? 1 : 0) != 0;
-  if (!ok) {
-    if (threadIdx.x == 0) atomicExch(err, 1);
-  } else {
-    // warp w: TMEM lanes 32 (w % 4) .. +31 = tile rows, columns 64 (w / 4) .. +63
-    const int row = (warp & 3) * 32 + lane;
-    const int64_t i = i0 + row;
-    for (int c0 = (warp >> 2) * 64; c0 < (warp >> 2) * 64 + 64; c0 += 16) {
-      uint32_t v[16];
-      const uint32_t taddr = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)c0;
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
-          "%11, %12, %13, %14, %15}, [%16];"
-          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
-            "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
-            "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-          : "r"(taddr));
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      if (i < m)
-#pragma unroll
-        for (int q = 0; q < 16; q++) {
-          const int64_t j = j0 + c0 + q;
-          if (j < ur.je && j <= i) F[i + j * m] -= __uint_as_float(v[q]);
-        }
-    }
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  __syncthreads();
-  if (warp == 0) {
-    // after a timeout the MMAs may still run: give them another bounded wait
-    if (!ok) {
-      tc_wait(smem_addr(mbar), 0);
-      tc_wait(smem_addr(mbar), 1);
-    }
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcN));
-  }
-}
-
-// ---- the outer-block update from packed operands (tensor-core fronts) ----
+// ---- the updates from packed operands (tensor-core fronts) ----
 //
-// The rank-256 update after an outer block reads the same operands from
-// every tile of a row or column: L[jb + 128 r .. +127][o0 .. o0 + kw) and
-// W[jb + 128 r .. +127][0 .. kw).  pack_outer_kernel splits them into TF32
-// high and low parts once per outer block and stores them, per 128-row block
-// r and 32-column chunk c, as four 16 KB tiles (A hi, A lo, B hi, B lo) in
-// the MMA's shared-memory layout (tc_off).  tc_outer_kernel is persistent
+// An update (update_range: the rank-256 one after an outer block, or a
+// panel's rank-64 one inside its block) reads the same operands from every
+// tile of a row or column: L[jb + 128 r .. +127][lc0 .. lc0 + kw) and
+// W[jb + 128 r .. +127][wc0 .. wc0 + kw).  pack_update_kernel splits them
+// into TF32 high and low parts once per update and stores them, per 128-row
+// block r and 32-column chunk c, as four 16 KB tiles (A hi, A lo, B hi, B lo)
+// in the MMA's shared-memory layout (tc_off).  tc_packed_kernel is persistent
 // (one CTA per SM walking a host-built list of the level's tiles) and
 // warp-specialised:
 //   warp 0 (one lane): copies each chunk's four tiles into a ring of
@@ -687,16 +553,16 @@ constexpr uint32_t kPkTile = kTcTileFloats;                // floats per 128 x 3
 constexpr uint32_t kPkBlock = 4 * kPkTile * kPkChunks;    // floats per 128-row block
 constexpr int kPkStages = 3;
 constexpr size_t kPkSmem = (size_t)kPkStages * 4 * kPkTile * sizeof(float) + 256;
-constexpr int kOuterThreads = 320;   // producer, MMA, 8 epilogue warps
+constexpr int kOuterThreads = 320;   // tc_packed_kernel: producer, MMA, 8 epilogue warps
 
 __global__ void __launch_bounds__(kTcThreads)
-    pack_outer_kernel(BigBatch b, LdltDev d, const float* __restrict__ front, int64_t o0,
-                      const float* __restrict__ Wbuf, float* __restrict__ packed) {
+    pack_update_kernel(BigBatch b, LdltDev d, const float* __restrict__ front, int64_t p0,
+                       int outer, const float* __restrict__ Wbuf, float* __restrict__ packed) {
   const int s = b.list[blockIdx.z];
   const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
   const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
   UpdateRange ur;
-  if (!update_range(o0, 1, k, m, ur)) return;
+  if (!update_range(p0, outer, k, m, ur)) return;
   const int rb = blockIdx.x, ch = blockIdx.y;
   const int64_t r0 = ur.jb + (int64_t)rb * kTcM;
   if (r0 >= m || ch * kTcKH >= ur.kw) return;
@@ -718,7 +584,7 @@ __global__ void __launch_bounds__(kTcThreads)
       const int c = ch * kTcKH + g * 4 + e;
       const bool in = c < ur.kw && i < m;
       const float av = in ? F[i + (ur.lc0 + c) * m] : 0.0f;
-      const float wv = in ? W[i + (ur.wc0 + c) * m] : 0.0f;
+      const float wv = in && i < ur.je ? W[i + (ur.wc0 + c) * m] : 0.0f;   // B: columns < je
       ahp[e] = tf32_hi(av);
       alp[e] = av - ahp[e];
       whp[e] = tf32_hi(wv);
@@ -752,9 +618,9 @@ struct OuterTile {
 };
 
 __global__ void __launch_bounds__(kOuterThreads, 1)
-    tc_outer_kernel(BigBatch b, LdltDev d, float* __restrict__ front, int64_t o0,
-                    const float* __restrict__ packed, const OuterTile* __restrict__ tiles,
-                    int n_tiles, int* __restrict__ err) {
+    tc_packed_kernel(BigBatch b, LdltDev d, float* __restrict__ front, int64_t p0, int outer,
+                     const float* __restrict__ packed, const OuterTile* __restrict__ tiles,
+                     int n_tiles, int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char pk_smem[];
   float* stage0 = reinterpret_cast<float*>(pk_smem);
   uint64_t* full = reinterpret_cast<uint64_t*>(stage0 + (size_t)kPkStages * 4 * kPkTile);
@@ -792,7 +658,7 @@ __global__ void __launch_bounds__(kOuterThreads, 1)
   };
   // the front of a tile: rows m, update range, chunks
   struct TileInfo {
-    int64_t m, i0, j0;
+    int64_t m, je, i0, j0;
     int nch;
     const float* pa;
     const float* pb;
@@ -804,9 +670,10 @@ __global__ void __launch_bounds__(kOuterThreads, 1)
     const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
     const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
     UpdateRange ur;
-    update_range(o0, 1, k, m, ur);   // the host listed only fronts whose range is not empty
+    update_range(p0, outer, k, m, ur);   // the host listed only fronts whose range is not empty
     const uint32_t rI = ot.tij >> 16, rJ = ot.tij & 0xFFFFu;
     ti.m = m;
+    ti.je = ur.je;
     ti.i0 = ur.jb + (int64_t)rI * kTcM;
     ti.j0 = ur.jb + (int64_t)rJ * kTcN;
     ti.nch = (int)((ur.kw + kTcKH - 1) / kTcKH);
@@ -908,7 +775,7 @@ __global__ void __launch_bounds__(kOuterThreads, 1)
       // the front's values of the first 32 columns first: their loads overlap
       // the tile's MMAs; the second 32 load while the first are stored
       float* fp = ti.F + i + (ti.j0 + cb) * ti.m;   // (i, j0 + cb); column stride m
-      const int64_t jlim = (row_in ? (i < ti.m - 1 ? i : ti.m - 1) : -1) - (ti.j0 + cb);
+      const int64_t jlim = (row_in ? (i < ti.je - 1 ? i : ti.je - 1) : -1) - (ti.j0 + cb);
       float cv[32];
 #pragma unroll
       for (int q = 0; q < 32; q++) cv[q] = q <= jlim ? fp[q * ti.m] : 0.0f;
@@ -1459,6 +1326,7 @@ struct nla3d_ldlt {
     int64_t wo_off = 0;                   // their W offsets in d_wo
     int64_t large_max_m = 0, large_max_k = 0;
     std::vector<int64_t> tile_off, tile_cnt;  // tensor-core fronts: per outer block, its tiles
+    std::vector<int64_t> itile_off, itile_cnt;  // and per panel, its in-block update's tiles
     std::vector<int64_t> ea_off, ea_cnt;  // children of the level's parents, by ordinal
     std::vector<uint32_t> ea_gy;          // column blocks per child (its update's size)
   };
@@ -1537,18 +1405,13 @@ cudaError_t enqueue_factor(nla3d_ldlt* h, const double* values) {
       const unsigned nf = (unsigned)L.large_cnt;
       constexpr int BT = TrailingShape<T>::BT, RT = TrailingShape<T>::RT;
       const bool tc = std::is_same<T, float>::value && h->tc;
-      // one update launch: rows from its range's first column to the largest
-      // front's last row, `col_tiles` tiles of columns
+      // one FMA update launch: rows from its range's first column to the
+      // largest front's last row, `col_tiles` tiles of columns
       auto update = [&](int64_t p, int outer, int64_t rows, unsigned col_tiles) {
         const unsigned rt = (unsigned)((rows + BT - 1) / BT);
         const dim3 grid(rt, std::min(rt, col_tiles), nf);
-        if (tc)
-          tc_trailing_kernel<<<grid, kTcThreads, kTcSmem, st>>>(
-              bb, h->dev, reinterpret_cast<float*>(front), p, outer,
-              reinterpret_cast<const float*>(W), h->d_err);
-        else
-          batched_trailing_kernel<T, BT, RT><<<grid, kThreads, 0, st>>>(bb, h->dev, front, p,
-                                                                         outer, W);
+        batched_trailing_kernel<T, BT, RT><<<grid, kThreads, 0, st>>>(bb, h->dev, front, p,
+                                                                       outer, W);
       };
       for (int64_t o0 = 0; o0 < L.large_max_k; o0 += kOuter) {
         const int64_t o_end = std::min<int64_t>(o0 + kOuter, L.large_max_k);
@@ -1562,22 +1425,35 @@ cudaError_t enqueue_factor(nla3d_ldlt* h, const double* values) {
                                                                          Li, W);
           // the panel's columns into the rest of its outer block (at most
           // kOuter - kPanel columns)
-          if (p0 + kPanel < o_end)
-            update(p0, 0, rest, (unsigned)((kOuter - kPanel + BT - 1) / BT));
+          if (p0 + kPanel < o_end) {
+            const int64_t pi = p0 / kPanel;
+            if (tc && L.itile_cnt[pi] > 0) {
+              const unsigned rb = (unsigned)((rest + kTcM - 1) / kTcM);
+              pack_update_kernel<<<dim3(rb, kPanel / kTcKH, nf), kTcThreads, 0, st>>>(
+                  bb, h->dev, reinterpret_cast<const float*>(front), p0, 0,
+                  reinterpret_cast<const float*>(W), h->d_pk);
+              const int nt = (int)L.itile_cnt[pi];
+              tc_packed_kernel<<<(unsigned)std::min(nt, h->n_sm), kOuterThreads, kPkSmem, st>>>(
+                  bb, h->dev, reinterpret_cast<float*>(front), p0, 0, h->d_pk,
+                  h->d_tiles + L.itile_off[pi], nt, h->d_err);
+            } else if (!tc) {
+              update(p0, 0, rest, (unsigned)((kOuter - kPanel + BT - 1) / BT));
+            }
+          }
         }
         // the outer block into every column after it (tensor-core fronts:
         // its operands packed once, then the tiles with bulk copies)
         const int64_t rest = L.large_max_m - o0 - 1;
         if (rest > 0 && tc) {
           const unsigned rb = (unsigned)((rest + kTcM - 1) / kTcM);
-          pack_outer_kernel<<<dim3(rb, kPkChunks, nf), kTcThreads, 0, st>>>(
-              bb, h->dev, reinterpret_cast<const float*>(front), o0,
+          pack_update_kernel<<<dim3(rb, kPkChunks, nf), kTcThreads, 0, st>>>(
+              bb, h->dev, reinterpret_cast<const float*>(front), o0, 1,
               reinterpret_cast<const float*>(W), h->d_pk);
           const int64_t ob = o0 / kOuter;
           const int nt = (int)L.tile_cnt[ob];
           if (nt > 0)
-            tc_outer_kernel<<<(unsigned)std::min(nt, h->n_sm), kOuterThreads, kPkSmem, st>>>(
-                bb, h->dev, reinterpret_cast<float*>(front), o0, h->d_pk,
+            tc_packed_kernel<<<(unsigned)std::min(nt, h->n_sm), kOuterThreads, kPkSmem, st>>>(
+                bb, h->dev, reinterpret_cast<float*>(front), o0, 1, h->d_pk,
                 h->d_tiles + L.tile_off[ob], nt, h->d_err);
         } else if (rest > 0) {
           update(o0, 1, rest, ~0u);
@@ -1764,6 +1640,25 @@ int nla3d_ldlt_create(int64_t n, const uint32_t* iofeir, const uint32_t* columns
         }
         lv.tile_cnt.push_back((int64_t)tiles.size() - lv.tile_off.back());
       }
+      // every panel's in-block update (update_range, inner): rows from
+      // jb = p0 + pb, columns jb .. min(o0 + kOuter, k)
+      for (int64_t p0 = 0; p0 < lv.large_max_k; p0 += kPanel) {
+        lv.itile_off.push_back((int64_t)tiles.size());
+        const int64_t o0 = p0 - p0 % kOuter;
+        for (int64_t z = 0; z < lv.large_cnt; z++) {
+          const int32_t s = lists[lv.large_off + z];
+          const int64_t k = S.k(s), m = S.m(s);
+          if (p0 >= k) continue;
+          const int64_t jb = p0 + std::min<int64_t>(kPanel, k - p0);
+          const int64_t je = std::min<int64_t>(o0 + kOuter, k);
+          if (jb >= je) continue;
+          const int64_t rb = (m - jb + kTcM - 1) / kTcM, cb = (je - jb + kTcN - 1) / kTcN;
+          for (int64_t ti = 0; ti < rb; ti++)
+            for (int64_t tj = 0; tj <= ti && tj < cb; tj++)
+              tiles.push_back(OuterTile{(uint32_t)z, (uint32_t)(ti << 16 | tj)});
+        }
+        lv.itile_cnt.push_back((int64_t)tiles.size() - lv.itile_off.back());
+      }
     }
     max_w = std::max(max_w, w);
     max_pk = std::max(max_pk, pk);
@@ -1860,9 +1755,7 @@ int nla3d_ldlt_create(int64_t n, const uint32_t* iofeir, const uint32_t* columns
   LCK(dalloc(h, &h->d_err, 1));
   LCK(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
   if (h->tc) {
-    LCK(cudaFuncSetAttribute(tc_trailing_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)kTcSmem));
-    LCK(cudaFuncSetAttribute(tc_outer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    LCK(cudaFuncSetAttribute(tc_packed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)kPkSmem));
     LCK(upload(h, &h->d_pko, pko));
     LCK(dalloc(h, &h->d_pk, (size_t)std::max<int64_t>(max_pk, 1)));
@@ -2170,9 +2063,9 @@ int nla3d_ldlt_solve_host(nla3d_ldlt* h, const double* values, const double* b_h
 int nla3d_ldlt_tc_check(int m, double* out) {
   // one front of m rows whose first kb pivots (one outer block: 256 when
   // m > 512, else 64) are done: the update of rows / columns kb .. m-1 by the
-  // FMA kernel and by both tensor-core kernels (operands staged through
-  // registers; operands packed, then bulk-copied) from the same random data;
-  // out[0] = max |difference| to the FMA result, out[1] = max |update|
+  // FMA kernel and by the tensor cores (operands packed, then bulk-copied by
+  // the persistent kernel) from the same random data; out[0] = max
+  // |difference|, out[1] = max |update|
   if (m < kPanel + 1 || m > 4096 || !out) return NLA3D_ERR_ARG;
   const int kb = m > 2 * kOuter ? kOuter : kPanel;
   const size_t mm = (size_t)m * m, mw = (size_t)m * kb;
@@ -2192,7 +2085,7 @@ int nla3d_ldlt_tc_check(int m, double* out) {
     if (e == cudaSuccess) allocs.push_back(*p);
     return e;
   };
-  float *F1 = nullptr, *F2 = nullptr, *F3 = nullptr, *dW = nullptr, *dP = nullptr;
+  float *F1 = nullptr, *F3 = nullptr, *dW = nullptr, *dP = nullptr;
   const size_t mp = (size_t)((m + kTcM - 1) / kTcM) * kPkBlock;
   std::vector<OuterTile> tl;   // the outer update's tiles, as the factorisation lists them
   const int rbk = (m - kb + kTcM - 1) / kTcM;
@@ -2206,7 +2099,6 @@ int nla3d_ldlt_tc_check(int m, double* out) {
   int64_t* rowp = nullptr;
   int32_t* snf = nullptr;
   cudaError_t e = dal((void**)&F1, mm * 4);
-  if (e == cudaSuccess) e = dal((void**)&F2, mm * 4);
   if (e == cudaSuccess) e = dal((void**)&F3, mm * 4);
   if (e == cudaSuccess) e = dal((void**)&dP, mp * 4);
   if (e == cudaSuccess) e = dal((void**)&dT, tl.size() * sizeof(OuterTile));
@@ -2226,7 +2118,6 @@ int nla3d_ldlt_tc_check(int m, double* out) {
   const int64_t rp[2] = {0, m};
   const int32_t sf[2] = {0, kb};
   if (e == cudaSuccess) e = cudaMemcpy(F1, F0.data(), mm * 4, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(F2, F0.data(), mm * 4, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(F3, F0.data(), mm * 4, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(dW, W.data(), mw * 4, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(err, 0, 4);
@@ -2236,10 +2127,7 @@ int nla3d_ldlt_tc_check(int m, double* out) {
   if (e == cudaSuccess) e = cudaMemcpy(rowp, rp, 16, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(snf, sf, 8, cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(tc_trailing_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)kTcSmem);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(tc_outer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    e = cudaFuncSetAttribute(tc_packed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)kPkSmem);
   int tc_err = 0;
   if (e == cudaSuccess) {
@@ -2252,17 +2140,15 @@ int nla3d_ldlt_tc_check(int m, double* out) {
     const unsigned t128 = (unsigned)((rest + 127) / 128);
     batched_trailing_kernel<float, 128, 8><<<dim3(t128, t128, 1), kThreads>>>(bb, d, F1, 0, 1,
                                                                                dW);
-    tc_trailing_kernel<<<dim3(t128, t128, 1), kTcThreads, kTcSmem>>>(bb, d, F2, 0, 1, dW, err);
-    pack_outer_kernel<<<dim3(t128, kPkChunks, 1), kTcThreads>>>(bb, d, F3, 0, dW, dP);
-    tc_outer_kernel<<<(unsigned)std::min<int>((int)tl.size(), n_sm), kOuterThreads, kPkSmem>>>(
-        bb, d, F3, 0, dP, dT, (int)tl.size(), err);
+    pack_update_kernel<<<dim3(t128, kPkChunks, 1), kTcThreads>>>(bb, d, F3, 0, 1, dW, dP);
+    tc_packed_kernel<<<(unsigned)std::min<int>((int)tl.size(), n_sm), kOuterThreads, kPkSmem>>>(
+        bb, d, F3, 0, 1, dP, dT, (int)tl.size(), err);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e == cudaSuccess) e = cudaMemcpy(&tc_err, err, 4, cudaMemcpyDeviceToHost);
   }
-  std::vector<float> R1(mm), R2(mm), R3(mm);
+  std::vector<float> R1(mm), R3(mm);
   if (e == cudaSuccess) e = cudaMemcpy(R1.data(), F1, mm * 4, cudaMemcpyDeviceToHost);
-  if (e == cudaSuccess) e = cudaMemcpy(R2.data(), F2, mm * 4, cudaMemcpyDeviceToHost);
   if (e == cudaSuccess) e = cudaMemcpy(R3.data(), F3, mm * 4, cudaMemcpyDeviceToHost);
   for (void* p : allocs) cudaFree(p);
   if (e != cudaSuccess) return NLA3D_ERR_CUDA;
@@ -2271,7 +2157,6 @@ int nla3d_ldlt_tc_check(int m, double* out) {
   for (int j = kb; j < m; j++)
     for (int i = j; i < m; i++) {
       const size_t q = (size_t)i + (size_t)j * m;
-      dmax = std::max(dmax, (double)std::fabs(R1[q] - R2[q]));
       dmax = std::max(dmax, (double)std::fabs(R1[q] - R3[q]));
       umax = std::max(umax, (double)std::fabs(R1[q] - F0[q]));
     }
