@@ -46,6 +46,22 @@ constexpr double kGaussA = 0.5773502691896258;        // isoparametric.h:127
 // Kuu entry t (assemble3 order, SOLID81.h:62-74) -> (a, i, b, k) packed.
 __constant__ uchar4 c_kuu_entry[kKuuPerElem];
 
+// FP64 kernel: the shape gradients of an element sum to zero at every Gauss
+// point (sum_b G_b = J^-1 sum_b dN_b/dxi = 0), so K(a,i; 7,k) = sum_g h_a . G_7
+// = -sum_{b<7} K(a,i; b,k).  The 63 entries of node 7's column (a < 7, all
+// nine (i,k)) are formed from the other 237 after the Gauss-point loop (7
+// adds each, in a fixed order) instead of 24 FMAs each inside it; they differ
+// from the direct sums by rounding only (|sum_b G_b| ~ eps |G|).
+constexpr int kKuuDerived = 63;
+constexpr int kKuuOwned = kKuuPerElem - kKuuDerived;                 // 237
+constexpr int kOwned64 = (kEPW * kKuuOwned + 31) / 32;               // per lane (30)
+// FP64 kernel block header: ownership words, stage positions, derived table
+constexpr size_t kHead64Bytes =
+    (sizeof(uint32_t) * kOwned64 * 32 + sizeof(uint16_t) * kOwned64 * 32 +
+     sizeof(uint16_t) * kKuuDerived * 8 + 15) / 16 * 16;
+__constant__ uint16_t c_kuu_owned[kKuuOwned];            // owned m -> assemble3 t
+__constant__ uint16_t c_kuu_derived[kKuuDerived * 8];    // target t, then its 7 sources
+
 // Mixed kernel: position in assemble3 order of the Kuu entry that
 // D[(i,k), a, b] = sum h_a[ik] . G_b (i <= k) stands for, at [(a * 6 +
 // hblock(i,k)) * 8 + b]: K(a,i; b,k) when a <= b, K(b,k; a,i) when a > b;
@@ -518,25 +534,32 @@ __global__ void __launch_bounds__(WPB * 32)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   // block header: the FP64 kernel's Kuu ownership words, the mixed kernel's
   // D -> assemble3 position table
-  uint32_t* dec = reinterpret_cast<uint32_t*>(smem_raw);  // [kOwned][32]
+  uint32_t* dec = reinterpret_cast<uint32_t*>(smem_raw);  // [kOwned64][32]
+  // FP64 kernel: each owned entry's stage position, and the derived entries'
+  // table (per-lane indices: shared memory, not the constant cache)
+  uint16_t* opos = reinterpret_cast<uint16_t*>(dec + kOwned64 * 32);   // [kOwned64][32]
+  uint16_t* dtab = opos + kOwned64 * 32;                               // [kKuuDerived][8]
   uint16_t* dpos = reinterpret_cast<uint16_t*>(smem_raw);  // [kDpos]
-  constexpr size_t kHead = kMixed ? kDposBytes : sizeof(uint32_t) * kOwned * 32;
+  constexpr size_t kHead = kMixed ? kDposBytes : kHead64Bytes;
   WarpSmem<TT>* sm = reinterpret_cast<WarpSmem<TT>*>(smem_raw + kHead) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
 
   if constexpr (kMixed) {
     for (int v = threadIdx.x; v < kDpos; v += blockDim.x) dpos[v] = c_dpos[v];
   } else
-  // Ownership of Kuu entries: lane owns x = lane + 32 m of the 4*300 entries
-  // of its warp's element quad.  Decode once: smem offsets of H[ik][.][slot a]
-  // and G[.][slot b].
-  for (int v = threadIdx.x; v < kOwned * 32; v += blockDim.x) {
+  // Ownership of Kuu entries: lane owns x = lane + 32 m of the 4*237 owned
+  // entries of its warp's element quad.  Decode once: smem offsets of
+  // H[ik][.][slot a] and G[.][slot b].
+  for (int v = threadIdx.x; v < kOwned64 * 32; v += blockDim.x) {
     const int m = v / 32, l = v % 32;
     const int x = l + 32 * m;
-    // entries past the quad's 1200 read slot 0 (in bounds) and are never written
+    // entries past the quad's 948 read slot 0 (in bounds) and are never written
     uint32_t word = 0u;
-    if (x < kEPW * kKuuPerElem) {
-      const int q = x / kKuuPerElem, t = x - q * kKuuPerElem;
+    uint16_t where = 0xFFFFu;
+    if (x < kEPW * kKuuOwned) {
+      const int q = x / kKuuOwned;
+      const int t = c_kuu_owned[x - q * kKuuOwned];
+      where = (uint16_t)(q * kKuuPerElem + t);
       const uchar4 en = c_kuu_entry[t];  // (a, i, b, k)
       // i <= k: h_a[ik] . G_b;  i > k: h_b[ki] . G_a (A symmetric)
       const bool up = en.y <= en.w;
@@ -546,7 +569,10 @@ __global__ void __launch_bounds__(WPB * 32)
       word = ho | (go << 16);
     }
     dec[m * 32 + l] = word;
+    opos[m * 32 + l] = where;
   }
+  if constexpr (!kMixed)
+    for (int v = threadIdx.x; v < kKuuDerived * 8; v += blockDim.x) dtab[v] = c_kuu_derived[v];
   __syncthreads();
 
   const uint32_t E = a.n_elems;  // end of this launch's element range
@@ -944,9 +970,9 @@ __global__ void __launch_bounds__(WPB * 32)
       }
       __syncwarp();
     } else {
-    TT acc[kOwned];
+    TT acc[kOwned64];
 #pragma unroll
-    for (int m = 0; m < kOwned; m++) acc[m] = (TT)0;
+    for (int m = 0; m < kOwned64; m++) acc[m] = (TT)0;
     double Fu[3] = {0.0, 0.0, 0.0};   // FP64 kernel (the mixed one wrote F_u and
     double Kup[3] = {0.0, 0.0, 0.0};  // K_up above)
     const int node = sub;
@@ -996,7 +1022,7 @@ __global__ void __launch_bounds__(WPB * 32)
         const TT* Hf = sm->H;
         const TT* Gf = &sm->G[0][0];
 #pragma unroll
-        for (int m = 0; m < kOwned; m++) {
+        for (int m = 0; m < kOwned64; m++) {
           const uint32_t word = dec[m * 32 + lane];
           const uint32_t ho = word & 0xFFFFu, go = word >> 16;
           TT v = acc[m];
@@ -1010,13 +1036,33 @@ __global__ void __launch_bounds__(WPB * 32)
     }
 
     // ---------------- write the element contributions ----------------
+    // the owned entries into the quad's stage (assemble3 order; A's scratch,
+    // dead after the Gauss-point loop), node 7's column from them, then all
+    // 4 x 300 written coalesced
+    TT* stage = &sm->A[0][0];
 #pragma unroll
+    for (int m = 0; m < kOwned64; m++) {
+      const uint16_t where = opos[m * 32 + lane];
+      if (where != 0xFFFFu) stage[where] = acc[m];
+    }
+    __syncwarp();
+    for (int dx = lane; dx < kEPW * kKuuDerived; dx += 32) {
+      const int qq = dx / kKuuDerived, j = dx - qq * kKuuDerived;
+      const TT* st = stage + qq * kKuuPerElem;
+      const uint16_t* dj = dtab + j * 8;
+      TT v = st[dj[1]];
+#pragma unroll
+      for (int c = 2; c < 8; c++) v += st[dj[c]];
+      stage[qq * kKuuPerElem + dj[0]] = -v;
+    }
+    __syncwarp();
+#pragma unroll 4
     for (int m = 0; m < kOwned; m++) {
       const int x = lane + 32 * m;
       if (x < kEPW * kKuuPerElem) {
         const int qq = x / kKuuPerElem, t = x - qq * kKuuPerElem;
         const uint32_t ee = e0 + qq;
-        if (ee < E) a.contribK[kdst((uint64_t)ee * kSolidKc + t)] = acc[m];
+        if (ee < E) a.contribK[kdst((uint64_t)ee * kSolidKc + t)] = stage[x];
       }
     }
     if (valid) {
@@ -1526,6 +1572,26 @@ cudaError_t ensure_tables() {
           else dp[at] = i == k ? (uint16_t)0xFFFF : (uint16_t)tpos[b][k][a][i];
         }
   err = cudaMemcpyToSymbol(c_dpos, dp, sizeof(dp));
+  if (err != cudaSuccess) return err;
+  // FP64 kernel: node 7's column (derived) and the other entries (owned)
+  uint16_t own[kKuuOwned], der[kKuuDerived * 8];
+  int no = 0, nd = 0;
+  for (int u = 0; u < kKuuPerElem; u++) {
+    const int a = h[u].x, i = h[u].y, b = h[u].z, k = h[u].w;
+    if (b == 7 && a < 7) {
+      uint16_t* row = der + 8 * nd++;
+      row[0] = (uint16_t)u;
+      for (int bb = 0; bb < 7; bb++)   // K(a,i; bb,k) by its assemble3 position
+        row[1 + bb] = (uint16_t)(a < bb ? tpos[a][i][bb][k]
+                                 : a > bb ? tpos[bb][k][a][i]
+                                 : (i <= k ? tpos[a][i][a][k] : tpos[a][k][a][i]));
+    } else {
+      own[no++] = (uint16_t)u;
+    }
+  }
+  if (no != kKuuOwned || nd != kKuuDerived) return cudaErrorInvalidValue;
+  err = cudaMemcpyToSymbol(c_kuu_owned, own, sizeof(own));
+  if (err == cudaSuccess) err = cudaMemcpyToSymbol(c_kuu_derived, der, sizeof(der));
   if (err == cudaSuccess) g_tables_ready[dev].store(true, std::memory_order_release);
   return err;
 }
@@ -1533,7 +1599,7 @@ cudaError_t ensure_tables() {
 }  // namespace
 
 size_t solid81_smem_bytes_wpb(bool mixed, int wpb) {
-  const size_t head = mixed ? kDposBytes : sizeof(uint32_t) * kOwned * 32;
+  const size_t head = mixed ? kDposBytes : kHead64Bytes;
   return head + wpb * (mixed ? sizeof(WarpSmem<float>) : sizeof(WarpSmem<double>));
 }
 
