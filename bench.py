@@ -34,19 +34,19 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 # FP64 flop per SOLID81 element of the algorithm the kernel runs (8 Gauss
-# points x 3664: kinematics 189, material + S + wDd 436, -wFS / w cof F 96,
+# points x 3628: kinematics 189, material + S + wDd 436, -wFS / w cof F 96,
 # tangent tensor A 513, h_a = A^T G_a for the 6 blocks i <= k 720, F_u + K_up
-# 288, the 237 accumulated K_uu entries 1422; plus 96, and 441 for the 63
-# entries of node 7's column derived from sum_b G_b = 0).  The executed FP64
-# instruction counters of one ncu capture give 29,793 per element (2 DFMA +
-# DMUL + DADD); that figure is used.  The Bh^T D Bh formulation costs 69,072
+# 288, the 231 accumulated K_uu entries 1386; plus 96, and 483 for the 69
+# entries of node 7's column and block derived from sum_b G_b = 0).  The
+# executed FP64 instruction counters of one ncu capture give 29,467 per
+# element (2 DFMA + DMUL + DADD); that figure is used.  The Bh^T D Bh formulation costs 69,072
 # (8 x 8634) for the same element.
-FLOP_PER_ELEM = 29793
+FLOP_PER_ELEM = 29467
 FLOP_PER_ELEM_BTDB = 69072
-# FP64 instructions per element in the same capture (12,536 DFMA + 3,480
-# DMUL + 1,241 DADD): a DMUL or DADD takes the pipe as long as a DFMA for half
+# FP64 instructions per element in the same capture (12,360 DFMA + 3,480
+# DMUL + 1,267 DADD): a DMUL or DADD takes the pipe as long as a DFMA for half
 # the flops, so the pipe's instruction rate is the tighter ceiling.
-FP64_INSTR_PER_ELEM = 17257
+FP64_INSTR_PER_ELEM = 17107
 # DRAM bytes per element of solid81_kernel<double> and of the K gather in one
 # ncu capture of a 40^3 block (64,000 elements, 9,675,406 K slots), used to
 # scale the traffic to the measured launch; the element kernel's writes are a

@@ -48,13 +48,19 @@ __constant__ uchar4 c_kuu_entry[kKuuPerElem];
 
 // FP64 kernel: the shape gradients of an element sum to zero at every Gauss
 // point (sum_b G_b = J^-1 sum_b dN_b/dxi = 0), so K(a,i; 7,k) = sum_g h_a . G_7
-// = -sum_{b<7} K(a,i; b,k).  The 63 entries of node 7's column (a < 7, all
-// nine (i,k)) are formed from the other 237 after the Gauss-point loop (7
-// adds each, in a fixed order) instead of 24 FMAs each inside it; they differ
-// from the direct sums by rounding only (|sum_b G_b| ~ eps |G|).
-constexpr int kKuuDerived = 63;
-constexpr int kKuuOwned = kKuuPerElem - kKuuDerived;                 // 237
-constexpr int kOwned64 = (kEPW * kKuuOwned + 31) / 32;               // per lane (30)
+// = -sum_{b<7} K(a,i; b,k), and likewise h_7 = -sum_{a<7} h_a.  The 63
+// entries of node 7's column (a < 7, all nine (i,k)) are formed from the
+// accumulated ones after the Gauss-point loop (7 adds each, in a fixed
+// order), and then the 6 of node 7's own block, K(7,i; 7,k) = -sum_{a<7}
+// K(a,i; 7,k), from those: 231 of the 300 entries take 24 FMAs each inside
+// the loop, the minimum for blocks whose rows and columns sum to zero.  The
+// formed entries differ from the direct sums by rounding only
+// (|sum_b G_b| ~ eps |G|).
+constexpr int kKuuColumn = 63;                                       // first pass
+constexpr int kKuuCorner = 6;                                        // second pass
+constexpr int kKuuDerived = kKuuColumn + kKuuCorner;                 // 69
+constexpr int kKuuOwned = kKuuPerElem - kKuuDerived;                 // 231
+constexpr int kOwned64 = (kEPW * kKuuOwned + 31) / 32;               // per lane (29)
 // FP64 kernel block header: ownership words, stage positions, derived table
 constexpr size_t kHead64Bytes =
     (sizeof(uint32_t) * kOwned64 * 32 + sizeof(uint16_t) * kOwned64 * 32 +
@@ -547,13 +553,13 @@ __global__ void __launch_bounds__(WPB * 32)
   if constexpr (kMixed) {
     for (int v = threadIdx.x; v < kDpos; v += blockDim.x) dpos[v] = c_dpos[v];
   } else
-  // Ownership of Kuu entries: lane owns x = lane + 32 m of the 4*237 owned
+  // Ownership of Kuu entries: lane owns x = lane + 32 m of the 4*231 owned
   // entries of its warp's element quad.  Decode once: smem offsets of
   // H[ik][.][slot a] and G[.][slot b].
   for (int v = threadIdx.x; v < kOwned64 * 32; v += blockDim.x) {
     const int m = v / 32, l = v % 32;
     const int x = l + 32 * m;
-    // entries past the quad's 948 read slot 0 (in bounds) and are never written
+    // entries past the quad's 924 read slot 0 (in bounds) and are never written
     uint32_t word = 0u;
     uint16_t where = 0xFFFFu;
     if (x < kEPW * kKuuOwned) {
@@ -1037,8 +1043,8 @@ __global__ void __launch_bounds__(WPB * 32)
 
     // ---------------- write the element contributions ----------------
     // the owned entries into the quad's stage (assemble3 order; A's scratch,
-    // dead after the Gauss-point loop), node 7's column from them, then all
-    // 4 x 300 written coalesced
+    // dead after the Gauss-point loop), node 7's column from them, node 7's
+    // block from that column, then all 4 x 300 written coalesced
     TT* stage = &sm->A[0][0];
 #pragma unroll
     for (int m = 0; m < kOwned64; m++) {
@@ -1046,8 +1052,18 @@ __global__ void __launch_bounds__(WPB * 32)
       if (where != 0xFFFFu) stage[where] = acc[m];
     }
     __syncwarp();
-    for (int dx = lane; dx < kEPW * kKuuDerived; dx += 32) {
-      const int qq = dx / kKuuDerived, j = dx - qq * kKuuDerived;
+    for (int dx = lane; dx < kEPW * kKuuColumn; dx += 32) {
+      const int qq = dx / kKuuColumn, j = dx - qq * kKuuColumn;
+      const TT* st = stage + qq * kKuuPerElem;
+      const uint16_t* dj = dtab + j * 8;
+      TT v = st[dj[1]];
+#pragma unroll
+      for (int c = 2; c < 8; c++) v += st[dj[c]];
+      stage[qq * kKuuPerElem + dj[0]] = -v;
+    }
+    __syncwarp();
+    if (lane < kEPW * kKuuCorner) {
+      const int qq = lane / kKuuCorner, j = kKuuColumn + lane - qq * kKuuCorner;
       const TT* st = stage + qq * kKuuPerElem;
       const uint16_t* dj = dtab + j * 8;
       TT v = st[dj[1]];
@@ -1573,9 +1589,10 @@ cudaError_t ensure_tables() {
         }
   err = cudaMemcpyToSymbol(c_dpos, dp, sizeof(dp));
   if (err != cudaSuccess) return err;
-  // FP64 kernel: node 7's column (derived) and the other entries (owned)
+  // FP64 kernel: node 7's column and block (derived) and the other entries
+  // (owned); the column's 63 rows come first, the block's 6 after them
   uint16_t own[kKuuOwned], der[kKuuDerived * 8];
-  int no = 0, nd = 0;
+  int no = 0, nd = 0, nc = kKuuColumn;
   for (int u = 0; u < kKuuPerElem; u++) {
     const int a = h[u].x, i = h[u].y, b = h[u].z, k = h[u].w;
     if (b == 7 && a < 7) {
@@ -1585,11 +1602,17 @@ cudaError_t ensure_tables() {
         row[1 + bb] = (uint16_t)(a < bb ? tpos[a][i][bb][k]
                                  : a > bb ? tpos[bb][k][a][i]
                                  : (i <= k ? tpos[a][i][a][k] : tpos[a][k][a][i]));
+    } else if (b == 7 && a == 7) {
+      if (nc >= kKuuDerived) return cudaErrorInvalidValue;
+      uint16_t* row = der + 8 * nc++;
+      row[0] = (uint16_t)u;
+      for (int aa = 0; aa < 7; aa++)   // K(aa,i; 7,k): node 7's column, formed first
+        row[1 + aa] = (uint16_t)tpos[aa][i][7][k];
     } else {
       own[no++] = (uint16_t)u;
     }
   }
-  if (no != kKuuOwned || nd != kKuuDerived) return cudaErrorInvalidValue;
+  if (no != kKuuOwned || nd != kKuuColumn || nc != kKuuDerived) return cudaErrorInvalidValue;
   err = cudaMemcpyToSymbol(c_kuu_owned, own, sizeof(own));
   if (err == cudaSuccess) err = cudaMemcpyToSymbol(c_kuu_derived, der, sizeof(der));
   if (err == cudaSuccess) g_tables_ready[dev].store(true, std::memory_order_release);
