@@ -956,33 +956,120 @@ __global__ void scale_pivots_kernel(BigBatch b, LdltDev d, const T* __restrict__
   vec[d.vec_off[s] + c] /= (double)F[c + c * m];
 }
 
-// backward: t_c = v_c - sum_{i >= k} L[i][c] x[rows[i]], 32 columns per block
-// (a warp per column)
+// Products of the large supernodes' solves.  With FP64 fronts they are FP64
+// FMAs.  With FP32 fronts the FP64 pipe (1/64 of the FP32 rate on this part,
+// and the float -> double conversion runs on it too) would bound every pass,
+// so a product f x of a front entry f and a vector entry x = xh + xl (two
+// floats, |xl| <= ulp(xh)/2) is formed exactly in FP32 (p = f xh, e = fma(f,
+// xh, -p)) and summed into a double-word accumulator (h, l) by TwoSum, l
+// collecting the rounding errors and f xl: the compensated dot product Dot2
+// of Ogita, Rump and Oishi (2005), error <= u |sum| + gamma_n^2 sum |f x|
+// with u = 2^-24, far below the FP32 factor's own error.  Each accumulator
+// adds in a fixed order, so a pass is run-to-run identical.
 template <typename T>
-__global__ void bwd_rest_kernel(BigBatch b, LdltDev d, const T* __restrict__ front,
-                                double* __restrict__ vec, const double* __restrict__ xf) {
+struct Dot;
+
+template <>
+struct Dot<double> {
+  using X = double;
+  double s = 0.0;
+  __device__ static X split(double x) { return x; }
+  __device__ void add(double f, X x) { s = fma(f, x, s); }
+  __device__ void merge(const Dot& o) { s += o.s; }
+  __device__ void shfl_xor(int lanemask) { s += __shfl_xor_sync(0xffffffffu, s, lanemask); }
+  __device__ void shfl_down(int delta) { s += __shfl_down_sync(0xffffffffu, s, delta); }
+  __device__ double value() const { return s; }
+};
+
+template <>
+struct Dot<float> {
+  using X = float2;
+  float h = 0.0f, l = 0.0f;
+  __device__ static X split(double x) {
+    const float xh = __double2float_rn(x);
+    return make_float2(xh, __double2float_rn(x - (double)xh));
+  }
+  // h + l += b (TwoSum of h and b; the error joins l)
+  __device__ void two_sum(float b, float bl) {
+    const float sum = __fadd_rn(h, b);
+    const float bv = __fsub_rn(sum, h);
+    const float err = __fadd_rn(__fsub_rn(h, __fsub_rn(sum, bv)), __fsub_rn(b, bv));
+    h = sum;
+    l = __fadd_rn(l, __fadd_rn(err, bl));
+  }
+  __device__ void add(float f, X x) {
+    const float p = __fmul_rn(f, x.x);
+    two_sum(p, __fmaf_rn(f, x.y, __fmaf_rn(f, x.x, -p)));
+  }
+  __device__ void merge(const Dot& o) { two_sum(o.h, o.l); }
+  __device__ void shfl_xor(int lanemask) {
+    Dot o;
+    o.h = __shfl_xor_sync(0xffffffffu, h, lanemask);
+    o.l = __shfl_xor_sync(0xffffffffu, l, lanemask);
+    merge(o);
+  }
+  __device__ void shfl_down(int delta) {
+    Dot o;
+    o.h = __shfl_down_sync(0xffffffffu, h, delta);
+    o.l = __shfl_down_sync(0xffffffffu, l, delta);
+    merge(o);
+  }
+  __device__ double value() const { return (double)h + (double)l; }
+};
+
+// backward, before the large supernodes' triangles: the solved ancestor
+// entries x[rows[i]], i >= k, gathered into v[k:m] (the update rows' slots,
+// free once the forward pass has added them into the parent), in the
+// products' operand form (a double, or its two-float split in its 8 bytes)
+template <typename T>
+__global__ void gather_rest_kernel(BigBatch b, LdltDev d, double* __restrict__ vec,
+                                   const double* __restrict__ xf) {
+  using X = typename Dot<T>::X;
+  static_assert(sizeof(X) == sizeof(double), "operand form fills a vector slot");
   const int s = b.list[blockIdx.y];
   const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
   const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
-  const int64_t cbeg = (int64_t)blockIdx.x * 32;
-  if (cbeg >= k) return;
-  const int32_t* rows = d.rows + d.row_ptr[s];
-  const T* F = front + d.front_off[s];
-  double* v = vec + d.vec_off[s];
+  const int64_t i = k + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  reinterpret_cast<X*>(vec + d.vec_off[s])[i] = Dot<T>::split(xf[d.rows[d.row_ptr[s] + i]]);
+}
+
+// backward: t_c = v_c - sum_{i >= k} L[i][c] xr_i (xr gathered into v[k:m]),
+// a warp per column: the column's contiguous segment and xr read by the
+// lanes, eight loads of each in flight, eight partial sums merged in a fixed
+// order
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    bwd_rest_kernel(BigBatch b, LdltDev d, const T* __restrict__ front,
+                    double* __restrict__ vec) {
+  using X = typename Dot<T>::X;
+  const int s = b.list[blockIdx.y];
+  const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
+  const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t cend = cbeg + 32 < k ? cbeg + 32 : k;
-  for (int64_t c = cbeg + warp; c < cend; c += blockDim.x / 32) {
-    double acc = 0.0, acc2 = 0.0;
-    int64_t i = k + lane;
-    for (; i + 32 < m; i += 64) {
-      acc += (double)F[i + c * m] * xf[rows[i]];
-      acc2 += (double)F[i + 32 + c * m] * xf[rows[i + 32]];
+  const int64_t c = (int64_t)blockIdx.x * (kThreads / 32) + warp;
+  if (c >= k) return;   // warp-uniform; no block barrier follows
+  const T* Fc = front + d.front_off[s] + c * m;
+  double* v = vec + d.vec_off[s];
+  const X* xr = reinterpret_cast<const X*>(v);
+  Dot<T> acc[8];
+  int64_t i = k + lane;
+  for (; i + 7 * 32 < m; i += 8 * 32) {
+    T f[8];
+    X x[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+      f[u] = Fc[i + 32 * u];
+      x[u] = xr[i + 32 * u];
     }
-    if (i < m) acc += (double)F[i + c * m] * xf[rows[i]];
-    acc += acc2;
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-    if (lane == 0) v[c] -= acc;
+#pragma unroll
+    for (int u = 0; u < 8; u++) acc[u].add(f[u], x[u]);
   }
+  for (; i < m; i += 32) acc[0].add(Fc[i], xr[i]);
+#pragma unroll
+  for (int u = 1; u < 8; u++) acc[0].merge(acc[u]);
+  for (int o = 16; o > 0; o >>= 1) acc[0].shfl_down(o);
+  if (lane == 0) v[c] -= acc[0].value();
 }
 
 // The forward and backward passes go by outer blocks of kOuter pivots (four
@@ -990,14 +1077,20 @@ __global__ void bwd_rest_kernel(BigBatch b, LdltDev d, const T* __restrict__ fro
 // by one CTA per supernode (panel by panel through the stored inverses, the
 // rows / columns inside the block updated in shared memory), then the rows
 // below it (forward) or the pivots before it (backward) with up to kOuter
-// products per entry.
+// products per entry.  Every product chain is split so that its loads are
+// issued together (the passes are bound by load latency, not bandwidth), and
+// the partial sums are merged in a fixed order (run-to-run identical).
 
-// forward, outer block o0: v_B <- L_BB^-1 v_B for the block's ob pivots
+// forward, outer block o0: v_B <- L_BB^-1 v_B for the block's ob pivots.
+// Per panel: y = Linv v_p, then the rows below the panel inside the block,
+// both by four threads per row (16 products each, merged by shuffles).
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
     fwd_block_kernel(BigBatch b, LdltDev d, const T* __restrict__ front,
                      const T* __restrict__ Linv, int64_t o0, double* __restrict__ vec) {
+  using X = typename Dot<T>::X;
   __shared__ double vb[kOuter];
+  __shared__ X xs[kPanel];
   const int s = b.list[blockIdx.x];
   const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
   const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
@@ -1008,86 +1101,134 @@ __global__ void __launch_bounds__(kThreads)
   const int t = threadIdx.x;
   if (t < ob) vb[t] = v[o0 + t];
   __syncthreads();
+  const int r = t >> 2, q = t & 3;   // kThreads = 4 x kPanel
   for (int p = 0; p < ob; p += kPanel) {
     const int cb = ob - p < kPanel ? ob - p : kPanel;
     const T* Li = Linv + b.li_off[blockIdx.x] + (uint64_t)((o0 + p) / kPanel) * kPanel * kPanel;
-    // the dot products in four independent partial sums (latency, not rate,
-    // bounds one chain)
-    double y = 0.0;
-    if (t < cb) {
-      double y1 = 0.0, y2 = 0.0, y3 = 0.0;
-      int c = 0;
-      for (; c + 3 <= t; c += 4) {
-        y += (double)Li[t + c * kPanel] * vb[p + c];
-        y1 += (double)Li[t + (c + 1) * kPanel] * vb[p + c + 1];
-        y2 += (double)Li[t + (c + 2) * kPanel] * vb[p + c + 2];
-        y3 += (double)Li[t + (c + 3) * kPanel] * vb[p + c + 3];
+    // (entries past cb are zero: the row products below read all kPanel)
+    if (t < kPanel) xs[t] = Dot<T>::split(t < cb ? vb[p + t] : 0.0);
+    __syncthreads();
+    // y_r = sum_c Linv[r][c] v_c (Linv's strict upper triangle holds zeros)
+    Dot<T> y;
+    if (r < cb) {
+      Dot<T> y1;
+#pragma unroll
+      for (int j = 0; j < kPanel / 4; j += 2) {
+        const int c0 = q + 4 * j, c1 = c0 + 4;
+        if (c0 < cb) y.add(Li[r + c0 * kPanel], xs[c0]);
+        if (c1 < cb) y1.add(Li[r + c1 * kPanel], xs[c1]);
       }
-      for (; c <= t; c++) y += (double)Li[t + c * kPanel] * vb[p + c];
-      y = (y + y1) + (y2 + y3);
+      y.merge(y1);
+    }
+    y.shfl_xor(1);
+    y.shfl_xor(2);
+    __syncthreads();
+    if (r < cb && q == 0) {
+      const double yv = y.value();
+      vb[p + r] = yv;
+      xs[r] = Dot<T>::split(yv);
     }
     __syncthreads();
-    if (t < cb) vb[p + t] = y;
-    __syncthreads();
-    for (int i = p + cb + t; i < ob; i += blockDim.x) {
-      const T* Fi = F + (o0 + i) + (o0 + p) * m;
-      double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
-      int c = 0;
-      for (; c + 3 < cb; c += 4) {
-        a0 += (double)Fi[(int64_t)c * m] * vb[p + c];
-        a1 += (double)Fi[(int64_t)(c + 1) * m] * vb[p + c + 1];
-        a2 += (double)Fi[(int64_t)(c + 2) * m] * vb[p + c + 2];
-        a3 += (double)Fi[(int64_t)(c + 3) * m] * vb[p + c + 3];
+    // the rows below the panel inside the block: four threads per row, 16
+    // columns each
+    for (int i0 = p + cb; i0 < ob; i0 += kThreads / 4) {
+      const int i = i0 + r;
+      Dot<T> a;
+      if (i < ob) {
+        const T* Fi = F + (o0 + i) + (o0 + p) * m;
+        const int c0 = q * (kPanel / 4);
+        T f[kPanel / 4];
+#pragma unroll
+        for (int u = 0; u < kPanel / 4; u++)
+          f[u] = c0 + u < cb ? Fi[(int64_t)(c0 + u) * m] : T(0);
+        Dot<T> a1;
+#pragma unroll
+        for (int u = 0; u < kPanel / 4; u += 2) {
+          a.add(f[u], xs[c0 + u]);
+          a1.add(f[u + 1], xs[c0 + u + 1]);
+        }
+        a.merge(a1);
       }
-      for (; c < cb; c++) a0 += (double)Fi[(int64_t)c * m] * vb[p + c];
-      vb[i] -= (a0 + a1) + (a2 + a3);
+      a.shfl_xor(1);
+      a.shfl_xor(2);
+      if (i < ob && q == 0) vb[i] -= a.value();
     }
     __syncthreads();
   }
   if (t < ob) v[o0 + t] = vb[t];
 }
 
-// forward, outer block o0: v[i] -= sum_c L[i][o0+c] y_c for the rows below the block
+// forward, outer block o0: v[i] -= sum_c L[i][o0+c] y_c for the rows below the
+// block, 32 rows per CTA: warp w takes the columns [32 w, 32 w + 32), lane =
+// row (each load one coalesced 32-row segment of a column, 32 in flight),
+// and the eight warps' partial sums are merged in a fixed order
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
     fwd_rows_block_kernel(BigBatch b, LdltDev d, const T* __restrict__ front, int64_t o0,
                           double* __restrict__ vec) {
-  __shared__ double yb[kOuter];
+  using X = typename Dot<T>::X;
+  constexpr int kWarps = kThreads / 32;
+  static_assert(kWarps * 32 == kOuter, "one warp per 32 columns of the outer block");
+  __shared__ X yb[kOuter];
+  __shared__ Dot<T> part[kWarps][32];
   const int s = b.list[blockIdx.y];
   const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
   const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
   if (o0 >= k) return;
   const int ob = (int)(k - o0 < kOuter ? k - o0 : kOuter);
-  const int64_t r0 = o0 + ob + (int64_t)blockIdx.x * blockDim.x;
+  const int64_t r0 = o0 + ob + (int64_t)blockIdx.x * 32;
   if (r0 >= m) return;
   const T* F = front + d.front_off[s];
   double* v = vec + d.vec_off[s];
-  if (threadIdx.x < ob) yb[threadIdx.x] = v[o0 + threadIdx.x];
+  if (threadIdx.x < ob) yb[threadIdx.x] = Dot<T>::split(v[o0 + threadIdx.x]);
   __syncthreads();
-  const int64_t i = r0 + threadIdx.x;
-  if (i < m) {
-    const T* Fi = F + i + o0 * m;
-    // four independent partial sums (the FP64 FMA latency, not its rate,
-    // bounds one long chain)
-    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
-    int c = 0;
-    for (; c + 3 < ob; c += 4) {
-      a0 += (double)Fi[(int64_t)c * m] * yb[c];
-      a1 += (double)Fi[(int64_t)(c + 1) * m] * yb[c + 1];
-      a2 += (double)Fi[(int64_t)(c + 2) * m] * yb[c + 2];
-      a3 += (double)Fi[(int64_t)(c + 3) * m] * yb[c + 3];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t i = r0 + lane;
+  const int cbeg = warp * 32;
+  Dot<T> a0, a1, a2, a3;
+  if (i < m && cbeg < ob) {
+    const T* Fi = F + i + (o0 + cbeg) * m;
+    if (ob - cbeg >= 32) {
+      T f[32];
+#pragma unroll
+      for (int u = 0; u < 32; u++) f[u] = Fi[(int64_t)u * m];
+#pragma unroll
+      for (int u = 0; u < 32; u += 4) {
+        a0.add(f[u], yb[cbeg + u]);
+        a1.add(f[u + 1], yb[cbeg + u + 1]);
+        a2.add(f[u + 2], yb[cbeg + u + 2]);
+        a3.add(f[u + 3], yb[cbeg + u + 3]);
+      }
+    } else {
+      for (int u = 0; u < ob - cbeg; u++) a0.add(Fi[(int64_t)u * m], yb[cbeg + u]);
     }
-    for (; c < ob; c++) a0 += (double)Fi[(int64_t)c * m] * yb[c];
-    v[i] -= (a0 + a1) + (a2 + a3);
+  }
+  a0.merge(a1);
+  a2.merge(a3);
+  a0.merge(a2);
+  part[warp][lane] = a0;
+  __syncthreads();
+  if (warp == 0 && i < m) {
+    Dot<T> sum = part[0][lane];
+#pragma unroll
+    for (int w = 1; w < kWarps; w++) sum.merge(part[w][lane]);
+    v[i] -= sum.value();
   }
 }
 
-// backward, outer block o0: x_B = L_BB^-T t_B for the block's pivots
+// backward, outer block o0: x_B = L_BB^-T t_B for the block's pivots.  Per
+// panel (last first): the panel's inverse staged in shared memory (coalesced),
+// x = Linv^T t_p by four threads per pivot, then t_j -= sum_c L[p+c][j] x_c
+// for the block's pivots j before the panel by four threads per j (16
+// contiguous products each), the partial sums merged by shuffles
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
     bwd_block_kernel(BigBatch b, LdltDev d, const T* __restrict__ front,
                      const T* __restrict__ Linv, int64_t o0, double* __restrict__ vec) {
+  using X = typename Dot<T>::X;
   __shared__ double tb[kOuter];
+  __shared__ X xs[kPanel];
+  __shared__ T Ls[kPanel][kPanel + 1];   // Ls[c][r] = Linv[r][c]
   const int s = b.list[blockIdx.x];
   const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
   const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
@@ -1097,39 +1238,61 @@ __global__ void __launch_bounds__(kThreads)
   double* v = vec + d.vec_off[s];
   const int t = threadIdx.x;
   if (t < ob) tb[t] = v[o0 + t];
-  __syncthreads();
+  const int r = t >> 2, q = t & 3;   // kThreads = 4 x kPanel
   for (int p = ((ob - 1) / kPanel) * kPanel; p >= 0; p -= kPanel) {
     const int cb = ob - p < kPanel ? ob - p : kPanel;
     const T* Li = Linv + b.li_off[blockIdx.x] + (uint64_t)((o0 + p) / kPanel) * kPanel * kPanel;
-    double x = 0.0;
-    if (t < cb) {
-      const T* Lt = Li + (int64_t)t * kPanel;
-      double x1 = 0.0, x2 = 0.0, x3 = 0.0;
-      int c = t;
-      for (; c + 3 < cb; c += 4) {
-        x += (double)Lt[c] * tb[p + c];
-        x1 += (double)Lt[c + 1] * tb[p + c + 1];
-        x2 += (double)Lt[c + 2] * tb[p + c + 2];
-        x3 += (double)Lt[c + 3] * tb[p + c + 3];
-      }
-      for (; c < cb; c++) x += (double)Lt[c] * tb[p + c];
-      x = (x + x1) + (x2 + x3);
+#pragma unroll 4
+    for (int e = t; e < kPanel * kPanel; e += kThreads) {
+      const int er = e % kPanel, ec = e / kPanel;
+      Ls[ec][er] = er < cb && ec < cb ? Li[er + ec * kPanel] : T(0);
     }
     __syncthreads();
-    if (t < cb) tb[p + t] = x;
+    // (entries past cb are zero: the products below read all kPanel)
+    if (t < kPanel) xs[t] = Dot<T>::split(t < cb ? tb[p + t] : 0.0);
     __syncthreads();
-    for (int j = t; j < p; j += blockDim.x) {
-      const T* Fj = F + (o0 + p) + (o0 + j) * m;
-      double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
-      int c = 0;
-      for (; c + 3 < cb; c += 4) {
-        a0 += (double)Fj[c] * tb[p + c];
-        a1 += (double)Fj[c + 1] * tb[p + c + 1];
-        a2 += (double)Fj[c + 2] * tb[p + c + 2];
-        a3 += (double)Fj[c + 3] * tb[p + c + 3];
+    // x_r = sum_{c >= r} Linv[c][r] t_c
+    Dot<T> x;
+    if (r < cb) {
+      Dot<T> x1;
+#pragma unroll
+      for (int j = 0; j < kPanel / 4; j += 2) {
+        const int c0 = q + 4 * j, c1 = c0 + 4;
+        if (c0 < cb) x.add(Ls[r][c0], xs[c0]);
+        if (c1 < cb) x1.add(Ls[r][c1], xs[c1]);
       }
-      for (; c < cb; c++) a0 += (double)Fj[c] * tb[p + c];
-      tb[j] -= (a0 + a1) + (a2 + a3);
+      x.merge(x1);
+    }
+    x.shfl_xor(1);
+    x.shfl_xor(2);
+    __syncthreads();
+    if (r < cb && q == 0) {
+      const double xv = x.value();
+      tb[p + r] = xv;
+      xs[r] = Dot<T>::split(xv);
+    }
+    __syncthreads();
+    // the pivots before the panel: column j's rows p .. p+cb, contiguous
+    for (int j0 = 0; j0 < p; j0 += kThreads / 4) {
+      const int j = j0 + r;
+      Dot<T> a;
+      if (j < p) {
+        const T* Fj = F + (o0 + p) + (o0 + j) * m;
+        const int c0 = q * (kPanel / 4);
+        T f[kPanel / 4];
+#pragma unroll
+        for (int u = 0; u < kPanel / 4; u++) f[u] = c0 + u < cb ? Fj[c0 + u] : T(0);
+        Dot<T> a1;
+#pragma unroll
+        for (int u = 0; u < kPanel / 4; u += 2) {
+          a.add(f[u], xs[c0 + u]);
+          a1.add(f[u + 1], xs[c0 + u + 1]);
+        }
+        a.merge(a1);
+      }
+      a.shfl_xor(1);
+      a.shfl_xor(2);
+      if (j < p && q == 0) tb[j] -= a.value();
     }
     __syncthreads();
   }
@@ -1137,12 +1300,13 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // backward, outer block o0: t[j] -= sum_c L[o0+c][j] x_c for the pivots j < o0
-// (a warp per column j, lanes over the block's rows)
+// (a warp per column j, lanes over the block's rows, eight loads in flight)
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
     bwd_cols_block_kernel(BigBatch b, LdltDev d, const T* __restrict__ front, int64_t o0,
                           double* __restrict__ vec) {
-  __shared__ double xb[kOuter];
+  using X = typename Dot<T>::X;
+  __shared__ X xb[kOuter];
   const int s = b.list[blockIdx.y];
   const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
   const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
@@ -1152,16 +1316,25 @@ __global__ void __launch_bounds__(kThreads)
   const int ob = (int)(k - o0 < kOuter ? k - o0 : kOuter);
   const T* F = front + d.front_off[s];
   double* v = vec + d.vec_off[s];
-  if (threadIdx.x < ob) xb[threadIdx.x] = v[o0 + threadIdx.x];
+  if (threadIdx.x < ob) xb[threadIdx.x] = Dot<T>::split(v[o0 + threadIdx.x]);
+  else if (threadIdx.x < kOuter) xb[threadIdx.x] = Dot<T>::split(0.0);
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t jend = jbeg + 32 < o0 ? jbeg + 32 : o0;
   for (int64_t j = jbeg + warp; j < jend; j += blockDim.x / 32) {
     const T* Fj = F + o0 + j * m;
-    double acc = 0.0;
-    for (int c = lane; c < ob; c += 32) acc += (double)Fj[c] * xb[c];
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-    if (lane == 0) v[j] -= acc;
+    T f[kOuter / 32];
+#pragma unroll
+    for (int u = 0; u < kOuter / 32; u++) f[u] = lane + 32 * u < ob ? Fj[lane + 32 * u] : T(0);
+    Dot<T> a0, a1;
+#pragma unroll
+    for (int u = 0; u < kOuter / 32; u += 2) {
+      a0.add(f[u], xb[lane + 32 * u]);
+      a1.add(f[u + 1], xb[lane + 32 * (u + 1)]);
+    }
+    a0.merge(a1);
+    for (int o = 16; o > 0; o >>= 1) a0.shfl_down(o);
+    if (lane == 0) v[j] -= a0.value();
   }
 }
 
@@ -1489,7 +1662,7 @@ cudaError_t enqueue_solve_core(nla3d_ldlt* h, const double* b) {
         fwd_block_kernel<T><<<nf, kThreads, 0, st>>>(bb, h->dev, front, Li, o0, h->d_vec);
         const int64_t rest = L.large_max_m - o0 - 1;
         if (rest > 0)
-          fwd_rows_block_kernel<T><<<dim3((unsigned)((rest + kThreads - 1) / kThreads), nf),
+          fwd_rows_block_kernel<T><<<dim3((unsigned)((rest + 31) / 32), nf),
                                      kThreads, 0, st>>>(bb, h->dev, front, o0, h->d_vec);
       }
       scale_pivots_kernel<T><<<dim3((unsigned)((L.large_max_k + kThreads - 1) / kThreads), nf),
@@ -1505,8 +1678,12 @@ cudaError_t enqueue_solve_core(nla3d_ldlt* h, const double* b) {
     if (L.large_cnt) {
       const BigBatch bb{h->d_lists + L.large_off, h->d_wo + L.wo_off, h->d_lio + L.wo_off};
       const unsigned nf = (unsigned)L.large_cnt;
-      bwd_rest_kernel<T><<<dim3((unsigned)((L.large_max_k + 31) / 32), nf), kThreads, 0, st>>>(
-          bb, h->dev, front, h->d_vec, h->d_xf);
+      const int64_t rest = L.large_max_m - 1;
+      gather_rest_kernel<T><<<dim3((unsigned)((rest + kThreads - 1) / kThreads), nf), kThreads,
+                              0, st>>>(bb, h->dev, h->d_vec, h->d_xf);
+      bwd_rest_kernel<T><<<dim3((unsigned)((L.large_max_k + kThreads / 32 - 1) / (kThreads / 32)),
+                                nf),
+                           kThreads, 0, st>>>(bb, h->dev, front, h->d_vec);
       for (int64_t o0 = ((L.large_max_k - 1) / kOuter) * kOuter; o0 >= 0; o0 -= kOuter) {
         bwd_block_kernel<T><<<nf, kThreads, 0, st>>>(bb, h->dev, front, Li, o0, h->d_vec);
         if (o0 > 0)
