@@ -1017,32 +1017,58 @@ struct Dot<float> {
   __device__ double value() const { return (double)h + (double)l; }
 };
 
+// FP32 fronts, FP64 products (the accurate mode of the refinement): the
+// entry widened exactly by integer operations (re-biased exponent, shifted
+// mantissa; zero by a select, subnormals and non-finite values by the
+// conversion instruction), so that each product takes one FP64 FMA
+__device__ __forceinline__ double widen(float f) {
+  const uint32_t bits = __float_as_uint(f);
+  const uint32_t mag = bits & 0x7FFFFFFFu;
+  const uint32_t ex = bits & 0x7F800000u;
+  if (mag != 0u && (ex == 0u || ex == 0x7F800000u)) return (double)f;
+  const uint32_t sign = bits & 0x80000000u;
+  const uint32_t hi = mag ? (sign | ((mag >> 3) + (896u << 20))) : sign;
+  const uint32_t lo = mag ? (bits << 29) : 0u;
+  return __hiloint2double((int)hi, (int)lo);
+}
+
+struct DotWide {
+  using X = double;
+  double s = 0.0;
+  __device__ static X split(double x) { return x; }
+  __device__ void add(float f, X x) { s = fma(widen(f), x, s); }
+  __device__ void merge(const DotWide& o) { s += o.s; }
+  __device__ void shfl_xor(int lanemask) { s += __shfl_xor_sync(0xffffffffu, s, lanemask); }
+  __device__ void shfl_down(int delta) { s += __shfl_down_sync(0xffffffffu, s, delta); }
+  __device__ double value() const { return s; }
+};
+
 // backward, before the large supernodes' triangles: the solved ancestor
 // entries x[rows[i]], i >= k, gathered into v[k:m] (the update rows' slots,
 // free once the forward pass has added them into the parent), in the
 // products' operand form (a double, or its two-float split in its 8 bytes)
-template <typename T>
+template <typename T, typename D>
 __global__ void gather_rest_kernel(BigBatch b, LdltDev d, double* __restrict__ vec,
                                    const double* __restrict__ xf) {
-  using X = typename Dot<T>::X;
+  using X = typename D::X;
   static_assert(sizeof(X) == sizeof(double), "operand form fills a vector slot");
   const int s = b.list[blockIdx.y];
   const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
   const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
   const int64_t i = k + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m) return;
-  reinterpret_cast<X*>(vec + d.vec_off[s])[i] = Dot<T>::split(xf[d.rows[d.row_ptr[s] + i]]);
+  reinterpret_cast<X*>(vec + d.vec_off[s])[i] = D::split(xf[d.rows[d.row_ptr[s] + i]]);
 }
 
 // backward: t_c = v_c - sum_{i >= k} L[i][c] xr_i (xr gathered into v[k:m]),
 // a warp per column: the column's contiguous segment and xr read by the
 // lanes, eight loads of each in flight, eight partial sums merged in a fixed
 // order
-template <typename T>
+template <typename T, typename D>
 __global__ void __launch_bounds__(kThreads)
     bwd_rest_kernel(BigBatch b, LdltDev d, const T* __restrict__ front,
                     double* __restrict__ vec) {
-  using X = typename Dot<T>::X;
+  using X = typename D::X;
   const int s = b.list[blockIdx.y];
   const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
   const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
@@ -1052,7 +1078,7 @@ __global__ void __launch_bounds__(kThreads)
   const T* Fc = front + d.front_off[s] + c * m;
   double* v = vec + d.vec_off[s];
   const X* xr = reinterpret_cast<const X*>(v);
-  Dot<T> acc[8];
+  D acc[8];
   int64_t i = k + lane;
   for (; i + 7 * 32 < m; i += 8 * 32) {
     T f[8];
@@ -1084,11 +1110,11 @@ __global__ void __launch_bounds__(kThreads)
 // forward, outer block o0: v_B <- L_BB^-1 v_B for the block's ob pivots.
 // Per panel: y = Linv v_p, then the rows below the panel inside the block,
 // both by four threads per row (16 products each, merged by shuffles).
-template <typename T>
+template <typename T, typename D>
 __global__ void __launch_bounds__(kThreads)
     fwd_block_kernel(BigBatch b, LdltDev d, const T* __restrict__ front,
                      const T* __restrict__ Linv, int64_t o0, double* __restrict__ vec) {
-  using X = typename Dot<T>::X;
+  using X = typename D::X;
   __shared__ double vb[kOuter];
   __shared__ X xs[kPanel];
   const int s = b.list[blockIdx.x];
@@ -1106,12 +1132,12 @@ __global__ void __launch_bounds__(kThreads)
     const int cb = ob - p < kPanel ? ob - p : kPanel;
     const T* Li = Linv + b.li_off[blockIdx.x] + (uint64_t)((o0 + p) / kPanel) * kPanel * kPanel;
     // (entries past cb are zero: the row products below read all kPanel)
-    if (t < kPanel) xs[t] = Dot<T>::split(t < cb ? vb[p + t] : 0.0);
+    if (t < kPanel) xs[t] = D::split(t < cb ? vb[p + t] : 0.0);
     __syncthreads();
     // y_r = sum_c Linv[r][c] v_c (Linv's strict upper triangle holds zeros)
-    Dot<T> y;
+    D y;
     if (r < cb) {
-      Dot<T> y1;
+      D y1;
 #pragma unroll
       for (int j = 0; j < kPanel / 4; j += 2) {
         const int c0 = q + 4 * j, c1 = c0 + 4;
@@ -1126,14 +1152,14 @@ __global__ void __launch_bounds__(kThreads)
     if (r < cb && q == 0) {
       const double yv = y.value();
       vb[p + r] = yv;
-      xs[r] = Dot<T>::split(yv);
+      xs[r] = D::split(yv);
     }
     __syncthreads();
     // the rows below the panel inside the block: four threads per row, 16
     // columns each
     for (int i0 = p + cb; i0 < ob; i0 += kThreads / 4) {
       const int i = i0 + r;
-      Dot<T> a;
+      D a;
       if (i < ob) {
         const T* Fi = F + (o0 + i) + (o0 + p) * m;
         const int c0 = q * (kPanel / 4);
@@ -1141,7 +1167,7 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
         for (int u = 0; u < kPanel / 4; u++)
           f[u] = c0 + u < cb ? Fi[(int64_t)(c0 + u) * m] : T(0);
-        Dot<T> a1;
+        D a1;
 #pragma unroll
         for (int u = 0; u < kPanel / 4; u += 2) {
           a.add(f[u], xs[c0 + u]);
@@ -1162,15 +1188,15 @@ __global__ void __launch_bounds__(kThreads)
 // block, 32 rows per CTA: warp w takes the columns [32 w, 32 w + 32), lane =
 // row (each load one coalesced 32-row segment of a column, 32 in flight),
 // and the eight warps' partial sums are merged in a fixed order
-template <typename T>
+template <typename T, typename D>
 __global__ void __launch_bounds__(kThreads)
     fwd_rows_block_kernel(BigBatch b, LdltDev d, const T* __restrict__ front, int64_t o0,
                           double* __restrict__ vec) {
-  using X = typename Dot<T>::X;
+  using X = typename D::X;
   constexpr int kWarps = kThreads / 32;
   static_assert(kWarps * 32 == kOuter, "one warp per 32 columns of the outer block");
   __shared__ X yb[kOuter];
-  __shared__ Dot<T> part[kWarps][32];
+  __shared__ D part[kWarps][32];
   const int s = b.list[blockIdx.y];
   const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
   const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
@@ -1180,12 +1206,12 @@ __global__ void __launch_bounds__(kThreads)
   if (r0 >= m) return;
   const T* F = front + d.front_off[s];
   double* v = vec + d.vec_off[s];
-  if (threadIdx.x < ob) yb[threadIdx.x] = Dot<T>::split(v[o0 + threadIdx.x]);
+  if (threadIdx.x < ob) yb[threadIdx.x] = D::split(v[o0 + threadIdx.x]);
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t i = r0 + lane;
   const int cbeg = warp * 32;
-  Dot<T> a0, a1, a2, a3;
+  D a0, a1, a2, a3;
   if (i < m && cbeg < ob) {
     const T* Fi = F + i + (o0 + cbeg) * m;
     if (ob - cbeg >= 32) {
@@ -1209,7 +1235,7 @@ __global__ void __launch_bounds__(kThreads)
   part[warp][lane] = a0;
   __syncthreads();
   if (warp == 0 && i < m) {
-    Dot<T> sum = part[0][lane];
+    D sum = part[0][lane];
 #pragma unroll
     for (int w = 1; w < kWarps; w++) sum.merge(part[w][lane]);
     v[i] -= sum.value();
@@ -1221,11 +1247,11 @@ __global__ void __launch_bounds__(kThreads)
 // x = Linv^T t_p by four threads per pivot, then t_j -= sum_c L[p+c][j] x_c
 // for the block's pivots j before the panel by four threads per j (16
 // contiguous products each), the partial sums merged by shuffles
-template <typename T>
+template <typename T, typename D>
 __global__ void __launch_bounds__(kThreads)
     bwd_block_kernel(BigBatch b, LdltDev d, const T* __restrict__ front,
                      const T* __restrict__ Linv, int64_t o0, double* __restrict__ vec) {
-  using X = typename Dot<T>::X;
+  using X = typename D::X;
   __shared__ double tb[kOuter];
   __shared__ X xs[kPanel];
   __shared__ T Ls[kPanel][kPanel + 1];   // Ls[c][r] = Linv[r][c]
@@ -1249,12 +1275,12 @@ __global__ void __launch_bounds__(kThreads)
     }
     __syncthreads();
     // (entries past cb are zero: the products below read all kPanel)
-    if (t < kPanel) xs[t] = Dot<T>::split(t < cb ? tb[p + t] : 0.0);
+    if (t < kPanel) xs[t] = D::split(t < cb ? tb[p + t] : 0.0);
     __syncthreads();
     // x_r = sum_{c >= r} Linv[c][r] t_c
-    Dot<T> x;
+    D x;
     if (r < cb) {
-      Dot<T> x1;
+      D x1;
 #pragma unroll
       for (int j = 0; j < kPanel / 4; j += 2) {
         const int c0 = q + 4 * j, c1 = c0 + 4;
@@ -1269,20 +1295,20 @@ __global__ void __launch_bounds__(kThreads)
     if (r < cb && q == 0) {
       const double xv = x.value();
       tb[p + r] = xv;
-      xs[r] = Dot<T>::split(xv);
+      xs[r] = D::split(xv);
     }
     __syncthreads();
     // the pivots before the panel: column j's rows p .. p+cb, contiguous
     for (int j0 = 0; j0 < p; j0 += kThreads / 4) {
       const int j = j0 + r;
-      Dot<T> a;
+      D a;
       if (j < p) {
         const T* Fj = F + (o0 + p) + (o0 + j) * m;
         const int c0 = q * (kPanel / 4);
         T f[kPanel / 4];
 #pragma unroll
         for (int u = 0; u < kPanel / 4; u++) f[u] = c0 + u < cb ? Fj[c0 + u] : T(0);
-        Dot<T> a1;
+        D a1;
 #pragma unroll
         for (int u = 0; u < kPanel / 4; u += 2) {
           a.add(f[u], xs[c0 + u]);
@@ -1301,11 +1327,11 @@ __global__ void __launch_bounds__(kThreads)
 
 // backward, outer block o0: t[j] -= sum_c L[o0+c][j] x_c for the pivots j < o0
 // (a warp per column j, lanes over the block's rows, eight loads in flight)
-template <typename T>
+template <typename T, typename D>
 __global__ void __launch_bounds__(kThreads)
     bwd_cols_block_kernel(BigBatch b, LdltDev d, const T* __restrict__ front, int64_t o0,
                           double* __restrict__ vec) {
-  using X = typename Dot<T>::X;
+  using X = typename D::X;
   __shared__ X xb[kOuter];
   const int s = b.list[blockIdx.y];
   const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
@@ -1316,8 +1342,8 @@ __global__ void __launch_bounds__(kThreads)
   const int ob = (int)(k - o0 < kOuter ? k - o0 : kOuter);
   const T* F = front + d.front_off[s];
   double* v = vec + d.vec_off[s];
-  if (threadIdx.x < ob) xb[threadIdx.x] = Dot<T>::split(v[o0 + threadIdx.x]);
-  else if (threadIdx.x < kOuter) xb[threadIdx.x] = Dot<T>::split(0.0);
+  if (threadIdx.x < ob) xb[threadIdx.x] = D::split(v[o0 + threadIdx.x]);
+  else if (threadIdx.x < kOuter) xb[threadIdx.x] = D::split(0.0);
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t jend = jbeg + 32 < o0 ? jbeg + 32 : o0;
@@ -1326,7 +1352,7 @@ __global__ void __launch_bounds__(kThreads)
     T f[kOuter / 32];
 #pragma unroll
     for (int u = 0; u < kOuter / 32; u++) f[u] = lane + 32 * u < ob ? Fj[lane + 32 * u] : T(0);
-    Dot<T> a0, a1;
+    D a0, a1;
 #pragma unroll
     for (int u = 0; u < kOuter / 32; u += 2) {
       a0.add(f[u], xb[lane + 32 * u]);
@@ -1475,6 +1501,10 @@ struct nla3d_ldlt {
   double* d_hb = nullptr;       // nla3d_ldlt_solve_host: b and x on the device
   double* d_hx = nullptr;
   cudaGraphExec_t factor_exec = nullptr, solve_exec = nullptr;
+  // FP32 fronts: the solve with FP64 products (the refinement's accurate
+  // mode, after the compensated-FP32 one stalls), and the mode in use
+  cudaGraphExec_t solve_exec_acc = nullptr;
+  int solve_accurate = 0;
   const double* factor_graph_values = nullptr;
   uint64_t* d_wo = nullptr;
   uint64_t* d_lio = nullptr;
@@ -1637,7 +1667,7 @@ cudaError_t enqueue_factor(nla3d_ldlt* h, const double* values) {
   return cudaGetLastError();
 }
 
-template <typename T>
+template <typename T, typename D>
 cudaError_t enqueue_solve_core(nla3d_ldlt* h, const double* b) {
   const LdltSymbolic& S = h->S;
   const T* front = static_cast<const T*>(h->d_front);
@@ -1659,10 +1689,10 @@ cudaError_t enqueue_solve_core(nla3d_ldlt* h, const double* b) {
       const BigBatch bb{h->d_lists + L.large_off, h->d_wo + L.wo_off, h->d_lio + L.wo_off};
       const unsigned nf = (unsigned)L.large_cnt;
       for (int64_t o0 = 0; o0 < L.large_max_k; o0 += kOuter) {
-        fwd_block_kernel<T><<<nf, kThreads, 0, st>>>(bb, h->dev, front, Li, o0, h->d_vec);
+        fwd_block_kernel<T, D><<<nf, kThreads, 0, st>>>(bb, h->dev, front, Li, o0, h->d_vec);
         const int64_t rest = L.large_max_m - o0 - 1;
         if (rest > 0)
-          fwd_rows_block_kernel<T><<<dim3((unsigned)((rest + 31) / 32), nf),
+          fwd_rows_block_kernel<T, D><<<dim3((unsigned)((rest + 31) / 32), nf),
                                      kThreads, 0, st>>>(bb, h->dev, front, o0, h->d_vec);
       }
       scale_pivots_kernel<T><<<dim3((unsigned)((L.large_max_k + kThreads - 1) / kThreads), nf),
@@ -1679,15 +1709,15 @@ cudaError_t enqueue_solve_core(nla3d_ldlt* h, const double* b) {
       const BigBatch bb{h->d_lists + L.large_off, h->d_wo + L.wo_off, h->d_lio + L.wo_off};
       const unsigned nf = (unsigned)L.large_cnt;
       const int64_t rest = L.large_max_m - 1;
-      gather_rest_kernel<T><<<dim3((unsigned)((rest + kThreads - 1) / kThreads), nf), kThreads,
+      gather_rest_kernel<T, D><<<dim3((unsigned)((rest + kThreads - 1) / kThreads), nf), kThreads,
                               0, st>>>(bb, h->dev, h->d_vec, h->d_xf);
-      bwd_rest_kernel<T><<<dim3((unsigned)((L.large_max_k + kThreads / 32 - 1) / (kThreads / 32)),
+      bwd_rest_kernel<T, D><<<dim3((unsigned)((L.large_max_k + kThreads / 32 - 1) / (kThreads / 32)),
                                 nf),
                            kThreads, 0, st>>>(bb, h->dev, front, h->d_vec);
       for (int64_t o0 = ((L.large_max_k - 1) / kOuter) * kOuter; o0 >= 0; o0 -= kOuter) {
-        bwd_block_kernel<T><<<nf, kThreads, 0, st>>>(bb, h->dev, front, Li, o0, h->d_vec);
+        bwd_block_kernel<T, D><<<nf, kThreads, 0, st>>>(bb, h->dev, front, Li, o0, h->d_vec);
         if (o0 > 0)
-          bwd_cols_block_kernel<T><<<dim3((unsigned)((o0 + 31) / 32), nf), kThreads, 0, st>>>(
+          bwd_cols_block_kernel<T, D><<<dim3((unsigned)((o0 + 31) / 32), nf), kThreads, 0, st>>>(
               bb, h->dev, front, o0, h->d_vec);
       }
       store_pivots_kernel<<<dim3((unsigned)((L.large_max_k + kThreads - 1) / kThreads), nf),
@@ -2044,25 +2074,31 @@ unsigned vec_blocks(int64_t n) {
 // graph and scatters (or adds) the result into `out`
 cudaError_t enqueue_solve_any(nla3d_ldlt* h, const double* rhs, double* out, int acc) {
   cudaError_t e = cudaSuccess;
-  if (!h->solve_exec) {
+  // FP64 fronts have one mode; FP32 fronts: compensated FP32 products, or
+  // FP64 ones in the accurate mode
+  const bool accurate = h->prec && h->solve_accurate;
+  cudaGraphExec_t& exec = accurate ? h->solve_exec_acc : h->solve_exec;
+  if (!exec) {
     cudaGraph_t g = nullptr;
     e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return e;
     const cudaError_t ec =
-        h->prec ? enqueue_solve_core<float>(h, h->d_rhs) : enqueue_solve_core<double>(h, h->d_rhs);
+        !h->prec ? enqueue_solve_core<double, Dot<double>>(h, h->d_rhs)
+        : accurate ? enqueue_solve_core<float, DotWide>(h, h->d_rhs)
+                   : enqueue_solve_core<float, Dot<float>>(h, h->d_rhs);
     e = cudaStreamEndCapture(h->stream, &g);
     if (ec != cudaSuccess) e = ec;
-    if (e == cudaSuccess) e = cudaGraphInstantiate(&h->solve_exec, g, 0);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, g, 0);
     if (g) cudaGraphDestroy(g);
     if (e != cudaSuccess) {
-      h->solve_exec = nullptr;
+      exec = nullptr;
       return e;
     }
   }
   if (rhs != h->d_rhs)
     e = cudaMemcpyAsync(h->d_rhs, rhs, sizeof(double) * h->S.n, cudaMemcpyDeviceToDevice,
                         h->stream);
-  if (e == cudaSuccess) e = cudaGraphLaunch(h->solve_exec, h->stream);
+  if (e == cudaSuccess) e = cudaGraphLaunch(exec, h->stream);
   if (e != cudaSuccess) return e;
   const unsigned nb = (unsigned)((h->S.n + kThreads - 1) / kThreads);
   solve_finish_kernel<<<nb, kThreads, 0, h->stream>>>(h->S.n, h->d_perm, h->d_xf, out, acc);
@@ -2193,16 +2229,21 @@ int nla3d_ldlt_solve(nla3d_ldlt* h, const double* values, const double* b, doubl
   if (!h || !values || !b || !x || max_refine < 0)
     return fail(h, NLA3D_ERR_ARG, "ldlt_solve: bad argument");
   if (!h->factored) return fail(h, NLA3D_ERR_ARG, "ldlt_solve: factor first");
+  h->solve_accurate = 0;
   cudaError_t e = enqueue_solve_any(h, b, x, 0);
   double rel = 0.0, prev = 0.0, rnorm = 0.0, bnorm = 0.0;
   int it = 0;
-  // plain refinement while it converges fast; GMRES with the same factor after
+  // plain refinement while it converges fast; GMRES with the same factor
+  // after, its preconditioner applied with FP64 products (FP32 fronts: the
+  // compensated FP32 products carry 2^-48 per operation, which a hard
+  // system's Krylov iteration can feel)
   for (;;) {
     if (e == cudaSuccess) e = residual_norms(h, values, x, b, &rnorm, &bnorm);
     if (e != cudaSuccess) return cuda_fail(h, e, "ldlt_solve");
     rel = rnorm / (bnorm > 0.0 ? bnorm : 1.0);
     if (!(rel > tol) || it >= max_refine) break;
     if (it > 0 && !(rel < 0.1 * prev)) {
+      h->solve_accurate = 1;
       e = gmres_refine(h, values, b, x, tol, max_refine, &it, &rel);
       if (e != cudaSuccess) return cuda_fail(h, e, "ldlt_solve (GMRES)");
       break;
@@ -2349,6 +2390,7 @@ int nla3d_ldlt_destroy(nla3d_ldlt* h) {
   if (h->own_stream && h->stream) cudaStreamSynchronize(h->stream);
   if (h->factor_exec) cudaGraphExecDestroy(h->factor_exec);
   if (h->solve_exec) cudaGraphExecDestroy(h->solve_exec);
+  if (h->solve_exec_acc) cudaGraphExecDestroy(h->solve_exec_acc);
   for (void* p : h->allocs) cudaFree(p);
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
   delete h;

@@ -414,6 +414,7 @@ def evaluate(problems, mlp, precision="fp64", linear_solver="direct",
     out = {k: [] for k in starts}
     out["learned_used"] = []
     wall = {}
+    phases = {}
     for pb in problems:
         be = make_backend(pb, precision, backend_factory)
         basis = basis_for(pb, be)
@@ -428,6 +429,9 @@ def evaluate(problems, mlp, precision="fp64", linear_solver="direct",
             t0 = time.perf_counter()
             s, _ = solve(pb, be, factory, linear_solver=linear_solver)
             wall[start] = wall.get(start, 0.0) + time.perf_counter() - t0
+            ph = phases.setdefault(start, {})
+            for key, val in getattr(s, "timing", {}).items():
+                ph[key] = ph.get(key, 0.0) + val
             s.close()
             out[start] += [r.iterations for r in s.records]
             if start == "learned":
@@ -437,7 +441,7 @@ def evaluate(problems, mlp, precision="fp64", linear_solver="direct",
                     f"{wall[start]:.1f} s, {s.factorizations} factorisations, "
                     f"{s.inexact_solves} inexact solves, {s.fp64_refactorizations} FP64 refactors")
     res = {k: float(np.mean(v)) for k, v in out.items() if v}
-    return res | {"steps": len(out[starts[0]]), "wall_s": wall}
+    return res | {"steps": len(out[starts[0]]), "wall_s": wall, "phase_s": phases}
 
 
 def benchmark(n_block_train=100, n_block_eval=50, block_batch=50, n_bar_train=12, block_n=10,

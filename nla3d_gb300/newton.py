@@ -20,6 +20,7 @@ residual is not smaller.
 from __future__ import annotations
 
 import dataclasses
+import time
 
 import numpy as np
 import scipy.sparse as sp
@@ -184,6 +185,11 @@ class NewtonSolver:
         self.R = np.zeros(self.n)
         self.records: list[StepRecord] = []
         self.reactions: list[np.ndarray] = [np.zeros(self.nc)]
+        # host wall time per phase (s): assemble (set_U + assembly + F to the
+        # host), factor, solve (with refinement), update (updateResults),
+        # vectors (right-hand side, residual, reactions)
+        self.timing = {"assemble": 0.0, "factor": 0.0, "solve": 0.0, "update": 0.0,
+                       "vectors": 0.0}
 
     def close(self):
         """Release the device factorisation (its fronts can take most of HBM)."""
@@ -211,9 +217,13 @@ class NewtonSolver:
             self._perm = fill_reducing_order(io, co, self._row_points(), self.nu)
             self._ldlt = DeviceLDLT.for_storage(
                 self.b, self._perm, {"gpu": "fp64", "gpu-fp32": "fp32", "gpu-tc": "fp32-tc"}[self.solver])
+        t0 = time.perf_counter()
         self._ldlt.factor(self.b)
+        t1 = time.perf_counter()
+        self.timing["factor"] += t1 - t0
         self.factorizations += 1
         x = self._ldlt.solve_host(self.b, rhs, max_refine=100, tol=1e-10, strict=False)
+        self.timing["solve"] += time.perf_counter() - t1
         self.krylov_iterations += self._ldlt.last_steps
         rel = self._ldlt.last_residual
         if rel <= 1e-10:
@@ -304,9 +314,12 @@ class NewtonSolver:
         return Uc
 
     def _assemble(self, U):
+        t0 = time.perf_counter()
         self.b.set_U(U)
         self.b.assemble()
-        return self.b.F()
+        F = self.b.F()
+        self.timing["assemble"] += time.perf_counter() - t0
+        return F
 
     def residual(self, F, dUc):
         """Equilibrium residual of the unknown + MPC rows.  The reference solves
@@ -361,8 +374,10 @@ class NewtonSolver:
                 F = self._assemble(self.U)
                 Uc = self._apply_bc(t)
                 dUc = Uc - Ucprev
+                t0 = time.perf_counter()
                 rhs = self._rhs(F, dUc)
                 rnorm = float(np.linalg.norm(self.residual(F, dUc)))
+                self.timing["vectors"] += time.perf_counter() - t0
                 rec.residuals.append(rnorm)
                 if self.residual_tol is not None and tc.eq_step > 1 and rnorm < self.residual_tol \
                         and not np.any(dUc):
@@ -378,10 +393,14 @@ class NewtonSolver:
                 self.U[: self.nc] = Uc
                 self.U[self.nc: self.nc + self.nu] += dUsl[: self.nu]
                 self.U[self.nc + self.nu:] = dUsl[self.nu:]
+                t0 = time.perf_counter()
                 self.R[: self.nc] = self._reactions(F, dUc, dUsl)
+                t1 = time.perf_counter()
+                self.timing["vectors"] += t1 - t0
                 Ucprev = Uc.copy()
                 self.b.set_U(self.U)
                 self.b.update()
+                self.timing["update"] += time.perf_counter() - t1
                 crit = float(np.abs(dUsl[: self.nu]).sum() / max(self.nu, 1)) / self.kinematic_tol
                 rec.criteria.append(crit)
                 if not np.isfinite(crit) or crit > 1e6:
