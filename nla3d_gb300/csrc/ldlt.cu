@@ -1364,6 +1364,232 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// FP32 fronts: the block triangles with their operands staged in shared
+// memory by asynchronous copies issued when the CTA starts (the stored
+// inverses of the block's four panels and the block's strictly lower part,
+// 166 KB), in the order the panels use them, so that the pass waits for one
+// copy latency per block instead of a chain of them; everything after
+// reads shared memory.  Columns are padded to 65 floats (two-way bank
+// conflicts at most for the four-threads-per-row products).
+constexpr int kLd = kPanel + 1;
+constexpr int kStageLi = 4 * kPanel * kLd;    // the four inverses
+constexpr int kStageTri = 6 * kPanel * kLd;   // panel pi >= 1: its rows x the 64 pi columns before it
+constexpr size_t kStagedSmem = sizeof(float) * (kStageLi + kStageTri) + sizeof(double) * kOuter +
+                               sizeof(double) * kPanel;
+static_assert(kOuter == 4 * kPanel, "four panels per outer block");
+
+__device__ __forceinline__ int tri_off(int pi) { return kPanel * kLd * (pi * (pi - 1) / 2); }
+
+__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
+  const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+// this thread's copies of all but the `pending` most recent groups have landed
+__device__ __forceinline__ void cp_async_wait(int pending) {
+  switch (pending) {
+    case 0: asm volatile("cp.async.wait_group 0;\n" ::: "memory"); break;
+    case 1: asm volatile("cp.async.wait_group 1;\n" ::: "memory"); break;
+    case 2: asm volatile("cp.async.wait_group 2;\n" ::: "memory"); break;
+    default: asm volatile("cp.async.wait_group 3;\n" ::: "memory"); break;
+  }
+}
+
+// forward, outer block o0, FP32 fronts (fwd_block_kernel's arithmetic): copy
+// group g holds panel g's inverse and the columns of panel g in the rows of
+// the later panels
+template <typename D>
+__global__ void __launch_bounds__(kThreads)
+    fwd_block_staged_kernel(BigBatch b, LdltDev d, const float* __restrict__ front,
+                            const float* __restrict__ Linv, int64_t o0,
+                            double* __restrict__ vec) {
+  using X = typename D::X;
+  static_assert(sizeof(X) == sizeof(double), "operand slots of 8 bytes");
+  extern __shared__ __align__(16) unsigned char staged_raw[];
+  float* Ls = reinterpret_cast<float*>(staged_raw);
+  float* Tb = Ls + kStageLi;
+  double* vb = reinterpret_cast<double*>(Tb + kStageTri);
+  X* xs = reinterpret_cast<X*>(vb + kOuter);
+  const int s = b.list[blockIdx.x];
+  const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
+  const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
+  if (o0 >= k) return;
+  const int ob = (int)(k - o0 < kOuter ? k - o0 : kOuter);
+  const int np = (ob + kPanel - 1) / kPanel;
+  const float* F = front + d.front_off[s];
+  const float* Li0 = Linv + b.li_off[blockIdx.x] + (uint64_t)(o0 / kPanel) * kPanel * kPanel;
+  double* v = vec + d.vec_off[s];
+  const int t = threadIdx.x;
+  for (int g = 0; g < np; g++) {
+    const int cbg = ob - g * kPanel < kPanel ? ob - g * kPanel : kPanel;
+    const float* Li = Li0 + (uint64_t)g * kPanel * kPanel;
+    for (int e = t; e < kPanel * kPanel; e += kThreads) {
+      const int er = e % kPanel, ec = e / kPanel;
+      if (er < cbg && ec < cbg) cp_async4(Ls + g * kPanel * kLd + ec * kLd + er, Li + e);
+    }
+    for (int pi = g + 1; pi < np; pi++) {
+      const int cbp = ob - pi * kPanel < kPanel ? ob - pi * kPanel : kPanel;
+      for (int e = t; e < kPanel * kPanel; e += kThreads) {
+        const int er = e % kPanel, ec = e / kPanel;
+        if (er < cbp)
+          cp_async4(Tb + tri_off(pi) + (g * kPanel + ec) * kLd + er,
+                    F + (o0 + pi * kPanel + er) + (o0 + g * kPanel + ec) * m);
+      }
+    }
+    cp_async_commit();
+  }
+  if (t < ob) vb[t] = v[o0 + t];
+  const int r = t >> 2, q = t & 3;   // kThreads = 4 x kPanel
+  for (int g = 0; g < np; g++) {
+    const int p = g * kPanel;
+    const int cb = ob - p < kPanel ? ob - p : kPanel;
+    cp_async_wait(np - 1 - g);
+    __syncthreads();
+    if (t < kPanel) xs[t] = D::split(t < cb ? vb[p + t] : 0.0);
+    __syncthreads();
+    // y_r = sum_c Linv[r][c] v_c
+    const float* L = Ls + g * kPanel * kLd;
+    D y;
+    if (r < cb) {
+      D y1;
+#pragma unroll
+      for (int j = 0; j < kPanel / 4; j += 2) {
+        const int c0 = q * (kPanel / 4) + j, c1 = c0 + 1;
+        if (c0 < cb) y.add(L[c0 * kLd + r], xs[c0]);
+        if (c1 < cb) y1.add(L[c1 * kLd + r], xs[c1]);
+      }
+      y.merge(y1);
+    }
+    y.shfl_xor(1);
+    y.shfl_xor(2);
+    __syncthreads();
+    if (r < cb && q == 0) {
+      const double yv = y.value();
+      vb[p + r] = yv;
+      xs[r] = D::split(yv);
+    }
+    __syncthreads();
+    // the rows of the later panels: four threads per row, 16 columns each
+    for (int i0 = p + cb; i0 < ob; i0 += kThreads / 4) {
+      const int i = i0 + r;
+      D a;
+      if (i < ob) {
+        const int pi = i / kPanel, rr = i - pi * kPanel;
+        const float* Tr = Tb + tri_off(pi) + p * kLd + rr;
+        D a1;
+#pragma unroll
+        for (int u = 0; u < kPanel / 4; u += 2) {
+          const int c0 = q * (kPanel / 4) + u, c1 = c0 + 1;
+          if (c0 < cb) a.add(Tr[c0 * kLd], xs[c0]);
+          if (c1 < cb) a1.add(Tr[c1 * kLd], xs[c1]);
+        }
+        a.merge(a1);
+      }
+      a.shfl_xor(1);
+      a.shfl_xor(2);
+      if (i < ob && q == 0) vb[i] -= a.value();
+    }
+    __syncthreads();
+  }
+  if (t < ob) v[o0 + t] = vb[t];
+}
+
+// backward, outer block o0, FP32 fronts (bwd_block_kernel's arithmetic):
+// copy groups in the backward order, group n = panel np-1-n's inverse and its
+// rows in the columns before it
+template <typename D>
+__global__ void __launch_bounds__(kThreads)
+    bwd_block_staged_kernel(BigBatch b, LdltDev d, const float* __restrict__ front,
+                            const float* __restrict__ Linv, int64_t o0,
+                            double* __restrict__ vec) {
+  using X = typename D::X;
+  static_assert(sizeof(X) == sizeof(double), "operand slots of 8 bytes");
+  extern __shared__ __align__(16) unsigned char staged_raw[];
+  float* Ls = reinterpret_cast<float*>(staged_raw);
+  float* Tb = Ls + kStageLi;
+  double* tb = reinterpret_cast<double*>(Tb + kStageTri);
+  X* xs = reinterpret_cast<X*>(tb + kOuter);
+  const int s = b.list[blockIdx.x];
+  const int64_t m = d.row_ptr[s + 1] - d.row_ptr[s];
+  const int64_t k = d.sn_first[s + 1] - d.sn_first[s];
+  if (o0 >= k) return;
+  const int ob = (int)(k - o0 < kOuter ? k - o0 : kOuter);
+  const int np = (ob + kPanel - 1) / kPanel;
+  const float* F = front + d.front_off[s];
+  const float* Li0 = Linv + b.li_off[blockIdx.x] + (uint64_t)(o0 / kPanel) * kPanel * kPanel;
+  double* v = vec + d.vec_off[s];
+  const int t = threadIdx.x;
+  for (int g = np - 1; g >= 0; g--) {
+    const int cbg = ob - g * kPanel < kPanel ? ob - g * kPanel : kPanel;
+    const float* Li = Li0 + (uint64_t)g * kPanel * kPanel;
+    for (int e = t; e < kPanel * kPanel; e += kThreads) {
+      const int er = e % kPanel, ec = e / kPanel;
+      if (er < cbg && ec < cbg) cp_async4(Ls + g * kPanel * kLd + ec * kLd + er, Li + e);
+    }
+    for (int e = t; e < kPanel * g * kPanel; e += kThreads) {
+      const int er = e % kPanel, ec = e / kPanel;   // row er of panel g, column ec < 64 g
+      if (er < cbg)
+        cp_async4(Tb + tri_off(g) + ec * kLd + er, F + (o0 + g * kPanel + er) + (o0 + ec) * m);
+    }
+    cp_async_commit();
+  }
+  if (t < ob) tb[t] = v[o0 + t];
+  const int r = t >> 2, q = t & 3;   // kThreads = 4 x kPanel
+  for (int g = np - 1; g >= 0; g--) {
+    const int p = g * kPanel;
+    const int cb = ob - p < kPanel ? ob - p : kPanel;
+    cp_async_wait(g);
+    __syncthreads();
+    if (t < kPanel) xs[t] = D::split(t < cb ? tb[p + t] : 0.0);
+    __syncthreads();
+    // x_r = sum_{c >= r} Linv[c][r] t_c (column r of the inverse)
+    const float* L = Ls + g * kPanel * kLd + r * kLd;
+    D x;
+    if (r < cb) {
+      D x1;
+#pragma unroll
+      for (int j = 0; j < kPanel / 4; j += 2) {
+        const int c0 = q * (kPanel / 4) + j, c1 = c0 + 1;
+        if (c0 < cb) x.add(L[c0], xs[c0]);
+        if (c1 < cb) x1.add(L[c1], xs[c1]);
+      }
+      x.merge(x1);
+    }
+    x.shfl_xor(1);
+    x.shfl_xor(2);
+    __syncthreads();
+    if (r < cb && q == 0) {
+      const double xv = x.value();
+      tb[p + r] = xv;
+      xs[r] = D::split(xv);
+    }
+    __syncthreads();
+    // the pivots before the panel: t_j -= sum_c L[p+c][j] x_c
+    for (int j0 = 0; j0 < p; j0 += kThreads / 4) {
+      const int j = j0 + r;
+      D a;
+      if (j < p) {
+        const float* Tj = Tb + tri_off(g) + j * kLd;
+        D a1;
+#pragma unroll
+        for (int u = 0; u < kPanel / 4; u += 2) {
+          const int c0 = q * (kPanel / 4) + u, c1 = c0 + 1;
+          if (c0 < cb) a.add(Tj[c0], xs[c0]);
+          if (c1 < cb) a1.add(Tj[c1], xs[c1]);
+        }
+        a.merge(a1);
+      }
+      a.shfl_xor(1);
+      a.shfl_xor(2);
+      if (j < p && q == 0) tb[j] -= a.value();
+    }
+    __syncthreads();
+  }
+  if (t < ob) v[o0 + t] = tb[t];
+}
+
 // the solved pivots of the large supernodes into xf (factor order)
 __global__ void store_pivots_kernel(BigBatch b, LdltDev d, const double* __restrict__ vec,
                                     double* __restrict__ xf) {
@@ -1689,7 +1915,11 @@ cudaError_t enqueue_solve_core(nla3d_ldlt* h, const double* b) {
       const BigBatch bb{h->d_lists + L.large_off, h->d_wo + L.wo_off, h->d_lio + L.wo_off};
       const unsigned nf = (unsigned)L.large_cnt;
       for (int64_t o0 = 0; o0 < L.large_max_k; o0 += kOuter) {
-        fwd_block_kernel<T, D><<<nf, kThreads, 0, st>>>(bb, h->dev, front, Li, o0, h->d_vec);
+        if constexpr (std::is_same<T, float>::value)
+          fwd_block_staged_kernel<D><<<nf, kThreads, kStagedSmem, st>>>(bb, h->dev, front, Li, o0,
+                                                                        h->d_vec);
+        else
+          fwd_block_kernel<T, D><<<nf, kThreads, 0, st>>>(bb, h->dev, front, Li, o0, h->d_vec);
         const int64_t rest = L.large_max_m - o0 - 1;
         if (rest > 0)
           fwd_rows_block_kernel<T, D><<<dim3((unsigned)((rest + 31) / 32), nf),
@@ -1715,7 +1945,11 @@ cudaError_t enqueue_solve_core(nla3d_ldlt* h, const double* b) {
                                 nf),
                            kThreads, 0, st>>>(bb, h->dev, front, h->d_vec);
       for (int64_t o0 = ((L.large_max_k - 1) / kOuter) * kOuter; o0 >= 0; o0 -= kOuter) {
-        bwd_block_kernel<T, D><<<nf, kThreads, 0, st>>>(bb, h->dev, front, Li, o0, h->d_vec);
+        if constexpr (std::is_same<T, float>::value)
+          bwd_block_staged_kernel<D><<<nf, kThreads, kStagedSmem, st>>>(bb, h->dev, front, Li, o0,
+                                                                        h->d_vec);
+        else
+          bwd_block_kernel<T, D><<<nf, kThreads, 0, st>>>(bb, h->dev, front, Li, o0, h->d_vec);
         if (o0 > 0)
           bwd_cols_block_kernel<T, D><<<dim3((unsigned)((o0 + 31) / 32), nf), kThreads, 0, st>>>(
               bb, h->dev, front, o0, h->d_vec);
@@ -2079,6 +2313,17 @@ cudaError_t enqueue_solve_any(nla3d_ldlt* h, const double* rhs, double* out, int
   const bool accurate = h->prec && h->solve_accurate;
   cudaGraphExec_t& exec = accurate ? h->solve_exec_acc : h->solve_exec;
   if (!exec) {
+    if (h->prec) {
+      // the staged block triangles take more than the default 48 KB
+      const void* kf[4] = {(const void*)fwd_block_staged_kernel<Dot<float>>,
+                           (const void*)bwd_block_staged_kernel<Dot<float>>,
+                           (const void*)fwd_block_staged_kernel<DotWide>,
+                           (const void*)bwd_block_staged_kernel<DotWide>};
+      for (const void* f : kf) {
+        e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStagedSmem);
+        if (e != cudaSuccess) return e;
+      }
+    }
     cudaGraph_t g = nullptr;
     e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return e;
