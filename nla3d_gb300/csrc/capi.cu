@@ -126,7 +126,10 @@ struct nla3d_ctx {
     int k;
     uint64_t s0, s1;
   };
-  cudaStream_t copy_stream = nullptr;
+  // copy streams: each run of K is copied in kCopyStreams parts, one per
+  // copy engine (one engine alone does not fill the host link)
+  static constexpr int kCopyStreams = 2;
+  cudaStream_t copy_stream[kCopyStreams] = {};
   std::vector<cudaEvent_t> chunk_ev;
   int plan_chunks = 0;
   std::vector<uint32_t> plan_eb;
@@ -535,7 +538,8 @@ int nla3d_destroy(nla3d_ctx* c) {
   c->allocs.clear();
   for (auto& v : c->ev) cudaEventDestroy(v);
   for (auto& v : c->chunk_ev) cudaEventDestroy(v);
-  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+  for (cudaStream_t cs : c->copy_stream)
+    if (cs) cudaStreamDestroy(cs);
   delete c;
   return NLA3D_OK;
 }
@@ -1216,10 +1220,11 @@ int nla3d_assemble_to_host(nla3d_ctx* c, int n_chunks, double* K1, double* K12, 
   }
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(c, e, "assemble_to_host: after the plan");
-  if (!c->copy_stream) {
-    e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
-    if (e != cudaSuccess) return cuda_fail(c, e, "assemble_to_host: stream");
-  }
+  for (cudaStream_t& cs : c->copy_stream)
+    if (!cs) {
+      e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+      if (e != cudaSuccess) return cuda_fail(c, e, "assemble_to_host: stream");
+    }
   while (c->chunk_ev.size() < 64) {
     cudaEvent_t ev;
     e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
@@ -1228,15 +1233,22 @@ int nla3d_assemble_to_host(nla3d_ctx* c, int n_chunks, double* K1, double* K12, 
   }
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(c, e, "assemble_to_host: after stream/events");
-  // copy K values [s0, s1) of the concatenated blocks into the block arrays
+  // copy K values [s0, s1) of the concatenated blocks into the block arrays,
+  // each piece in equal parts on the copy streams
+  constexpr int ncs = nla3d_ctx::kCopyStreams;
   auto copy_range = [&](uint64_t s0, uint64_t s1) -> cudaError_t {
     for (int b = 0; b < 3 && s0 < s1; b++) {
       const uint64_t lo = m.val_off[b], hi = lo + m.blk[b].nnz();
       const uint64_t a = std::max(s0, lo), z = std::min(s1, hi);
       if (a >= z) continue;
-      cudaError_t err = cudaMemcpyAsync(host[b] + (a - lo), c->d_K + a, sizeof(double) * (z - a),
-                                        cudaMemcpyDeviceToHost, c->copy_stream);
-      if (err != cudaSuccess) return err;
+      for (int h = 0; h < ncs; h++) {
+        const uint64_t p0 = a + (z - a) * h / ncs, p1 = a + (z - a) * (h + 1) / ncs;
+        if (p0 >= p1) continue;
+        cudaError_t err = cudaMemcpyAsync(host[b] + (p0 - lo), c->d_K + p0,
+                                          sizeof(double) * (p1 - p0), cudaMemcpyDeviceToHost,
+                                          c->copy_stream[h]);
+        if (err != cudaSuccess) return err;
+      }
     }
     return cudaSuccess;
   };
@@ -1259,8 +1271,8 @@ int nla3d_assemble_to_host(nla3d_ctx* c, int n_chunks, double* K1, double* K12, 
     if (e == cudaSuccess && k == n - 1) where = "MPC rows", e = enqueue_mpc(c);
     if (r0 == ri && k < n - 1) continue;  // nothing to copy after this range
     if (e == cudaSuccess) where = "event record", e = cudaEventRecord(c->chunk_ev[k], c->stream);
-    if (e == cudaSuccess)
-      where = "stream wait", e = cudaStreamWaitEvent(c->copy_stream, c->chunk_ev[k], 0);
+    for (int h = 0; h < ncs && e == cudaSuccess; h++)
+      where = "stream wait", e = cudaStreamWaitEvent(c->copy_stream[h], c->chunk_ev[k], 0);
     for (size_t q = r0; q < ri && e == cudaSuccess; q++) {
       where = "K copy";
       e = copy_range(runs[q].s0, runs[q].s1);
@@ -1268,8 +1280,9 @@ int nla3d_assemble_to_host(nla3d_ctx* c, int n_chunks, double* K1, double* K12, 
   }
   if (e == cudaSuccess)
     where = "F copy", e = cudaMemcpyAsync(F, c->d_F, sizeof(double) * c->Utot(),
-                                          cudaMemcpyDeviceToHost, c->copy_stream);
-  if (e == cudaSuccess) where = "copy stream sync", e = cudaStreamSynchronize(c->copy_stream);
+                                          cudaMemcpyDeviceToHost, c->copy_stream[ncs - 1]);
+  for (int h = 0; h < ncs && e == cudaSuccess; h++)
+    where = "copy stream sync", e = cudaStreamSynchronize(c->copy_stream[h]);
   if (e != cudaSuccess) return cuda_fail(c, e, (std::string("assemble_to_host: ") + where).c_str());
   return NLA3D_OK;
 }
