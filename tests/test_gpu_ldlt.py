@@ -37,14 +37,14 @@ def _order(s):
     return ldlt.saddle_order(io, co, nested_dissection(K, pts, leaf=16), s.n_unk)
 
 
-def _check(s, precision="fp64", tol=1e-13, seed=0):
+def _check(s, precision="fp64", tol=1e-13, seed=0, max_refine=10):
     io, co = s.pattern(2)
     n2 = io.size - 1
     A = csr_full(io, co, s.K(2), n2, n2, True).tocsc()
     b = np.random.default_rng(seed).standard_normal(n2)
     solver = ldlt.DeviceLDLT.for_storage(s, _order(s), precision)
     solver.factor(s)
-    x = solver.solve_host(s, b, max_refine=10, tol=tol)
+    x = solver.solve_host(s, b, max_refine=max_refine, tol=tol)
     assert solver.info()["nonfinite"] == 0
     xr = spla.spsolve(A, b)
     assert np.linalg.norm(b - A @ x) <= tol * np.linalg.norm(b) * 1.01
@@ -103,6 +103,19 @@ def test_fp32_fronts_on_a_nearly_incompressible_block():
     u, p = mg.twist_state(mesh, angle_deg=30.0, stretch=1.2, noise_frac=0.01, seed=4)
     s = _storage(mesh, u, p, None, True)
     solver, x = _check(s, "fp32", 1e-12)
+    assert solver.last_steps >= 2
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp32-tc"])
+def test_fp32_fronts_nearly_incompressible_blocked(precision):
+    """K/G = 1e6 on a 12^3 block: FP32 fronts above 256 rows (the blocked
+    solve, its plain steps with compensated FP32 products, then GMRES with
+    FP64 products), refined to 1e-12 and equal to SciPy's solution."""
+    mesh = mg.solid81_block(12, 12, 12, 1.0 / 12, mg.MAT_NEO_HOOKEAN, (1.0, 1.0e6), clamp_z0=True)
+    u, p = mg.twist_state(mesh, angle_deg=30.0, stretch=1.2, noise_frac=0.01, seed=4)
+    s = _storage(mesh, u, p, None, True)
+    solver, x = _check(s, precision, 1e-12, max_refine=60)
+    assert solver.info()["max_front"] > 256
     assert solver.last_steps >= 2
 
 
