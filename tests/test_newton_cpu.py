@@ -25,6 +25,11 @@ def test_rigid_body_mpc_rotx_reaction_curve_oracle_backend():
     s = NewtonSolver(m, fixes, n_loadsteps=20, n_iterations=15).solve()
     err = rb.curve_error(s, mesh, ref)
     assert err < rb.THRESHOLD, err
+    # host time per phase: every phase accounted, the host solve none of the
+    # device ones (factor / solve are the device LDL^T's)
+    assert set(s.timing) == {"assemble", "factor", "solve", "update", "vectors"}
+    assert all(v >= 0.0 for v in s.timing.values())
+    assert s.timing["assemble"] > 0.0 and s.timing["factor"] == 0.0
 
 
 def test_residual_criterion_converges_quadratically_and_keeps_the_curve():
