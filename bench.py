@@ -43,10 +43,10 @@ sys.path.insert(0, ROOT)
 # (8 x 8634) for the same element.
 FLOP_PER_ELEM = 29467
 FLOP_PER_ELEM_BTDB = 69072
-# FP64 instructions per element in the same capture (12,360 DFMA + 3,480
-# DMUL + 1,267 DADD): a DMUL or DADD takes the pipe as long as a DFMA for half
+# FP64 instructions per element in the same capture (12,744 DFMA + 3,096
+# DMUL + 883 DADD): a DMUL or DADD takes the pipe as long as a DFMA for half
 # the flops, so the pipe's instruction rate is the tighter ceiling.
-FP64_INSTR_PER_ELEM = 17107
+FP64_INSTR_PER_ELEM = 16723
 # DRAM bytes per element of solid81_kernel<double> and of the K gather in one
 # ncu capture of a 40^3 block (64,000 elements, 9,675,406 K slots), used to
 # scale the traffic to the measured launch; the element kernel's writes are a
